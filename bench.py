@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Benchmark of the batched diffeqsolve hot path on GB300.
+
+Workload (the uneven-batching configuration): Van der Pol x' = y,
+y' = mu (1 - x^2) y - x with mu ~ LogUniform[0.1, 10], (x0, y0) ~ U[-2, 2]^2,
+per-trajectory t1 ~ U[5, 50], batch 65536 per GPU; Dopri5 with
+PIDController(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4), dt0=None,
+SaveAt(t1=True); FP32 state with FP64 t/dt; one persistent launch captured as a
+CUDA graph.  Inputs are seeded synthetic draws of exactly that distribution.
+
+One step = one solve of the whole batch.  `value` is trajectories/s with
+inputs resident in HBM (fused kernel K1); `e2e` is the same metric through the
+public diffeqsolve call with pinned host inputs copied in and results copied
+out every step.  The plain one-trajectory-per-thread kernel K0 is timed the
+same way and reported beside it, together with the max relative error of both
+against the FP64 oracle and the oracle's own throughput on the host cores.
+
+`--impl reference` times the reference path's CPU implementation -- the FP64
+oracle restatement of Diffrax's loop (the reference itself is JAX and cannot
+be installed here) -- on all host cores, on a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "trajectories/s (Van der Pol, Dopri5+PID rtol 1e-6, uneven t1, batch 65536)"
+UNIT = "trajectories/s"
+WORKLOAD = "vdp_dopri5_pid_uneven_t1_b65536"
+# Algorithmic work per attempted Dopri5 step on Van der Pol (d = 2), counting
+# an FMA as 2 flops: 6 field evaluations x 5, 7 stage scalings x 2, 20
+# nonzero stage coefficients x 2 dims x 2 + 12 adds, 6 error terms x 2 x 2,
+# and ~26 for the scaled RMS norm and PID factor.
+FP32_FLOPS_PER_STEP = 6 * 5 + 14 + 92 + 24 + 26
+FP64_OPS_PER_STEP = 6      # dt, t + dt, dt * factor, clip compare, loop compare, min
+BYTES_PER_TRAJ = 8 + 4 + 8 + 8 + 8 + 4 + 12  # y0, mu, t1, ys, ts, result, stats
+FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12
+FP64_PEAK_TFLOPS_NOMINAL = 1.25
+
+
+def vdp_inputs(B: int, seed: int):
+    rng = np.random.default_rng(seed)
+    mu = np.exp(rng.uniform(np.log(0.1), np.log(10.0), B))
+    y0 = rng.uniform(-2.0, 2.0, (B, 2))
+    t1 = rng.uniform(5.0, 50.0, B)
+    return mu, y0, t1
+
+
+def oracle_solve(mu, y0, t1, nthreads):
+    import oracle as O
+    d = O.make_desc(solver=O.DOPRI5, controller=O.PID, field=O.VAN_DER_POL, dim=2,
+                    rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4, save_t1=1, n_args=1)
+    return O.solve(d, 0.0, t1, None, y0, args=mu[:, None], nthreads=nthreads)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "fused_kernel_vdp_dopri5.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-i", str(self.index), "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    """CPU implementation of the path (the FP64 oracle restatement) on all host
+    cores, `sample` trajectories per step."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    sample = args.ref_sample
+    mu, y0, t1 = vdp_inputs(sample, args.seed)
+    for _ in range(args.warmup):
+        oracle_solve(mu, y0, t1, cores)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        oracle_solve(mu, y0, t1, cores)
+        times.append(time.perf_counter() - t)
+    v = sample / statistics.mean(times)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "batch_per_step": sample,
+                   "note": "Diffrax (JAX) is not installable offline; this is the FP64 C "
+                           "restatement of its solve loop with OpenMP over trajectories"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{sample} trajectories of the workload per step"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbdx", choices=["gbdx", "reference"])
+    ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--ref-sample", type=int, default=8192)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    import diffrax_gb300 as dfx
+    from diffrax_gb300._integrate import Lowered
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    B = args.batch
+    mu, y0, t1 = vdp_inputs(B, args.seed + rank)
+    pid = dfx.PIDController(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4)
+    term = dfx.ODETerm(dfx.VanDerPol())
+    y0_d = torch.tensor(y0, dtype=torch.float32, device=dev)
+    mu_d = torch.tensor(mu[:, None], dtype=torch.float32, device=dev)
+    t1_d = torch.tensor(t1, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def lowered(kernel):
+        return Lowered(term, dfx.Dopri5(), 0.0, t1_d, None, y0_d, mu_d, dfx.SaveAt(t1=True),
+                       pid, None, 4096, kernel, 0, 0)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def time_kernel(kernel, steps, sampler=None):
+        low = lowered(kernel)
+        for _ in range(args.warmup):
+            low.run_forward()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            outs = low.run_forward()
+        g.replay()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        barrier()
+        if sampler:
+            sampler.start()
+        wall = time.perf_counter()
+        for e0, e1 in evs:
+            flush.fill_(1.0)          # evict L2 between timed solves (not timed)
+            e0.record()
+            g.replay()
+            e1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall
+        barrier()
+        clocks = sampler.stop() if sampler else None
+        ms = [a.elapsed_time(b) for a, b in evs]
+        ms_step = statistics.mean(ms)
+        if world > 1:
+            t = torch.tensor([ms_step], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms_step = float(t.item())
+        return ms_step, outs, clocks, wall
+
+    sampler = ClockSampler(local)
+    ms_fused, outs, clocks, wall = time_kernel("fused", args.steps, sampler)
+    ms_plain, outs_plain, _, _ = time_kernel("plain", max(3, args.steps // 2))
+    value = B * world / (ms_fused / 1e3)
+    plain_value = B * world / (ms_plain / 1e3)
+
+    ys, ts_out, res, stats = outs
+    steps_total = int(stats[:, 0].sum().item())
+    ok = bool((res == 0).all().item())
+
+    # End to end through the public call: pinned host inputs in, results out.
+    y0_h = torch.tensor(y0, dtype=torch.float32).pin_memory()
+    mu_h = torch.tensor(mu[:, None], dtype=torch.float32).pin_memory()
+    t1_h = torch.tensor(t1, dtype=torch.float64).pin_memory()
+    ys_h = torch.empty((B, 1, 2), dtype=torch.float32).pin_memory()
+    res_h = torch.empty((B,), dtype=torch.int32).pin_memory()
+
+    def e2e_step():
+        sol = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1_h, None, y0_h, mu_h,
+                              stepsize_controller=pid, throw=False)
+        ys_h.copy_(sol.ys, non_blocking=True)
+        res_h.copy_(sol.result, non_blocking=True)
+        torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        e2e_step()
+        e2e_t.append(time.perf_counter() - t)
+    e2e_s = statistics.mean(e2e_t)
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = B * (2 * 4 + 4 + 8) + 8
+    d2h = B * (2 * 4 + 4)
+
+    if rank == 0:
+        peaks, src = measured_peaks()
+        t_s = ms_fused / 1e3
+        fp32 = steps_total * FP32_FLOPS_PER_STEP / t_s / 1e12
+        fp64 = steps_total * FP64_OPS_PER_STEP / t_s / 1e12
+        gbs = B * BYTES_PER_TRAJ / t_s / 1e9
+        traffic = ncu_traffic()
+        roofline = {
+            "bound": "fp32", "achieved": fp32, "peak": FP32_PEAK_TFLOPS_NOMINAL,
+            "unit": "TFLOP/s", "frac": fp32 / FP32_PEAK_TFLOPS_NOMINAL, "traffic": traffic,
+            "peak_source": "nominal FP32 FMA rate at 2.07 GHz (no measured FP32 peak)",
+            "work": f"{FP32_FLOPS_PER_STEP} FP32 flop per attempted step x "
+                    f"{steps_total} attempted steps per launch",
+            "fp64": {"achieved": fp64, "peak": FP64_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
+                     "frac": fp64 / FP64_PEAK_TFLOPS_NOMINAL},
+            "hbm": {"achieved": gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                    "frac": gbs / peaks.get("hbm_gbs", 6800.0), "peak_source": src,
+                    "algorithmic_bytes_per_launch": B * BYTES_PER_TRAJ},
+        }
+        # Accuracy of both kernels against the FP64 oracle on the same inputs.
+        n_chk = min(B, 4096)
+        ref = oracle_solve(mu[:n_chk], y0[:n_chk], t1[:n_chk], os.cpu_count() or 1)
+        def err(o):
+            a = o[0][:n_chk].double().cpu().numpy()
+            per = np.abs(a - ref["ys"]).max(axis=(1, 2)) / np.abs(ref["ys"]).max(axis=(1, 2))
+            return float(per.max()), float(np.median(per))
+        fused_err = err(outs)
+        plain_err = err(outs_plain)
+        cpu = None
+        if not args.no_cpu_baseline:
+            cores = os.cpu_count() or 1
+            ns = min(B, 16384)
+            t = time.perf_counter()
+            oracle_solve(mu[:ns], y0[:ns], t1[:ns], cores)
+            dt = time.perf_counter() - t
+            cpu = {"value": ns / dt, "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": f"first {ns} trajectories of the batch, FP64 oracle, "
+                             f"OpenMP over trajectories ({dt:.1f} s)"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_fused,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 state, f64 time", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "batch_per_gpu": B, "solver": "Dopri5",
+                       "controller": "PID(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4)",
+                       "saveat": "t1", "kernel": "fused persistent (CUDA graph)",
+                       "l2": "256 MB buffer written between timed solves"},
+            "e2e": {"value": B * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "plain": {"value": plain_value, "ms_per_step": ms_plain,
+                      "max_rel_err_vs_fp64_oracle": plain_err[0],
+                      "median_rel_err_vs_fp64_oracle": plain_err[1]},
+            "fused_over_plain": value / plain_value,
+            "max_rel_err_vs_fp64_oracle": fused_err[0],
+            "median_rel_err_vs_fp64_oracle": fused_err[1],
+            "all_successful": ok,
+            "attempted_steps_per_launch": steps_total,
+            "wall_s_timed_region": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

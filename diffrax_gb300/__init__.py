@@ -1,0 +1,27 @@
+"""diffrax_gb300: GB300-native batched diffeqsolve.
+
+A drop-in for ``jax.vmap(diffrax.diffeqsolve)`` over registered vector fields,
+executed by hand-written sm_103a kernels in libgbdx.so (see include/gbdx.h).
+"""
+from ._core import (
+    AbstractAdjoint, AbstractField, AbstractSolver, AbstractStepSizeController, AbstractTerm,
+    BacksolveAdjoint, ConstantStepSize, ControlTerm, Dopri5, Euler, Heun, LotkaVolterra,
+    MultiTerm, ODETerm, OrnsteinUhlenbeck, PIDController, RecursiveCheckpointAdjoint,
+    RESULTS, SaveAt, Solution, Tsit5, VanDerPol, VirtualBrownianTree, adjoint_rms_seminorm,
+    rms_norm,
+)
+from ._integrate import diffeqsolve, lower, oracle_fields
+
+__version__ = "0.1.0"
+
+
+def build(force: bool = False) -> str:
+    """Compile libgbdx.so for sm_103a (in-tree) and return its path."""
+    from . import _build
+    return _build.build(force=force)
+
+
+def load_library():
+    """Load libgbdx.so (building it when stale)."""
+    from . import _lib
+    return _lib.load()

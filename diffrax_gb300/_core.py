@@ -1,0 +1,269 @@
+"""Diffrax-compatible objects: fields, terms, solvers, controllers, SaveAt,
+adjoints, RESULTS and Solution.
+
+Names, defaults and argument meaning follow Diffrax v0.7.2; each class cites
+the reference definition it mirrors.  These objects carry no computation --
+``diffeqsolve`` lowers them to a ``gbdx_problem_desc`` and calls libgbdx.so.
+"""
+from __future__ import annotations
+
+import dataclasses
+import enum
+from typing import Any, Optional, Sequence
+
+# ---------------------------------------------------------------------------
+# Registered vector fields.  A field is a vector_field(t, y, args) that the
+# library knows how to evaluate on the GPU.
+# ---------------------------------------------------------------------------
+
+
+class AbstractField:
+    field_id: int = -1
+    n_args: int = 0
+
+    def dim_for(self, dim: int) -> int:
+        return dim
+
+
+class LotkaVolterra(AbstractField):
+    """x' = a x - b x y,  y' = -c y + d x y.  args = (a, b, c, d), shared or per
+    trajectory ([4] or [B, 4])."""
+    field_id = 0
+    n_args = 4
+
+
+class VanDerPol(AbstractField):
+    """x' = y,  y' = mu (1 - x^2) y - x.  args = mu ([1], [B] or [B, 1])."""
+    field_id = 1
+    n_args = 1
+
+
+class OrnsteinUhlenbeck(AbstractField):
+    """Drift theta (mu - y) and, inside a ControlTerm, constant diagonal
+    diffusion sigma.  args = (theta, mu, sigma)."""
+    field_id = 2
+    n_args = 3
+
+
+# ---------------------------------------------------------------------------
+# Terms (diffrax/_term.py).
+# ---------------------------------------------------------------------------
+
+
+class AbstractTerm:
+    pass
+
+
+class ODETerm(AbstractTerm):
+    """f(t, y, args) dt (diffrax/_term.py:174-226)."""
+
+    def __init__(self, vector_field: AbstractField):
+        if not isinstance(vector_field, AbstractField):
+            raise TypeError("ODETerm needs a registered vector field "
+                            "(LotkaVolterra, VanDerPol, OrnsteinUhlenbeck, MLPField)")
+        self.vector_field = vector_field
+
+
+class ControlTerm(AbstractTerm):
+    """g(t, y, args) dW with a diagonal g (diffrax/_term.py:271-555)."""
+
+    def __init__(self, vector_field: Any, control: Any):
+        self.vector_field = vector_field
+        self.control = control
+
+
+class MultiTerm(AbstractTerm):
+    """Sum of terms (diffrax/_term.py:666-731)."""
+
+    def __init__(self, *terms: AbstractTerm):
+        self.terms = tuple(terms)
+
+
+class VirtualBrownianTree:
+    """Brownian motion on [t0, t1] discretised to `tol`, evaluated by binary
+    bridge descent (diffrax/_brownian/tree.py:177-354, BrownianIncrement).
+
+    `key` is an integer seed of this library's counter-based generator
+    (Philox4x32-10); trajectory b of a batch uses its own independent path.
+    """
+
+    def __init__(self, t0: float, t1: float, tol: float, shape: Sequence[int] | int,
+                 key: int = 0):
+        if not t0 < t1:
+            raise ValueError("t0 must be strictly less than t1")
+        self.t0, self.t1, self.tol = float(t0), float(t1), float(tol)
+        self.shape = (shape,) if isinstance(shape, int) else tuple(shape)
+        self.key = int(key)
+
+
+# ---------------------------------------------------------------------------
+# Solvers (diffrax/_solver/*.py).
+# ---------------------------------------------------------------------------
+
+
+class AbstractSolver:
+    solver_id: int = -1
+    _order: int = 0
+    _strong_order: Optional[float] = None
+
+    def order(self, terms=None) -> int:
+        return self._order
+
+    def strong_order(self, terms=None) -> Optional[float]:
+        return self._strong_order
+
+    def __eq__(self, other):
+        return type(self) is type(other)
+
+    def __hash__(self):
+        return hash(type(self))
+
+    def __repr__(self):
+        return f"{type(self).__name__}()"
+
+
+class Euler(AbstractSolver):
+    """diffrax/_solver/euler.py:17-73."""
+    solver_id, _order, _strong_order = 0, 1, 0.5
+
+
+class Heun(AbstractSolver):
+    """diffrax/_solver/heun.py:20-45."""
+    solver_id, _order, _strong_order = 1, 2, 0.5
+
+
+class Dopri5(AbstractSolver):
+    """diffrax/_solver/dopri5.py:53-100."""
+    solver_id, _order = 2, 5
+
+
+class Tsit5(AbstractSolver):
+    """diffrax/_solver/tsit5.py:159-190."""
+    solver_id, _order = 3, 5
+
+
+# ---------------------------------------------------------------------------
+# Step size controllers.
+# ---------------------------------------------------------------------------
+
+
+class AbstractStepSizeController:
+    pass
+
+
+@dataclasses.dataclass(frozen=True)
+class ConstantStepSize(AbstractStepSizeController):
+    """diffrax/_step_size_controller/constant.py:20-104."""
+
+
+def rms_norm(x):  # marker for PIDController(norm=...), optx.rms_norm
+    raise NotImplementedError("rms_norm is evaluated inside the kernels")
+
+
+def adjoint_rms_seminorm(x):  # marker, diffrax/_misc.py:85-116
+    raise NotImplementedError("adjoint_rms_seminorm is evaluated inside the kernels")
+
+
+@dataclasses.dataclass(frozen=True)
+class PIDController(AbstractStepSizeController):
+    """diffrax/_step_size_controller/pid.py:109-580 (same fields and defaults)."""
+    rtol: float
+    atol: float
+    pcoeff: float = 0.0
+    icoeff: float = 1.0
+    dcoeff: float = 0.0
+    dtmin: Optional[float] = None
+    dtmax: Optional[float] = None
+    force_dtmin: bool = True
+    factormin: float = 0.2
+    factormax: float = 10.0
+    safety: float = 0.9
+    error_order: Optional[float] = None
+    norm: Any = rms_norm
+
+
+# ---------------------------------------------------------------------------
+# SaveAt (diffrax/_saveat.py:14-105).
+# ---------------------------------------------------------------------------
+
+
+class SaveAt:
+    def __init__(self, *, t0: bool = False, t1: bool = False, ts=None, steps: bool = False,
+                 dense: bool = False, solver_state: bool = False,
+                 controller_state: bool = False, made_jump: bool = False):
+        if steps or dense:
+            raise NotImplementedError("SaveAt(steps=...) and SaveAt(dense=...) are not "
+                                      "supported by this library")
+        if solver_state or controller_state or made_jump:
+            raise NotImplementedError("saving solver/controller state is not supported")
+        if not (t0 or t1 or ts is not None):
+            raise ValueError("Empty saveat -- nothing will be saved.")
+        self.t0, self.t1, self.ts = bool(t0), bool(t1), ts
+
+
+# ---------------------------------------------------------------------------
+# Adjoints (diffrax/_adjoint.py).
+# ---------------------------------------------------------------------------
+
+
+class AbstractAdjoint:
+    pass
+
+
+@dataclasses.dataclass(frozen=True)
+class RecursiveCheckpointAdjoint(AbstractAdjoint):
+    """diffrax/_adjoint.py:179-312.  `checkpoints` bounds the per-trajectory
+    checkpoint slots; None means ceil(log2(max_steps)) slots as the reference."""
+    checkpoints: Optional[int] = None
+
+
+class BacksolveAdjoint(AbstractAdjoint):
+    """diffrax/_adjoint.py:737-871.  kwargs override the backward solve."""
+
+    _valid = {"dt0", "solver", "stepsize_controller", "adjoint", "max_steps", "throw"}
+
+    def __init__(self, **kwargs):
+        diff = set(kwargs) - self._valid
+        if diff:
+            raise ValueError("The following keyword argments are not valid for "
+                             f"`BacksolveAdjoint`: {diff}")
+        self.kwargs = kwargs
+
+
+# ---------------------------------------------------------------------------
+# RESULTS and Solution (diffrax/_solution.py).
+# ---------------------------------------------------------------------------
+
+
+class RESULTS(enum.IntEnum):
+    successful = 0
+    max_steps_reached = 1
+    dt_min_reached = 2
+    event_occurred = 3
+    max_steps_rejected = 4
+    internal_error = 5
+
+
+RESULT_MESSAGES = {
+    RESULTS.successful: "",
+    RESULTS.max_steps_reached: "The maximum number of solver steps was reached. Try "
+                               "increasing `max_steps`.",
+    RESULTS.dt_min_reached: "The minimum step size was reached in the differential "
+                            "equation solver.",
+    RESULTS.event_occurred: "Terminating differential equation solve because an event "
+                            "occurred.",
+    RESULTS.max_steps_rejected: "Maximum number of rejected steps was reached.",
+    RESULTS.internal_error: "An internal error occurred.",
+}
+
+
+@dataclasses.dataclass
+class Solution:
+    """Batched diffrax.Solution: every per-trajectory field has a leading batch
+    dimension (diffrax/_solution.py:82-201)."""
+    t0: Any
+    t1: Any
+    ts: Any        # [B, n_save] float64
+    ys: Any        # [B, n_save, dim]
+    stats: dict    # num_steps / num_accepted_steps / num_rejected_steps: [B] int32
+    result: Any    # [B] int32 RESULTS codes

@@ -1,0 +1,271 @@
+"""diffeqsolve: lowers Diffrax-style objects to a gbdx problem and runs it.
+
+Batched ("vmapped") semantics: ``y0`` is [B, dim]; ``t0``, ``t1`` and ``dt0``
+are scalars or [B]; ``args`` is shared ([n_args]) or per trajectory
+([B, n_args]).  Every array lives on the GPU during the solve; host tensors are
+copied in (and the caller copies results out).  Reference entry point:
+diffrax/_integrate.py:888-1543.
+"""
+from __future__ import annotations
+
+import math
+from typing import Any, Optional
+
+import torch
+
+from . import _lib
+from ._core import (
+    RESULT_MESSAGES, RESULTS, AbstractField, BacksolveAdjoint, ConstantStepSize, ControlTerm,
+    Euler, MultiTerm, ODETerm, OrnsteinUhlenbeck, PIDController,
+    RecursiveCheckpointAdjoint, SaveAt, Solution, VirtualBrownianTree, adjoint_rms_seminorm,
+)
+
+KERNELS = {"auto": 0, "plain": 1, "fused": 2}
+
+
+def _split_terms(terms):
+    """Return (drift_field, diffusion, brownian) from ODETerm or
+    MultiTerm(ODETerm, ControlTerm)."""
+    if isinstance(terms, ODETerm):
+        return terms.vector_field, None, None
+    if isinstance(terms, MultiTerm):
+        drift = diff = None
+        for t in terms.terms:
+            if isinstance(t, ODETerm) and drift is None:
+                drift = t.vector_field
+            elif isinstance(t, ControlTerm) and diff is None:
+                diff = t
+            else:
+                raise NotImplementedError("MultiTerm must be (ODETerm, ControlTerm)")
+        if drift is None or diff is None:
+            raise NotImplementedError("MultiTerm must be (ODETerm, ControlTerm)")
+        if not isinstance(diff.control, VirtualBrownianTree):
+            raise NotImplementedError("ControlTerm must be driven by a VirtualBrownianTree")
+        return drift, diff, diff.control
+    if isinstance(terms, ControlTerm):
+        raise NotImplementedError("a bare ControlTerm is not supported; use "
+                                  "MultiTerm(ODETerm(...), ControlTerm(...))")
+    raise TypeError(f"unsupported terms {terms!r}")
+
+
+def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype,
+          max_steps: int, n_ts: int, adjoint=None, kernel: str = "auto",
+          block_threads: int = 0, ctas_per_sm: int = 0) -> dict:
+    """Descriptor fields (gbdx_problem_desc) for one solve."""
+    drift, diff, bm = _split_terms(terms)
+    if not isinstance(drift, AbstractField):
+        raise TypeError("the drift must be a registered vector field")
+    f = dict(solver=solver.solver_id, field=drift.field_id, dim=int(dim),
+             n_ts=int(n_ts), save_t0=int(saveat.t0), save_t1=int(saveat.t1),
+             max_steps=int(max_steps), n_args=drift.n_args,
+             dtype=0 if dtype == torch.float32 else 1, kernel=KERNELS[kernel],
+             block_threads=int(block_threads), ctas_per_sm=int(ctas_per_sm),
+             rtol=0.0, atol=0.0, pcoeff=0.0, icoeff=1.0, dcoeff=0.0, safety=0.9,
+             factormin=0.2, factormax=10.0, dtmin=None, dtmax=None, force_dtmin=1,
+             error_order=0.0, mlp_depth=0, mlp_widths=(), diffusion=0, vbt_t0=0.0,
+             vbt_t1=1.0, vbt_tol=1e-3, seed=0, norm=0, adjoint=0, checkpoints=0)
+    if hasattr(drift, "lower_fields"):
+        f.update(drift.lower_fields(dim))
+    if isinstance(stepsize_controller, PIDController):
+        c = stepsize_controller
+        f.update(controller=1, rtol=float(c.rtol), atol=float(c.atol),
+                 pcoeff=float(c.pcoeff), icoeff=float(c.icoeff), dcoeff=float(c.dcoeff),
+                 safety=float(c.safety), factormin=float(c.factormin),
+                 factormax=float(c.factormax),
+                 dtmin=None if c.dtmin is None else float(c.dtmin),
+                 dtmax=None if c.dtmax is None else float(c.dtmax),
+                 force_dtmin=int(bool(c.force_dtmin)),
+                 error_order=0.0 if c.error_order is None else float(c.error_order),
+                 norm=1 if c.norm is adjoint_rms_seminorm else 0)
+    elif isinstance(stepsize_controller, ConstantStepSize):
+        f.update(controller=0)
+    else:
+        raise TypeError(f"unsupported step size controller {stepsize_controller!r}")
+    if diff is not None:
+        if isinstance(solver, Euler) and isinstance(stepsize_controller, PIDController):
+            raise ValueError("An SDE should not be solved with adaptive step sizes with "
+                             "Euler's method, as it may not converge to the correct "
+                             "solution.")
+        vf = diff.vector_field
+        if isinstance(vf, OrnsteinUhlenbeck):
+            f["diffusion"] = 1
+        elif hasattr(vf, "diffusion_id"):
+            f["diffusion"] = vf.diffusion_id
+        else:
+            raise NotImplementedError("unsupported diffusion")
+        f.update(vbt_t0=bm.t0, vbt_t1=bm.t1, vbt_tol=bm.tol, seed=bm.key)
+    if isinstance(adjoint, RecursiveCheckpointAdjoint):
+        cp = adjoint.checkpoints
+        if cp is None:
+            cp = max(1, math.ceil(math.log2(max(int(max_steps), 2))))
+        f.update(adjoint=1, checkpoints=int(cp))
+    elif isinstance(adjoint, BacksolveAdjoint):
+        f.update(adjoint=2)
+    return f
+
+
+def oracle_fields(fields: dict) -> dict:
+    """The subset of a lowered descriptor that the FP64 oracle understands."""
+    return {k: v for k, v in fields.items() if k in _lib.ORACLE_FIELDS and k != "pad0"}
+
+
+def _device():
+    if not torch.cuda.is_available():
+        raise RuntimeError("diffrax_gb300 needs a CUDA device: there is no CPU path")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _time_arrays(t0, t1, dt0, B, dev):
+    def as_t(x):
+        if isinstance(x, torch.Tensor):
+            return x.to(device=dev, dtype=torch.float64).reshape(-1)
+        return torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    vals = [as_t(t0), as_t(t1)] + ([as_t(dt0)] if dt0 is not None else [])
+    if all(v.numel() == 1 for v in vals):
+        return vals[0], vals[1], (vals[2] if dt0 is not None else None), 0
+    out = [v.expand(B).contiguous() if v.numel() == 1 else v.contiguous() for v in vals]
+    for v in out:
+        if v.numel() != B:
+            raise ValueError("t0, t1 and dt0 must be scalars or have one entry per trajectory")
+    return out[0], out[1], (out[2] if dt0 is not None else None), 1
+
+
+def _capturing() -> bool:
+    return torch.cuda.is_available() and torch.cuda.is_current_stream_capturing()
+
+
+def _host_checks(t0, t1, dt0, ts, tstride):
+    """The reference's dt0-sign and saveat.ts checks (_integrate.py:1036-1045,
+    1222-1235).  Skipped while a CUDA graph is being captured."""
+    if _capturing():
+        return
+    if dt0 is not None:
+        if bool(((t1 - t0) * dt0 < 0).any()):
+            raise ValueError("Must have (t1 - t0) * dt0 >= 0")
+    if ts is not None and ts.numel() > 0:
+        direction = torch.where(t0 < t1, 1.0, -1.0)
+        tsd = ts.reshape(1, -1) * direction.reshape(-1, 1)
+        if ts.numel() > 1 and bool((tsd[:, 1:] < tsd[:, :-1]).any()):
+            raise RuntimeError("saveat.ts must be increasing or decreasing.")
+        lo = (t0 * direction).reshape(-1, 1)
+        hi = (t1 * direction).reshape(-1, 1)
+        if bool(((tsd > hi) | (tsd < lo)).any()):
+            raise RuntimeError("saveat.ts must lie between t0 and t1.")
+
+
+class Lowered:
+    """A lowered, validated solve ready for the C ABI (reused by autograd)."""
+
+    def __init__(self, terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
+                 adjoint, max_steps, kernel, block_threads, ctas_per_sm):
+        dev = _device()
+        if not isinstance(y0, torch.Tensor):
+            y0 = torch.as_tensor(y0)
+        if y0.dtype not in (torch.float32, torch.float64):
+            y0 = y0.to(torch.float64)
+        if y0.dim() != 2:
+            raise ValueError("y0 must be [batch, dim] (vmapped semantics)")
+        self.dtype = y0.dtype
+        self.B, self.dim = int(y0.shape[0]), int(y0.shape[1])
+        self.y0 = y0.to(dev).contiguous()
+        if max_steps is None:
+            raise NotImplementedError("max_steps=None is not supported")
+        ts = saveat.ts
+        if ts is not None:
+            ts = torch.as_tensor(ts, dtype=torch.float64).to(dev).reshape(-1).contiguous()
+        self.save_ts = ts
+        n_ts = 0 if ts is None else int(ts.numel())
+        self.fields = lower(terms, solver, stepsize_controller, saveat, dim=self.dim,
+                            dtype=self.dtype, max_steps=max_steps, n_ts=n_ts,
+                            adjoint=adjoint, kernel=kernel, block_threads=block_threads,
+                            ctas_per_sm=ctas_per_sm)
+        drift = _split_terms(terms)[0]
+        self.drift = drift
+        self.problem = _lib.get_problem(self.fields)
+        self.t0, self.t1, self.dt0, self.tstride = _time_arrays(t0, t1, dt0, self.B, dev)
+        _host_checks(self.t0, self.t1, self.dt0, ts, self.tstride)
+        na = drift.n_args
+        if na:
+            if args is None:
+                raise ValueError(f"{type(drift).__name__} needs args with {na} entries")
+            a = torch.as_tensor(args).to(device=dev, dtype=self.dtype)
+            if a.numel() == na:
+                a = a.reshape(na).contiguous()
+                self.args_stride = 0
+            elif a.numel() == self.B * na:
+                a = a.reshape(self.B, na).contiguous()
+                self.args_stride = na
+            else:
+                raise ValueError(f"args must have shape [{na}] or [batch, {na}]")
+            self.args = a
+        else:
+            self.args = None
+            self.args_stride = 0
+        self.params = drift.flat_params(self.dtype, dev) if hasattr(drift, "flat_params") else None
+        self.n_save = self.problem.n_save
+        self.device = dev
+
+    def run_forward(self, stream=None):
+        dev = self.device
+        B, D, n_save = self.B, self.dim, self.n_save
+        ys = torch.empty((B, n_save, D), dtype=self.dtype, device=dev)
+        ts_out = torch.empty((B, n_save), dtype=torch.float64, device=dev)
+        res = torch.empty((B,), dtype=torch.int32, device=dev)
+        stats = torch.empty((B, 3), dtype=torch.int32, device=dev)
+        ws_bytes = self.problem.workspace_size(B)
+        ws = torch.empty((max(ws_bytes, 1),), dtype=torch.uint8, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev).cuda_stream
+        p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        rc = self.problem.lib.gbdx_solve_fwd(
+            self.problem.handle, B, p(self.t0), p(self.t1), p(self.dt0), self.tstride,
+            p(self.y0), p(self.args), self.args_stride, p(self.params), p(self.save_ts),
+            p(ys), p(ts_out), p(res), p(stats), p(ws), ws_bytes, stream)
+        _lib.check(rc, "gbdx_solve_fwd")
+        return ys, ts_out, res, stats
+
+
+def _raise_on_failure(result: torch.Tensor):
+    if _capturing():
+        return
+    bad = result != 0
+    if bool(bad.any()):
+        code = int(result[bad][0].item())
+        n = int(bad.sum().item())
+        raise RuntimeError(f"{RESULT_MESSAGES.get(RESULTS(code), 'failed')} "
+                           f"({n} of {result.numel()} trajectories failed)")
+
+
+def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
+                saveat: SaveAt = SaveAt(t1=True),
+                stepsize_controller=ConstantStepSize(),
+                adjoint=RecursiveCheckpointAdjoint(), event=None,
+                max_steps: Optional[int] = 4096, throw: bool = True,
+                progress_meter: Any = None, solver_state=None, controller_state=None,
+                made_jump=None, kernel: str = "auto", block_threads: int = 0,
+                ctas_per_sm: int = 0) -> Solution:
+    """Batched diffrax.diffeqsolve on the GPU (diffrax/_integrate.py:888-1543).
+
+    Extra keyword arguments select the GB300 execution policy: ``kernel`` is
+    "fused" (persistent work-stealing integrator, the default) or "plain" (one
+    trajectory per thread); ``block_threads`` / ``ctas_per_sm`` override the
+    autotuned launch shape of the fused kernel.
+    """
+    if event is not None:
+        raise NotImplementedError("events are not supported")
+    if solver_state is not None or controller_state is not None or made_jump is not None:
+        raise NotImplementedError("resuming from solver/controller state is not supported")
+    from ._autograd import needs_grad, solve_with_grad
+    low = Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
+                  adjoint, max_steps, kernel, block_threads, ctas_per_sm)
+    if needs_grad(low, y0, args):
+        ys, ts_out, res, stats = solve_with_grad(low, y0, args)
+    else:
+        ys, ts_out, res, stats = low.run_forward()
+    sol = Solution(t0=t0, t1=t1, ts=ts_out, ys=ys,
+                   stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],
+                              num_rejected_steps=stats[:, 2], max_steps=max_steps),
+                   result=res)
+    if throw:
+        _raise_on_failure(res)
+    return sol

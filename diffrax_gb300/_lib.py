@@ -1,0 +1,149 @@
+"""ctypes binding of libgbdx.so (include/gbdx.h).
+
+The library is the only execution path: if it cannot be built or loaded, or no
+CUDA device is present, every solve raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import threading
+
+from . import _build
+
+_c = ctypes
+i32, i64, f64, u64 = _c.c_int32, _c.c_int64, _c.c_double, _c.c_uint64
+vp = _c.c_void_p
+dp = _c.POINTER(_c.c_double)
+ip = _c.POINTER(_c.c_int32)
+
+
+class ProblemDesc(_c.Structure):
+    """Mirror of gbdx_problem_desc."""
+    _fields_ = [
+        ("solver", i32), ("controller", i32), ("field", i32), ("dim", i32),
+        ("rtol", f64), ("atol", f64), ("pcoeff", f64), ("icoeff", f64),
+        ("dcoeff", f64), ("safety", f64), ("factormin", f64), ("factormax", f64),
+        ("dtmin", f64), ("dtmax", f64), ("force_dtmin", i32), ("error_order", f64),
+        ("n_ts", i32), ("save_t0", i32), ("save_t1", i32), ("max_steps", i32),
+        ("n_args", i32), ("mlp_depth", i32), ("mlp_widths", i32 * 9), ("diffusion", i32),
+        ("vbt_t0", f64), ("vbt_t1", f64), ("vbt_tol", f64), ("seed", u64),
+        ("norm", i32), ("pad0", i32),
+        ("dtype", i32), ("kernel", i32), ("adjoint", i32), ("checkpoints", i32),
+        ("block_threads", i32), ("ctas_per_sm", i32),
+    ]
+
+
+# The leading block shared with the oracle descriptor.
+ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:30]
+
+_lock = threading.Lock()
+_LIB = None
+
+
+def load():
+    """Build (when stale) and load libgbdx.so; raise loudly on failure."""
+    global _LIB
+    with _lock:
+        if _LIB is not None:
+            return _LIB
+        path = _build.LIB_PATH
+        if _build.is_stale():
+            path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"libgbdx.so is missing at {path}")
+        lib = _c.CDLL(path)
+        lib.gbdx_problem_create.argtypes = [_c.POINTER(ProblemDesc), _c.POINTER(vp)]
+        lib.gbdx_problem_create.restype = i32
+        lib.gbdx_problem_destroy.argtypes = [vp]
+        lib.gbdx_problem_destroy.restype = i32
+        lib.gbdx_num_saves.argtypes = [vp]
+        lib.gbdx_num_saves.restype = i32
+        lib.gbdx_workspace_size.argtypes = [vp, i64]
+        lib.gbdx_workspace_size.restype = _c.c_size_t
+        lib.gbdx_param_count.argtypes = [vp]
+        lib.gbdx_param_count.restype = i64
+        lib.gbdx_solve_fwd.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, i64, vp, vp, vp,
+                                       vp, vp, vp, vp, _c.c_size_t, vp]
+        lib.gbdx_solve_fwd.restype = i32
+        lib.gbdx_last_error.argtypes = []
+        lib.gbdx_last_error.restype = _c.c_char_p
+        lib.gbdx_version.restype = i32
+        lib.gbdx_problem_desc_size.restype = _c.c_size_t
+        if lib.gbdx_problem_desc_size() != _c.sizeof(ProblemDesc):
+            raise RuntimeError("gbdx_problem_desc layout mismatch between Python and C")
+        _LIB = lib
+        return lib
+
+
+def last_error() -> str:
+    return load().gbdx_last_error().decode()
+
+
+class GbdxError(RuntimeError):
+    pass
+
+
+def check(rc: int, what: str):
+    if rc != 0:
+        msg = last_error()
+        if rc == -1:
+            raise ValueError(f"{what}: {msg}")
+        raise GbdxError(f"{what} failed ({rc}): {msg}")
+
+
+def make_desc(fields: dict) -> ProblemDesc:
+    d = ProblemDesc()
+    for k, v in fields.items():
+        if k == "mlp_widths":
+            d.mlp_widths = (i32 * 9)(*([int(x) for x in v] + [0] * (9 - len(v))))
+        elif k in ("dtmin", "dtmax") and v is None:
+            setattr(d, k, math.nan)
+        else:
+            setattr(d, k, v)
+    return d
+
+
+class Problem:
+    """Owns a gbdx_problem handle."""
+
+    def __init__(self, fields: dict):
+        self.lib = load()
+        self.fields = dict(fields)
+        self.desc = make_desc(fields)
+        h = vp()
+        check(self.lib.gbdx_problem_create(_c.byref(self.desc), _c.byref(h)),
+              "gbdx_problem_create")
+        self.handle = h
+
+    @property
+    def n_save(self) -> int:
+        return self.lib.gbdx_num_saves(self.handle)
+
+    def workspace_size(self, batch: int) -> int:
+        return self.lib.gbdx_workspace_size(self.handle, batch)
+
+    def param_count(self) -> int:
+        return self.lib.gbdx_param_count(self.handle)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self.lib.gbdx_problem_destroy(h)
+            except Exception:
+                pass
+
+
+_problem_cache: dict = {}
+
+
+def get_problem(fields: dict) -> Problem:
+    key = tuple(sorted((k, tuple(v) if isinstance(v, (list, tuple)) else v)
+                       for k, v in fields.items()))
+    p = _problem_cache.get(key)
+    if p is None:
+        p = Problem(fields)
+        _problem_cache[key] = p
+    return p

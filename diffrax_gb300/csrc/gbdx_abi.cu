@@ -1,0 +1,250 @@
+// gbdx_abi.cu -- the extern "C" boundary of libgbdx.so.
+//
+// Validation mirrors the ValueErrors that diffeqsolve raises at trace time
+// (diffrax/_integrate.py:1036-1154, pid.py:437-447, constant.py:42-46).  A
+// solve never allocates: scratch comes from the caller's workspace.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+
+#include "../../include/gbdx.h"
+#include "gbdx_launch.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(GBDX_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+constexpr size_t kQueueBytes = 256;
+
+}  // namespace
+
+struct gbdx_problem {
+  gbdx_problem_desc d;
+  int n_save;
+  double c1, c2, c3;  // PID exponents
+  gbdx::OdeEntry ode;
+};
+
+extern "C" {
+
+int gbdx_version(void) { return 1; }
+
+size_t gbdx_problem_desc_size(void) { return sizeof(gbdx_problem_desc); }
+
+const char *gbdx_last_error(void) { return g_last_error.c_str(); }
+
+static int solver_order(int solver) {
+  switch (solver) {
+    case GBDX_EULER: return 1;
+    case GBDX_HEUN: return 2;
+    default: return 5;
+  }
+}
+static double solver_strong_order(int solver) {
+  return (solver == GBDX_EULER || solver == GBDX_HEUN) ? 0.5 : 0.0;
+}
+
+int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
+  if (!desc || !out) return fail(GBDX_ERR_INVALID, "null descriptor or output handle");
+  *out = nullptr;
+  const gbdx_problem_desc &d = *desc;
+  if (d.solver < GBDX_EULER || d.solver > GBDX_TSIT5)
+    return fail(GBDX_ERR_INVALID, "unknown solver %d", d.solver);
+  if (d.controller != GBDX_CONSTANT && d.controller != GBDX_PID)
+    return fail(GBDX_ERR_INVALID, "unknown step size controller %d", d.controller);
+  if (d.dtype != GBDX_F32 && d.dtype != GBDX_F64)
+    return fail(GBDX_ERR_INVALID, "unknown dtype %d", d.dtype);
+  if (d.dim < 1) return fail(GBDX_ERR_INVALID, "state dimension must be positive");
+  if (d.max_steps < 1) return fail(GBDX_ERR_INVALID, "max_steps must be a positive integer");
+  if (d.n_ts < 0) return fail(GBDX_ERR_INVALID, "negative number of SaveAt(ts=...) points");
+  const int n_save = (d.save_t0 ? 1 : 0) + d.n_ts + (d.save_t1 ? 1 : 0);
+  if (n_save < 1) return fail(GBDX_ERR_INVALID, "SaveAt must save at least one point");
+  const bool sde = d.diffusion != GBDX_DIFF_NONE;
+  // pid.py:437-447: adaptive stepping needs an error estimate.
+  if (d.controller == GBDX_PID && d.solver == GBDX_EULER)
+    return fail(GBDX_ERR_INVALID,
+                "Cannot use adaptive step sizes with a solver that does not provide error "
+                "estimates.");
+  // _integrate.py:1145-1151
+  if (sde && d.controller == GBDX_PID && d.solver == GBDX_EULER)
+    return fail(GBDX_ERR_INVALID,
+                "An SDE should not be solved with adaptive step sizes with Euler's method.");
+  if (d.controller == GBDX_PID) {
+    if (!(d.rtol >= 0) || !(d.atol >= 0))
+      return fail(GBDX_ERR_INVALID, "rtol and atol must be non-negative");
+    if (!(d.factormin > 0) || !(d.factormax > 0) || !(d.safety > 0))
+      return fail(GBDX_ERR_INVALID, "factormin, factormax and safety must be positive");
+  }
+
+  gbdx_problem *p = new gbdx_problem();
+  p->d = d;
+  p->n_save = n_save;
+  double order = d.error_order > 0 ? d.error_order
+                                   : (sde ? solver_strong_order(d.solver) + 0.5
+                                          : (double)solver_order(d.solver));
+  p->c1 = (d.icoeff + d.pcoeff + d.dcoeff) / order;
+  p->c2 = -(d.pcoeff + 2 * d.dcoeff) / order;
+  p->c3 = d.dcoeff / order;
+  p->ode = gbdx::OdeEntry{nullptr, nullptr};
+  if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
+               d.field == GBDX_ORNSTEIN_UHLENBECK)) {
+    p->ode = d.dtype == GBDX_F32 ? gbdx::find_ode_entry_f32(d.solver, d.field, d.dim)
+                                 : gbdx::find_ode_entry_f64(d.solver, d.field, d.dim);
+    if (!p->ode.launch) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED, "no kernel for field %d with state dimension %d",
+                  d.field, d.dim);
+    }
+  } else {
+    delete p;
+    return fail(GBDX_ERR_UNSUPPORTED, "field %d (diffusion %d) is not available", d.field,
+                d.diffusion);
+  }
+  *out = p;
+  return GBDX_OK;
+}
+
+int gbdx_problem_destroy(gbdx_problem *problem) {
+  delete problem;
+  return GBDX_OK;
+}
+
+int gbdx_num_saves(const gbdx_problem *problem) { return problem ? problem->n_save : -1; }
+
+int64_t gbdx_param_count(const gbdx_problem *problem) {
+  if (!problem) return -1;
+  const gbdx_problem_desc &d = problem->d;
+  int64_t n = 0;
+  if (d.field == GBDX_MLP)
+    for (int l = 0; l < d.mlp_depth; l++)
+      n += (int64_t)d.mlp_widths[l] * d.mlp_widths[l + 1] + d.mlp_widths[l + 1];
+  if (d.field == GBDX_LINEAR) n += (int64_t)d.dim * d.dim;
+  if (d.diffusion == GBDX_DIFF_TANH_DIAG) n += (int64_t)d.dim * d.dim + d.dim;
+  return n;
+}
+
+size_t gbdx_workspace_size(const gbdx_problem *problem, int64_t batch) {
+  (void)batch;
+  if (!problem) return 0;
+  return kQueueBytes;
+}
+
+static int device_sm_count(int *sms) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  e = cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  return GBDX_OK;
+}
+
+int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
+                   const double *t1, const double *dt0, int64_t time_stride,
+                   const void *y0, const void *args, int64_t args_stride,
+                   const void *params, const double *save_ts, void *ys_out,
+                   double *ts_out, int32_t *result_out, int32_t *stats_out,
+                   void *workspace, size_t workspace_bytes, void *stream) {
+  if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
+  const gbdx_problem_desc &d = problem->d;
+  if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
+  if (batch == 0) return GBDX_OK;
+  if (!t0 || !t1 || !y0 || !ys_out || !ts_out || !result_out || !stats_out)
+    return fail(GBDX_ERR_INVALID, "null input or output pointer");
+  if (time_stride != 0 && time_stride != 1)
+    return fail(GBDX_ERR_INVALID, "time_stride must be 0 or 1");
+  if (d.controller == GBDX_CONSTANT && !dt0)
+    return fail(GBDX_ERR_INVALID,
+                "Constant step size solvers cannot select step size automatically; please "
+                "pass a value for `dt0`.");
+  if (d.n_ts > 0 && !save_ts) return fail(GBDX_ERR_INVALID, "SaveAt(ts=...) without ts");
+  if (d.n_args > 0 && !args) return fail(GBDX_ERR_INVALID, "field arguments missing");
+  if (workspace_bytes < gbdx_workspace_size(problem, batch) || !workspace)
+    return fail(GBDX_ERR_WORKSPACE, "workspace of %zu bytes is smaller than %zu",
+                workspace_bytes, gbdx_workspace_size(problem, batch));
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+
+  gbdx::SolveParams P;
+  memset(&P, 0, sizeof P);
+  P.batch = batch;
+  P.t0 = t0;
+  P.t1 = t1;
+  P.dt0 = dt0;
+  P.time_stride = time_stride;
+  P.y0 = y0;
+  P.args = args;
+  P.args_stride = args_stride;
+  P.params = params;
+  P.save_ts = save_ts;
+  P.ys_out = ys_out;
+  P.ts_out = ts_out;
+  P.result_out = result_out;
+  P.stats_out = stats_out;
+  P.controller = d.controller;
+  P.rtol = d.rtol;
+  P.atol = d.atol;
+  P.safety = d.safety;
+  P.factormin = d.factormin;
+  P.factormax = d.factormax;
+  P.has_dtmin = !isnan(d.dtmin);
+  P.has_dtmax = !isnan(d.dtmax);
+  P.dtmin = d.dtmin;
+  P.dtmax = d.dtmax;
+  P.force_dtmin = d.force_dtmin;
+  P.c1 = problem->c1;
+  P.c2 = problem->c2;
+  P.c3 = problem->c3;
+  P.n_ts = d.n_ts;
+  P.save_t0 = d.save_t0 ? 1 : 0;
+  P.save_t1 = d.save_t1 ? 1 : 0;
+  P.n_save = problem->n_save;
+  P.max_steps = d.max_steps;
+  P.queue = reinterpret_cast<unsigned long long *>(workspace);
+
+  gbdx::LaunchCfg cfg;
+  cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;
+  cfg.block = d.block_threads > 0 ? d.block_threads : 128;
+  if (cfg.block % 32 != 0 || cfg.block > 256)
+    return fail(GBDX_ERR_INVALID, "block_threads must be a multiple of 32 up to 256");
+  cfg.grid = 1;
+  if (cfg.kernel == GBDX_KERNEL_FUSED) {
+    int sms = 0;
+    int rc = device_sm_count(&sms);
+    if (rc != GBDX_OK) return rc;
+    int per_sm = d.ctas_per_sm;
+    if (per_sm <= 0) {
+      cudaError_t e = problem->ode.occupancy(cfg.block, &per_sm);
+      if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
+      if (per_sm < 1) per_sm = 1;
+    }
+    int64_t grid = (int64_t)sms * per_sm;
+    const int64_t needed = (batch + cfg.block - 1) / cfg.block;
+    if (grid > needed) grid = needed;
+    cfg.grid = (int)grid;
+    cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_fail(e, "queue reset");
+  }
+  cudaError_t e = problem->ode.launch(P, cfg, s);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return GBDX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,271 @@
+// gbdx_common.cuh -- device building blocks of the batched integrator.
+//
+// Everything a trajectory needs lives in registers: the state y, the RK stage
+// increments k_i, the FSAL vector, the PID history and the time grid.  Time t
+// and step size dt are FP64; the state, stages and error norm are in the state
+// dtype T (FP32 or FP64).  Semantics follow Diffrax v0.7.2:
+//   loop body ........ diffrax/_integrate.py:365-662
+//   ERK step ......... diffrax/_solver/runge_kutta.py:446-1203
+//   PID .............. diffrax/_step_size_controller/pid.py:394-567
+//   constant ......... diffrax/_step_size_controller/constant.py:59-104
+//   interpolants ..... diffrax/_solver/tsit5.py:103-156,
+//                      diffrax/_local_interpolation.py:29-139
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "../../include/gbdx.h"
+
+namespace gbdx {
+
+// ---------------------------------------------------------------------------
+// Butcher tableaus (published method constants; the reference stores the same
+// numbers in tsit5.py:18-100, dopri5.py:11-33, heun.py:12-17, euler.py).
+// ---------------------------------------------------------------------------
+template <int SOLVER>
+struct Tab;
+
+template <>
+struct Tab<GBDX_TSIT5> {
+  static constexpr int S = 7;
+  static constexpr bool FSAL = true, SSAL = true;
+  static constexpr int ORDER = 5;
+  static constexpr double STRONG_ORDER = 0.0;
+  __host__ __device__ static constexpr double bs(int j) {
+    constexpr double v[7] = {
+        0.9646076681806522951816731316512876333711995238157997181903319145764851595234062815396e-1,
+        1.0 / 100,
+        0.4798896504144995747752495322905965199130404621990332488332634944254542060153074523509,
+        1.379008574103741893192274821856872770756462643091360525934940067397245698027561293331,
+        -3.290069515436080679901047585711363850115683290894936158531296799594813811049925401677,
+        2.324710524099773982415355918398765796109060233222962411944060046314465391054716027841,
+        0.0};
+    return v[j];
+  }
+  __host__ __device__ static constexpr double c(int i) {
+    constexpr double v[7] = {
+        0.0, 161.0 / 1000, 327.0 / 1000, 9.0 / 10,
+        0.9800255409045096857298102862870245954942137979563024768854764293221195950761080302604,
+        1.0, 1.0};
+    return v[i];
+  }
+  __host__ __device__ static constexpr double a(int i, int j) {
+    constexpr double v[7][6] = {
+        {0, 0, 0, 0, 0, 0},
+        {161.0 / 1000, 0, 0, 0, 0, 0},
+        {-0.8480655492356988544426874250230774675121177393430391537369234245294192976164141156943e-2,
+         0.3354806554923569885444268742502307746751211773934303915373692342452941929761641411569, 0,
+         0, 0, 0},
+        {2.897153057105493432130432594192938764924887287701866490314866693455023795137503079289,
+         -6.359448489975074843148159912383825625952700647415626703305928850207288721235210244366,
+         4.362295432869581411017727318190886861027813359713760212991062156752264926097707165077, 0,
+         0, 0},
+        {5.325864828439256604428877920840511317836476253097040101202360397727981648835607691791,
+         -11.74888356406282787774717033978577296188744178259862899288666928009020615663593781589,
+         7.495539342889836208304604784564358155658679161518186721010132816213648793440552049753,
+         -0.9249506636175524925650207933207191611349983406029535244034750452930469056411389539635e-1,
+         0, 0},
+        {5.861455442946420028659251486982647890394337666164814434818157239052507339770711679748,
+         -12.92096931784710929170611868178335939541780751955743459166312250439928519268343184452,
+         8.159367898576158643180400794539253485181918321135053305748355423955009222648673734986,
+         -0.7158497328140099722453054252582973869127213147363544882721139659546372402303777878835e-1,
+         -0.2826905039406838290900305721271224146717633626879770007617876201276764571291579142206e-1,
+         0},
+        {0.9646076681806522951816731316512876333711995238157997181903319145764851595234062815396e-1,
+         1.0 / 100,
+         0.4798896504144995747752495322905965199130404621990332488332634944254542060153074523509,
+         1.379008574103741893192274821856872770756462643091360525934940067397245698027561293331,
+         -3.290069515436080679901047585711363850115683290894936158531296799594813811049925401677,
+         2.324710524099773982415355918398765796109060233222962411944060046314465391054716027841}};
+    return v[i][j];
+  }
+  __host__ __device__ static constexpr double b(int j) { return bs(j); }
+  __host__ __device__ static constexpr double e(int j) {
+    constexpr double v[7] = {
+        0.9646076681806522951816731316512876333711995238157997181903319145764851595234062815396e-1 -
+            0.9468075576583945807478876255758922856117527357724631226139574065785592789071067303271e-1,
+        1.0 / 100 -
+            0.9183565540343253096776363936645313759813746240984095238905939532922955247253608687270e-2,
+        0.4798896504144995747752495322905965199130404621990332488332634944254542060153074523509 -
+            0.4877705284247615707855642599631228241516691959761363774365216240304071651579571959813,
+        1.379008574103741893192274821856872770756462643091360525934940067397245698027561293331 -
+            1.234297566930478985655109673884237654035539930748192848315425833500484878378061439761,
+        -3.290069515436080679901047585711363850115683290894936158531296799594813811049925401677 +
+            2.707712349983525454881109975059321670689605166938197378763992255714444407154902012702,
+        2.324710524099773982415355918398765796109060233222962411944060046314465391054716027841 -
+            1.866628418170587035753719399566211498666255505244122593996591602841258328965767580089,
+        -1.0 / 66};
+    return v[j];
+  }
+};
+
+template <>
+struct Tab<GBDX_DOPRI5> {
+  static constexpr int S = 7;
+  static constexpr bool FSAL = true, SSAL = true;
+  static constexpr int ORDER = 5;
+  static constexpr double STRONG_ORDER = 0.0;
+  __host__ __device__ static constexpr double c(int i) {
+    constexpr double v[7] = {0.0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1.0, 1.0};
+    return v[i];
+  }
+  __host__ __device__ static constexpr double a(int i, int j) {
+    constexpr double v[7][6] = {
+        {0, 0, 0, 0, 0, 0},
+        {1.0 / 5, 0, 0, 0, 0, 0},
+        {3.0 / 40, 9.0 / 40, 0, 0, 0, 0},
+        {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0, 0},
+        {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0, 0},
+        {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656, 0},
+        {35.0 / 384, 0.0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84}};
+    return v[i][j];
+  }
+  __host__ __device__ static constexpr double b(int j) {
+    constexpr double v[7] = {35.0 / 384, 0.0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784,
+                             11.0 / 84, 0.0};
+    return v[j];
+  }
+  __host__ __device__ static constexpr double e(int j) {
+    constexpr double v[7] = {35.0 / 384 - 1951.0 / 21600, 0.0, 500.0 / 1113 - 22642.0 / 50085,
+                             125.0 / 192 - 451.0 / 720, -2187.0 / 6784 - -12231.0 / 42400,
+                             11.0 / 84 - 649.0 / 6300, -1.0 / 60.0};
+    return v[j];
+  }
+  // Dense-output midpoint weights (dopri5.py:36-47).
+  __host__ __device__ static constexpr double cmid(int j) {
+    constexpr double v[7] = {6025192743.0 / 30085553152.0 / 2, 0.0,
+                             51252292925.0 / 65400821598.0 / 2,
+                             -2691868925.0 / 45128329728.0 / 2,
+                             187940372067.0 / 1594534317056.0 / 2,
+                             -1776094331.0 / 19743644256.0 / 2, 11237099.0 / 235043384.0 / 2};
+    return v[j];
+  }
+};
+
+template <>
+struct Tab<GBDX_HEUN> {
+  static constexpr int S = 2;
+  static constexpr bool FSAL = false, SSAL = false;
+  static constexpr int ORDER = 2;
+  static constexpr double STRONG_ORDER = 0.5;
+  __host__ __device__ static constexpr double c(int i) { return i == 0 ? 0.0 : 1.0; }
+  __host__ __device__ static constexpr double a(int i, int j) { return (i == 1 && j == 0) ? 1.0 : 0.0; }
+  __host__ __device__ static constexpr double b(int j) { return 0.5; }
+  __host__ __device__ static constexpr double e(int j) { return j == 0 ? 0.5 : -0.5; }
+};
+
+template <>
+struct Tab<GBDX_EULER> {
+  static constexpr int S = 1;
+  static constexpr bool FSAL = false, SSAL = false;
+  static constexpr int ORDER = 1;
+  static constexpr double STRONG_ORDER = 0.5;
+  __host__ __device__ static constexpr double c(int) { return 0.0; }
+  __host__ __device__ static constexpr double a(int, int) { return 0.0; }
+  __host__ __device__ static constexpr double b(int) { return 1.0; }
+  __host__ __device__ static constexpr double e(int) { return 0.0; }
+};
+
+// ---------------------------------------------------------------------------
+// Precision helpers.
+// ---------------------------------------------------------------------------
+template <class T>
+struct Math;
+template <>
+struct Math<float> {
+  __device__ static __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+  __device__ static __forceinline__ float abs_(float x) { return fabsf(x); }
+  __device__ static __forceinline__ float log2_(float x) { return log2f(x); }
+  __device__ static __forceinline__ float exp2_(float x) { return exp2f(x); }
+  __device__ static __forceinline__ float tanh_(float x) { return tanhf(x); }
+};
+template <>
+struct Math<double> {
+  __device__ static __forceinline__ double sqrt_(double x) { return sqrt(x); }
+  __device__ static __forceinline__ double abs_(double x) { return fabs(x); }
+  __device__ static __forceinline__ double log2_(double x) { return log2(x); }
+  __device__ static __forceinline__ double exp2_(double x) { return exp2(x); }
+  __device__ static __forceinline__ double tanh_(double x) { return tanh(x); }
+};
+
+__device__ __forceinline__ bool is_nan_(float x) { return isnan(x); }
+__device__ __forceinline__ bool is_nan_(double x) { return isnan(x); }
+
+// nextafter(x, -inf) and nextafter(x, +inf) on the IEEE bit pattern.
+__device__ __forceinline__ double next_down(double x) {
+  if (isnan(x) || x == -INFINITY) return x;
+  if (x == 0.0) return -4.9406564584124654e-324;
+  long long b = __double_as_longlong(x);
+  b += (x > 0.0) ? -1 : 1;
+  return __longlong_as_double(b);
+}
+__device__ __forceinline__ double next_up(double x) { return -next_down(-x); }
+
+// t1 minus 100 ULP (_integrate.py:319-322): the threshold above which tnext
+// is snapped to t1.
+__device__ __forceinline__ double t1_clip_floor(double t1) {
+  double x = t1;
+#pragma unroll 1
+  for (int i = 0; i < 100; i++) x = next_down(x);
+  return x;
+}
+
+// ---------------------------------------------------------------------------
+// Registered analytic vector fields.  All are autonomous, so stage times are
+// never formed (runge_kutta.py:1023 computes them only to pass to vf).
+// ---------------------------------------------------------------------------
+template <class T>
+struct LotkaVolterra {
+  static constexpr int D = 2, NARGS = 4;
+  __device__ static __forceinline__ void vf(const T *a, const T *y, T *o) {
+    o[0] = a[0] * y[0] - a[1] * y[0] * y[1];
+    o[1] = -a[2] * y[1] + a[3] * y[0] * y[1];
+  }
+};
+
+template <class T>
+struct VanDerPol {
+  static constexpr int D = 2, NARGS = 1;
+  __device__ static __forceinline__ void vf(const T *a, const T *y, T *o) {
+    o[0] = y[1];
+    o[1] = a[0] * (T(1) - y[0] * y[0]) * y[1] - y[0];
+  }
+};
+
+template <class T, int D_>
+struct OrnsteinUhlenbeck {
+  static constexpr int D = D_, NARGS = 3;
+  __device__ static __forceinline__ void vf(const T *a, const T *y, T *o) {
+#pragma unroll
+    for (int i = 0; i < D; i++) o[i] = a[0] * (a[1] - y[i]);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Kernel parameters shared by every analytic-field launch.
+// ---------------------------------------------------------------------------
+struct SolveParams {
+  int64_t batch;
+  const double *t0, *t1, *dt0;
+  int64_t time_stride;
+  const void *y0;
+  const void *args;
+  int64_t args_stride;
+  const void *params;
+  const double *save_ts;
+  void *ys_out;
+  double *ts_out;
+  int32_t *result_out;
+  int32_t *stats_out;
+  // controller / problem constants
+  int controller;
+  double rtol, atol, safety, factormin, factormax, dtmin, dtmax;
+  int has_dtmin, has_dtmax, force_dtmin;
+  double c1, c2, c3;  // PID exponents (i+p+d)/k, -(p+2d)/k, d/k
+  int n_ts, save_t0, save_t1, n_save, max_steps;
+  unsigned long long *queue;  // work-stealing counter (fused kernel)
+};
+
+}  // namespace gbdx

@@ -1,0 +1,56 @@
+// gbdx_ode_impl.cuh -- launchers of the analytic-field kernels (K0 plain,
+// K1 fused) for one state dtype.  Included once per dtype translation unit so
+// the instantiations compile in parallel.
+#pragma once
+
+#include "gbdx_launch.h"
+#include "gbdx_traj.cuh"
+
+namespace gbdx {
+
+template <int SOLVER, class FIELD, class T>
+cudaError_t launch_ode(const SolveParams &P, const LaunchCfg &cfg, cudaStream_t s) {
+  if (P.batch <= 0) return cudaSuccess;
+  if (cfg.kernel == GBDX_KERNEL_PLAIN) {
+    const int64_t blocks = (P.batch + 127) / 128;
+    plain_kernel<SOLVER, FIELD, T><<<(unsigned)blocks, 128, 0, s>>>(P);
+  } else {
+    fused_kernel<SOLVER, FIELD, T><<<cfg.grid, cfg.block, 0, s>>>(P);
+  }
+  return cudaGetLastError();
+}
+
+template <int SOLVER, class FIELD, class T>
+cudaError_t occupancy_ode(int block, int *ctas_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      ctas_per_sm, fused_kernel<SOLVER, FIELD, T>, block, 0);
+}
+
+template <class T>
+OdeEntry find_ode_entry_t(int solver, int field, int dim) {
+#define GBDX_ENTRY(S, F) \
+  OdeEntry { &launch_ode<S, F, T>, &occupancy_ode<S, F, T> }
+#define GBDX_SOLVERS(F)                                        \
+  switch (solver) {                                            \
+    case GBDX_EULER: return GBDX_ENTRY(GBDX_EULER, F);         \
+    case GBDX_HEUN: return GBDX_ENTRY(GBDX_HEUN, F);           \
+    case GBDX_DOPRI5: return GBDX_ENTRY(GBDX_DOPRI5, F);       \
+    case GBDX_TSIT5: return GBDX_ENTRY(GBDX_TSIT5, F);         \
+    default: return OdeEntry{nullptr, nullptr};                \
+  }
+  if (field == GBDX_LOTKA_VOLTERRA && dim == 2) { GBDX_SOLVERS(LotkaVolterra<T>) }
+  if (field == GBDX_VAN_DER_POL && dim == 2) { GBDX_SOLVERS(VanDerPol<T>) }
+  using OU1 = OrnsteinUhlenbeck<T, 1>;
+  using OU2 = OrnsteinUhlenbeck<T, 2>;
+  using OU4 = OrnsteinUhlenbeck<T, 4>;
+  if (field == GBDX_ORNSTEIN_UHLENBECK) {
+    if (dim == 1) { GBDX_SOLVERS(OU1) }
+    if (dim == 2) { GBDX_SOLVERS(OU2) }
+    if (dim == 4) { GBDX_SOLVERS(OU4) }
+  }
+#undef GBDX_SOLVERS
+#undef GBDX_ENTRY
+  return OdeEntry{nullptr, nullptr};
+}
+
+}  // namespace gbdx

@@ -1,0 +1,393 @@
+// gbdx_traj.cuh -- one trajectory of a vmapped diffeqsolve, held in registers.
+//
+// Traj<SOLVER, FIELD, T>::step() is one iteration of the reference's outer
+// while-loop body (diffrax/_integrate.py:365-662): an explicit RK step, the
+// NaN->inf error guard (:386), the controller (pid.py:394-567 or
+// constant.py:59-104), clip-to-end (:410-413, 278-284), the keep/reject select
+// (:422-430), the step counters (:433-437) and the SaveAt(ts) loop (:456-487).
+// init() follows diffeqsolve's set-up (:1036-1305) and finish() the t1 save and
+// max_steps_reached result (:847-883).
+#pragma once
+
+#include "gbdx_common.cuh"
+
+namespace gbdx {
+
+template <class T>
+__device__ __forceinline__ T tsit5_w(int j, T t) {
+  // Tsit5 dense-output weights b_j(theta) (tsit5.py:119-150).
+  switch (j) {
+    case 0:
+      return T(-1.0530884977290216) * t * (t - T(1.3299890189751412)) *
+             (t * t - T(1.4364028541716351) * t + T(0.7139816917074209));
+    case 1:
+      return T(0.1017) * t * t * (t * t - T(2.1966568338249754) * t + T(1.2949852507374631));
+    case 2:
+      return T(2.490627285651252793) * t * t *
+             (t * t - T(2.38535645472061657) * t + T(1.57803468208092486));
+    case 3:
+      return T(-16.54810288924490272) * (t - T(1.21712927295533244)) *
+             (t - T(0.61620406037800089)) * t * t;
+    case 4:
+      return T(47.37952196281928122) * (t - T(1.203071208372362603)) *
+             (t - T(0.658047292653547382)) * t * t;
+    case 5:
+      return T(-34.87065786149660974) * (t - T(1.2)) * (t - T(0.666666666666666667)) * t * t;
+    default:
+      return T(2.5) * (t - T(1)) * (t - T(0.6)) * t * t;
+  }
+}
+
+template <int SOLVER, class FIELD, class T>
+struct Traj {
+  using TB = Tab<SOLVER>;
+  static constexpr int D = FIELD::D;
+  static constexpr int S = TB::S;
+  static constexpr int NA = FIELD::NARGS > 0 ? FIELD::NARGS : 1;
+  static constexpr bool F32 = sizeof(T) == 4;
+
+  T y[D];
+  T f0[D];  // FSAL: f(t_n, y_n) from the last stage of the previous step
+  T args[NA];
+  double tprev, tnext, t1, floor1;
+  // PID history (pid.py:388-392).  FP32 keeps log2 of the inverse scaled
+  // errors so the factor is one exp2 of a weighted sum; FP64 keeps the values.
+  T h1, h2;
+  int at_dtmin;
+  int sc, nc;  // ConstantStepSize state (constant.py:41-57)
+  double t0s, t1s;
+  int first, dir, save_index, ts_index, nsteps, nacc, nrej, result;
+  int64_t idx;
+
+  __device__ __forceinline__ bool running(const SolveParams &P) const {
+    return tprev < t1 && result == GBDX_SUCCESSFUL && nsteps < P.max_steps;
+  }
+
+  __device__ __forceinline__ T *ys_row(const SolveParams &P, int slot) const {
+    return reinterpret_cast<T *>(P.ys_out) + (idx * P.n_save + slot) * D;
+  }
+
+  __device__ void init(const SolveParams &P, int64_t i) {
+    idx = i;
+    const int64_t ti = i * P.time_stride;
+    double a = P.t0[ti], b = P.t1[ti];
+    dir = (a < b) ? 1 : -1;  // _integrate.py:1160
+    a *= dir;
+    b *= dir;
+    t1 = b;
+    const T *y0 = reinterpret_cast<const T *>(P.y0) + i * D;
+#pragma unroll
+    for (int n = 0; n < D; n++) y[n] = y0[n];
+    const T *ag = reinterpret_cast<const T *>(P.args) + i * P.args_stride;
+#pragma unroll
+    for (int n = 0; n < FIELD::NARGS; n++) args[n] = ag[n];
+    double tn;
+    if (P.controller == GBDX_PID) {
+      // Terms are wrapped before PIDController.init (_integrate.py:1172-1176,
+      // 1254), so dt0=None selects 0.01 (pid.py:48-49).
+      double h = P.dt0 ? P.dt0[ti] * dir : 0.01;
+      if (P.has_dtmax) h = fmin(h, P.dtmax);
+      if (P.has_dtmin) h = fmax(h, P.dtmin);
+      tn = a + h;
+      h1 = F32 ? T(0) : T(1);
+      h2 = h1;
+      at_dtmin = 0;
+    } else {
+      double h = P.dt0[ti] * dir;
+      sc = 1;
+      nc = (int)ceil((b - a) / next_up(h));
+      t0s = a;
+      t1s = b;
+      tn = a + h;
+    }
+    tnext = fmin(tn, b);
+    tprev = a;
+    floor1 = t1_clip_floor(b);
+    first = 1;
+    save_index = 0;
+    ts_index = 0;
+    nsteps = nacc = nrej = 0;
+    result = GBDX_SUCCESSFUL;
+    if (P.save_t0) {
+      T *o = ys_row(P, 0);
+#pragma unroll
+      for (int n = 0; n < D; n++) o[n] = y[n];
+      P.ts_out[idx * P.n_save] = a * dir;
+      save_index = 1;
+    }
+  }
+
+  // One loop iteration.
+  __device__ void step(const SolveParams &P) {
+    const double dt = tnext - tprev;
+    const T h = T(dir * dt);
+    T k[S][D];
+    T f[D], yi[D], y1[D], err[D], flast[D];
+    // Stage 0: FSAL reuse except on the first step (runge_kutta.py:684-700).
+    if (TB::FSAL && !first) {
+#pragma unroll
+      for (int n = 0; n < D; n++) f[n] = f0[n];
+    } else {
+      FIELD::vf(args, y, f);
+    }
+#pragma unroll
+    for (int n = 0; n < D; n++) k[0][n] = f[n] * h;
+#pragma unroll
+    for (int i = 1; i < S; i++) {
+#pragma unroll
+      for (int n = 0; n < D; n++) {
+        T inc = T(0);
+#pragma unroll
+        for (int j = 0; j < i; j++)
+          if (TB::a(i, j) != 0.0) inc += T(TB::a(i, j)) * k[j][n];
+        yi[n] = y[n] + inc;
+      }
+      FIELD::vf(args, yi, f);
+#pragma unroll
+      for (int n = 0; n < D; n++) k[i][n] = f[n] * h;
+      if (i == S - 1) {
+#pragma unroll
+        for (int n = 0; n < D; n++) flast[n] = f[n];
+      }
+    }
+    // y1 (SSAL: the last stage's input, runge_kutta.py:1177-1185) and the
+    // embedded error estimate (:1186-1197).
+#pragma unroll
+    for (int n = 0; n < D; n++) {
+      if constexpr (TB::SSAL) {
+        y1[n] = yi[n];
+      } else {
+        T inc = T(0);
+#pragma unroll
+        for (int j = 0; j < S; j++) inc += T(TB::b(j)) * k[j][n];
+        y1[n] = y[n] + inc;
+      }
+      T e = T(0);
+#pragma unroll
+      for (int j = 0; j < S; j++)
+        if (TB::e(j) != 0.0) e += T(TB::e(j)) * k[j][n];
+      err[n] = is_nan_(e) ? T(INFINITY) : e;
+    }
+
+    bool keep;
+    double nt0, nt1;
+    if (P.controller == GBDX_PID) {
+      // scaled = rms(err / (atol + rtol max(|y0|, |y1|))), y1 -> y0 if NaN
+      // (pid.py:466-492).
+      bool any_nan = false;
+#pragma unroll
+      for (int n = 0; n < D; n++) any_nan |= is_nan_(y1[n]);
+      T acc = T(0);
+#pragma unroll
+      for (int n = 0; n < D; n++) {
+        T ym = fmax(Math<T>::abs_(y[n]), Math<T>::abs_(any_nan ? y[n] : y1[n]));
+        T s = err[n] / (T(P.atol) + ym * T(P.rtol));
+        acc += s * s;
+      }
+      const double prev_dt = dt;
+      T factor;
+      T hnew;
+      if constexpr (F32) {
+        // log2(1/scaled) = 0.5 (log2 D - log2 acc); keep <=> scaled < 1.
+        const T scaled = Math<T>::sqrt_(acc) / Math<T>::sqrt_(T(D));
+        keep = scaled < T(1);
+        T lg = -Math<T>::log2_(scaled);
+        T ex = T(0);
+        if (P.c1 != 0.0) ex += T(P.c1) * lg;
+        if (P.c2 != 0.0) ex += T(P.c2) * h1;
+        if (P.c3 != 0.0) ex += T(P.c3) * h2;
+        factor = T(P.safety) * Math<T>::exp2_(ex);
+        hnew = isinf(lg) ? T(0) : lg;  // inv in {0, inf} -> 1 (pid.py:538)
+      } else {
+        const T scaled = Math<T>::sqrt_(acc) / Math<T>::sqrt_(T(D));
+        keep = scaled < T(1);
+        T inv = T(1) / scaled;
+        T f1 = (P.c1 == 0.0) ? T(1) : T(pow(double(inv), P.c1));
+        T f2 = (P.c2 == 0.0) ? T(1) : T(pow(double(h1), P.c2));
+        T f3 = (P.c3 == 0.0) ? T(1) : T(pow(double(h2), P.c3));
+        factor = T(P.safety) * f1 * f2 * f3;
+        hnew = (inv == T(0) || isinf(inv)) ? T(1) : inv;
+      }
+      if (P.has_dtmin) keep = keep || at_dtmin;
+      const T fmn = keep ? T(1) : T(P.factormin);
+      const T fmx = keep ? T(P.factormax) : T(P.safety);
+      factor = fmin(fmax(factor, fmn), fmx);
+      double dtn = prev_dt * double(factor);
+      if (P.has_dtmax) dtn = fmin(dtn, P.dtmax);
+      if (P.has_dtmin) {
+        if (!P.force_dtmin && dtn < P.dtmin && result == GBDX_SUCCESSFUL)
+          result = GBDX_DT_MIN_REACHED;
+        if (at_dtmin && factor == T(1)) dtn = P.dtmin;
+        at_dtmin = dtn <= P.dtmin;
+        dtn = fmax(dtn, P.dtmin);
+      }
+      nt0 = keep ? tnext : tprev;
+      nt1 = nt0 + dtn;
+      if (keep) {
+        h2 = h1;
+        h1 = hnew;
+      }
+    } else {
+      keep = true;
+      const int s2 = sc + 1;
+      double tn = t0s + (t1s - t0s) * (double(s2) / double(nc));
+      if (s2 == nc) tn = t1s;
+      sc = s2;
+      nt0 = tnext;
+      nt1 = tn;
+    }
+    // Book-keeping (_integrate.py:410-413).
+    nt0 = fmin(nt0, t1);
+    if (nt1 > floor1) nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
+
+    if (keep) {
+      // SaveAt(ts): every ts <= tnext of the step just taken, interpolated
+      // inside [tprev, tnext] (_integrate.py:456-487).
+      while (ts_index < P.n_ts) {
+        const double tsv = __ldg(P.save_ts + ts_index);
+        const double tsd = dir * tsv;
+        if (!(tsd <= tnext)) break;
+        const double thd = (tprev == tnext) ? 0.0 : (tsd - tprev) / (tnext - tprev);
+        const T th = T(thd);
+        T *o = ys_row(P, save_index);
+#pragma unroll
+        for (int n = 0; n < D; n++) o[n] = interp(th, n, k, y1);
+        P.ts_out[idx * P.n_save + save_index] = tsv;
+        ts_index++;
+        save_index++;
+      }
+#pragma unroll
+      for (int n = 0; n < D; n++) y[n] = y1[n];
+      if (TB::FSAL) {
+#pragma unroll
+        for (int n = 0; n < D; n++) f0[n] = flast[n];
+        first = 0;
+      }
+      nacc++;
+    } else {
+      nrej++;
+    }
+    nsteps++;
+    tprev = nt0;
+    tnext = nt1;
+  }
+
+  // Dense output inside the step, component n.  y holds y0 of the step.
+  __device__ __forceinline__ T interp(T th, int n, const T (&k)[S][D], const T (&y1)[D]) const {
+    if constexpr (SOLVER == GBDX_TSIT5) {
+      T acc = T(0);
+#pragma unroll
+      for (int j = 0; j < 7; j++) acc += tsit5_w<T>(j, th) * k[j < S ? j : 0][n];
+      return y[n] + acc;
+    } else if constexpr (SOLVER == GBDX_DOPRI5) {
+      // FourthOrderPolynomialInterpolation (_local_interpolation.py:95-139)
+      T cm = T(0);
+#pragma unroll
+      for (int j = 0; j < S; j++) cm += T(Tab<GBDX_DOPRI5>::cmid(j < 7 ? j : 0)) * k[j][n];
+      const T y0 = y[n], yy1 = y1[n], ymid = y0 + cm;
+      const T fa = k[0][n], fb = k[S - 1][n];
+      const T a = T(2) * (fb - fa) - T(8) * (yy1 + y0) + T(16) * ymid;
+      const T b = T(5) * fa - T(3) * fb + T(18) * y0 + T(14) * yy1 - T(32) * ymid;
+      const T c = fb - T(4) * fa - T(11) * y0 - T(5) * yy1 + T(16) * ymid;
+      return (((a * th + b) * th + c) * th + fa) * th + y0;
+    } else if constexpr (SOLVER == GBDX_HEUN) {
+      // ThirdOrderHermitePolynomialInterpolation.from_k (:50-92)
+      const T y0 = y[n], yy1 = y1[n], ka = k[0][n], kb = k[S - 1][n];
+      const T a = ka + kb + T(2) * y0 - T(2) * yy1;
+      const T b = T(-2) * ka - kb - T(3) * y0 + T(3) * yy1;
+      return ((a * th + b) * th + ka) * th + y0;
+    } else {
+      return y[n] + th * (y1[n] - y[n]);  // LocalLinearInterpolation (:29-47)
+    }
+  }
+
+  __device__ void finish(const SolveParams &P) {
+    const double t0 = P.t0[idx * P.time_stride] * dir;
+    // t0 == t1: the ts outputs are y0 (_integrate.py:823-845).
+    if (t0 == t1) {
+      for (int m = 0; m < P.n_ts; m++) {
+        T *o = ys_row(P, save_index);
+#pragma unroll
+        for (int n = 0; n < D; n++) o[n] = y[n];
+        P.ts_out[idx * P.n_save + save_index] = t0 * dir;
+        save_index++;
+      }
+    }
+    if (P.save_t1) {
+      T *o = ys_row(P, save_index);
+#pragma unroll
+      for (int n = 0; n < D; n++) o[n] = y[n];
+      P.ts_out[idx * P.n_save + save_index] = tprev * dir;
+      save_index++;
+    }
+    for (int m = save_index; m < P.n_save; m++) {
+      T *o = ys_row(P, m);
+#pragma unroll
+      for (int n = 0; n < D; n++) o[n] = T(INFINITY);
+      P.ts_out[idx * P.n_save + m] = INFINITY;
+    }
+    int r = result;
+    if (r == GBDX_SUCCESSFUL && tprev < t1) r = GBDX_MAX_STEPS_REACHED;  // :883
+    P.result_out[idx] = r;
+    P.stats_out[idx * 3 + 0] = nsteps;
+    P.stats_out[idx * 3 + 1] = nacc;
+    P.stats_out[idx * 3 + 2] = nrej;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// K0: the plain form -- one trajectory per thread, one launch, no refill.
+// ---------------------------------------------------------------------------
+template <int SOLVER, class FIELD, class T>
+__global__ void __launch_bounds__(128) plain_kernel(SolveParams P) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= P.batch) return;
+  Traj<SOLVER, FIELD, T> tr;
+  tr.init(P, i);
+  while (tr.running(P)) tr.step(P);
+  tr.finish(P);
+}
+
+// ---------------------------------------------------------------------------
+// K1: the fused persistent form.  A grid sized to the SM count keeps every lane
+// busy: when a lane's trajectory finishes it takes the next trajectory index
+// from a device counter (one warp-aggregated atomicAdd per refill), so warps
+// never idle on the longest lane of a fixed group.
+// ---------------------------------------------------------------------------
+template <int SOLVER, class FIELD, class T>
+__global__ void __launch_bounds__(256) fused_kernel(SolveParams P) {
+  Traj<SOLVER, FIELD, T> tr;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  bool active = false;
+  bool drained = false;  // warp-uniform: the queue has no more work
+  while (true) {
+    if (!drained) {
+      const unsigned need = __ballot_sync(0xffffffffu, !active);
+      if (need) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(P.queue, (unsigned long long)__popc(need));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base + __popc(need) >= (unsigned long long)P.batch) drained = true;
+        if (!active) {
+          const unsigned long long mine = base + __popc(need & lt_mask);
+          if (mine < (unsigned long long)P.batch) {
+            tr.init(P, (int64_t)mine);
+            active = true;
+          }
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active) {
+      if (tr.running(P)) {
+        tr.step(P);
+      } else {
+        tr.finish(P);
+        active = false;
+      }
+    }
+  }
+}
+
+}  // namespace gbdx

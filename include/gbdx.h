@@ -1,0 +1,155 @@
+/*
+ * gbdx.h -- C ABI of the GB300-native batched diffeqsolve library (libgbdx.so).
+ *
+ * One problem handle describes a vmapped Diffrax solve: the solver, the step
+ * size controller, the registered vector field, what to save and how to
+ * differentiate.  Every array argument is a caller-owned CUDA device pointer;
+ * the library performs no allocation inside a solve and never synchronises the
+ * host (results, including per-trajectory RESULTS codes, stay on the device).
+ * Every call returns 0 on success or a negative gbdx_status; the message of the
+ * last failure on the calling thread is available from gbdx_last_error().
+ *
+ * Reference interfaces replaced (paths inside the Diffrax v0.7.2 tree):
+ *   gbdx_problem_create   <- the static arguments of diffeqsolve
+ *                            (diffrax/_integrate.py:888-911) and their checks
+ *                            (diffrax/_integrate.py:1036-1265)
+ *   gbdx_solve_fwd        <- jax.vmap(diffeqsolve) forward:
+ *                            AbstractAdjoint.loop (diffrax/_adjoint.py:121-143)
+ *                            driving loop() (diffrax/_integrate.py:302-885)
+ *   gbdx_solve_bwd        <- the VJP of that solve under
+ *                            RecursiveCheckpointAdjoint (diffrax/_adjoint.py:179-312)
+ *   gbdx_backsolve_bwd    <- BacksolveAdjoint's backward pass
+ *                            (diffrax/_adjoint.py:572-734, AdjointTerm
+ *                            diffrax/_term.py:767-910)
+ *   gbdx_vbt_increments   <- VirtualBrownianTree.evaluate(t0, t1)
+ *                            (diffrax/_brownian/tree.py:325-354)
+ */
+#ifndef GBDX_H_
+#define GBDX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Solvers (diffrax/_solver/{euler,heun,dopri5,tsit5}.py). */
+enum gbdx_solver { GBDX_EULER = 0, GBDX_HEUN = 1, GBDX_DOPRI5 = 2, GBDX_TSIT5 = 3 };
+/* Step size controllers (diffrax/_step_size_controller/{constant,pid}.py). */
+enum gbdx_controller { GBDX_CONSTANT = 0, GBDX_PID = 1 };
+/* Registered vector fields. */
+enum gbdx_field {
+  GBDX_LOTKA_VOLTERRA = 0,     /* args (a, b, c, d) */
+  GBDX_VAN_DER_POL = 1,        /* args (mu) */
+  GBDX_ORNSTEIN_UHLENBECK = 2, /* args (theta, mu, sigma); drift theta (mu - y) */
+  GBDX_MLP = 3,                /* eqx.nn.MLP, tanh hidden, identity output */
+  GBDX_LINEAR = 4              /* y' = A y, A in params */
+};
+/* Diagonal diffusion of a ControlTerm driven by a VirtualBrownianTree. */
+enum gbdx_diffusion { GBDX_DIFF_NONE = 0, GBDX_DIFF_OU = 1, GBDX_DIFF_TANH_DIAG = 2 };
+enum gbdx_dtype { GBDX_F32 = 0, GBDX_F64 = 1 };
+/* Kernel family: PLAIN is one trajectory per thread launched once per
+ * trajectory; FUSED is the persistent work-stealing integrator. */
+enum gbdx_kernel { GBDX_KERNEL_AUTO = 0, GBDX_KERNEL_PLAIN = 1, GBDX_KERNEL_FUSED = 2 };
+enum gbdx_adjoint { GBDX_ADJ_NONE = 0, GBDX_ADJ_RECURSIVE = 1, GBDX_ADJ_BACKSOLVE = 2 };
+enum gbdx_norm { GBDX_NORM_RMS = 0, GBDX_NORM_ADJOINT_SEMI = 1 };
+
+/* RESULTS codes written per trajectory (diffrax/_solution.py:13-31). */
+enum gbdx_result {
+  GBDX_SUCCESSFUL = 0,
+  GBDX_MAX_STEPS_REACHED = 1,
+  GBDX_DT_MIN_REACHED = 2,
+  GBDX_EVENT_OCCURRED = 3,
+  GBDX_MAX_STEPS_REJECTED = 4,
+  GBDX_INTERNAL_ERROR = 5
+};
+
+enum gbdx_status {
+  GBDX_OK = 0,
+  GBDX_ERR_INVALID = -1,     /* a ValueError in the reference */
+  GBDX_ERR_UNSUPPORTED = -2, /* combination outside this library's scope */
+  GBDX_ERR_CUDA = -3,        /* a CUDA runtime error */
+  GBDX_ERR_WORKSPACE = -4    /* workspace too small */
+};
+
+/* Problem descriptor.  The leading block is shared with the FP64 oracle's
+ * descriptor; the trailing block selects precision and kernels. */
+typedef struct gbdx_problem_desc {
+  int32_t solver, controller, field, dim;
+  double rtol, atol, pcoeff, icoeff, dcoeff, safety, factormin, factormax;
+  double dtmin, dtmax; /* NaN means None */
+  int32_t force_dtmin;
+  double error_order;  /* 0 means the solver's own (diffrax/_solver/base.py:97-120) */
+  int32_t n_ts, save_t0, save_t1, max_steps;
+  int32_t n_args;
+  int32_t mlp_depth;     /* number of linear layers */
+  int32_t mlp_widths[9]; /* widths[0] = dim, widths[mlp_depth] = dim */
+  int32_t diffusion;     /* gbdx_diffusion */
+  double vbt_t0, vbt_t1, vbt_tol;
+  uint64_t seed;
+  int32_t norm;          /* backsolve adjoint norm (gbdx_norm) */
+  int32_t pad0;
+  /* GB300 execution policy */
+  int32_t dtype;         /* gbdx_dtype of y, args and params */
+  int32_t kernel;        /* gbdx_kernel */
+  int32_t adjoint;       /* gbdx_adjoint */
+  int32_t checkpoints;   /* RecursiveCheckpointAdjoint(checkpoints=...) slots */
+  int32_t block_threads; /* 0 = autotuned */
+  int32_t ctas_per_sm;   /* 0 = autotuned */
+} gbdx_problem_desc;
+
+typedef struct gbdx_problem gbdx_problem;
+
+/* Validates the descriptor and builds a handle.  Errors mirror the reference's
+ * ValueErrors (adaptive Euler, Euler with an SDE and an adaptive controller,
+ * ConstantStepSize without dt0 is checked at solve time, and so on). */
+int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out);
+int gbdx_problem_destroy(gbdx_problem *problem);
+
+/* Number of saved points per trajectory: save_t0 + n_ts + save_t1. */
+int gbdx_num_saves(const gbdx_problem *problem);
+
+/* Device workspace (bytes) a forward solve over `batch` trajectories needs. */
+size_t gbdx_workspace_size(const gbdx_problem *problem, int64_t batch);
+
+/*
+ * Forward solve of `batch` independent trajectories.
+ *   t0, t1, dt0 : device f64 [batch] (time_stride 1) or [1] (time_stride 0);
+ *                 dt0 may be NULL, meaning dt0=None.
+ *   y0          : device [batch, dim] in desc.dtype.
+ *   args        : device [batch, n_args] (args_stride n_args) or [n_args]
+ *                 (args_stride 0) in desc.dtype; NULL when n_args == 0.
+ *   params      : device MLP / linear / diffusion parameters in desc.dtype
+ *                 (layout in gbdx_param_count); NULL for analytic fields.
+ *   save_ts     : device f64 [n_ts], increasing, inside [t0, t1].
+ *   ys_out      : device [batch, n_saves, dim] in desc.dtype (unsaved = +inf).
+ *   ts_out      : device f64 [batch, n_saves].
+ *   result_out  : device int32 [batch] gbdx_result codes.
+ *   stats_out   : device int32 [batch, 3] (num_steps, accepted, rejected).
+ *   workspace   : device scratch of gbdx_workspace_size bytes.
+ *   stream      : cudaStream_t (NULL = legacy default stream).
+ */
+int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
+                   const double *t1, const double *dt0, int64_t time_stride,
+                   const void *y0, const void *args, int64_t args_stride,
+                   const void *params, const double *save_ts, void *ys_out,
+                   double *ts_out, int32_t *result_out, int32_t *stats_out,
+                   void *workspace, size_t workspace_bytes, void *stream);
+
+/* Number of parameters of the MLP / linear field plus diffusion, in the flat
+ * layout [W_0 (out x in, row-major), b_0, W_1, b_1, ..., W_sigma, b_sigma]. */
+int64_t gbdx_param_count(const gbdx_problem *problem);
+
+/* sizeof(gbdx_problem_desc), for bindings to check their struct layout. */
+size_t gbdx_problem_desc_size(void);
+
+/* Library version and the message of the last error on this thread. */
+int gbdx_version(void);
+const char *gbdx_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBDX_H_ */

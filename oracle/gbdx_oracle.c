@@ -1,0 +1,1100 @@
+/*
+ * gbdx_oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * An FP64 CPU restatement of Diffrax's batched `diffeqsolve` hot path, used as
+ * the parity oracle for the CUDA kernels and as the timed CPU baseline.  It is
+ * never linked into, loaded by, or called from the product library; only the
+ * tests, the smoke check and the CPU-baseline leg of the benchmark load it.
+ *
+ * Each block below names the reference file:line it restates (paths are
+ * relative to the Diffrax source tree, v0.7.2).
+ *
+ *   solve loop ............ diffrax/_integrate.py:302-885, 1036-1305
+ *   explicit RK step ...... diffrax/_solver/runge_kutta.py:446-1203
+ *   tableaus .............. diffrax/_solver/{tsit5,dopri5,heun,euler}.py
+ *   interpolants .......... diffrax/_solver/tsit5.py:103-156,
+ *                           diffrax/_local_interpolation.py:29-139
+ *   PID controller ........ diffrax/_step_size_controller/pid.py:316-567
+ *   constant step size .... diffrax/_step_size_controller/constant.py:20-104
+ *   terms ................. diffrax/_term.py:174-226, 271-555, 666-764
+ *   virtual Brownian tree . diffrax/_brownian/tree.py:245-354, 366-448,
+ *                           607-621, 626-773 (BrownianIncrement branch)
+ *   gradients ............. diffrax/_adjoint.py:179-312 (discretise-then-
+ *                           optimise: exact VJP of the accepted-step map with
+ *                           the controller under stop_gradient, pid.py:374,
+ *                           499-501, 529-530), diffrax/_adjoint.py:538-734 and
+ *                           diffrax/_term.py:767-910 (backsolve).
+ *
+ * Built with -ffp-contract=off so that x86-64 and aarch64 give identical bits.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+enum { ORC_EULER = 0, ORC_HEUN = 1, ORC_DOPRI5 = 2, ORC_TSIT5 = 3 };
+enum { ORC_CONSTANT = 0, ORC_PID = 1 };
+enum {
+  ORC_LOTKA_VOLTERRA = 0,
+  ORC_VAN_DER_POL = 1,
+  ORC_ORNSTEIN_UHLENBECK = 2,
+  ORC_MLP = 3,
+  ORC_LINEAR = 4,   /* y' = A y, A a dim x dim matrix passed as params */
+  ORC_CALLBACK = 5  /* arbitrary host callback, forward only */
+};
+enum { ORC_DIFF_NONE = 0, ORC_DIFF_OU = 1, ORC_DIFF_TANH_DIAG = 2 };
+enum { ORC_NORM_RMS = 0, ORC_NORM_ADJOINT_SEMI = 1 };
+
+/* RESULTS codes (diffrax/_solution.py:13-31): successful must be 0. */
+enum {
+  ORC_SUCCESSFUL = 0,
+  ORC_MAX_STEPS_REACHED = 1,
+  ORC_DT_MIN_REACHED = 2,
+  ORC_EVENT_OCCURRED = 3,
+  ORC_MAX_STEPS_REJECTED = 4,
+  ORC_INTERNAL_ERROR = 5
+};
+
+typedef void (*orc_vf_cb)(double t, const double *y, double *out, int dim,
+                          void *ctx);
+
+/* Mirrors the problem descriptor of the product ABI (include/gbdx.h). */
+typedef struct {
+  int32_t solver, controller, field, dim;
+  double rtol, atol, pcoeff, icoeff, dcoeff, safety, factormin, factormax;
+  double dtmin, dtmax; /* NaN = None */
+  int32_t force_dtmin;
+  double error_order; /* 0 = solver default */
+  int32_t n_ts, save_t0, save_t1, max_steps;
+  int32_t n_args;
+  int32_t mlp_depth;      /* number of linear layers */
+  int32_t mlp_widths[9];  /* widths[0] = in, widths[depth] = out */
+  int32_t diffusion;      /* ORC_DIFF_* */
+  double vbt_t0, vbt_t1, vbt_tol;
+  uint64_t seed;
+  int32_t norm;           /* used by the backsolve adjoint only */
+  int32_t pad_;
+} orc_desc;
+
+/* ------------------------------------------------------------------------ */
+/* Butcher tableaus.  Coefficients are the published method constants as the */
+/* reference writes them (tsit5.py:18-100, dopri5.py:11-33, heun.py:12-17); */
+/* the error rows are evaluated as the same FP64 differences.                */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int s;          /* stages */
+  int fsal, ssal; /* runge_kutta.py:143-165 */
+  double a[7][7]; /* a[i][j], j < i */
+  double b[7], e[7], c[7];
+  int order;      /* ODE order; error_order for ODEs (base.py:97-120) */
+  double strong_order;
+} Tableau;
+
+static Tableau TSIT5, DOPRI5, HEUN, EULER;
+
+static void init_tableaus(void) {
+  static int done = 0;
+  if (done) return;
+  memset(&TSIT5, 0, sizeof TSIT5);
+  TSIT5.s = 7; TSIT5.fsal = 1; TSIT5.ssal = 1; TSIT5.order = 5;
+  TSIT5.strong_order = 0.0;
+  TSIT5.c[1] = 161.0 / 1000; TSIT5.c[2] = 327.0 / 1000; TSIT5.c[3] = 9.0 / 10;
+  TSIT5.c[4] = 0.9800255409045096857298102862870245954942137979563024768854764293221195950761080302604;
+  TSIT5.c[5] = 1.0; TSIT5.c[6] = 1.0;
+  TSIT5.a[1][0] = 161.0 / 1000;
+  TSIT5.a[2][0] = -0.8480655492356988544426874250230774675121177393430391537369234245294192976164141156943e-2;
+  TSIT5.a[2][1] = 0.3354806554923569885444268742502307746751211773934303915373692342452941929761641411569;
+  TSIT5.a[3][0] = 2.897153057105493432130432594192938764924887287701866490314866693455023795137503079289;
+  TSIT5.a[3][1] = -6.359448489975074843148159912383825625952700647415626703305928850207288721235210244366;
+  TSIT5.a[3][2] = 4.362295432869581411017727318190886861027813359713760212991062156752264926097707165077;
+  TSIT5.a[4][0] = 5.325864828439256604428877920840511317836476253097040101202360397727981648835607691791;
+  TSIT5.a[4][1] = -11.74888356406282787774717033978577296188744178259862899288666928009020615663593781589;
+  TSIT5.a[4][2] = 7.495539342889836208304604784564358155658679161518186721010132816213648793440552049753;
+  TSIT5.a[4][3] = -0.9249506636175524925650207933207191611349983406029535244034750452930469056411389539635e-1;
+  TSIT5.a[5][0] = 5.861455442946420028659251486982647890394337666164814434818157239052507339770711679748;
+  TSIT5.a[5][1] = -12.92096931784710929170611868178335939541780751955743459166312250439928519268343184452;
+  TSIT5.a[5][2] = 8.159367898576158643180400794539253485181918321135053305748355423955009222648673734986;
+  TSIT5.a[5][3] = -0.7158497328140099722453054252582973869127213147363544882721139659546372402303777878835e-1;
+  TSIT5.a[5][4] = -0.2826905039406838290900305721271224146717633626879770007617876201276764571291579142206e-1;
+  {
+    const double bs[6] = {
+        0.9646076681806522951816731316512876333711995238157997181903319145764851595234062815396e-1,
+        1.0 / 100,
+        0.4798896504144995747752495322905965199130404621990332488332634944254542060153074523509,
+        1.379008574103741893192274821856872770756462643091360525934940067397245698027561293331,
+        -3.290069515436080679901047585711363850115683290894936158531296799594813811049925401677,
+        2.324710524099773982415355918398765796109060233222962411944060046314465391054716027841};
+    for (int j = 0; j < 6; j++) { TSIT5.a[6][j] = bs[j]; TSIT5.b[j] = bs[j]; }
+    TSIT5.b[6] = 0.0;
+    TSIT5.e[0] = bs[0] - 0.9468075576583945807478876255758922856117527357724631226139574065785592789071067303271e-1;
+    TSIT5.e[1] = bs[1] - 0.9183565540343253096776363936645313759813746240984095238905939532922955247253608687270e-2;
+    TSIT5.e[2] = bs[2] - 0.4877705284247615707855642599631228241516691959761363774365216240304071651579571959813;
+    TSIT5.e[3] = bs[3] - 1.234297566930478985655109673884237654035539930748192848315425833500484878378061439761;
+    TSIT5.e[4] = bs[4] + 2.707712349983525454881109975059321670689605166938197378763992255714444407154902012702;
+    TSIT5.e[5] = bs[5] - 1.866628418170587035753719399566211498666255505244122593996591602841258328965767580089;
+    TSIT5.e[6] = -1.0 / 66;
+  }
+
+  memset(&DOPRI5, 0, sizeof DOPRI5);
+  DOPRI5.s = 7; DOPRI5.fsal = 1; DOPRI5.ssal = 1; DOPRI5.order = 5;
+  DOPRI5.c[1] = 1.0 / 5; DOPRI5.c[2] = 3.0 / 10; DOPRI5.c[3] = 4.0 / 5;
+  DOPRI5.c[4] = 8.0 / 9; DOPRI5.c[5] = 1.0; DOPRI5.c[6] = 1.0;
+  DOPRI5.a[1][0] = 1.0 / 5;
+  DOPRI5.a[2][0] = 3.0 / 40; DOPRI5.a[2][1] = 9.0 / 40;
+  DOPRI5.a[3][0] = 44.0 / 45; DOPRI5.a[3][1] = -56.0 / 15; DOPRI5.a[3][2] = 32.0 / 9;
+  DOPRI5.a[4][0] = 19372.0 / 6561; DOPRI5.a[4][1] = -25360.0 / 2187;
+  DOPRI5.a[4][2] = 64448.0 / 6561; DOPRI5.a[4][3] = -212.0 / 729;
+  DOPRI5.a[5][0] = 9017.0 / 3168; DOPRI5.a[5][1] = -355.0 / 33;
+  DOPRI5.a[5][2] = 46732.0 / 5247; DOPRI5.a[5][3] = 49.0 / 176;
+  DOPRI5.a[5][4] = -5103.0 / 18656;
+  DOPRI5.a[6][0] = 35.0 / 384; DOPRI5.a[6][1] = 0.0; DOPRI5.a[6][2] = 500.0 / 1113;
+  DOPRI5.a[6][3] = 125.0 / 192; DOPRI5.a[6][4] = -2187.0 / 6784; DOPRI5.a[6][5] = 11.0 / 84;
+  for (int j = 0; j < 6; j++) DOPRI5.b[j] = DOPRI5.a[6][j];
+  DOPRI5.b[6] = 0.0;
+  DOPRI5.e[0] = 35.0 / 384 - 1951.0 / 21600;
+  DOPRI5.e[1] = 0.0;
+  DOPRI5.e[2] = 500.0 / 1113 - 22642.0 / 50085;
+  DOPRI5.e[3] = 125.0 / 192 - 451.0 / 720;
+  DOPRI5.e[4] = -2187.0 / 6784 - -12231.0 / 42400;
+  DOPRI5.e[5] = 11.0 / 84 - 649.0 / 6300;
+  DOPRI5.e[6] = -1.0 / 60.0;
+
+  memset(&HEUN, 0, sizeof HEUN);
+  HEUN.s = 2; HEUN.fsal = 0; HEUN.ssal = 0; HEUN.order = 2; HEUN.strong_order = 0.5;
+  HEUN.c[1] = 1.0; HEUN.a[1][0] = 1.0;
+  HEUN.b[0] = 0.5; HEUN.b[1] = 0.5; HEUN.e[0] = 0.5; HEUN.e[1] = -0.5;
+
+  memset(&EULER, 0, sizeof EULER);
+  EULER.s = 1; EULER.order = 1; EULER.strong_order = 0.5; EULER.b[0] = 1.0;
+  done = 1;
+}
+
+static const Tableau *tableau_of(int solver) {
+  switch (solver) {
+    case ORC_EULER: return &EULER;
+    case ORC_HEUN: return &HEUN;
+    case ORC_DOPRI5: return &DOPRI5;
+    default: return &TSIT5;
+  }
+}
+
+/* Dopri5 dense-output midpoint weights (dopri5.py:36-47). */
+static const double DOPRI5_CMID[7] = {
+    6025192743.0 / 30085553152.0 / 2, 0.0, 51252292925.0 / 65400821598.0 / 2,
+    -2691868925.0 / 45128329728.0 / 2, 187940372067.0 / 1594534317056.0 / 2,
+    -1776094331.0 / 19743644256.0 / 2, 11237099.0 / 235043384.0 / 2};
+
+/* ------------------------------------------------------------------------ */
+/* Counter-based normal generator (Philox4x32-10, Salmon et al. 2011) and the */
+/* virtual Brownian tree that consumes it.  The kernels use the same integer  */
+/* stream; only the uniform -> normal transform differs in precision.        */
+/* ------------------------------------------------------------------------ */
+static void philox4x32_10(uint32_t ctr[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; r++) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * ctr[0];
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * ctr[2];
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ ctr[1] ^ k0, n2 = hi0 ^ ctr[3] ^ k1;
+    ctr[0] = n0; ctr[1] = lo1; ctr[2] = n2; ctr[3] = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+}
+
+enum { VBT_ROOT = 0, VBT_MID = 1, VBT_LEAF = 2 };
+
+/* Four standard normals for (trajectory, tree node, draw kind, dims 4q..4q+3). */
+static void normal4(uint64_t seed, uint32_t traj, uint32_t node, uint32_t kind,
+                    uint32_t q, double z[4]) {
+  uint32_t c[4] = {traj, node, (kind << 24) | q, 0x5EEDu};
+  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  double u[4];
+  for (int i = 0; i < 4; i++) u[i] = ((double)(c[i] >> 8) + 0.5) * (1.0 / 16777216.0);
+  const double two_pi = 6.283185307179586476925286766559;
+  double r0 = sqrt(-2.0 * log(u[0])), r1 = sqrt(-2.0 * log(u[2]));
+  z[0] = r0 * cos(two_pi * u[1]); z[1] = r0 * sin(two_pi * u[1]);
+  z[2] = r1 * cos(two_pi * u[3]); z[3] = r1 * sin(two_pi * u[3]);
+}
+
+static void normals(uint64_t seed, uint32_t traj, uint32_t node, uint32_t kind,
+                    int dim, double *out) {
+  for (int q = 0; q * 4 < dim; q++) {
+    double z[4];
+    normal4(seed, traj, node, kind, (uint32_t)q, z);
+    for (int i = 0; i < 4 && q * 4 + i < dim; i++) out[q * 4 + i] = z[i];
+  }
+}
+
+/* W(r) on the unit interval by binary bridge descent: tree.py:366-448 (loop),
+ * 626-773 (BrownianIncrement arch, lines 752-768), 607-621 (final bridge). */
+static void vbt_eval_unit(uint64_t seed, uint32_t traj, double tol_unit, double r,
+                          int dim, double *w_r) {
+  double ws[64], wu[64], wsu[64], z[64];
+  int level = 0;
+  double s = 0.0;
+  uint32_t node = 1;
+  normals(seed, traj, 0, VBT_ROOT, dim, z);
+  for (int i = 0; i < dim; i++) { ws[i] = 0.0; wu[i] = z[i]; wsu[i] = z[i]; }
+  while (ldexp(1.0, -level) > tol_unit) {
+    double su = ldexp(1.0, -level);
+    double st = su / 2;
+    double t = s + st;
+    double root_su = sqrt(su);
+    normals(seed, traj, node, VBT_MID, dim, z);
+    int right = r > t;
+    for (int i = 0; i < dim; i++) {
+      double mean = 0.5 * wsu[i];
+      double term2 = (root_su / 2) * z[i];
+      double w_st = mean + term2, w_tu = mean - term2;
+      double w_t = ws[i] + w_st;
+      if (right) { ws[i] = w_t; wsu[i] = w_tu; }
+      else { wu[i] = w_t; wsu[i] = w_st; }
+    }
+    if (right) s = t;
+    node = 2 * node + (uint32_t)right;
+    level++;
+  }
+  double su = ldexp(1.0, -level);
+  double sr = r - s; if (sr < 0) sr = 0;
+  double ru = su - sr; if (ru < 0) ru = 0;
+  normals(seed, traj, node, VBT_LEAF, dim, z);
+  double bbs = sqrt(sr * ru / su);
+  for (int i = 0; i < dim; i++) w_r[i] = (ws[i] + sr / su * wsu[i]) + bbs * z[i];
+  (void)wu;
+}
+
+/* VirtualBrownianTree.evaluate(ta, tb) (tree.py:325-354): rescale to [0,1],
+ * difference of two evaluations, multiply by sqrt(T). */
+static void vbt_increment(const orc_desc *d, uint32_t traj, double ta, double tb,
+                          double *dw) {
+  double T = d->vbt_t1 - d->vbt_t0;
+  double tol_unit = d->vbt_tol / T;
+  double ra = (ta - d->vbt_t0) / T, rb = (tb - d->vbt_t0) / T;
+  double wa[64], wb[64];
+  vbt_eval_unit(d->seed, traj, tol_unit, ra, d->dim, wa);
+  vbt_eval_unit(d->seed, traj, tol_unit, rb, d->dim, wb);
+  double sq = sqrt(T);
+  for (int i = 0; i < d->dim; i++) dw[i] = sq * (wb[i] - wa[i]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Vector fields.                                                            */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  const orc_desc *d;
+  const double *args;   /* this trajectory's analytic args */
+  const double *params; /* MLP / linear / diffusion parameters (flat) */
+  orc_vf_cb cb;
+  void *cb_ctx;
+} Field;
+
+/* Flat MLP layout: for each layer l, W_l [out x in] row-major then b_l [out];
+ * then (diffusion ORC_DIFF_TANH_DIAG) W_sigma [dim x dim], b_sigma [dim]. */
+static int64_t mlp_param_count(const orc_desc *d) {
+  int64_t n = 0;
+  for (int l = 0; l < d->mlp_depth; l++)
+    n += (int64_t)d->mlp_widths[l] * d->mlp_widths[l + 1] + d->mlp_widths[l + 1];
+  return n;
+}
+
+#define MAXW 512
+
+/* eqx.nn.MLP semantics: tanh on hidden layers, identity output.  When acts is
+ * non-NULL the hidden activations are stored for the VJP. */
+static void mlp_forward(const orc_desc *d, const double *P, const double *x,
+                        double *out, double *acts) {
+  double buf0[MAXW], buf1[MAXW];
+  const double *in = x;
+  double *cur = buf0;
+  const double *p = P;
+  int aoff = 0;
+  for (int l = 0; l < d->mlp_depth; l++) {
+    int ni = d->mlp_widths[l], no = d->mlp_widths[l + 1];
+    const double *W = p, *b = p + (int64_t)ni * no;
+    double *dst = (l == d->mlp_depth - 1) ? out : cur;
+    for (int o = 0; o < no; o++) {
+      double acc = 0.0;
+      for (int i = 0; i < ni; i++) acc += W[(int64_t)o * ni + i] * in[i];
+      acc += b[o];
+      dst[o] = (l == d->mlp_depth - 1) ? acc : tanh(acc);
+    }
+    if (l < d->mlp_depth - 1) {
+      if (acts) { memcpy(acts + aoff, dst, sizeof(double) * no); aoff += no; }
+      in = dst;
+      cur = (cur == buf0) ? buf1 : buf0;
+    }
+    p += (int64_t)ni * no + no;
+  }
+}
+
+/* VJP of the MLP: gx += J^T g; gP += dOut/dP^T g (if gP). */
+static void mlp_vjp(const orc_desc *d, const double *P, const double *x,
+                    const double *g, double *gx, double *gP) {
+  double acts[MAXW * 8];
+  double out[MAXW];
+  mlp_forward(d, P, x, out, acts);
+  /* offsets of each layer's params and activations */
+  int64_t poff[9];
+  int aoff[9];
+  poff[0] = 0; aoff[0] = 0;
+  for (int l = 0; l < d->mlp_depth; l++) {
+    int ni = d->mlp_widths[l], no = d->mlp_widths[l + 1];
+    poff[l + 1] = poff[l] + (int64_t)ni * no + no;
+    aoff[l + 1] = aoff[l] + ((l < d->mlp_depth - 1) ? no : 0);
+  }
+  double gcur[MAXW], gprev[MAXW];
+  int no_last = d->mlp_widths[d->mlp_depth];
+  memcpy(gcur, g, sizeof(double) * no_last);
+  for (int l = d->mlp_depth - 1; l >= 0; l--) {
+    int ni = d->mlp_widths[l], no = d->mlp_widths[l + 1];
+    const double *W = P + poff[l];
+    const double *xin = (l == 0) ? x : acts + aoff[l - 1];
+    /* gcur is dL/d(pre-activation) of layer l. */
+    if (gP) {
+      double *gW = gP + poff[l], *gb = gW + (int64_t)ni * no;
+      for (int o = 0; o < no; o++) {
+        for (int i = 0; i < ni; i++) gW[(int64_t)o * ni + i] += gcur[o] * xin[i];
+        gb[o] += gcur[o];
+      }
+    }
+    for (int i = 0; i < ni; i++) {
+      double acc = 0.0;
+      for (int o = 0; o < no; o++) acc += W[(int64_t)o * ni + i] * gcur[o];
+      gprev[i] = acc;
+    }
+    if (l > 0) {
+      const double *h = acts + aoff[l - 1];
+      for (int i = 0; i < ni; i++) gcur[i] = gprev[i] * (1.0 - h[i] * h[i]);
+    } else {
+      for (int i = 0; i < ni; i++) gx[i] += gprev[i];
+    }
+  }
+}
+
+static void field_drift(const Field *F, double t, const double *y, double *out) {
+  const orc_desc *d = F->d;
+  const double *a = F->args;
+  switch (d->field) {
+    case ORC_LOTKA_VOLTERRA: /* x' = a x - b x y, y' = -c y + d x y */
+      out[0] = a[0] * y[0] - a[1] * y[0] * y[1];
+      out[1] = -a[2] * y[1] + a[3] * y[0] * y[1];
+      break;
+    case ORC_VAN_DER_POL: /* x' = y, y' = mu (1 - x^2) y - x */
+      out[0] = y[1];
+      out[1] = a[0] * (1.0 - y[0] * y[0]) * y[1] - y[0];
+      break;
+    case ORC_ORNSTEIN_UHLENBECK: /* drift theta (mu - y), args (theta, mu, sigma) */
+      for (int i = 0; i < d->dim; i++) out[i] = a[0] * (a[1] - y[i]);
+      break;
+    case ORC_MLP:
+      mlp_forward(d, F->params, y, out, NULL);
+      break;
+    case ORC_LINEAR:
+      for (int i = 0; i < d->dim; i++) {
+        double acc = 0.0;
+        for (int j = 0; j < d->dim; j++) acc += F->params[i * d->dim + j] * y[j];
+        out[i] = acc;
+      }
+      break;
+    case ORC_CALLBACK:
+      F->cb(t, y, out, d->dim, F->cb_ctx);
+      break;
+  }
+}
+
+static int64_t diffusion_param_offset(const orc_desc *d) {
+  return d->field == ORC_MLP ? mlp_param_count(d) : 0;
+}
+
+/* Diagonal diffusion sigma(y) (ControlTerm with a diagonal operator,
+ * _term.py:417-427).  OU: sigma constant (args[2]).  TANH_DIAG:
+ * sigma = 0.1 tanh(W y + b). */
+static void field_diffusion(const Field *F, const double *y, double *sig) {
+  const orc_desc *d = F->d;
+  if (d->diffusion == ORC_DIFF_OU) {
+    for (int i = 0; i < d->dim; i++) sig[i] = F->args[2];
+  } else if (d->diffusion == ORC_DIFF_TANH_DIAG) {
+    const double *W = F->params + diffusion_param_offset(d);
+    const double *b = W + d->dim * d->dim;
+    for (int i = 0; i < d->dim; i++) {
+      double acc = 0.0;
+      for (int j = 0; j < d->dim; j++) acc += W[i * d->dim + j] * y[j];
+      sig[i] = 0.1 * tanh(acc + b[i]);
+    }
+  } else {
+    for (int i = 0; i < d->dim; i++) sig[i] = 0.0;
+  }
+}
+
+/* VJP of the drift: gy += J^T g; gargs += (dF/dargs)^T g; gP += (dF/dP)^T g. */
+static void field_drift_vjp(const Field *F, const double *y, const double *g,
+                            double *gy, double *gargs, double *gP) {
+  const orc_desc *d = F->d;
+  const double *a = F->args;
+  switch (d->field) {
+    case ORC_LOTKA_VOLTERRA:
+      gy[0] += g[0] * (a[0] - a[1] * y[1]) + g[1] * (a[3] * y[1]);
+      gy[1] += g[0] * (-a[1] * y[0]) + g[1] * (-a[2] + a[3] * y[0]);
+      if (gargs) {
+        gargs[0] += g[0] * y[0];
+        gargs[1] += -g[0] * y[0] * y[1];
+        gargs[2] += -g[1] * y[1];
+        gargs[3] += g[1] * y[0] * y[1];
+      }
+      break;
+    case ORC_VAN_DER_POL:
+      gy[0] += g[1] * (-2.0 * a[0] * y[0] * y[1] - 1.0);
+      gy[1] += g[0] + g[1] * a[0] * (1.0 - y[0] * y[0]);
+      if (gargs) gargs[0] += g[1] * (1.0 - y[0] * y[0]) * y[1];
+      break;
+    case ORC_ORNSTEIN_UHLENBECK:
+      for (int i = 0; i < d->dim; i++) {
+        gy[i] += -a[0] * g[i];
+        if (gargs) { gargs[0] += g[i] * (a[1] - y[i]); gargs[1] += g[i] * a[0]; }
+      }
+      break;
+    case ORC_MLP:
+      mlp_vjp(d, F->params, y, g, gy, gP);
+      break;
+    case ORC_LINEAR:
+      for (int i = 0; i < d->dim; i++)
+        for (int j = 0; j < d->dim; j++) {
+          gy[j] += F->params[i * d->dim + j] * g[i];
+          if (gP) gP[i * d->dim + j] += g[i] * y[j];
+        }
+      break;
+    default:
+      break;
+  }
+}
+
+/* VJP of y -> sigma(y) * dw (elementwise). */
+static void field_diffusion_vjp(const Field *F, const double *y, const double *dw,
+                                const double *g, double *gy, double *gargs,
+                                double *gP) {
+  const orc_desc *d = F->d;
+  if (d->diffusion == ORC_DIFF_OU) {
+    if (gargs) for (int i = 0; i < d->dim; i++) gargs[2] += g[i] * dw[i];
+  } else if (d->diffusion == ORC_DIFF_TANH_DIAG) {
+    int64_t off = diffusion_param_offset(d);
+    const double *W = F->params + off;
+    const double *b = W + d->dim * d->dim;
+    for (int i = 0; i < d->dim; i++) {
+      double acc = 0.0;
+      for (int j = 0; j < d->dim; j++) acc += W[i * d->dim + j] * y[j];
+      double th = tanh(acc + b[i]);
+      double gz = g[i] * dw[i] * 0.1 * (1.0 - th * th);
+      for (int j = 0; j < d->dim; j++) {
+        gy[j] += W[i * d->dim + j] * gz;
+        if (gP) gP[off + i * d->dim + j] += gz * y[j];
+      }
+      if (gP) gP[off + d->dim * d->dim + i] += gz;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* One explicit RK step (runge_kutta.py:446-1203, explicit branch).          */
+/*                                                                           */
+/* k_i = vf(t_i, y_i) * control (+ sigma(y_i) * dW for the SDE MultiTerm,     */
+/* _term.py:711-722).  Time is in the direction-normalised coordinate; the    */
+/* WrapTerm (_term.py:734-764) evaluates the field at dir * t and multiplies  */
+/* the control by dir.                                                       */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int dim;
+  double k[7][64];
+  double ystage[7][64];
+  double y0[64], y1[64], err[64];
+  double fsal_f[64];
+  double dw[64];
+  double tprev, tnext;
+} StepOut;
+
+static void rk_step(const Field *F, const Tableau *tab, int dir, double tprev,
+                    double tnext, const double *y0, int have_f0, const double *f0,
+                    const double *dw, StepOut *so) {
+  const orc_desc *d = F->d;
+  const int D = d->dim;
+  const double dt = tnext - tprev;
+  const double control = dir * dt;
+  double f[64], sig[64];
+  so->dim = D;
+  so->tprev = tprev; so->tnext = tnext;
+  memcpy(so->y0, y0, sizeof(double) * D);
+  if (dw) memcpy(so->dw, dw, sizeof(double) * D);
+  for (int i = 0; i < tab->s; i++) {
+    double *yi = so->ystage[i];
+    if (i == 0) {
+      memcpy(yi, y0, sizeof(double) * D);
+    } else {
+      for (int n = 0; n < D; n++) {
+        double inc = 0.0;
+        for (int j = 0; j < i; j++) inc += tab->a[i][j] * so->k[j][n];
+        yi[n] = y0[n] + inc;
+      }
+    }
+    /* runge_kutta.py:1023: t_i = t1 if c_i == 1 else t0 + c_i dt */
+    double ti = (tab->c[i] == 1.0) ? tnext : tprev + tab->c[i] * dt;
+    if (i == 0 && have_f0 && tab->fsal) {
+      memcpy(f, f0, sizeof(double) * D);
+    } else {
+      field_drift(F, dir * ti, yi, f);
+    }
+    if (tab->fsal && i == tab->s - 1) memcpy(so->fsal_f, f, sizeof(double) * D);
+    if (d->diffusion != ORC_DIFF_NONE) {
+      field_diffusion(F, yi, sig);
+      for (int n = 0; n < D; n++) so->k[i][n] = f[n] * control + sig[n] * dw[n];
+    } else {
+      for (int n = 0; n < D; n++) so->k[i][n] = f[n] * control;
+    }
+  }
+  if (tab->ssal) {
+    memcpy(so->y1, so->ystage[tab->s - 1], sizeof(double) * D);
+  } else {
+    for (int n = 0; n < D; n++) {
+      double inc = 0.0;
+      for (int j = 0; j < tab->s; j++) inc += tab->b[j] * so->k[j][n];
+      so->y1[n] = y0[n] + inc;
+    }
+  }
+  for (int n = 0; n < D; n++) {
+    double e = 0.0;
+    for (int j = 0; j < tab->s; j++) e += tab->e[j] * so->k[j][n];
+    so->err[n] = e;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Dense interpolation inside the step just taken.                           */
+/* ------------------------------------------------------------------------ */
+/* linear_rescale (_misc.py:71-82) */
+static double linear_rescale(double t0, double t, double t1) {
+  if (t0 == t1) return 0.0;
+  return (t - t0) / (t1 - t0);
+}
+
+/* Tsit5 interpolation weights b_i(theta) (tsit5.py:119-150). */
+static void tsit5_weights(double t, double w[7]) {
+  w[0] = -1.0530884977290216 * t * (t - 1.3299890189751412) *
+         (t * t - 1.4364028541716351 * t + 0.7139816917074209);
+  w[1] = 0.1017 * t * t * (t * t - 2.1966568338249754 * t + 1.2949852507374631);
+  w[2] = 2.490627285651252793 * t * t * (t * t - 2.38535645472061657 * t + 1.57803468208092486);
+  w[3] = -16.54810288924490272 * (t - 1.21712927295533244) * (t - 0.61620406037800089) * t * t;
+  w[4] = 47.37952196281928122 * (t - 1.203071208372362603) * (t - 0.658047292653547382) * t * t;
+  w[5] = -34.87065786149660974 * (t - 1.2) * (t - 0.666666666666666667) * t * t;
+  w[6] = 2.5 * (t - 1) * (t - 0.6) * t * t;
+}
+
+/* Coefficients of the interpolant as a linear map of (y0, y1, k_j):
+ * out = ay0 * y0 + ay1 * y1 + sum_j g[j] k_j.  Used by the VJP. */
+static void interp_linear_coeffs(int solver, int s, double th, double *ay0,
+                                 double *ay1, double g[7]) {
+  for (int j = 0; j < 7; j++) g[j] = 0.0;
+  double t2 = th * th, t3 = t2 * th, t4 = t3 * th;
+  switch (solver) {
+    case ORC_TSIT5:
+      *ay0 = 1.0; *ay1 = 0.0; tsit5_weights(th, g);
+      break;
+    case ORC_DOPRI5: {
+      /* _local_interpolation.py:109-127 expanded in the monomials. */
+      double M = 16 * t4 - 32 * t3 + 16 * t2;
+      *ay0 = -8 * t4 + 18 * t3 - 11 * t2 + 1 + M;
+      *ay1 = -8 * t4 + 14 * t3 - 5 * t2;
+      for (int j = 0; j < 7; j++) g[j] = M * DOPRI5_CMID[j];
+      g[0] += -2 * t4 + 5 * t3 - 4 * t2 + th;
+      g[6] += 2 * t4 - 3 * t3 + t2;
+      break;
+    }
+    case ORC_HEUN: /* _local_interpolation.py:61-66 */
+      *ay0 = 2 * t3 - 3 * t2 + 1;
+      *ay1 = -2 * t3 + 3 * t2;
+      g[0] = t3 - 2 * t2 + th;
+      g[s - 1] = t3 - t2;
+      break;
+    default: /* Euler: LocalLinearInterpolation */
+      *ay0 = 1.0 - th; *ay1 = th;
+      break;
+  }
+}
+
+/* Forward evaluation, following the reference's evaluation order. */
+static void interp_eval(int solver, const StepOut *so, int s, double t, double *out) {
+  const int D = so->dim;
+  double th = linear_rescale(so->tprev, t, so->tnext);
+  switch (solver) {
+    case ORC_TSIT5: {
+      double w[7];
+      tsit5_weights(th, w);
+      for (int n = 0; n < D; n++) {
+        double acc = 0.0;
+        for (int j = 0; j < 7; j++) acc += w[j] * so->k[j][n];
+        out[n] = so->y0[n] + acc;
+      }
+      break;
+    }
+    case ORC_DOPRI5:
+      for (int n = 0; n < D; n++) {
+        double cm = 0.0;
+        for (int j = 0; j < 7; j++) cm += DOPRI5_CMID[j] * so->k[j][n];
+        double y0 = so->y0[n], y1 = so->y1[n], ymid = y0 + cm;
+        double f0 = so->k[0][n], f1 = so->k[6][n];
+        double a = 2 * (f1 - f0) - 8 * (y1 + y0) + 16 * ymid;
+        double b = 5 * f0 - 3 * f1 + 18 * y0 + 14 * y1 - 32 * ymid;
+        double c = f1 - 4 * f0 - 11 * y0 - 5 * y1 + 16 * ymid;
+        out[n] = (((a * th + b) * th + c) * th + f0) * th + y0;
+      }
+      break;
+    case ORC_HEUN:
+      for (int n = 0; n < D; n++) {
+        double y0 = so->y0[n], y1 = so->y1[n], k0 = so->k[0][n], k1 = so->k[s - 1][n];
+        double a = k0 + k1 + 2 * y0 - 2 * y1;
+        double b = -2 * k0 - k1 - 3 * y0 + 3 * y1;
+        out[n] = ((a * th + b) * th + k0) * th + y0;
+      }
+      break;
+    default:
+      for (int n = 0; n < D; n++) out[n] = so->y0[n] + th * (so->y1[n] - so->y0[n]);
+      break;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Step-size controllers.                                                    */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  /* PID (pid.py:388-392) */
+  double prev_inv, prev_prev_inv;
+  int at_dtmin;
+  /* Constant (constant.py:41-57) */
+  int steps_completed, num_steps;
+  double t0_sim, t1_sim;
+} CtrlState;
+
+static double prevbefore(double x) { return nextafter(x, -INFINITY); }
+
+/* optx.rms_norm: two_norm / sqrt(size). */
+static double rms_norm(const double *x, int n) {
+  double acc = 0.0;
+  for (int i = 0; i < n; i++) acc += x[i] * x[i];
+  return sqrt(acc) / sqrt((double)n);
+}
+
+/* PIDController.adapt_step_size (pid.py:394-567).  `scaled` is precomputed by
+ * the caller because the backsolve adjoint uses a different norm. */
+static int pid_adapt(const orc_desc *d, double error_order, double t0, double t1,
+                     double scaled, CtrlState *cs, double *next_t0, double *next_t1,
+                     int *result) {
+  int has_dtmin = !isnan(d->dtmin), has_dtmax = !isnan(d->dtmax);
+  int keep = scaled < 1.0;
+  if (has_dtmin) keep = keep | cs->at_dtmin;
+  double prev_dt = t1 - t0;
+  double inv = 1.0 / scaled;
+  double c1 = (d->icoeff + d->pcoeff + d->dcoeff) / error_order;
+  double c2 = -(d->pcoeff + 2 * d->dcoeff) / error_order;
+  double c3 = d->dcoeff / error_order;
+  double f1 = (c1 == 0) ? 1.0 : pow(inv, c1);
+  double f2 = (c2 == 0) ? 1.0 : pow(cs->prev_inv, c2);
+  double f3 = (c3 == 0) ? 1.0 : pow(cs->prev_prev_inv, c3);
+  double fmin = keep ? 1.0 : d->factormin;
+  double fmax = keep ? d->factormax : d->safety;
+  double factor = d->safety * f1 * f2 * f3;
+  factor = fmax < (factor > fmin ? factor : fmin) ? fmax : (factor > fmin ? factor : fmin);
+  double dt = prev_dt * factor;
+  if (inv == 0.0 || isinf(inv)) inv = 1.0;
+  *result = ORC_SUCCESSFUL;
+  if (has_dtmax) dt = dt < d->dtmax ? dt : d->dtmax;
+  int at_dtmin = cs->at_dtmin;
+  if (has_dtmin) {
+    if (!d->force_dtmin && dt < d->dtmin) *result = ORC_DT_MIN_REACHED;
+    if (at_dtmin && factor == 1.0) dt = d->dtmin;
+    at_dtmin = dt <= d->dtmin;
+    dt = dt > d->dtmin ? dt : d->dtmin;
+  }
+  *next_t0 = keep ? t1 : t0;
+  *next_t1 = *next_t0 + dt;
+  double new_inv = keep ? inv : cs->prev_inv;
+  double new_prev = keep ? cs->prev_inv : cs->prev_prev_inv;
+  cs->prev_inv = new_inv;
+  cs->prev_prev_inv = new_prev;
+  cs->at_dtmin = at_dtmin;
+  return keep;
+}
+
+/* ConstantStepSize.adapt_step_size (constant.py:59-104). */
+static int constant_adapt(double t1, CtrlState *cs, double *next_t0, double *next_t1) {
+  int sc = cs->steps_completed + 1;
+  double t1n = cs->t0_sim + (cs->t1_sim - cs->t0_sim) * ((double)sc / (double)cs->num_steps);
+  if (sc == cs->num_steps) t1n = cs->t1_sim;
+  cs->steps_completed = sc;
+  *next_t0 = t1;
+  *next_t1 = t1n;
+  return 1;
+}
+
+static double error_order_of(const orc_desc *d, const Tableau *tab) {
+  if (d->error_order > 0) return d->error_order;
+  if (d->diffusion != ORC_DIFF_NONE) return tab->strong_order + 0.5;
+  return (double)tab->order;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The per-trajectory solve loop (_integrate.py:302-885, init 1036-1305).    */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  /* inputs */
+  const orc_desc *d;
+  const double *t0, *t1, *dt0; /* dt0 may be NULL (None) */
+  int64_t time_stride;
+  const double *y0;
+  const double *args;
+  int64_t args_stride;
+  const double *params;
+  const double *ts;
+  orc_vf_cb cb;
+  void *cb_ctx;
+  /* outputs */
+  double *ys_out, *ts_out;
+  int32_t *result, *stats;
+} SolveIO;
+
+/* A record of one accepted step, kept for the discretise-then-optimise VJP. */
+typedef struct {
+  double tprev, tnext;
+  int save_lo, save_hi; /* save indices [lo, hi) produced by this step */
+} TapeStep;
+
+typedef struct {
+  TapeStep *steps;
+  double *ys;  /* y at the start of each accepted step [n x D] */
+  int n, cap;
+  int dir;
+  int t0_eq_t1;
+  int t1_slot;
+} Tape;
+
+static void tape_push(Tape *tp, int D, double tprev, double tnext, const double *y,
+                      int lo, int hi) {
+  if (tp->n == tp->cap) {
+    tp->cap = tp->cap ? tp->cap * 2 : 64;
+    tp->steps = (TapeStep *)realloc(tp->steps, sizeof(TapeStep) * tp->cap);
+    tp->ys = (double *)realloc(tp->ys, sizeof(double) * D * tp->cap);
+  }
+  tp->steps[tp->n].tprev = tprev;
+  tp->steps[tp->n].tnext = tnext;
+  tp->steps[tp->n].save_lo = lo;
+  tp->steps[tp->n].save_hi = hi;
+  memcpy(tp->ys + (int64_t)tp->n * D, y, sizeof(double) * D);
+  tp->n++;
+}
+
+static int n_save_of(const orc_desc *d) {
+  return (d->save_t0 ? 1 : 0) + d->n_ts + (d->save_t1 ? 1 : 0);
+}
+
+static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
+  const orc_desc *d = io->d;
+  const Tableau *tab = tableau_of(d->solver);
+  const int D = d->dim;
+  const int n_save = n_save_of(d);
+  Field F = {d, io->args + bidx * io->args_stride, io->params, io->cb, io->cb_ctx};
+  double *ys = io->ys_out + bidx * (int64_t)n_save * D;
+  double *tso = io->ts_out + bidx * (int64_t)n_save;
+  for (int64_t i = 0; i < (int64_t)n_save * D; i++) ys[i] = INFINITY;
+  for (int i = 0; i < n_save; i++) tso[i] = INFINITY;
+
+  double t0 = io->t0[bidx * io->time_stride], t1 = io->t1[bidx * io->time_stride];
+  /* _integrate.py:1157-1166: direction = where(t0 < t1, 1, -1) */
+  int dir = (t0 < t1) ? 1 : -1;
+  t0 *= dir; t1 *= dir;
+  int has_dt0 = io->dt0 != NULL;
+  double dt0 = has_dt0 ? io->dt0[bidx * io->time_stride] * dir : 0.0;
+  double y[64];
+  memcpy(y, io->y0 + bidx * D, sizeof(double) * D);
+  if (tape) { tape->dir = dir; tape->t0_eq_t1 = (t0 == t1); }
+
+  /* controller init (pid.py:316-392, constant.py:30-57) */
+  CtrlState cs;
+  memset(&cs, 0, sizeof cs);
+  double tnext;
+  if (d->controller == ORC_PID) {
+    /* The terms are already wrapped when init runs (_integrate.py:1172-1176,
+     * 1254), so _select_initial_step returns 0.01 (pid.py:48-49). */
+    double h = has_dt0 ? dt0 : 0.01;
+    if (!isnan(d->dtmax)) h = h < d->dtmax ? h : d->dtmax;
+    if (!isnan(d->dtmin)) h = h > d->dtmin ? h : d->dtmin;
+    tnext = t0 + h;
+    cs.prev_inv = 1.0; cs.prev_prev_inv = 1.0; cs.at_dtmin = 0;
+  } else {
+    cs.steps_completed = 1;
+    cs.num_steps = (int)ceil((t1 - t0) / nextafter(dt0, INFINITY));
+    cs.t0_sim = t0; cs.t1_sim = t1;
+    tnext = t0 + dt0;
+  }
+  tnext = tnext < t1 ? tnext : t1;
+  double tprev = t0;
+  double t1_clip_floor = t1;
+  for (int i = 0; i < 100; i++) t1_clip_floor = prevbefore(t1_clip_floor);
+  const double eord = error_order_of(d, tab);
+
+  int save_index = 0, ts_index = 0;
+  if (d->save_t0) {
+    for (int n = 0; n < D; n++) ys[n] = y[n];
+    tso[0] = t0;
+    save_index = 1;
+  }
+  int first_step = 1;
+  double f0[64];
+  memset(f0, 0, sizeof f0);
+  int result = ORC_SUCCESSFUL;
+  int num_steps = 0, num_acc = 0, num_rej = 0;
+  StepOut so;
+  double dw[64];
+  while (tprev < t1 && result == ORC_SUCCESSFUL) {
+    if (num_steps >= d->max_steps) break;
+    const double *dwp = NULL;
+    if (d->diffusion != ORC_DIFF_NONE) {
+      vbt_increment(d, (uint32_t)bidx, dir * tprev, dir * tnext, dw);
+      dwp = dw;
+    }
+    rk_step(&F, tab, dir, tprev, tnext, y, !first_step, f0, dwp, &so);
+    for (int n = 0; n < D; n++)
+      if (isnan(so.err[n])) so.err[n] = INFINITY; /* _integrate.py:386 */
+    int keep, cres = ORC_SUCCESSFUL;
+    double nt0, nt1;
+    if (d->controller == ORC_PID) {
+      /* pid.py:466-492: scale against max(|y0|, |y1|), y1 replaced by y0 if NaN */
+      int any_nan = 0;
+      for (int n = 0; n < D; n++) any_nan |= isnan(so.y1[n]);
+      double sc[64];
+      for (int n = 0; n < D; n++) {
+        double a0 = fabs(y[n]), a1 = fabs(any_nan ? y[n] : so.y1[n]);
+        double ym = a0 > a1 ? a0 : a1;
+        sc[n] = so.err[n] / (d->atol + ym * d->rtol);
+      }
+      double scaled = rms_norm(sc, D);
+      keep = pid_adapt(d, eord, tprev, tnext, scaled, &cs, &nt0, &nt1, &cres);
+    } else {
+      keep = constant_adapt(tnext, &cs, &nt0, &nt1);
+    }
+    /* _integrate.py:410-413 */
+    nt0 = nt0 < t1 ? nt0 : t1;
+    if (nt1 > t1_clip_floor) nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
+    if (keep) {
+      int lo = save_index;
+      /* _integrate.py:456-487: save every ts <= tnext of the step just taken */
+      while (ts_index < d->n_ts && dir * io->ts[ts_index] <= tnext) {
+        interp_eval(d->solver, &so, tab->s, dir * io->ts[ts_index], ys + (int64_t)save_index * D);
+        tso[save_index] = dir * io->ts[ts_index];
+        ts_index++; save_index++;
+      }
+      if (tape) tape_push(tape, D, tprev, tnext, y, lo, save_index);
+      memcpy(y, so.y1, sizeof(double) * D);
+      if (tab->fsal) { memcpy(f0, so.fsal_f, sizeof(double) * D); first_step = 0; }
+    }
+    if (result == ORC_SUCCESSFUL) result = cres;
+    num_steps++;
+    if (keep) num_acc++; else num_rej++;
+    tprev = nt0;
+    tnext = nt1;
+  }
+  /* _integrate.py:823-845: t0 == t1 fills the ts outputs with y0 */
+  if (t0 == t1) {
+    for (int i = 0; i < d->n_ts; i++) {
+      for (int n = 0; n < D; n++) ys[(int64_t)save_index * D + n] = y[n];
+      tso[save_index] = t0;
+      save_index++;
+    }
+  }
+  /* _integrate.py:847-877: the t1 save goes to the next free slot */
+  if (d->save_t1) {
+    for (int n = 0; n < D; n++) ys[(int64_t)save_index * D + n] = y[n];
+    tso[save_index] = tprev;
+    if (tape) tape->t1_slot = save_index;
+    save_index++;
+  }
+  if (result == ORC_SUCCESSFUL && tprev < t1) result = ORC_MAX_STEPS_REACHED;
+  for (int i = 0; i < n_save; i++) tso[i] *= dir;
+  io->result[bidx] = result;
+  io->stats[bidx * 3 + 0] = num_steps;
+  io->stats[bidx * 3 + 1] = num_acc;
+  io->stats[bidx * 3 + 2] = num_rej;
+}
+
+static void validate_desc(const orc_desc *d) { (void)d; init_tableaus(); }
+
+int orc_solve(const orc_desc *d, int64_t B, const double *t0, const double *t1,
+              const double *dt0, int64_t time_stride, const double *y0,
+              const double *args, int64_t args_stride, const double *params,
+              const double *ts, orc_vf_cb cb, void *cb_ctx, double *ys_out,
+              double *ts_out, int32_t *result, int32_t *stats, int nthreads) {
+  validate_desc(d);
+  if (d->dim > 64 || d->dim < 1) return -1;
+  SolveIO io = {d, t0, t1, dt0, time_stride, y0, args, args_stride, params, ts,
+                cb, cb_ctx, ys_out, ts_out, result, stats};
+#ifdef _OPENMP
+  if (nthreads > 0 && d->field != ORC_CALLBACK) {
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (int64_t b = 0; b < B; b++) solve_one(&io, b, NULL);
+    return 0;
+  }
+#endif
+  (void)nthreads;
+  for (int64_t b = 0; b < B; b++) solve_one(&io, b, NULL);
+  return 0;
+}
+
+/* Brownian increments of the oracle's tree, for checking the kernels' tree. */
+int orc_vbt_increments(const orc_desc *d, int64_t n, const uint32_t *traj,
+                       const double *ta, const double *tb, double *dw) {
+  for (int64_t i = 0; i < n; i++) vbt_increment(d, traj[i], ta[i], tb[i], dw + i * d->dim);
+  return 0;
+}
+
+int orc_normal4(uint64_t seed, uint32_t traj, uint32_t node, uint32_t kind, uint32_t q,
+                double *z) {
+  normal4(seed, traj, node, kind, q, z);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* RecursiveCheckpointAdjoint gradient (_adjoint.py:179-312).                */
+/*                                                                           */
+/* The reference differentiates the discrete solver: rejected steps get zero */
+/* cotangent through `where(keep, ...)` (_integrate.py:422-424) and the step */
+/* sizes are under stop_gradient, so the gradient is the VJP of the chain of */
+/* accepted steps on the realised time grid.  Checkpointing only changes the */
+/* recomputation schedule, not the values, so the oracle tapes every step.   */
+/* ------------------------------------------------------------------------ */
+static void step_vjp(const Field *F, const Tableau *tab, int dir, const StepOut *so,
+                     const double *gy1_in, double kbar[7][64], double *gy0,
+                     double *gargs, double *gP) {
+  const orc_desc *d = F->d;
+  const int D = d->dim;
+  const double control = dir * (so->tnext - so->tprev);
+  double gy1[64];
+  memcpy(gy1, gy1_in, sizeof(double) * D);
+  double ybar[7][64];
+  memset(ybar, 0, sizeof ybar);
+  if (tab->ssal) {
+    for (int n = 0; n < D; n++) ybar[tab->s - 1][n] += gy1[n];
+  } else {
+    for (int n = 0; n < D; n++) {
+      gy0[n] += gy1[n];
+      for (int j = 0; j < tab->s; j++) kbar[j][n] += tab->b[j] * gy1[n];
+    }
+  }
+  for (int i = tab->s - 1; i >= 0; i--) {
+    double g[64];
+    for (int n = 0; n < D; n++) g[n] = kbar[i][n] * control;
+    double gyi[64];
+    memcpy(gyi, ybar[i], sizeof(double) * D);
+    field_drift_vjp(F, so->ystage[i], g, gyi, gargs, gP);
+    if (d->diffusion != ORC_DIFF_NONE)
+      field_diffusion_vjp(F, so->ystage[i], so->dw, kbar[i], gyi, gargs, gP);
+    for (int n = 0; n < D; n++) gy0[n] += gyi[n];
+    for (int j = 0; j < i; j++)
+      for (int n = 0; n < D; n++) kbar[j][n] += tab->a[i][j] * gyi[n];
+  }
+}
+
+/* grad_ys: cotangent of the saved ys [B, n_save, D].  Outputs: grad_y0 [B, D],
+ * grad_args [B, n_args] (per trajectory), grad_params [n_params] summed over
+ * the batch (the caller gives nthreads private buffers via grad_params_tmp). */
+int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
+                       const double *t1, const double *dt0, int64_t time_stride,
+                       const double *y0, const double *args, int64_t args_stride,
+                       const double *params, int64_t n_params, const double *ts,
+                       const double *grad_ys, double *ys_out, double *ts_out,
+                       int32_t *result, int32_t *stats, double *grad_y0,
+                       double *grad_args, double *grad_params, int nthreads) {
+  validate_desc(d);
+  if (d->dim > 64 || d->dim < 1) return -1;
+  const Tableau *tab = tableau_of(d->solver);
+  const int D = d->dim;
+  const int n_save = n_save_of(d);
+  SolveIO io = {d, t0, t1, dt0, time_stride, y0, args, args_stride, params, ts,
+                NULL, NULL, ys_out, ts_out, result, stats};
+  int nt = 1;
+#ifdef _OPENMP
+  nt = nthreads > 0 ? nthreads : 1;
+#endif
+  double *gp_all = (double *)calloc((size_t)nt * (size_t)(n_params > 0 ? n_params : 1), sizeof(double));
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nt)
+#endif
+  for (int64_t b = 0; b < B; b++) {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    double *gP = n_params > 0 ? gp_all + (size_t)tid * n_params : NULL;
+    Tape tape;
+    memset(&tape, 0, sizeof tape);
+    solve_one(&io, b, &tape);
+    Field F = {d, args + b * args_stride, params, NULL, NULL};
+    const double *gys = grad_ys + b * (int64_t)n_save * D;
+    double gy[64];
+    memset(gy, 0, sizeof gy);
+    double *gargs = grad_args ? grad_args + b * d->n_args : NULL;
+    if (gargs) memset(gargs, 0, sizeof(double) * d->n_args);
+    /* t1 save reads the final state; t0 == t1 saves read y0 */
+    if (d->save_t1) for (int n = 0; n < D; n++) gy[n] += gys[(int64_t)tape.t1_slot * D + n];
+    if (tape.t0_eq_t1) {
+      int base = d->save_t0 ? 1 : 0;
+      for (int i = 0; i < d->n_ts; i++)
+        for (int n = 0; n < D; n++) gy[n] += gys[(int64_t)(base + i) * D + n];
+    }
+    StepOut so;
+    double f0dummy[64];
+    double dw[64];
+    for (int si = tape.n - 1; si >= 0; si--) {
+      TapeStep *st = &tape.steps[si];
+      const double *ystart = tape.ys + (int64_t)si * D;
+      const double *dwp = NULL;
+      if (d->diffusion != ORC_DIFF_NONE) {
+        vbt_increment(d, (uint32_t)b, tape.dir * st->tprev, tape.dir * st->tnext, dw);
+        dwp = dw;
+      }
+      rk_step(&F, tab, tape.dir, st->tprev, st->tnext, ystart, 0, f0dummy, dwp, &so);
+      double kbar[7][64];
+      memset(kbar, 0, sizeof kbar);
+      double gy0[64], gy1[64];
+      memset(gy0, 0, sizeof gy0);
+      memcpy(gy1, gy, sizeof(double) * D);
+      for (int m = st->save_lo; m < st->save_hi; m++) {
+        double tsv = ts_out[b * n_save + m] * tape.dir;
+        double th = linear_rescale(st->tprev, tsv, st->tnext);
+        double ay0, ay1, g[7];
+        interp_linear_coeffs(d->solver, tab->s, th, &ay0, &ay1, g);
+        const double *go = gys + (int64_t)m * D;
+        for (int n = 0; n < D; n++) {
+          gy0[n] += ay0 * go[n];
+          gy1[n] += ay1 * go[n];
+          for (int j = 0; j < tab->s; j++) kbar[j][n] += g[j] * go[n];
+        }
+      }
+      step_vjp(&F, tab, tape.dir, &so, gy1, kbar, gy0, gargs, gP);
+      memcpy(gy, gy0, sizeof(double) * D);
+    }
+    if (d->save_t0) for (int n = 0; n < D; n++) gy[n] += gys[n];
+    memcpy(grad_y0 + b * D, gy, sizeof(double) * D);
+    free(tape.steps);
+    free(tape.ys);
+  }
+  if (grad_params && n_params > 0) {
+    for (int64_t p = 0; p < n_params; p++) {
+      double acc = 0.0;
+      for (int t = 0; t < nt; t++) acc += gp_all[(size_t)t * n_params + p];
+      grad_params[p] = acc;
+    }
+  }
+  free(gp_all);
+  return 0;
+}
+
+int orc_abi_version(void) { return 1; }
+int orc_desc_size(void) { return (int)sizeof(orc_desc); }

@@ -1,0 +1,117 @@
+"""The C ABI: the library builds and loads, exports every symbol declared in
+include/gbdx.h, agrees with the Python descriptor layout and validates problems
+the way the reference raises ValueErrors.  No kernel runs here."""
+import ctypes
+import os
+import re
+
+import pytest
+import torch
+
+import diffrax_gb300 as dfx
+from diffrax_gb300 import _lib
+from diffrax_gb300._integrate import _host_checks
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "gbdx.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbdx_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = header_functions()
+    assert "gbdx_solve_fwd" in names and len(names) >= 8
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in gbdx.h but not exported"
+
+
+def test_descriptor_layout():
+    lib = _lib.load()
+    assert lib.gbdx_problem_desc_size() == ctypes.sizeof(_lib.ProblemDesc)
+    assert lib.gbdx_version() >= 1
+
+
+def _fields(**kw):
+    base = dfx.lower(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(),
+                     dfx.PIDController(rtol=1e-6, atol=1e-9), dfx.SaveAt(t1=True), dim=2,
+                     dtype=torch.float32, max_steps=4096, n_ts=0)
+    base.update(kw)
+    return base
+
+
+def test_problem_create_and_queries():
+    p = _lib.Problem(_fields())
+    assert p.n_save == 1
+    assert p.workspace_size(1000) >= 8
+    p2 = _lib.Problem(_fields(n_ts=7, save_t0=1))
+    assert p2.n_save == 9
+
+
+@pytest.mark.parametrize("bad, msg", [
+    (dict(solver=0), "error estimates"),          # adaptive Euler (pid.py:437-447)
+    (dict(solver=9), "unknown solver"),
+    (dict(max_steps=0), "max_steps"),
+    (dict(save_t1=0), "at least one"),
+    (dict(dtype=7), "dtype"),
+])
+def test_problem_validation(bad, msg):
+    with pytest.raises(ValueError, match=msg):
+        _lib.Problem(_fields(**bad))
+
+
+def test_unsupported_dimension():
+    with pytest.raises(_lib.GbdxError):
+        _lib.Problem(_fields(dim=3))
+
+
+def test_sde_euler_adaptive_rejected():
+    # _integrate.py:1145-1151
+    bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (1,), key=0)
+    terms = dfx.MultiTerm(dfx.ODETerm(dfx.OrnsteinUhlenbeck()),
+                          dfx.ControlTerm(dfx.OrnsteinUhlenbeck(), bm))
+    with pytest.raises(ValueError, match="SDE"):
+        dfx.lower(terms, dfx.Euler(), dfx.PIDController(rtol=1e-3, atol=1e-3),
+                  dfx.SaveAt(t1=True), dim=1, dtype=torch.float32, max_steps=10, n_ts=0)
+
+
+def test_host_checks():
+    t0 = torch.tensor([0.1], dtype=torch.float64)
+    t1 = torch.tensor([1.1], dtype=torch.float64)
+    with pytest.raises(ValueError):
+        _host_checks(t0, t1, torch.tensor([-0.1], dtype=torch.float64), None, 0)
+    # test/test_saveat_solution.py:89-94: ts outside [t0, t1] raise RuntimeError.
+    with pytest.raises(RuntimeError):
+        _host_checks(t0, t1, None, torch.tensor([0.0], dtype=torch.float64), 0)
+    with pytest.raises(RuntimeError):
+        _host_checks(t0, t1, None, torch.tensor([3.0], dtype=torch.float64), 0)
+    with pytest.raises(RuntimeError):
+        _host_checks(t0, t1, None, torch.tensor([0.8, 0.5], dtype=torch.float64), 0)
+    _host_checks(t0, t1, None, torch.tensor([0.5, 0.8], dtype=torch.float64), 0)
+    # backwards in time: decreasing ts are valid
+    _host_checks(t1, t0, None, torch.tensor([0.8, 0.5], dtype=torch.float64), 0)
+
+
+def test_saveat_validation():
+    with pytest.raises(ValueError):
+        dfx.SaveAt()
+    with pytest.raises(NotImplementedError):
+        dfx.SaveAt(dense=True)
+
+
+def test_backsolve_kwargs_validation():
+    with pytest.raises(ValueError):
+        dfx.BacksolveAdjoint(foo=1)
+    dfx.BacksolveAdjoint(solver=dfx.Dopri5())
+
+
+def test_no_cpu_fallback():
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(RuntimeError, match="CUDA"):
+        dfx.diffeqsolve(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(), 0.0, 1.0, None,
+                        torch.zeros(4, 2), torch.ones(1),
+                        stepsize_controller=dfx.PIDController(rtol=1e-6, atol=1e-9))

@@ -1,0 +1,206 @@
+"""GPU parity of the analytic-field kernels (K0 plain, K1 fused) against the
+FP64 oracle on identical seeded inputs.
+
+FP64-state runs must reproduce the oracle's step sequence (identical step and
+rejection counts) and its values to 1e-9 relative; FP32-state runs (FP64 time)
+must agree within the stated tolerance of the solve.
+"""
+import numpy as np
+import pytest
+import torch
+
+import diffrax_gb300 as dfx
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SOLVERS = {"euler": dfx.Euler(), "heun": dfx.Heun(), "dopri5": dfx.Dopri5(),
+           "tsit5": dfx.Tsit5()}
+
+
+def run_both(field, solver, controller, saveat, t0, t1, dt0, y0, args, dtype, kernel,
+             max_steps=4096):
+    dev = torch.device("cuda")
+    y0_t = torch.tensor(y0, dtype=dtype, device=dev)
+    args_t = None if args is None else torch.tensor(args, dtype=dtype, device=dev)
+    tt = lambda x: torch.tensor(x, dtype=torch.float64, device=dev) if isinstance(  # noqa
+        x, np.ndarray) else x
+    sol = dfx.diffeqsolve(dfx.ODETerm(field), solver, tt(t0), tt(t1), tt(dt0), y0_t, args_t,
+                          saveat=saveat, stepsize_controller=controller,
+                          max_steps=max_steps, throw=False, kernel=kernel)
+    torch.cuda.synchronize()
+    ts = None if saveat.ts is None else np.asarray(saveat.ts, dtype=np.float64)
+    fields = dfx.lower(dfx.ODETerm(field), solver, controller, saveat, dim=y0.shape[1],
+                       dtype=dtype, max_steps=max_steps, n_ts=0 if ts is None else ts.size)
+    d = O.make_desc(**dfx.oracle_fields(fields))
+    r = O.solve(d, t0, t1, dt0, y0, args=args, ts=ts, nthreads=8)
+    return sol, r
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    fin = np.isfinite(b)
+    assert np.array_equal(fin, np.isfinite(a))
+    scale = np.maximum(np.abs(b[fin]).max(), 1e-300)
+    return float(np.abs(a[fin] - b[fin]).max() / scale)
+
+
+LV_ARGS = np.array([0.1, 0.02, 0.4, 0.02])
+
+
+@pytest.mark.parametrize("kernel", ["plain", "fused"])
+@pytest.mark.parametrize("solver", ["heun", "dopri5", "tsit5"])
+def test_lotka_volterra_fp64_matches_oracle(kernel, solver):
+    # Config: LV, PID(1e-6, 1e-8), t in [0, 140], dt0 = 0.1, 100 saves.
+    rng = np.random.default_rng(0)
+    y0 = rng.uniform(5, 15, (256, 2))
+    ts = np.linspace(0.0, 140.0, 100)
+    sol, r = run_both(dfx.LotkaVolterra(), SOLVERS[solver],
+                      dfx.PIDController(rtol=1e-6, atol=1e-8), dfx.SaveAt(ts=ts), 0.0, 140.0,
+                      0.1, y0, LV_ARGS, torch.float64, kernel, max_steps=100000)
+    stats = sol.stats
+    assert np.array_equal(sol.result.cpu().numpy(), r["result"])
+    assert np.array_equal(stats["num_steps"].cpu().numpy(), r["stats"][:, 0])
+    assert np.array_equal(stats["num_rejected_steps"].cpu().numpy(), r["stats"][:, 2])
+    assert rel_err(sol.ys.cpu().numpy(), r["ys"]) < 1e-9
+    assert np.array_equal(sol.ts.cpu().numpy(), r["ts"])
+
+
+@pytest.mark.parametrize("kernel", ["plain", "fused"])
+def test_lotka_volterra_config1_fp32(kernel):
+    # Config 1 (batch 1024, Tsit5, PID(1e-6, 1e-8), 100 ts) with FP32 state.
+    rng = np.random.default_rng(1)
+    y0 = rng.uniform(5, 15, (1024, 2))
+    ts = np.linspace(0.0, 140.0, 100)
+    sol, r = run_both(dfx.LotkaVolterra(), dfx.Tsit5(),
+                      dfx.PIDController(rtol=1e-6, atol=1e-8), dfx.SaveAt(ts=ts), 0.0, 140.0,
+                      0.1, y0, LV_ARGS, torch.float32, kernel)
+    assert (sol.result == 0).all()
+    err = rel_err(sol.ys.cpu().numpy(), r["ys"])
+    print(f"LV config-1 FP32 {kernel}: max rel err vs FP64 oracle {err:.3e}")
+    assert err < 2e-3
+    steps = sol.stats["num_steps"].cpu().numpy()
+    assert abs(steps.mean() / r["stats"][:, 0].mean() - 1) < 0.05
+
+
+def vdp_inputs(B, seed):
+    rng = np.random.default_rng(seed)
+    mu = np.exp(rng.uniform(np.log(0.1), np.log(10.0), B))
+    y0 = rng.uniform(-2, 2, (B, 2))
+    t1 = rng.uniform(5, 50, B)
+    return mu, y0, t1
+
+
+@pytest.mark.parametrize("kernel", ["plain", "fused"])
+def test_van_der_pol_uneven_fp64(kernel):
+    mu, y0, t1 = vdp_inputs(512, 2)
+    sol, r = run_both(dfx.VanDerPol(), dfx.Dopri5(),
+                      dfx.PIDController(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4),
+                      dfx.SaveAt(t1=True), 0.0, t1, None, y0, mu[:, None], torch.float64,
+                      kernel)
+    assert np.array_equal(sol.stats["num_steps"].cpu().numpy(), r["stats"][:, 0])
+    assert rel_err(sol.ys.cpu().numpy(), r["ys"]) < 1e-9
+    assert np.array_equal(sol.ts.cpu().numpy(), r["ts"])
+
+
+@pytest.mark.parametrize("kernel", ["plain", "fused"])
+def test_van_der_pol_config2_fp32(kernel):
+    # Config 2 distribution; FP32 state with FP64 t/dt against the FP64 oracle.
+    mu, y0, t1 = vdp_inputs(8192, 3)
+    sol, r = run_both(dfx.VanDerPol(), dfx.Dopri5(),
+                      dfx.PIDController(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4),
+                      dfx.SaveAt(t1=True), 0.0, t1, None, y0, mu[:, None], torch.float32,
+                      kernel)
+    assert (sol.result == 0).all()
+    ys = sol.ys.cpu().numpy()
+    per = np.abs(ys - r["ys"]).max(axis=(1, 2)) / np.abs(r["ys"]).max(axis=(1, 2))
+    print(f"VdP config-2 FP32 {kernel}: median rel err {np.median(per):.2e} max {per.max():.2e}")
+    assert np.median(per) < 1e-4
+    assert np.quantile(per, 0.99) < 5e-3
+    assert np.array_equal(sol.ts.cpu().numpy(), r["ts"])
+
+
+@pytest.mark.parametrize("solver", list(SOLVERS))
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_constant_step_all_solvers(solver, dtype):
+    # y' = -y (OU with theta = 1, mu = 0), ConstantStepSize, t0 = 0, t1 = 1,
+    # dt0 = 0.01 (test/test_integrate.py:48-141) and saves at ts.
+    y0 = np.linspace(-2, 2, 64).reshape(32, 2)
+    ts = np.array([0.0, 0.25, 0.5, 0.999, 1.0])
+    sol, r = run_both(dfx.OrnsteinUhlenbeck(), SOLVERS[solver], dfx.ConstantStepSize(),
+                      dfx.SaveAt(ts=ts, t1=True, t0=True), 0.0, 1.0, 0.01, y0,
+                      np.array([1.0, 0.0, 0.0]), dtype, "fused")
+    tol = 1e-12 if dtype == torch.float64 else 2e-6
+    assert rel_err(sol.ys.cpu().numpy(), r["ys"]) < tol
+    assert np.allclose(sol.ys[:, -1].cpu().numpy(), y0 * np.exp(-1), rtol=1e-2, atol=1e-2)
+    assert np.array_equal(sol.stats["num_steps"].cpu().numpy(), r["stats"][:, 0])
+
+
+@pytest.mark.parametrize("kernel", ["plain", "fused"])
+def test_edge_cases_fp64(kernel):
+    ou = dfx.OrnsteinUhlenbeck()
+    args = np.array([0.5, 0.0, 0.0])
+    pid = dfx.PIDController(rtol=1e-8, atol=1e-8)
+    y0 = np.array([[2.1], [1.0], [-3.0]])
+    # Backwards in time with decreasing ts.
+    sol, r = run_both(ou, dfx.Dopri5(), pid, dfx.SaveAt(ts=np.array([0.8, 0.5]), t1=True),
+                      1.1, 0.1, None, y0, args, torch.float64, kernel)
+    assert rel_err(sol.ys.cpu().numpy(), r["ys"]) < 1e-10
+    assert np.allclose(sol.ys[0, -1, 0].item(), 2.1 * np.exp(-0.5 * -1.0), rtol=1e-6)
+    # t0 == t1.
+    sol, r = run_both(ou, dfx.Tsit5(), pid, dfx.SaveAt(ts=np.array([0.3, 0.3]), t1=True),
+                      0.3, 0.3, None, y0, args, torch.float64, kernel)
+    assert np.array_equal(sol.ys.cpu().numpy(), r["ys"])
+    assert (sol.stats["num_steps"] == 0).all()
+    # max_steps reached: result code, t1 save in the next free slot, +inf after.
+    sol, r = run_both(ou, dfx.Tsit5(), dfx.ConstantStepSize(),
+                      dfx.SaveAt(ts=np.array([0.2, 0.7, 0.9]), t1=True), 0.0, 1.0, 0.1, y0,
+                      args, torch.float64, kernel, max_steps=5)
+    assert (sol.result == 1).all()
+    assert np.array_equal(np.isinf(sol.ys.cpu().numpy()), np.isinf(r["ys"]))
+    assert rel_err(sol.ys.cpu().numpy(), r["ys"]) < 1e-12
+    # Per-trajectory t1 / dt0 arrays, dtmax.
+    t1 = np.array([0.5, 1.0, 2.0])
+    sol, r = run_both(ou, dfx.Dopri5(), dfx.PIDController(rtol=1e-6, atol=1e-6, dtmax=0.05),
+                      dfx.SaveAt(t1=True), 0.0, t1, np.array([0.01, 0.02, 0.03]), y0, args,
+                      torch.float64, kernel)
+    assert np.array_equal(sol.stats["num_steps"].cpu().numpy(), r["stats"][:, 0])
+    assert rel_err(sol.ys.cpu().numpy(), r["ys"]) < 1e-10
+
+
+def test_throw_raises_on_max_steps():
+    dev = torch.device("cuda")
+    with pytest.raises(RuntimeError, match="maximum number of solver steps"):
+        dfx.diffeqsolve(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(), 0.0, 50.0, None,
+                        torch.zeros(8, 2, device=dev) + 1.0, torch.ones(1, device=dev),
+                        stepsize_controller=dfx.PIDController(rtol=1e-8, atol=1e-8),
+                        max_steps=3)
+
+
+def test_empty_batch_and_single_trajectory():
+    dev = torch.device("cuda")
+    pid = dfx.PIDController(rtol=1e-6, atol=1e-9)
+    sol = dfx.diffeqsolve(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(), 0.0, 5.0, None,
+                          torch.zeros(0, 2, device=dev), torch.ones(1, device=dev),
+                          stepsize_controller=pid)
+    assert sol.ys.shape == (0, 1, 2)
+    sol = dfx.diffeqsolve(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(), 0.0, 5.0, None,
+                          torch.ones(1, 2, device=dev), torch.ones(1, device=dev),
+                          stepsize_controller=pid)
+    assert sol.ys.shape == (1, 1, 2) and torch.isfinite(sol.ys).all()
+
+
+def test_fused_is_deterministic():
+    mu, y0, t1 = vdp_inputs(4096, 9)
+    dev = torch.device("cuda")
+    outs = []
+    for _ in range(2):
+        sol = dfx.diffeqsolve(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(), 0.0,
+                              torch.tensor(t1, device=dev), None,
+                              torch.tensor(y0, dtype=torch.float32, device=dev),
+                              torch.tensor(mu, dtype=torch.float32, device=dev),
+                              stepsize_controller=dfx.PIDController(rtol=1e-6, atol=1e-9,
+                                                                    pcoeff=0.3, icoeff=0.4))
+        outs.append(sol.ys.cpu())
+    assert torch.equal(outs[0], outs[1])

@@ -1,0 +1,419 @@
+"""Pins of the FP64 oracle against the reference's own known-answer tests.
+
+Each test restates a reference test (cited) with the oracle in place of
+Diffrax.  The DETEST pin reads the problem definitions from the reference's
+test file at run time (it is skipped where the reference tree is absent).
+"""
+import ast
+import math
+import os
+
+import numpy as np
+import pytest
+import scipy.integrate
+import scipy.linalg
+import scipy.stats
+
+import oracle as O
+from conftest import tree_allclose
+
+SOLVERS = [O.EULER, O.HEUN, O.DOPRI5, O.TSIT5]
+ORDERS = {O.EULER: 1, O.HEUN: 2, O.DOPRI5: 5, O.TSIT5: 5}
+
+
+def _decay(**kw):
+    # y' = -0.5 y, t in [0.1, 1.1], y0 = 2.1, Dopri5, PID(1e-8, 1e-8), dt0=None
+    # (test/test_saveat_solution.py:24-40)
+    d = O.make_desc(solver=O.DOPRI5, controller=O.PID, field=O.LINEAR, dim=1, rtol=1e-8,
+                    atol=1e-8, **kw)
+    return d
+
+
+def test_saveat_t1_decay():
+    # test/test_saveat_solution.py:62-87
+    r = O.solve(_decay(save_t1=1), 0.1, 1.1, None, [[2.1]], params=[[-0.5]])
+    assert r["ts"][0, 0] == 1.1
+    assert tree_allclose(r["ys"][0, 0], 2.1 * math.exp(-0.5))
+    assert r["stats"][0, 0] > 0 and r["result"][0] == 0
+
+
+def test_saveat_t0_decay():
+    # test/test_saveat_solution.py:43-60
+    r = O.solve(_decay(save_t0=1, save_t1=0), 0.1, 1.1, None, [[2.1]], params=[[-0.5]])
+    assert r["ts"].shape == (1, 1) and r["ts"][0, 0] == 0.1 and r["ys"][0, 0, 0] == 2.1
+
+
+def test_saveat_ts_decay():
+    # test/test_saveat_solution.py:96-113
+    r = O.solve(_decay(n_ts=2, save_t1=0), 0.1, 1.1, None, [[2.1]], params=[[-0.5]],
+                ts=[0.5, 0.8])
+    assert r["ts"][0, 0] == 0.5 and r["ts"][0, 1] == 0.8
+    assert tree_allclose(r["ys"][0, 0], 2.1 * math.exp(-0.2))
+    assert tree_allclose(r["ys"][0, 1], 2.1 * math.exp(-0.35))
+
+
+@pytest.mark.parametrize("solver", SOLVERS)
+@pytest.mark.parametrize("ctrl", ["constant", "pid", "pi"])
+def test_basic_decay(solver, ctrl):
+    # y' = -y on [0, 1], dt0 = 0.01 (test/test_integrate.py:48-141)
+    if ctrl != "constant" and solver == O.EULER:
+        return
+    kw = dict(controller=O.CONSTANT) if ctrl == "constant" else dict(
+        controller=O.PID, rtol=1e-5, atol=1e-8)
+    if ctrl == "pi":
+        kw.update(pcoeff=0.3, icoeff=0.3)
+    d = O.make_desc(solver=solver, field=O.LINEAR, dim=1, **kw)
+    y0 = np.array([[0.7], [-1.3], [2.0]])
+    r = O.solve(d, 0.0, 1.0, 0.01, y0, params=[[-1.0]])
+    assert tree_allclose(r["ys"][:, 0], y0 * math.exp(-1), rtol=1e-2, atol=1e-2)
+
+
+@pytest.mark.parametrize("solver", SOLVERS)
+def test_ode_order(solver):
+    # Linear ODE against expm, fitted order (test/test_integrate.py:144-190).
+    rng = np.random.default_rng(5678)
+    A = rng.standard_normal((10, 10)) * 0.5
+    y0 = rng.standard_normal(10)
+    true = scipy.linalg.expm(4.0 * A) @ y0
+    d = O.make_desc(solver=solver, controller=O.CONSTANT, field=O.LINEAR, dim=10,
+                    max_steps=1 << 20)
+    exps, errs = [], []
+    for e in [0, -1, -2, -3, -4, -6, -8, -12]:
+        r = O.solve(d, 0.0, 4.0, 2.0 ** e, y0[None], params=A)
+        err = np.sum(np.abs(r["ys"][0, -1] - true))
+        if err < 2 ** -28:
+            break
+        exps.append(e)
+        errs.append(np.log2(err))
+    order = scipy.stats.linregress(exps, errs).slope
+    assert -0.9 < order - ORDERS[solver] < 0.9
+
+
+def test_backwards_in_time():
+    # t1 < t0 integrates backwards (_integrate.py:1157-1176): y' = -0.5 y from
+    # t=1.1 to t=0.1 multiplies by exp(0.5).
+    d = _decay(n_ts=2, save_t1=1)
+    r = O.solve(d, 1.1, 0.1, None, [[2.1]], params=[[-0.5]], ts=[0.8, 0.5])
+    assert tree_allclose(r["ys"][0, 0], 2.1 * math.exp(0.15))
+    assert tree_allclose(r["ys"][0, 1], 2.1 * math.exp(0.3))
+    assert tree_allclose(r["ys"][0, 2], 2.1 * math.exp(0.5))
+    assert r["ts"][0, 0] == 0.8 and r["ts"][0, 2] == 0.1
+
+
+def test_t0_equals_t1():
+    # _integrate.py:823-845: ts are filled with y0, t1 saves y0.
+    d = _decay(n_ts=2, save_t1=1)
+    r = O.solve(d, 0.3, 0.3, None, [[2.1]], params=[[-0.5]], ts=[0.3, 0.3])
+    assert np.all(r["ys"] == 2.1) and r["stats"][0, 0] == 0 and r["result"][0] == 0
+
+
+def test_max_steps_reached():
+    # _integrate.py:883: unfinished solves report max_steps_reached; the t1 save
+    # takes the next free slot and later slots stay +inf.
+    d = O.make_desc(solver=O.TSIT5, controller=O.CONSTANT, field=O.LINEAR, dim=1, n_ts=3,
+                    save_t1=1, max_steps=5)
+    r = O.solve(d, 0.0, 1.0, 0.1, [[1.0]], params=[[-1.0]], ts=[0.2, 0.7, 0.9])
+    assert r["result"][0] == 1 and r["stats"][0, 0] == 5
+    assert np.isfinite(r["ys"][0, 0, 0]) and r["ts"][0, 1] == 0.5
+    assert np.all(np.isinf(r["ys"][0, 2:])) and np.all(np.isinf(r["ts"][0, 2:]))
+
+
+def test_constant_grid():
+    # constant.py:48-57, 84-90: N = ceil((t1 - t0) / nextafter(dt0)) steps,
+    # t_n = t0 + (t1 - t0) n / N, the last one exactly t1.
+    d = O.make_desc(solver=O.EULER, controller=O.CONSTANT, field=O.LINEAR, dim=1)
+    r = O.solve(d, 0.0, 1.0, 0.1, [[1.0]], params=[[0.0]])
+    assert r["stats"][0, 0] == 10
+    r = O.solve(d, 0.0, 1.0, 0.3, [[1.0]], params=[[0.0]])
+    assert r["stats"][0, 0] == 4
+
+
+def test_dtmax_dtmin():
+    d = O.make_desc(solver=O.TSIT5, controller=O.PID, field=O.LINEAR, dim=1, rtol=1e-3,
+                    atol=1e-6, dtmax=0.05)
+    r = O.solve(d, 0.0, 1.0, None, [[1.0]], params=[[-1.0]])
+    assert r["stats"][0, 1] >= 20
+    d = O.make_desc(solver=O.TSIT5, controller=O.PID, field=O.LINEAR, dim=1, rtol=1e-12,
+                    atol=1e-12, dtmin=0.1)
+    r = O.solve(d, 0.0, 1.0, 0.1, [[1.0]], params=[[-1.0]])
+    assert r["stats"][0, 1] <= 11 and r["result"][0] == 0
+    d = O.make_desc(solver=O.TSIT5, controller=O.PID, field=O.LINEAR, dim=1, rtol=1e-12,
+                    atol=1e-12, dtmin=0.1, force_dtmin=0)
+    r = O.solve(d, 0.0, 1.0, 0.1, [[1.0]], params=[[-1.0]], )
+    assert r["result"][0] == 2
+
+
+# --- local interpolants (test/test_local_interpolation.py:8-60) -------------
+
+def test_hermite_interpolant_exact_on_cubics():
+    # A cubic solution is reproduced exactly by Heun's Hermite interpolant when
+    # y1 and the endpoint slopes are exact.  With y' = 3 t^2 integrated by Heun
+    # the stage slopes are exact and y1 is the trapezoid value, so interpolate
+    # y = t^3 on one step and compare with the cubic Hermite formula.
+    d = O.make_desc(solver=O.HEUN, controller=O.CONSTANT, field=O.CALLBACK, dim=1, n_ts=3)
+    ts = [2.2, 2.6, 3.5]
+    r = O.solve(d, 2.0, 3.9, 1.9, [[8.0]], ts=ts, callback=lambda t, y: np.array([3 * t * t]))
+    h = 1.9
+    y0, y1 = 8.0, 8.0 + 0.5 * h * (3 * 4.0 + 3 * 3.9 ** 2)
+    k0, k1 = 3 * 4.0 * h, 3 * 3.9 ** 2 * h
+    for i, t in enumerate(ts):
+        th = (t - 2.0) / h
+        a = k0 + k1 + 2 * y0 - 2 * y1
+        b = -2 * k0 - k1 - 3 * y0 + 3 * y1
+        assert np.isclose(r["ys"][0, i, 0], ((a * th + b) * th + k0) * th + y0, rtol=1e-13)
+
+
+@pytest.mark.parametrize("solver", [O.DOPRI5, O.TSIT5])
+def test_high_order_interpolants(solver):
+    # Dense output of the 5th-order methods is accurate to ~tolerance.
+    d = O.make_desc(solver=solver, controller=O.PID, field=O.LINEAR, dim=1, rtol=1e-10,
+                    atol=1e-10, n_ts=50, save_t1=0)
+    ts = np.linspace(0.0, 3.0, 50)
+    r = O.solve(d, 0.0, 3.0, None, [[1.3]], params=[[-0.7]], ts=ts)
+    assert np.allclose(r["ys"][0, :, 0], 1.3 * np.exp(-0.7 * ts), rtol=1e-7, atol=1e-9)
+
+
+# --- DETEST against scipy DOP853 (test/test_detest.py:390-469) --------------
+
+REF_DETEST = "/root/reference/test/test_detest.py"
+
+
+class _At:
+    def __init__(self, arr):
+        self.arr = arr
+
+    def __getitem__(self, idx):
+        arr = self.arr
+
+        class _Set:
+            def set(self, v):
+                out = np.array(arr, dtype=float).view(_AtArray)
+                out[idx] = v
+                return out
+        return _Set()
+
+
+class _AtArray(np.ndarray):
+    @property
+    def at(self):
+        return _At(self)
+
+
+class _JnpShim:
+    def __getattr__(self, name):
+        fn = getattr(np, name)
+        if callable(fn):
+            def wrapped(*a, **k):
+                out = fn(*a, **k)
+                return out.view(_AtArray) if isinstance(out, np.ndarray) else out
+            return wrapped
+        return fn
+
+
+class _JaxShim:
+    class numpy_rank_promotion:
+        def __init__(self, *_):
+            pass
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            return False
+
+
+def _flatten(tree):
+    if isinstance(tree, (tuple, list)):
+        parts = [_flatten(x) for x in tree]
+        leaves = np.concatenate([p[0] for p in parts]) if parts else np.zeros(0)
+
+        def unflat(v, parts=parts, typ=type(tree)):
+            out, i = [], 0
+            for (lv, uf) in parts:
+                out.append(uf(v[i:i + lv.size]))
+                i += lv.size
+            return typ(out)
+        return leaves, unflat
+    a = np.asarray(tree, dtype=float)
+    shape = a.shape
+    return a.reshape(-1), (lambda v, shape=shape: np.asarray(v).reshape(shape))
+
+
+def _detest_problems():
+    src = open(REF_DETEST).read()
+    tree = ast.parse(src)
+    ns = {"jnp": _JnpShim(), "jax": _JaxShim(), "math": math, "np": np}
+    names = []
+    def is_problem(n):
+        return n[:2] in ("_a", "_b", "_c", "_d", "_e") and n[2:].isdigit()
+    for node in tree.body:
+        keep = False
+        if isinstance(node, ast.FunctionDef):
+            keep = is_problem(node.name) or node.name == "_make_d"
+            if is_problem(node.name):
+                names.append(node.name)
+        elif isinstance(node, ast.Assign) and len(node.targets) == 1 and \
+                isinstance(node.targets[0], ast.Name) and is_problem(node.targets[0].id):
+            keep = True
+            names.append(node.targets[0].id)
+        if keep:
+            exec(compile(ast.Module(body=[node], type_ignores=[]), REF_DETEST, "exec"), ns)
+    return ns, names
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DETEST), reason="reference tree absent")
+@pytest.mark.parametrize("solver", [O.HEUN, O.DOPRI5, O.TSIT5])
+def test_detest_against_scipy(solver):
+    ns, names = _detest_problems()
+    assert len(names) == 25
+    checked = 0
+    for name in names:
+        higher = name[1] != "a"
+        if higher and ORDERS[solver] < 4:
+            continue
+        diffeq, init = ns[name]()
+        y0, unflat = _flatten(init)
+        if y0.size > 64:
+            continue
+
+        def fn(t, y, diffeq=diffeq, unflat=unflat):
+            return _flatten(diffeq(t, unflat(y), None))[0]
+        tol = 1e-6 if ORDERS[solver] < 4 else 1e-8
+        d = O.make_desc(solver=solver, controller=O.PID, field=O.CALLBACK, dim=y0.size,
+                        rtol=tol, atol=tol, max_steps=16 ** 4)
+        r = O.solve(d, 0.0, 20.0, None, y0[None], callback=fn)
+        ref = scipy.integrate.solve_ivp(fn, (0, 20), y0, method="DOP853", rtol=1e-8,
+                                        atol=1e-8, t_eval=[20]).y[:, 0]
+        t2 = 1e-3 if ORDERS[solver] < 4 else 4e-5
+        assert r["result"][0] == 0, name
+        assert tree_allclose(r["ys"][0, 0], ref, rtol=t2, atol=t2), name
+        checked += 1
+    assert checked >= 5
+
+
+# --- gradients: oracle VJP against central finite differences ---------------
+# (test/test_adjoint.py:33-215 checks adjoints against finite differences.)
+
+def _fd_check(desc, t0, t1, dt0, y0, args=None, params=None, ts=None, eps=1e-6, tol=1e-5):
+    rng = np.random.default_rng(0)
+    n_save = desc.save_t0 + desc.n_ts + desc.save_t1
+    gys = rng.standard_normal((y0.shape[0], n_save, desc.dim))
+
+    def loss(y0_, args_, params_):
+        r = O.solve(desc, t0, t1, dt0, y0_, args=args_, params=params_, ts=ts)
+        return float(np.sum(r["ys"] * gys))
+    g = O.grad_recursive(desc, t0, t1, dt0, y0, gys, args=args, params=params, ts=ts)
+    # y0
+    for i in range(y0.shape[1]):
+        e = np.zeros_like(y0)
+        e[:, i] = eps
+        fd = (loss(y0 + e, args, params) - loss(y0 - e, args, params)) / (2 * eps)
+        assert np.isclose(g["grad_y0"][:, i].sum(), fd, rtol=tol, atol=tol)
+    if args is not None:
+        a = np.asarray(args, dtype=float)
+        for i in range(a.shape[-1]):
+            e = np.zeros_like(a)
+            e[..., i] = eps
+            fd = (loss(y0, a + e, params) - loss(y0, a - e, params)) / (2 * eps)
+            assert np.isclose(g["grad_args"][:, i].sum(), fd, rtol=tol, atol=tol)
+    if params is not None:
+        p = np.asarray(params, dtype=float).reshape(-1)
+        idx = rng.choice(p.size, size=min(8, p.size), replace=False)
+        for j in idx:
+            e = np.zeros_like(p)
+            e[j] = eps
+            fd = (loss(y0, args, p + e) - loss(y0, args, p - e)) / (2 * eps)
+            assert np.isclose(g["grad_params"][j], fd, rtol=tol, atol=tol)
+    return g
+
+
+@pytest.mark.parametrize("solver", [O.EULER, O.HEUN, O.DOPRI5, O.TSIT5])
+def test_grad_lotka_volterra_constant_steps(solver):
+    # With a fixed grid the discrete map is smooth: FD and VJP agree tightly.
+    d = O.make_desc(solver=solver, controller=O.CONSTANT, field=O.LOTKA_VOLTERRA, dim=2,
+                    n_ts=5, save_t1=1, n_args=4)
+    y0 = np.array([[10.0, 5.0], [7.0, 12.0]])
+    _fd_check(d, 0.0, 10.0, 0.05, y0, args=np.array([0.1, 0.02, 0.4, 0.02]),
+              ts=np.linspace(0, 10, 5), tol=1e-6)
+
+
+@pytest.mark.parametrize("solver", [O.HEUN, O.DOPRI5, O.TSIT5])
+def test_grad_lotka_volterra_pid(solver):
+    # Under PID the controller is stop-gradient (pid.py:374, 499-501, 529-530);
+    # FD also sees dt's dependence on the state, which shrinks with the
+    # tolerance, so compare at a tight tolerance.
+    tol = 1e-10 if solver != O.HEUN else 1e-7
+    d = O.make_desc(solver=solver, controller=O.PID, field=O.LOTKA_VOLTERRA, dim=2,
+                    rtol=tol, atol=tol, n_ts=5, save_t1=1, n_args=4, max_steps=100000)
+    y0 = np.array([[10.0, 5.0], [7.0, 12.0]])
+    _fd_check(d, 0.0, 10.0, 0.1, y0, args=np.array([0.1, 0.02, 0.4, 0.02]),
+              ts=np.linspace(0, 10, 5), tol=1e-5 if solver != O.HEUN else 1e-3)
+
+
+def test_grad_van_der_pol_per_trajectory_args():
+    d = O.make_desc(solver=O.DOPRI5, controller=O.PID, field=O.VAN_DER_POL, dim=2, rtol=1e-10,
+                    atol=1e-12, pcoeff=0.3, icoeff=0.4, save_t1=1, n_args=1)
+    y0 = np.array([[1.0, -0.5], [0.3, 1.5]])
+    _fd_check(d, 0.0, 5.0, None, y0, args=np.array([[1.3], [0.4]]), tol=1e-5)
+
+
+def test_grad_mlp():
+    rng = np.random.default_rng(3)
+    widths = [4, 8, 8, 4]
+    P = []
+    for i in range(3):
+        P.append(rng.standard_normal((widths[i + 1], widths[i])) / np.sqrt(widths[i]))
+        P.append(rng.standard_normal(widths[i + 1]) * 0.1)
+    params = np.concatenate([p.reshape(-1) for p in P])
+    d = O.make_desc(solver=O.TSIT5, controller=O.PID, field=O.MLP, dim=4, rtol=1e-10,
+                    atol=1e-10, save_t1=1, mlp_depth=3, mlp_widths=widths)
+    y0 = rng.standard_normal((3, 4))
+    _fd_check(d, 0.0, 1.0, None, y0, params=params, tol=1e-5)
+
+
+def test_grad_sde_heun_tanh_diffusion():
+    rng = np.random.default_rng(4)
+    widths = [3, 6, 3]
+    P = []
+    for i in range(2):
+        P.append(rng.standard_normal((widths[i + 1], widths[i])) / np.sqrt(widths[i]))
+        P.append(np.zeros(widths[i + 1]))
+    P.append(rng.standard_normal((3, 3)) / np.sqrt(3))
+    P.append(rng.standard_normal(3) * 0.1)
+    params = np.concatenate([p.reshape(-1) for p in P])
+    d = O.make_desc(solver=O.HEUN, controller=O.CONSTANT, field=O.MLP, dim=3, save_t1=1,
+                    mlp_depth=2, mlp_widths=widths, diffusion=O.DIFF_TANH_DIAG,
+                    vbt_t0=0.0, vbt_t1=1.0, vbt_tol=1e-3, seed=99)
+    y0 = rng.standard_normal((2, 3))
+    _fd_check(d, 0.0, 1.0, 0.01, y0, params=params, tol=1e-5)
+
+
+# --- virtual Brownian tree statistics (test/test_brownian.py:117-494) --------
+
+def test_vbt_increment_distribution():
+    d = O.make_desc(dim=4, vbt_t0=0.0, vbt_t1=1.0, vbt_tol=1e-3, seed=7)
+    n = 4000
+    traj = np.arange(n, dtype=np.uint32)
+    ta = np.full(n, 0.23)
+    tb = np.full(n, 0.61)
+    w = O.vbt_increments(d, traj, ta, tb)
+    z = (w / np.sqrt(0.61 - 0.23)).reshape(-1)
+    assert scipy.stats.kstest(z, "norm").pvalue > 1e-3
+    # Chen's relation is exact and disjoint increments are uncorrelated.
+    w1 = O.vbt_increments(d, traj, ta, np.full(n, 0.4))
+    w2 = O.vbt_increments(d, traj, np.full(n, 0.4), tb)
+    assert np.allclose(w1 + w2, w, atol=1e-12)
+    assert abs(np.corrcoef(w1.reshape(-1), w2.reshape(-1))[0, 1]) < 0.05
+
+
+def test_vbt_conditional_bridge():
+    # W(s) given W(0)=0 and W(1) has mean s W(1) and variance s (1 - s).
+    d = O.make_desc(dim=1, vbt_t0=0.0, vbt_t1=1.0, vbt_tol=2 ** -12, seed=3)
+    n = 20000
+    traj = np.arange(n, dtype=np.uint32)
+    w1 = O.vbt_increments(d, traj, np.zeros(n), np.ones(n))[:, 0]
+    s = 0.37
+    ws = O.vbt_increments(d, traj, np.zeros(n), np.full(n, s))[:, 0]
+    resid = (ws - s * w1) / np.sqrt(s * (1 - s))
+    assert scipy.stats.kstest(resid, "norm").pvalue > 1e-3
+    assert abs(np.corrcoef(resid, w1)[0, 1]) < 0.03
