@@ -181,6 +181,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--ref-sample", type=int, default=8192)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", default=None, choices=["fused", "plain"],
+                    help="run warmup + steps eager solves of one kernel only (for ncu)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -250,6 +252,18 @@ def main():
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             ms_step = float(t.item())
         return ms_step, outs, clocks, wall
+
+    if args.profile:
+        low = lowered(args.profile)
+        for _ in range(args.warmup + args.steps):
+            outs = low.run_forward()
+        torch.cuda.synchronize()
+        ok = bool((outs[2] == 0).all().item())
+        print(json.dumps({"profile": args.profile, "solves": args.warmup + args.steps,
+                          "all_successful": ok}))
+        if not ok:
+            sys.exit(1)
+        return
 
     sampler = ClockSampler(local)
     ms_fused, outs, clocks, wall = time_kernel("fused", args.steps, sampler)

@@ -22,6 +22,9 @@ LIB_PATH = os.path.join(OUT_DIR, "libgbdx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr"] + ARCH
+# The FP64-state kernels are the parity mode: no FMA contraction, so their
+# arithmetic rounds like the oracle's (built with -ffp-contract=off).
+PER_FILE_FLAGS = {"gbdx_ode_f64.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -58,7 +61,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src: str) -> str:
         obj = os.path.join(OBJ_DIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [cc] + NVCC_FLAGS + ["-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
+        cmd = [cc] + NVCC_FLAGS + PER_FILE_FLAGS.get(os.path.basename(src), []) + [
+            "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "../../include/gbdx.h"
 
@@ -193,23 +194,43 @@ struct Math<double> {
 __device__ __forceinline__ bool is_nan_(float x) { return isnan(x); }
 __device__ __forceinline__ bool is_nan_(double x) { return isnan(x); }
 
-// nextafter(x, -inf) and nextafter(x, +inf) on the IEEE bit pattern.
-__device__ __forceinline__ double next_down(double x) {
-  if (isnan(x) || x == -INFINITY) return x;
-  if (x == 0.0) return -4.9406564584124654e-324;
+// Order-preserving integer key of a double: key(a) < key(b) <=> a < b for
+// non-NaN values (with -0 one below +0).  Comparisons on keys run on the
+// integer pipes, which matters on GB300 where FP64 issue is ~1/64 of FP32.
+__host__ __device__ __forceinline__ long long order_key(double x) {
+#ifdef __CUDA_ARCH__
   long long b = __double_as_longlong(x);
-  b += (x > 0.0) ? -1 : 1;
-  return __longlong_as_double(b);
+#else
+  long long b;
+  memcpy(&b, &x, sizeof b);
+#endif
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
-__device__ __forceinline__ double next_up(double x) { return -next_down(-x); }
-
-// t1 minus 100 ULP (_integrate.py:319-322): the threshold above which tnext
-// is snapped to t1.
-__device__ __forceinline__ double t1_clip_floor(double t1) {
-  double x = t1;
-#pragma unroll 1
-  for (int i = 0; i < 100; i++) x = next_down(x);
+__host__ __device__ __forceinline__ double from_order_key(long long k) {
+  long long b = k >= 0 ? k : (k ^ 0x7fffffffffffffffLL);
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(b);
+#else
+  double x;
+  memcpy(&x, &b, sizeof x);
   return x;
+#endif
+}
+
+// nextafter(x, +inf) for finite x.
+__device__ __forceinline__ double next_up(double x) {
+  long long k = order_key(x) + 1;
+  if (k == 0) k = 1;  // from -0 the next value up is +denorm_min
+  return from_order_key(k);
+}
+
+// t1 minus 100 ULP (_integrate.py:319-322): 100 applications of
+// nextafter(., -inf), the threshold above which tnext snaps to t1.
+__device__ __forceinline__ double t1_clip_floor(double t1) {
+  long long k = order_key(t1);
+  long long k2 = k - 100;
+  if (k >= 0 && k2 < 0) k2 -= 1;  // the key space holds both +0 and -0
+  return from_order_key(k2);
 }
 
 // ---------------------------------------------------------------------------

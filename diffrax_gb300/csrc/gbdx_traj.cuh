@@ -60,7 +60,13 @@ struct Traj {
   int64_t idx;
 
   __device__ __forceinline__ bool running(const SolveParams &P) const {
-    return tprev < t1 && result == GBDX_SUCCESSFUL && nsteps < P.max_steps;
+    bool before_end;
+    if constexpr (F32) {
+      before_end = order_key(tprev) < order_key(t1);
+    } else {
+      before_end = tprev < t1;
+    }
+    return before_end && result == GBDX_SUCCESSFUL && nsteps < P.max_steps;
   }
 
   __device__ __forceinline__ T *ys_row(const SolveParams &P, int slot) const {
@@ -120,7 +126,8 @@ struct Traj {
   // One loop iteration.
   __device__ void step(const SolveParams &P) {
     const double dt = tnext - tprev;
-    const T h = T(dir * dt);
+    // control = dir * dt (WrapTerm, _term.py:742-745); a sign flip in FP32 mode
+    const T h = F32 ? T(dir > 0 ? dt : -dt) : T(dir * dt);
     T k[S][D];
     T f[D], yi[D], y1[D], err[D], flast[D];
     // Stage 0: FSAL reuse except on the first step (runge_kutta.py:684-700).
@@ -136,11 +143,21 @@ struct Traj {
     for (int i = 1; i < S; i++) {
 #pragma unroll
       for (int n = 0; n < D; n++) {
-        T inc = T(0);
+        if constexpr (F32) {
+          // y0 first, newest stage last: only one FMA waits on k_{i-1}.
+          T acc = y[n];
 #pragma unroll
-        for (int j = 0; j < i; j++)
-          if (TB::a(i, j) != 0.0) inc += T(TB::a(i, j)) * k[j][n];
-        yi[n] = y[n] + inc;
+          for (int j = 0; j < i; j++)
+            if (TB::a(i, j) != 0.0) acc = fmaf(T(TB::a(i, j)), k[j][n], acc);
+          yi[n] = acc;
+        } else {
+          // Reference order: increment first, then y0 (runge_kutta.py:866-871).
+          T inc = T(0);
+#pragma unroll
+          for (int j = 0; j < i; j++)
+            if (TB::a(i, j) != 0.0) inc += T(TB::a(i, j)) * k[j][n];
+          yi[n] = y[n] + inc;
+        }
       }
       FIELD::vf(args, yi, f);
 #pragma unroll
@@ -177,28 +194,36 @@ struct Traj {
       bool any_nan = false;
 #pragma unroll
       for (int n = 0; n < D; n++) any_nan |= is_nan_(y1[n]);
-      T acc = T(0);
-#pragma unroll
-      for (int n = 0; n < D; n++) {
-        T ym = fmax(Math<T>::abs_(y[n]), Math<T>::abs_(any_nan ? y[n] : y1[n]));
-        T s = err[n] / (T(P.atol) + ym * T(P.rtol));
-        acc += s * s;
-      }
       const double prev_dt = dt;
       T factor;
       T hnew;
       if constexpr (F32) {
-        // log2(1/scaled) = 0.5 (log2 D - log2 acc); keep <=> scaled < 1.
-        const T scaled = Math<T>::sqrt_(acc) / Math<T>::sqrt_(T(D));
-        keep = scaled < T(1);
-        T lg = -Math<T>::log2_(scaled);
+        // Sum of squares of err / (atol + rtol max(|y0|, |y1|)); keep <=> RMS < 1
+        // <=> acc < D.  log2(1 / rms) = 0.5 (log2 D - log2 acc), so the factor
+        // safety * inv^c1 * prev^c2 * prev2^c3 is one exp2 of a weighted sum.
+        T acc = T(0);
+#pragma unroll
+        for (int n = 0; n < D; n++) {
+          T ym = fmaxf(fabsf(y[n]), fabsf(any_nan ? y[n] : y1[n]));
+          T s = __fdividef(err[n], fmaf(ym, T(P.rtol), T(P.atol)));
+          acc = fmaf(s, s, acc);
+        }
+        keep = acc < T(D);
+        const T lg = T(0.5) * (Math<T>::log2_(T(D)) - __log2f(acc));
         T ex = T(0);
         if (P.c1 != 0.0) ex += T(P.c1) * lg;
         if (P.c2 != 0.0) ex += T(P.c2) * h1;
         if (P.c3 != 0.0) ex += T(P.c3) * h2;
-        factor = T(P.safety) * Math<T>::exp2_(ex);
-        hnew = isinf(lg) ? T(0) : lg;  // inv in {0, inf} -> 1 (pid.py:538)
+        factor = T(P.safety) * exp2f(ex);
+        hnew = isinf(lg) ? T(0) : lg;  // inv in {0, inf} -> 1 (pid.py:536-538)
       } else {
+        T acc = T(0);
+#pragma unroll
+        for (int n = 0; n < D; n++) {
+          T ym = fmax(Math<T>::abs_(y[n]), Math<T>::abs_(any_nan ? y[n] : y1[n]));
+          T s = err[n] / (T(P.atol) + ym * T(P.rtol));
+          acc += s * s;
+        }
         const T scaled = Math<T>::sqrt_(acc) / Math<T>::sqrt_(T(D));
         keep = scaled < T(1);
         T inv = T(1) / scaled;
@@ -236,9 +261,15 @@ struct Traj {
       nt0 = tnext;
       nt1 = tn;
     }
-    // Book-keeping (_integrate.py:410-413).
-    nt0 = fmin(nt0, t1);
-    if (nt1 > floor1) nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
+    // Book-keeping (_integrate.py:410-413).  tprev and tnext never exceed t1
+    // (tnext starts at min(t0 + dt0, t1) and is clipped below), so the
+    // minimum with t1 is the identity; FP32 mode skips it and compares keys.
+    if constexpr (F32) {
+      if (order_key(nt1) > order_key(floor1)) nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
+    } else {
+      nt0 = fmin(nt0, t1);
+      if (nt1 > floor1) nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
+    }
 
     if (keep) {
       // SaveAt(ts): every ts <= tnext of the step just taken, interpolated
