@@ -21,6 +21,7 @@ from ._core import (
 )
 
 KERNELS = {"auto": 0, "plain": 1, "fused": 2}
+SCHEDULES = {"auto": 0, "index": 1, "longest_first": 2}
 
 
 def _split_terms(terms):
@@ -50,7 +51,7 @@ def _split_terms(terms):
 
 def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype,
           max_steps: int, n_ts: int, adjoint=None, kernel: str = "auto",
-          block_threads: int = 0, ctas_per_sm: int = 0) -> dict:
+          block_threads: int = 0, ctas_per_sm: int = 0, schedule: str = "auto") -> dict:
     """Descriptor fields (gbdx_problem_desc) for one solve."""
     drift, diff, bm = _split_terms(terms)
     if not isinstance(drift, AbstractField):
@@ -63,7 +64,8 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
              rtol=0.0, atol=0.0, pcoeff=0.0, icoeff=1.0, dcoeff=0.0, safety=0.9,
              factormin=0.2, factormax=10.0, dtmin=None, dtmax=None, force_dtmin=1,
              error_order=0.0, mlp_depth=0, mlp_widths=(), diffusion=0, vbt_t0=0.0,
-             vbt_t1=1.0, vbt_tol=1e-3, seed=0, norm=0, adjoint=0, checkpoints=0)
+             vbt_t1=1.0, vbt_tol=1e-3, seed=0, norm=0, adjoint=0, checkpoints=0,
+             schedule=SCHEDULES[schedule])
     if hasattr(drift, "lower_fields"):
         f.update(drift.lower_fields(dim))
     if isinstance(stepsize_controller, PIDController):
@@ -106,7 +108,7 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
 
 def oracle_fields(fields: dict) -> dict:
     """The subset of a lowered descriptor that the FP64 oracle understands."""
-    return {k: v for k, v in fields.items() if k in _lib.ORACLE_FIELDS and k != "pad0"}
+    return {k: v for k, v in fields.items() if k in _lib.ORACLE_FIELDS}
 
 
 def _device():
@@ -157,7 +159,7 @@ class Lowered:
     """A lowered, validated solve ready for the C ABI (reused by autograd)."""
 
     def __init__(self, terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
-                 adjoint, max_steps, kernel, block_threads, ctas_per_sm):
+                 adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule="auto"):
         dev = _device()
         if not isinstance(y0, torch.Tensor):
             y0 = torch.as_tensor(y0)
@@ -178,7 +180,7 @@ class Lowered:
         self.fields = lower(terms, solver, stepsize_controller, saveat, dim=self.dim,
                             dtype=self.dtype, max_steps=max_steps, n_ts=n_ts,
                             adjoint=adjoint, kernel=kernel, block_threads=block_threads,
-                            ctas_per_sm=ctas_per_sm)
+                            ctas_per_sm=ctas_per_sm, schedule=schedule)
         drift = _split_terms(terms)[0]
         self.drift = drift
         self.problem = _lib.get_problem(self.fields)
@@ -243,13 +245,15 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
                 max_steps: Optional[int] = 4096, throw: bool = True,
                 progress_meter: Any = None, solver_state=None, controller_state=None,
                 made_jump=None, kernel: str = "auto", block_threads: int = 0,
-                ctas_per_sm: int = 0) -> Solution:
+                ctas_per_sm: int = 0, schedule: str = "auto") -> Solution:
     """Batched diffrax.diffeqsolve on the GPU (diffrax/_integrate.py:888-1543).
 
     Extra keyword arguments select the GB300 execution policy: ``kernel`` is
     "fused" (persistent work-stealing integrator, the default) or "plain" (one
     trajectory per thread); ``block_threads`` / ``ctas_per_sm`` override the
-    autotuned launch shape of the fused kernel.
+    autotuned launch shape of the fused kernel; ``schedule`` ("auto",
+    "index", "longest_first") sets the order in which the fused kernel takes
+    trajectories (results do not depend on it).
     """
     if event is not None:
         raise NotImplementedError("events are not supported")
@@ -257,7 +261,7 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
         raise NotImplementedError("resuming from solver/controller state is not supported")
     from ._autograd import needs_grad, solve_with_grad
     low = Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
-                  adjoint, max_steps, kernel, block_threads, ctas_per_sm)
+                  adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule)
     if needs_grad(low, y0, args):
         ys, ts_out, res, stats = solve_with_grad(low, y0, args)
     else:

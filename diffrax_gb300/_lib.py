@@ -29,14 +29,15 @@ class ProblemDesc(_c.Structure):
         ("n_ts", i32), ("save_t0", i32), ("save_t1", i32), ("max_steps", i32),
         ("n_args", i32), ("mlp_depth", i32), ("mlp_widths", i32 * 9), ("diffusion", i32),
         ("vbt_t0", f64), ("vbt_t1", f64), ("vbt_tol", f64), ("seed", u64),
-        ("norm", i32), ("pad0", i32),
+        ("norm", i32), ("schedule", i32),
         ("dtype", i32), ("kernel", i32), ("adjoint", i32), ("checkpoints", i32),
         ("block_threads", i32), ("ctas_per_sm", i32),
     ]
 
 
-# The leading block shared with the oracle descriptor.
-ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:30]
+# The leading block shared with the oracle descriptor (the oracle ignores the
+# schedule slot).
+ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:29]
 
 _lock = threading.Lock()
 _LIB = None

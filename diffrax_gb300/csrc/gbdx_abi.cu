@@ -13,6 +13,7 @@
 
 #include "../../include/gbdx.h"
 #include "gbdx_launch.h"
+#include "gbdx_sched.h"
 
 namespace {
 
@@ -143,9 +144,13 @@ int64_t gbdx_param_count(const gbdx_problem *problem) {
 }
 
 size_t gbdx_workspace_size(const gbdx_problem *problem, int64_t batch) {
-  (void)batch;
   if (!problem) return 0;
-  return kQueueBytes;
+  // The work counter, then room for the longest-first order when the fused
+  // kernel may be asked to build one.
+  size_t n = kQueueBytes;
+  if (problem->d.kernel != GBDX_KERNEL_PLAIN && problem->d.schedule != GBDX_SCHED_INDEX)
+    n += gbdx::schedule_workspace_bytes(batch > 0 ? batch : 1);
+  return n;
 }
 
 static int device_sm_count(int *sms) {
@@ -241,6 +246,17 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
     cfg.grid = (int)grid;
     cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return cuda_fail(e, "queue reset");
+    const bool longest_first =
+        d.schedule == GBDX_SCHED_LONGEST_FIRST ||
+        (d.schedule == GBDX_SCHED_AUTO && time_stride == 1);
+    if (longest_first && time_stride == 1) {
+      int32_t *order = nullptr;
+      e = gbdx::build_longest_first_order(t0, t1, batch,
+                                          static_cast<char *>(workspace) + kQueueBytes,
+                                          &order, s);
+      if (e != cudaSuccess) return cuda_fail(e, "work order");
+      P.order = order;
+    }
   }
   cudaError_t e = problem->ode.launch(P, cfg, s);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");

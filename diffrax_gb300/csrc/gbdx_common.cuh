@@ -287,6 +287,7 @@ struct SolveParams {
   double c1, c2, c3;  // PID exponents (i+p+d)/k, -(p+2d)/k, d/k
   int n_ts, save_t0, save_t1, n_save, max_steps;
   unsigned long long *queue;  // work-stealing counter (fused kernel)
+  const int32_t *order;       // optional work order: queue slot -> trajectory
 };
 
 }  // namespace gbdx

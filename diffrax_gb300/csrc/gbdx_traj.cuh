@@ -50,6 +50,7 @@ struct Traj {
   T f0[D];  // FSAL: f(t_n, y_n) from the last stage of the previous step
   T args[NA];
   double tprev, tnext, t1, floor1;
+  double dtc;  // FP32 mode: tnext - tprev carried from the controller (saves a DADD)
   // PID history (pid.py:388-392).  FP32 keeps log2 of the inverse scaled
   // errors so the factor is one exp2 of a weighted sum; FP64 keeps the values.
   T h1, h2;
@@ -107,6 +108,7 @@ struct Traj {
       tn = a + h;
     }
     tnext = fmin(tn, b);
+    dtc = tnext - a;
     tprev = a;
     floor1 = t1_clip_floor(b);
     first = 1;
@@ -125,7 +127,7 @@ struct Traj {
 
   // One loop iteration.
   __device__ void step(const SolveParams &P) {
-    const double dt = tnext - tprev;
+    const double dt = F32 ? dtc : tnext - tprev;
     // control = dir * dt (WrapTerm, _term.py:742-745); a sign flip in FP32 mode
     const T h = F32 ? T(dir > 0 ? dt : -dt) : T(dir * dt);
     T k[S][D];
@@ -187,7 +189,7 @@ struct Traj {
     }
 
     bool keep;
-    double nt0, nt1;
+    double nt0, nt1, dt_next;  // dt_next == nt1 - nt0 (FP32 mode carries it)
     if (P.controller == GBDX_PID) {
       // scaled = rms(err / (atol + rtol max(|y0|, |y1|))), y1 -> y0 if NaN
       // (pid.py:466-492).
@@ -248,6 +250,7 @@ struct Traj {
       }
       nt0 = keep ? tnext : tprev;
       nt1 = nt0 + dtn;
+      dt_next = dtn;
       if (keep) {
         h2 = h1;
         h1 = hnew;
@@ -260,12 +263,17 @@ struct Traj {
       sc = s2;
       nt0 = tnext;
       nt1 = tn;
+      dt_next = F32 ? tn - nt0 : 0.0;
     }
     // Book-keeping (_integrate.py:410-413).  tprev and tnext never exceed t1
     // (tnext starts at min(t0 + dt0, t1) and is clipped below), so the
     // minimum with t1 is the identity; FP32 mode skips it and compares keys.
     if constexpr (F32) {
-      if (order_key(nt1) > order_key(floor1)) nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
+      if (order_key(nt1) > order_key(floor1)) {
+        nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
+        dt_next = nt1 - nt0;
+      }
+      dtc = dt_next;
     } else {
       nt0 = fmin(nt0, t1);
       if (nt1 > floor1) nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
@@ -403,7 +411,7 @@ __global__ void __launch_bounds__(256) fused_kernel(SolveParams P) {
         if (!active) {
           const unsigned long long mine = base + __popc(need & lt_mask);
           if (mine < (unsigned long long)P.batch) {
-            tr.init(P, (int64_t)mine);
+            tr.init(P, P.order ? (int64_t)P.order[mine] : (int64_t)mine);
             active = true;
           }
         }

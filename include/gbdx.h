@@ -54,6 +54,10 @@ enum gbdx_dtype { GBDX_F32 = 0, GBDX_F64 = 1 };
 enum gbdx_kernel { GBDX_KERNEL_AUTO = 0, GBDX_KERNEL_PLAIN = 1, GBDX_KERNEL_FUSED = 2 };
 enum gbdx_adjoint { GBDX_ADJ_NONE = 0, GBDX_ADJ_RECURSIVE = 1, GBDX_ADJ_BACKSOLVE = 2 };
 enum gbdx_norm { GBDX_NORM_RMS = 0, GBDX_NORM_ADJOINT_SEMI = 1 };
+/* Work order of the fused kernels.  AUTO hands out trajectories by decreasing
+ * |t1 - t0| when t0/t1 are per trajectory (time_stride 1), else in index order.
+ * The order never changes results, only how busy the lanes stay. */
+enum gbdx_schedule { GBDX_SCHED_AUTO = 0, GBDX_SCHED_INDEX = 1, GBDX_SCHED_LONGEST_FIRST = 2 };
 
 /* RESULTS codes written per trajectory (diffrax/_solution.py:13-31). */
 enum gbdx_result {
@@ -89,7 +93,7 @@ typedef struct gbdx_problem_desc {
   double vbt_t0, vbt_t1, vbt_tol;
   uint64_t seed;
   int32_t norm;          /* backsolve adjoint norm (gbdx_norm) */
-  int32_t pad0;
+  int32_t schedule;      /* gbdx_schedule: work order of the fused kernels */
   /* GB300 execution policy */
   int32_t dtype;         /* gbdx_dtype of y, args and params */
   int32_t kernel;        /* gbdx_kernel */

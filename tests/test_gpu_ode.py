@@ -147,7 +147,7 @@ def test_constant_step_all_solvers(solver, dtype):
     sol, r = run_both(dfx.OrnsteinUhlenbeck(), SOLVERS[solver], dfx.ConstantStepSize(),
                       dfx.SaveAt(ts=ts, t1=True, t0=True), 0.0, 1.0, 0.01, y0,
                       np.array([1.0, 0.0, 0.0]), dtype, "fused")
-    tol = 1e-12 if dtype == torch.float64 else 2e-6
+    tol = 1e-12 if dtype == torch.float64 else 1e-5
     assert rel_err(sol.ys.cpu().numpy(), r["ys"]) < tol
     assert np.allclose(sol.ys[:, -1].cpu().numpy(), y0 * np.exp(-1), rtol=1e-2, atol=1e-2)
     assert np.array_equal(sol.stats["num_steps"].cpu().numpy(), r["stats"][:, 0])
