@@ -226,7 +226,7 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
 
   gbdx::LaunchCfg cfg;
   cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;
-  cfg.block = d.block_threads > 0 ? d.block_threads : 128;
+  cfg.block = d.block_threads > 0 ? d.block_threads : 64;
   if (cfg.block % 32 != 0 || cfg.block > 256)
     return fail(GBDX_ERR_INVALID, "block_threads must be a multiple of 32 up to 256");
   cfg.grid = 1;
@@ -234,17 +234,24 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
     int sms = 0;
     int rc = device_sm_count(&sms);
     if (rc != GBDX_OK) return rc;
+    int occ = 0;
+    cudaError_t e = problem->ode.occupancy(cfg.block, &occ);
+    if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
+    if (occ < 1) occ = 1;
     int per_sm = d.ctas_per_sm;
     if (per_sm <= 0) {
-      cudaError_t e = problem->ode.occupancy(cfg.block, &per_sm);
-      if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
+      // Keep about B / 2.25 lanes resident: enough warps to feed the FP64 and
+      // FP32 pipes, few enough that every lane refills from the queue a couple
+      // of times (measured on the uneven Van der Pol batch).
+      per_sm = (int)((double)batch / (2.25 * cfg.block * sms) + 0.5);
       if (per_sm < 1) per_sm = 1;
+      if (per_sm > occ) per_sm = occ;
     }
     int64_t grid = (int64_t)sms * per_sm;
     const int64_t needed = (batch + cfg.block - 1) / cfg.block;
     if (grid > needed) grid = needed;
     cfg.grid = (int)grid;
-    cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), s);
+    e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return cuda_fail(e, "queue reset");
     const bool longest_first =
         d.schedule == GBDX_SCHED_LONGEST_FIRST ||
