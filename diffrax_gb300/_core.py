@@ -45,6 +45,77 @@ class OrnsteinUhlenbeck(AbstractField):
     n_args = 3
 
 
+def _flat(tensors, dtype, device):
+    import torch
+    return torch.cat([t.detach().reshape(-1) if not t.requires_grad else t.reshape(-1)
+                      for t in tensors]).to(device=device, dtype=torch.float32).contiguous()
+
+
+class MLPField(AbstractField):
+    """An eqx.nn.MLP vector field f(t, y) = W2 tanh(W1 tanh(W0 y + b0) + b1) + b2
+    (tanh on the hidden layers, identity output; equinox/nn/_mlp.py semantics)
+    given its weights as tensors.  weights[l] is [out, in] as in a Linear layer.
+
+    precision "bf16" runs the products on the tensor cores with BF16 operands
+    and FP32 accumulation; "fp32" runs them in FP32 (parity mode)."""
+    field_id = 3
+    n_args = 0
+
+    def __init__(self, weights, biases, precision: str = "bf16"):
+        if len(weights) != len(biases):
+            raise ValueError("one bias per weight")
+        if precision not in ("bf16", "fp32"):
+            raise ValueError("precision must be 'bf16' or 'fp32'")
+        self.weights = list(weights)
+        self.biases = list(biases)
+        self.precision = precision
+
+    @property
+    def widths(self):
+        return [int(self.weights[0].shape[1])] + [int(w.shape[0]) for w in self.weights]
+
+    def lower_fields(self, dim):
+        w = self.widths
+        if w[0] != dim or w[-1] != dim:
+            raise ValueError(f"MLP maps {w[0]} -> {w[-1]} but the state has dimension {dim}")
+        return dict(mlp_depth=len(self.weights), mlp_widths=tuple(w),
+                    mlp_precision=0 if self.precision == "bf16" else 1)
+
+    def tensors(self):
+        out = []
+        for W, b in zip(self.weights, self.biases):
+            out += [W, b]
+        return out
+
+    def flat_params(self, dtype, device):
+        return _flat(self.tensors(), dtype, device)
+
+    @property
+    def requires_grad(self):
+        return any(getattr(t, "requires_grad", False) for t in self.tensors())
+
+
+class TanhDiagonalDiffusion:
+    """Diagonal diffusion g(y) = scale * tanh(W y + b) of a ControlTerm, with W
+    [dim, dim]: dY_i = f_i dt + g_i(Y) dW_i."""
+    diffusion_id = 2
+
+    def __init__(self, weight, bias, scale: float = 0.1):
+        if float(scale) != 0.1:
+            raise NotImplementedError("the tanh diffusion is compiled with scale 0.1")
+        self.weight, self.bias, self.scale = weight, bias, float(scale)
+
+    def tensors(self):
+        return [self.weight, self.bias]
+
+    def flat_params(self, dtype, device):
+        return _flat(self.tensors(), dtype, device)
+
+    @property
+    def requires_grad(self):
+        return any(getattr(t, "requires_grad", False) for t in self.tensors())
+
+
 # ---------------------------------------------------------------------------
 # Terms (diffrax/_term.py).
 # ---------------------------------------------------------------------------

@@ -65,7 +65,7 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
              factormin=0.2, factormax=10.0, dtmin=None, dtmax=None, force_dtmin=1,
              error_order=0.0, mlp_depth=0, mlp_widths=(), diffusion=0, vbt_t0=0.0,
              vbt_t1=1.0, vbt_tol=1e-3, seed=0, norm=0, adjoint=0, checkpoints=0,
-             schedule=SCHEDULES[schedule])
+             schedule=SCHEDULES[schedule], mlp_precision=0, pad1=0)
     if hasattr(drift, "lower_fields"):
         f.update(drift.lower_fields(dim))
     if isinstance(stepsize_controller, PIDController):
@@ -203,7 +203,17 @@ class Lowered:
         else:
             self.args = None
             self.args_stride = 0
-        self.params = drift.flat_params(self.dtype, dev) if hasattr(drift, "flat_params") else None
+        _, diff_term, _ = _split_terms(terms)
+        self.diffusion = None if diff_term is None else diff_term.vector_field
+        parts = []
+        if hasattr(drift, "flat_params"):
+            parts.append(drift.flat_params(self.dtype, dev))
+        if self.diffusion is not None and hasattr(self.diffusion, "flat_params"):
+            parts.append(self.diffusion.flat_params(self.dtype, dev))
+        self.params = torch.cat(parts).contiguous() if parts else None
+        if self.params is not None and self.params.numel() != self.problem.param_count():
+            raise ValueError(f"expected {self.problem.param_count()} field parameters, "
+                             f"got {self.params.numel()}")
         self.n_save = self.problem.n_save
         self.device = dev
 

@@ -31,7 +31,8 @@ class ProblemDesc(_c.Structure):
         ("vbt_t0", f64), ("vbt_t1", f64), ("vbt_tol", f64), ("seed", u64),
         ("norm", i32), ("schedule", i32),
         ("dtype", i32), ("kernel", i32), ("adjoint", i32), ("checkpoints", i32),
-        ("block_threads", i32), ("ctas_per_sm", i32),
+        ("block_threads", i32), ("ctas_per_sm", i32), ("mlp_precision", i32),
+        ("pad1", i32),
     ]
 
 

@@ -43,6 +43,8 @@ struct gbdx_problem {
   int n_save;
   double c1, c2, c3;  // PID exponents
   gbdx::OdeEntry ode;
+  bool mlp;           // MLP-field row-tile integrator (256 threads per CTA)
+  int rows_per_cta;
 };
 
 extern "C" {
@@ -106,6 +108,8 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   p->c2 = -(d.pcoeff + 2 * d.dcoeff) / order;
   p->c3 = d.dcoeff / order;
   p->ode = gbdx::OdeEntry{nullptr, nullptr};
+  p->mlp = false;
+  p->rows_per_cta = 1;
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
                d.field == GBDX_ORNSTEIN_UHLENBECK)) {
     p->ode = d.dtype == GBDX_F32 ? gbdx::find_ode_entry_f32(d.solver, d.field, d.dim)
@@ -115,6 +119,39 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       return fail(GBDX_ERR_UNSUPPORTED, "no kernel for field %d with state dimension %d",
                   d.field, d.dim);
     }
+  } else if (d.field == GBDX_MLP) {
+    const int *w = d.mlp_widths;
+    if (d.mlp_depth != 3 || w[0] != d.dim || w[3] != d.dim || w[1] != w[2]) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED,
+                  "MLP fields must be dim -> width -> width -> dim (got depth %d)",
+                  d.mlp_depth);
+    }
+    if (d.dtype != GBDX_F32) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED, "MLP fields run with FP32 state");
+    }
+    if (sde && d.diffusion != GBDX_DIFF_TANH_DIAG) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED, "MLP drifts take the tanh diagonal diffusion");
+    }
+    if (d.kernel == GBDX_KERNEL_PLAIN) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED, "MLP fields run on the fused kernel only");
+    }
+    const bool precise = d.mlp_precision == GBDX_MLP_FP32;
+    const int D = d.dim, H = w[1];
+    if (D == 64 && H == 128) p->ode = gbdx::find_mlp_entry_d64h128(d.solver, precise, sde);
+    if (D == 64 && H == 256) p->ode = gbdx::find_mlp_entry_d64h256(d.solver, precise, sde);
+    if (D == 32 && H == 64) p->ode = gbdx::find_mlp_entry_d32h64(d.solver, precise, sde);
+    if (!p->ode.launch) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED,
+                  "no MLP kernel for dim %d, width %d, solver %d%s", D, H, d.solver,
+                  sde ? " (SDE)" : "");
+    }
+    p->mlp = true;
+    p->rows_per_cta = H >= 256 ? 16 : 32;
   } else {
     delete p;
     return fail(GBDX_ERR_UNSUPPORTED, "field %d (diffusion %d) is not available", d.field,
@@ -182,6 +219,7 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                 "pass a value for `dt0`.");
   if (d.n_ts > 0 && !save_ts) return fail(GBDX_ERR_INVALID, "SaveAt(ts=...) without ts");
   if (d.n_args > 0 && !args) return fail(GBDX_ERR_INVALID, "field arguments missing");
+  if (problem->mlp && !params) return fail(GBDX_ERR_INVALID, "MLP parameters missing");
   if (workspace_bytes < gbdx_workspace_size(problem, batch) || !workspace)
     return fail(GBDX_ERR_WORKSPACE, "workspace of %zu bytes is smaller than %zu",
                 workspace_bytes, gbdx_workspace_size(problem, batch));
@@ -223,10 +261,15 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   P.n_save = problem->n_save;
   P.max_steps = d.max_steps;
   P.queue = reinterpret_cast<unsigned long long *>(workspace);
+  P.mlp = static_cast<const float *>(params);
+  P.seed = d.seed;
+  P.vbt_t0 = d.vbt_t0;
+  P.vbt_len = d.vbt_t1 - d.vbt_t0;
+  P.vbt_tol_unit = d.vbt_tol / (d.vbt_t1 - d.vbt_t0);
 
   gbdx::LaunchCfg cfg;
   cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;
-  cfg.block = d.block_threads > 0 ? d.block_threads : 64;
+  cfg.block = problem->mlp ? 256 : (d.block_threads > 0 ? d.block_threads : 64);
   if (cfg.block % 32 != 0 || cfg.block > 256)
     return fail(GBDX_ERR_INVALID, "block_threads must be a multiple of 32 up to 256");
   cfg.grid = 1;
@@ -239,6 +282,7 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
     if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
     if (occ < 1) occ = 1;
     int per_sm = d.ctas_per_sm;
+    if (per_sm <= 0 && problem->mlp) per_sm = occ;
     if (per_sm <= 0) {
       // Keep about B / 2.25 lanes resident: enough warps to feed the FP64 and
       // FP32 pipes, few enough that every lane refills from the queue a couple
@@ -248,7 +292,8 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
       if (per_sm > occ) per_sm = occ;
     }
     int64_t grid = (int64_t)sms * per_sm;
-    const int64_t needed = (batch + cfg.block - 1) / cfg.block;
+    const int rows = problem->mlp ? problem->rows_per_cta : cfg.block;
+    const int64_t needed = (batch + rows - 1) / rows;
     if (grid > needed) grid = needed;
     cfg.grid = (int)grid;
     e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), s);

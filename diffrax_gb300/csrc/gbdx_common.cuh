@@ -288,6 +288,16 @@ struct SolveParams {
   int n_ts, save_t0, save_t1, n_save, max_steps;
   unsigned long long *queue;  // work-stealing counter (fused kernel)
   const int32_t *order;       // optional work order: queue slot -> trajectory
+  // MLP fields and SDEs
+  const float *mlp;           // flat FP32 parameters (W0, b0, W1, b1, W2, b2, Ws, bs)
+  uint64_t seed;              // Brownian generator seed
+  double vbt_t0, vbt_len, vbt_tol_unit;
+  // Recursive-checkpoint tape (forward pass of a differentiated solve)
+  double *tape_t;             // [batch, max_steps + 1] accepted-step time grid
+  float *tape_y;              // [batch, checkpoints, dim] state checkpoints
+  int32_t *tape_n;            // [batch] accepted steps
+  int32_t *tape_stride;       // [batch] accepted steps between checkpoints
+  int checkpoints;
 };
 
 }  // namespace gbdx

@@ -25,5 +25,8 @@ struct OdeEntry {
 
 OdeEntry find_ode_entry_f32(int solver, int field, int dim);
 OdeEntry find_ode_entry_f64(int solver, int field, int dim);
+OdeEntry find_mlp_entry_d64h128(int solver, bool precise, bool sde);
+OdeEntry find_mlp_entry_d64h256(int solver, bool precise, bool sde);
+OdeEntry find_mlp_entry_d32h64(int solver, bool precise, bool sde);
 
 }  // namespace gbdx

@@ -1,0 +1,724 @@
+// gbdx_mlp.cuh -- fused integrator for MLP vector fields (neural ODEs/SDEs).
+//
+// One CTA of 8 warps integrates a tile of M trajectories ("rows") in lockstep;
+// rows finish independently and are refilled from the work counter.  Per RK
+// stage the tile evaluates the field as a chain of tensor-core products,
+//   F = W2 tanh(W1 tanh(W0 Y + b0) + b1) + b2        (eqx.nn.MLP semantics)
+// with the weights resident in shared memory as BF16 and FP32 accumulation.
+// The RK state of every (row, component) -- y, the stage increments k_i, the
+// FSAL vector and the error estimate -- lives in registers in the layout of
+// the last product's accumulator fragments, so all stage arithmetic is
+// register-local.  Per-row scalars (FP64 t and dt, PID history, counters) live
+// in shared memory and are advanced by one thread per row.
+//
+// Semantics follow the analytic-field kernels (gbdx_traj.cuh), which in turn
+// follow diffrax/_integrate.py:302-885 and the files cited there.  The SDE
+// variant is Heun/Euler on MultiTerm(ODETerm(MLP), ControlTerm(diag
+// 0.1 tanh(Ws y + bs), VirtualBrownianTree)) (_term.py:666-731, 271-555,
+// _brownian/tree.py:325-354, 366-448, 607-621, 752-768).
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "gbdx_common.cuh"
+#include "gbdx_mma.cuh"
+#include "gbdx_traj.cuh"
+#include "gbdx_vbt.cuh"
+
+namespace gbdx {
+
+template <int D_, int H_>
+struct MlpShape {
+  static constexpr int D = D_, H = H_;
+  static constexpr int M = (H_ >= 256) ? 16 : 32;  // rows per CTA
+  static constexpr int THREADS = 256, WARPS = 8;
+  static constexpr int PD = D + 8, PH = H + 8;      // padded smem row strides (bf16)
+  static constexpr int MT = M / 16, NT = D / 8, NTH = H / 8;
+  static constexpr int TPW = MT * NT / WARPS;       // output tiles per warp
+  static constexpr int TPWH = MT * NTH / WARPS;     // hidden tiles per warp
+  static constexpr int NE = 4 * TPW;                // owned elements per thread
+  static_assert(MT * NT % WARPS == 0 && TPW >= 1, "tile split");
+  static_assert(MT * NTH % WARPS == 0 && NTH % TPWH == 0, "hidden tile split");
+  static_assert(NT % TPW == 0, "output tile split");
+  // flat parameter offsets (FP32, row-major [out][in])
+  static constexpr int OW0 = 0, OB0 = OW0 + H * D, OW1 = OB0 + H, OB1 = OW1 + H * H,
+                       OW2 = OB1 + H, OB2 = OW2 + D * H, OWS = OB2 + D, OBS = OWS + D * D;
+};
+
+template <int M>
+struct RowState {
+  double tprev[M], tnext[M], t1[M], floor1[M], dtc[M], tp_old[M], tn_old[M], t0s[M], t1s[M];
+  long long idx[M];
+  float h[M], hist1[M], hist2[M], acc[M], theta[M];
+  int active[M], first[M], keep[M], anynan[M], dir[M], save_index[M], ts_index[M];
+  int nsteps[M], nacc[M], nrej[M], result[M], sflag[M], sslot[M], fin[M], nfill[M];
+  int loaded[M], sc[M], nc[M], cpstride[M], cpslot[M], cpcompact[M], at_dtmin[M], live[M];
+};
+
+template <class SH, bool PRECISE, bool SDE>
+struct MlpSmem;
+
+template <class SH, bool SDE>
+struct MlpSmem<SH, false, SDE> {
+  __nv_bfloat16 W0[SH::H][SH::PD];
+  __nv_bfloat16 W1[SH::H][SH::PH];
+  __nv_bfloat16 W2[SH::D][SH::PH];
+  __nv_bfloat16 Ws[SDE ? SH::D : 1][SH::PD];
+  float b0[SH::H], b1[SH::H], b2[SH::D], bs[SH::D];
+  __nv_bfloat16 X[SH::M][SH::PD];
+  __nv_bfloat16 A1[SH::M][SH::PH];
+  __nv_bfloat16 A2[SH::M][SH::PH];
+  RowState<SH::M> rows;
+};
+
+template <class SH, bool SDE>
+struct MlpSmem<SH, true, SDE> {
+  float b0[SH::H], b1[SH::H], b2[SH::D], bs[SH::D];
+  float X[SH::M][SH::D + 1];
+  float A1[SH::M][SH::H + 1];
+  float A2[SH::M][SH::H + 1];
+  RowState<SH::M> rows;
+};
+
+// (row, col) of owned element e of this thread in the output-tile layout.
+template <class SH>
+__device__ __forceinline__ void elem_rc(int e, int warp, int lane, int &row, int &col) {
+  const int j = e >> 2, q = e & 3;
+  const int t = warp * SH::TPW + j;
+  const int mt = t / SH::NT, nt = t % SH::NT;
+  row = mt * 16 + (lane >> 2) + ((q >> 1) << 3);
+  col = nt * 8 + 2 * (lane & 3) + (q & 1);
+}
+
+template <class SH, bool PRECISE, bool SDE>
+struct MlpField {
+  using Sm = MlpSmem<SH, PRECISE, SDE>;
+  static constexpr int D = SH::D, H = SH::H, M = SH::M, NE = SH::NE;
+
+  // Stage the weights (BF16 mode) and biases into shared memory.
+  __device__ static void stage(Sm &sm, const float *P, int tid) {
+    for (int i = tid; i < H; i += SH::THREADS) {
+      sm.b0[i] = P[SH::OB0 + i];
+      sm.b1[i] = P[SH::OB1 + i];
+    }
+    for (int i = tid; i < D; i += SH::THREADS) {
+      sm.b2[i] = P[SH::OB2 + i];
+      if (SDE) sm.bs[i] = P[SH::OBS + i];
+    }
+    if constexpr (!PRECISE) {
+      for (int i = tid; i < H * D; i += SH::THREADS)
+        sm.W0[i / D][i % D] = __float2bfloat16_rn(P[SH::OW0 + i]);
+      for (int i = tid; i < H * H; i += SH::THREADS)
+        sm.W1[i / H][i % H] = __float2bfloat16_rn(P[SH::OW1 + i]);
+      for (int i = tid; i < D * H; i += SH::THREADS)
+        sm.W2[i / H][i % H] = __float2bfloat16_rn(P[SH::OW2 + i]);
+      if (SDE)
+        for (int i = tid; i < D * D; i += SH::THREADS)
+          sm.Ws[i / D][i % D] = __float2bfloat16_rn(P[SH::OWS + i]);
+    }
+  }
+
+  // Write the stage input Y (owned elements) as the first product's operand.
+  __device__ static void put_x(Sm &sm, const float (&Y)[NE], int warp, int lane) {
+#pragma unroll
+    for (int e = 0; e < NE; e += 2) {
+      int row, col;
+      elem_rc<SH>(e, warp, lane, row, col);
+      if constexpr (PRECISE) {
+        sm.X[row][col] = Y[e];
+        sm.X[row][col + 1] = Y[e + 1];
+      } else {
+        *reinterpret_cast<uint32_t *>(&sm.X[row][col]) = pack_bf16x2(Y[e], Y[e + 1]);
+      }
+    }
+  }
+
+  // F = MLP(X) and (SDE) sigma = 0.1 tanh(Ws X + bs), both in the owned layout.
+  // X must have been written and synchronised.  Ends synchronised so that X,
+  // A1 and A2 may be rewritten by the caller after its next barrier.
+  __device__ static void eval(Sm &sm, const float *P, float (&F)[NE], float (&sig)[NE],
+                              int tid, int warp, int lane) {
+    if constexpr (PRECISE) {
+      const float *W0 = P + SH::OW0, *W1 = P + SH::OW1, *W2 = P + SH::OW2, *Ws = P + SH::OWS;
+      for (int i = tid; i < M * H; i += SH::THREADS) {
+        const int r = i / H, n = i % H;
+        float a = sm.b0[n];
+        for (int k = 0; k < D; k++) a = fmaf(sm.X[r][k], __ldg(W0 + n * D + k), a);
+        sm.A1[r][n] = tanhf(a);
+      }
+      if (SDE) {
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          int row, col;
+          elem_rc<SH>(e, warp, lane, row, col);
+          float a = sm.bs[col];
+          for (int k = 0; k < D; k++) a = fmaf(sm.X[row][k], __ldg(Ws + col * D + k), a);
+          sig[e] = 0.1f * tanhf(a);
+        }
+      }
+      __syncthreads();
+      for (int i = tid; i < M * H; i += SH::THREADS) {
+        const int r = i / H, n = i % H;
+        float a = sm.b1[n];
+        for (int k = 0; k < H; k++) a = fmaf(sm.A1[r][k], __ldg(W1 + n * H + k), a);
+        sm.A2[r][n] = tanhf(a);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        float a = sm.b2[col];
+        for (int k = 0; k < H; k++) a = fmaf(sm.A2[row][k], __ldg(W2 + col * H + k), a);
+        F[e] = a;
+      }
+    } else {
+      const int g = lane >> 2, c = lane & 3;
+      {  // layer 0: A1 = tanh(X W0^T + b0)
+        const int t0 = warp * SH::TPWH, mt = t0 / SH::NTH, nt0 = t0 % SH::NTH;
+        float acc[SH::TPWH][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        warp_tile_gemm<D, SH::TPWH>(acc, &sm.X[mt * 16][0], SH::PD, &sm.W0[nt0 * 8][0], SH::PD,
+                                    lane);
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) {
+          const int col = (nt0 + j) * 8 + 2 * c, r0 = mt * 16 + g;
+          const float bb0 = sm.b0[col], bb1 = sm.b0[col + 1];
+          *reinterpret_cast<uint32_t *>(&sm.A1[r0][col]) =
+              pack_bf16x2(tanh_fast(acc[j][0] + bb0), tanh_fast(acc[j][1] + bb1));
+          *reinterpret_cast<uint32_t *>(&sm.A1[r0 + 8][col]) =
+              pack_bf16x2(tanh_fast(acc[j][2] + bb0), tanh_fast(acc[j][3] + bb1));
+        }
+      }
+      if (SDE) {  // diffusion product on the same operand
+        const int t0 = warp * SH::TPW, mt = t0 / SH::NT, nt0 = t0 % SH::NT;
+        float acc[SH::TPW][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        warp_tile_gemm<D, SH::TPW>(acc, &sm.X[mt * 16][0], SH::PD, &sm.Ws[nt0 * 8][0], SH::PD,
+                                   lane);
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          int row, col;
+          elem_rc<SH>(e, warp, lane, row, col);
+          sig[e] = 0.1f * tanh_fast(acc[e >> 2][e & 3] + sm.bs[col]);
+        }
+      }
+      __syncthreads();
+      {  // layer 1: A2 = tanh(A1 W1^T + b1)
+        const int t0 = warp * SH::TPWH, mt = t0 / SH::NTH, nt0 = t0 % SH::NTH;
+        float acc[SH::TPWH][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        warp_tile_gemm<H, SH::TPWH>(acc, &sm.A1[mt * 16][0], SH::PH, &sm.W1[nt0 * 8][0], SH::PH,
+                                    lane);
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) {
+          const int col = (nt0 + j) * 8 + 2 * c, r0 = mt * 16 + g;
+          const float bb0 = sm.b1[col], bb1 = sm.b1[col + 1];
+          *reinterpret_cast<uint32_t *>(&sm.A2[r0][col]) =
+              pack_bf16x2(tanh_fast(acc[j][0] + bb0), tanh_fast(acc[j][1] + bb1));
+          *reinterpret_cast<uint32_t *>(&sm.A2[r0 + 8][col]) =
+              pack_bf16x2(tanh_fast(acc[j][2] + bb0), tanh_fast(acc[j][3] + bb1));
+        }
+      }
+      __syncthreads();
+      {  // layer 2: F = A2 W2^T + b2, straight into the owned layout
+        const int t0 = warp * SH::TPW, mt = t0 / SH::NT, nt0 = t0 % SH::NT;
+        float acc[SH::TPW][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        warp_tile_gemm<H, SH::TPW>(acc, &sm.A2[mt * 16][0], SH::PH, &sm.W2[nt0 * 8][0], SH::PH,
+                                   lane);
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          int row, col;
+          elem_rc<SH>(e, warp, lane, row, col);
+          F[e] = acc[e >> 2][e & 3] + sm.b2[col];
+        }
+      }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Per-row controller (one thread per row).  The FP32-state rules of
+// Traj::step: log-domain PID, integer-key time comparisons, carried dt.
+// ---------------------------------------------------------------------------
+template <int M>
+__device__ __forceinline__ bool row_running(const RowState<M> &R, int r, int max_steps) {
+  return R.active[r] && order_key(R.tprev[r]) < order_key(R.t1[r]) &&
+         R.result[r] == GBDX_SUCCESSFUL && R.nsteps[r] < max_steps;
+}
+
+template <int M>
+__device__ void row_init(RowState<M> &R, int r, int64_t i, const SolveParams &P) {
+  const int64_t ti = i * P.time_stride;
+  double a = P.t0[ti], b = P.t1[ti];
+  const int dir = (a < b) ? 1 : -1;
+  a *= dir;
+  b *= dir;
+  R.idx[r] = i;
+  R.dir[r] = dir;
+  R.t1[r] = b;
+  double tn;
+  if (P.controller == GBDX_PID) {
+    double h = P.dt0 ? P.dt0[ti] * dir : 0.01;
+    if (P.has_dtmax) h = fmin(h, P.dtmax);
+    if (P.has_dtmin) h = fmax(h, P.dtmin);
+    tn = a + h;
+    R.hist1[r] = 0.f;
+    R.hist2[r] = 0.f;
+  } else {
+    const double h = P.dt0[ti] * dir;
+    R.sc[r] = 1;
+    R.nc[r] = (int)ceil((b - a) / next_up(h));
+    R.t0s[r] = a;
+    R.t1s[r] = b;
+    tn = a + h;
+  }
+  R.tnext[r] = fmin(tn, b);
+  R.dtc[r] = R.tnext[r] - a;
+  R.tprev[r] = a;
+  R.floor1[r] = t1_clip_floor(b);
+  R.first[r] = 1;
+  R.save_index[r] = 0;
+  R.ts_index[r] = 0;
+  R.nsteps[r] = R.nacc[r] = R.nrej[r] = 0;
+  R.result[r] = GBDX_SUCCESSFUL;
+  R.active[r] = 1;
+  R.cpstride[r] = 1;
+  R.cpslot[r] = 0;
+  R.cpcompact[r] = 0;
+  R.at_dtmin[r] = 0;
+  R.live[r] = 0;
+  if (P.save_t0) {
+    P.ts_out[i * P.n_save] = a * dir;
+    R.save_index[r] = 1;
+  }
+  if (P.tape_t) P.tape_t[i * (P.max_steps + 1)] = a;
+}
+
+// The controller's decision for row r after the error norm acc = sum of
+// squared scaled errors over the D components (pid.py:466-567,
+// constant.py:59-104, _integrate.py:410-413).
+template <int M>
+__device__ void row_control(RowState<M> &R, int r, int D, const SolveParams &P) {
+  const double dt = R.dtc[r];
+  bool keep;
+  double nt0, nt1, dtn;
+  if (P.controller == GBDX_PID) {
+    const float acc = R.acc[r];
+    keep = acc < float(D);
+    const float lg = 0.5f * (log2f(float(D)) - __log2f(acc));
+    float ex = 0.f;
+    if (P.c1 != 0.0) ex += float(P.c1) * lg;
+    if (P.c2 != 0.0) ex += float(P.c2) * R.hist1[r];
+    if (P.c3 != 0.0) ex += float(P.c3) * R.hist2[r];
+    float factor = float(P.safety) * exp2f(ex);
+    const float hnew = isinf(lg) ? 0.f : lg;
+    if (P.has_dtmin) keep = keep || R.at_dtmin[r];
+    const float fmn = keep ? 1.f : float(P.factormin);
+    const float fmx = keep ? float(P.factormax) : float(P.safety);
+    factor = fminf(fmaxf(factor, fmn), fmx);
+    dtn = dt * double(factor);
+    if (P.has_dtmax) dtn = fmin(dtn, P.dtmax);
+    if (P.has_dtmin) {
+      if (!P.force_dtmin && dtn < P.dtmin && R.result[r] == GBDX_SUCCESSFUL)
+        R.result[r] = GBDX_DT_MIN_REACHED;
+      if (R.at_dtmin[r] && factor == 1.f) dtn = P.dtmin;
+      R.at_dtmin[r] = dtn <= P.dtmin;
+      dtn = fmax(dtn, P.dtmin);
+    }
+    nt0 = keep ? R.tnext[r] : R.tprev[r];
+    nt1 = nt0 + dtn;
+    if (keep) {
+      R.hist2[r] = R.hist1[r];
+      R.hist1[r] = hnew;
+    }
+  } else {
+    keep = true;
+    const int s2 = R.sc[r] + 1;
+    double tn = R.t0s[r] + (R.t1s[r] - R.t0s[r]) * (double(s2) / double(R.nc[r]));
+    if (s2 == R.nc[r]) tn = R.t1s[r];
+    R.sc[r] = s2;
+    nt0 = R.tnext[r];
+    nt1 = tn;
+    dtn = tn - nt0;
+  }
+  if (order_key(nt1) > order_key(R.floor1[r])) {
+    nt1 = keep ? R.t1[r] : nt0 + 0.5 * (R.t1[r] - nt0);
+    dtn = nt1 - nt0;
+  }
+  R.keep[r] = keep;
+  R.tp_old[r] = R.tprev[r];
+  R.tn_old[r] = R.tnext[r];
+  if (keep) {
+    R.nacc[r]++;
+    R.first[r] = 0;
+    if (P.tape_t) P.tape_t[R.idx[r] * (P.max_steps + 1) + R.nacc[r]] = R.tnext[r];
+    // Online thinning of the state checkpoints: every accepted step while the
+    // slots last, then every 2nd, 4th, ... step.
+    if (P.tape_y) {
+      const int n = R.nacc[r];
+      int stride = R.cpstride[r];
+      int compact = 0;
+      int slot = -1;
+      if (n % stride == 0) {
+        slot = n / stride;
+        if (slot >= P.checkpoints) {
+          compact = 1;
+          stride *= 2;
+          slot = n / stride;
+        }
+      }
+      R.cpstride[r] = stride;
+      R.cpslot[r] = slot;
+      R.cpcompact[r] = compact;
+    }
+  } else {
+    R.nrej[r]++;
+    if (P.tape_y) R.cpslot[r] = -1;
+  }
+  R.nsteps[r]++;
+  R.tprev[r] = nt0;
+  R.tnext[r] = nt1;
+  R.dtc[r] = dtn;
+}
+
+// Initial state of freshly loaded rows: y0, a zero FSAL vector, the t0 save,
+// the first state checkpoint and (SDE) the Brownian value at t0.
+template <class SH, bool SDE, int M, int NE>
+__device__ __forceinline__ void load_rows(float (&Y0)[NE], float (&F0)[NE], float (&Wb)[NE],
+                                          const SolveParams &P, const RowState<M> &R, int warp,
+                                          int lane) {
+  constexpr int D = SH::D;
+#pragma unroll
+  for (int e = 0; e < NE; e += 2) {
+    int row, col;
+    elem_rc<SH>(e, warp, lane, row, col);
+    if (R.loaded[row]) {
+      const int64_t i = R.idx[row];
+      const float *y0 = reinterpret_cast<const float *>(P.y0) + i * D + col;
+      Y0[e] = y0[0];
+      Y0[e + 1] = y0[1];
+      F0[e] = F0[e + 1] = 0.f;
+      if (P.save_t0) {
+        float *o = reinterpret_cast<float *>(P.ys_out) + (i * P.n_save) * D + col;
+        o[0] = Y0[e];
+        o[1] = Y0[e + 1];
+      }
+      if (P.tape_y) {
+        float *o = P.tape_y + (i * P.checkpoints) * D + col;
+        o[0] = Y0[e];
+        o[1] = Y0[e + 1];
+      }
+      if (SDE) {
+        const float2 w = vbt_w_pair(P, i, R.tprev[row] * R.dir[row], col);
+        Wb[e] = w.x;
+        Wb[e + 1] = w.y;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The kernel.
+// ---------------------------------------------------------------------------
+template <int SOLVER, int D, int H, bool PRECISE, bool SDE>
+__global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
+  using SH = MlpShape<D, H>;
+  using FLD = MlpField<SH, PRECISE, SDE>;
+  using Sm = typename FLD::Sm;
+  using TB = Tab<SOLVER>;
+  constexpr int S = TB::S, NE = SH::NE, M = SH::M;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Sm &sm = *reinterpret_cast<Sm *>(smem_raw);
+  RowState<M> &R = sm.rows;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float *W = P.mlp;
+
+  FLD::stage(sm, W, tid);
+  if (tid < M) {
+    const unsigned long long q = atomicAdd(P.queue, 1ull);
+    if (q < (unsigned long long)P.batch) {
+      row_init(R, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P);
+      R.loaded[tid] = 1;
+    } else {
+      R.active[tid] = 0;
+      R.loaded[tid] = 0;
+    }
+  }
+  __syncthreads();
+
+  float Y0[NE], F0[NE], Wb[NE];
+#pragma unroll
+  for (int e = 0; e < NE; e++) {
+    int row, col;
+    elem_rc<SH>(e, warp, lane, row, col);
+    Y0[e] = 0.f;
+    F0[e] = 0.f;
+    Wb[e] = 0.f;
+  }
+  load_rows<SH, SDE>(Y0, F0, Wb, P, R, warp, lane);
+  __syncthreads();
+  if (tid < M) R.loaded[tid] = 0;
+
+  float K[S][NE], Yi[NE], F[NE], sig[NE], dW[NE], Wn[NE];
+  while (true) {
+    // ---- one lockstep step -------------------------------------------------
+    int live = 0, first_live = 0;
+    if (tid < M) {
+      live = row_running(R, tid, P.max_steps);
+      first_live = live && R.first[tid];
+      R.live[tid] = live;
+      R.acc[tid] = 0.f;
+      R.anynan[tid] = 0;
+      // control h = dir * dt as FP32 (WrapTerm, _term.py:742-745)
+      R.h[tid] = live ? float(R.dir[tid] > 0 ? R.dtc[tid] : -R.dtc[tid]) : 0.f;
+    }
+    const int any_first = __syncthreads_or(first_live);
+    float hrow[NE];
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      int row, col;
+      elem_rc<SH>(e, warp, lane, row, col);
+      hrow[e] = R.h[row];
+    }
+    if (SDE) {
+      // Brownian increment over [tprev, tnext] of every owned element; W at
+      // tprev is carried from the previous accepted step.
+#pragma unroll
+      for (int e = 0; e < NE; e += 2) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        Wn[e] = Wn[e + 1] = 0.f;
+        dW[e] = dW[e + 1] = 0.f;
+        if (R.live[row]) {
+          const float2 w = vbt_w_pair(P, R.idx[row], R.tnext[row] * R.dir[row], col);
+          Wn[e] = w.x;
+          Wn[e + 1] = w.y;
+          dW[e] = w.x - Wb[e];
+          dW[e + 1] = w.y - Wb[e + 1];
+        }
+      }
+    }
+    // stage 0 (FSAL reuse unless some row is on its first step)
+    if (!TB::FSAL || any_first) {
+      FLD::put_x(sm, Y0, warp, lane);
+      __syncthreads();
+      FLD::eval(sm, W, F, sig, tid, warp, lane);
+    } else {
+#pragma unroll
+      for (int e = 0; e < NE; e++) F[e] = F0[e];
+    }
+#pragma unroll
+    for (int e = 0; e < NE; e++) K[0][e] = SDE ? F[e] * hrow[e] + sig[e] * dW[e] : F[e] * hrow[e];
+#pragma unroll
+    for (int i = 1; i < S; i++) {
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        float a = Y0[e];
+#pragma unroll
+        for (int j = 0; j < i; j++)
+          if (TB::a(i, j) != 0.0) a = fmaf(float(TB::a(i, j)), K[j][e], a);
+        Yi[e] = a;
+      }
+      __syncthreads();  // the previous product has finished reading X
+      FLD::put_x(sm, Yi, warp, lane);
+      __syncthreads();
+      FLD::eval(sm, W, F, sig, tid, warp, lane);
+#pragma unroll
+      for (int e = 0; e < NE; e++)
+        K[i][e] = SDE ? F[e] * hrow[e] + sig[e] * dW[e] : F[e] * hrow[e];
+    }
+    // y1, error estimate, per-row scaled error norm
+    float Y1[NE], Er[NE];
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      if constexpr (TB::SSAL) {
+        Y1[e] = Yi[e];
+      } else {
+        float a = Y0[e];
+#pragma unroll
+        for (int j = 0; j < S; j++) a = fmaf(float(TB::b(j)), K[j][e], a);
+        Y1[e] = a;
+      }
+      float er = 0.f;
+#pragma unroll
+      for (int j = 0; j < S; j++)
+        if (TB::e(j) != 0.0) er = fmaf(float(TB::e(j)), K[j][e], er);
+      Er[e] = isnan(er) ? INFINITY : er;
+    }
+    if (P.controller == GBDX_PID) {
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        if (isnan(Y1[e])) R.anynan[row] = 1;
+      }
+      __syncthreads();
+      // rows of this thread: for each tile two rows (g, g + 8)
+#pragma unroll
+      for (int j = 0; j < SH::TPW; j++) {
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+          int row, col;
+          elem_rc<SH>(j * 4 + half * 2, warp, lane, row, col);
+          const bool nanrow = R.anynan[row];
+          float part = 0.f;
+#pragma unroll
+          for (int q = 0; q < 2; q++) {
+            const int e = j * 4 + half * 2 + q;
+            const float ym = fmaxf(fabsf(Y0[e]), fabsf(nanrow ? Y0[e] : Y1[e]));
+            const float s = __fdividef(Er[e], fmaf(ym, float(P.rtol), float(P.atol)));
+            part = fmaf(s, s, part);
+          }
+          part += __shfl_xor_sync(0xffffffffu, part, 1);
+          part += __shfl_xor_sync(0xffffffffu, part, 2);
+          if ((lane & 3) == 0) atomicAdd(&R.acc[row], part);
+        }
+      }
+    }
+    __syncthreads();
+    if (tid < M && live) row_control(R, tid, D, P);
+    __syncthreads();
+    // ---- SaveAt(ts) inside accepted steps (_integrate.py:456-487) ----------
+    while (true) {
+      int fl = 0;
+      if (tid < M) {
+        R.sflag[tid] = 0;
+        if (live && R.keep[tid] && R.ts_index[tid] < P.n_ts) {
+          const double tsv = __ldg(P.save_ts + R.ts_index[tid]);
+          const double tsd = R.dir[tid] * tsv;
+          if (tsd <= R.tn_old[tid]) {
+            const double tp = R.tp_old[tid], tn = R.tn_old[tid];
+            R.theta[tid] = float(tp == tn ? 0.0 : (tsd - tp) / (tn - tp));
+            R.sslot[tid] = R.save_index[tid];
+            P.ts_out[R.idx[tid] * P.n_save + R.save_index[tid]] = tsv;
+            R.ts_index[tid]++;
+            R.save_index[tid]++;
+            R.sflag[tid] = 1;
+            fl = 1;
+          }
+        }
+      }
+      if (!__syncthreads_or(fl)) break;
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        if (R.sflag[row]) {
+          const float th = R.theta[row];
+          float v;
+          if constexpr (SOLVER == GBDX_TSIT5) {
+            float a = 0.f;
+#pragma unroll
+            for (int j = 0; j < 7; j++) a = fmaf(tsit5_w<float>(j, th), K[j < S ? j : 0][e], a);
+            v = Y0[e] + a;
+          } else if constexpr (SOLVER == GBDX_DOPRI5) {
+            float cm = 0.f;
+#pragma unroll
+            for (int j = 0; j < S; j++)
+              cm = fmaf(float(Tab<GBDX_DOPRI5>::cmid(j < 7 ? j : 0)), K[j][e], cm);
+            const float y0 = Y0[e], y1 = Y1[e], ym = y0 + cm, fa = K[0][e], fb = K[S - 1][e];
+            const float a = 2.f * (fb - fa) - 8.f * (y1 + y0) + 16.f * ym;
+            const float b = 5.f * fa - 3.f * fb + 18.f * y0 + 14.f * y1 - 32.f * ym;
+            const float c = fb - 4.f * fa - 11.f * y0 - 5.f * y1 + 16.f * ym;
+            v = (((a * th + b) * th + c) * th + fa) * th + y0;
+          } else if constexpr (SOLVER == GBDX_HEUN) {
+            const float y0 = Y0[e], y1 = Y1[e], ka = K[0][e], kb = K[S - 1][e];
+            const float a = ka + kb + 2.f * y0 - 2.f * y1;
+            const float b = -2.f * ka - kb - 3.f * y0 + 3.f * y1;
+            v = ((a * th + b) * th + ka) * th + y0;
+          } else {
+            v = Y0[e] + th * (Y1[e] - Y0[e]);
+          }
+          reinterpret_cast<float *>(P.ys_out)[(R.idx[row] * P.n_save + R.sslot[row]) * D + col] =
+              v;
+        }
+      }
+      __syncthreads();
+    }
+    // ---- accept: advance the state, FSAL vector, Brownian cache, tape -------
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      int row, col;
+      elem_rc<SH>(e, warp, lane, row, col);
+      if (R.live[row] && R.keep[row]) {
+        Y0[e] = Y1[e];
+        if (TB::FSAL) F0[e] = F[e];  // field value of the last stage (FSAL)
+        if (SDE) Wb[e] = Wn[e];
+        if (P.tape_y && R.cpslot[row] >= 0) {
+          float *base = P.tape_y + R.idx[row] * P.checkpoints * D + col;
+          if (R.cpcompact[row] & 1)
+            for (int s2 = 1; s2 < P.checkpoints / 2; s2++) base[s2 * D] = base[2 * s2 * D];
+          base[R.cpslot[row] * D] = Y0[e];
+        }
+      }
+    }
+    // ---- finished rows: t1 save, outputs, refill ----------------------------
+    int fin = 0;
+    if (tid < M) {
+      R.fin[tid] = 0;
+      if (R.active[tid] && !row_running(R, tid, P.max_steps)) {
+        const int64_t i = R.idx[tid];
+        const int dir = R.dir[tid];
+        const double t0 = P.t0[i * P.time_stride] * dir;
+        int si = R.save_index[tid];
+        R.nfill[tid] = (t0 == R.t1[tid]) ? P.n_ts : 0;
+        R.sslot[tid] = si;  // first slot written by the element pass
+        for (int m = 0; m < R.nfill[tid]; m++) P.ts_out[i * P.n_save + si + m] = t0 * dir;
+        si += R.nfill[tid];
+        if (P.save_t1) P.ts_out[i * P.n_save + si++] = R.tprev[tid] * dir;
+        for (int m = si; m < P.n_save; m++) P.ts_out[i * P.n_save + m] = INFINITY;
+        int res = R.result[tid];
+        if (res == GBDX_SUCCESSFUL && order_key(R.tprev[tid]) < order_key(R.t1[tid]))
+          res = GBDX_MAX_STEPS_REACHED;
+        P.result_out[i] = res;
+        P.stats_out[i * 3 + 0] = R.nsteps[tid];
+        P.stats_out[i * 3 + 1] = R.nacc[tid];
+        P.stats_out[i * 3 + 2] = R.nrej[tid];
+        if (P.tape_n) {
+          P.tape_n[i] = R.nacc[tid];
+          P.tape_stride[i] = R.cpstride[tid];
+        }
+        R.fin[tid] = 1;
+        fin = 1;
+      }
+    }
+    if (__syncthreads_or(fin)) {
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        if (R.fin[row]) {
+          float *o = reinterpret_cast<float *>(P.ys_out) + R.idx[row] * P.n_save * D + col;
+          int si = R.sslot[row];
+          for (int m = 0; m < R.nfill[row]; m++) o[(si + m) * D] = Y0[e];
+          si += R.nfill[row];
+          if (P.save_t1) o[(si++) * D] = Y0[e];
+          for (int m = si; m < P.n_save; m++) o[m * D] = INFINITY;
+        }
+      }
+      __syncthreads();
+      if (tid < M && R.fin[tid]) {
+        const unsigned long long q = atomicAdd(P.queue, 1ull);
+        if (q < (unsigned long long)P.batch) {
+          row_init(R, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P);
+          R.loaded[tid] = 1;
+        } else {
+          R.active[tid] = 0;
+        }
+      }
+      __syncthreads();
+      load_rows<SH, SDE>(Y0, F0, Wb, P, R, warp, lane);
+      __syncthreads();
+      if (tid < M) R.loaded[tid] = 0;
+    }
+    if (!__syncthreads_or(tid < M && R.active[tid])) break;
+  }
+}
+
+}  // namespace gbdx

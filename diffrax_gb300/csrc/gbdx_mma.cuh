@@ -1,0 +1,101 @@
+// gbdx_mma.cuh -- warp-level BF16 tensor-core tile products for the MLP
+// vector fields (mma.sync.m16n8k16, FP32 accumulate) with ldmatrix operand
+// loads from padded shared memory.
+//
+// Fragment layout of one m16n8 accumulator tile held by a warp (g = lane / 4,
+// c = lane % 4): c[0], c[1] -> (row g, cols 2c, 2c+1); c[2], c[3] ->
+// (row g + 8, cols 2c, 2c+1).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace gbdx {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// A fragment of a 16x16 bf16 tile from row-major smem (row stride `ld` elements).
+__device__ __forceinline__ void ldsm_a(uint32_t (&a)[4], const __nv_bfloat16 *base, int ld,
+                                       int lane) {
+  const __nv_bfloat16 *p = base + (lane & 15) * ld + (lane >> 4) * 8;
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
+               : "r"(smem_u32(p)));
+}
+
+// B fragments of two adjacent n8 tiles (16 x 16 of W, W row-major [n][k]).
+// b[0..1] -> n tile 0, b[2..3] -> n tile 1.
+__device__ __forceinline__ void ldsm_b2(uint32_t (&b)[4], const __nv_bfloat16 *base, int ld,
+                                        int lane) {
+  // lanes 0-7: n 0-7 @ k0; 8-15: n 0-7 @ k0+8; 16-23: n 8-15 @ k0; 24-31: n 8-15 @ k0+8
+  const int n = (lane & 7) + ((lane >> 4) << 3);
+  const int k = ((lane >> 3) & 1) * 8;
+  const __nv_bfloat16 *p = base + n * ld + k;
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3])
+               : "r"(smem_u32(p)));
+}
+
+// B fragment of one n8 tile.
+__device__ __forceinline__ void ldsm_b1(uint32_t (&b)[2], const __nv_bfloat16 *base, int ld,
+                                        int lane) {
+  const int n = lane & 7;
+  const int k = ((lane >> 3) & 1) * 8;
+  const __nv_bfloat16 *p = base + n * ld + k;
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n"
+               : "=r"(b[0]), "=r"(b[1])
+               : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// C[16 mt .. +16, 8 nt .. +8*NTW) += A[16 rows, K] * W[8 nt.., K]^T for NTW
+// adjacent n8 tiles (NTW even uses x4 B loads).
+template <int K, int NTW>
+__device__ __forceinline__ void warp_tile_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *A,
+                                               int lda, const __nv_bfloat16 *W, int ldw,
+                                               int lane) {
+#pragma unroll
+  for (int kk = 0; kk < K / 16; kk++) {
+    uint32_t a[4];
+    ldsm_a(a, A + kk * 16, lda, lane);
+    if constexpr (NTW % 2 == 0) {
+#pragma unroll
+      for (int j = 0; j < NTW; j += 2) {
+        uint32_t b[4];
+        ldsm_b2(b, W + (j * 8) * ldw + kk * 16, ldw, lane);
+        mma_bf16(acc[j], a, b[0], b[1]);
+        mma_bf16(acc[j + 1], a, b[2], b[3]);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NTW; j++) {
+        uint32_t b[2];
+        ldsm_b1(b, W + (j * 8) * ldw + kk * 16, ldw, lane);
+        mma_bf16(acc[j], a, b[0], b[1]);
+      }
+    }
+  }
+}
+
+}  // namespace gbdx

@@ -57,6 +57,9 @@ enum gbdx_norm { GBDX_NORM_RMS = 0, GBDX_NORM_ADJOINT_SEMI = 1 };
 /* Work order of the fused kernels.  AUTO hands out trajectories by decreasing
  * |t1 - t0| when t0/t1 are per trajectory (time_stride 1), else in index order.
  * The order never changes results, only how busy the lanes stay. */
+/* Arithmetic of the MLP field: BF16 operands on the tensor cores with FP32
+ * accumulation (the product path), or FP32 SIMT products (parity mode). */
+enum gbdx_mlp_precision { GBDX_MLP_BF16 = 0, GBDX_MLP_FP32 = 1 };
 enum gbdx_schedule { GBDX_SCHED_AUTO = 0, GBDX_SCHED_INDEX = 1, GBDX_SCHED_LONGEST_FIRST = 2 };
 
 /* RESULTS codes written per trajectory (diffrax/_solution.py:13-31). */
@@ -101,6 +104,8 @@ typedef struct gbdx_problem_desc {
   int32_t checkpoints;   /* RecursiveCheckpointAdjoint(checkpoints=...) slots */
   int32_t block_threads; /* 0 = autotuned */
   int32_t ctas_per_sm;   /* 0 = autotuned */
+  int32_t mlp_precision; /* gbdx_mlp_precision of the MLP field's products */
+  int32_t pad1;
 } gbdx_problem_desc;
 
 typedef struct gbdx_problem gbdx_problem;
