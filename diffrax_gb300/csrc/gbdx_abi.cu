@@ -38,6 +38,12 @@ constexpr size_t kQueueBytes = 256;
 
 }  // namespace
 
+namespace gbdx {
+// Records `msg` as this thread's last error and returns `code` (for the other
+// translation units of the library).
+int set_last_error(int code, const char *msg) { return fail(code, "%s", msg); }
+}  // namespace gbdx
+
 struct gbdx_problem {
   gbdx_problem_desc d;
   int n_save;

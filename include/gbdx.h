@@ -146,6 +146,28 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    double *ts_out, int32_t *result_out, int32_t *stats_out,
                    void *workspace, size_t workspace_bytes, void *stream);
 
+/*
+ * Forward solve for callers that cannot allocate device memory.  It has no
+ * counterpart in the reference.  Callers such as real-time or embedded hosts
+ * that reserve all device memory at start-up, or plugin hosts that only hand
+ * the solver its input and output buffers, cannot allocate the workspace of
+ * gbdx_solve_fwd; this entry point takes the same
+ * arguments without it and runs the same solve, using instead a fixed 4 MiB
+ * scratch array that every GPU loading the library holds until the process
+ * exits.  Batches whose workspace would exceed it (more than 1,047,360
+ * trajectories on the fused kernels) are rejected with GBDX_ERR_WORKSPACE.
+ * The first call on a device looks up the array's device address on that
+ * device; make that first call before any stream capture.  All calls share the
+ * one array (the solve clears what must start at zero), so calls that overlap
+ * on the GPU race: serialise them on one stream.
+ */
+int gbdx_solve_fwd_noalloc(const gbdx_problem *problem, int64_t batch, const double *t0,
+                           const double *t1, const double *dt0, int64_t time_stride,
+                           const void *y0, const void *args, int64_t args_stride,
+                           const void *params, const double *save_ts, void *ys_out,
+                           double *ts_out, int32_t *result_out, int32_t *stats_out,
+                           void *stream);
+
 /* Number of parameters of the MLP / linear field plus diffusion, in the flat
  * layout [W_0 (out x in, row-major), b_0, W_1, b_1, ..., W_sigma, b_sigma]. */
 int64_t gbdx_param_count(const gbdx_problem *problem);
