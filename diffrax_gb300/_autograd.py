@@ -1,19 +1,71 @@
 """torch.autograd bridge: the forward and adjoint kernels behind one
-autograd.Function per adjoint kind."""
+autograd.Function per adjoint kind (diffrax/_adjoint.py)."""
 from __future__ import annotations
 
 import torch
 
+from ._core import BacksolveAdjoint, RecursiveCheckpointAdjoint
 
-def needs_grad(low, y0, args) -> bool:
+
+def _drift_and_diffusion(terms):
+    from ._integrate import _split_terms
+    drift, diff, _ = _split_terms(terms)
+    return drift, (None if diff is None else diff.vector_field)
+
+
+def needs_grad(terms, y0, args) -> bool:
     if not torch.is_grad_enabled():
         return False
     if isinstance(y0, torch.Tensor) and y0.requires_grad:
         return True
     if isinstance(args, torch.Tensor) and args.requires_grad:
         return True
-    return bool(getattr(low.drift, "requires_grad", False))
+    drift, diffusion = _drift_and_diffusion(terms)
+    return bool(getattr(drift, "requires_grad", False) or
+                getattr(diffusion, "requires_grad", False))
+
+
+class _RecursiveCheckpointSolve(torch.autograd.Function):
+    """RecursiveCheckpointAdjoint (diffrax/_adjoint.py:179-312): the forward
+    kernel records the accepted-step grid and state checkpoints in the
+    workspace; the backward kernel returns dL/dy0 and dL/dparams."""
+
+    @staticmethod
+    def forward(ctx, low, y0, params):
+        ys, ts, res, stats, ws = low.run_forward(y0=y0.detach(), params=params.detach(),
+                                                 keep_workspace=True)
+        ctx.low = low
+        ctx.save_for_backward(y0, params)
+        ctx.ws = ws
+        ctx.mark_non_differentiable(ts, res, stats)
+        return ys, ts, res, stats
+
+    @staticmethod
+    def backward(ctx, grad_ys, _gts, _gres, _gstats):
+        y0, params = ctx.saved_tensors
+        low = ctx.low
+        if grad_ys is None:
+            grad_ys = torch.zeros((low.B, low.n_save, low.dim), dtype=low.dtype,
+                                  device=low.device)
+        grad_y0, grad_params = low.run_backward(ctx.ws, grad_ys, y0.detach(), params.detach())
+        ctx.ws = None
+        return (None, grad_y0 if ctx.needs_input_grad[1] else None,
+                grad_params.to(params.dtype) if ctx.needs_input_grad[2] else None)
 
 
 def solve_with_grad(low, y0, args):
-    raise NotImplementedError("gradients for this field are not available")
+    if isinstance(args, torch.Tensor) and args.requires_grad:
+        raise NotImplementedError("gradients with respect to args are not available")
+    if low.params is None:
+        raise NotImplementedError("gradients are available for MLP fields")
+    if isinstance(low.adjoint, RecursiveCheckpointAdjoint):
+        y0_dev = y0 if isinstance(y0, torch.Tensor) else torch.as_tensor(y0)
+        y0_dev = y0_dev.to(device=low.device, dtype=low.dtype)
+        if not y0_dev.is_contiguous():
+            y0_dev = y0_dev.contiguous()
+        if not y0_dev.requires_grad:
+            y0_dev = y0_dev.detach()
+        return _RecursiveCheckpointSolve.apply(low, y0_dev, low.params)
+    if isinstance(low.adjoint, BacksolveAdjoint):
+        raise NotImplementedError("BacksolveAdjoint gradients are not available yet")
+    raise NotImplementedError(f"adjoint {low.adjoint!r} is not supported")

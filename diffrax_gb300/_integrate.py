@@ -159,7 +159,8 @@ class Lowered:
     """A lowered, validated solve ready for the C ABI (reused by autograd)."""
 
     def __init__(self, terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
-                 adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule="auto"):
+                 adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule="auto",
+                 want_grad=False):
         dev = _device()
         if not isinstance(y0, torch.Tensor):
             y0 = torch.as_tensor(y0)
@@ -177,9 +178,12 @@ class Lowered:
             ts = torch.as_tensor(ts, dtype=torch.float64).to(dev).reshape(-1).contiguous()
         self.save_ts = ts
         n_ts = 0 if ts is None else int(ts.numel())
+        # The adjoint shapes the problem only when a gradient will be taken:
+        # a plain forward solve records no tape.
+        self.adjoint = adjoint if want_grad else None
         self.fields = lower(terms, solver, stepsize_controller, saveat, dim=self.dim,
                             dtype=self.dtype, max_steps=max_steps, n_ts=n_ts,
-                            adjoint=adjoint, kernel=kernel, block_threads=block_threads,
+                            adjoint=self.adjoint, kernel=kernel, block_threads=block_threads,
                             ctas_per_sm=ctas_per_sm, schedule=schedule)
         drift = _split_terms(terms)[0]
         self.drift = drift
@@ -217,9 +221,11 @@ class Lowered:
         self.n_save = self.problem.n_save
         self.device = dev
 
-    def run_forward(self, stream=None):
+    def run_forward(self, stream=None, y0=None, params=None, keep_workspace=False):
         dev = self.device
         B, D, n_save = self.B, self.dim, self.n_save
+        y0 = self.y0 if y0 is None else y0
+        params = self.params if params is None else params
         ys = torch.empty((B, n_save, D), dtype=self.dtype, device=dev)
         ts_out = torch.empty((B, n_save), dtype=torch.float64, device=dev)
         res = torch.empty((B,), dtype=torch.int32, device=dev)
@@ -231,10 +237,29 @@ class Lowered:
         p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
         rc = self.problem.lib.gbdx_solve_fwd(
             self.problem.handle, B, p(self.t0), p(self.t1), p(self.dt0), self.tstride,
-            p(self.y0), p(self.args), self.args_stride, p(self.params), p(self.save_ts),
+            p(y0), p(self.args), self.args_stride, p(params), p(self.save_ts),
             p(ys), p(ts_out), p(res), p(stats), p(ws), ws_bytes, stream)
         _lib.check(rc, "gbdx_solve_fwd")
+        if keep_workspace:
+            return ys, ts_out, res, stats, ws
         return ys, ts_out, res, stats
+
+    def run_backward(self, ws, grad_ys, y0, params, stream=None):
+        """dL/dy0 and dL/dparams from the tape the forward left in `ws`."""
+        dev = self.device
+        grad_ys = grad_ys.to(device=dev, dtype=self.dtype).contiguous()
+        grad_y0 = torch.empty((self.B, self.dim), dtype=self.dtype, device=dev)
+        n_params = 0 if params is None else int(params.numel())
+        grad_params = torch.empty((max(n_params, 1),), dtype=torch.float32, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev).cuda_stream
+        p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        rc = self.problem.lib.gbdx_solve_bwd(
+            self.problem.handle, self.B, p(self.t0), p(self.t1), p(self.dt0), self.tstride,
+            p(y0), p(self.args), self.args_stride, p(params), p(self.save_ts), p(grad_ys),
+            p(grad_y0), p(grad_params), p(ws), ws.numel(), stream)
+        _lib.check(rc, "gbdx_solve_bwd")
+        return grad_y0, grad_params[:n_params]
 
 
 def _raise_on_failure(result: torch.Tensor):
@@ -270,9 +295,11 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     if solver_state is not None or controller_state is not None or made_jump is not None:
         raise NotImplementedError("resuming from solver/controller state is not supported")
     from ._autograd import needs_grad, solve_with_grad
+    want_grad = needs_grad(terms, y0, args)
     low = Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
-                  adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule)
-    if needs_grad(low, y0, args):
+                  adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule,
+                  want_grad=want_grad)
+    if want_grad:
         ys, ts_out, res, stats = solve_with_grad(low, y0, args)
     else:
         ys, ts_out, res, stats = low.run_forward()

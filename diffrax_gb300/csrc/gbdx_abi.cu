@@ -49,9 +49,69 @@ struct gbdx_problem {
   int n_save;
   double c1, c2, c3;  // PID exponents
   gbdx::OdeEntry ode;
-  bool mlp;           // MLP-field row-tile integrator (256 threads per CTA)
+  gbdx::BwdEntry bwd;  // RecursiveCheckpointAdjoint backward (MLP fields)
+  bool mlp;            // MLP-field row-tile integrator (256 threads per CTA)
   int rows_per_cta;
 };
+
+namespace {
+
+// Workspace of one solve: the work counter, the work order, and (recursive
+// adjoint) the tape the backward reads plus its scratch.
+struct WsLayout {
+  size_t order, tape_t, tape_y, tape_n, tape_s, scratch, psum, pcomp, total;
+  int seg_max, n_cta;
+};
+
+size_t up256(size_t x) { return (x + 255) / 256 * 256; }
+
+int ws_layout(const gbdx_problem *p, int64_t batch, WsLayout *L) {
+  const gbdx_problem_desc &d = p->d;
+  const size_t B = size_t(batch > 0 ? batch : 1);
+  size_t off = kQueueBytes;
+  L->order = off;
+  if (d.kernel != GBDX_KERNEL_PLAIN && d.schedule != GBDX_SCHED_INDEX)
+    off += up256(gbdx::schedule_workspace_bytes(int64_t(B)));
+  L->tape_t = L->tape_y = L->tape_n = L->tape_s = L->scratch = L->psum = L->pcomp = off;
+  L->seg_max = 0;
+  L->n_cta = 0;
+  if (d.adjoint == GBDX_ADJ_RECURSIVE && p->bwd.launch) {
+    const int C = d.checkpoints > 1 ? d.checkpoints : 2;
+    L->tape_t = off;
+    off += up256(B * size_t(d.max_steps + 1) * sizeof(double));
+    L->tape_y = off;
+    off += up256(B * size_t(C) * d.dim * sizeof(float));
+    L->tape_n = off;
+    off += up256(B * sizeof(int32_t));
+    L->tape_s = off;
+    off += up256(B * sizeof(int32_t));
+    // With C slots the checkpoint stride stays below 2 max_steps / C + 1.
+    int seg = (2 * d.max_steps + C - 1) / C + 1;
+    if (seg > d.max_steps + 1) seg = d.max_steps + 1;
+    L->seg_max = seg;
+    L->scratch = off;
+    off += up256(B * size_t(seg) * d.dim * sizeof(float));
+    int dev = 0, sms = 0, occ = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = p->bwd.occupancy(&occ);
+    if (e != cudaSuccess) return cuda_fail(e, "backward launch shape");
+    if (occ < 1) occ = 1;
+    int64_t grid = int64_t(sms) * occ;
+    const int64_t needed = (int64_t(B) + p->rows_per_cta - 1) / p->rows_per_cta;
+    if (grid > needed) grid = needed;
+    L->n_cta = int(grid);
+    const size_t np = size_t(gbdx_param_count(p));
+    L->psum = off;
+    off += up256(size_t(L->n_cta) * np * sizeof(float));
+    L->pcomp = off;
+    off += up256(size_t(L->n_cta) * np * sizeof(float));
+  }
+  L->total = off;
+  return GBDX_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -114,6 +174,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   p->c2 = -(d.pcoeff + 2 * d.dcoeff) / order;
   p->c3 = d.dcoeff / order;
   p->ode = gbdx::OdeEntry{nullptr, nullptr};
+  p->bwd = gbdx::BwdEntry{nullptr, nullptr};
   p->mlp = false;
   p->rows_per_cta = 1;
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
@@ -158,6 +219,15 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     }
     p->mlp = true;
     p->rows_per_cta = H >= 256 ? 16 : 32;
+    if (d.adjoint == GBDX_ADJ_RECURSIVE) {
+      if (D == 64 && H == 128) p->bwd = gbdx::find_mlp_bwd_entry_d64h128(d.solver, precise, sde);
+      if (D == 64 && H == 256) p->bwd = gbdx::find_mlp_bwd_entry_d64h256(d.solver, precise, sde);
+      if (D == 32 && H == 64) p->bwd = gbdx::find_mlp_bwd_entry_d32h64(d.solver, precise, sde);
+      if (!p->bwd.launch) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED, "no backward kernel for this MLP problem");
+      }
+    }
   } else {
     delete p;
     return fail(GBDX_ERR_UNSUPPORTED, "field %d (diffusion %d) is not available", d.field,
@@ -188,12 +258,9 @@ int64_t gbdx_param_count(const gbdx_problem *problem) {
 
 size_t gbdx_workspace_size(const gbdx_problem *problem, int64_t batch) {
   if (!problem) return 0;
-  // The work counter, then room for the longest-first order when the fused
-  // kernel may be asked to build one.
-  size_t n = kQueueBytes;
-  if (problem->d.kernel != GBDX_KERNEL_PLAIN && problem->d.schedule != GBDX_SCHED_INDEX)
-    n += gbdx::schedule_workspace_bytes(batch > 0 ? batch : 1);
-  return n;
+  WsLayout L;
+  if (ws_layout(problem, batch, &L) != GBDX_OK) return 0;
+  return L.total;
 }
 
 static int device_sm_count(int *sms) {
@@ -205,18 +272,14 @@ static int device_sm_count(int *sms) {
   return GBDX_OK;
 }
 
-int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
-                   const double *t1, const double *dt0, int64_t time_stride,
-                   const void *y0, const void *args, int64_t args_stride,
-                   const void *params, const double *save_ts, void *ys_out,
-                   double *ts_out, int32_t *result_out, int32_t *stats_out,
-                   void *workspace, size_t workspace_bytes, void *stream) {
-  if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
+// Checks shared by the solve entry points and the kernel parameters they share.
+static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
+                   const double *t1, const double *dt0, int64_t time_stride, const void *y0,
+                   const void *args, int64_t args_stride, const void *params,
+                   const double *save_ts, void *workspace, size_t workspace_bytes,
+                   gbdx::SolveParams *out, WsLayout *L) {
   const gbdx_problem_desc &d = problem->d;
-  if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
-  if (batch == 0) return GBDX_OK;
-  if (!t0 || !t1 || !y0 || !ys_out || !ts_out || !result_out || !stats_out)
-    return fail(GBDX_ERR_INVALID, "null input or output pointer");
+  if (!t0 || !t1 || !y0) return fail(GBDX_ERR_INVALID, "null input pointer");
   if (time_stride != 0 && time_stride != 1)
     return fail(GBDX_ERR_INVALID, "time_stride must be 0 or 1");
   if (d.controller == GBDX_CONSTANT && !dt0)
@@ -226,12 +289,12 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   if (d.n_ts > 0 && !save_ts) return fail(GBDX_ERR_INVALID, "SaveAt(ts=...) without ts");
   if (d.n_args > 0 && !args) return fail(GBDX_ERR_INVALID, "field arguments missing");
   if (problem->mlp && !params) return fail(GBDX_ERR_INVALID, "MLP parameters missing");
-  if (workspace_bytes < gbdx_workspace_size(problem, batch) || !workspace)
+  const int rc = ws_layout(problem, batch, L);
+  if (rc != GBDX_OK) return rc;
+  if (workspace_bytes < L->total || !workspace)
     return fail(GBDX_ERR_WORKSPACE, "workspace of %zu bytes is smaller than %zu",
-                workspace_bytes, gbdx_workspace_size(problem, batch));
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-
-  gbdx::SolveParams P;
+                workspace_bytes, L->total);
+  gbdx::SolveParams &P = *out;
   memset(&P, 0, sizeof P);
   P.batch = batch;
   P.t0 = t0;
@@ -243,10 +306,6 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   P.args_stride = args_stride;
   P.params = params;
   P.save_ts = save_ts;
-  P.ys_out = ys_out;
-  P.ts_out = ts_out;
-  P.result_out = result_out;
-  P.stats_out = stats_out;
   P.controller = d.controller;
   P.rtol = d.rtol;
   P.atol = d.atol;
@@ -272,6 +331,59 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   P.vbt_t0 = d.vbt_t0;
   P.vbt_len = d.vbt_t1 - d.vbt_t0;
   P.vbt_tol_unit = d.vbt_tol / (d.vbt_t1 - d.vbt_t0);
+  if (d.adjoint == GBDX_ADJ_RECURSIVE && problem->bwd.launch) {
+    char *w = static_cast<char *>(workspace);
+    P.tape_t = reinterpret_cast<double *>(w + L->tape_t);
+    P.tape_y = reinterpret_cast<float *>(w + L->tape_y);
+    P.tape_n = reinterpret_cast<int32_t *>(w + L->tape_n);
+    P.tape_stride = reinterpret_cast<int32_t *>(w + L->tape_s);
+    P.checkpoints = d.checkpoints > 1 ? d.checkpoints : 2;
+  }
+  return GBDX_OK;
+}
+
+// Reset the work counter and (per-trajectory intervals) build the
+// longest-first order, both on stream s.
+static int start_queue(const gbdx_problem *problem, gbdx::SolveParams &P, void *workspace,
+                       cudaStream_t s) {
+  const gbdx_problem_desc &d = problem->d;
+  cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return cuda_fail(e, "queue reset");
+  const bool longest_first = d.schedule == GBDX_SCHED_LONGEST_FIRST ||
+                             (d.schedule == GBDX_SCHED_AUTO && P.time_stride == 1);
+  if (longest_first && P.time_stride == 1) {
+    int32_t *order = nullptr;
+    e = gbdx::build_longest_first_order(P.t0, P.t1, P.batch,
+                                        static_cast<char *>(workspace) + kQueueBytes, &order,
+                                        s);
+    if (e != cudaSuccess) return cuda_fail(e, "work order");
+    P.order = order;
+  }
+  return GBDX_OK;
+}
+
+int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
+                   const double *t1, const double *dt0, int64_t time_stride,
+                   const void *y0, const void *args, int64_t args_stride,
+                   const void *params, const double *save_ts, void *ys_out,
+                   double *ts_out, int32_t *result_out, int32_t *stats_out,
+                   void *workspace, size_t workspace_bytes, void *stream) {
+  if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
+  const gbdx_problem_desc &d = problem->d;
+  if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
+  if (batch == 0) return GBDX_OK;
+  if (!ys_out || !ts_out || !result_out || !stats_out)
+    return fail(GBDX_ERR_INVALID, "null output pointer");
+  gbdx::SolveParams P;
+  WsLayout L;
+  int rc = prepare(problem, batch, t0, t1, dt0, time_stride, y0, args, args_stride, params,
+                   save_ts, workspace, workspace_bytes, &P, &L);
+  if (rc != GBDX_OK) return rc;
+  P.ys_out = ys_out;
+  P.ts_out = ts_out;
+  P.result_out = result_out;
+  P.stats_out = stats_out;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
 
   gbdx::LaunchCfg cfg;
   cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;
@@ -281,7 +393,7 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   cfg.grid = 1;
   if (cfg.kernel == GBDX_KERNEL_FUSED) {
     int sms = 0;
-    int rc = device_sm_count(&sms);
+    rc = device_sm_count(&sms);
     if (rc != GBDX_OK) return rc;
     int occ = 0;
     cudaError_t e = problem->ode.occupancy(cfg.block, &occ);
@@ -302,22 +414,54 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
     const int64_t needed = (batch + rows - 1) / rows;
     if (grid > needed) grid = needed;
     cfg.grid = (int)grid;
-    e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return cuda_fail(e, "queue reset");
-    const bool longest_first =
-        d.schedule == GBDX_SCHED_LONGEST_FIRST ||
-        (d.schedule == GBDX_SCHED_AUTO && time_stride == 1);
-    if (longest_first && time_stride == 1) {
-      int32_t *order = nullptr;
-      e = gbdx::build_longest_first_order(t0, t1, batch,
-                                          static_cast<char *>(workspace) + kQueueBytes,
-                                          &order, s);
-      if (e != cudaSuccess) return cuda_fail(e, "work order");
-      P.order = order;
-    }
+    rc = start_queue(problem, P, workspace, s);
+    if (rc != GBDX_OK) return rc;
   }
   cudaError_t e = problem->ode.launch(P, cfg, s);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return GBDX_OK;
+}
+
+int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
+                   const double *t1, const double *dt0, int64_t time_stride,
+                   const void *y0, const void *args, int64_t args_stride,
+                   const void *params, const double *save_ts, const void *grad_ys,
+                   void *grad_y0, void *grad_params, void *workspace,
+                   size_t workspace_bytes, void *stream) {
+  if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
+  if (problem->d.adjoint != GBDX_ADJ_RECURSIVE || !problem->bwd.launch)
+    return fail(GBDX_ERR_UNSUPPORTED,
+                "the problem was not created with RecursiveCheckpointAdjoint on an MLP field");
+  if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
+  if (!grad_ys || !grad_y0 || !grad_params)
+    return fail(GBDX_ERR_INVALID, "null gradient pointer");
+  gbdx::SolveParams P;
+  WsLayout L;
+  int rc = prepare(problem, batch, t0, t1, dt0, time_stride, y0, args, args_stride, params,
+                   save_ts, workspace, workspace_bytes, &P, &L);
+  if (rc != GBDX_OK) return rc;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int np = int(gbdx_param_count(problem));
+  char *w = static_cast<char *>(workspace);
+  gbdx::BwdParams Q;
+  Q.grad_ys = static_cast<const float *>(grad_ys);
+  Q.grad_y0 = static_cast<float *>(grad_y0);
+  Q.part_sum = reinterpret_cast<float *>(w + L.psum);
+  Q.part_comp = reinterpret_cast<float *>(w + L.pcomp);
+  Q.scratch = reinterpret_cast<float *>(w + L.scratch);
+  Q.seg_max = L.seg_max;
+  Q.n_params = np;
+  cudaError_t e = cudaMemsetAsync(w + L.psum, 0, L.total - L.psum, s);
+  if (e != cudaSuccess) return cuda_fail(e, "gradient partial reset");
+  if (batch > 0) {
+    rc = start_queue(problem, P, workspace, s);
+    if (rc != GBDX_OK) return rc;
+    e = problem->bwd.launch(P, Q, L.n_cta, s);
+    if (e != cudaSuccess) return cuda_fail(e, "backward launch");
+  }
+  e = gbdx::launch_reduce_partials(Q.part_sum, Q.part_comp, batch > 0 ? L.n_cta : 0, np,
+                                   static_cast<float *>(grad_params), s);
+  if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
   return GBDX_OK;
 }
 

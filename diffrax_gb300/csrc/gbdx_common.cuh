@@ -300,4 +300,15 @@ struct SolveParams {
   int checkpoints;
 };
 
+// Backward (RecursiveCheckpointAdjoint) arguments.
+struct BwdParams {
+  const float *grad_ys;   // [batch, n_save, D]
+  float *grad_y0;         // [batch, D]
+  float *part_sum;        // [n_cta, n_params] per-CTA partial gradients
+  float *part_comp;       // [n_cta, n_params] Kahan compensation
+  float *scratch;         // [batch, seg_max, D] segment recompute states
+  int seg_max;
+  int n_params;
+};
+
 }  // namespace gbdx

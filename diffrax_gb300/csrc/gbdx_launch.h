@@ -25,6 +25,19 @@ struct OdeEntry {
 
 OdeEntry find_ode_entry_f32(int solver, int field, int dim);
 OdeEntry find_ode_entry_f64(int solver, int field, int dim);
+using BwdLaunchFn = cudaError_t (*)(const SolveParams &, const BwdParams &, int grid,
+                                    cudaStream_t);
+using BwdOccFn = cudaError_t (*)(int *ctas_per_sm);
+struct BwdEntry {
+  BwdLaunchFn launch;
+  BwdOccFn occupancy;
+};
+BwdEntry find_mlp_bwd_entry_d64h128(int solver, bool precise, bool sde);
+BwdEntry find_mlp_bwd_entry_d64h256(int solver, bool precise, bool sde);
+BwdEntry find_mlp_bwd_entry_d32h64(int solver, bool precise, bool sde);
+// grad[p] = compensated sum over CTAs of (psum - pcomp)[cta][p]
+cudaError_t launch_reduce_partials(const float *psum, const float *pcomp, int n_cta,
+                                   int n_params, float *out, cudaStream_t s);
 OdeEntry find_mlp_entry_d64h128(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d64h256(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d32h64(int solver, bool precise, bool sde);

@@ -112,7 +112,7 @@ struct MlpField {
         sm.W1[i / H][i % H] = __float2bfloat16_rn(P[SH::OW1 + i]);
       for (int i = tid; i < D * H; i += SH::THREADS)
         sm.W2[i / H][i % H] = __float2bfloat16_rn(P[SH::OW2 + i]);
-      if (SDE)
+      if constexpr (SDE)
         for (int i = tid; i < D * D; i += SH::THREADS)
           sm.Ws[i / D][i % D] = __float2bfloat16_rn(P[SH::OWS + i]);
     }
@@ -146,7 +146,7 @@ struct MlpField {
         for (int k = 0; k < D; k++) a = fmaf(sm.X[r][k], __ldg(W0 + n * D + k), a);
         sm.A1[r][n] = tanhf(a);
       }
-      if (SDE) {
+      if constexpr (SDE) {
 #pragma unroll
         for (int e = 0; e < NE; e++) {
           int row, col;
@@ -191,7 +191,7 @@ struct MlpField {
               pack_bf16x2(tanh_fast(acc[j][2] + bb0), tanh_fast(acc[j][3] + bb1));
         }
       }
-      if (SDE) {  // diffusion product on the same operand
+      if constexpr (SDE) {  // diffusion product on the same operand
         const int t0 = warp * SH::TPW, mt = t0 / SH::NT, nt0 = t0 % SH::NT;
         float acc[SH::TPW][4];
 #pragma unroll

@@ -49,6 +49,41 @@ __device__ __forceinline__ void ldsm_b1(uint32_t (&b)[2], const __nv_bfloat16 *b
                : "r"(smem_u32(p)));
 }
 
+// A fragment of the TRANSPOSE of a row-major smem matrix G [m][o]: the 16x16
+// tile with rows o0..o0+15 and columns (k) m0..m0+15 of G^T.
+__device__ __forceinline__ void ldsm_at(uint32_t (&a)[4], const __nv_bfloat16 *G, int ld,
+                                        int m0, int o0, int lane) {
+  const int m = m0 + (lane & 7) + ((lane >> 4) << 3);
+  const int o = o0 + ((lane >> 3) & 1) * 8;
+  const __nv_bfloat16 *p = G + m * ld + o;
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
+               : "r"(smem_u32(p)));
+}
+
+// B fragments of two adjacent n8 tiles of a K x N operand stored row-major as
+// [k][n] in smem (e.g. a weight W [in][out] read as W^T, or activations
+// [row][feature] as the K = rows operand): k0..k0+15, n0..n0+15.
+__device__ __forceinline__ void ldsm_bt2(uint32_t (&b)[4], const __nv_bfloat16 *S, int ld,
+                                         int k0, int n0, int lane) {
+  const int k = k0 + (lane & 7) + ((lane >> 3) & 1) * 8;
+  const int n = n0 + ((lane >> 4) << 3);
+  const __nv_bfloat16 *p = S + k * ld + n;
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3])
+               : "r"(smem_u32(p)));
+}
+
+// B fragment of one n8 tile of a [k][n] row-major operand.
+__device__ __forceinline__ void ldsm_bt1(uint32_t (&b)[2], const __nv_bfloat16 *S, int ld,
+                                         int k0, int n0, int lane) {
+  const int k = k0 + (lane & 7) + ((lane >> 3) & 1) * 8;
+  const __nv_bfloat16 *p = S + k * ld + n0;
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
+               : "=r"(b[0]), "=r"(b[1])
+               : "r"(smem_u32(p)));
+}
+
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
                                          uint32_t b1) {
   asm volatile(
@@ -92,6 +127,64 @@ __device__ __forceinline__ void warp_tile_gemm(float (&acc)[NTW][4], const __nv_
       for (int j = 0; j < NTW; j++) {
         uint32_t b[2];
         ldsm_b1(b, W + (j * 8) * ldw + kk * 16, ldw, lane);
+        mma_bf16(acc[j], a, b[0], b[1]);
+      }
+    }
+  }
+}
+
+// acc[j] += A[16 rows at a_row0, K] * B[K, 8 (n0 + 8 j)], with A row-major
+// [row][k] and B row-major [k][n] (transposed loads).
+template <int K, int NTW>
+__device__ __forceinline__ void warp_tile_gemm_bt(float (&acc)[NTW][4], const __nv_bfloat16 *A,
+                                                  int lda, const __nv_bfloat16 *B, int ldb,
+                                                  int n0, int lane) {
+#pragma unroll
+  for (int kk = 0; kk < K / 16; kk++) {
+    uint32_t a[4];
+    ldsm_a(a, A + kk * 16, lda, lane);
+    if constexpr (NTW % 2 == 0) {
+#pragma unroll
+      for (int j = 0; j < NTW; j += 2) {
+        uint32_t b[4];
+        ldsm_bt2(b, B, ldb, kk * 16, n0 + j * 8, lane);
+        mma_bf16(acc[j], a, b[0], b[1]);
+        mma_bf16(acc[j + 1], a, b[2], b[3]);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NTW; j++) {
+        uint32_t b[2];
+        ldsm_bt1(b, B, ldb, kk * 16, n0 + j * 8, lane);
+        mma_bf16(acc[j], a, b[0], b[1]);
+      }
+    }
+  }
+}
+
+// acc[j] += G^T[16 outputs at o0, M rows] * S[M rows, 8 (n0 + 8 j)]: weight
+// gradient tiles (K = the M rows of the tile).
+template <int M, int NTW>
+__device__ __forceinline__ void warp_tile_gemm_tt(float (&acc)[NTW][4], const __nv_bfloat16 *G,
+                                                  int ldg, int o0, const __nv_bfloat16 *S,
+                                                  int lds, int n0, int lane) {
+#pragma unroll
+  for (int kk = 0; kk < M / 16; kk++) {
+    uint32_t a[4];
+    ldsm_at(a, G, ldg, kk * 16, o0, lane);
+    if constexpr (NTW % 2 == 0) {
+#pragma unroll
+      for (int j = 0; j < NTW; j += 2) {
+        uint32_t b[4];
+        ldsm_bt2(b, S, lds, kk * 16, n0 + j * 8, lane);
+        mma_bf16(acc[j], a, b[0], b[1]);
+        mma_bf16(acc[j + 1], a, b[2], b[3]);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NTW; j++) {
+        uint32_t b[2];
+        ldsm_bt1(b, S, lds, kk * 16, n0 + j * 8, lane);
         mma_bf16(acc[j], a, b[0], b[1]);
       }
     }

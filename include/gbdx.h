@@ -147,6 +147,24 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    void *workspace, size_t workspace_bytes, void *stream);
 
 /*
+ * Backward of a solve under RecursiveCheckpointAdjoint (MLP fields): the
+ * discretise-then-optimise VJP of the accepted-step map (the controller is
+ * stop-gradient, as in the reference).  Call it after gbdx_solve_fwd on the
+ * same problem, inputs and workspace: the forward recorded its accepted-step
+ * time grid and state checkpoints there.
+ *   grad_ys     : device [batch, n_saves, dim] cotangent of ys (desc.dtype).
+ *   grad_y0     : device [batch, dim] output, dL/dy0.
+ *   grad_params : device [gbdx_param_count] output, dL/dparams summed over the
+ *                 batch with compensated (Kahan) accumulation.
+ */
+int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
+                   const double *t1, const double *dt0, int64_t time_stride,
+                   const void *y0, const void *args, int64_t args_stride,
+                   const void *params, const double *save_ts, const void *grad_ys,
+                   void *grad_y0, void *grad_params, void *workspace,
+                   size_t workspace_bytes, void *stream);
+
+/*
  * Forward solve for callers that cannot allocate device memory.  It has no
  * counterpart in the reference.  Callers such as real-time or embedded hosts
  * that reserve all device memory at start-up, or plugin hosts that only hand
