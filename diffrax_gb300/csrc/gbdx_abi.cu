@@ -337,7 +337,9 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
     P.tape_y = reinterpret_cast<float *>(w + L->tape_y);
     P.tape_n = reinterpret_cast<int32_t *>(w + L->tape_n);
     P.tape_stride = reinterpret_cast<int32_t *>(w + L->tape_s);
-    P.checkpoints = d.checkpoints > 1 ? d.checkpoints : 2;
+    // An even slot count keeps the online thinning exact: when the slots
+    // fill at step n = C s, n is a multiple of the doubled stride 2 s.
+    P.checkpoints = d.checkpoints >= 4 ? (d.checkpoints / 2) * 2 : 2;
   }
   return GBDX_OK;
 }
