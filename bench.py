@@ -171,6 +171,192 @@ def run_reference(args):
     }), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# The other configurations, measured beside the headline workload.
+# ---------------------------------------------------------------------------
+
+def _events_time(fn, steps, warmup, flush):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return statistics.median(ms)
+
+
+def _mlp_np(widths, seed):
+    """eqx.nn.MLP-style weights N(0, 1/fan_in), zero biases, from a seed."""
+    rng = np.random.default_rng(seed)
+    Ws = [(rng.standard_normal((widths[i + 1], widths[i])) / np.sqrt(widths[i]))
+          .astype(np.float32) for i in range(len(widths) - 1)]
+    bs = [np.zeros(widths[i + 1], np.float32) for i in range(len(widths) - 1)]
+    return Ws, bs
+
+
+def _rel_per_traj(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    ax = tuple(range(1, a.ndim))
+    return np.abs(a - b).max(axis=ax) / np.abs(b).max(axis=ax)
+
+
+def _oracle_rate(fn, n, cores):
+    t = time.perf_counter()
+    fn()
+    dt = time.perf_counter() - t
+    return {"value": n / dt, "cores": cores, "kind": "port",
+            "sample": f"{n} trajectories, FP64 oracle, {dt:.2f} s"}
+
+
+def workload_lotka_volterra(dev, flush, steps, warmup):
+    """Lotka-Volterra, Tsit5 + PID(1e-6, 1e-8), batch 1024, 100 ts on [0, 140]."""
+    import torch
+    import diffrax_gb300 as dfx
+    import oracle as O
+    from diffrax_gb300._integrate import Lowered
+    B = 1024
+    rng = np.random.default_rng(11)
+    y0 = rng.uniform(5, 15, (B, 2))
+    ts = np.linspace(0.0, 140.0, 100)
+    args = np.array([0.1, 0.02, 0.4, 0.02])
+    pid = dfx.PIDController(rtol=1e-6, atol=1e-8)
+    out = {"workload": "lotka_volterra_tsit5_pid_b1024_ts100"}
+    ref = O.solve(O.make_desc(solver=O.TSIT5, controller=O.PID, field=O.LOTKA_VOLTERRA,
+                              dim=2, rtol=1e-6, atol=1e-8, n_ts=100, save_t1=0, n_args=4),
+                  0.0, 140.0, 0.1, y0, args=args, ts=ts, nthreads=os.cpu_count() or 1)
+    for dt_name, dtype in (("f32", torch.float32), ("f64", torch.float64)):
+        for kern in ("fused", "plain"):
+            low = Lowered(dfx.ODETerm(dfx.LotkaVolterra()), dfx.Tsit5(), 0.0, 140.0, 0.1,
+                          torch.tensor(y0, dtype=dtype, device=dev),
+                          torch.tensor(args, dtype=dtype, device=dev), dfx.SaveAt(ts=ts), pid,
+                          None, 4096, kern, 0, 0)
+            ms = _events_time(low.run_forward, steps, warmup, flush)
+            ys = low.run_forward()[0].double().cpu().numpy()
+            e = _rel_per_traj(ys, ref["ys"])
+            out[f"{kern}_{dt_name}"] = {"traj_per_s": B / (ms / 1e3), "ms": ms,
+                                        "max_rel_err_vs_fp64_oracle": float(e.max())}
+    out["fused_over_plain_f32"] = out["fused_f32"]["traj_per_s"] / out["plain_f32"]["traj_per_s"]
+    cores = os.cpu_count() or 1
+    out["cpu_baseline"] = _oracle_rate(lambda: O.solve(
+        O.make_desc(solver=O.TSIT5, controller=O.PID, field=O.LOTKA_VOLTERRA, dim=2, rtol=1e-6,
+                    atol=1e-8, n_ts=100, save_t1=0, n_args=4),
+        0.0, 140.0, 0.1, y0, args=args, ts=ts, nthreads=cores), B, cores)
+    return out
+
+
+def workload_neural(dev, flush, steps, warmup, kind):
+    """Neural ODE (64-128-128-64, Tsit5 PID(1e-5, 1e-7), batch 8192, t1 save,
+    RecursiveCheckpointAdjoint(64), loss mean y(t1)^2), the wide neural ODE
+    forward (64-256-256-64, batch 16384, 32 ts) or the neural SDE (drift
+    32-64-64-32, diffusion 0.1 tanh(W y + b), Heun dt 0.01, VBT tol 1e-3,
+    batch 32768, RecursiveCheckpointAdjoint)."""
+    import torch
+    import diffrax_gb300 as dfx
+    import oracle as O
+    from diffrax_gb300._integrate import Lowered
+    cores = os.cpu_count() or 1
+    if kind == "ode":
+        widths, B, seed = [64, 128, 128, 64], 8192, 21
+        solver, ctrl, dt0 = dfx.Tsit5(), dfx.PIDController(rtol=1e-5, atol=1e-7), None
+        saveat, ts, cps, sde = dfx.SaveAt(t1=True), None, 64, False
+        name = "neural_ode_64_128_tsit5_pid_b8192_recursive64"
+    elif kind == "wide":
+        widths, B, seed = [64, 256, 256, 64], 16384, 22
+        solver, ctrl, dt0 = dfx.Tsit5(), dfx.PIDController(rtol=1e-5, atol=1e-7), None
+        ts = np.linspace(0.0, 1.0, 32)
+        saveat, cps, sde = dfx.SaveAt(ts=ts), 64, False
+        name = "neural_ode_64_256_tsit5_pid_b16384_ts32_forward"
+    else:
+        widths, B, seed = [32, 64, 64, 32], 32768, 23
+        solver, ctrl, dt0 = dfx.Heun(), dfx.ConstantStepSize(), 0.01
+        saveat, ts, cps, sde = dfx.SaveAt(t1=True), None, 16, True
+        name = "neural_sde_32_64_heun_dt0.01_vbt1e-3_b32768_recursive16"
+    D = widths[0]
+    Ws, bs = _mlp_np(widths, seed)
+    rng = np.random.default_rng(seed + 1)
+    y0 = rng.standard_normal((B, D)).astype(np.float32)
+    params = [np.concatenate([W.reshape(-1), b]) for W, b in zip(Ws, bs)]
+    tW = [torch.tensor(W, device=dev) for W in Ws]
+    tb = [torch.tensor(b, device=dev) for b in bs]
+    y0_d = torch.tensor(y0, device=dev)
+    out = {"workload": name}
+
+    def terms_for(prec):
+        field = dfx.MLPField(tW, tb, precision=prec)
+        if not sde:
+            return dfx.ODETerm(field)
+        bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (D,), key=seed)
+        return dfx.MultiTerm(dfx.ODETerm(field),
+                             dfx.ControlTerm(dfx.TanhDiagonalDiffusion(tWs, tbs), bm))
+    if sde:
+        Wsig = (rng.standard_normal((D, D)) / np.sqrt(D)).astype(np.float32)
+        bsig = np.zeros(D, np.float32)
+        tWs, tbs = torch.tensor(Wsig, device=dev), torch.tensor(bsig, device=dev)
+        params += [Wsig.reshape(-1), bsig]
+    params = np.concatenate(params).astype(np.float64)
+
+    def lowered(kern, grad, prec="bf16"):
+        return Lowered(terms_for(prec), solver, 0.0, 1.0, dt0, y0_d, None, saveat, ctrl,
+                       dfx.RecursiveCheckpointAdjoint(checkpoints=cps), 4096, kern, 0, 0,
+                       want_grad=grad)
+    fwd = lowered("fused", False)
+    ms_f = _events_time(fwd.run_forward, steps, warmup, flush)
+    ys = fwd.run_forward()[0]
+    out["fused_forward"] = {"traj_per_s": B / (ms_f / 1e3), "ms": ms_f}
+    plain = lowered("plain", False)
+    ms_p = _events_time(plain.run_forward, max(2, steps // 4), 1, flush)
+    out["plain_forward"] = {"traj_per_s": B / (ms_p / 1e3), "ms": ms_p}
+    out["fused_over_plain_forward"] = ms_p / ms_f
+    # accuracy of the BF16 tensor-core forward against the FP64 oracle
+    n_chk = 256
+    fields = dfx.lower(terms_for("bf16"), solver, ctrl, saveat, dim=D, dtype=torch.float32,
+                       max_steps=4096, n_ts=0 if ts is None else len(ts))
+    desc = O.make_desc(**dfx.oracle_fields(fields))
+    ref = O.solve(desc, 0.0, 1.0, dt0, y0[:n_chk].astype(np.float64), params=params, ts=ts,
+                  nthreads=cores)
+    e = _rel_per_traj(ys[:n_chk].double().cpu().numpy(), ref["ys"])
+    out["fused_forward"]["max_rel_err_vs_fp64_oracle"] = float(e.max())
+    out["fused_forward"]["median_rel_err_vs_fp64_oracle"] = float(np.median(e))
+    out["mean_attempted_steps"] = float(fwd.run_forward()[3][:, 0].float().mean().item())
+    out["cpu_baseline_forward"] = _oracle_rate(
+        lambda: O.solve(desc, 0.0, 1.0, dt0, y0[:512].astype(np.float64), params=params, ts=ts,
+                        nthreads=cores), 512, cores)
+    if kind == "wide":
+        return out
+    # forward + RecursiveCheckpointAdjoint backward of loss = mean(y(t1)^2)
+    grad = lowered("fused", True)
+
+    def fwd_bwd():
+        ys_, _, _, _, ws = grad.run_forward(keep_workspace=True)
+        gys = ys_ * (2.0 / ys_.numel())
+        return grad.run_backward(ws, gys, grad.y0, grad.params)
+    ms_g = _events_time(fwd_bwd, steps, warmup, flush)
+    out["fused_forward_adjoint"] = {"grads_per_s": B / (ms_g / 1e3), "ms": ms_g,
+                                    "unit": "trajectory gradients/s"}
+    gy0, gp = fwd_bwd()
+    n_g = 64
+    ys_g = grad.run_forward()[0][:n_g].double().cpu().numpy()
+    gys = 2.0 * ys_g / (B * D)
+    r = O.grad_recursive(desc, 0.0, 1.0, dt0, y0[:n_g].astype(np.float64), gys, params=params,
+                         ts=ts, nthreads=cores)
+    out["fused_forward_adjoint"]["dL_dy0_max_rel_err_vs_fp64_oracle"] = float(
+        np.abs(gy0[:n_g].double().cpu().numpy() - r["grad_y0"]).max()
+        / np.abs(r["grad_y0"]).max())
+    out["cpu_baseline_forward_adjoint"] = _oracle_rate(
+        lambda: O.grad_recursive(desc, 0.0, 1.0, dt0, y0[:n_g].astype(np.float64), gys,
+                                 params=params, ts=ts, nthreads=cores), n_g, cores)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -181,6 +367,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--ref-sample", type=int, default=8192)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the other configurations")
     ap.add_argument("--profile", default=None, choices=["fused", "plain"],
                     help="run warmup + steps eager solves of one kernel only (for ncu)")
     args = ap.parse_args()
@@ -306,6 +494,16 @@ def main():
     h2d = B * (2 * 4 + 4 + 8) + 8
     d2h = B * (2 * 4 + 4)
 
+    others = {}
+    if rank == 0 and not args.headline_only:
+        try:
+            others["lotka_volterra"] = workload_lotka_volterra(dev, flush, 10, 3)
+            others["neural_ode"] = workload_neural(dev, flush, 5, 3, "ode")
+            others["neural_ode_wide"] = workload_neural(dev, flush, 5, 3, "wide")
+            others["neural_sde"] = workload_neural(dev, flush, 5, 3, "sde")
+        except Exception as exc:  # report, never hide the headline line
+            others["error"] = f"{type(exc).__name__}: {exc}"
+
     if rank == 0:
         peaks, src = measured_peaks()
         t_s = ms_fused / 1e3
@@ -373,6 +571,7 @@ def main():
             "all_successful": ok,
             "attempted_steps_per_launch": steps_total,
             "wall_s_timed_region": wall,
+            "other_configs": others,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

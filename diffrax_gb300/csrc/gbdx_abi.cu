@@ -202,12 +202,23 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       delete p;
       return fail(GBDX_ERR_UNSUPPORTED, "MLP drifts take the tanh diagonal diffusion");
     }
-    if (d.kernel == GBDX_KERNEL_PLAIN) {
-      delete p;
-      return fail(GBDX_ERR_UNSUPPORTED, "MLP fields run on the fused kernel only");
-    }
     const bool precise = d.mlp_precision == GBDX_MLP_FP32;
     const int D = d.dim, H = w[1];
+    if (d.kernel == GBDX_KERNEL_PLAIN) {
+      // The plain form: one trajectory per thread, FP32 CUDA-core products.
+      if (d.adjoint == GBDX_ADJ_RECURSIVE) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED, "the plain MLP kernel has no backward");
+      }
+      p->ode = gbdx::find_mlp_plain_entry(d.solver, D, H, sde);
+      if (!p->ode.launch) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED, "no plain kernel for dim %d, width %d, solver %d",
+                    D, H, d.solver);
+      }
+      *out = p;
+      return GBDX_OK;
+    }
     if (D == 64 && H == 128) p->ode = gbdx::find_mlp_entry_d64h128(d.solver, precise, sde);
     if (D == 64 && H == 256) p->ode = gbdx::find_mlp_entry_d64h256(d.solver, precise, sde);
     if (D == 32 && H == 64) p->ode = gbdx::find_mlp_entry_d32h64(d.solver, precise, sde);

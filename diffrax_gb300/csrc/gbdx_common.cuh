@@ -233,14 +233,18 @@ __device__ __forceinline__ double t1_clip_floor(double t1) {
   return from_order_key(k2);
 }
 
+struct SolveParams;
+
 // ---------------------------------------------------------------------------
 // Registered analytic vector fields.  All are autonomous, so stage times are
-// never formed (runge_kutta.py:1023 computes them only to pass to vf).
+// never formed (runge_kutta.py:1023 computes them only to pass to vf).  A
+// field may carry a diagonal diffusion (SDE = true, sigma()).
 // ---------------------------------------------------------------------------
 template <class T>
 struct LotkaVolterra {
   static constexpr int D = 2, NARGS = 4;
-  __device__ static __forceinline__ void vf(const T *a, const T *y, T *o) {
+  static constexpr bool SDE = false;
+  __device__ static __forceinline__ void vf(const SolveParams &, const T *a, const T *y, T *o) {
     o[0] = a[0] * y[0] - a[1] * y[0] * y[1];
     o[1] = -a[2] * y[1] + a[3] * y[0] * y[1];
   }
@@ -249,7 +253,8 @@ struct LotkaVolterra {
 template <class T>
 struct VanDerPol {
   static constexpr int D = 2, NARGS = 1;
-  __device__ static __forceinline__ void vf(const T *a, const T *y, T *o) {
+  static constexpr bool SDE = false;
+  __device__ static __forceinline__ void vf(const SolveParams &, const T *a, const T *y, T *o) {
     o[0] = y[1];
     o[1] = a[0] * (T(1) - y[0] * y[0]) * y[1] - y[0];
   }
@@ -258,7 +263,8 @@ struct VanDerPol {
 template <class T, int D_>
 struct OrnsteinUhlenbeck {
   static constexpr int D = D_, NARGS = 3;
-  __device__ static __forceinline__ void vf(const T *a, const T *y, T *o) {
+  static constexpr bool SDE = false;
+  __device__ static __forceinline__ void vf(const SolveParams &, const T *a, const T *y, T *o) {
 #pragma unroll
     for (int i = 0; i < D; i++) o[i] = a[0] * (a[1] - y[i]);
   }

@@ -38,6 +38,7 @@ BwdEntry find_mlp_bwd_entry_d32h64(int solver, bool precise, bool sde);
 // grad[p] = compensated sum over CTAs of (psum - pcomp)[cta][p]
 cudaError_t launch_reduce_partials(const float *psum, const float *pcomp, int n_cta,
                                    int n_params, float *out, cudaStream_t s);
+OdeEntry find_mlp_plain_entry(int solver, int D, int H, bool sde);
 OdeEntry find_mlp_entry_d64h128(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d64h256(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d32h64(int solver, bool precise, bool sde);

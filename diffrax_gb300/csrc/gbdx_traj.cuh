@@ -10,6 +10,7 @@
 #pragma once
 
 #include "gbdx_common.cuh"
+#include "gbdx_vbt.cuh"
 
 namespace gbdx {
 
@@ -59,6 +60,7 @@ struct Traj {
   double t0s, t1s;
   int first, dir, save_index, ts_index, nsteps, nacc, nrej, result;
   int64_t idx;
+  T wb[FIELD::SDE ? D : 1];  // SDE: W(tprev) of every component (FP32 fields only)
 
   __device__ __forceinline__ bool running(const SolveParams &P) const {
     bool before_end;
@@ -111,6 +113,14 @@ struct Traj {
     dtc = tnext - a;
     tprev = a;
     floor1 = t1_clip_floor(b);
+    if constexpr (FIELD::SDE) {
+#pragma unroll
+      for (int n = 0; n < D; n += 2) {
+        const float2 w = vbt_w_pair(P, i, a * dir, n);
+        wb[n] = w.x;
+        wb[n + 1] = w.y;
+      }
+    }
     first = 1;
     save_index = 0;
     ts_index = 0;
@@ -132,15 +142,33 @@ struct Traj {
     const T h = F32 ? T(dir > 0 ? dt : -dt) : T(dir * dt);
     T k[S][D];
     T f[D], yi[D], y1[D], err[D], flast[D];
+    T dw[FIELD::SDE ? D : 1], wn[FIELD::SDE ? D : 1], sg[FIELD::SDE ? D : 1];
+    if constexpr (FIELD::SDE) {
+      // Brownian increment over [tprev, tnext] (ControlTerm, _term.py:420-427)
+#pragma unroll
+      for (int n = 0; n < D; n += 2) {
+        const float2 w = vbt_w_pair(P, idx, tnext * dir, n);
+        wn[n] = w.x;
+        wn[n + 1] = w.y;
+        dw[n] = w.x - wb[n];
+        dw[n + 1] = w.y - wb[n + 1];
+      }
+    }
     // Stage 0: FSAL reuse except on the first step (runge_kutta.py:684-700).
     if (TB::FSAL && !first) {
 #pragma unroll
       for (int n = 0; n < D; n++) f[n] = f0[n];
     } else {
-      FIELD::vf(args, y, f);
+      FIELD::vf(P, args, y, f);
     }
+    if constexpr (FIELD::SDE) {
+      FIELD::sigma(P, args, y, sg);
 #pragma unroll
-    for (int n = 0; n < D; n++) k[0][n] = f[n] * h;
+      for (int n = 0; n < D; n++) k[0][n] = f[n] * h + sg[n] * dw[n];
+    } else {
+#pragma unroll
+      for (int n = 0; n < D; n++) k[0][n] = f[n] * h;
+    }
 #pragma unroll
     for (int i = 1; i < S; i++) {
 #pragma unroll
@@ -161,9 +189,15 @@ struct Traj {
           yi[n] = y[n] + inc;
         }
       }
-      FIELD::vf(args, yi, f);
+      FIELD::vf(P, args, yi, f);
+      if constexpr (FIELD::SDE) {
+        FIELD::sigma(P, args, yi, sg);
 #pragma unroll
-      for (int n = 0; n < D; n++) k[i][n] = f[n] * h;
+        for (int n = 0; n < D; n++) k[i][n] = f[n] * h + sg[n] * dw[n];
+      } else {
+#pragma unroll
+        for (int n = 0; n < D; n++) k[i][n] = f[n] * h;
+      }
       if (i == S - 1) {
 #pragma unroll
         for (int n = 0; n < D; n++) flast[n] = f[n];
@@ -297,6 +331,10 @@ struct Traj {
       }
 #pragma unroll
       for (int n = 0; n < D; n++) y[n] = y1[n];
+      if constexpr (FIELD::SDE) {
+#pragma unroll
+        for (int n = 0; n < D; n++) wb[n] = wn[n];
+      }
       if (TB::FSAL) {
 #pragma unroll
         for (int n = 0; n < D; n++) f0[n] = flast[n];
