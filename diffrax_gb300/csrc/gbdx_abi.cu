@@ -232,7 +232,8 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     p->rows_per_cta = H >= 256 ? 16 : 32;
     if (d.adjoint == GBDX_ADJ_RECURSIVE) {
       if (D == 64 && H == 128) p->bwd = gbdx::find_mlp_bwd_entry_d64h128(d.solver, precise, sde);
-      if (D == 64 && H == 256) p->bwd = gbdx::find_mlp_bwd_entry_d64h256(d.solver, precise, sde);
+      // (width 256 does not fit the backward's weights and operands in
+      // shared memory; that shape is differentiated by BacksolveAdjoint)
       if (D == 32 && H == 64) p->bwd = gbdx::find_mlp_bwd_entry_d32h64(d.solver, precise, sde);
       if (!p->bwd.launch) {
         delete p;

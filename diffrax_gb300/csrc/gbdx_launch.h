@@ -33,7 +33,6 @@ struct BwdEntry {
   BwdOccFn occupancy;
 };
 BwdEntry find_mlp_bwd_entry_d64h128(int solver, bool precise, bool sde);
-BwdEntry find_mlp_bwd_entry_d64h256(int solver, bool precise, bool sde);
 BwdEntry find_mlp_bwd_entry_d32h64(int solver, bool precise, bool sde);
 // grad[p] = compensated sum over CTAs of (psum - pcomp)[cta][p]
 cudaError_t launch_reduce_partials(const float *psum, const float *pcomp, int n_cta,

@@ -32,11 +32,19 @@ struct MlpShape {
   static constexpr int D = D_, H = H_;
   static constexpr int M = (H_ >= 256) ? 16 : 32;  // rows per CTA
   static constexpr int THREADS = 256, WARPS = 8;
+  // Tight layout at width 256: the layer-1 output overwrites the layer-0
+  // activations (A2 aliases A1) and W0 is unpadded, so BF16 weights plus hi/lo
+  // activations fit the 227 KB of shared memory.
+  static constexpr bool TIGHT = H_ >= 256;
   static constexpr int PD = D + 8, PH = H + 8;      // padded smem row strides (bf16)
+  static constexpr int PW0 = TIGHT ? D : D + 8;     // row stride of W0
   static constexpr int MT = M / 16, NT = D / 8, NTH = H / 8;
   static constexpr int TPW = MT * NT / WARPS;       // output tiles per warp
   static constexpr int TPWH = MT * NTH / WARPS;     // hidden tiles per warp
   static constexpr int NE = 4 * TPW;                // owned elements per thread
+  // Weights are held as BF16 hi/lo pairs when both halves fit in shared
+  // memory (width <= 128); at width 256 only the hi half (the BF16 weights).
+  static constexpr bool WSPLIT = H_ <= 128;
   static_assert(MT * NT % WARPS == 0 && TPW >= 1, "tile split");
   static_assert(MT * NTH % WARPS == 0 && NTH % TPWH == 0, "hidden tile split");
   static_assert(NT % TPW == 0, "output tile split");
@@ -58,17 +66,54 @@ struct RowState {
 template <class SH, bool PRECISE, bool SDE>
 struct MlpSmem;
 
+// lo halves of the weights (present only when they fit)
+template <class SH, bool SDE, bool ON>
+struct WeightLo {
+  __nv_bfloat16 W0l[SH::H][SH::PW0];
+  __nv_bfloat16 W1l[SH::H][SH::PH];
+  __nv_bfloat16 W2l[SH::D][SH::PH];
+  __nv_bfloat16 Wsl[SDE ? SH::D : 1][SH::PD];
+};
 template <class SH, bool SDE>
-struct MlpSmem<SH, false, SDE> {
-  __nv_bfloat16 W0[SH::H][SH::PD];
+struct WeightLo<SH, SDE, false> {};
+
+// A2 storage (aliased onto A1 in the tight layout)
+template <class SH, bool OWN>
+struct Act2 {
+  __nv_bfloat16 A2s[SH::M][SH::PH], A2ls[SH::M][SH::PH];
+};
+template <class SH>
+struct Act2<SH, false> {};
+
+template <class SH, bool SDE>
+struct MlpSmem<SH, false, SDE> : WeightLo<SH, SDE, SH::WSPLIT>, Act2<SH, !SH::TIGHT> {
+  __nv_bfloat16 W0[SH::H][SH::PW0];
   __nv_bfloat16 W1[SH::H][SH::PH];
   __nv_bfloat16 W2[SH::D][SH::PH];
   __nv_bfloat16 Ws[SDE ? SH::D : 1][SH::PD];
   float b0[SH::H], b1[SH::H], b2[SH::D], bs[SH::D];
-  __nv_bfloat16 X[SH::M][SH::PD];
-  __nv_bfloat16 A1[SH::M][SH::PH];
-  __nv_bfloat16 A2[SH::M][SH::PH];
+  // stage input and hidden activations as hi/lo BF16 pairs
+  __nv_bfloat16 X[SH::M][SH::PD], Xl[SH::M][SH::PD];
+  __nv_bfloat16 A1[SH::M][SH::PH], A1l[SH::M][SH::PH];
   RowState<SH::M> rows;
+  __device__ __nv_bfloat16 (*a2())[SH::PH] {
+    if constexpr (SH::TIGHT) return A1; else return this->A2s;
+  }
+  __device__ __nv_bfloat16 (*a2l())[SH::PH] {
+    if constexpr (SH::TIGHT) return A1l; else return this->A2ls;
+  }
+  __device__ const __nv_bfloat16 *w0l(int r) const {
+    if constexpr (SH::WSPLIT) return &this->W0l[r][0]; else return nullptr;
+  }
+  __device__ const __nv_bfloat16 *w1l(int r) const {
+    if constexpr (SH::WSPLIT) return &this->W1l[r][0]; else return nullptr;
+  }
+  __device__ const __nv_bfloat16 *w2l(int r) const {
+    if constexpr (SH::WSPLIT) return &this->W2l[r][0]; else return nullptr;
+  }
+  __device__ const __nv_bfloat16 *wsl(int r) const {
+    if constexpr (SH::WSPLIT && SDE) return &this->Wsl[r][0]; else return nullptr;
+  }
 };
 
 template <class SH, bool SDE>
@@ -106,15 +151,20 @@ struct MlpField {
       if (SDE) sm.bs[i] = P[SH::OBS + i];
     }
     if constexpr (!PRECISE) {
+      constexpr bool WS = SH::WSPLIT;
       for (int i = tid; i < H * D; i += SH::THREADS)
-        sm.W0[i / D][i % D] = __float2bfloat16_rn(P[SH::OW0 + i]);
+        split_store(P[SH::OW0 + i], &sm.W0[i / D][i % D],
+                    WS ? const_cast<__nv_bfloat16 *>(sm.w0l(i / D)) + i % D : nullptr);
       for (int i = tid; i < H * H; i += SH::THREADS)
-        sm.W1[i / H][i % H] = __float2bfloat16_rn(P[SH::OW1 + i]);
+        split_store(P[SH::OW1 + i], &sm.W1[i / H][i % H],
+                    WS ? const_cast<__nv_bfloat16 *>(sm.w1l(i / H)) + i % H : nullptr);
       for (int i = tid; i < D * H; i += SH::THREADS)
-        sm.W2[i / H][i % H] = __float2bfloat16_rn(P[SH::OW2 + i]);
+        split_store(P[SH::OW2 + i], &sm.W2[i / H][i % H],
+                    WS ? const_cast<__nv_bfloat16 *>(sm.w2l(i / H)) + i % H : nullptr);
       if constexpr (SDE)
         for (int i = tid; i < D * D; i += SH::THREADS)
-          sm.Ws[i / D][i % D] = __float2bfloat16_rn(P[SH::OWS + i]);
+          split_store(P[SH::OWS + i], &sm.Ws[i / D][i % D],
+                      WS ? const_cast<__nv_bfloat16 *>(sm.wsl(i / D)) + i % D : nullptr);
     }
   }
 
@@ -128,9 +178,21 @@ struct MlpField {
         sm.X[row][col] = Y[e];
         sm.X[row][col + 1] = Y[e + 1];
       } else {
-        *reinterpret_cast<uint32_t *>(&sm.X[row][col]) = pack_bf16x2(Y[e], Y[e + 1]);
+        store_split2(Y[e], Y[e + 1], &sm.X[row][col], &sm.Xl[row][col]);
       }
     }
+  }
+
+  // acc += (Ah + Al)[rows, K] (Wh + Wl)[n, K]^T without the lo*lo term: three
+  // BF16 tensor-core products (two when the weights are not split).
+  template <int K, int NTW>
+  __device__ static __forceinline__ void split_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *Ah,
+                                                    const __nv_bfloat16 *Al, int lda,
+                                                    const __nv_bfloat16 *Wh,
+                                                    const __nv_bfloat16 *Wl, int ldw, int lane) {
+    warp_tile_gemm<K, NTW>(acc, Ah, lda, Wh, ldw, lane);
+    warp_tile_gemm<K, NTW>(acc, Al, lda, Wh, ldw, lane);
+    if constexpr (SH::WSPLIT) warp_tile_gemm<K, NTW>(acc, Ah, lda, Wl, ldw, lane);
   }
 
   // F = MLP(X) and (SDE) sigma = 0.1 tanh(Ws X + bs), both in the owned layout.
@@ -179,16 +241,16 @@ struct MlpField {
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        warp_tile_gemm<D, SH::TPWH>(acc, &sm.X[mt * 16][0], SH::PD, &sm.W0[nt0 * 8][0], SH::PD,
-                                    lane);
+        split_gemm<D, SH::TPWH>(acc, &sm.X[mt * 16][0], &sm.Xl[mt * 16][0], SH::PD,
+                                &sm.W0[nt0 * 8][0], sm.w0l(nt0 * 8), SH::PW0, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
           const int col = (nt0 + j) * 8 + 2 * c, r0 = mt * 16 + g;
           const float bb0 = sm.b0[col], bb1 = sm.b0[col + 1];
-          *reinterpret_cast<uint32_t *>(&sm.A1[r0][col]) =
-              pack_bf16x2(tanh_fast(acc[j][0] + bb0), tanh_fast(acc[j][1] + bb1));
-          *reinterpret_cast<uint32_t *>(&sm.A1[r0 + 8][col]) =
-              pack_bf16x2(tanh_fast(acc[j][2] + bb0), tanh_fast(acc[j][3] + bb1));
+          store_split2(tanhf(acc[j][0] + bb0), tanhf(acc[j][1] + bb1), &sm.A1[r0][col],
+                       &sm.A1l[r0][col]);
+          store_split2(tanhf(acc[j][2] + bb0), tanhf(acc[j][3] + bb1), &sm.A1[r0 + 8][col],
+                       &sm.A1l[r0 + 8][col]);
         }
       }
       if constexpr (SDE) {  // diffusion product on the same operand
@@ -196,13 +258,13 @@ struct MlpField {
         float acc[SH::TPW][4];
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        warp_tile_gemm<D, SH::TPW>(acc, &sm.X[mt * 16][0], SH::PD, &sm.Ws[nt0 * 8][0], SH::PD,
-                                   lane);
+        split_gemm<D, SH::TPW>(acc, &sm.X[mt * 16][0], &sm.Xl[mt * 16][0], SH::PD,
+                               &sm.Ws[nt0 * 8][0], sm.wsl(nt0 * 8), SH::PD, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) {
           int row, col;
           elem_rc<SH>(e, warp, lane, row, col);
-          sig[e] = 0.1f * tanh_fast(acc[e >> 2][e & 3] + sm.bs[col]);
+          sig[e] = 0.1f * tanhf(acc[e >> 2][e & 3] + sm.bs[col]);
         }
       }
       __syncthreads();
@@ -211,16 +273,19 @@ struct MlpField {
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        warp_tile_gemm<H, SH::TPWH>(acc, &sm.A1[mt * 16][0], SH::PH, &sm.W1[nt0 * 8][0], SH::PH,
-                                    lane);
+        split_gemm<H, SH::TPWH>(acc, &sm.A1[mt * 16][0], &sm.A1l[mt * 16][0], SH::PH,
+                                &sm.W1[nt0 * 8][0], sm.w1l(nt0 * 8), SH::PH, lane);
+        if constexpr (SH::TIGHT) __syncthreads();  // every warp has read A1
+        auto A2 = sm.a2();
+        auto A2l = sm.a2l();
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
           const int col = (nt0 + j) * 8 + 2 * c, r0 = mt * 16 + g;
           const float bb0 = sm.b1[col], bb1 = sm.b1[col + 1];
-          *reinterpret_cast<uint32_t *>(&sm.A2[r0][col]) =
-              pack_bf16x2(tanh_fast(acc[j][0] + bb0), tanh_fast(acc[j][1] + bb1));
-          *reinterpret_cast<uint32_t *>(&sm.A2[r0 + 8][col]) =
-              pack_bf16x2(tanh_fast(acc[j][2] + bb0), tanh_fast(acc[j][3] + bb1));
+          store_split2(tanhf(acc[j][0] + bb0), tanhf(acc[j][1] + bb1), &A2[r0][col],
+                       &A2l[r0][col]);
+          store_split2(tanhf(acc[j][2] + bb0), tanhf(acc[j][3] + bb1), &A2[r0 + 8][col],
+                       &A2l[r0 + 8][col]);
         }
       }
       __syncthreads();
@@ -229,8 +294,8 @@ struct MlpField {
         float acc[SH::TPW][4];
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        warp_tile_gemm<H, SH::TPW>(acc, &sm.A2[mt * 16][0], SH::PH, &sm.W2[nt0 * 8][0], SH::PH,
-                                   lane);
+        split_gemm<H, SH::TPW>(acc, &sm.a2()[mt * 16][0], &sm.a2l()[mt * 16][0], SH::PH,
+                               &sm.W2[nt0 * 8][0], sm.w2l(nt0 * 8), SH::PH, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) {
           int row, col;

@@ -102,8 +102,9 @@ struct BwdSmem<SH, true, SDE> {
 // BF16 products, accumulated into this CTA's Kahan partials.
 template <class SH, int O, int N>
 __device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *G, int ldg,
-                                         const __nv_bfloat16 *S, int lds, int off,
-                                         float *psum, float *pcomp, int warp, int lane) {
+                                         const __nv_bfloat16 *S, const __nv_bfloat16 *Sl,
+                                         int lds, int off, float *psum, float *pcomp, int warp,
+                                         int lane) {
   constexpr int TILES = (O / 16) * (N / 8);
   static_assert(TILES % SH::WARPS == 0, "weight-gradient tile split");
   constexpr int T = TILES / SH::WARPS;
@@ -118,6 +119,7 @@ __device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *G, int ldg,
 #pragma unroll
     for (int j = 0; j < CH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
     warp_tile_gemm_tt<SH::M, CH>(acc, G, ldg, ot * 16, S, lds, nt0 * 8, lane);
+    warp_tile_gemm_tt<SH::M, CH>(acc, G, ldg, ot * 16, Sl, lds, nt0 * 8, lane);
 #pragma unroll
     for (int j = 0; j < CH; j++)
 #pragma unroll
@@ -231,13 +233,18 @@ struct MlpVjp {
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         warp_tile_gemm_bt<D, SH::TPWH>(acc, &sm.G3[mt * 16][0], SH::PD, &sm.f.W2[0][0],
                                        SH::PH, nt0 * 8, lane);
+        if constexpr (SH::WSPLIT)
+          warp_tile_gemm_bt<D, SH::TPWH>(acc, &sm.G3[mt * 16][0], SH::PD, sm.f.w2l(0),
+                                         SH::PH, nt0 * 8, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
           for (int hr = 0; hr < 2; hr++) {
             const int row = mt * 16 + g + hr * 8, col = (nt0 + j) * 8 + 2 * c;
-            const float a0 = __bfloat162float(sm.f.A2[row][col]);
-            const float a1 = __bfloat162float(sm.f.A2[row][col + 1]);
+            const float a0 = __bfloat162float(sm.f.a2()[row][col]) +
+                             __bfloat162float(sm.f.a2l()[row][col]);
+            const float a1 = __bfloat162float(sm.f.a2()[row][col + 1]) +
+                             __bfloat162float(sm.f.a2l()[row][col + 1]);
             const float v0 = acc[j][2 * hr] * (1.f - a0 * a0);
             const float v1 = acc[j][2 * hr + 1] * (1.f - a1 * a1);
             *reinterpret_cast<uint32_t *>(&sm.G2[row][col]) = pack_bf16x2(v0, v1);
@@ -245,8 +252,8 @@ struct MlpVjp {
             if (v1 != 0.f) atomicAdd(&sm.db1[col + 1], v1);
           }
       }
-      dw_tiles<SH, D, H>(&sm.G3[0][0], SH::PD, &sm.f.A2[0][0], SH::PH, SH::OW2, psum, pcomp,
-                         warp, lane);
+      dw_tiles<SH, D, H>(&sm.G3[0][0], SH::PD, &sm.f.a2()[0][0], &sm.f.a2l()[0][0], SH::PH,
+                         SH::OW2, psum, pcomp, warp, lane);
       __syncthreads();
       {  // 3. G1 = (G2 W1) * (1 - A1^2)
         const int t0 = warp * SH::TPWH, mt = t0 / SH::NTH, nt0 = t0 % SH::NTH;
@@ -255,13 +262,18 @@ struct MlpVjp {
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         warp_tile_gemm_bt<H, SH::TPWH>(acc, &sm.G2[mt * 16][0], SH::PH, &sm.f.W1[0][0],
                                        SH::PH, nt0 * 8, lane);
+        if constexpr (SH::WSPLIT)
+          warp_tile_gemm_bt<H, SH::TPWH>(acc, &sm.G2[mt * 16][0], SH::PH, sm.f.w1l(0),
+                                         SH::PH, nt0 * 8, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
           for (int hr = 0; hr < 2; hr++) {
             const int row = mt * 16 + g + hr * 8, col = (nt0 + j) * 8 + 2 * c;
-            const float a0 = __bfloat162float(sm.f.A1[row][col]);
-            const float a1 = __bfloat162float(sm.f.A1[row][col + 1]);
+            const float a0 = __bfloat162float(sm.f.A1[row][col]) +
+                             __bfloat162float(sm.f.A1l[row][col]);
+            const float a1 = __bfloat162float(sm.f.A1[row][col + 1]) +
+                             __bfloat162float(sm.f.A1l[row][col + 1]);
             const float v0 = acc[j][2 * hr] * (1.f - a0 * a0);
             const float v1 = acc[j][2 * hr + 1] * (1.f - a1 * a1);
             *reinterpret_cast<uint32_t *>(&sm.G1[row][col]) = pack_bf16x2(v0, v1);
@@ -269,27 +281,34 @@ struct MlpVjp {
             if (v1 != 0.f) atomicAdd(&sm.db0[col + 1], v1);
           }
       }
-      dw_tiles<SH, H, H>(&sm.G2[0][0], SH::PH, &sm.f.A1[0][0], SH::PH, SH::OW1, psum, pcomp,
-                         warp, lane);
+      dw_tiles<SH, H, H>(&sm.G2[0][0], SH::PH, &sm.f.A1[0][0], &sm.f.A1l[0][0], SH::PH,
+                         SH::OW1, psum, pcomp, warp, lane);
       __syncthreads();
       {  // 4. gY = G1 W0 (+ Gs Ws), owned layout
         const int t0 = warp * SH::TPW, mt = t0 / SH::NT, nt0 = t0 % SH::NT;
         float acc[SH::TPW][4];
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        warp_tile_gemm_bt<H, SH::TPW>(acc, &sm.G1[mt * 16][0], SH::PH, &sm.f.W0[0][0], SH::PD,
+        warp_tile_gemm_bt<H, SH::TPW>(acc, &sm.G1[mt * 16][0], SH::PH, &sm.f.W0[0][0], SH::PW0,
                                       nt0 * 8, lane);
-        if constexpr (SDE)
+        if constexpr (SH::WSPLIT)
+          warp_tile_gemm_bt<H, SH::TPW>(acc, &sm.G1[mt * 16][0], SH::PH, sm.f.w0l(0),
+                                        SH::PW0, nt0 * 8, lane);
+        if constexpr (SDE) {
           warp_tile_gemm_bt<D, SH::TPW>(acc, &sm.Gs[mt * 16][0], SH::PD, &sm.f.Ws[0][0],
                                         SH::PD, nt0 * 8, lane);
+          if constexpr (SH::WSPLIT)
+            warp_tile_gemm_bt<D, SH::TPW>(acc, &sm.Gs[mt * 16][0], SH::PD, sm.f.wsl(0),
+                                          SH::PD, nt0 * 8, lane);
+        }
 #pragma unroll
         for (int e = 0; e < NE; e++) gY[e] = acc[e >> 2][e & 3];
       }
-      dw_tiles<SH, H, D>(&sm.G1[0][0], SH::PH, &sm.f.X[0][0], SH::PD, SH::OW0, psum, pcomp,
-                         warp, lane);
+      dw_tiles<SH, H, D>(&sm.G1[0][0], SH::PH, &sm.f.X[0][0], &sm.f.Xl[0][0], SH::PD, SH::OW0,
+                         psum, pcomp, warp, lane);
       if constexpr (SDE)
-        dw_tiles<SH, D, D>(&sm.Gs[0][0], SH::PD, &sm.f.X[0][0], SH::PD, SH::OWS, psum, pcomp,
-                           warp, lane);
+        dw_tiles<SH, D, D>(&sm.Gs[0][0], SH::PD, &sm.f.X[0][0], &sm.f.Xl[0][0], SH::PD,
+                           SH::OWS, psum, pcomp, warp, lane);
     }
   }
 };

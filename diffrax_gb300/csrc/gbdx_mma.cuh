@@ -98,6 +98,23 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   return *reinterpret_cast<uint32_t *>(&v);
 }
 
+// x ~ hi + lo with hi = bf16(x), lo = bf16(x - hi): about 16 significant bits.
+__device__ __forceinline__ void split_store(float x, __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(x);
+  *hi = h;
+  if (lo) *lo = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
+// Two adjacent values as hi/lo BF16x2 words.
+__device__ __forceinline__ void store_split2(float x0, float x1, __nv_bfloat16 *hi,
+                                             __nv_bfloat16 *lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+  *reinterpret_cast<__nv_bfloat162 *>(hi) = h;
+  *reinterpret_cast<__nv_bfloat162 *>(lo) = l;
+}
+
 __device__ __forceinline__ float tanh_fast(float x) {
   float y;
   asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
