@@ -57,7 +57,10 @@ class MLPField(AbstractField):
     given its weights as tensors.  weights[l] is [out, in] as in a Linear layer.
 
     precision "bf16" runs the products on the tensor cores with BF16 operands
-    and FP32 accumulation; "fp32" runs them in FP32 (parity mode)."""
+    and FP32 accumulation.  Operands are split into hi/lo BF16 pairs (three
+    products per tile, ~16 significant bits) so the field stays smooth under
+    adaptive stepping; at width 256 the weights are held as single BF16 values.
+    "fp32" runs the products in FP32 on the CUDA cores (parity mode)."""
     field_id = 3
     n_args = 0
 

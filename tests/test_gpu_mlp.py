@@ -151,8 +151,10 @@ def test_mlp_uneven_t1_row_refill():
 
 @pytest.mark.parametrize("widths", [[64, 128, 128, 64], [64, 256, 256, 64], [32, 64, 64, 32]])
 def test_mlp_bf16_error_level(widths):
-    # BF16 operands on the tensor cores: the error against the FP64 oracle is
-    # the BF16 rounding of weights and activations (~2^-9 relative per product).
+    # BF16 tensor-core products on hi/lo operand pairs: up to width 128 the
+    # weights and activations carry ~16 significant bits and the solve matches
+    # the FP64 oracle to FP32-state accuracy; at width 256 the weights are the
+    # BF16 weights (2^-9 relative), a smooth model difference.
     rng = np.random.default_rng(14)
     y0 = rng.standard_normal((256, widths[0]))
     sol, r = run_mlp(widths, dfx.Tsit5(), dfx.PIDController(rtol=1e-5, atol=1e-7),
@@ -161,7 +163,13 @@ def test_mlp_bf16_error_level(widths):
     err = per_traj_err(sol, r)
     print(f"MLP {widths} bf16: rel err vs FP64 oracle median {np.median(err):.2e} "
           f"max {err.max():.2e}")
-    assert np.median(err) < 1e-2 and err.max() < 5e-2
+    if widths[1] <= 128:
+        assert err.max() < 1e-4
+    else:
+        assert np.median(err) < 1e-2 and err.max() < 5e-2
+    # a smooth field keeps the PID step count at the FP64 controller's level
+    steps = sol.stats["num_steps"].cpu().numpy()
+    assert steps.mean() < 1.6 * r["stats"][:, 0].mean()
 
 
 def sde_setup(seed):
@@ -195,4 +203,4 @@ def test_neural_sde_bf16_error_level():
                      diffusion=sde_setup(18), bm=bm)
     err = per_traj_err(sol, r)
     print(f"neural SDE bf16: median rel err {np.median(err):.2e} max {err.max():.2e}")
-    assert np.median(err) < 1e-2 and err.max() < 5e-2
+    assert err.max() < 1e-4
