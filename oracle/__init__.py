@@ -30,6 +30,7 @@ EULER, HEUN, DOPRI5, TSIT5 = 0, 1, 2, 3
 CONSTANT, PID = 0, 1
 LOTKA_VOLTERRA, VAN_DER_POL, ORNSTEIN_UHLENBECK, MLP, LINEAR, CALLBACK = 0, 1, 2, 3, 4, 5
 DIFF_NONE, DIFF_OU, DIFF_TANH_DIAG = 0, 1, 2
+NORM_RMS, NORM_ADJOINT_SEMI = 0, 1
 RESULT_NAMES = {0: "successful", 1: "max_steps_reached", 2: "dt_min_reached",
                 3: "event_occurred", 4: "max_steps_rejected", 5: "internal_error"}
 
@@ -107,6 +108,9 @@ def load():
                                        dp, dp, i64, dp, i64, dp, dp, dp, dp, ip, ip, dp,
                                        dp, dp, ctypes.c_int]
     lib.orc_grad_recursive.restype = ctypes.c_int
+    lib.orc_backsolve.argtypes = [ctypes.POINTER(OracleDesc), i64, dp, dp, dp, i64, dp, dp,
+                                  dp, dp, i64, dp, i64, dp, dp, dp, ip, ip, ctypes.c_int]
+    lib.orc_backsolve.restype = ctypes.c_int
     lib.orc_vbt_increments.argtypes = [ctypes.POINTER(OracleDesc), i64,
                                        ctypes.POINTER(ctypes.c_uint32), dp, dp, dp]
     lib.orc_normal4.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
@@ -231,6 +235,40 @@ def grad_recursive(desc: OracleDesc, t0, t1, dt0, y0, grad_ys, args=None, params
         raise ValueError(f"oracle rejected the problem (code {rc})")
     return dict(ys=ys, ts=ts_out, result=res, stats=stats, grad_y0=gy0,
                 grad_args=gargs[:, :desc.n_args], grad_params=gp[:n_params])
+
+
+def backsolve(desc: OracleDesc, t0, t1, dt0, ts_saved, ys, grad_ys, args=None,
+              params=None, nthreads: int = 1):
+    """BacksolveAdjoint backward from the forward's saved (ts, ys) and their
+    cotangent.  `desc` describes the backward solve (solver, controller, norm)
+    and the forward's SaveAt.  Returns dict with grad_y0 [B,D], grad_args
+    [B,n_args], grad_params [P] (summed over the batch), result [B] and stats
+    [B,3] (steps, accepted, rejected over all segments)."""
+    lib = load()
+    ys = np.asarray(ys, dtype=np.float64)
+    B = ys.shape[0]
+    n_save = desc.save_t0 + desc.n_ts + desc.save_t1
+    t0, t1, dt0, tstride, _, args_arr, astride, params_arr, _ = _prep(
+        desc, B, t0, t1, dt0, np.zeros((B, desc.dim)), args, params, None)
+    ts_saved = _f64(ts_saved, (B, n_save))
+    ys = _f64(ys, (B, n_save, desc.dim))
+    gys = _f64(grad_ys, (B, n_save, desc.dim))
+    gy0 = np.zeros((B, desc.dim))
+    gargs = np.zeros((B, max(desc.n_args, 1)))
+    n_params = params_arr.size if params is not None else 0
+    gp = np.zeros(max(n_params, 1))
+    res = np.empty(B, dtype=np.int32)
+    stats = np.empty((B, 3), dtype=np.int32)
+    rc = lib.orc_backsolve(ctypes.byref(desc), B, _dptr(t0), _dptr(t1), _dptr(dt0), tstride,
+                           _dptr(ts_saved), _dptr(ys), _dptr(gys), _dptr(args_arr), astride,
+                           _dptr(params_arr), n_params, _dptr(gy0),
+                           _dptr(gargs) if desc.n_args else None, _dptr(gp),
+                           res.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                           stats.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), int(nthreads))
+    if rc != 0:
+        raise ValueError(f"oracle rejected the problem (code {rc})")
+    return dict(result=res, stats=stats, grad_y0=gy0, grad_args=gargs[:, :desc.n_args],
+                grad_params=gp[:n_params])
 
 
 def vbt_increments(desc: OracleDesc, traj, ta, tb):

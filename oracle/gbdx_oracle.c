@@ -1096,5 +1096,283 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
   return 0;
 }
 
+/* ------------------------------------------------------------------------ */
+/* BacksolveAdjoint backward (_adjoint.py:572-734).                          */
+/*                                                                           */
+/* For each pair of adjacent saved times, in reverse, a diffeqsolve of the   */
+/* augmented state z = [y | a_y | a_args | a_theta] from ts[j] back to       */
+/* ts[j-1] (t0 for the last segment unless t0 itself was saved), started at  */
+/* the saved y with a_y += dL/dys[j] (:646-650).  The augmented field is     */
+/* AdjointTerm.vf (_term.py:886-910): (f, -a^T df/dy, -a^T df/dargs,          */
+/* -a^T df/dtheta).  Solver and controller state carry across segments       */
+/* (:656-674); made_jump=True (and the first segment's solver init) means    */
+/* the FSAL vector is recomputed at every segment start.  The initial step   */
+/* of every segment is chosen as in diffeqsolve with controller_state given  */
+/* (_integrate.py:1252-1265): dt0=None -> PID init (0.01 for wrapped terms,   */
+/* clipped to dtmin/dtmax); an explicit dt0 -> t0 + dt0 unclipped after the   */
+/* first segment.  ConstantStepSize's carried state (constant.py:59-104)     */
+/* keeps extending the first segment's grid in later segments, as it does in */
+/* the reference.                                                            */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int64_t N;       /* augmented size 2D + n_args + n_params */
+  double *k[7], *zs, *z1, *err, *fsal, *f, *sc;
+} AugWork;
+
+static void aug_alloc(AugWork *w, int64_t N) {
+  w->N = N;
+  for (int i = 0; i < 7; i++) w->k[i] = (double *)calloc((size_t)N, sizeof(double));
+  w->zs = (double *)calloc((size_t)N, sizeof(double));
+  w->z1 = (double *)calloc((size_t)N, sizeof(double));
+  w->err = (double *)calloc((size_t)N, sizeof(double));
+  w->fsal = (double *)calloc((size_t)N, sizeof(double));
+  w->f = (double *)calloc((size_t)N, sizeof(double));
+  w->sc = (double *)calloc((size_t)N, sizeof(double));
+}
+
+static void aug_free(AugWork *w) {
+  for (int i = 0; i < 7; i++) free(w->k[i]);
+  free(w->zs); free(w->z1); free(w->err); free(w->fsal); free(w->f); free(w->sc);
+}
+
+/* AdjointTerm.vf at z (only the y and a_y parts of z enter). */
+static void aug_vf(const Field *F, double t, const double *z, double *out, int64_t N) {
+  const orc_desc *d = F->d;
+  const int D = d->dim, na = d->n_args;
+  field_drift(F, t, z, out);
+  memset(out + D, 0, sizeof(double) * (size_t)(N - D));
+  field_drift_vjp(F, z, z + D, out + D, na ? out + 2 * D : NULL,
+                  N > 2 * D + na ? out + 2 * D + na : NULL);
+  for (int64_t n = D; n < N; n++) out[n] = -out[n];
+}
+
+/* One explicit RK step of the augmented system (runge_kutta.py:446-1203). */
+static void aug_step(const Field *F, const Tableau *tab, int dir, double tprev,
+                     double tnext, const double *z0, int have_f0, AugWork *w) {
+  const int D2 = 2 * F->d->dim;
+  const int64_t N = w->N;
+  const double dt = tnext - tprev, control = dir * dt;
+  for (int i = 0; i < tab->s; i++) {
+    /* stage input: only y and a_y feed the field */
+    for (int n = 0; n < D2; n++) {
+      double inc = 0.0;
+      for (int j = 0; j < i; j++) inc += tab->a[i][j] * w->k[j][n];
+      w->zs[n] = z0[n] + inc;
+    }
+    double ti = (tab->c[i] == 1.0) ? tnext : tprev + tab->c[i] * dt;
+    if (i == 0 && have_f0 && tab->fsal) {
+      memcpy(w->f, w->fsal, sizeof(double) * (size_t)N);
+    } else {
+      aug_vf(F, dir * ti, w->zs, w->f, N);
+    }
+    if (tab->fsal && i == tab->s - 1) memcpy(w->fsal, w->f, sizeof(double) * (size_t)N);
+    for (int64_t n = 0; n < N; n++) w->k[i][n] = w->f[n] * control;
+  }
+  for (int64_t n = 0; n < N; n++) {
+    if (tab->ssal && n < D2) {
+      w->z1[n] = w->zs[n];
+    } else {
+      double inc = 0.0;
+      for (int j = 0; j < tab->s; j++) inc += tab->b[j] * w->k[j][n];
+      w->z1[n] = z0[n] + inc;
+    }
+    double e = 0.0;
+    for (int j = 0; j < tab->s; j++) e += tab->e[j] * w->k[j][n];
+    w->err[n] = isnan(e) ? INFINITY : e; /* _integrate.py:386 */
+  }
+}
+
+/* Leaves of the augmented pytree, for the per-leaf NaN rule of pid.py:
+ * 475-481: y, a_y, a_args, then each parameter array of the field. */
+static int aug_leaves(const orc_desc *d, int64_t *bounds) {
+  int nl = 0;
+  int64_t o = 0;
+  bounds[nl++] = o; o += d->dim;
+  bounds[nl++] = o; o += d->dim;
+  if (d->n_args) { bounds[nl++] = o; o += d->n_args; }
+  if (d->field == ORC_MLP) {
+    for (int l = 0; l < d->mlp_depth; l++) {
+      int ni = d->mlp_widths[l], no = d->mlp_widths[l + 1];
+      bounds[nl++] = o; o += (int64_t)ni * no;
+      bounds[nl++] = o; o += no;
+    }
+  } else if (d->field == ORC_LINEAR) {
+    bounds[nl++] = o; o += (int64_t)d->dim * d->dim;
+  }
+  bounds[nl] = o;
+  return nl;
+}
+
+typedef struct {
+  const orc_desc *d;
+  const double *t0, *t1, *dt0;
+  int64_t time_stride;
+  const double *ts_saved, *ys, *grad_ys;
+  const double *args;
+  int64_t args_stride;
+  const double *params;
+  int64_t n_params;
+  double *grad_y0, *grad_args;
+  int32_t *result, *stats;
+} BsIO;
+
+static void backsolve_one(const BsIO *io, int64_t b, double *gP, AugWork *w) {
+  const orc_desc *d = io->d;
+  const Tableau *tab = tableau_of(d->solver);
+  const int D = d->dim, na = d->n_args;
+  const int64_t N = w->N;
+  const int n_save = n_save_of(d);
+  Field F = {d, io->args + b * io->args_stride, io->params, NULL, NULL};
+  const double *T = io->ts_saved + b * n_save;
+  const double *Y = io->ys + b * (int64_t)n_save * D;
+  const double *G = io->grad_ys + b * (int64_t)n_save * D;
+  const double t0 = io->t0[b * io->time_stride], t1 = io->t1[b * io->time_stride];
+  const int dir = (t0 < t1) ? -1 : 1; /* every segment runs against the forward */
+  const int has_dt0 = io->dt0 != NULL;
+  const double h0 = has_dt0 ? fabs(io->dt0[b * io->time_stride]) : 0.0;
+  const double eord = error_order_of(d, tab);
+  const int n_norm = d->norm == ORC_NORM_ADJOINT_SEMI ? 2 * D : (int)N;
+  int64_t leaf[64];
+  const int nleaf = aug_leaves(d, leaf);
+
+  double *z = (double *)calloc((size_t)N, sizeof(double));
+  CtrlState cs;
+  memset(&cs, 0, sizeof cs);
+  int first_seg = 1, result = ORC_SUCCESSFUL;
+  int tot = 0, acc = 0, rej = 0;
+  const int jlo = d->save_t0 ? 1 : 0;
+  for (int j = n_save - 1; j >= jlo; j--) {
+    const double target = j >= 1 ? T[j - 1] : t0;
+    memcpy(z, Y + (int64_t)j * D, sizeof(double) * D);
+    for (int n = 0; n < D; n++) z[D + n] += G[(int64_t)j * D + n];
+    const double ts_ = dir * T[j], te = dir * target;
+    double tnext;
+    if (d->controller == ORC_PID) {
+      if (first_seg || !has_dt0) {
+        double h = has_dt0 ? h0 : 0.01;
+        if (!isnan(d->dtmax)) h = h < d->dtmax ? h : d->dtmax;
+        if (!isnan(d->dtmin)) h = h > d->dtmin ? h : d->dtmin;
+        tnext = ts_ + h;
+      } else {
+        tnext = ts_ + h0;
+      }
+      if (first_seg) { cs.prev_inv = 1.0; cs.prev_prev_inv = 1.0; cs.at_dtmin = 0; }
+    } else {
+      if (first_seg) {
+        cs.steps_completed = 1;
+        cs.num_steps = (int)ceil((te - ts_) / nextafter(h0, INFINITY));
+        cs.t0_sim = ts_; cs.t1_sim = te;
+      }
+      tnext = ts_ + h0;
+    }
+    first_seg = 0;
+    tnext = tnext < te ? tnext : te;
+    double tprev = ts_;
+    double floor_te = te;
+    for (int i = 0; i < 100; i++) floor_te = prevbefore(floor_te);
+    int have_f0 = 0, nsteps = 0, seg_result = ORC_SUCCESSFUL;
+    while (tprev < te && seg_result == ORC_SUCCESSFUL) {
+      if (nsteps >= d->max_steps) break;
+      aug_step(&F, tab, dir, tprev, tnext, z, have_f0, w);
+      int keep, cres = ORC_SUCCESSFUL;
+      double nt0, nt1;
+      if (d->controller == ORC_PID) {
+        double ssum = 0.0;
+        for (int l = 0; l < nleaf; l++) {
+          if (leaf[l] >= n_norm) break;
+          int any_nan = 0;
+          for (int64_t n = leaf[l]; n < leaf[l + 1]; n++) any_nan |= isnan(w->z1[n]);
+          for (int64_t n = leaf[l]; n < leaf[l + 1] && n < n_norm; n++) {
+            double a0 = fabs(z[n]), a1 = fabs(any_nan ? z[n] : w->z1[n]);
+            double ym = a0 > a1 ? a0 : a1;
+            double s = w->err[n] / (d->atol + ym * d->rtol);
+            ssum += s * s;
+          }
+        }
+        double scaled = sqrt(ssum) / sqrt((double)n_norm);
+        keep = pid_adapt(d, eord, tprev, tnext, scaled, &cs, &nt0, &nt1, &cres);
+      } else {
+        keep = constant_adapt(tnext, &cs, &nt0, &nt1);
+      }
+      nt0 = nt0 < te ? nt0 : te;
+      if (nt1 > floor_te) nt1 = keep ? te : nt0 + 0.5 * (te - nt0);
+      if (keep) {
+        memcpy(z, w->z1, sizeof(double) * (size_t)N);
+        if (tab->fsal) have_f0 = 1;
+      }
+      if (seg_result == ORC_SUCCESSFUL) seg_result = cres;
+      nsteps++;
+      tot++;
+      if (keep) acc++; else rej++;
+      tprev = nt0;
+      tnext = nt1;
+    }
+    if (seg_result == ORC_SUCCESSFUL && tprev < te) seg_result = ORC_MAX_STEPS_REACHED;
+    if (result == ORC_SUCCESSFUL) result = seg_result;
+  }
+  if (d->save_t0)
+    for (int n = 0; n < D; n++) z[D + n] += G[n];
+  memcpy(io->grad_y0 + b * D, z + D, sizeof(double) * D);
+  if (io->grad_args && na) memcpy(io->grad_args + b * na, z + 2 * D, sizeof(double) * na);
+  if (gP)
+    for (int64_t p = 0; p < io->n_params; p++) gP[p] += z[2 * D + na + p];
+  io->result[b] = result;
+  io->stats[b * 3 + 0] = tot;
+  io->stats[b * 3 + 1] = acc;
+  io->stats[b * 3 + 2] = rej;
+  free(z);
+}
+
+/* ts_saved [B, n_save] and ys [B, n_save, D] are the forward's saved outputs,
+ * grad_ys their cotangent.  d describes the backward solve (its solver,
+ * controller and norm) and the forward's SaveAt.  Outputs: grad_y0 [B, D],
+ * grad_args [B, n_args], grad_params [n_params] summed over the batch,
+ * result [B] and stats [B, 3] (steps, accepted, rejected over all segments). */
+int orc_backsolve(const orc_desc *d, int64_t B, const double *t0, const double *t1,
+                  const double *dt0, int64_t time_stride, const double *ts_saved,
+                  const double *ys, const double *grad_ys, const double *args,
+                  int64_t args_stride, const double *params, int64_t n_params,
+                  double *grad_y0, double *grad_args, double *grad_params,
+                  int32_t *result, int32_t *stats, int nthreads) {
+  validate_desc(d);
+  if (d->dim > 64 || d->dim < 1) return -1;
+  if (d->field == ORC_CALLBACK || d->diffusion != ORC_DIFF_NONE) return -2;
+  const int64_t N = 2 * (int64_t)d->dim + d->n_args + n_params;
+  BsIO io = {d, t0, t1, dt0, time_stride, ts_saved, ys, grad_ys, args, args_stride,
+             params, n_params, grad_y0, grad_args, result, stats};
+  int nt = 1;
+#ifdef _OPENMP
+  nt = nthreads > 0 ? nthreads : 1;
+#endif
+  (void)nthreads;
+  double *gp_all = (double *)calloc((size_t)nt * (size_t)(n_params > 0 ? n_params : 1), sizeof(double));
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    AugWork w;
+    aug_alloc(&w, N);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+    for (int64_t b = 0; b < B; b++)
+      backsolve_one(&io, b, n_params > 0 ? gp_all + (size_t)tid * n_params : NULL, &w);
+    aug_free(&w);
+  }
+  if (grad_params && n_params > 0) {
+    for (int64_t p = 0; p < n_params; p++) {
+      double acc = 0.0;
+      for (int t = 0; t < nt; t++) acc += gp_all[(size_t)t * n_params + p];
+      grad_params[p] = acc;
+    }
+  }
+  free(gp_all);
+  return 0;
+}
+
 int orc_abi_version(void) { return 1; }
 int orc_desc_size(void) { return (int)sizeof(orc_desc); }

@@ -388,6 +388,115 @@ def test_grad_sde_heun_tanh_diffusion():
     _fd_check(d, 0.0, 1.0, 0.01, y0, params=params, tol=1e-5)
 
 
+# --- BacksolveAdjoint (test/test_adjoint.py:33-215) ---------------------------
+
+_BS_A = np.array([[0.1, -1.0], [1.0, -0.1]])  # _VectorField with args (0.1, -1), (1, -0.1)
+
+
+def _linear_exact_grads(A, y0, t0, saved_ts, G):
+    """dL/dy0 and dL/dA of L = sum_k <G_k, y(t_k)> for y' = A y, exactly:
+    exp(A^T tau) G_k and the Frechet derivative of the matrix exponential."""
+    gy = np.zeros(A.shape[0])
+    gA = np.zeros_like(A)
+    for tk, g in zip(saved_ts, G):
+        tau = tk - t0
+        gy += scipy.linalg.expm(A.T * tau) @ g
+        if tau > 0:
+            gA += scipy.linalg.expm_frechet(A.T * tau, tau * np.outer(g, y0),
+                                            compute_expm=False)
+    return gy, gA
+
+
+@pytest.mark.parametrize("save_t0", [1, 0])
+@pytest.mark.parametrize("save_t1", [1, 0])
+@pytest.mark.parametrize("ts", [None, [0.3], [2.0], [9.5], [1.0, 7.0], [0.3, 7.0, 9.5]])
+def test_backsolve_against_recursive_and_exact(save_t0, save_t1, ts):
+    # test/test_adjoint.py:139-163: on y' = A y over [0.3, 9.5], Tsit5 with
+    # PID(1e-8, 1e-8) and dt0=None, BacksolveAdjoint agrees with the
+    # discretise-then-optimise gradient at atol 1e-5 for every SaveAt.
+    if not save_t0 and not save_t1 and ts is None:
+        pytest.skip("empty SaveAt")
+    d = O.make_desc(solver=O.TSIT5, controller=O.PID, field=O.LINEAR, dim=2, rtol=1e-8,
+                    atol=1e-8, save_t0=save_t0, save_t1=save_t1,
+                    n_ts=0 if ts is None else len(ts))
+    y0 = np.array([[0.9, 5.4]])
+    fwd = O.solve(d, 0.3, 9.5, None, y0, params=_BS_A, ts=ts)
+    G = np.ones_like(fwd["ys"])
+    rec = O.grad_recursive(d, 0.3, 9.5, None, y0, G, params=_BS_A, ts=ts)
+    bs = O.backsolve(d, 0.3, 9.5, None, fwd["ts"], fwd["ys"], G, params=_BS_A)
+    assert bs["result"][0] == 0
+    assert tree_allclose(bs["grad_y0"], rec["grad_y0"], atol=1e-5)
+    assert tree_allclose(bs["grad_params"], rec["grad_params"], atol=1e-5)
+    gy, gA = _linear_exact_grads(_BS_A, y0[0], 0.3, fwd["ts"][0], G[0])
+    assert tree_allclose(bs["grad_y0"][0], gy, atol=1e-5)
+    assert tree_allclose(bs["grad_params"].reshape(2, 2), gA, atol=1e-5)
+
+
+def test_backsolve_seminorm():
+    # adjoint_rms_seminorm (_misc.py:85-116) drops a_args and a_theta from the
+    # error norm: fewer steps, same gradient to the tolerance.
+    kw = dict(solver=O.TSIT5, controller=O.PID, field=O.LINEAR, dim=2, rtol=1e-8, atol=1e-8,
+              n_ts=2, save_t1=1)
+    d = O.make_desc(**kw)
+    ds = O.make_desc(norm=O.NORM_ADJOINT_SEMI, **kw)
+    y0 = np.array([[0.9, 5.4]])
+    ts = [1.0, 7.0]
+    fwd = O.solve(d, 0.3, 9.5, None, y0, params=_BS_A, ts=ts)
+    G = np.ones_like(fwd["ys"])
+    full = O.backsolve(d, 0.3, 9.5, None, fwd["ts"], fwd["ys"], G, params=_BS_A)
+    semi = O.backsolve(ds, 0.3, 9.5, None, fwd["ts"], fwd["ys"], G, params=_BS_A)
+    assert semi["stats"][0, 0] != full["stats"][0, 0]
+    gy, gA = _linear_exact_grads(_BS_A, y0[0], 0.3, fwd["ts"][0], G[0])
+    assert tree_allclose(semi["grad_y0"][0], gy, atol=1e-5)
+    assert tree_allclose(semi["grad_params"].reshape(2, 2), gA, rtol=1e-4, atol=1e-5)
+
+
+def test_backsolve_mlp_converges_to_recursive():
+    # Optimise-then-discretise and discretise-then-optimise gradients agree as
+    # the tolerance shrinks (both converge to the continuous gradient).
+    rng = np.random.default_rng(5)
+    widths = [4, 8, 8, 4]
+    P = []
+    for i in range(3):
+        P.append(rng.standard_normal((widths[i + 1], widths[i])) / np.sqrt(widths[i]))
+        P.append(rng.standard_normal(widths[i + 1]) * 0.1)
+    params = np.concatenate([p.reshape(-1) for p in P])
+    y0 = rng.standard_normal((3, 4))
+    ts = np.linspace(0.0, 1.0, 5)
+    errs = []
+    for tol in (1e-5, 1e-8):
+        d = O.make_desc(solver=O.TSIT5, controller=O.PID, field=O.MLP, dim=4, rtol=tol,
+                        atol=tol, n_ts=5, mlp_depth=3, mlp_widths=widths)
+        fwd = O.solve(d, 0.0, 1.0, None, y0, params=params, ts=ts)
+        G = rng.standard_normal(fwd["ys"].shape)
+        rec = O.grad_recursive(d, 0.0, 1.0, None, y0, G, params=params, ts=ts)
+        bs = O.backsolve(d, 0.0, 1.0, None, fwd["ts"], fwd["ys"], G, params=params)
+        scale = max(np.abs(rec["grad_params"]).max(), np.abs(rec["grad_y0"]).max())
+        errs.append(max(np.abs(bs["grad_params"] - rec["grad_params"]).max(),
+                        np.abs(bs["grad_y0"] - rec["grad_y0"]).max()) / scale)
+    assert errs[1] < 1e-6 and errs[1] < errs[0] / 10
+
+
+def test_backsolve_constant_steps_converge():
+    # ConstantStepSize: the backward reuses the forward's controller; its
+    # carried state extends the first segment's grid (constant.py:59-104).
+    # Halving dt0 shrinks the Heun gradient error ~4x.  (With a zero-length
+    # first segment, e.g. SaveAt(ts=[..., t1], t1=True), that grid has zero
+    # steps and the reference's constant controller produces NaN times.)
+    y0 = np.array([[0.9, 5.4]])
+    ts = [1.0, 2.5, 4.0]
+    errs = []
+    for dt0 in (0.02, 0.01):
+        d = O.make_desc(solver=O.HEUN, controller=O.CONSTANT, field=O.LINEAR, dim=2, n_ts=3,
+                        save_t1=0)
+        fwd = O.solve(d, 0.3, 4.0, dt0, y0, params=_BS_A, ts=ts)
+        G = np.ones_like(fwd["ys"])
+        bs = O.backsolve(d, 0.3, 4.0, dt0, fwd["ts"], fwd["ys"], G, params=_BS_A)
+        gy, gA = _linear_exact_grads(_BS_A, y0[0], 0.3, fwd["ts"][0], G[0])
+        errs.append(np.abs(bs["grad_params"].reshape(2, 2) - gA).max())
+    assert 3.0 < errs[0] / errs[1] < 5.0
+
+
 # --- virtual Brownian tree statistics (test/test_brownian.py:117-494) --------
 
 def test_vbt_increment_distribution():
