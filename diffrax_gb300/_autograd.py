@@ -53,6 +53,32 @@ class _RecursiveCheckpointSolve(torch.autograd.Function):
                 grad_params.to(params.dtype) if ctx.needs_input_grad[2] else None)
 
 
+class _BacksolveSolve(torch.autograd.Function):
+    """BacksolveAdjoint (diffrax/_adjoint.py:538-734): the forward keeps only
+    the saved (ts, ys); the backward kernel solves the augmented adjoint system
+    backwards between the saved times and returns dL/dy0 and dL/dparams."""
+
+    @staticmethod
+    def forward(ctx, low, y0, params):
+        ys, ts, res, stats = low.run_forward(y0=y0.detach(), params=params.detach())
+        ctx.low = low
+        ctx.save_for_backward(params, ys, ts)
+        ctx.mark_non_differentiable(ts, res, stats)
+        return ys, ts, res, stats
+
+    @staticmethod
+    def backward(ctx, grad_ys, _gts, _gres, _gstats):
+        params, ys, ts = ctx.saved_tensors
+        low = ctx.low
+        if grad_ys is None:
+            grad_ys = torch.zeros_like(ys)
+        grad_y0, grad_params, res, stats = low.run_backsolve(ts, ys.detach(), grad_ys,
+                                                             params.detach())
+        low.bwd_result, low.bwd_stats = res, stats
+        return (None, grad_y0 if ctx.needs_input_grad[1] else None,
+                grad_params.to(params.dtype) if ctx.needs_input_grad[2] else None)
+
+
 def solve_with_grad(low, y0, args):
     if isinstance(args, torch.Tensor) and args.requires_grad:
         raise NotImplementedError("gradients with respect to args are not available")
@@ -67,5 +93,11 @@ def solve_with_grad(low, y0, args):
             y0_dev = y0_dev.detach()
         return _RecursiveCheckpointSolve.apply(low, y0_dev, low.params)
     if isinstance(low.adjoint, BacksolveAdjoint):
-        raise NotImplementedError("BacksolveAdjoint gradients are not available yet")
+        y0_dev = y0 if isinstance(y0, torch.Tensor) else torch.as_tensor(y0)
+        y0_dev = y0_dev.to(device=low.device, dtype=low.dtype)
+        if not y0_dev.is_contiguous():
+            y0_dev = y0_dev.contiguous()
+        if not y0_dev.requires_grad:
+            y0_dev = y0_dev.detach()
+        return _BacksolveSolve.apply(low, y0_dev, low.params)
     raise NotImplementedError(f"adjoint {low.adjoint!r} is not supported")

@@ -181,15 +181,37 @@ class Lowered:
         # The adjoint shapes the problem only when a gradient will be taken:
         # a plain forward solve records no tape.
         self.adjoint = adjoint if want_grad else None
+        backsolve = isinstance(self.adjoint, BacksolveAdjoint)
         self.fields = lower(terms, solver, stepsize_controller, saveat, dim=self.dim,
                             dtype=self.dtype, max_steps=max_steps, n_ts=n_ts,
-                            adjoint=self.adjoint, kernel=kernel, block_threads=block_threads,
-                            ctas_per_sm=ctas_per_sm, schedule=schedule)
+                            adjoint=None if backsolve else self.adjoint, kernel=kernel,
+                            block_threads=block_threads, ctas_per_sm=ctas_per_sm,
+                            schedule=schedule)
         drift = _split_terms(terms)[0]
         self.drift = drift
         self.problem = _lib.get_problem(self.fields)
         self.t0, self.t1, self.dt0, self.tstride = _time_arrays(t0, t1, dt0, self.B, dev)
         _host_checks(self.t0, self.t1, self.dt0, ts, self.tstride)
+        self.bwd_problem = None
+        if backsolve:
+            # The backward solve reuses the forward's solver and controller
+            # unless BacksolveAdjoint(**kwargs) overrides them
+            # (diffrax/_adjoint.py:623-633).
+            kw = self.adjoint.kwargs
+            self.bwd_fields = lower(terms, kw.get("solver", solver),
+                                    kw.get("stepsize_controller", stepsize_controller), saveat,
+                                    dim=self.dim, dtype=self.dtype,
+                                    max_steps=kw.get("max_steps", max_steps), n_ts=n_ts,
+                                    adjoint=self.adjoint, kernel=kernel, schedule=schedule)
+            self.bwd_problem = _lib.get_problem(self.bwd_fields)
+            self.bwd_dt0 = self.dt0
+            if kw.get("dt0") is not None:
+                self.bwd_dt0 = _time_arrays(t0, t1, kw["dt0"], self.B, dev)[2]
+                if self.bwd_dt0.numel() != self.t0.numel():
+                    self.bwd_dt0 = self.bwd_dt0.expand(self.t0.numel()).contiguous()
+            if self.bwd_fields["controller"] == 0 and self.bwd_dt0 is None:
+                raise ValueError("Constant step size solvers cannot select step size "
+                                 "automatically; please pass a value for `dt0`.")
         na = drift.n_args
         if na:
             if args is None:
@@ -262,6 +284,30 @@ class Lowered:
         return grad_y0, grad_params[:n_params]
 
 
+    def run_backsolve(self, ts_out, ys, grad_ys, params, stream=None):
+        """BacksolveAdjoint backward from the forward's saved (ts, ys):
+        dL/dy0, dL/dparams and the backward's RESULTS codes and step counts."""
+        dev = self.device
+        prob = self.bwd_problem
+        grad_ys = grad_ys.to(device=dev, dtype=self.dtype).contiguous()
+        grad_y0 = torch.empty((self.B, self.dim), dtype=self.dtype, device=dev)
+        n_params = int(params.numel())
+        grad_params = torch.empty((max(n_params, 1),), dtype=torch.float32, device=dev)
+        res = torch.empty((self.B,), dtype=torch.int32, device=dev)
+        stats = torch.empty((self.B, 3), dtype=torch.int32, device=dev)
+        ws_bytes = prob.workspace_size(self.B)
+        ws = torch.empty((max(ws_bytes, 1),), dtype=torch.uint8, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev).cuda_stream
+        p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        rc = prob.lib.gbdx_backsolve_bwd(
+            prob.handle, self.B, p(self.t0), p(self.t1), p(self.bwd_dt0), self.tstride,
+            p(ts_out.contiguous()), p(ys.contiguous()), p(grad_ys), p(params), p(grad_y0),
+            p(grad_params), p(res), p(stats), p(ws), ws_bytes, stream)
+        _lib.check(rc, "gbdx_backsolve_bwd")
+        return grad_y0, grad_params[:n_params], res, stats
+
+
 def _raise_on_failure(result: torch.Tensor):
     if _capturing():
         return
@@ -307,6 +353,9 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
                    stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],
                               num_rejected_steps=stats[:, 2], max_steps=max_steps),
                    result=res)
+    # the lowered solve; after a backward pass under BacksolveAdjoint it holds
+    # the backward's RESULTS codes and step counts (bwd_result, bwd_stats)
+    sol.lowered = low
     if throw:
         _raise_on_failure(res)
     return sol

@@ -50,6 +50,7 @@ struct gbdx_problem {
   double c1, c2, c3;  // PID exponents
   gbdx::OdeEntry ode;
   gbdx::BwdEntry bwd;  // RecursiveCheckpointAdjoint backward (MLP fields)
+  gbdx::BsEntry bs;    // BacksolveAdjoint backward (MLP fields)
   bool mlp;            // MLP-field row-tile integrator (256 threads per CTA)
   int rows_per_cta;
 };
@@ -60,8 +61,15 @@ namespace {
 // adjoint) the tape the backward reads plus its scratch.
 struct WsLayout {
   size_t order, tape_t, tape_y, tape_n, tape_s, scratch, psum, pcomp, total;
+  size_t frag, rec, ath;  // backsolve: B fragments, stage records, a_theta
   int seg_max, n_cta;
+  bool track;
 };
+
+// Backsolve tracks a_theta per row when its PID error norm runs over it.
+bool bs_tracks(const gbdx_problem_desc &d) {
+  return d.controller == GBDX_PID && d.norm == GBDX_NORM_RMS;
+}
 
 size_t up256(size_t x) { return (x + 255) / 256 * 256; }
 
@@ -75,6 +83,33 @@ int ws_layout(const gbdx_problem *p, int64_t batch, WsLayout *L) {
   L->tape_t = L->tape_y = L->tape_n = L->tape_s = L->scratch = L->psum = L->pcomp = off;
   L->seg_max = 0;
   L->n_cta = 0;
+  L->frag = L->rec = L->ath = off;
+  L->track = false;
+  if (d.adjoint == GBDX_ADJ_BACKSOLVE && p->bs.launch) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = p->bs.occupancy(&occ);
+    if (e != cudaSuccess) return cuda_fail(e, "backsolve launch shape");
+    if (occ < 1) occ = 1;
+    int64_t grid = int64_t(sms) * occ;
+    const int64_t needed = (int64_t(B) + p->bs.rows - 1) / p->bs.rows;
+    if (grid > needed) grid = needed;
+    L->n_cta = int(grid);
+    const size_t np = size_t(gbdx_param_count(p));
+    const size_t D = size_t(d.dim), H = size_t(d.mlp_widths[1]);
+    L->frag = off;
+    if (p->bs.gfrag) off += 4 * up256(D * H * 2);
+    L->rec = off;
+    off += up256(size_t(L->n_cta) * p->bs.stages * p->bs.rows * p->bs.rec * sizeof(float));
+    L->psum = off;
+    off += up256(size_t(L->n_cta) * np * sizeof(float));
+    L->pcomp = off;
+    off += up256(size_t(L->n_cta) * np * sizeof(float));
+    L->track = bs_tracks(d);
+    L->ath = off;
+    if (L->track) off += up256(size_t(L->n_cta) * p->bs.rows * 2 * np * sizeof(float));
+  }
   if (d.adjoint == GBDX_ADJ_RECURSIVE && p->bwd.launch) {
     const int C = d.checkpoints > 1 ? d.checkpoints : 2;
     L->tape_t = off;
@@ -175,6 +210,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   p->c3 = d.dcoeff / order;
   p->ode = gbdx::OdeEntry{nullptr, nullptr};
   p->bwd = gbdx::BwdEntry{nullptr, nullptr};
+  p->bs = gbdx::BsEntry{nullptr, nullptr, 0, 0, 0, 0};
   p->mlp = false;
   p->rows_per_cta = 1;
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
@@ -206,7 +242,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     const int D = d.dim, H = w[1];
     if (d.kernel == GBDX_KERNEL_PLAIN) {
       // The plain form: one trajectory per thread, FP32 CUDA-core products.
-      if (d.adjoint == GBDX_ADJ_RECURSIVE) {
+      if (d.adjoint != GBDX_ADJ_NONE) {
         delete p;
         return fail(GBDX_ERR_UNSUPPORTED, "the plain MLP kernel has no backward");
       }
@@ -238,6 +274,25 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       if (!p->bwd.launch) {
         delete p;
         return fail(GBDX_ERR_UNSUPPORTED, "no backward kernel for this MLP problem");
+      }
+    }
+    if (d.adjoint == GBDX_ADJ_BACKSOLVE) {
+      if (sde) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED, "BacksolveAdjoint is available for MLP ODEs");
+      }
+      if (D == 64 && H == 256) p->bs = gbdx::find_backsolve_entry_d64h256(d.solver, precise);
+      if (D == 64 && H == 128) p->bs = gbdx::find_backsolve_entry_d64h128(d.solver, precise);
+      if (D == 32 && H == 64) p->bs = gbdx::find_backsolve_entry_d32h64(d.solver, precise);
+      if (!p->bs.launch) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED,
+                    "no backsolve kernel for dim %d, width %d, solver %d%s", D, H, d.solver,
+                    precise ? " (FP32 products)" : "");
+      }
+      if (d.norm != GBDX_NORM_RMS && d.norm != GBDX_NORM_ADJOINT_SEMI) {
+        delete p;
+        return fail(GBDX_ERR_INVALID, "unknown norm %d", d.norm);
       }
     }
   } else {
@@ -474,6 +529,78 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
     if (e != cudaSuccess) return cuda_fail(e, "backward launch");
   }
   e = gbdx::launch_reduce_partials(Q.part_sum, Q.part_comp, batch > 0 ? L.n_cta : 0, np,
+                                   static_cast<float *>(grad_params), s);
+  if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
+  return GBDX_OK;
+}
+
+int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
+                       const double *t1, const double *dt0, int64_t time_stride,
+                       const double *save_ts, const void *ys, const void *grad_ys,
+                       const void *params, void *grad_y0, void *grad_params,
+                       int32_t *result_out, int32_t *stats_out, void *workspace,
+                       size_t workspace_bytes, void *stream) {
+  if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
+  const gbdx_problem_desc &d = problem->d;
+  if (d.adjoint != GBDX_ADJ_BACKSOLVE || !problem->bs.launch)
+    return fail(GBDX_ERR_UNSUPPORTED,
+                "the problem was not created with BacksolveAdjoint on an MLP field");
+  if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
+  if (!grad_ys || !grad_y0 || !grad_params || !ys || !result_out || !stats_out)
+    return fail(GBDX_ERR_INVALID, "null pointer argument");
+  if (batch > 0 && !save_ts) return fail(GBDX_ERR_INVALID, "the forward's saved times are missing");
+  gbdx::SolveParams P;
+  WsLayout L;
+  // y0 is not read by the backward; the saved states stand in for the check.
+  int rc = prepare(problem, batch, t0, t1, dt0, time_stride, ys, nullptr, 0, params, save_ts,
+                   workspace, workspace_bytes, &P, &L);
+  if (rc != GBDX_OK) return rc;
+  P.result_out = result_out;
+  P.stats_out = stats_out;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int np = int(gbdx_param_count(problem));
+  const int D = d.dim, H = d.mlp_widths[1];
+  char *w = static_cast<char *>(workspace);
+  gbdx::BsParams Q;
+  memset(&Q, 0, sizeof Q);
+  Q.ys = static_cast<const float *>(ys);
+  Q.grad_ys = static_cast<const float *>(grad_ys);
+  Q.grad_y0 = static_cast<float *>(grad_y0);
+  Q.psum = reinterpret_cast<float *>(w + L.psum);
+  Q.pcomp = reinterpret_cast<float *>(w + L.pcomp);
+  Q.rec = reinterpret_cast<float *>(w + L.rec);
+  Q.ath = L.track ? reinterpret_cast<float *>(w + L.ath) : nullptr;
+  Q.track = L.track ? 1 : 0;
+  Q.n_norm = float(L.track ? 2 * D + np : 2 * D);
+  cudaError_t e = cudaMemsetAsync(w + L.psum, 0, L.ath - L.psum, s);
+  if (e != cudaSuccess) return cuda_fail(e, "gradient partial reset");
+  if (batch > 0) {
+    if (problem->bs.gfrag) {
+      const size_t part = up256(size_t(D) * H * 2);
+      uint2 *f = reinterpret_cast<uint2 *>(w + L.frag);
+      const float *W = static_cast<const float *>(params);
+      const int ow0 = 0, ow2 = H * D + H + H * H + H;
+      Q.w0f = f;
+      Q.w0v = reinterpret_cast<uint2 *>(w + L.frag + part);
+      Q.w2f = reinterpret_cast<uint2 *>(w + L.frag + 2 * part);
+      Q.w2v = reinterpret_cast<uint2 *>(w + L.frag + 3 * part);
+      // layer 0 forward: B[k][n] = W0[n][k] (K = D, N = H); VJP: B = W0 (K = H, N = D)
+      e = gbdx::launch_frag_prep(W + ow0, D, D, H, 1, const_cast<uint2 *>(Q.w0f), s);
+      if (e == cudaSuccess)
+        e = gbdx::launch_frag_prep(W + ow0, D, H, D, 0, const_cast<uint2 *>(Q.w0v), s);
+      // layer 2 forward: B[k][n] = W2[n][k] (K = H, N = D); VJP: B = W2 (K = D, N = H)
+      if (e == cudaSuccess)
+        e = gbdx::launch_frag_prep(W + ow2, H, H, D, 1, const_cast<uint2 *>(Q.w2f), s);
+      if (e == cudaSuccess)
+        e = gbdx::launch_frag_prep(W + ow2, H, D, H, 0, const_cast<uint2 *>(Q.w2v), s);
+      if (e != cudaSuccess) return cuda_fail(e, "weight fragments");
+    }
+    e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_fail(e, "queue reset");
+    e = problem->bs.launch(P, Q, L.n_cta, s);
+    if (e != cudaSuccess) return cuda_fail(e, "backsolve launch");
+  }
+  e = gbdx::launch_reduce_partials(Q.psum, Q.pcomp, batch > 0 ? L.n_cta : 0, np,
                                    static_cast<float *>(grad_params), s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
   return GBDX_OK;

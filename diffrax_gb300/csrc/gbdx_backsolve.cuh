@@ -1,0 +1,985 @@
+// gbdx_backsolve.cuh -- BacksolveAdjoint backward for MLP fields
+// (diffrax/_adjoint.py:572-734, AdjointTerm diffrax/_term.py:767-910).
+//
+// Per trajectory the backward is a chain of reverse-time solves of the
+// augmented state z = (y, a, a_theta), one per pair of adjacent saved times
+// ts[j] -> ts[j-1] (t0 after the first save unless t0 itself was saved),
+// started from the saved y with a += dL/dys[j] (_adjoint.py:646-650).  The
+// augmented field is AdjointTerm.vf: (f, -a^T df/dy, -a^T df/dtheta).  Solver
+// and controller state carry from segment to segment; every segment starts
+// with a fresh FSAL evaluation (made_jump) and the initial step of
+// diffeqsolve with a passed controller state (_integrate.py:1252-1265).
+//
+// A CTA of 8 warps integrates a tile of M trajectories ("rows") in lockstep,
+// as the forward kernel does; each row walks its own segments and refills
+// from the work counter after its last one.  Per RK stage the tile evaluates
+// f and the VJP a^T df/dy as chains of tensor-core products with hi/lo BF16
+// operands (or FP32 CUDA-core products in the parity mode) and records, per
+// row, the vector pairs whose outer products are -a^T df/dtheta:
+//   (dz0, x) for W0/b0, (dz1, h1) for W1/b1, (a, h2) for W2/b2,
+// where x is the stage input, h1, h2 the hidden activations and dz0, dz1 the
+// cotangents of the pre-activations.  The parameter part of the state never
+// exists per stage: after the stages a parameter pass contracts the records
+// with the tableau weights for every parameter of the row,
+//   da_theta = -h sum_j b_j u_j (x) v_j,   err_theta = -h sum_j e_j u_j (x) v_j.
+//   * PIDController with rms_norm (the reference's default): the error norm
+//     runs over a_theta, so every row keeps its a_theta in HBM (double
+//     buffered).  Before the controller decision the pass reads a_theta0,
+//     writes the candidate a_theta1 and adds the scaled squared errors to the
+//     row's norm; the buffers flip on accept, and a finished row folds its
+//     a_theta into the CTA's Kahan partial gradient.
+//   * adjoint_rms_seminorm or ConstantStepSize: the norm does not see
+//     a_theta; after the decision the pass adds the accepted increments into
+//     the CTA's Kahan partial gradient.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "gbdx_common.cuh"
+#include "gbdx_mlp_bwd.cuh"
+#include "gbdx_mma.cuh"
+#include "gbdx_traj.cuh"
+
+namespace gbdx {
+
+template <int D_, int H_>
+struct BsShape {
+  static constexpr int D = D_, H = H_;
+  static constexpr int M = D_ >= 64 ? 16 : 32;  // rows per CTA
+  static constexpr int THREADS = 256, WARPS = 8;
+  // Width 256: W1 stays in shared memory as BF16; W0 and W2 are read as
+  // pre-arranged BF16 fragments from global memory (L2).  Narrower fields
+  // keep all three as hi/lo BF16 pairs in shared memory.
+  static constexpr bool GFRAG = H_ >= 256;
+  static constexpr bool WSPLIT = !GFRAG;
+  static constexpr int PD = D + 8, PH = H + 8;
+  static constexpr int MT = M / 16, NT = D / 8, NTH = H / 8;
+  static constexpr int TPW = MT * NT / WARPS;    // output tiles per warp
+  static constexpr int TPWH = MT * NTH / WARPS;  // hidden tiles per warp
+  static constexpr int NE = 4 * TPW;             // owned elements per thread
+  static_assert(MT * NT % WARPS == 0 && TPW >= 1, "tile split");
+  static_assert(MT * NTH % WARPS == 0 && NTH % TPWH == 0, "hidden tile split");
+  static_assert(NT % TPW == 0, "output tile split");
+  // flat parameter offsets (FP32, row-major [out][in]), as MlpShape
+  static constexpr int OW0 = 0, OB0 = OW0 + H * D, OW1 = OB0 + H, OB1 = OW1 + H * H,
+                       OW2 = OB1 + H, OB2 = OW2 + D * H, NP = OB2 + D;
+  // per (stage, row) record: x, a, h1, h2, dz0, dz1 (FP32)
+  static constexpr int RX = 0, RG = D, RH1 = 2 * D, RH2 = 2 * D + H, RZ0 = 2 * D + 2 * H,
+                       RZ1 = 2 * D + 3 * H, REC = 2 * D + 4 * H;
+  static_assert(NP % 4 == 0 && D % 4 == 0 && H % 4 == 0, "vector alignment");
+};
+
+template <int M>
+struct BsRows {
+  double tprev[M], tnext[M], te[M], floor_te[M], dtc[M], t0s[M], t1s[M];
+  long long idx[M];
+  float h[M], hist1[M], hist2[M], acc[M];
+  int active[M], want[M], first[M], keep[M], nan_y[M], nan_a[M], dir[M];
+  int seg[M], jold[M], trans[M], newtraj[M], done[M], firstseg[M];
+  int nseg[M], nsteps[M], nacc[M], nrej[M], result[M], sres[M], sc[M], nc[M], at_dtmin[M];
+  int live[M], cur[M], zero[M];
+};
+
+template <class SH, bool GF>
+struct BsWeights;
+template <class SH>
+struct BsWeights<SH, false> {
+  __nv_bfloat16 W0[SH::H][SH::PD], W0l[SH::H][SH::PD];
+  __nv_bfloat16 W1[SH::H][SH::PH], W1l[SH::H][SH::PH];
+  __nv_bfloat16 W2[SH::D][SH::PH], W2l[SH::D][SH::PH];
+};
+template <class SH>
+struct BsWeights<SH, true> {
+  __nv_bfloat16 W1[SH::H][SH::PH];
+};
+
+template <class SH, bool PRECISE>
+struct BsSmem;
+
+template <class SH>
+struct BsSmem<SH, false> : BsWeights<SH, SH::GFRAG> {
+  float b0[SH::H], b1[SH::H], b2[SH::D];
+  __nv_bfloat16 X[SH::M][SH::PD], Xl[SH::M][SH::PD];
+  __nv_bfloat16 G[SH::M][SH::PD], Gl[SH::M][SH::PD];
+  __nv_bfloat16 R1[SH::M][SH::PH], R1l[SH::M][SH::PH];  // h1, then dz0
+  __nv_bfloat16 R2[SH::M][SH::PH], R2l[SH::M][SH::PH];  // h2, then dz1
+  __align__(16) float cf[SH::H][16];                    // parameter-pass coefficients
+  float red[SH::WARPS];
+  BsRows<SH::M> rows;
+};
+
+template <class SH>
+struct BsSmem<SH, true> {
+  float b0[SH::H], b1[SH::H], b2[SH::D];
+  float X[SH::M][SH::D + 1], G[SH::M][SH::D + 1];
+  float R1[SH::M][SH::H + 1], R2[SH::M][SH::H + 1];
+  __align__(16) float cf[SH::H][16];
+  float red[SH::WARPS];
+  BsRows<SH::M> rows;
+};
+
+// acc[j] += (Ah + Al)[16 rows, K] B[K, 8 (nt0 + j)] where the B fragments of
+// a fixed matrix are pre-arranged in global memory as [n8 tile][k16 tile][lane].
+template <int K, int NTW>
+__device__ __forceinline__ void gemm_gfrag(float (&acc)[NTW][4], const __nv_bfloat16 *Ah,
+                                           const __nv_bfloat16 *Al, int lda, const uint2 *frag,
+                                           int nt0, int lane) {
+#pragma unroll 4
+  for (int kk = 0; kk < K / 16; kk++) {
+    uint32_t ah[4], al[4];
+    ldsm_a(ah, Ah + kk * 16, lda, lane);
+    ldsm_a(al, Al + kk * 16, lda, lane);
+#pragma unroll
+    for (int j = 0; j < NTW; j++) {
+      const uint2 b = __ldg(frag + (size_t((nt0 + j) * (K / 16) + kk) << 5) + lane);
+      mma_bf16(acc[j], ah, b.x, b.y);
+      mma_bf16(acc[j], al, b.x, b.y);
+    }
+  }
+}
+
+template <class SH, bool PRECISE>
+struct BsField {
+  using Sm = BsSmem<SH, PRECISE>;
+  static constexpr int D = SH::D, H = SH::H, M = SH::M, NE = SH::NE, REC = SH::REC;
+
+  __device__ static void stage(Sm &sm, const float *P, int tid) {
+    for (int i = tid; i < H; i += SH::THREADS) {
+      sm.b0[i] = P[SH::OB0 + i];
+      sm.b1[i] = P[SH::OB1 + i];
+    }
+    for (int i = tid; i < D; i += SH::THREADS) sm.b2[i] = P[SH::OB2 + i];
+    if constexpr (!PRECISE) {
+      if constexpr (SH::GFRAG) {
+        for (int i = tid; i < H * H; i += SH::THREADS)
+          sm.W1[i / H][i % H] = __float2bfloat16_rn(P[SH::OW1 + i]);
+      } else {
+        for (int i = tid; i < H * D; i += SH::THREADS)
+          split_store(P[SH::OW0 + i], &sm.W0[i / D][i % D], &sm.W0l[i / D][i % D]);
+        for (int i = tid; i < H * H; i += SH::THREADS)
+          split_store(P[SH::OW1 + i], &sm.W1[i / H][i % H], &sm.W1l[i / H][i % H]);
+        for (int i = tid; i < D * H; i += SH::THREADS)
+          split_store(P[SH::OW2 + i], &sm.W2[i / H][i % H], &sm.W2l[i / H][i % H]);
+      }
+    }
+  }
+
+  // Stage inputs (owned layout) -> product operands and the x, a records.
+  __device__ static void put(Sm &sm, const float (&Y)[NE], const float (&A)[NE], float *rec,
+                             int warp, int lane) {
+#pragma unroll
+    for (int e = 0; e < NE; e += 2) {
+      int row, col;
+      elem_rc<SH>(e, warp, lane, row, col);
+      if constexpr (PRECISE) {
+        sm.X[row][col] = Y[e];
+        sm.X[row][col + 1] = Y[e + 1];
+        sm.G[row][col] = A[e];
+        sm.G[row][col + 1] = A[e + 1];
+      } else {
+        store_split2(Y[e], Y[e + 1], &sm.X[row][col], &sm.Xl[row][col]);
+        store_split2(A[e], A[e + 1], &sm.G[row][col], &sm.Gl[row][col]);
+      }
+      *reinterpret_cast<float2 *>(rec + row * REC + SH::RX + col) = make_float2(Y[e], Y[e + 1]);
+      *reinterpret_cast<float2 *>(rec + row * REC + SH::RG + col) = make_float2(A[e], A[e + 1]);
+    }
+  }
+
+  // acc += (Ah + Al) (Wh + Wl)^T over K (no lo*lo term), W row-major [n][k].
+  template <int K, int NTW>
+  __device__ static __forceinline__ void fwd_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *Ah,
+                                                  const __nv_bfloat16 *Al, int lda,
+                                                  const __nv_bfloat16 *Wh,
+                                                  const __nv_bfloat16 *Wl, int ldw, int lane) {
+    warp_tile_gemm<K, NTW>(acc, Ah, lda, Wh, ldw, lane);
+    warp_tile_gemm<K, NTW>(acc, Al, lda, Wh, ldw, lane);
+    if (Wl) warp_tile_gemm<K, NTW>(acc, Ah, lda, Wl, ldw, lane);
+  }
+  // acc += (Ah + Al) (Wh + Wl) over K, W row-major [k][n] (transposed loads).
+  template <int K, int NTW>
+  __device__ static __forceinline__ void vjp_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *Ah,
+                                                  const __nv_bfloat16 *Al, int lda,
+                                                  const __nv_bfloat16 *Wh,
+                                                  const __nv_bfloat16 *Wl, int ldw, int n0,
+                                                  int lane) {
+    warp_tile_gemm_bt<K, NTW>(acc, Ah, lda, Wh, ldw, n0, lane);
+    warp_tile_gemm_bt<K, NTW>(acc, Al, lda, Wh, ldw, n0, lane);
+    if (Wl) warp_tile_gemm_bt<K, NTW>(acc, Ah, lda, Wl, ldw, n0, lane);
+  }
+
+  // Hidden-tile epilogue helper: write v to R (split) and to the record.
+  __device__ static __forceinline__ void put_hidden(Sm &sm, int which, int row, int col,
+                                                    float v0, float v1, float *rec, int roff) {
+    if constexpr (PRECISE) {
+      auto R = which == 1 ? sm.R1 : sm.R2;
+      R[row][col] = v0;
+      R[row][col + 1] = v1;
+    } else {
+      if (which == 1)
+        store_split2(v0, v1, &sm.R1[row][col], &sm.R1l[row][col]);
+      else
+        store_split2(v0, v1, &sm.R2[row][col], &sm.R2l[row][col]);
+    }
+    *reinterpret_cast<float2 *>(rec + row * REC + roff + col) = make_float2(v0, v1);
+  }
+
+  // F = MLP(X) and GY = A^T dMLP/dX (owned layout) with the stage records.
+  // X and G must have been written and synchronised.  Ends with every warp
+  // past its last read of R1 only after the caller's next barrier.
+  __device__ static void eval(Sm &sm, const float *P, const BsParams &Q, float (&F)[NE],
+                              float (&GY)[NE], float *rec, int tid, int warp, int lane) {
+    if constexpr (PRECISE) {
+      const float *W0 = P + SH::OW0, *W1 = P + SH::OW1, *W2 = P + SH::OW2;
+      for (int i = tid; i < M * H; i += SH::THREADS) {
+        const int r = i / H, n = i % H;
+        float a = sm.b0[n];
+        for (int k = 0; k < D; k++) a = fmaf(sm.X[r][k], __ldg(W0 + n * D + k), a);
+        const float v = tanhf(a);
+        sm.R1[r][n] = v;
+        rec[r * REC + SH::RH1 + n] = v;
+      }
+      __syncthreads();
+      for (int i = tid; i < M * H; i += SH::THREADS) {
+        const int r = i / H, n = i % H;
+        float a = sm.b1[n];
+        for (int k = 0; k < H; k++) a = fmaf(sm.R1[r][k], __ldg(W1 + n * H + k), a);
+        const float v = tanhf(a);
+        sm.R2[r][n] = v;
+        rec[r * REC + SH::RH2 + n] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        float a = sm.b2[col];
+        for (int k = 0; k < H; k++) a = fmaf(sm.R2[row][k], __ldg(W2 + col * H + k), a);
+        F[e] = a;
+      }
+      __syncthreads();
+      // dz1 = (G W2) * (1 - h2^2), in place of h2
+      for (int i = tid; i < M * H; i += SH::THREADS) {
+        const int r = i / H, n = i % H;
+        float a = 0.f;
+        for (int d = 0; d < D; d++) a = fmaf(sm.G[r][d], __ldg(W2 + d * H + n), a);
+        const float h2 = sm.R2[r][n];
+        const float v = a * (1.f - h2 * h2);
+        sm.R2[r][n] = v;
+        rec[r * REC + SH::RZ1 + n] = v;
+      }
+      __syncthreads();
+      // dz0 = (dz1 W1) * (1 - h1^2), in place of h1
+      for (int i = tid; i < M * H; i += SH::THREADS) {
+        const int r = i / H, n = i % H;
+        float a = 0.f;
+        for (int o = 0; o < H; o++) a = fmaf(sm.R2[r][o], __ldg(W1 + o * H + n), a);
+        const float h1 = sm.R1[r][n];
+        const float v = a * (1.f - h1 * h1);
+        sm.R1[r][n] = v;
+        rec[r * REC + SH::RZ0 + n] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        float a = 0.f;
+        for (int o = 0; o < H; o++) a = fmaf(sm.R1[row][o], __ldg(W0 + o * D + col), a);
+        GY[e] = a;
+      }
+    } else {
+      const int g = lane >> 2, c = lane & 3;
+      const int th0 = warp * SH::TPWH, mth = th0 / SH::NTH, nth0 = th0 % SH::NTH;
+      const int to0 = warp * SH::TPW, mto = to0 / SH::NT, nto0 = to0 % SH::NT;
+      {  // layer 0: h1 = tanh(X W0^T + b0) -> R1
+        float acc[SH::TPWH][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        if constexpr (SH::GFRAG)
+          gemm_gfrag<D, SH::TPWH>(acc, &sm.X[mth * 16][0], &sm.Xl[mth * 16][0], SH::PD, Q.w0f,
+                                  nth0, lane);
+        else
+          fwd_gemm<D, SH::TPWH>(acc, &sm.X[mth * 16][0], &sm.Xl[mth * 16][0], SH::PD,
+                                &sm.W0[nth0 * 8][0], &sm.W0l[nth0 * 8][0], SH::PD, lane);
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) {
+          const int col = (nth0 + j) * 8 + 2 * c, r0 = mth * 16 + g;
+          const float bb0 = sm.b0[col], bb1 = sm.b0[col + 1];
+          put_hidden(sm, 1, r0, col, tanhf(acc[j][0] + bb0), tanhf(acc[j][1] + bb1), rec,
+                     SH::RH1);
+          put_hidden(sm, 1, r0 + 8, col, tanhf(acc[j][2] + bb0), tanhf(acc[j][3] + bb1), rec,
+                     SH::RH1);
+        }
+      }
+      __syncthreads();
+      {  // layer 1: h2 = tanh(R1 W1^T + b1) -> R2
+        float acc[SH::TPWH][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        const __nv_bfloat16 *w1l = nullptr;
+        if constexpr (SH::WSPLIT) w1l = &sm.W1l[nth0 * 8][0];
+        fwd_gemm<H, SH::TPWH>(acc, &sm.R1[mth * 16][0], &sm.R1l[mth * 16][0], SH::PH,
+                              &sm.W1[nth0 * 8][0], w1l, SH::PH, lane);
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) {
+          const int col = (nth0 + j) * 8 + 2 * c, r0 = mth * 16 + g;
+          const float bb0 = sm.b1[col], bb1 = sm.b1[col + 1];
+          put_hidden(sm, 2, r0, col, tanhf(acc[j][0] + bb0), tanhf(acc[j][1] + bb1), rec,
+                     SH::RH2);
+          put_hidden(sm, 2, r0 + 8, col, tanhf(acc[j][2] + bb0), tanhf(acc[j][3] + bb1), rec,
+                     SH::RH2);
+        }
+      }
+      __syncthreads();
+      {  // layer 2: F = R2 W2^T + b2 (owned layout)
+        float acc[SH::TPW][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        if constexpr (SH::GFRAG)
+          gemm_gfrag<H, SH::TPW>(acc, &sm.R2[mto * 16][0], &sm.R2l[mto * 16][0], SH::PH, Q.w2f,
+                                 nto0, lane);
+        else
+          fwd_gemm<H, SH::TPW>(acc, &sm.R2[mto * 16][0], &sm.R2l[mto * 16][0], SH::PH,
+                               &sm.W2[nto0 * 8][0], &sm.W2l[nto0 * 8][0], SH::PH, lane);
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          int row, col;
+          elem_rc<SH>(e, warp, lane, row, col);
+          F[e] = acc[e >> 2][e & 3] + sm.b2[col];
+        }
+      }
+      __syncthreads();  // every warp has read h2 as an operand
+      {  // dz1 = (G W2) * (1 - h2^2) -> R2 in place
+        float acc[SH::TPWH][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        if constexpr (SH::GFRAG)
+          gemm_gfrag<D, SH::TPWH>(acc, &sm.G[mth * 16][0], &sm.Gl[mth * 16][0], SH::PD, Q.w2v,
+                                  nth0, lane);
+        else
+          vjp_gemm<D, SH::TPWH>(acc, &sm.G[mth * 16][0], &sm.Gl[mth * 16][0], SH::PD,
+                                &sm.W2[0][0], &sm.W2l[0][0], SH::PH, nth0 * 8, lane);
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++)
+#pragma unroll
+          for (int hr = 0; hr < 2; hr++) {
+            const int row = mth * 16 + g + hr * 8, col = (nth0 + j) * 8 + 2 * c;
+            const float a0 = __bfloat162float(sm.R2[row][col]) + __bfloat162float(sm.R2l[row][col]);
+            const float a1 =
+                __bfloat162float(sm.R2[row][col + 1]) + __bfloat162float(sm.R2l[row][col + 1]);
+            put_hidden(sm, 2, row, col, acc[j][2 * hr] * (1.f - a0 * a0),
+                       acc[j][2 * hr + 1] * (1.f - a1 * a1), rec, SH::RZ1);
+          }
+      }
+      __syncthreads();
+      {  // dz0 = (R2 W1) * (1 - h1^2) -> R1 in place
+        float acc[SH::TPWH][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        const __nv_bfloat16 *w1l = nullptr;
+        if constexpr (SH::WSPLIT) w1l = &sm.W1l[0][0];
+        vjp_gemm<H, SH::TPWH>(acc, &sm.R2[mth * 16][0], &sm.R2l[mth * 16][0], SH::PH,
+                              &sm.W1[0][0], w1l, SH::PH, nth0 * 8, lane);
+#pragma unroll
+        for (int j = 0; j < SH::TPWH; j++)
+#pragma unroll
+          for (int hr = 0; hr < 2; hr++) {
+            const int row = mth * 16 + g + hr * 8, col = (nth0 + j) * 8 + 2 * c;
+            const float a0 = __bfloat162float(sm.R1[row][col]) + __bfloat162float(sm.R1l[row][col]);
+            const float a1 =
+                __bfloat162float(sm.R1[row][col + 1]) + __bfloat162float(sm.R1l[row][col + 1]);
+            put_hidden(sm, 1, row, col, acc[j][2 * hr] * (1.f - a0 * a0),
+                       acc[j][2 * hr + 1] * (1.f - a1 * a1), rec, SH::RZ0);
+          }
+      }
+      __syncthreads();
+      {  // GY = R1 W0 (owned layout)
+        float acc[SH::TPW][4];
+#pragma unroll
+        for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+        if constexpr (SH::GFRAG)
+          gemm_gfrag<H, SH::TPW>(acc, &sm.R1[mto * 16][0], &sm.R1l[mto * 16][0], SH::PH, Q.w0v,
+                                 nto0, lane);
+        else
+          vjp_gemm<H, SH::TPW>(acc, &sm.R1[mto * 16][0], &sm.R1l[mto * 16][0], SH::PH,
+                               &sm.W0[0][0], &sm.W0l[0][0], SH::PD, nto0 * 8, lane);
+#pragma unroll
+        for (int e = 0; e < NE; e++) GY[e] = acc[e >> 2][e & 3];
+      }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// The parameter pass of one row and one layer W [NO][NI], b [NO]: stage
+// vectors u (length NO, record offset UOFF) and v (length NI, VOFF).
+// NORM: a1 = a0 + da written to the candidate buffer, returns this thread's
+// share of sum (err / (atol + rtol max(|a0|, |a1|)))^2.  Otherwise da is added
+// to the CTA partial (Kahan).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void kahan4(float *sum, float *comp, const float (&x)[4]) {
+  float4 s = *reinterpret_cast<float4 *>(sum), c = *reinterpret_cast<float4 *>(comp);
+  float sv[4] = {s.x, s.y, s.z, s.w}, cv[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const float y = x[q] - cv[q];
+    const float t = sv[q] + y;
+    cv[q] = (t - sv[q]) - y;
+    sv[q] = t;
+  }
+  *reinterpret_cast<float4 *>(sum) = make_float4(sv[0], sv[1], sv[2], sv[3]);
+  *reinterpret_cast<float4 *>(comp) = make_float4(cv[0], cv[1], cv[2], cv[3]);
+}
+
+__device__ __forceinline__ float scaled_sq(float a0, float a1, float err, float rtol,
+                                           float atol) {
+  // pid.py:475-492 (a NaN candidate falls back to a0 for the scale);
+  // _integrate.py:386 (a NaN error counts as infinite).
+  const float m = fmaxf(fabsf(a0), fabsf(isnan(a1) ? a0 : a1));
+  const float s = isnan(err) ? INFINITY : __fdividef(err, fmaf(m, rtol, atol));
+  return s * s;
+}
+
+template <class SH, int SOLVER, int NO, int NI, int UOFF, int VOFF, int WOFF, int BOFF, bool NORM>
+__device__ __forceinline__ float theta_layer(float (*cf)[16], const float *rec_r, float h,
+                                             const float *a0, float *a1, float *psum,
+                                             float *pcomp, float rtol, float atol, int tid) {
+  using TB = Tab<SOLVER>;
+  constexpr int S = TB::S, STR = SH::M * SH::REC;
+  // 1. per-output coefficients: cf[o][j] = -h b_j u_j[o], cf[o][8 + j] = -h e_j u_j[o]
+  for (int o = tid; o < NO; o += SH::THREADS) {
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const float u = -h * rec_r[j * STR + UOFF + o];
+      cf[o][j] = float(TB::b(j)) * u;
+      cf[o][8 + j] = float(TB::e(j)) * u;
+    }
+  }
+  __syncthreads();
+  constexpr int TPR = NI / 4, RPI = SH::THREADS / TPR;
+  static_assert(SH::THREADS % TPR == 0, "parameter pass split");
+  const int i4 = (tid % TPR) * 4, orow = tid / TPR;
+  float v[S][4];
+#pragma unroll
+  for (int j = 0; j < S; j++) {
+    const float4 t = *reinterpret_cast<const float4 *>(rec_r + j * STR + VOFF + i4);
+    v[j][0] = t.x;
+    v[j][1] = t.y;
+    v[j][2] = t.z;
+    v[j][3] = t.w;
+  }
+  float accn = 0.f;
+#pragma unroll 4
+  for (int o = orow; o < NO; o += RPI) {
+    const int p = WOFF + o * NI + i4;
+    float x0[4] = {0.f, 0.f, 0.f, 0.f};
+    if (NORM && a0) {
+      const float4 t = __ldcs(reinterpret_cast<const float4 *>(a0 + p));
+      x0[0] = t.x;
+      x0[1] = t.y;
+      x0[2] = t.z;
+      x0[3] = t.w;
+    }
+    float db[4], de[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) db[q] = de[q] = 0.f;
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const float cb = cf[o][j], ce = cf[o][8 + j];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (TB::b(j) != 0.0) db[q] = fmaf(cb, v[j][q], db[q]);
+        if (TB::e(j) != 0.0) de[q] = fmaf(ce, v[j][q], de[q]);
+      }
+    }
+    if constexpr (NORM) {
+      float x1[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        x1[q] = x0[q] + db[q];
+        accn += scaled_sq(x0[q], x1[q], de[q], rtol, atol);
+      }
+      __stcs(reinterpret_cast<float4 *>(a1 + p), make_float4(x1[0], x1[1], x1[2], x1[3]));
+    } else {
+      kahan4(psum + p, pcomp + p, db);
+    }
+  }
+  // biases (v = 1)
+  for (int o = tid; o < NO; o += SH::THREADS) {
+    float db = 0.f, de = 0.f;
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      db += cf[o][j];
+      de += cf[o][8 + j];
+    }
+    const int p = BOFF + o;
+    if constexpr (NORM) {
+      const float x0 = a0 ? a0[p] : 0.f;
+      const float x1 = x0 + db;
+      a1[p] = x1;
+      accn += scaled_sq(x0, x1, de, rtol, atol);
+    } else {
+      kahan_add(psum + p, pcomp + p, db);
+    }
+  }
+  __syncthreads();  // cf is rewritten by the next layer
+  return accn;
+}
+
+template <class SH, int SOLVER, bool NORM>
+__device__ __forceinline__ float theta_pass(float (*cf)[16], const float *rec_r, float h,
+                                            const float *a0, float *a1, float *psum,
+                                            float *pcomp, float rtol, float atol, int tid) {
+  constexpr int D = SH::D, H = SH::H;
+  float s = 0.f;
+  s += theta_layer<SH, SOLVER, H, D, SH::RZ0, SH::RX, SH::OW0, SH::OB0, NORM>(
+      cf, rec_r, h, a0, a1, psum, pcomp, rtol, atol, tid);
+  s += theta_layer<SH, SOLVER, H, H, SH::RZ1, SH::RH1, SH::OW1, SH::OB1, NORM>(
+      cf, rec_r, h, a0, a1, psum, pcomp, rtol, atol, tid);
+  s += theta_layer<SH, SOLVER, D, H, SH::RG, SH::RH2, SH::OW2, SH::OB2, NORM>(
+      cf, rec_r, h, a0, a1, psum, pcomp, rtol, atol, tid);
+  return s;
+}
+
+// Block-wide sum of one value per thread, returned to every thread.
+template <class SH>
+__device__ __forceinline__ float block_sum(float *red, float x, int tid) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if ((tid & 31) == 0) red[tid >> 5] = x;
+  __syncthreads();
+  float t = 0.f;
+#pragma unroll
+  for (int w = 0; w < SH::WARPS; w++) t += red[w];
+  __syncthreads();
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// Per-row scalar logic (one thread per row).
+// ---------------------------------------------------------------------------
+template <int M>
+__device__ __forceinline__ bool bs_running(const BsRows<M> &R, int r, int max_steps) {
+  return R.active[r] && order_key(R.tprev[r]) < order_key(R.te[r]) &&
+         R.sres[r] == GBDX_SUCCESSFUL && R.nseg[r] < max_steps;
+}
+
+// Advance row r from segment jold to the next segment that takes a step
+// (skipping empty ones): its times and the controller's initial step
+// (_integrate.py:1252-1265, pid.py:316-392, constant.py:30-57).  Sets seg and
+// done (no segment left).
+template <int M>
+__device__ void bs_next_segment(BsRows<M> &R, int r, const SolveParams &P) {
+  const int64_t i = R.idx[r];
+  const double *T = P.save_ts + i * P.n_save;
+  const int64_t ti = i * P.time_stride;
+  const double t0 = P.t0[ti];
+  const int jlo = P.save_t0 ? 1 : 0;
+  const int dir = R.dir[r];
+  int j = R.jold[r] - 1;
+  for (; j >= jlo; j--) {
+    const double ts_ = dir * T[j], te = dir * (j >= 1 ? T[j - 1] : t0);
+    double tn;
+    if (P.controller == GBDX_PID) {
+      if (R.firstseg[r] || !P.dt0) {
+        double hh = P.dt0 ? fabs(P.dt0[ti]) : 0.01;
+        if (P.has_dtmax) hh = fmin(hh, P.dtmax);
+        if (P.has_dtmin) hh = fmax(hh, P.dtmin);
+        tn = ts_ + hh;
+      } else {
+        tn = ts_ + fabs(P.dt0[ti]);
+      }
+      if (R.firstseg[r]) {
+        R.hist1[r] = 0.f;
+        R.hist2[r] = 0.f;
+        R.at_dtmin[r] = 0;
+      }
+    } else {
+      const double h0 = fabs(P.dt0[ti]);
+      if (R.firstseg[r]) {
+        R.sc[r] = 1;
+        R.nc[r] = (int)ceil((te - ts_) / next_up(h0));
+        R.t0s[r] = ts_;
+        R.t1s[r] = te;
+      }
+      tn = ts_ + h0;
+    }
+    R.firstseg[r] = 0;
+    R.tprev[r] = ts_;
+    R.te[r] = te;
+    R.tnext[r] = fmin(tn, te);
+    R.dtc[r] = R.tnext[r] - ts_;
+    R.floor_te[r] = t1_clip_floor(te);
+    R.nseg[r] = 0;
+    R.first[r] = 1;
+    R.sres[r] = GBDX_SUCCESSFUL;
+    if (order_key(ts_) < order_key(te)) break;
+  }
+  R.seg[r] = j;
+  R.done[r] = j < jlo;
+}
+
+// The controller's decision for row r (pid.py:394-567, constant.py:59-104,
+// _integrate.py:410-413) on the sum of squared scaled errors R.acc over
+// n_norm components.
+template <int M>
+__device__ void bs_row_control(BsRows<M> &R, int r, float n_norm, const SolveParams &P) {
+  const double dt = R.dtc[r];
+  bool keep;
+  double nt0, nt1, dtn;
+  if (P.controller == GBDX_PID) {
+    const float acc = R.acc[r];
+    keep = acc < n_norm;
+    const float lg = 0.5f * (log2f(n_norm) - __log2f(acc));
+    float ex = 0.f;
+    if (P.c1 != 0.0) ex += float(P.c1) * lg;
+    if (P.c2 != 0.0) ex += float(P.c2) * R.hist1[r];
+    if (P.c3 != 0.0) ex += float(P.c3) * R.hist2[r];
+    float factor = float(P.safety) * exp2f(ex);
+    const float hnew = isinf(lg) ? 0.f : lg;
+    if (P.has_dtmin) keep = keep || R.at_dtmin[r];
+    const float fmn = keep ? 1.f : float(P.factormin);
+    const float fmx = keep ? float(P.factormax) : float(P.safety);
+    factor = fminf(fmaxf(factor, fmn), fmx);
+    dtn = dt * double(factor);
+    if (P.has_dtmax) dtn = fmin(dtn, P.dtmax);
+    if (P.has_dtmin) {
+      if (!P.force_dtmin && dtn < P.dtmin && R.sres[r] == GBDX_SUCCESSFUL)
+        R.sres[r] = GBDX_DT_MIN_REACHED;
+      if (R.at_dtmin[r] && factor == 1.f) dtn = P.dtmin;
+      R.at_dtmin[r] = dtn <= P.dtmin;
+      dtn = fmax(dtn, P.dtmin);
+    }
+    nt0 = keep ? R.tnext[r] : R.tprev[r];
+    nt1 = nt0 + dtn;
+    if (keep) {
+      R.hist2[r] = R.hist1[r];
+      R.hist1[r] = hnew;
+    }
+  } else {
+    keep = true;
+    const int s2 = R.sc[r] + 1;
+    double tn = R.t0s[r] + (R.t1s[r] - R.t0s[r]) * (double(s2) / double(R.nc[r]));
+    if (s2 == R.nc[r]) tn = R.t1s[r];
+    R.sc[r] = s2;
+    nt0 = R.tnext[r];
+    nt1 = tn;
+  }
+  if (!(nt0 < R.te[r])) nt0 = R.te[r];
+  if (order_key(nt1) > order_key(R.floor_te[r])) nt1 = keep ? R.te[r] : nt0 + 0.5 * (R.te[r] - nt0);
+  dtn = nt1 - nt0;
+  R.keep[r] = keep;
+  if (keep) {
+    R.nacc[r]++;
+    R.first[r] = 0;
+  } else {
+    R.nrej[r]++;
+  }
+  R.nsteps[r]++;
+  R.nseg[r]++;
+  R.tprev[r] = nt0;
+  R.tnext[r] = nt1;
+  R.dtc[r] = dtn;
+}
+
+// ---------------------------------------------------------------------------
+// The kernel.
+// ---------------------------------------------------------------------------
+template <int SOLVER, int D, int H, bool PRECISE>
+__global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, BsParams Q) {
+  using SH = BsShape<D, H>;
+  using FLD = BsField<SH, PRECISE>;
+  using Sm = typename FLD::Sm;
+  using TB = Tab<SOLVER>;
+  constexpr int S = TB::S, NE = SH::NE, M = SH::M, REC = SH::REC, NP = SH::NP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Sm &sm = *reinterpret_cast<Sm *>(smem_raw);
+  BsRows<M> &R = sm.rows;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float *W = P.mlp;
+  float *rec = Q.rec + size_t(blockIdx.x) * S * M * REC;
+  float *psum = Q.psum + size_t(blockIdx.x) * NP;
+  float *pcomp = Q.pcomp + size_t(blockIdx.x) * NP;
+  float *ath = Q.track ? Q.ath + size_t(blockIdx.x) * M * 2 * NP : nullptr;
+  const float rtol = float(P.rtol), atol = float(P.atol);
+
+  FLD::stage(sm, W, tid);
+  if (tid < M) {
+    R.active[tid] = 0;
+    R.want[tid] = 1;
+    R.live[tid] = 0;
+  }
+  __syncthreads();
+
+  float Y0[NE], A0[NE], F0[NE], GY0[NE];
+#pragma unroll
+  for (int e = 0; e < NE; e++) Y0[e] = A0[e] = F0[e] = GY0[e] = 0.f;
+
+  // Segment transitions: finished segments advance (adding the cotangents of
+  // the saves they pass), finished rows write their outputs and refill.
+  auto transitions = [&]() {
+    while (true) {
+      int need = 0;
+      if (tid < M) {
+        const int r = tid;
+        R.trans[r] = 0;
+        if (R.active[r] && !bs_running(R, r, P.max_steps)) {
+          int sres = R.sres[r];
+          if (sres == GBDX_SUCCESSFUL && order_key(R.tprev[r]) < order_key(R.te[r]))
+            sres = GBDX_MAX_STEPS_REACHED;
+          if (R.result[r] == GBDX_SUCCESSFUL) R.result[r] = sres;
+          R.jold[r] = R.seg[r];
+          R.trans[r] = 1;
+          R.newtraj[r] = 0;
+        } else if (!R.active[r] && R.want[r]) {
+          const unsigned long long q = atomicAdd(P.queue, 1ull);
+          if (q < (unsigned long long)P.batch) {
+            const int64_t i = P.order ? (int64_t)P.order[q] : (int64_t)q;
+            const int64_t ti = i * P.time_stride;
+            R.idx[r] = i;
+            R.dir[r] = (P.t0[ti] < P.t1[ti]) ? -1 : 1;
+            R.jold[r] = P.n_save;
+            R.firstseg[r] = 1;
+            R.result[r] = GBDX_SUCCESSFUL;
+            R.nsteps[r] = R.nacc[r] = R.nrej[r] = 0;
+            R.cur[r] = 0;
+            R.zero[r] = 1;
+            R.active[r] = 1;
+            R.trans[r] = 1;
+            R.newtraj[r] = 1;
+          } else {
+            R.want[r] = 0;
+          }
+        }
+        if (R.trans[r]) bs_next_segment(R, r, P);
+        need = R.trans[r];
+      }
+      if (!__syncthreads_or(need)) break;
+      // element pass: a += dL/dys over the saves passed, y from the new save
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        if (R.trans[row]) {
+          const int64_t i = R.idx[row];
+          if (R.newtraj[row]) A0[e] = 0.f;
+          const int jn = R.seg[row] > 0 ? R.seg[row] : 0;
+          for (int jj = jn; jj < R.jold[row]; jj++)
+            A0[e] += Q.grad_ys[(i * P.n_save + jj) * D + col];
+          if (R.done[row]) {
+            Q.grad_y0[i * D + col] = A0[e];
+          } else {
+            Y0[e] = Q.ys[(i * P.n_save + R.seg[row]) * D + col];
+          }
+        }
+      }
+      __syncthreads();
+      // finished rows: results, the a_theta fold, a fresh trajectory next time
+      for (int r = 0; r < M; r++) {
+        if (!(R.trans[r] && R.done[r])) continue;
+        if (Q.track && !R.zero[r]) {
+          const float *a = ath + (size_t(r) * 2 + R.cur[r]) * NP;
+          for (int p = tid * 4; p < NP; p += SH::THREADS * 4) {
+            const float4 t = __ldcs(reinterpret_cast<const float4 *>(a + p));
+            const float x[4] = {t.x, t.y, t.z, t.w};
+            kahan4(psum + p, pcomp + p, x);
+          }
+        }
+      }
+      if (tid < M && R.trans[tid] && R.done[tid]) {
+        const int64_t i = R.idx[tid];
+        P.result_out[i] = R.result[tid];
+        P.stats_out[i * 3 + 0] = R.nsteps[tid];
+        P.stats_out[i * 3 + 1] = R.nacc[tid];
+        P.stats_out[i * 3 + 2] = R.nrej[tid];
+        R.active[tid] = 0;
+      }
+      __syncthreads();
+    }
+  };
+
+  transitions();
+  float KY[S][NE], KA[S][NE], Yi[NE], Ai[NE], F[NE], GY[NE];
+  while (__syncthreads_or(tid < M && R.active[tid])) {
+    // ---- one lockstep step ---------------------------------------------------
+    int first_live = 0;
+    if (tid < M) {
+      const int live = R.active[tid];
+      first_live = live && R.first[tid];
+      R.live[tid] = live;
+      R.acc[tid] = 0.f;
+      R.nan_y[tid] = R.nan_a[tid] = 0;
+      // control h = dir * dt as FP32 (WrapTerm, _term.py:742-745)
+      R.h[tid] = live ? float(R.dir[tid] > 0 ? R.dtc[tid] : -R.dtc[tid]) : 0.f;
+    }
+    const int any_first = __syncthreads_or(first_live);
+    float hrow[NE];
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      int row, col;
+      elem_rc<SH>(e, warp, lane, row, col);
+      hrow[e] = R.h[row];
+    }
+#pragma unroll
+    for (int i = 0; i < S; i++) {
+      float *rec_s = rec + size_t(i) * M * REC;
+      if (i == 0) {
+        if (!TB::FSAL || any_first) {
+          FLD::put(sm, Y0, A0, rec_s, warp, lane);
+          __syncthreads();
+          FLD::eval(sm, W, Q, F, GY, rec_s, tid, warp, lane);
+        } else {
+#pragma unroll
+          for (int e = 0; e < NE; e++) {
+            F[e] = F0[e];
+            GY[e] = GY0[e];
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          Yi[e] = Y0[e];
+          Ai[e] = A0[e];
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+          float a = Y0[e], b = A0[e];
+#pragma unroll
+          for (int j = 0; j < i; j++)
+            if (TB::a(i, j) != 0.0) {
+              a = fmaf(float(TB::a(i, j)), KY[j][e], a);
+              b = fmaf(float(TB::a(i, j)), KA[j][e], b);
+            }
+          Yi[e] = a;
+          Ai[e] = b;
+        }
+        __syncthreads();  // the previous products have finished reading X, G, R1
+        FLD::put(sm, Yi, Ai, rec_s, warp, lane);
+        __syncthreads();
+        FLD::eval(sm, W, Q, F, GY, rec_s, tid, warp, lane);
+      }
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        KY[i][e] = F[e] * hrow[e];
+        KA[i][e] = -GY[e] * hrow[e];
+      }
+    }
+    // y1, a1, error estimates, the (y, a) part of the error norm
+    float Y1[NE], A1[NE], ErY[NE], ErA[NE];
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      if constexpr (TB::SSAL) {
+        Y1[e] = Yi[e];
+        A1[e] = Ai[e];
+      } else {
+        float a = Y0[e], b = A0[e];
+#pragma unroll
+        for (int j = 0; j < S; j++) {
+          a = fmaf(float(TB::b(j)), KY[j][e], a);
+          b = fmaf(float(TB::b(j)), KA[j][e], b);
+        }
+        Y1[e] = a;
+        A1[e] = b;
+      }
+      float ey = 0.f, ea = 0.f;
+#pragma unroll
+      for (int j = 0; j < S; j++)
+        if (TB::e(j) != 0.0) {
+          ey = fmaf(float(TB::e(j)), KY[j][e], ey);
+          ea = fmaf(float(TB::e(j)), KA[j][e], ea);
+        }
+      ErY[e] = isnan(ey) ? INFINITY : ey;
+      ErA[e] = isnan(ea) ? INFINITY : ea;
+    }
+    __syncthreads();  // every warp is past its last read of the stage operands
+    if (P.controller == GBDX_PID) {
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        if (isnan(Y1[e])) R.nan_y[row] = 1;
+        if (isnan(A1[e])) R.nan_a[row] = 1;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < SH::TPW; j++) {
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+          int row, col;
+          elem_rc<SH>(j * 4 + half * 2, warp, lane, row, col);
+          const bool ny = R.nan_y[row], na = R.nan_a[row];
+          float part = 0.f;
+#pragma unroll
+          for (int q = 0; q < 2; q++) {
+            const int e = j * 4 + half * 2 + q;
+            const float my = fmaxf(fabsf(Y0[e]), fabsf(ny ? Y0[e] : Y1[e]));
+            const float sy = __fdividef(ErY[e], fmaf(my, rtol, atol));
+            const float ma = fmaxf(fabsf(A0[e]), fabsf(na ? A0[e] : A1[e]));
+            const float sa = __fdividef(ErA[e], fmaf(ma, rtol, atol));
+            part = fmaf(sy, sy, part);
+            part = fmaf(sa, sa, part);
+          }
+          part += __shfl_xor_sync(0xffffffffu, part, 1);
+          part += __shfl_xor_sync(0xffffffffu, part, 2);
+          if ((lane & 3) == 0) atomicAdd(&R.acc[row], part);
+        }
+      }
+      __syncthreads();
+      // the a_theta part of the norm: one parameter pass per live row
+      if (Q.track) {
+        for (int r = 0; r < M; r++) {
+          if (!R.live[r]) continue;
+          const float *a0p = R.zero[r] ? nullptr : ath + (size_t(r) * 2 + R.cur[r]) * NP;
+          float *a1p = ath + (size_t(r) * 2 + (R.cur[r] ^ 1)) * NP;
+          const float s = theta_pass<SH, SOLVER, true>(sm.cf, rec + size_t(r) * REC, R.h[r],
+                                                       a0p, a1p, psum, pcomp, rtol, atol, tid);
+          const float tot = block_sum<SH>(sm.red, s, tid);
+          if (tid == 0) R.acc[r] += tot;
+        }
+        __syncthreads();
+      }
+    }
+    if (tid < M && R.live[tid]) bs_row_control(R, tid, Q.n_norm, P);
+    __syncthreads();
+    // accepted increments of untracked a_theta go straight to the partials
+    if (!Q.track) {
+      for (int r = 0; r < M; r++) {
+        if (!(R.live[r] && R.keep[r])) continue;
+        theta_pass<SH, SOLVER, false>(sm.cf, rec + size_t(r) * REC, R.h[r], nullptr, nullptr,
+                                      psum, pcomp, rtol, atol, tid);
+      }
+    }
+    // ---- accept: state, FSAL vectors and records, a_theta buffers --------------
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+      int row, col;
+      elem_rc<SH>(e, warp, lane, row, col);
+      if (R.live[row] && R.keep[row]) {
+        Y0[e] = Y1[e];
+        A0[e] = A1[e];
+        if (TB::FSAL) {
+          F0[e] = F[e];
+          GY0[e] = GY[e];
+        }
+      }
+    }
+    if constexpr (TB::FSAL) {
+      for (int r = 0; r < M; r++) {
+        if (!(R.live[r] && R.keep[r])) continue;
+        const float *src = rec + (size_t(S - 1) * M + r) * REC;
+        float *dst = rec + size_t(r) * REC;
+        for (int k = tid * 4; k < REC; k += SH::THREADS * 4)
+          *reinterpret_cast<float4 *>(dst + k) = *reinterpret_cast<const float4 *>(src + k);
+      }
+    }
+    __syncthreads();
+    if (tid < M && R.live[tid] && R.keep[tid] && Q.track) {
+      R.cur[tid] ^= 1;
+      R.zero[tid] = 0;
+    }
+    __syncthreads();
+    transitions();
+  }
+}
+
+}  // namespace gbdx

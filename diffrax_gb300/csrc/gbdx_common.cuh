@@ -306,6 +306,19 @@ struct SolveParams {
   int checkpoints;
 };
 
+// BacksolveAdjoint backward arguments.
+struct BsParams {
+  const float *ys;       // [batch, n_save, D] the forward's saved states
+  const float *grad_ys;  // [batch, n_save, D]
+  float *grad_y0;        // [batch, D]
+  float *psum, *pcomp;   // [n_cta, NP] Kahan partial gradients
+  float *rec;            // [n_cta, S, M, REC] stage records
+  float *ath;            // [n_cta, M, 2, NP] per-row a_theta (tracked norm only)
+  const uint2 *w0f, *w0v, *w2f, *w2v;  // B fragments (width 256)
+  int track;             // the error norm runs over a_theta
+  float n_norm;          // number of components in the error norm
+};
+
 // Backward (RecursiveCheckpointAdjoint) arguments.
 struct BwdParams {
   const float *grad_ys;   // [batch, n_save, D]

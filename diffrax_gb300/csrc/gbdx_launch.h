@@ -37,6 +37,24 @@ BwdEntry find_mlp_bwd_entry_d32h64(int solver, bool precise, bool sde);
 // grad[p] = compensated sum over CTAs of (psum - pcomp)[cta][p]
 cudaError_t launch_reduce_partials(const float *psum, const float *pcomp, int n_cta,
                                    int n_params, float *out, cudaStream_t s);
+// BacksolveAdjoint backward (MLP fields).
+struct BsParams;
+using BsLaunchFn = cudaError_t (*)(const SolveParams &, const BsParams &, int grid,
+                                   cudaStream_t);
+struct BsEntry {
+  BsLaunchFn launch;
+  BwdOccFn occupancy;
+  int rows;    // trajectories per CTA
+  int stages;  // RK stages (stage records per row)
+  int rec;     // floats per stage record
+  int gfrag;   // W0/W2 read as global B fragments
+};
+BsEntry find_backsolve_entry_d64h256(int solver, bool precise);
+BsEntry find_backsolve_entry_d64h128(int solver, bool precise);
+BsEntry find_backsolve_entry_d32h64(int solver, bool precise);
+// BF16 mma B fragments of B[k][n] = trans ? W[n][k] : W[k][n] (K x N).
+cudaError_t launch_frag_prep(const float *W, int ldw, int K, int N, int trans, uint2 *out,
+                             cudaStream_t s);
 OdeEntry find_mlp_plain_entry(int solver, int D, int H, bool sde);
 OdeEntry find_mlp_entry_d64h128(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d64h256(int solver, bool precise, bool sde);

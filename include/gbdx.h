@@ -21,8 +21,6 @@
  *   gbdx_backsolve_bwd    <- BacksolveAdjoint's backward pass
  *                            (diffrax/_adjoint.py:572-734, AdjointTerm
  *                            diffrax/_term.py:767-910)
- *   gbdx_vbt_increments   <- VirtualBrownianTree.evaluate(t0, t1)
- *                            (diffrax/_brownian/tree.py:325-354)
  */
 #ifndef GBDX_H_
 #define GBDX_H_
@@ -163,6 +161,35 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    const void *params, const double *save_ts, const void *grad_ys,
                    void *grad_y0, void *grad_params, void *workspace,
                    size_t workspace_bytes, void *stream);
+
+/*
+ * Backward of a solve under BacksolveAdjoint (MLP fields, ODEs): reverse-time
+ * solves of the augmented state (y, a, a_theta) between adjacent saved times
+ * (diffrax/_adjoint.py:572-734) with the problem's solver and controller --
+ * create the problem with adjoint = GBDX_ADJ_BACKSOLVE and the backward's
+ * solver, controller and norm (desc.norm: GBDX_NORM_RMS runs the error norm
+ * over every a_theta component as the reference's default does,
+ * GBDX_NORM_ADJOINT_SEMI over (y, a) only), and the forward's SaveAt.
+ *   t0, t1, dt0, time_stride : the forward's (dt0 may be NULL for PID).
+ *   save_ts     : device [batch, n_saves] FP64, the forward's ts_out.
+ *   ys          : device [batch, n_saves, dim] FP32, the forward's ys_out.
+ *   grad_ys     : device [batch, n_saves, dim] FP32 cotangent of ys.
+ *   params      : device FP32 field parameters (flat layout).
+ *   grad_y0     : device [batch, dim] FP32 output, dL/dy0.
+ *   grad_params : device [gbdx_param_count] FP32 output, dL/dparams summed
+ *                 over the batch with compensated (Kahan) accumulation.
+ *   result_out  : device [batch] int32, the first failing RESULTS code of the
+ *                 backward's solves (0 = successful).
+ *   stats_out   : device [batch, 3] int32, backward steps / accepted /
+ *                 rejected over all segments.
+ * The workspace is gbdx_workspace_size(problem, batch) bytes.
+ */
+int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
+                       const double *t1, const double *dt0, int64_t time_stride,
+                       const double *save_ts, const void *ys, const void *grad_ys,
+                       const void *params, void *grad_y0, void *grad_params,
+                       int32_t *result_out, int32_t *stats_out, void *workspace,
+                       size_t workspace_bytes, void *stream);
 
 /*
  * Forward solve for callers that cannot allocate device memory.  It has no

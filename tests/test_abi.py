@@ -108,6 +108,30 @@ def test_backsolve_kwargs_validation():
     dfx.BacksolveAdjoint(solver=dfx.Dopri5())
 
 
+def _mlp_fields(widths, solver, **kw):
+    W = [torch.zeros(widths[i + 1], widths[i]) for i in range(3)]
+    b = [torch.zeros(widths[i + 1]) for i in range(3)]
+    f = dfx.lower(dfx.ODETerm(dfx.MLPField(W, b)), solver,
+                  dfx.PIDController(rtol=1e-5, atol=1e-7), dfx.SaveAt(ts=[0.5, 1.0]),
+                  dim=widths[0], dtype=torch.float32, max_steps=64, n_ts=2,
+                  adjoint=dfx.BacksolveAdjoint())
+    f.update(kw)
+    return f
+
+
+def test_backsolve_problem_creation():
+    p = _lib.Problem(_mlp_fields([64, 256, 256, 64], dfx.Tsit5()))
+    assert p.param_count() == 64 * 256 + 256 + 256 * 256 + 256 + 256 * 64 + 64
+    _lib.Problem(_mlp_fields([32, 64, 64, 32], dfx.Heun()))
+    _lib.Problem(_mlp_fields([32, 64, 64, 32], dfx.Tsit5(), norm=1))
+    with pytest.raises(_lib.GbdxError, match="backsolve"):
+        _lib.Problem(_mlp_fields([64, 256, 256, 64], dfx.Heun()))
+    with pytest.raises(ValueError, match="norm"):
+        _lib.Problem(_mlp_fields([32, 64, 64, 32], dfx.Tsit5(), norm=5))
+    with pytest.raises(_lib.GbdxError, match="plain"):
+        _lib.Problem(_mlp_fields([32, 64, 64, 32], dfx.Tsit5(), kernel=1))
+
+
 def test_no_cpu_fallback():
     if torch.cuda.is_available():
         pytest.skip("a GPU is present")
