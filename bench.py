@@ -253,6 +253,97 @@ def workload_lotka_volterra(dev, flush, steps, warmup):
     return out
 
 
+def workload_backsolve(dev, flush, steps, warmup, terms_for, solver, ctrl, saveat, ts, y0,
+                       y0_d, params, desc, B, D):
+    """Forward + BacksolveAdjoint backward of loss = sum over the saved points of
+    mean(y^2): the reference's default rms_norm (a_theta in the error norm,
+    streamed from HBM) and adjoint_rms_seminorm.  Width 256 holds BF16
+    weights, so the oracle runs with the same BF16-rounded weights."""
+    import torch
+    import diffrax_gb300 as dfx
+    import oracle as O
+    from diffrax_gb300._integrate import Lowered
+    cores = os.cpu_count() or 1
+    p_bf16 = torch.tensor(params, dtype=torch.float32).to(torch.bfloat16).double().numpy()
+    # biases stay FP32 (only the weight matrices are BF16 operands)
+    widths = [64, 256, 256, 64]
+    off = 0
+    for i in range(3):
+        n_w = widths[i] * widths[i + 1]
+        p_bf16[off + n_w:off + n_w + widths[i + 1]] = params[off + n_w:off + n_w + widths[i + 1]]
+        off += n_w + widths[i + 1]
+    out = {}
+    for name, adj in (("rms_norm", dfx.BacksolveAdjoint()),
+                      ("seminorm", dfx.BacksolveAdjoint(stepsize_controller=dfx.PIDController(
+                          rtol=ctrl.rtol, atol=ctrl.atol, norm=dfx.adjoint_rms_seminorm)))):
+        low = Lowered(terms_for("bf16"), solver, 0.0, 1.0, None, y0_d, None, saveat, ctrl, adj,
+                      4096, "fused", 0, 0, want_grad=True)
+
+        def fwd_bwd():
+            ys_, ts_, _, _ = low.run_forward()
+            gys = ys_ * (2.0 / (B * D))
+            return low.run_backsolve(ts_, ys_, gys, low.params)
+        ms = _events_time(fwd_bwd, steps, warmup, flush)
+        gy0, gp, res, st = fwd_bwd()
+        n_g = 32
+        ys_, ts_, _, _ = low.run_forward()
+        ys_g = ys_[:n_g].double().cpu().numpy()
+        bdesc = O.make_desc(**dfx.oracle_fields(low.bwd_fields))
+        # the oracle gradient of the first n_g trajectories, from the same saves
+        gys = 2.0 * ys_g / (B * D)
+        t = time.perf_counter()
+        r = O.backsolve(bdesc, 0.0, 1.0, None, ts_[:n_g].cpu().numpy(), ys_g, gys,
+                        params=p_bf16, nthreads=cores)
+        dt_cpu = time.perf_counter() - t
+        gy0_g = gy0[:n_g].double().cpu().numpy()
+        ent = {"grads_per_s": B / (ms / 1e3), "ms": ms, "unit": "trajectory gradients/s",
+               "mean_backward_steps": float(st[:, 0].float().mean().item()),
+               "backward_failures": int((res != 0).sum().item()),
+               "dL_dy0_max_rel_err_vs_fp64_oracle": float(
+                   np.abs(gy0_g - r["grad_y0"]).max() / np.abs(r["grad_y0"]).max()),
+               "oracle_mean_backward_steps": float(r["stats"][:, 0].mean()),
+               "cpu_baseline": {"value": n_g / dt_cpu, "unit": "trajectory gradients/s",
+                                "cores": cores, "kind": "port",
+                                "sample": f"{n_g} trajectories backward only, FP64 oracle, "
+                                          f"{dt_cpu:.2f} s"}}
+        if name == "rms_norm":
+            # a_theta double buffer: read a_theta0 + write the candidate per row-step
+            n_par = int(low.params.numel())
+            ent["a_theta_stream_bytes"] = float(st[:, 0].double().sum().item()) * 2 * 4 * n_par
+            ent["a_theta_stream_GBps"] = ent["a_theta_stream_bytes"] / (ms / 1e3) / 1e9
+        out[f"backsolve_{name}"] = ent
+    return out
+
+
+def profile_backsolve(dev, B, seminorm, n):
+    """n forward + BacksolveAdjoint backward solves of the wide neural ODE
+    (64-256-256-64, Tsit5 PID(1e-5, 1e-7), 32 ts) at batch B, for ncu."""
+    import torch
+    import diffrax_gb300 as dfx
+    from diffrax_gb300._integrate import Lowered
+    widths = [64, 256, 256, 64]
+    Ws, bs = _mlp_np(widths, 22)
+    y0 = np.random.default_rng(23).standard_normal((B, 64)).astype(np.float32)
+    field = dfx.MLPField([torch.tensor(W, device=dev) for W in Ws],
+                         [torch.tensor(b, device=dev) for b in bs])
+    ctrl = dfx.PIDController(rtol=1e-5, atol=1e-7)
+    adj = dfx.BacksolveAdjoint(stepsize_controller=dfx.PIDController(
+        rtol=1e-5, atol=1e-7, norm=dfx.adjoint_rms_seminorm)) if seminorm else \
+        dfx.BacksolveAdjoint()
+    low = Lowered(dfx.ODETerm(field), dfx.Tsit5(), 0.0, 1.0, None,
+                  torch.tensor(y0, device=dev), None, dfx.SaveAt(ts=np.linspace(0, 1, 32)),
+                  ctrl, adj, 4096, "fused", 0, 0, want_grad=True)
+    for _ in range(n):
+        ys, ts, res, _ = low.run_forward()
+        _, _, bres, _ = low.run_backsolve(ts, ys, ys * (2.0 / ys.numel()), low.params)
+    torch.cuda.synchronize()
+    ok = bool((res == 0).all().item()) and bool((bres == 0).all().item())
+    print(json.dumps({"profile": "backsolve", "seminorm": seminorm, "solves": n,
+                      "all_successful": ok}))
+    if not ok:
+        sys.exit(1)
+
+
 def workload_neural(dev, flush, steps, warmup, kind):
     """Neural ODE (64-128-128-64, Tsit5 PID(1e-5, 1e-7), batch 8192, t1 save,
     RecursiveCheckpointAdjoint(64), loss mean y(t1)^2), the wide neural ODE
@@ -331,6 +422,8 @@ def workload_neural(dev, flush, steps, warmup, kind):
         lambda: O.solve(desc, 0.0, 1.0, dt0, y0[:512].astype(np.float64), params=params, ts=ts,
                         nthreads=cores), 512, cores)
     if kind == "wide":
+        out.update(workload_backsolve(dev, flush, steps, warmup, terms_for, solver, ctrl,
+                                      saveat, ts, y0, y0_d, params, desc, B, D))
         return out
     # forward + RecursiveCheckpointAdjoint backward of loss = mean(y(t1)^2)
     grad = lowered("fused", True)
@@ -369,8 +462,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the other configurations")
-    ap.add_argument("--profile", default=None, choices=["fused", "plain"],
-                    help="run warmup + steps eager solves of one kernel only (for ncu)")
+    ap.add_argument("--profile", default=None,
+                    choices=["fused", "plain", "backsolve", "backsolve_seminorm"],
+                    help="run warmup + steps eager solves of one kernel only (for ncu); "
+                         "backsolve*: forward + backward of the wide neural ODE at --batch")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -441,6 +536,10 @@ def main():
             ms_step = float(t.item())
         return ms_step, outs, clocks, wall
 
+    if args.profile and args.profile.startswith("backsolve"):
+        profile_backsolve(dev, B, args.profile == "backsolve_seminorm",
+                          args.warmup + args.steps)
+        return
     if args.profile:
         low = lowered(args.profile)
         for _ in range(args.warmup + args.steps):

@@ -108,7 +108,7 @@ int ws_layout(const gbdx_problem *p, int64_t batch, WsLayout *L) {
     off += up256(size_t(L->n_cta) * np * sizeof(float));
     L->track = bs_tracks(d);
     L->ath = off;
-    if (L->track) off += up256(size_t(L->n_cta) * p->bs.rows * 2 * np * sizeof(float));
+    off += up256(size_t(L->n_cta) * p->bs.rows * 2 * np * sizeof(float));
   }
   if (d.adjoint == GBDX_ADJ_RECURSIVE && p->bwd.launch) {
     const int C = d.checkpoints > 1 ? d.checkpoints : 2;
@@ -569,7 +569,7 @@ int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double 
   Q.psum = reinterpret_cast<float *>(w + L.psum);
   Q.pcomp = reinterpret_cast<float *>(w + L.pcomp);
   Q.rec = reinterpret_cast<float *>(w + L.rec);
-  Q.ath = L.track ? reinterpret_cast<float *>(w + L.ath) : nullptr;
+  Q.ath = reinterpret_cast<float *>(w + L.ath);
   Q.track = L.track ? 1 : 0;
   Q.n_norm = float(L.track ? 2 * D + np : 2 * D);
   cudaError_t e = cudaMemsetAsync(w + L.psum, 0, L.ath - L.psum, s);

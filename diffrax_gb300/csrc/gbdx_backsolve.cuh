@@ -29,8 +29,9 @@
 //     row's norm; the buffers flip on accept, and a finished row folds its
 //     a_theta into the CTA's Kahan partial gradient.
 //   * adjoint_rms_seminorm or ConstantStepSize: the norm does not see
-//     a_theta; after the decision the pass adds the accepted increments into
-//     the CTA's Kahan partial gradient.
+//     a_theta; after the decision the pass adds the accepted increments to
+//     the row's a_theta in place.
+// Either way a finished row folds its a_theta into the CTA's Kahan partial.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -96,23 +97,50 @@ struct BsWeights<SH, true> {
 template <class SH, bool PRECISE>
 struct BsSmem;
 
+// Stage operands (hi/lo BF16): X the stage input, G its cotangent a, R1 h1
+// then dz0, R2 h2 then dz1.
+template <class SH>
+struct BsAct {
+  __nv_bfloat16 X[SH::M][SH::PD], Xl[SH::M][SH::PD];
+  __nv_bfloat16 G[SH::M][SH::PD], Gl[SH::M][SH::PD];
+  __nv_bfloat16 R1[SH::M][SH::PH], R1l[SH::M][SH::PH];
+  __nv_bfloat16 R2[SH::M][SH::PH], R2l[SH::M][SH::PH];
+};
+// Operands of the tensor-core parameter pass of one row and layer:
+// o-side vectors U0 = -h u0, A2 = sum_j b_j du_j, A3 = sum_j e_j du_j and the
+// stage differences du_j = -h (u_j - u_0) (BF16, [o][k = j - 1]); i-side
+// vectors v0, B1 = v0 + sum_j b_j dv_j, B3 = sum_j e_j dv_j and b_j dv_j,
+// e_j dv_j (BF16, [k][i]).
+template <class SH>
+struct BsPassOps {
+  float U0[SH::H], A2[SH::H], A3[SH::H], v0[SH::H], B1[SH::H], B3[SH::H];
+  __nv_bfloat16 Du[SH::H][24];
+  __nv_bfloat16 Bb[16][SH::PH], Be[16][SH::PH];
+};
+
 template <class SH>
 struct BsSmem<SH, false> : BsWeights<SH, SH::GFRAG> {
   float b0[SH::H], b1[SH::H], b2[SH::D];
-  __nv_bfloat16 X[SH::M][SH::PD], Xl[SH::M][SH::PD];
-  __nv_bfloat16 G[SH::M][SH::PD], Gl[SH::M][SH::PD];
-  __nv_bfloat16 R1[SH::M][SH::PH], R1l[SH::M][SH::PH];  // h1, then dz0
-  __nv_bfloat16 R2[SH::M][SH::PH], R2l[SH::M][SH::PH];  // h2, then dz1
-  __align__(16) float cf[SH::H][16];                    // parameter-pass coefficients
+  union {  // the stage products and the parameter pass never overlap
+    BsAct<SH> a;
+    BsPassOps<SH> p;
+    float cf[SH::H][16];  // FP32 parameter-pass coefficients
+  };
   float red[SH::WARPS];
   BsRows<SH::M> rows;
+};
+
+// FP32 stage operands of the parity mode.
+template <class SH>
+struct BsActF32 {
+  float X[SH::M][SH::D + 1], G[SH::M][SH::D + 1];
+  float R1[SH::M][SH::H + 1], R2[SH::M][SH::H + 1];
 };
 
 template <class SH>
 struct BsSmem<SH, true> {
   float b0[SH::H], b1[SH::H], b2[SH::D];
-  float X[SH::M][SH::D + 1], G[SH::M][SH::D + 1];
-  float R1[SH::M][SH::H + 1], R2[SH::M][SH::H + 1];
+  BsActF32<SH> a;
   __align__(16) float cf[SH::H][16];
   float red[SH::WARPS];
   BsRows<SH::M> rows;
@@ -172,13 +200,13 @@ struct BsField {
       int row, col;
       elem_rc<SH>(e, warp, lane, row, col);
       if constexpr (PRECISE) {
-        sm.X[row][col] = Y[e];
-        sm.X[row][col + 1] = Y[e + 1];
-        sm.G[row][col] = A[e];
-        sm.G[row][col + 1] = A[e + 1];
+        sm.a.X[row][col] = Y[e];
+        sm.a.X[row][col + 1] = Y[e + 1];
+        sm.a.G[row][col] = A[e];
+        sm.a.G[row][col + 1] = A[e + 1];
       } else {
-        store_split2(Y[e], Y[e + 1], &sm.X[row][col], &sm.Xl[row][col]);
-        store_split2(A[e], A[e + 1], &sm.G[row][col], &sm.Gl[row][col]);
+        store_split2(Y[e], Y[e + 1], &sm.a.X[row][col], &sm.a.Xl[row][col]);
+        store_split2(A[e], A[e + 1], &sm.a.G[row][col], &sm.a.Gl[row][col]);
       }
       *reinterpret_cast<float2 *>(rec + row * REC + SH::RX + col) = make_float2(Y[e], Y[e + 1]);
       *reinterpret_cast<float2 *>(rec + row * REC + SH::RG + col) = make_float2(A[e], A[e + 1]);
@@ -211,14 +239,14 @@ struct BsField {
   __device__ static __forceinline__ void put_hidden(Sm &sm, int which, int row, int col,
                                                     float v0, float v1, float *rec, int roff) {
     if constexpr (PRECISE) {
-      auto R = which == 1 ? sm.R1 : sm.R2;
+      auto R = which == 1 ? sm.a.R1 : sm.a.R2;
       R[row][col] = v0;
       R[row][col + 1] = v1;
     } else {
       if (which == 1)
-        store_split2(v0, v1, &sm.R1[row][col], &sm.R1l[row][col]);
+        store_split2(v0, v1, &sm.a.R1[row][col], &sm.a.R1l[row][col]);
       else
-        store_split2(v0, v1, &sm.R2[row][col], &sm.R2l[row][col]);
+        store_split2(v0, v1, &sm.a.R2[row][col], &sm.a.R2l[row][col]);
     }
     *reinterpret_cast<float2 *>(rec + row * REC + roff + col) = make_float2(v0, v1);
   }
@@ -233,18 +261,18 @@ struct BsField {
       for (int i = tid; i < M * H; i += SH::THREADS) {
         const int r = i / H, n = i % H;
         float a = sm.b0[n];
-        for (int k = 0; k < D; k++) a = fmaf(sm.X[r][k], __ldg(W0 + n * D + k), a);
+        for (int k = 0; k < D; k++) a = fmaf(sm.a.X[r][k], __ldg(W0 + n * D + k), a);
         const float v = tanhf(a);
-        sm.R1[r][n] = v;
+        sm.a.R1[r][n] = v;
         rec[r * REC + SH::RH1 + n] = v;
       }
       __syncthreads();
       for (int i = tid; i < M * H; i += SH::THREADS) {
         const int r = i / H, n = i % H;
         float a = sm.b1[n];
-        for (int k = 0; k < H; k++) a = fmaf(sm.R1[r][k], __ldg(W1 + n * H + k), a);
+        for (int k = 0; k < H; k++) a = fmaf(sm.a.R1[r][k], __ldg(W1 + n * H + k), a);
         const float v = tanhf(a);
-        sm.R2[r][n] = v;
+        sm.a.R2[r][n] = v;
         rec[r * REC + SH::RH2 + n] = v;
       }
       __syncthreads();
@@ -253,7 +281,7 @@ struct BsField {
         int row, col;
         elem_rc<SH>(e, warp, lane, row, col);
         float a = sm.b2[col];
-        for (int k = 0; k < H; k++) a = fmaf(sm.R2[row][k], __ldg(W2 + col * H + k), a);
+        for (int k = 0; k < H; k++) a = fmaf(sm.a.R2[row][k], __ldg(W2 + col * H + k), a);
         F[e] = a;
       }
       __syncthreads();
@@ -261,10 +289,10 @@ struct BsField {
       for (int i = tid; i < M * H; i += SH::THREADS) {
         const int r = i / H, n = i % H;
         float a = 0.f;
-        for (int d = 0; d < D; d++) a = fmaf(sm.G[r][d], __ldg(W2 + d * H + n), a);
-        const float h2 = sm.R2[r][n];
+        for (int d = 0; d < D; d++) a = fmaf(sm.a.G[r][d], __ldg(W2 + d * H + n), a);
+        const float h2 = sm.a.R2[r][n];
         const float v = a * (1.f - h2 * h2);
-        sm.R2[r][n] = v;
+        sm.a.R2[r][n] = v;
         rec[r * REC + SH::RZ1 + n] = v;
       }
       __syncthreads();
@@ -272,10 +300,10 @@ struct BsField {
       for (int i = tid; i < M * H; i += SH::THREADS) {
         const int r = i / H, n = i % H;
         float a = 0.f;
-        for (int o = 0; o < H; o++) a = fmaf(sm.R2[r][o], __ldg(W1 + o * H + n), a);
-        const float h1 = sm.R1[r][n];
+        for (int o = 0; o < H; o++) a = fmaf(sm.a.R2[r][o], __ldg(W1 + o * H + n), a);
+        const float h1 = sm.a.R1[r][n];
         const float v = a * (1.f - h1 * h1);
-        sm.R1[r][n] = v;
+        sm.a.R1[r][n] = v;
         rec[r * REC + SH::RZ0 + n] = v;
       }
       __syncthreads();
@@ -284,7 +312,7 @@ struct BsField {
         int row, col;
         elem_rc<SH>(e, warp, lane, row, col);
         float a = 0.f;
-        for (int o = 0; o < H; o++) a = fmaf(sm.R1[row][o], __ldg(W0 + o * D + col), a);
+        for (int o = 0; o < H; o++) a = fmaf(sm.a.R1[row][o], __ldg(W0 + o * D + col), a);
         GY[e] = a;
       }
     } else {
@@ -296,10 +324,10 @@ struct BsField {
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         if constexpr (SH::GFRAG)
-          gemm_gfrag<D, SH::TPWH>(acc, &sm.X[mth * 16][0], &sm.Xl[mth * 16][0], SH::PD, Q.w0f,
+          gemm_gfrag<D, SH::TPWH>(acc, &sm.a.X[mth * 16][0], &sm.a.Xl[mth * 16][0], SH::PD, Q.w0f,
                                   nth0, lane);
         else
-          fwd_gemm<D, SH::TPWH>(acc, &sm.X[mth * 16][0], &sm.Xl[mth * 16][0], SH::PD,
+          fwd_gemm<D, SH::TPWH>(acc, &sm.a.X[mth * 16][0], &sm.a.Xl[mth * 16][0], SH::PD,
                                 &sm.W0[nth0 * 8][0], &sm.W0l[nth0 * 8][0], SH::PD, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
@@ -318,7 +346,7 @@ struct BsField {
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         const __nv_bfloat16 *w1l = nullptr;
         if constexpr (SH::WSPLIT) w1l = &sm.W1l[nth0 * 8][0];
-        fwd_gemm<H, SH::TPWH>(acc, &sm.R1[mth * 16][0], &sm.R1l[mth * 16][0], SH::PH,
+        fwd_gemm<H, SH::TPWH>(acc, &sm.a.R1[mth * 16][0], &sm.a.R1l[mth * 16][0], SH::PH,
                               &sm.W1[nth0 * 8][0], w1l, SH::PH, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
@@ -336,10 +364,10 @@ struct BsField {
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         if constexpr (SH::GFRAG)
-          gemm_gfrag<H, SH::TPW>(acc, &sm.R2[mto * 16][0], &sm.R2l[mto * 16][0], SH::PH, Q.w2f,
+          gemm_gfrag<H, SH::TPW>(acc, &sm.a.R2[mto * 16][0], &sm.a.R2l[mto * 16][0], SH::PH, Q.w2f,
                                  nto0, lane);
         else
-          fwd_gemm<H, SH::TPW>(acc, &sm.R2[mto * 16][0], &sm.R2l[mto * 16][0], SH::PH,
+          fwd_gemm<H, SH::TPW>(acc, &sm.a.R2[mto * 16][0], &sm.a.R2l[mto * 16][0], SH::PH,
                                &sm.W2[nto0 * 8][0], &sm.W2l[nto0 * 8][0], SH::PH, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) {
@@ -354,19 +382,19 @@ struct BsField {
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         if constexpr (SH::GFRAG)
-          gemm_gfrag<D, SH::TPWH>(acc, &sm.G[mth * 16][0], &sm.Gl[mth * 16][0], SH::PD, Q.w2v,
+          gemm_gfrag<D, SH::TPWH>(acc, &sm.a.G[mth * 16][0], &sm.a.Gl[mth * 16][0], SH::PD, Q.w2v,
                                   nth0, lane);
         else
-          vjp_gemm<D, SH::TPWH>(acc, &sm.G[mth * 16][0], &sm.Gl[mth * 16][0], SH::PD,
+          vjp_gemm<D, SH::TPWH>(acc, &sm.a.G[mth * 16][0], &sm.a.Gl[mth * 16][0], SH::PD,
                                 &sm.W2[0][0], &sm.W2l[0][0], SH::PH, nth0 * 8, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
           for (int hr = 0; hr < 2; hr++) {
             const int row = mth * 16 + g + hr * 8, col = (nth0 + j) * 8 + 2 * c;
-            const float a0 = __bfloat162float(sm.R2[row][col]) + __bfloat162float(sm.R2l[row][col]);
+            const float a0 = __bfloat162float(sm.a.R2[row][col]) + __bfloat162float(sm.a.R2l[row][col]);
             const float a1 =
-                __bfloat162float(sm.R2[row][col + 1]) + __bfloat162float(sm.R2l[row][col + 1]);
+                __bfloat162float(sm.a.R2[row][col + 1]) + __bfloat162float(sm.a.R2l[row][col + 1]);
             put_hidden(sm, 2, row, col, acc[j][2 * hr] * (1.f - a0 * a0),
                        acc[j][2 * hr + 1] * (1.f - a1 * a1), rec, SH::RZ1);
           }
@@ -378,16 +406,16 @@ struct BsField {
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         const __nv_bfloat16 *w1l = nullptr;
         if constexpr (SH::WSPLIT) w1l = &sm.W1l[0][0];
-        vjp_gemm<H, SH::TPWH>(acc, &sm.R2[mth * 16][0], &sm.R2l[mth * 16][0], SH::PH,
+        vjp_gemm<H, SH::TPWH>(acc, &sm.a.R2[mth * 16][0], &sm.a.R2l[mth * 16][0], SH::PH,
                               &sm.W1[0][0], w1l, SH::PH, nth0 * 8, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
           for (int hr = 0; hr < 2; hr++) {
             const int row = mth * 16 + g + hr * 8, col = (nth0 + j) * 8 + 2 * c;
-            const float a0 = __bfloat162float(sm.R1[row][col]) + __bfloat162float(sm.R1l[row][col]);
+            const float a0 = __bfloat162float(sm.a.R1[row][col]) + __bfloat162float(sm.a.R1l[row][col]);
             const float a1 =
-                __bfloat162float(sm.R1[row][col + 1]) + __bfloat162float(sm.R1l[row][col + 1]);
+                __bfloat162float(sm.a.R1[row][col + 1]) + __bfloat162float(sm.a.R1l[row][col + 1]);
             put_hidden(sm, 1, row, col, acc[j][2 * hr] * (1.f - a0 * a0),
                        acc[j][2 * hr + 1] * (1.f - a1 * a1), rec, SH::RZ0);
           }
@@ -398,10 +426,10 @@ struct BsField {
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         if constexpr (SH::GFRAG)
-          gemm_gfrag<H, SH::TPW>(acc, &sm.R1[mto * 16][0], &sm.R1l[mto * 16][0], SH::PH, Q.w0v,
+          gemm_gfrag<H, SH::TPW>(acc, &sm.a.R1[mto * 16][0], &sm.a.R1l[mto * 16][0], SH::PH, Q.w0v,
                                  nto0, lane);
         else
-          vjp_gemm<H, SH::TPW>(acc, &sm.R1[mto * 16][0], &sm.R1l[mto * 16][0], SH::PH,
+          vjp_gemm<H, SH::TPW>(acc, &sm.a.R1[mto * 16][0], &sm.a.R1l[mto * 16][0], SH::PH,
                                &sm.W0[0][0], &sm.W0l[0][0], SH::PD, nto0 * 8, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) GY[e] = acc[e >> 2][e & 3];
@@ -431,12 +459,14 @@ __device__ __forceinline__ void kahan4(float *sum, float *comp, const float (&x)
   *reinterpret_cast<float4 *>(comp) = make_float4(cv[0], cv[1], cv[2], cv[3]);
 }
 
+// (err / (atol + rtol max(|a0|, |a1|)))^2.  pid.py:475-492 scales a NaN
+// candidate by a0: fmaxf returns its non-NaN operand.  A NaN error
+// (infinite in _integrate.py:386) makes the row's norm NaN, which the
+// controller treats as infinite: rejected, factor clipped to factormin.
 __device__ __forceinline__ float scaled_sq(float a0, float a1, float err, float rtol,
                                            float atol) {
-  // pid.py:475-492 (a NaN candidate falls back to a0 for the scale);
-  // _integrate.py:386 (a NaN error counts as infinite).
-  const float m = fmaxf(fabsf(a0), fabsf(isnan(a1) ? a0 : a1));
-  const float s = isnan(err) ? INFINITY : __fdividef(err, fmaf(m, rtol, atol));
+  const float m = fmaxf(fabsf(a0), fabsf(a1));
+  const float s = __fdividef(err, fmaf(m, rtol, atol));
   return s * s;
 }
 
@@ -469,39 +499,48 @@ __device__ __forceinline__ float theta_layer(float (*cf)[16], const float *rec_r
     v[j][3] = t.w;
   }
   float accn = 0.f;
-#pragma unroll 4
-  for (int o = orow; o < NO; o += RPI) {
-    const int p = WOFF + o * NI + i4;
-    float x0[4] = {0.f, 0.f, 0.f, 0.f};
-    if (NORM && a0) {
-      const float4 t = __ldcs(reinterpret_cast<const float4 *>(a0 + p));
-      x0[0] = t.x;
-      x0[1] = t.y;
-      x0[2] = t.z;
-      x0[3] = t.w;
-    }
-    float db[4], de[4];
+  // U output rows per batch: their loads are all issued before any is used,
+  // so every thread keeps U vector loads in flight.
+  constexpr int U = 8;
+  for (int ob = orow; ob < NO; ob += RPI * U) {
+    float x0[U][4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) db[q] = de[q] = 0.f;
+    for (int u = 0; u < U; u++) {
+      const int o = ob + u * RPI;
 #pragma unroll
-    for (int j = 0; j < S; j++) {
-      const float cb = cf[o][j], ce = cf[o][8 + j];
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        if (TB::b(j) != 0.0) db[q] = fmaf(cb, v[j][q], db[q]);
-        if (TB::e(j) != 0.0) de[q] = fmaf(ce, v[j][q], de[q]);
+      for (int q = 0; q < 4; q++) x0[u][q] = 0.f;
+      if (o < NO && a0) {
+        const float4 t = __ldcs(reinterpret_cast<const float4 *>(a0 + WOFF + o * NI + i4));
+        x0[u][0] = t.x;
+        x0[u][1] = t.y;
+        x0[u][2] = t.z;
+        x0[u][3] = t.w;
       }
     }
-    if constexpr (NORM) {
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int o = ob + u * RPI;
+      if (o >= NO) break;
+      const int p = WOFF + o * NI + i4;
+      float db[4], de[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) db[q] = de[q] = 0.f;
+#pragma unroll
+      for (int j = 0; j < S; j++) {
+        const float cb = cf[o][j], ce = cf[o][8 + j];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (TB::b(j) != 0.0) db[q] = fmaf(cb, v[j][q], db[q]);
+          if (NORM && TB::e(j) != 0.0) de[q] = fmaf(ce, v[j][q], de[q]);
+        }
+      }
       float x1[4];
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-        x1[q] = x0[q] + db[q];
-        accn += scaled_sq(x0[q], x1[q], de[q], rtol, atol);
+        x1[q] = x0[u][q] + db[q];
+        if (NORM) accn += scaled_sq(x0[u][q], x1[q], de[q], rtol, atol);
       }
       __stcs(reinterpret_cast<float4 *>(a1 + p), make_float4(x1[0], x1[1], x1[2], x1[3]));
-    } else {
-      kahan4(psum + p, pcomp + p, db);
     }
   }
   // biases (v = 1)
@@ -513,14 +552,10 @@ __device__ __forceinline__ float theta_layer(float (*cf)[16], const float *rec_r
       de += cf[o][8 + j];
     }
     const int p = BOFF + o;
-    if constexpr (NORM) {
-      const float x0 = a0 ? a0[p] : 0.f;
-      const float x1 = x0 + db;
-      a1[p] = x1;
-      accn += scaled_sq(x0, x1, de, rtol, atol);
-    } else {
-      kahan_add(psum + p, pcomp + p, db);
-    }
+    const float x0 = a0 ? a0[p] : 0.f;
+    const float x1 = x0 + db;
+    a1[p] = x1;
+    if (NORM) accn += scaled_sq(x0, x1, de, rtol, atol);
   }
   __syncthreads();  // cf is rewritten by the next layer
   return accn;
@@ -539,6 +574,208 @@ __device__ __forceinline__ float theta_pass(float (*cf)[16], const float *rec_r,
   s += theta_layer<SH, SOLVER, D, H, SH::RG, SH::RH2, SH::OW2, SH::OB2, NORM>(
       cf, rec_r, h, a0, a1, psum, pcomp, rtol, atol, tid);
   return s;
+}
+
+// Tensor-core parameter pass of one row and one layer under the tracked norm.
+// With du_j = -h (u_j - u_0), dv_j = v_j - v_0 and sum_j b_j = 1, sum_j e_j = 0,
+//   da  = -h sum_j b_j u_j v_j = U0 B1 + A2 v0 + sum_j du_j (b_j dv_j),
+//   err = -h sum_j e_j u_j v_j = U0 B3 + A3 v0 + sum_j du_j (e_j dv_j):
+// a rank-2 FP32 part, computed into the accumulators, plus a product over the
+// stages whose factors are O(h) stage differences, so one BF16 tensor-core
+// product per m16n8 tile carries it to well below FP32 rounding of da.  The
+// error estimate loses no digits to the cancellation of its weights.
+// The a_theta0 values of U consecutive tiles of this warp.  In the tensor-core
+// mode a row's weight gradients are stored in fragment order: tile t of a
+// layer holds its 128 values at WOFF + 128 t + 4 lane + q, q indexing the
+// accumulator elements (g, 2c), (g, 2c + 1), (g + 8, 2c), (g + 8, 2c + 1).
+template <int U, int TPW, int WOFF>
+__device__ __forceinline__ void tc_load(float (&x)[U][4], const float *a0, int tb, int warp,
+                                        int lane) {
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int t = warp * TPW + tb + u;
+    if (a0) {
+      const float4 v = __ldcs(reinterpret_cast<const float4 *>(a0 + WOFF + t * 128 + lane * 4));
+      x[u][0] = v.x;
+      x[u][1] = v.y;
+      x[u][2] = v.z;
+      x[u][3] = v.w;
+    } else {
+      x[u][0] = x[u][1] = x[u][2] = x[u][3] = 0.f;
+    }
+  }
+}
+
+// U tiles: a1 = a0 + da (fragment layout); returns the tiles' share of the
+// scaled squared errors when NORM.
+template <class SH, int S, int U, int NTL, int TPW, int NI, int WOFF, bool NORM>
+__device__ __forceinline__ float tc_tiles(BsPassOps<SH> &ps, const float (&x0)[U][4], float *a1,
+                                          int tb, int warp, int lane, float rtol, float atol) {
+  const int g = lane >> 2, c = lane & 3;
+  float accn = 0.f;
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int t = warp * TPW + tb + u, ot = t / NTL, nt = t % NTL;
+    const int og = ot * 16 + g, ic = nt * 8 + 2 * c;
+    uint32_t a[4], bb[2], be[2];
+    ldsm_a(a, &ps.Du[ot * 16][0], 24, lane);
+    ldsm_bt1(bb, &ps.Bb[0][0], SH::PH, 0, nt * 8, lane);
+    const float u0a = ps.U0[og], u0b = ps.U0[og + 8];
+    const float a2a = ps.A2[og], a2b = ps.A2[og + 8];
+    const float2 v0 = *reinterpret_cast<const float2 *>(&ps.v0[ic]);
+    const float2 b1 = *reinterpret_cast<const float2 *>(&ps.B1[ic]);
+    float cb[4] = {fmaf(u0a, b1.x, a2a * v0.x), fmaf(u0a, b1.y, a2a * v0.y),
+                   fmaf(u0b, b1.x, a2b * v0.x), fmaf(u0b, b1.y, a2b * v0.y)};
+    if constexpr (S > 1) mma_bf16(cb, a, bb[0], bb[1]);
+    float x1[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) x1[q] = x0[u][q] + cb[q];
+    if constexpr (NORM) {
+      ldsm_bt1(be, &ps.Be[0][0], SH::PH, 0, nt * 8, lane);
+      const float a3a = ps.A3[og], a3b = ps.A3[og + 8];
+      const float2 b3 = *reinterpret_cast<const float2 *>(&ps.B3[ic]);
+      float ce[4] = {fmaf(u0a, b3.x, a3a * v0.x), fmaf(u0a, b3.y, a3a * v0.y),
+                     fmaf(u0b, b3.x, a3b * v0.x), fmaf(u0b, b3.y, a3b * v0.y)};
+      if constexpr (S > 1) mma_bf16(ce, a, be[0], be[1]);
+#pragma unroll
+      for (int q = 0; q < 4; q++) accn += scaled_sq(x0[u][q], x1[q], ce[q], rtol, atol);
+    }
+    __stcs(reinterpret_cast<float4 *>(a1 + WOFF + t * 128 + lane * 4),
+           make_float4(x1[0], x1[1], x1[2], x1[3]));
+  }
+  return accn;
+}
+
+template <class SH, int SOLVER, int NO, int NI, int UOFF, int VOFF, int WOFF, int BOFF, bool NORM>
+__device__ __forceinline__ float theta_layer_tc(BsPassOps<SH> &ps, const float *rec_r, float h,
+                                                const float *a0, float *a1, float rtol,
+                                                float atol, int tid, int warp, int lane) {
+  using TB = Tab<SOLVER>;
+  constexpr int S = TB::S, STR = SH::M * SH::REC;
+  static_assert(S - 1 <= 16, "stage differences fit one k16 slice");
+  constexpr int NTL = NI / 8, TILES = (NO / 16) * NTL, TPW = TILES / SH::WARPS;
+  static_assert(TILES % SH::WARPS == 0, "parameter tiles split");
+  constexpr int U = TPW < 16 ? TPW : 16;  // tiles per load batch
+  static_assert(TPW % U == 0, "parameter tile batches");
+  const int g = lane >> 2, c = lane & 3;
+  float accn = 0.f;
+  // the first batch's loads do not depend on the operands: issue them first
+  float xa[U][4], xb[U][4];
+  tc_load<U, TPW, WOFF>(xa, a0, 0, warp, lane);
+  // 1. operands
+  for (int i = tid; i < NI; i += SH::THREADS) {
+    float vv[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) vv[j] = rec_r[j * STR + VOFF + i];
+    float b1 = vv[0], b3 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      float bb = 0.f, be = 0.f;
+      if (k + 1 < S) {
+        const float dv = vv[k + 1] - vv[0];
+        bb = float(TB::b(k + 1)) * dv;
+        be = float(TB::e(k + 1)) * dv;
+        b1 += bb;
+        b3 += be;
+      }
+      ps.Bb[k][i] = __float2bfloat16_rn(bb);
+      ps.Be[k][i] = __float2bfloat16_rn(be);
+    }
+    ps.v0[i] = vv[0];
+    ps.B1[i] = b1;
+    ps.B3[i] = b3;
+  }
+  for (int o = tid; o < NO; o += SH::THREADS) {
+    float uu[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) uu[j] = -h * rec_r[j * STR + UOFF + o];
+    float a2 = 0.f, a3 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      float du = 0.f;
+      if (k + 1 < S) {
+        du = uu[k + 1] - uu[0];
+        a2 = fmaf(float(TB::b(k + 1)), du, a2);
+        a3 = fmaf(float(TB::e(k + 1)), du, a3);
+      }
+      ps.Du[o][k] = __float2bfloat16_rn(du);
+    }
+    ps.U0[o] = uu[0];
+    ps.A2[o] = a2;
+    ps.A3[o] = a3;
+  }
+  __syncthreads();  // the operands are complete
+  // 2. the weight tiles: warp w takes a contiguous run of m16n8 tiles, in
+  // batches of U whose loads are issued one batch ahead (double buffered)
+#pragma unroll 1
+  for (int tb = 0; tb < TPW; tb += 2 * U) {
+    if (tb + U < TPW) tc_load<U, TPW, WOFF>(xb, a0, tb + U, warp, lane);
+    accn += tc_tiles<SH, S, U, NTL, TPW, NI, WOFF, NORM>(ps, xa, a1, tb, warp, lane, rtol, atol);
+    if (tb + U >= TPW) break;
+    if (tb + 2 * U < TPW) tc_load<U, TPW, WOFF>(xa, a0, tb + 2 * U, warp, lane);
+    accn += tc_tiles<SH, S, U, NTL, TPW, NI, WOFF, NORM>(ps, xb, a1, tb + U, warp, lane, rtol,
+                                                         atol);
+  }
+  // 3. biases: da = U0 + A2, err = A3
+  for (int o = tid; o < NO; o += SH::THREADS) {
+    const int p = BOFF + o;
+    const float x0 = a0 ? a0[p] : 0.f;
+    const float x1 = x0 + (ps.U0[o] + ps.A2[o]);
+    a1[p] = x1;
+    if (NORM) accn += scaled_sq(x0, x1, ps.A3[o], rtol, atol);
+  }
+  __syncthreads();  // the operands are rewritten by the next layer
+  return accn;
+}
+
+template <class SH, int SOLVER, bool NORM>
+__device__ __forceinline__ float theta_pass_tc(BsPassOps<SH> &ps, const float *rec_r, float h,
+                                               const float *a0, float *a1, float rtol,
+                                               float atol, int tid, int warp, int lane) {
+  constexpr int D = SH::D, H = SH::H;
+  float s = 0.f;
+  s += theta_layer_tc<SH, SOLVER, H, D, SH::RZ0, SH::RX, SH::OW0, SH::OB0, NORM>(
+      ps, rec_r, h, a0, a1, rtol, atol, tid, warp, lane);
+  s += theta_layer_tc<SH, SOLVER, H, H, SH::RZ1, SH::RH1, SH::OW1, SH::OB1, NORM>(
+      ps, rec_r, h, a0, a1, rtol, atol, tid, warp, lane);
+  s += theta_layer_tc<SH, SOLVER, D, H, SH::RG, SH::RH2, SH::OW2, SH::OB2, NORM>(
+      ps, rec_r, h, a0, a1, rtol, atol, tid, warp, lane);
+  return s;
+}
+
+// Fold a finished row's a_theta into the CTA's Kahan partial (flat layout).
+// The tensor-core mode stores the weight blocks in fragment order.
+template <class SH, int NO, int NI, int WOFF, bool FRAG>
+__device__ __forceinline__ void fold_weights(const float *a, float *psum, float *pcomp, int tid) {
+  for (int e = tid * 4; e < NO * NI; e += SH::THREADS * 4) {
+    const float4 v = __ldcs(reinterpret_cast<const float4 *>(a + WOFF + e));
+    if constexpr (FRAG) {
+      const int t = e >> 7, lane = (e & 127) >> 2;
+      const int og = (t / (NI / 8)) * 16 + (lane >> 2), ic = (t % (NI / 8)) * 8 + 2 * (lane & 3);
+      const int p0 = WOFF + og * NI + ic, p1 = p0 + 8 * NI;
+      kahan_add(psum + p0, pcomp + p0, v.x);
+      kahan_add(psum + p0 + 1, pcomp + p0 + 1, v.y);
+      kahan_add(psum + p1, pcomp + p1, v.z);
+      kahan_add(psum + p1 + 1, pcomp + p1 + 1, v.w);
+    } else {
+      const float x[4] = {v.x, v.y, v.z, v.w};
+      kahan4(psum + WOFF + e, pcomp + WOFF + e, x);
+    }
+  }
+}
+
+template <class SH, bool FRAG>
+__device__ __forceinline__ void fold_row(const float *a, float *psum, float *pcomp, int tid) {
+  constexpr int D = SH::D, H = SH::H;
+  fold_weights<SH, H, D, SH::OW0, FRAG>(a, psum, pcomp, tid);
+  fold_weights<SH, H, H, SH::OW1, FRAG>(a, psum, pcomp, tid);
+  fold_weights<SH, D, H, SH::OW2, FRAG>(a, psum, pcomp, tid);
+  for (int o = tid; o < H; o += SH::THREADS) {
+    kahan_add(psum + SH::OB0 + o, pcomp + SH::OB0 + o, a[SH::OB0 + o]);
+    kahan_add(psum + SH::OB1 + o, pcomp + SH::OB1 + o, a[SH::OB1 + o]);
+  }
+  for (int o = tid; o < D; o += SH::THREADS)
+    kahan_add(psum + SH::OB2 + o, pcomp + SH::OB2 + o, a[SH::OB2 + o]);
 }
 
 // Block-wide sum of one value per thread, returned to every thread.
@@ -700,7 +937,7 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
   float *rec = Q.rec + size_t(blockIdx.x) * S * M * REC;
   float *psum = Q.psum + size_t(blockIdx.x) * NP;
   float *pcomp = Q.pcomp + size_t(blockIdx.x) * NP;
-  float *ath = Q.track ? Q.ath + size_t(blockIdx.x) * M * 2 * NP : nullptr;
+  float *ath = Q.ath + size_t(blockIdx.x) * M * 2 * NP;
   const float rtol = float(P.rtol), atol = float(P.atol);
 
   FLD::stage(sm, W, tid);
@@ -777,14 +1014,8 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
       // finished rows: results, the a_theta fold, a fresh trajectory next time
       for (int r = 0; r < M; r++) {
         if (!(R.trans[r] && R.done[r])) continue;
-        if (Q.track && !R.zero[r]) {
-          const float *a = ath + (size_t(r) * 2 + R.cur[r]) * NP;
-          for (int p = tid * 4; p < NP; p += SH::THREADS * 4) {
-            const float4 t = __ldcs(reinterpret_cast<const float4 *>(a + p));
-            const float x[4] = {t.x, t.y, t.z, t.w};
-            kahan4(psum + p, pcomp + p, x);
-          }
-        }
+        if (!R.zero[r])
+          fold_row<SH, !PRECISE>(ath + (size_t(r) * 2 + R.cur[r]) * NP, psum, pcomp, tid);
       }
       if (tid < M && R.trans[tid] && R.done[tid]) {
         const int64_t i = R.idx[tid];
@@ -931,8 +1162,13 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
           if (!R.live[r]) continue;
           const float *a0p = R.zero[r] ? nullptr : ath + (size_t(r) * 2 + R.cur[r]) * NP;
           float *a1p = ath + (size_t(r) * 2 + (R.cur[r] ^ 1)) * NP;
-          const float s = theta_pass<SH, SOLVER, true>(sm.cf, rec + size_t(r) * REC, R.h[r],
-                                                       a0p, a1p, psum, pcomp, rtol, atol, tid);
+          float s;
+          if constexpr (PRECISE)
+            s = theta_pass<SH, SOLVER, true>(sm.cf, rec + size_t(r) * REC, R.h[r], a0p, a1p,
+                                             psum, pcomp, rtol, atol, tid);
+          else
+            s = theta_pass_tc<SH, SOLVER, true>(sm.p, rec + size_t(r) * REC, R.h[r], a0p, a1p,
+                                                rtol, atol, tid, warp, lane);
           const float tot = block_sum<SH>(sm.red, s, tid);
           if (tid == 0) R.acc[r] += tot;
         }
@@ -941,12 +1177,18 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
     }
     if (tid < M && R.live[tid]) bs_row_control(R, tid, Q.n_norm, P);
     __syncthreads();
-    // accepted increments of untracked a_theta go straight to the partials
+    // untracked a_theta: add the accepted increments in place
     if (!Q.track) {
       for (int r = 0; r < M; r++) {
         if (!(R.live[r] && R.keep[r])) continue;
-        theta_pass<SH, SOLVER, false>(sm.cf, rec + size_t(r) * REC, R.h[r], nullptr, nullptr,
-                                      psum, pcomp, rtol, atol, tid);
+        float *ap = ath + size_t(r) * 2 * NP;
+        const float *a0p = R.zero[r] ? nullptr : ap;
+        if constexpr (PRECISE)
+          theta_pass<SH, SOLVER, false>(sm.cf, rec + size_t(r) * REC, R.h[r], a0p, ap, psum,
+                                        pcomp, rtol, atol, tid);
+        else
+          theta_pass_tc<SH, SOLVER, false>(sm.p, rec + size_t(r) * REC, R.h[r], a0p, ap, rtol,
+                                           atol, tid, warp, lane);
       }
     }
     // ---- accept: state, FSAL vectors and records, a_theta buffers --------------
@@ -973,8 +1215,8 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
       }
     }
     __syncthreads();
-    if (tid < M && R.live[tid] && R.keep[tid] && Q.track) {
-      R.cur[tid] ^= 1;
+    if (tid < M && R.live[tid] && R.keep[tid]) {
+      if (Q.track) R.cur[tid] ^= 1;
       R.zero[tid] = 0;
     }
     __syncthreads();
