@@ -444,6 +444,18 @@ def workload_neural(dev, flush, steps, warmup, kind):
     out["fused_forward_adjoint"]["dL_dy0_max_rel_err_vs_fp64_oracle"] = float(
         np.abs(gy0[:n_g].double().cpu().numpy() - r["grad_y0"]).max()
         / np.abs(r["grad_y0"]).max())
+    # the plain form: forward with the full tape + one-trajectory-per-thread
+    # backward on the CUDA cores (FP32)
+    pgrad = lowered("plain", True)
+
+    def fwd_bwd_plain():
+        ys_, _, _, _, ws = pgrad.run_forward(keep_workspace=True)
+        gys_ = ys_ * (2.0 / ys_.numel())
+        return pgrad.run_backward(ws, gys_, pgrad.y0, pgrad.params)
+    ms_pg = _events_time(fwd_bwd_plain, max(2, steps // 2), 1, flush)
+    out["plain_forward_adjoint"] = {"grads_per_s": B / (ms_pg / 1e3), "ms": ms_pg,
+                                    "unit": "trajectory gradients/s"}
+    out["fused_over_plain_forward_adjoint"] = ms_pg / ms_g
     out["cpu_baseline_forward_adjoint"] = _oracle_rate(
         lambda: O.grad_recursive(desc, 0.0, 1.0, dt0, y0[:n_g].astype(np.float64), gys,
                                  params=params, ts=ts, nthreads=cores), n_g, cores)

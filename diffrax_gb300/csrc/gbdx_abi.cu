@@ -110,7 +110,23 @@ int ws_layout(const gbdx_problem *p, int64_t batch, WsLayout *L) {
     L->ath = off;
     off += up256(size_t(L->n_cta) * p->bs.rows * 2 * np * sizeof(float));
   }
-  if (d.adjoint == GBDX_ADJ_RECURSIVE && p->bwd.launch) {
+  if (d.adjoint == GBDX_ADJ_RECURSIVE && p->bwd.launch && d.kernel == GBDX_KERNEL_PLAIN) {
+    // the plain backward: full tape, per-trajectory cotangents dP [P][B]
+    const size_t C = size_t(d.max_steps) + 1;
+    L->tape_t = off;
+    off += up256(B * C * sizeof(double));
+    L->tape_y = off;
+    off += up256(B * C * d.dim * sizeof(float));
+    L->tape_n = off;
+    off += up256(B * sizeof(int32_t));
+    L->tape_s = off;
+    off += up256(B * sizeof(int32_t));
+    L->scratch = off;
+    L->psum = off;
+    off += up256(B * size_t(gbdx_param_count(p)) * sizeof(float));
+    L->pcomp = off;
+    L->n_cta = int(B);
+  } else if (d.adjoint == GBDX_ADJ_RECURSIVE && p->bwd.launch) {
     const int C = d.checkpoints > 1 ? d.checkpoints : 2;
     L->tape_t = off;
     off += up256(B * size_t(d.max_steps + 1) * sizeof(double));
@@ -242,9 +258,17 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     const int D = d.dim, H = w[1];
     if (d.kernel == GBDX_KERNEL_PLAIN) {
       // The plain form: one trajectory per thread, FP32 CUDA-core products.
-      if (d.adjoint != GBDX_ADJ_NONE) {
+      if (d.adjoint == GBDX_ADJ_BACKSOLVE) {
         delete p;
-        return fail(GBDX_ERR_UNSUPPORTED, "the plain MLP kernel has no backward");
+        return fail(GBDX_ERR_UNSUPPORTED, "the plain MLP kernel has no backsolve backward");
+      }
+      if (d.adjoint == GBDX_ADJ_RECURSIVE) {
+        p->bwd = gbdx::find_mlp_plain_bwd_entry(d.solver, D, H, sde);
+        if (!p->bwd.launch) {
+          delete p;
+          return fail(GBDX_ERR_UNSUPPORTED, "no plain backward for dim %d, width %d, solver %d",
+                      D, H, d.solver);
+        }
       }
       p->ode = gbdx::find_mlp_plain_entry(d.solver, D, H, sde);
       if (!p->ode.launch) {
@@ -405,8 +429,11 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
     P.tape_n = reinterpret_cast<int32_t *>(w + L->tape_n);
     P.tape_stride = reinterpret_cast<int32_t *>(w + L->tape_s);
     // An even slot count keeps the online thinning exact: when the slots
-    // fill at step n = C s, n is a multiple of the doubled stride 2 s.
-    P.checkpoints = d.checkpoints >= 4 ? (d.checkpoints / 2) * 2 : 2;
+    // fill at step n = C s, n is a multiple of the doubled stride 2 s.  The
+    // plain form tapes every accepted step.
+    P.checkpoints = d.kernel == GBDX_KERNEL_PLAIN
+                        ? d.max_steps + 1
+                        : (d.checkpoints >= 4 ? (d.checkpoints / 2) * 2 : 2);
   }
   return GBDX_OK;
 }
@@ -522,14 +549,20 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   Q.n_params = np;
   cudaError_t e = cudaMemsetAsync(w + L.psum, 0, L.total - L.psum, s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient partial reset");
+  const bool plain = problem->d.kernel == GBDX_KERNEL_PLAIN;
   if (batch > 0) {
-    rc = start_queue(problem, P, workspace, s);
-    if (rc != GBDX_OK) return rc;
+    if (!plain) {
+      rc = start_queue(problem, P, workspace, s);
+      if (rc != GBDX_OK) return rc;
+    }
     e = problem->bwd.launch(P, Q, L.n_cta, s);
     if (e != cudaSuccess) return cuda_fail(e, "backward launch");
   }
-  e = gbdx::launch_reduce_partials(Q.part_sum, Q.part_comp, batch > 0 ? L.n_cta : 0, np,
-                                   static_cast<float *>(grad_params), s);
+  if (plain)
+    e = gbdx::launch_reduce_columns(Q.part_sum, np, batch, static_cast<float *>(grad_params), s);
+  else
+    e = gbdx::launch_reduce_partials(Q.part_sum, Q.part_comp, batch > 0 ? L.n_cta : 0, np,
+                                     static_cast<float *>(grad_params), s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
   return GBDX_OK;
 }

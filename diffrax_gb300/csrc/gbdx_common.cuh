@@ -244,6 +244,7 @@ template <class T>
 struct LotkaVolterra {
   static constexpr int D = 2, NARGS = 4;
   static constexpr bool SDE = false;
+  static constexpr bool TAPE = false;  // no gradient tape (forward only)
   __device__ static __forceinline__ void vf(const SolveParams &, const T *a, const T *y, T *o) {
     o[0] = a[0] * y[0] - a[1] * y[0] * y[1];
     o[1] = -a[2] * y[1] + a[3] * y[0] * y[1];
@@ -254,6 +255,7 @@ template <class T>
 struct VanDerPol {
   static constexpr int D = 2, NARGS = 1;
   static constexpr bool SDE = false;
+  static constexpr bool TAPE = false;  // no gradient tape (forward only)
   __device__ static __forceinline__ void vf(const SolveParams &, const T *a, const T *y, T *o) {
     o[0] = y[1];
     o[1] = a[0] * (T(1) - y[0] * y[0]) * y[1] - y[0];
@@ -264,6 +266,7 @@ template <class T, int D_>
 struct OrnsteinUhlenbeck {
   static constexpr int D = D_, NARGS = 3;
   static constexpr bool SDE = false;
+  static constexpr bool TAPE = false;  // no gradient tape (forward only)
   __device__ static __forceinline__ void vf(const SolveParams &, const T *a, const T *y, T *o) {
 #pragma unroll
     for (int i = 0; i < D; i++) o[i] = a[0] * (a[1] - y[i]);

@@ -56,6 +56,12 @@ BsEntry find_backsolve_entry_d32h64(int solver, bool precise);
 cudaError_t launch_frag_prep(const float *W, int ldw, int K, int N, int trans, uint2 *out,
                              cudaStream_t s);
 OdeEntry find_mlp_plain_entry(int solver, int D, int H, bool sde);
+// The plain (one trajectory per thread) RecursiveCheckpointAdjoint backward:
+// full tape, per-trajectory parameter cotangents dP [n_params][batch].
+BwdEntry find_mlp_plain_bwd_entry(int solver, int D, int H, bool sde);
+// out[p] = compensated sum over the batch of dP[p][:]
+cudaError_t launch_reduce_columns(const float *dP, int64_t n_params, int64_t batch, float *out,
+                                  cudaStream_t s);
 OdeEntry find_mlp_entry_d64h128(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d64h256(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d32h64(int solver, bool precise, bool sde);

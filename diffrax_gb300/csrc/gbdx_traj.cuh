@@ -126,6 +126,15 @@ struct Traj {
     ts_index = 0;
     nsteps = nacc = nrej = 0;
     result = GBDX_SUCCESSFUL;
+    if constexpr (FIELD::TAPE) {
+      // full gradient tape: the time and state at every accepted step
+      if (P.tape_t) {
+        P.tape_t[i * (P.max_steps + 1)] = a;
+        T *o = reinterpret_cast<T *>(P.tape_y) + i * int64_t(P.checkpoints) * D;
+#pragma unroll
+        for (int n = 0; n < D; n++) o[n] = y[n];
+      }
+    }
     if (P.save_t0) {
       T *o = ys_row(P, 0);
 #pragma unroll
@@ -331,6 +340,14 @@ struct Traj {
       }
 #pragma unroll
       for (int n = 0; n < D; n++) y[n] = y1[n];
+      if constexpr (FIELD::TAPE) {
+        if (P.tape_t) {
+          P.tape_t[idx * (P.max_steps + 1) + nacc + 1] = tnext;
+          T *o = reinterpret_cast<T *>(P.tape_y) + (idx * int64_t(P.checkpoints) + nacc + 1) * D;
+#pragma unroll
+          for (int n = 0; n < D; n++) o[n] = y1[n];
+        }
+      }
       if constexpr (FIELD::SDE) {
 #pragma unroll
         for (int n = 0; n < D; n++) wb[n] = wn[n];
@@ -406,6 +423,12 @@ struct Traj {
     int r = result;
     if (r == GBDX_SUCCESSFUL && tprev < t1) r = GBDX_MAX_STEPS_REACHED;  // :883
     P.result_out[idx] = r;
+    if constexpr (FIELD::TAPE) {
+      if (P.tape_n) {
+        P.tape_n[idx] = nacc;
+        P.tape_stride[idx] = 1;
+      }
+    }
     P.stats_out[idx * 3 + 0] = nsteps;
     P.stats_out[idx * 3 + 1] = nacc;
     P.stats_out[idx * 3 + 2] = nrej;

@@ -28,7 +28,7 @@ def params_np(widths, seed, bias_scale=0.1):
 
 
 def grad_case(widths, solver, controller, saveat, t1, dt0, B, precision, checkpoints,
-              seed=0, sde=False, max_steps=4096):
+              seed=0, sde=False, max_steps=4096, kernel="fused"):
     dev = torch.device("cuda")
     rng = np.random.default_rng(seed + 100)
     D = widths[0]
@@ -57,7 +57,8 @@ def grad_case(widths, solver, controller, saveat, t1, dt0, B, precision, checkpo
         t1, np.ndarray) else t1
     sol = dfx.diffeqsolve(terms, solver, 0.0, t1_arg, dt0, y0_t, saveat=saveat,
                           stepsize_controller=controller, max_steps=max_steps,
-                          adjoint=dfx.RecursiveCheckpointAdjoint(checkpoints=checkpoints))
+                          adjoint=dfx.RecursiveCheckpointAdjoint(checkpoints=checkpoints),
+                          kernel=kernel)
     n_save = sol.ys.shape[1]
     G = rng.standard_normal((B, n_save, D))
     loss = (sol.ys.double() * torch.tensor(G, device=dev)).sum()
@@ -148,3 +149,22 @@ def test_grad_bf16_error_level(widths, sde):
     e0, ep = rel(g_y0, r["grad_y0"]), rel(g_p, r["grad_params"])
     print(f"grad bf16 {widths}: dL/dy0 rel {e0:.2e}, dL/dtheta rel {ep:.2e}")
     assert e0 < 3e-2 and ep < 3e-2
+
+
+@pytest.mark.parametrize("sde", [False, True])
+def test_grad_plain_kernel(sde):
+    # The plain form (one trajectory per thread, FP32 CUDA-core products, full
+    # tape): the neural ODE 64-128-128-64 with Tsit5 + PID and the neural SDE
+    # 32-64-64-32 with Heun, against the FP64 oracle.
+    if sde:
+        g_y0, g_p, r, steps = grad_case([32, 64, 64, 32], dfx.Heun(), dfx.ConstantStepSize(),
+                                        dfx.SaveAt(t1=True), 1.0, 0.01, 40, "fp32",
+                                        checkpoints=16, seed=11, sde=True, kernel="plain")
+    else:
+        g_y0, g_p, r, steps = grad_case([64, 128, 128, 64], dfx.Tsit5(), dfx.ConstantStepSize(),
+                                        dfx.SaveAt(t1=True, ts=np.array([0.4, 0.7])), 1.0, 0.05,
+                                        40, "fp32", checkpoints=64, seed=12, kernel="plain")
+    assert np.array_equal(steps, r["stats"][:, 0])
+    e0, ep = rel(g_y0, r["grad_y0"]), rel(g_p, r["grad_params"])
+    print(f"plain backward (sde={sde}): dL/dy0 rel {e0:.2e}, dL/dtheta rel {ep:.2e}")
+    assert e0 < 1e-4 and ep < 1e-4
