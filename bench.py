@@ -307,6 +307,17 @@ def workload_backsolve(dev, flush, steps, warmup, terms_for, solver, ctrl, savea
                                 "sample": f"{n_g} trajectories backward only, FP64 oracle, "
                                           f"{dt_cpu:.2f} s"}}
         if name == "rms_norm":
+            # the plain form: one trajectory per thread, FP32 CUDA cores
+            plow = Lowered(terms_for("bf16"), solver, 0.0, 1.0, None, y0_d, None, saveat, ctrl,
+                           adj, 4096, "plain", 0, 0, want_grad=True)
+
+            def fwd_bwd_plain():
+                ys_, ts_, _, _ = plow.run_forward()
+                gys_ = ys_ * (2.0 / (B * D))
+                return plow.run_backsolve(ts_, ys_, gys_, plow.params)
+            ms_p = _events_time(fwd_bwd_plain, 1, 1, flush)
+            ent["plain_forward_adjoint"] = {"grads_per_s": B / (ms_p / 1e3), "ms": ms_p}
+            ent["fused_over_plain"] = ms_p / ms
             # a_theta double buffer: read a_theta0 + write the candidate per row-step
             n_par = int(low.params.numel())
             ent["a_theta_stream_bytes"] = float(st[:, 0].double().sum().item()) * 2 * 4 * n_par

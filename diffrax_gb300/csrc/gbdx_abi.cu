@@ -85,7 +85,13 @@ int ws_layout(const gbdx_problem *p, int64_t batch, WsLayout *L) {
   L->n_cta = 0;
   L->frag = L->rec = L->ath = off;
   L->track = false;
-  if (d.adjoint == GBDX_ADJ_BACKSOLVE && p->bs.launch) {
+  if (d.adjoint == GBDX_ADJ_BACKSOLVE && p->bs.launch && d.kernel == GBDX_KERNEL_PLAIN) {
+    // the plain backsolve: a_theta and two stage accumulators per trajectory
+    L->n_cta = int(B);
+    L->track = bs_tracks(d);
+    L->frag = L->rec = L->psum = L->pcomp = L->ath = off;
+    off += up256(3 * B * size_t(gbdx_param_count(p)) * sizeof(float));
+  } else if (d.adjoint == GBDX_ADJ_BACKSOLVE && p->bs.launch) {
     int dev = 0, sms = 0, occ = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -259,8 +265,13 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     if (d.kernel == GBDX_KERNEL_PLAIN) {
       // The plain form: one trajectory per thread, FP32 CUDA-core products.
       if (d.adjoint == GBDX_ADJ_BACKSOLVE) {
-        delete p;
-        return fail(GBDX_ERR_UNSUPPORTED, "the plain MLP kernel has no backsolve backward");
+        p->bs = sde ? gbdx::BsEntry{nullptr, nullptr, 0, 0, 0, 0}
+                    : gbdx::find_plain_backsolve_entry(d.solver, D, H);
+        if (!p->bs.launch) {
+          delete p;
+          return fail(GBDX_ERR_UNSUPPORTED,
+                      "no plain backsolve for dim %d, width %d, solver %d", D, H, d.solver);
+        }
       }
       if (d.adjoint == GBDX_ADJ_RECURSIVE) {
         p->bwd = gbdx::find_mlp_plain_bwd_entry(d.solver, D, H, sde);
@@ -605,7 +616,15 @@ int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double 
   Q.ath = reinterpret_cast<float *>(w + L.ath);
   Q.track = L.track ? 1 : 0;
   Q.n_norm = float(L.track ? 2 * D + np : 2 * D);
-  cudaError_t e = cudaMemsetAsync(w + L.psum, 0, L.ath - L.psum, s);
+  cudaError_t e;
+  if (problem->d.kernel == GBDX_KERNEL_PLAIN) {
+    e = problem->bs.launch(P, Q, 0, s);
+    if (e != cudaSuccess) return cuda_fail(e, "plain backsolve launch");
+    e = gbdx::launch_reduce_columns(Q.ath, np, batch, static_cast<float *>(grad_params), s);
+    if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
+    return GBDX_OK;
+  }
+  e = cudaMemsetAsync(w + L.psum, 0, L.ath - L.psum, s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient partial reset");
   if (batch > 0) {
     if (problem->bs.gfrag) {

@@ -52,6 +52,9 @@ struct BsEntry {
 BsEntry find_backsolve_entry_d64h256(int solver, bool precise);
 BsEntry find_backsolve_entry_d64h128(int solver, bool precise);
 BsEntry find_backsolve_entry_d32h64(int solver, bool precise);
+// The plain (one trajectory per thread) backsolve: a_theta and the stage
+// accumulators as [n_params][batch] columns in the workspace.
+BsEntry find_plain_backsolve_entry(int solver, int D, int H);
 // BF16 mma B fragments of B[k][n] = trans ? W[n][k] : W[k][n] (K x N).
 cudaError_t launch_frag_prep(const float *W, int ldw, int K, int N, int trans, uint2 *out,
                              cudaStream_t s);

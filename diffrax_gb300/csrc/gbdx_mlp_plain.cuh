@@ -52,14 +52,13 @@ struct MlpPlainField {
     }
   }
 
-  // gy += (df/dy)^T g + (d sigma/dy)^T (gs) and the parameter cotangents added
-  // to this trajectory's column of dP ([NP][stride] layout, coalesced across
-  // the threads of a warp).
-  __device__ static void vjp(const float *W, const float *y, const float *g, const float *gs,
-                             float *gy, float *dP, int64_t stride) {
+  // gy += (df/dy)^T g + (d sigma/dy)^T (gs); every parameter cotangent v_p
+  // (each parameter once) is handed to add(p, v_p).
+  template <class ADD>
+  __device__ static void vjp_with(const float *W, const float *y, const float *g, const float *gs,
+                                  float *gy, ADD add) {
     float h1[H], h2[H], dz[H], dz0[H];
     hidden(W, y, h1, h2);
-    auto add = [&](int p, float v) { dP[p * stride] += v; };
 #pragma unroll 1
     for (int o = 0; o < D; o++) {
       const float go = g[o];
@@ -113,6 +112,13 @@ struct MlpPlainField {
         gy[k] += a;
       }
     }
+  }
+
+  // The parameter cotangents added to this trajectory's column of dP
+  // ([NP][stride] layout, coalesced across the threads of a warp).
+  __device__ static void vjp(const float *W, const float *y, const float *g, const float *gs,
+                             float *gy, float *dP, int64_t stride) {
+    vjp_with(W, y, g, gs, gy, [&](int p, float v) { dP[p * stride] += v; });
   }
 };
 

@@ -36,7 +36,7 @@ def mlp_params(widths, seed, bias_scale=0.1, bf16_weights=False):
 
 
 def backsolve_case(widths, solver, controller, ts, B, precision, seed=0, seminorm=False,
-                   t1=1.0, dt0=None, bf16_weights=False, grad_ys=None, y0=None):
+                   t1=1.0, dt0=None, bf16_weights=False, grad_ys=None, y0=None, kernel="fused"):
     dev = torch.device("cuda")
     rng = np.random.default_rng(seed + 100)
     D = widths[0]
@@ -56,7 +56,7 @@ def backsolve_case(widths, solver, controller, ts, B, precision, seed=0, seminor
     y0_t = torch.tensor(y0, dtype=torch.float32, device=dev, requires_grad=True)
     sol = dfx.diffeqsolve(dfx.ODETerm(field), solver, 0.0, t1, dt0, y0_t,
                           saveat=dfx.SaveAt(ts=ts), stepsize_controller=controller,
-                          adjoint=adjoint)
+                          adjoint=adjoint, kernel=kernel)
     ys = sol.ys.double()
     G = grad_ys(ys.detach().cpu().numpy()) if grad_ys else rng.standard_normal(ys.shape)
     loss = (ys * torch.tensor(G, device=dev)).sum()
@@ -219,3 +219,18 @@ def test_backsolve_neural_ode_wide_finite_differences():
         errs.append(abs(fd - c["g_params"] @ v) / np.linalg.norm(c["g_params"]))
     print(f"backsolve vs central differences: max rel err {max(errs):.2e}")
     assert max(errs) < 1e-3
+
+
+def test_backsolve_plain_kernel():
+    # The plain form (one trajectory per thread, FP32 CUDA-core products) of
+    # the wide neural ODE's backsolve, against the FP64 oracle.
+    ts = np.linspace(0.0, 1.0, 8)
+    c = backsolve_case([64, 256, 256, 64], dfx.Tsit5(), PID, ts, 12, "fp32", seed=13,
+                       grad_ys=_c4_grad_ys, kernel="plain")
+    r = c["oracle"]
+    e0, ep = rel(c["g_y0"], r["grad_y0"]), rel(c["g_params"], r["grad_params"])
+    print(f"plain backsolve: dL/dy0 {e0:.2e}, dL/dtheta {ep:.2e}, "
+          f"steps {c['stats'][:, 0].mean():.1f} (oracle {r['stats'][:, 0].mean():.1f})")
+    assert np.all(c["result"] == 0)
+    check_steps(c, False, 7)
+    assert e0 < 1e-4 and ep < 1e-4
