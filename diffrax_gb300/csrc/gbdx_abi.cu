@@ -433,6 +433,10 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
   P.vbt_t0 = d.vbt_t0;
   P.vbt_len = d.vbt_t1 - d.vbt_t0;
   P.vbt_tol_unit = d.vbt_tol / (d.vbt_t1 - d.vbt_t0);
+  // GB300 issues FP64 at ~1/64 of the FP32 rate: the per-evaluation division
+  // and square root of the tree's time scaling are done once here.
+  P.vbt_inv_len = 1.0 / (d.vbt_t1 - d.vbt_t0);
+  P.vbt_sqrt_len = float(sqrt(d.vbt_t1 - d.vbt_t0));
   if (d.adjoint == GBDX_ADJ_RECURSIVE && problem->bwd.launch) {
     char *w = static_cast<char *>(workspace);
     P.tape_t = reinterpret_cast<double *>(w + L->tape_t);

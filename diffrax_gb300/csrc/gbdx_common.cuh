@@ -301,6 +301,8 @@ struct SolveParams {
   const float *mlp;           // flat FP32 parameters (W0, b0, W1, b1, W2, b2, Ws, bs)
   uint64_t seed;              // Brownian generator seed
   double vbt_t0, vbt_len, vbt_tol_unit;
+  double vbt_inv_len;         // 1 / vbt_len
+  float vbt_sqrt_len;         // sqrt(vbt_len) as FP32
   // Recursive-checkpoint tape (forward pass of a differentiated solve)
   double *tape_t;             // [batch, max_steps + 1] accepted-step time grid
   float *tape_y;              // [batch, checkpoints, dim] state checkpoints

@@ -452,6 +452,53 @@ __device__ void row_control(RowState<M> &R, int r, int D, const SolveParams &P) 
   R.dtc[r] = dtn;
 }
 
+// Brownian values W(t) of this thread's owned elements (rows r0 and r0 + 8,
+// columns c, c + 1 of one quad of dimensions) for the rows with flag[row] set,
+// at time tsel[row] (FP64, times dir).  The two lanes that share a quad split
+// the work by row -- the even lane descends the tree for r0, the odd lane for
+// r0 + 8, each for all four dimensions of the quad from its cached path -- and
+// swap halves.  Every lane of the warp must call it.
+template <class SH, int M, int NE>
+__device__ __forceinline__ void vbt_owned(const SolveParams &P, const RowState<M> &R,
+                                          const int *flag, const double *tsel,
+                                          VbtQuadCache &vc, float (&W)[NE], int warp, int lane) {
+  static_assert(NE == 4, "one output tile per thread");
+  int row0, col0;
+  elem_rc<SH>(0, warp, lane, row0, col0);
+  const bool odd = lane & 1;
+  const int myrow = odd ? row0 + 8 : row0;
+  float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (flag[myrow]) w = vbt_w_quad(P, R.idx[myrow], tsel[myrow] * R.dir[myrow], col0 >> 2, vc);
+  const float sx = odd ? w.x : w.z, sy = odd ? w.y : w.w;
+  const float rx = __shfl_xor_sync(0xffffffffu, sx, 1), ry = __shfl_xor_sync(0xffffffffu, sy, 1);
+  if (odd) {
+    W[0] = rx;
+    W[1] = ry;
+    W[2] = w.z;
+    W[3] = w.w;
+  } else {
+    W[0] = w.x;
+    W[1] = w.y;
+    W[2] = rx;
+    W[3] = ry;
+  }
+}
+
+// W(t0) of freshly loaded rows (SDE).
+template <class SH, int M, int NE>
+__device__ __forceinline__ void load_brownian(const SolveParams &P, const RowState<M> &R,
+                                              VbtQuadCache &vc, float (&Wb)[NE], int warp,
+                                              int lane) {
+  float W[NE];
+  vbt_owned<SH>(P, R, R.loaded, R.tprev, vc, W, warp, lane);
+#pragma unroll
+  for (int e = 0; e < NE; e++) {
+    int row, col;
+    elem_rc<SH>(e, warp, lane, row, col);
+    if (R.loaded[row]) Wb[e] = W[e];
+  }
+}
+
 // Initial state of freshly loaded rows: y0, a zero FSAL vector, the t0 save,
 // the first state checkpoint and (SDE) the Brownian value at t0.
 template <class SH, bool SDE, int M, int NE>
@@ -478,11 +525,6 @@ __device__ __forceinline__ void load_rows(float (&Y0)[NE], float (&F0)[NE], floa
         float *o = P.tape_y + (i * P.checkpoints) * D + col;
         o[0] = Y0[e];
         o[1] = Y0[e + 1];
-      }
-      if (SDE) {
-        const float2 w = vbt_w_pair(P, i, R.tprev[row] * R.dir[row], col);
-        Wb[e] = w.x;
-        Wb[e + 1] = w.y;
       }
     }
   }
@@ -526,7 +568,11 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
     F0[e] = 0.f;
     Wb[e] = 0.f;
   }
+  VbtQuadCache vc;
+  vc.traj = -1;
+  vc.node = 0;
   load_rows<SH, SDE>(Y0, F0, Wb, P, R, warp, lane);
+  if constexpr (SDE) load_brownian<SH>(P, R, vc, Wb, warp, lane);
   __syncthreads();
   if (tid < M) R.loaded[tid] = 0;
 
@@ -551,23 +597,12 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
       elem_rc<SH>(e, warp, lane, row, col);
       hrow[e] = R.h[row];
     }
-    if (SDE) {
+    if constexpr (SDE) {
       // Brownian increment over [tprev, tnext] of every owned element; W at
       // tprev is carried from the previous accepted step.
+      vbt_owned<SH>(P, R, R.live, R.tnext, vc, Wn, warp, lane);
 #pragma unroll
-      for (int e = 0; e < NE; e += 2) {
-        int row, col;
-        elem_rc<SH>(e, warp, lane, row, col);
-        Wn[e] = Wn[e + 1] = 0.f;
-        dW[e] = dW[e + 1] = 0.f;
-        if (R.live[row]) {
-          const float2 w = vbt_w_pair(P, R.idx[row], R.tnext[row] * R.dir[row], col);
-          Wn[e] = w.x;
-          Wn[e + 1] = w.y;
-          dW[e] = w.x - Wb[e];
-          dW[e + 1] = w.y - Wb[e + 1];
-        }
-      }
+      for (int e = 0; e < NE; e++) dW[e] = Wn[e] - Wb[e];
     }
     // stage 0 (FSAL reuse unless some row is on its first step)
     if (!TB::FSAL || any_first) {
@@ -779,6 +814,7 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
       }
       __syncthreads();
       load_rows<SH, SDE>(Y0, F0, Wb, P, R, warp, lane);
+      if constexpr (SDE) load_brownian<SH>(P, R, vc, Wb, warp, lane);
       __syncthreads();
       if (tid < M) R.loaded[tid] = 0;
     }

@@ -49,7 +49,7 @@ __device__ __forceinline__ float2 vbt_normal_pair(uint64_t seed, uint32_t traj, 
 // sqrt(T) W_unit(r) for dimensions (col, col + 1) of trajectory `traj` at time t.
 static __device__ __noinline__ float2 vbt_w_pair(const SolveParams &P, int64_t traj, double t,
                                           int col) {
-  const float r = float((t - P.vbt_t0) / P.vbt_len);
+  const float r = float((t - P.vbt_t0) * P.vbt_inv_len);
   const float tol = float(P.vbt_tol_unit);
   const uint32_t tj = uint32_t(traj);
   float2 z = vbt_normal_pair(P.seed, tj, 0u, kVbtRoot, col);
@@ -81,8 +81,134 @@ static __device__ __noinline__ float2 vbt_w_pair(const SolveParams &P, int64_t t
   const float sr = fmaxf(r - s, 0.f), ru = fmaxf(su - sr, 0.f);
   z = vbt_normal_pair(P.seed, tj, node, kVbtLeaf, col);
   const float bb = sqrtf(sr * ru / su), f = sr / su;
-  const float sq = float(sqrt(P.vbt_len));
+  const float sq = P.vbt_sqrt_len;
   return make_float2(sq * (ws0 + f * wsu0 + bb * z.x), sq * (ws1 + f * wsu1 + bb * z.y));
+}
+
+// Normals of the quad of dimensions 4 quad .. 4 quad + 3 for one tree node:
+// both Box-Muller pairs of one Philox block (vbt_normal_pair returns one).
+__device__ __forceinline__ float4 vbt_normal_quad(uint64_t seed, uint32_t traj, uint32_t node,
+                                                  uint32_t kind, int quad) {
+  uint32_t c[4] = {traj, node, (kind << 24) | uint32_t(quad), 0x5EEDu};
+  philox4x32_10(c, uint32_t(seed), uint32_t(seed >> 32));
+  float out[4];
+#pragma unroll
+  for (int p = 0; p < 2; p++) {
+    const float u = (float(c[2 * p] >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    const float v = (float(c[2 * p + 1] >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    const float rad = sqrtf(-2.0f * logf(u));
+    float sn, co;
+    sincospif(2.0f * v, &sn, &co);
+    out[2 * p] = rad * co;
+    out[2 * p + 1] = rad * sn;
+  }
+  return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// The bridge state of one descent path for a quad of dimensions: W at the
+// start of each level's dyadic interval and the increment across it.
+// Consecutive evaluations of a solve lie close together, so their paths share
+// the upper levels; an evaluation re-descends only below the deepest level
+// whose interval also contains the new time.
+constexpr int kVbtCacheLevels = 24;
+struct VbtQuadCache {
+  float ws[kVbtCacheLevels + 1][4], wsu[kVbtCacheLevels + 1][4];
+  uint32_t node;  // heap index of the cached path's leaf interval
+  long long traj; // trajectory of the cached path (-1: none)
+};
+
+// sqrt(T) W_unit(r) for the quad of dimensions of trajectory `traj` at time t:
+// the values of vbt_w_pair, descending from the cached path.
+static __device__ __noinline__ float4 vbt_w_quad(const SolveParams &P, int64_t traj, double t, int quad,
+                                          VbtQuadCache &C) {
+  const float r = float((t - P.vbt_t0) * P.vbt_inv_len);
+  const float tol = float(P.vbt_tol_unit);
+  const uint32_t tj = uint32_t(traj);
+  // the new path: levels and leaf node, by the comparisons of vbt_w_pair
+  float s = 0.f, su = 1.f;
+  uint32_t node = 1;
+  int L = 0;
+  while (su > tol) {
+    const float st = 0.5f * su, tm = s + st;
+    const bool right = r > tm;
+    if (right) s = tm;
+    node = 2 * node + (right ? 1u : 0u);
+    su = st;
+    L++;
+  }
+  int d = 0;
+  if (L <= kVbtCacheLevels && C.traj == (long long)traj) {
+    const uint32_t x = node ^ C.node;
+    d = x == 0 ? L : L - 1 - (31 - __clz(x));  // levels shared with the cached path
+  } else {
+    const float4 z = vbt_normal_quad(P.seed, tj, 0u, kVbtRoot, quad);
+    if (L <= kVbtCacheLevels) {
+      C.traj = (long long)traj;
+#pragma unroll
+      for (int q = 0; q < 4; q++) C.ws[0][q] = 0.f;
+      C.wsu[0][0] = z.x;
+      C.wsu[0][1] = z.y;
+      C.wsu[0][2] = z.z;
+      C.wsu[0][3] = z.w;
+    }
+  }
+  float ws[4], wsu[4];
+  if (L <= kVbtCacheLevels) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      ws[q] = C.ws[d][q];
+      wsu[q] = C.wsu[d][q];
+    }
+  } else {  // deeper than the cache: plain descent from the root
+    const float4 z = vbt_normal_quad(P.seed, tj, 0u, kVbtRoot, quad);
+    ws[0] = ws[1] = ws[2] = ws[3] = 0.f;
+    wsu[0] = z.x;
+    wsu[1] = z.y;
+    wsu[2] = z.z;
+    wsu[3] = z.w;
+  }
+  // replay the first d decisions for the interval at level d
+  s = 0.f;
+  su = 1.f;
+  for (int l = 0; l < d; l++) {
+    const float st = 0.5f * su, tm = s + st;
+    if (r > tm) s = tm;
+    su = st;
+  }
+  for (int l = d; l < L; l++) {
+    const float st = 0.5f * su, tm = s + st;
+    const float4 z = vbt_normal_quad(P.seed, tj, node >> (L - l), kVbtMid, quad);
+    const float a = 0.5f * sqrtf(su);
+    const float zz[4] = {z.x, z.y, z.z, z.w};
+    const bool right = r > tm;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const float m = 0.5f * wsu[q];
+      const float wst = m + a * zz[q], wtu = m - a * zz[q];
+      if (right) {
+        ws[q] += wst;
+        wsu[q] = wtu;
+      } else {
+        wsu[q] = wst;
+      }
+    }
+    if (right) s = tm;
+    su = st;
+    if (l + 1 <= kVbtCacheLevels) {
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        C.ws[l + 1][q] = ws[q];
+        C.wsu[l + 1][q] = wsu[q];
+      }
+    }
+  }
+  C.node = node;
+  const float sr = fmaxf(r - s, 0.f), ru = fmaxf(su - sr, 0.f);
+  const float4 z = vbt_normal_quad(P.seed, tj, node, kVbtLeaf, quad);
+  const float bb = sqrtf(sr * ru / su), f = sr / su;
+  const float sq = P.vbt_sqrt_len;
+  return make_float4(sq * (ws[0] + f * wsu[0] + bb * z.x), sq * (ws[1] + f * wsu[1] + bb * z.y),
+                     sq * (ws[2] + f * wsu[2] + bb * z.z), sq * (ws[3] + f * wsu[3] + bb * z.w));
 }
 
 }  // namespace gbdx
