@@ -307,6 +307,17 @@ def workload_backsolve(dev, flush, steps, warmup, terms_for, solver, ctrl, savea
                                 "sample": f"{n_g} trajectories backward only, FP64 oracle, "
                                           f"{dt_cpu:.2f} s"}}
         if name == "rms_norm":
+            peaks, src = measured_peaks()
+            n_par = int(low.params.numel())
+            stream = float(st[:, 0].double().sum().item()) * 2 * 4 * n_par
+            ent["roofline"] = {
+                "bound": "hbm", "achieved": stream / (ms / 1e3) / 1e9,
+                "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                "frac": stream / (ms / 1e3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
+                "peak_source": src,
+                "work": "a_theta double buffer: 8 bytes per parameter per trajectory-step "
+                        "(read a_theta0, write the candidate); timed region = forward + "
+                        "backward"}
             # the plain form: one trajectory per thread, FP32 CUDA cores
             plow = Lowered(terms_for("bf16"), solver, 0.0, 1.0, None, y0_d, None, saveat, ctrl,
                            adj, 4096, "plain", 0, 0, want_grad=True)
@@ -318,10 +329,7 @@ def workload_backsolve(dev, flush, steps, warmup, terms_for, solver, ctrl, savea
             ms_p = _events_time(fwd_bwd_plain, 1, 0, flush)  # one ~40 s solve
             ent["plain_forward_adjoint"] = {"grads_per_s": B / (ms_p / 1e3), "ms": ms_p}
             ent["fused_over_plain"] = ms_p / ms
-            # a_theta double buffer: read a_theta0 + write the candidate per row-step
-            n_par = int(low.params.numel())
-            ent["a_theta_stream_bytes"] = float(st[:, 0].double().sum().item()) * 2 * 4 * n_par
-            ent["a_theta_stream_GBps"] = ent["a_theta_stream_bytes"] / (ms / 1e3) / 1e9
+            ent["a_theta_stream_bytes"] = stream
         out[f"backsolve_{name}"] = ent
     return out
 
@@ -351,6 +359,50 @@ def profile_backsolve(dev, B, seminorm, n):
     ok = bool((res == 0).all().item()) and bool((bres == 0).all().item())
     print(json.dumps({"profile": "backsolve", "seminorm": seminorm, "solves": n,
                       "all_successful": ok}))
+    if not ok:
+        sys.exit(1)
+
+
+def profile_neural(dev, which, B, n):
+    """n fused solves of a neural workload at batch B, for ncu: the forward of
+    the neural ODE (64-128-128-64), its forward + RecursiveCheckpointAdjoint
+    backward, the wide neural ODE forward or the neural SDE forward."""
+    import torch
+    import diffrax_gb300 as dfx
+    from diffrax_gb300._integrate import Lowered
+    wide, sde = which == "neural_ode_wide", which == "neural_sde"
+    widths = [64, 256, 256, 64] if wide else ([32, 64, 64, 32] if sde else [64, 128, 128, 64])
+    D = widths[0]
+    Ws, bs = _mlp_np(widths, 21)
+    y0 = torch.tensor(np.random.default_rng(24).standard_normal((B, D)).astype(np.float32),
+                      device=dev)
+    field = dfx.MLPField([torch.tensor(W, device=dev) for W in Ws],
+                         [torch.tensor(b, device=dev) for b in bs])
+    if sde:
+        rng = np.random.default_rng(25)
+        Wsig = torch.tensor((rng.standard_normal((D, D)) / np.sqrt(D)).astype(np.float32),
+                            device=dev)
+        bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (D,), key=23)
+        terms = dfx.MultiTerm(dfx.ODETerm(field), dfx.ControlTerm(
+            dfx.TanhDiagonalDiffusion(Wsig, torch.zeros(D, device=dev)), bm))
+        solver, ctrl, dt0, saveat = dfx.Heun(), dfx.ConstantStepSize(), 0.01, dfx.SaveAt(t1=True)
+    else:
+        terms = dfx.ODETerm(field)
+        solver, ctrl, dt0 = dfx.Tsit5(), dfx.PIDController(rtol=1e-5, atol=1e-7), None
+        saveat = dfx.SaveAt(ts=np.linspace(0, 1, 32)) if wide else dfx.SaveAt(t1=True)
+    grad = which == "neural_ode_grad"
+    low = Lowered(terms, solver, 0.0, 1.0, dt0, y0, None, saveat, ctrl,
+                  dfx.RecursiveCheckpointAdjoint(checkpoints=64), 4096, "fused", 0, 0,
+                  want_grad=grad)
+    for _ in range(n):
+        if grad:
+            ys, _, res, _, ws = low.run_forward(keep_workspace=True)
+            low.run_backward(ws, ys * (2.0 / ys.numel()), low.y0, low.params)
+        else:
+            ys, _, res, _ = low.run_forward()
+    torch.cuda.synchronize()
+    ok = bool((res == 0).all().item())
+    print(json.dumps({"profile": which, "solves": n, "all_successful": ok}))
     if not ok:
         sys.exit(1)
 
@@ -429,6 +481,22 @@ def workload_neural(dev, flush, steps, warmup, kind):
     out["fused_forward"]["max_rel_err_vs_fp64_oracle"] = float(e.max())
     out["fused_forward"]["median_rel_err_vs_fp64_oracle"] = float(np.median(e))
     out["mean_attempted_steps"] = float(fwd.run_forward()[3][:, 0].float().mean().item())
+    # Tensor-core roofline of the fused forward: algorithmic field flops
+    # (2 sum in*out per evaluation, Tsit5/Dopri5 6 evaluations per attempted
+    # step, Heun 2) against the measured dense BF16 peak; the hi/lo operands
+    # execute 3x (2x with single-BF16 weights) as many tensor-core flops.
+    peaks, src = measured_peaks()
+    evals = 2 if kind == "sde" else 6
+    fl_eval = 2 * sum(widths[i] * widths[i + 1] for i in range(3))
+    if sde:
+        fl_eval += 2 * D * D
+    alg = B * out["mean_attempted_steps"] * evals * fl_eval / (ms_f / 1e3) / 1e12
+    mult = 3 if widths[1] <= 128 else 2
+    out["fused_forward"]["roofline"] = {
+        "bound": "tensor", "achieved": alg, "peak": peaks.get("bf16_tflops", 1900.0),
+        "unit": "TFLOP/s", "frac": alg / peaks.get("bf16_tflops", 1900.0), "peak_source": src,
+        "executed_tensor_tflops": alg * mult,
+        "work": f"{fl_eval} flop per field evaluation x {evals} evaluations per attempted step"}
     out["cpu_baseline_forward"] = _oracle_rate(
         lambda: O.solve(desc, 0.0, 1.0, dt0, y0[:512].astype(np.float64), params=params, ts=ts,
                         nthreads=cores), 512, cores)
@@ -486,7 +554,8 @@ def main():
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the other configurations")
     ap.add_argument("--profile", default=None,
-                    choices=["fused", "plain", "backsolve", "backsolve_seminorm"],
+                    choices=["fused", "plain", "backsolve", "backsolve_seminorm", "neural_ode",
+                             "neural_ode_grad", "neural_ode_wide", "neural_sde"],
                     help="run warmup + steps eager solves of one kernel only (for ncu); "
                          "backsolve*: forward + backward of the wide neural ODE at --batch")
     args = ap.parse_args()
@@ -563,6 +632,9 @@ def main():
         profile_backsolve(dev, B, args.profile == "backsolve_seminorm",
                           args.warmup + args.steps)
         return
+    if args.profile and args.profile.startswith("neural"):
+        profile_neural(dev, args.profile, B, args.warmup + args.steps)
+        return
     if args.profile:
         low = lowered(args.profile)
         for _ in range(args.warmup + args.steps):
@@ -633,17 +705,25 @@ def main():
         fp64 = steps_total * FP64_OPS_PER_STEP / t_s / 1e12
         gbs = B * BYTES_PER_TRAJ / t_s / 1e9
         traffic = ncu_traffic()
+        # The fused kernel's own bound is FP64 issue (t and dt in FP64 on a part
+        # whose FP64 pipe runs at ~1/64 of the FP32 rate; ncu: FP64 pipe 73 %
+        # active, DRAM 0.03 %): the HBM line is reported in the contract's
+        # form, with the compute rates that explain it beside it.
+        hbm_peak = peaks.get("hbm_gbs", 6800.0)
         roofline = {
-            "bound": "fp32", "achieved": fp32, "peak": FP32_PEAK_TFLOPS_NOMINAL,
-            "unit": "TFLOP/s", "frac": fp32 / FP32_PEAK_TFLOPS_NOMINAL, "traffic": traffic,
-            "peak_source": "nominal FP32 FMA rate at 2.07 GHz (no measured FP32 peak)",
-            "work": f"{FP32_FLOPS_PER_STEP} FP32 flop per attempted step x "
-                    f"{steps_total} attempted steps per launch",
+            "bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+            "frac": gbs / hbm_peak, "traffic": traffic, "peak_source": src,
+            "work": f"{BYTES_PER_TRAJ} algorithmic bytes per trajectory x {B} per launch",
+            "limiter": "FP64 issue of the t/dt updates (ncu: FP64 pipe 73 % active); "
+                       "see profiles/fused_kernel_vdp_dopri5.md",
             "fp64": {"achieved": fp64, "peak": FP64_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
-                     "frac": fp64 / FP64_PEAK_TFLOPS_NOMINAL},
-            "hbm": {"achieved": gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                    "frac": gbs / peaks.get("hbm_gbs", 6800.0), "peak_source": src,
-                    "algorithmic_bytes_per_launch": B * BYTES_PER_TRAJ},
+                     "frac": fp64 / FP64_PEAK_TFLOPS_NOMINAL,
+                     "peak_source": "nominal GB300 FP64 rate"},
+            "fp32": {"achieved": fp32, "peak": FP32_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
+                     "frac": fp32 / FP32_PEAK_TFLOPS_NOMINAL,
+                     "work": f"{FP32_FLOPS_PER_STEP} FP32 flop per attempted step x "
+                             f"{steps_total} attempted steps per launch",
+                     "peak_source": "nominal FP32 FMA rate at 2.07 GHz"},
         }
         # Accuracy of both kernels against the FP64 oracle on the same inputs.
         n_chk = min(B, 4096)
