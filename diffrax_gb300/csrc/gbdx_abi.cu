@@ -656,8 +656,13 @@ int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double 
     e = problem->bs.launch(P, Q, L.n_cta, s);
     if (e != cudaSuccess) return cuda_fail(e, "backsolve launch");
   }
-  e = gbdx::launch_reduce_partials(Q.psum, Q.pcomp, batch > 0 ? L.n_cta : 0, np,
-                                   static_cast<float *>(grad_params), s);
+  // the tensor-core mode keeps the weight blocks in fragment order
+  if (d.mlp_precision == GBDX_MLP_FP32)
+    e = gbdx::launch_reduce_partials(Q.psum, Q.pcomp, batch > 0 ? L.n_cta : 0, np,
+                                     static_cast<float *>(grad_params), s);
+  else
+    e = gbdx::launch_reduce_partials_frag(Q.psum, Q.pcomp, batch > 0 ? L.n_cta : 0, D, H,
+                                          static_cast<float *>(grad_params), s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
   return GBDX_OK;
 }

@@ -657,16 +657,21 @@ __device__ __forceinline__ float theta_layer_tc(BsPassOps<SH> &ps, const float *
   static_assert(TILES % SH::WARPS == 0, "parameter tiles split");
   constexpr int U = TPW < 16 ? TPW : 16;  // tiles per load batch
   static_assert(TPW % U == 0, "parameter tile batches");
-  const int g = lane >> 2, c = lane & 3;
   float accn = 0.f;
-  // the first batch's loads do not depend on the operands: issue them first
+  // 1. operands.  The record loads go first, then the first tile batch of
+  // a_theta0 (independent of the operands), then the operand arithmetic.
+  static_assert(NI <= SH::THREADS && NO <= SH::THREADS, "one operand row per thread");
+  const bool own_i = tid < NI, own_o = tid < NO;
+  float vv[S], uu[S];
+#pragma unroll
+  for (int j = 0; j < S; j++) {
+    vv[j] = own_i ? rec_r[j * STR + VOFF + tid] : 0.f;
+    uu[j] = own_o ? -h * rec_r[j * STR + UOFF + tid] : 0.f;
+  }
   float xa[U][4], xb[U][4];
   tc_load<U, TPW, WOFF>(xa, a0, 0, warp, lane);
-  // 1. operands
-  for (int i = tid; i < NI; i += SH::THREADS) {
-    float vv[S];
-#pragma unroll
-    for (int j = 0; j < S; j++) vv[j] = rec_r[j * STR + VOFF + i];
+  if (own_i) {
+    const int i = tid;
     float b1 = vv[0], b3 = 0.f;
 #pragma unroll
     for (int k = 0; k < 16; k++) {
@@ -685,10 +690,8 @@ __device__ __forceinline__ float theta_layer_tc(BsPassOps<SH> &ps, const float *
     ps.B1[i] = b1;
     ps.B3[i] = b3;
   }
-  for (int o = tid; o < NO; o += SH::THREADS) {
-    float uu[S];
-#pragma unroll
-    for (int j = 0; j < S; j++) uu[j] = -h * rec_r[j * STR + UOFF + o];
+  if (own_o) {
+    const int o = tid;
     float a2 = 0.f, a3 = 0.f;
 #pragma unroll
     for (int k = 0; k < 16; k++) {
@@ -743,39 +746,43 @@ __device__ __forceinline__ float theta_pass_tc(BsPassOps<SH> &ps, const float *r
   return s;
 }
 
-// Fold a finished row's a_theta into the CTA's Kahan partial (flat layout).
-// The tensor-core mode stores the weight blocks in fragment order.
-template <class SH, int NO, int NI, int WOFF, bool FRAG>
-__device__ __forceinline__ void fold_weights(const float *a, float *psum, float *pcomp, int tid) {
-  for (int e = tid * 4; e < NO * NI; e += SH::THREADS * 4) {
-    const float4 v = __ldcs(reinterpret_cast<const float4 *>(a + WOFF + e));
-    if constexpr (FRAG) {
-      const int t = e >> 7, lane = (e & 127) >> 2;
-      const int og = (t / (NI / 8)) * 16 + (lane >> 2), ic = (t % (NI / 8)) * 8 + 2 * (lane & 3);
-      const int p0 = WOFF + og * NI + ic, p1 = p0 + 8 * NI;
-      kahan_add(psum + p0, pcomp + p0, v.x);
-      kahan_add(psum + p0 + 1, pcomp + p0 + 1, v.y);
-      kahan_add(psum + p1, pcomp + p1, v.z);
-      kahan_add(psum + p1 + 1, pcomp + p1 + 1, v.w);
-    } else {
-      const float x[4] = {v.x, v.y, v.z, v.w};
-      kahan4(psum + WOFF + e, pcomp + WOFF + e, x);
+// Fold a finished row's a_theta into the CTA's Kahan partial.  The partial
+// has the row buffers' layout (the weight blocks in fragment order in the
+// tensor-core mode), so the fold is elementwise; the final reduction
+// restores the flat order.
+template <class SH>
+__device__ __forceinline__ void fold_row(const float *a, float *psum, float *pcomp, int tid) {
+  constexpr int NP = SH::NP, STEP = SH::THREADS * 4, U = 4;
+  for (int e0 = tid * 4; e0 < NP; e0 += STEP * U) {
+    float4 v[U], sm[U], cp[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int e = e0 + u * STEP;
+      if (e < NP) {
+        v[u] = __ldcs(reinterpret_cast<const float4 *>(a + e));
+        sm[u] = *reinterpret_cast<const float4 *>(psum + e);
+        cp[u] = *reinterpret_cast<const float4 *>(pcomp + e);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int e = e0 + u * STEP;
+      if (e < NP) {
+        float sv[4] = {sm[u].x, sm[u].y, sm[u].z, sm[u].w};
+        float cv[4] = {cp[u].x, cp[u].y, cp[u].z, cp[u].w};
+        const float xv[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const float y = xv[q] - cv[q];
+          const float t = sv[q] + y;
+          cv[q] = (t - sv[q]) - y;
+          sv[q] = t;
+        }
+        *reinterpret_cast<float4 *>(psum + e) = make_float4(sv[0], sv[1], sv[2], sv[3]);
+        *reinterpret_cast<float4 *>(pcomp + e) = make_float4(cv[0], cv[1], cv[2], cv[3]);
+      }
     }
   }
-}
-
-template <class SH, bool FRAG>
-__device__ __forceinline__ void fold_row(const float *a, float *psum, float *pcomp, int tid) {
-  constexpr int D = SH::D, H = SH::H;
-  fold_weights<SH, H, D, SH::OW0, FRAG>(a, psum, pcomp, tid);
-  fold_weights<SH, H, H, SH::OW1, FRAG>(a, psum, pcomp, tid);
-  fold_weights<SH, D, H, SH::OW2, FRAG>(a, psum, pcomp, tid);
-  for (int o = tid; o < H; o += SH::THREADS) {
-    kahan_add(psum + SH::OB0 + o, pcomp + SH::OB0 + o, a[SH::OB0 + o]);
-    kahan_add(psum + SH::OB1 + o, pcomp + SH::OB1 + o, a[SH::OB1 + o]);
-  }
-  for (int o = tid; o < D; o += SH::THREADS)
-    kahan_add(psum + SH::OB2 + o, pcomp + SH::OB2 + o, a[SH::OB2 + o]);
 }
 
 // Block-wide sum of one value per thread, returned to every thread.
@@ -1014,8 +1021,7 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
       // finished rows: results, the a_theta fold, a fresh trajectory next time
       for (int r = 0; r < M; r++) {
         if (!(R.trans[r] && R.done[r])) continue;
-        if (!R.zero[r])
-          fold_row<SH, !PRECISE>(ath + (size_t(r) * 2 + R.cur[r]) * NP, psum, pcomp, tid);
+        if (!R.zero[r]) fold_row<SH>(ath + (size_t(r) * 2 + R.cur[r]) * NP, psum, pcomp, tid);
       }
       if (tid < M && R.trans[tid] && R.done[tid]) {
         const int64_t i = R.idx[tid];
@@ -1206,12 +1212,13 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
       }
     }
     if constexpr (TB::FSAL) {
-      for (int r = 0; r < M; r++) {
-        if (!(R.live[r] && R.keep[r])) continue;
-        const float *src = rec + (size_t(S - 1) * M + r) * REC;
-        float *dst = rec + size_t(r) * REC;
-        for (int k = tid * 4; k < REC; k += SH::THREADS * 4)
-          *reinterpret_cast<float4 *>(dst + k) = *reinterpret_cast<const float4 *>(src + k);
+      // the last stage's records become the next step's stage 0 (all rows at
+      // once: independent loads)
+      for (int f = tid * 4; f < M * REC; f += SH::THREADS * 4) {
+        const int r = f / REC;
+        if (R.live[r] && R.keep[r])
+          *reinterpret_cast<float4 *>(rec + f) =
+              *reinterpret_cast<const float4 *>(rec + size_t(S - 1) * M * REC + f);
       }
     }
     __syncthreads();
