@@ -458,10 +458,10 @@ __device__ void row_control(RowState<M> &R, int r, int D, const SolveParams &P) 
 // the work by row -- the even lane descends the tree for r0, the odd lane for
 // r0 + 8, each for all four dimensions of the quad from its cached path -- and
 // swap halves.  Every lane of the warp must call it.
-template <class SH, int M, int NE>
-__device__ __forceinline__ void vbt_owned(const SolveParams &P, const RowState<M> &R,
-                                          const int *flag, const double *tsel,
-                                          VbtQuadCache &vc, float (&W)[NE], int warp, int lane) {
+template <class SH, class ROWS, int NE>
+__device__ __forceinline__ void vbt_owned(const SolveParams &P, const ROWS &R, const int *flag,
+                                          const double *tsel, VbtQuadCache &vc, float (&W)[NE],
+                                          int warp, int lane) {
   static_assert(NE == 4, "one output tile per thread");
   int row0, col0;
   elem_rc<SH>(0, warp, lane, row0, col0);

@@ -425,6 +425,9 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
   }
 
   float K[S][NE], F[NE], sig[NE], dW[NE];
+  VbtQuadCache vc;  // this lane's tree path (SDE)
+  vc.traj = -1;
+  vc.node = 0;
   while (true) {
     // ---- A. row set-up: the step this row works on -----------------------
     if (tid < M) {
@@ -456,19 +459,14 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
       elem_rc<SH>(e, warp, lane, row, col);
       hrow[e] = R.h[row];
     }
-    if (SDE) {
+    if constexpr (SDE) {
+      // W at both ends of the step from the lane's cached tree path (the
+      // evaluations of consecutive iterations lie within a step or two)
+      float wa[NE], wb[NE];
+      vbt_owned<SH>(P, R, R.live, R.t_lo, vc, wa, warp, lane);
+      vbt_owned<SH>(P, R, R.live, R.t_hi, vc, wb, warp, lane);
 #pragma unroll
-      for (int e = 0; e < NE; e += 2) {
-        int row, col;
-        elem_rc<SH>(e, warp, lane, row, col);
-        dW[e] = dW[e + 1] = 0.f;
-        if (R.live[row]) {
-          const float2 a = vbt_w_pair(P, R.idx[row], R.t_lo[row] * R.dir[row], col);
-          const float2 b = vbt_w_pair(P, R.idx[row], R.t_hi[row] * R.dir[row], col);
-          dW[e] = b.x - a.x;
-          dW[e + 1] = b.y - a.y;
-        }
-      }
+      for (int e = 0; e < NE; e++) dW[e] = wb[e] - wa[e];
     }
     // ---- B. forward stages of the step ----------------------------------
     float Yi[NE];
