@@ -115,6 +115,17 @@ __device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *G, int ldg,
   for (int ch = 0; ch < T / CH; ch++) {
     const int t = warp * T + ch * CH;
     const int ot = t / (N / 8), nt0 = t % (N / 8);
+    // the partials this chunk updates are loaded before its products, so the
+    // L2 latency overlaps the tensor-core work
+    float2 ps[CH][2], pc[CH][2];
+#pragma unroll
+    for (int j = 0; j < CH; j++)
+#pragma unroll
+      for (int hr = 0; hr < 2; hr++) {
+        const int p = off + (ot * 16 + g + hr * 8) * N + (nt0 + j) * 8 + 2 * c;
+        ps[j][hr] = *reinterpret_cast<const float2 *>(psum + p);
+        pc[j][hr] = *reinterpret_cast<const float2 *>(pcomp + p);
+      }
     float acc[CH][4];
 #pragma unroll
     for (int j = 0; j < CH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
@@ -123,11 +134,15 @@ __device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *G, int ldg,
 #pragma unroll
     for (int j = 0; j < CH; j++)
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int o = ot * 16 + g + ((q >> 1) << 3);
-        const int n = (nt0 + j) * 8 + 2 * c + (q & 1);
-        const int p = off + o * N + n;
-        kahan_add(psum + p, pcomp + p, acc[j][q]);
+      for (int hr = 0; hr < 2; hr++) {
+        const int p = off + (ot * 16 + g + hr * 8) * N + (nt0 + j) * 8 + 2 * c;
+        float s0 = ps[j][hr].x, s1 = ps[j][hr].y, c0 = pc[j][hr].x, c1 = pc[j][hr].y;
+        const float y0 = acc[j][2 * hr] - c0, y1 = acc[j][2 * hr + 1] - c1;
+        const float t0 = s0 + y0, t1 = s1 + y1;
+        c0 = (t0 - s0) - y0;
+        c1 = (t1 - s1) - y1;
+        *reinterpret_cast<float2 *>(psum + p) = make_float2(t0, t1);
+        *reinterpret_cast<float2 *>(pcomp + p) = make_float2(c0, c1);
       }
   }
 }
