@@ -422,6 +422,14 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
   P.c1 = problem->c1;
   P.c2 = problem->c2;
   P.c3 = problem->c3;
+  P.rtol_f = float(d.rtol);
+  P.atol_f = float(d.atol);
+  P.safety_f = float(d.safety);
+  P.factormin_f = float(d.factormin);
+  P.factormax_f = float(d.factormax);
+  P.c1_f = float(problem->c1);
+  P.c2_f = float(problem->c2);
+  P.c3_f = float(problem->c3);
   P.n_ts = d.n_ts;
   P.save_t0 = d.save_t0 ? 1 : 0;
   P.save_t1 = d.save_t1 ? 1 : 0;

@@ -876,14 +876,14 @@ __device__ void bs_row_control(BsRows<M> &R, int r, float n_norm, const SolvePar
     keep = acc < n_norm;
     const float lg = 0.5f * (log2f(n_norm) - __log2f(acc));
     float ex = 0.f;
-    if (P.c1 != 0.0) ex += float(P.c1) * lg;
-    if (P.c2 != 0.0) ex += float(P.c2) * R.hist1[r];
-    if (P.c3 != 0.0) ex += float(P.c3) * R.hist2[r];
-    float factor = float(P.safety) * exp2f(ex);
+    if (P.c1_f != 0.f) ex += P.c1_f * lg;
+    if (P.c2_f != 0.f) ex += P.c2_f * R.hist1[r];
+    if (P.c3_f != 0.f) ex += P.c3_f * R.hist2[r];
+    float factor = P.safety_f * exp2f(ex);
     const float hnew = isinf(lg) ? 0.f : lg;
     if (P.has_dtmin) keep = keep || R.at_dtmin[r];
-    const float fmn = keep ? 1.f : float(P.factormin);
-    const float fmx = keep ? float(P.factormax) : float(P.safety);
+    const float fmn = keep ? 1.f : P.factormin_f;
+    const float fmx = keep ? P.factormax_f : P.safety_f;
     factor = fminf(fmaxf(factor, fmn), fmx);
     dtn = dt * double(factor);
     if (P.has_dtmax) dtn = fmin(dtn, P.dtmax);
@@ -945,7 +945,7 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
   float *psum = Q.psum + size_t(blockIdx.x) * NP;
   float *pcomp = Q.pcomp + size_t(blockIdx.x) * NP;
   float *ath = Q.ath + size_t(blockIdx.x) * M * 2 * NP;
-  const float rtol = float(P.rtol), atol = float(P.atol);
+  const float rtol = P.rtol_f, atol = P.atol_f;
 
   FLD::stage(sm, W, tid);
   if (tid < M) {

@@ -294,6 +294,10 @@ struct SolveParams {
   double rtol, atol, safety, factormin, factormax, dtmin, dtmax;
   int has_dtmin, has_dtmax, force_dtmin;
   double c1, c2, c3;  // PID exponents (i+p+d)/k, -(p+2d)/k, d/k
+  // FP32 copies of the controller constants for the FP32-state kernels (the
+  // FP64 pipe of GB300 issues at ~1/64 of the FP32 rate: no per-step
+  // conversions)
+  float rtol_f, atol_f, safety_f, factormin_f, factormax_f, c1_f, c2_f, c3_f;
   int n_ts, save_t0, save_t1, n_save, max_steps;
   unsigned long long *queue;  // work-stealing counter (fused kernel)
   const int32_t *order;       // optional work order: queue slot -> trajectory

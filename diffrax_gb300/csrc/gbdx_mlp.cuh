@@ -378,14 +378,14 @@ __device__ void row_control(RowState<M> &R, int r, int D, const SolveParams &P) 
     keep = acc < float(D);
     const float lg = 0.5f * (log2f(float(D)) - __log2f(acc));
     float ex = 0.f;
-    if (P.c1 != 0.0) ex += float(P.c1) * lg;
-    if (P.c2 != 0.0) ex += float(P.c2) * R.hist1[r];
-    if (P.c3 != 0.0) ex += float(P.c3) * R.hist2[r];
-    float factor = float(P.safety) * exp2f(ex);
+    if (P.c1_f != 0.f) ex += P.c1_f * lg;
+    if (P.c2_f != 0.f) ex += P.c2_f * R.hist1[r];
+    if (P.c3_f != 0.f) ex += P.c3_f * R.hist2[r];
+    float factor = P.safety_f * exp2f(ex);
     const float hnew = isinf(lg) ? 0.f : lg;
     if (P.has_dtmin) keep = keep || R.at_dtmin[r];
-    const float fmn = keep ? 1.f : float(P.factormin);
-    const float fmx = keep ? float(P.factormax) : float(P.safety);
+    const float fmn = keep ? 1.f : P.factormin_f;
+    const float fmx = keep ? P.factormax_f : P.safety_f;
     factor = fminf(fmaxf(factor, fmn), fmx);
     dtn = dt * double(factor);
     if (P.has_dtmax) dtn = fmin(dtn, P.dtmax);
@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
           for (int q = 0; q < 2; q++) {
             const int e = j * 4 + half * 2 + q;
             const float ym = fmaxf(fabsf(Y0[e]), fabsf(nanrow ? Y0[e] : Y1[e]));
-            const float s = __fdividef(Er[e], fmaf(ym, float(P.rtol), float(P.atol)));
+            const float s = __fdividef(Er[e], fmaf(ym, P.rtol_f, P.atol_f));
             part = fmaf(s, s, part);
           }
           part += __shfl_xor_sync(0xffffffffu, part, 1);

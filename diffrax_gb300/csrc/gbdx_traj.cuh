@@ -250,16 +250,16 @@ struct Traj {
 #pragma unroll
         for (int n = 0; n < D; n++) {
           T ym = fmaxf(fabsf(y[n]), fabsf(any_nan ? y[n] : y1[n]));
-          T s = __fdividef(err[n], fmaf(ym, T(P.rtol), T(P.atol)));
+          T s = __fdividef(err[n], fmaf(ym, P.rtol_f, P.atol_f));
           acc = fmaf(s, s, acc);
         }
         keep = acc < T(D);
         const T lg = T(0.5) * (Math<T>::log2_(T(D)) - __log2f(acc));
         T ex = T(0);
-        if (P.c1 != 0.0) ex += T(P.c1) * lg;
-        if (P.c2 != 0.0) ex += T(P.c2) * h1;
-        if (P.c3 != 0.0) ex += T(P.c3) * h2;
-        factor = T(P.safety) * exp2f(ex);
+        if (P.c1_f != 0.f) ex += P.c1_f * lg;
+        if (P.c2_f != 0.f) ex += P.c2_f * h1;
+        if (P.c3_f != 0.f) ex += P.c3_f * h2;
+        factor = P.safety_f * exp2f(ex);
         hnew = isinf(lg) ? T(0) : lg;  // inv in {0, inf} -> 1 (pid.py:536-538)
       } else {
         T acc = T(0);
@@ -279,8 +279,9 @@ struct Traj {
         hnew = (inv == T(0) || isinf(inv)) ? T(1) : inv;
       }
       if (P.has_dtmin) keep = keep || at_dtmin;
-      const T fmn = keep ? T(1) : T(P.factormin);
-      const T fmx = keep ? T(P.factormax) : T(P.safety);
+      const T fmn = keep ? T(1) : (F32 ? T(P.factormin_f) : T(P.factormin));
+      const T fmx = keep ? (F32 ? T(P.factormax_f) : T(P.factormax))
+                         : (F32 ? T(P.safety_f) : T(P.safety));
       factor = fmin(fmax(factor, fmn), fmx);
       double dtn = prev_dt * double(factor);
       if (P.has_dtmax) dtn = fmin(dtn, P.dtmax);
