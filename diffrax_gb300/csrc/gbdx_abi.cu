@@ -521,10 +521,11 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
     int per_sm = d.ctas_per_sm;
     if (per_sm <= 0 && problem->mlp) per_sm = occ;
     if (per_sm <= 0) {
-      // Keep about B / 2.25 lanes resident: enough warps to feed the FP64 and
-      // FP32 pipes, few enough that every lane refills from the queue a couple
-      // of times (measured on the uneven Van der Pol batch).
-      per_sm = (int)((double)batch / (2.25 * cfg.block * sms) + 0.5);
+      // Keep about B / 1.7 lanes resident: enough warps to hide the step's
+      // dependency latency, few enough that lanes refill from the queue and
+      // the longest trajectories (started first) meet little contention
+      // (measured on the uneven Van der Pol batch).
+      per_sm = (int)((double)batch / (1.7 * cfg.block * sms) + 0.5);
       if (per_sm < 1) per_sm = 1;
       if (per_sm > occ) per_sm = occ;
     }

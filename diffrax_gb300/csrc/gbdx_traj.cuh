@@ -10,6 +10,7 @@
 #pragma once
 
 #include "gbdx_common.cuh"
+#include "gbdx_f64i.cuh"
 #include "gbdx_vbt.cuh"
 
 namespace gbdx {
@@ -39,7 +40,12 @@ __device__ __forceinline__ T tsit5_w(int j, T t) {
   }
 }
 
-template <int SOLVER, class FIELD, class T>
+// LAT selects the form of the FP32 copy of dt for the FP32-state kernels: the
+// hardware conversion (shortest latency; the fused kernel, whose time is set
+// by the step latency of its longest trajectories) or the integer-pipe one
+// (no FP64-pipe issue; the plain kernel, which keeps every trajectory
+// resident and is bound by FP64 issue).  Both give the same value.
+template <int SOLVER, class FIELD, class T, bool LAT = false>
 struct Traj {
   using TB = Tab<SOLVER>;
   static constexpr int D = FIELD::D;
@@ -52,6 +58,12 @@ struct Traj {
   T args[NA];
   double tprev, tnext, t1, floor1;
   double dtc;  // FP32 mode: tnext - tprev carried from the controller (saves a DADD)
+  // FP32 mode: the clip of tnext against t1 (_integrate.py:410-413) of the
+  // previous step is checked after this step's stages rather than before them
+  // (pend); a step that ran with a size the check would have changed is
+  // discarded and run again.  pkeep is that previous step's keep.
+  bool pend, pkeep;
+  bool live;  // tprev < t1, maintained without an FP64 comparison
   // PID history (pid.py:388-392).  FP32 keeps log2 of the inverse scaled
   // errors so the factor is one exp2 of a weighted sum; FP64 keeps the values.
   T h1, h2;
@@ -63,13 +75,7 @@ struct Traj {
   T wb[FIELD::SDE ? D : 1];  // SDE: W(tprev) of every component (FP32 fields only)
 
   __device__ __forceinline__ bool running(const SolveParams &P) const {
-    bool before_end;
-    if constexpr (F32) {
-      before_end = order_key(tprev) < order_key(t1);
-    } else {
-      before_end = tprev < t1;
-    }
-    return before_end && result == GBDX_SUCCESSFUL && nsteps < P.max_steps;
+    return live && result == GBDX_SUCCESSFUL && nsteps < P.max_steps;
   }
 
   __device__ __forceinline__ T *ys_row(const SolveParams &P, int slot) const {
@@ -111,6 +117,9 @@ struct Traj {
     }
     tnext = fmin(tn, b);
     dtc = tnext - a;
+    pend = false;
+    pkeep = true;
+    live = a < b;
     tprev = a;
     floor1 = t1_clip_floor(b);
     if constexpr (FIELD::SDE) {
@@ -148,7 +157,13 @@ struct Traj {
   __device__ void step(const SolveParams &P) {
     const double dt = F32 ? dtc : tnext - tprev;
     // control = dir * dt (WrapTerm, _term.py:742-745); a sign flip in FP32 mode
-    const T h = F32 ? T(dir > 0 ? dt : -dt) : T(dir * dt);
+    T h;
+    if constexpr (F32) {
+      const float hm = LAT ? float(dt) : f64i_to_f32(dt);
+      h = dir > 0 ? hm : -hm;
+    } else {
+      h = T(dir * dt);
+    }
     T k[S][D];
     T f[D], yi[D], y1[D], err[D], flast[D];
     T dw[FIELD::SDE ? D : 1], wn[FIELD::SDE ? D : 1], sg[FIELD::SDE ? D : 1];
@@ -231,6 +246,20 @@ struct Traj {
       err[n] = is_nan_(e) ? T(INFINITY) : e;
     }
 
+    if constexpr (F32) {
+      if (pend) {
+        pend = false;
+        if (order_key(tnext) > order_key(floor1)) {
+          tnext = pkeep ? t1 : tprev + 0.5 * (t1 - tprev);
+          dtc = tnext - tprev;
+          return;  // run the step again with the clipped size
+        }
+      }
+    }
+    // tnext never exceeds t1 here (it is min(t0 + dt0, t1) or clipped), so
+    // after the step tprev < t1 unless this step is kept and ends at t1
+    // (keys: a +0 tnext against a -0 t1 also ends).
+    const bool at_end = order_key(tnext) >= order_key(t1);
     bool keep;
     double nt0, nt1, dt_next;  // dt_next == nt1 - nt0 (FP32 mode carries it)
     if (P.controller == GBDX_PID) {
@@ -282,15 +311,23 @@ struct Traj {
       const T fmn = keep ? T(1) : (F32 ? T(P.factormin_f) : T(P.factormin));
       const T fmx = keep ? (F32 ? T(P.factormax_f) : T(P.factormax))
                          : (F32 ? T(P.safety_f) : T(P.safety));
-      factor = fmin(fmax(factor, fmn), fmx);
-      double dtn = prev_dt * double(factor);
-      if (P.has_dtmax) dtn = fmin(dtn, P.dtmax);
+      factor = F32 ? fminf(fmaxf(factor, fmn), fmx) : fmin(fmax(factor, fmn), fmx);
+      // FP32 mode: the widening of the factor and the comparisons run on the
+      // integer pipes (dt, dtmin and dtmax are never NaN); GB300's FP64
+      // conversions take as long as its FP64 multiply.
+      double dtn;
+      if constexpr (F32) {
+        dtn = prev_dt * f64i_from_f32(factor);
+      } else {
+        dtn = prev_dt * double(factor);
+      }
+      if (P.has_dtmax && order_key(dtn) > order_key(P.dtmax)) dtn = P.dtmax;
       if (P.has_dtmin) {
-        if (!P.force_dtmin && dtn < P.dtmin && result == GBDX_SUCCESSFUL)
-          result = GBDX_DT_MIN_REACHED;
+        const bool below = order_key(dtn) < order_key(P.dtmin);
+        if (!P.force_dtmin && below && result == GBDX_SUCCESSFUL) result = GBDX_DT_MIN_REACHED;
         if (at_dtmin && factor == T(1)) dtn = P.dtmin;
-        at_dtmin = dtn <= P.dtmin;
-        dtn = fmax(dtn, P.dtmin);
+        at_dtmin = order_key(dtn) <= order_key(P.dtmin);
+        if (at_dtmin) dtn = P.dtmin;
       }
       nt0 = keep ? tnext : tprev;
       nt1 = nt0 + dtn;
@@ -310,14 +347,13 @@ struct Traj {
       dt_next = F32 ? tn - nt0 : 0.0;
     }
     // Book-keeping (_integrate.py:410-413).  tprev and tnext never exceed t1
-    // (tnext starts at min(t0 + dt0, t1) and is clipped below), so the
-    // minimum with t1 is the identity; FP32 mode skips it and compares keys.
+    // (tnext starts at min(t0 + dt0, t1) and is clipped), so the minimum with
+    // t1 is the identity; FP32 mode skips it and defers the clip to the next
+    // step (pend).
     if constexpr (F32) {
-      if (order_key(nt1) > order_key(floor1)) {
-        nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
-        dt_next = nt1 - nt0;
-      }
       dtc = dt_next;
+      pend = true;
+      pkeep = keep;
     } else {
       nt0 = fmin(nt0, t1);
       if (nt1 > floor1) nt1 = keep ? t1 : nt0 + 0.5 * (t1 - nt0);
@@ -328,8 +364,8 @@ struct Traj {
       // inside [tprev, tnext] (_integrate.py:456-487).
       while (ts_index < P.n_ts) {
         const double tsv = __ldg(P.save_ts + ts_index);
-        const double tsd = dir * tsv;
-        if (!(tsd <= tnext)) break;
+        const double tsd = dir > 0 ? tsv : -tsv;
+        if (order_key(tsd) > order_key(tnext)) break;  // save times are never NaN
         const double thd = (tprev == tnext) ? 0.0 : (tsd - tprev) / (tnext - tprev);
         const T th = T(thd);
         T *o = ys_row(P, save_index);
@@ -365,6 +401,7 @@ struct Traj {
     nsteps++;
     tprev = nt0;
     tnext = nt1;
+    live = !(keep && at_end);
   }
 
   // Dense output inside the step, component n.  y holds y0 of the step.
@@ -457,7 +494,7 @@ __global__ void __launch_bounds__(128) plain_kernel(SolveParams P) {
 // ---------------------------------------------------------------------------
 template <int SOLVER, class FIELD, class T>
 __global__ void __launch_bounds__(256) fused_kernel(SolveParams P) {
-  Traj<SOLVER, FIELD, T> tr;
+  Traj<SOLVER, FIELD, T, true> tr;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   bool active = false;
