@@ -15,6 +15,14 @@
 
 namespace gbdx {
 
+// 1/x to the MUFU reciprocal's accuracy (the reciprocal inside __fdividef),
+// for normal x.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 template <class T>
 __device__ __forceinline__ T tsit5_w(int j, T t) {
   // Tsit5 dense-output weights b_j(theta) (tsit5.py:119-150).
@@ -275,11 +283,14 @@ struct Traj {
         // Sum of squares of err / (atol + rtol max(|y0|, |y1|)); keep <=> RMS < 1
         // <=> acc < D.  log2(1 / rms) = 0.5 (log2 D - log2 acc), so the factor
         // safety * inv^c1 * prev^c2 * prev2^c3 is one exp2 of a weighted sum.
+        // The reciprocal of the tolerance scale depends on y1 only, so it is
+        // formed while the last stage's field evaluation (which the error
+        // estimate waits for) is in flight.
         T acc = T(0);
 #pragma unroll
         for (int n = 0; n < D; n++) {
           T ym = fmaxf(fabsf(y[n]), fabsf(any_nan ? y[n] : y1[n]));
-          T s = __fdividef(err[n], fmaf(ym, P.rtol_f, P.atol_f));
+          T s = err[n] * rcp_approx(fmaf(ym, P.rtol_f, P.atol_f));
           acc = fmaf(s, s, acc);
         }
         keep = acc < T(D);
