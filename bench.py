@@ -705,17 +705,19 @@ def main():
         fp64 = steps_total * FP64_OPS_PER_STEP / t_s / 1e12
         gbs = B * BYTES_PER_TRAJ / t_s / 1e9
         traffic = ncu_traffic()
-        # The fused kernel's own bound is FP64 issue (t and dt in FP64 on a part
-        # whose FP64 pipe runs at ~1/64 of the FP32 rate; ncu: FP64 pipe 73 %
-        # active, DRAM 0.03 %): the HBM line is reported in the contract's
-        # form, with the compute rates that explain it beside it.
+        # The fused kernel's own bound is step latency: the longest trajectory's
+        # dependent steps (each FP64 instruction holds an SM sub-partition's
+        # FP64 unit for ~64 cycles on GB300), not HBM (DRAM ~0.03 %): the HBM
+        # line is reported in the contract's form, with the compute rates
+        # beside it.
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
         roofline = {
             "bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
             "frac": gbs / hbm_peak, "traffic": traffic, "peak_source": src,
             "work": f"{BYTES_PER_TRAJ} algorithmic bytes per trajectory x {B} per launch",
-            "limiter": "FP64 issue of the t/dt updates (ncu: FP64 pipe 73 % active); "
-                       "see profiles/fused_kernel_vdp_dopri5.md",
+            "limiter": "step latency of the longest trajectories (1031 dependent Dopri5 "
+                       "steps; each FP64 instruction holds an SM sub-partition's FP64 unit "
+                       "~64 cycles); see profiles/fused_kernel_vdp_dopri5.md",
             "fp64": {"achieved": fp64, "peak": FP64_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
                      "frac": fp64 / FP64_PEAK_TFLOPS_NOMINAL,
                      "peak_source": "nominal GB300 FP64 rate"},
