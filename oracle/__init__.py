@@ -21,6 +21,7 @@ from .build import build_oracle, oracle_lib_path
 
 __all__ = [
     "OracleDesc", "load", "solve", "grad_recursive", "vbt_increments", "normal4",
+    "dense_evaluate", "n_saves", "STAGES",
     "EULER", "HEUN", "DOPRI5", "TSIT5", "CONSTANT", "PID",
     "LOTKA_VOLTERRA", "VAN_DER_POL", "ORNSTEIN_UHLENBECK", "MLP", "LINEAR", "CALLBACK",
     "DIFF_NONE", "DIFF_OU", "DIFF_TANH_DIAG", "RESULT_NAMES",
@@ -51,7 +52,8 @@ class OracleDesc(ctypes.Structure):
         ("mlp_widths", ctypes.c_int32 * 9), ("diffusion", ctypes.c_int32),
         ("vbt_t0", ctypes.c_double), ("vbt_t1", ctypes.c_double),
         ("vbt_tol", ctypes.c_double), ("seed", ctypes.c_uint64),
-        ("norm", ctypes.c_int32), ("pad_", ctypes.c_int32),
+        ("norm", ctypes.c_int32), ("save_steps", ctypes.c_int32),
+        ("save_dense", ctypes.c_int32), ("pad_", ctypes.c_int32),
     ]
 
 
@@ -61,7 +63,19 @@ _DEFAULTS = dict(solver=TSIT5, controller=PID, field=LOTKA_VOLTERRA, dim=2,
                  dtmax=math.nan, force_dtmin=1, error_order=0.0, n_ts=0,
                  save_t0=0, save_t1=1, max_steps=4096, n_args=0, mlp_depth=0,
                  mlp_widths=(), diffusion=DIFF_NONE, vbt_t0=0.0, vbt_t1=1.0,
-                 vbt_tol=1e-3, seed=0, norm=0)
+                 vbt_tol=1e-3, seed=0, norm=0, save_steps=0, save_dense=0)
+
+STAGES = {EULER: 1, HEUN: 2, DOPRI5: 7, TSIT5: 7}
+
+
+def n_saves(desc) -> int:
+    """Output length of the descriptor's SaveAt (_integrate.py:1273-1293)."""
+    n = desc.save_t0 + desc.n_ts
+    if desc.save_steps:
+        n += desc.max_steps // desc.save_steps
+    if desc.save_t1 and (desc.save_steps == 0 or desc.max_steps % desc.save_steps):
+        n += 1
+    return n
 
 
 def make_desc(**kw) -> OracleDesc:
@@ -104,6 +118,11 @@ def load():
                               i64, dp, dp, VF_CB, ctypes.c_void_p, dp, dp, ip, ip,
                               ctypes.c_int]
     lib.orc_solve.restype = ctypes.c_int
+    lib.orc_solve_dense.argtypes = lib.orc_solve.argtypes[:-1] + [dp, dp, ip, ctypes.c_int]
+    lib.orc_solve_dense.restype = ctypes.c_int
+    lib.orc_dense_evaluate.argtypes = [ctypes.POINTER(OracleDesc), i64, dp, dp, i64, dp, dp,
+                                       dp, ip, i64, dp, i64, ctypes.c_int, ctypes.c_int, dp]
+    lib.orc_dense_evaluate.restype = ctypes.c_int
     lib.orc_grad_recursive.argtypes = [ctypes.POINTER(OracleDesc), i64, dp, dp, dp, i64,
                                        dp, dp, i64, dp, i64, dp, dp, dp, dp, ip, ip, dp,
                                        dp, dp, ctypes.c_int]
@@ -178,11 +197,17 @@ def solve(desc: OracleDesc, t0, t1, dt0, y0, args=None, params=None, ts=None,
     B = y0.shape[0] if y0.ndim == 2 else 1
     t0, t1, dt0, tstride, y0, args_arr, astride, params, ts = _prep(
         desc, B, t0, t1, dt0, y0, args, params, ts)
-    n_save = desc.save_t0 + desc.n_ts + desc.save_t1
+    n_save = n_saves(desc)
     ys = np.empty((B, n_save, desc.dim))
     ts_out = np.empty((B, n_save))
     res = np.empty(B, dtype=np.int32)
     stats = np.empty((B, 3), dtype=np.int32)
+    dense = None
+    if desc.save_dense:
+        L = desc.max_steps + 1
+        rec = (2 + STAGES[desc.solver]) * desc.dim
+        dense = dict(ts=np.empty((B, L)), info=np.empty((B, L - 1, rec)),
+                     n=np.empty(B, dtype=np.int32))
     cb = VF_CB(0)
     keep = None
     if callback is not None:
@@ -193,15 +218,47 @@ def solve(desc: OracleDesc, t0, t1, dt0, y0, args=None, params=None, ts=None,
             ov = np.ctypeslib.as_array(outp, shape=(dim,))
             ov[:] = callback(t, yv.copy())
         keep = cb = VF_CB(_cb)
-    rc = lib.orc_solve(ctypes.byref(desc), B, _dptr(t0), _dptr(t1), _dptr(dt0), tstride,
-                       _dptr(y0), _dptr(args_arr), astride, _dptr(params), _dptr(ts), cb,
-                       None, _dptr(ys), _dptr(ts_out),
-                       res.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
-                       stats.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), int(nthreads))
+    ip = ctypes.POINTER(ctypes.c_int32)
+    rc = lib.orc_solve_dense(ctypes.byref(desc), B, _dptr(t0), _dptr(t1), _dptr(dt0), tstride,
+                             _dptr(y0), _dptr(args_arr), astride, _dptr(params), _dptr(ts), cb,
+                             None, _dptr(ys), _dptr(ts_out), res.ctypes.data_as(ip),
+                             stats.ctypes.data_as(ip),
+                             _dptr(dense["ts"]) if dense else None,
+                             _dptr(dense["info"]) if dense else None,
+                             dense["n"].ctypes.data_as(ip) if dense else None, int(nthreads))
     del keep
     if rc != 0:
         raise ValueError(f"oracle rejected the problem (code {rc})")
-    return dict(ys=ys, ts=ts_out, result=res, stats=stats)
+    out = dict(ys=ys, ts=ts_out, result=res, stats=stats)
+    if dense:
+        out.update(dense_ts=dense["ts"], dense_info=dense["info"], dense_n=dense["n"])
+    return out
+
+
+def dense_evaluate(desc: OracleDesc, t0, t1, y0, sol, query, left=True, order=0):
+    """DenseInterpolation.evaluate (order 0) or .derivative (order 1) of a
+    solve(..., save_dense=1) result at `query` ([Q] shared or [B, Q]).
+    Returns [B, Q, dim]."""
+    lib = load()
+    y0 = _f64(y0)
+    B = y0.shape[0]
+    t0 = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, np.float64), (B,)))
+    t1 = np.ascontiguousarray(np.broadcast_to(np.asarray(t1, np.float64), (B,)))
+    q = _f64(query)
+    if q.ndim == 1:
+        Q, qstride = q.shape[0], 0
+    else:
+        Q, qstride = q.shape[1], q.shape[1]
+    out = np.empty((B, Q, desc.dim))
+    ip = ctypes.POINTER(ctypes.c_int32)
+    dn = np.ascontiguousarray(sol["dense_n"], dtype=np.int32)
+    rc = lib.orc_dense_evaluate(ctypes.byref(desc), B, _dptr(t0), _dptr(t1), 1, _dptr(y0),
+                                _dptr(_f64(sol["dense_ts"])), _dptr(_f64(sol["dense_info"])),
+                                dn.ctypes.data_as(ip), Q, _dptr(q), qstride, int(bool(left)),
+                                int(order), _dptr(out))
+    if rc != 0:
+        raise ValueError(f"oracle rejected the evaluation (code {rc})")
+    return out
 
 
 def grad_recursive(desc: OracleDesc, t0, t1, dt0, y0, grad_ys, args=None, params=None,
@@ -213,7 +270,7 @@ def grad_recursive(desc: OracleDesc, t0, t1, dt0, y0, grad_ys, args=None, params
     B = y0.shape[0]
     t0, t1, dt0, tstride, y0, args_arr, astride, params_arr, ts = _prep(
         desc, B, t0, t1, dt0, y0, args, params, ts)
-    n_save = desc.save_t0 + desc.n_ts + desc.save_t1
+    n_save = n_saves(desc)
     gys = _f64(grad_ys, (B, n_save, desc.dim))
     ys = np.empty((B, n_save, desc.dim))
     ts_out = np.empty((B, n_save))

@@ -76,6 +76,8 @@ typedef struct {
   double vbt_t0, vbt_t1, vbt_tol;
   uint64_t seed;
   int32_t norm;           /* used by the backsolve adjoint only */
+  int32_t save_steps;     /* SaveAt(steps=n): every n-th accepted step; 0 = off */
+  int32_t save_dense;     /* SaveAt(dense=True) */
   int32_t pad_;
 } orc_desc;
 
@@ -759,6 +761,11 @@ typedef struct {
   /* outputs */
   double *ys_out, *ts_out;
   int32_t *result, *stats;
+  /* SaveAt(dense=True): step times [B, max_steps + 1] (the direction-flipped
+   * frame of the loop, +inf where unused), per accepted step (y0, y1, k_0..k_{s-1})
+   * [B, max_steps, (2 + s) dim] (+inf where unused), and steps + 1 [B] */
+  double *dense_ts, *dense_info;
+  int32_t *dense_n;
 } SolveIO;
 
 /* A record of one accepted step, kept for the discretise-then-optimise VJP. */
@@ -791,9 +798,16 @@ static void tape_push(Tape *tp, int D, double tprev, double tnext, const double 
   tp->n++;
 }
 
+/* Output size of a SaveAt (_integrate.py:1273-1293). */
 static int n_save_of(const orc_desc *d) {
-  return (d->save_t0 ? 1 : 0) + d->n_ts + (d->save_t1 ? 1 : 0);
+  int n = (d->save_t0 ? 1 : 0) + d->n_ts;
+  if (d->save_steps > 0) n += d->max_steps / d->save_steps;
+  if (d->save_t1 && (d->save_steps == 0 || d->max_steps % d->save_steps != 0)) n += 1;
+  return n;
 }
+
+/* Dense info record length of one accepted step: (y0, y1, k_0..k_{s-1}). */
+static int dense_rec_of(const orc_desc *d) { return (2 + tableau_of(d->solver)->s) * d->dim; }
 
 static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
   const orc_desc *d = io->d;
@@ -846,6 +860,17 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
     tso[0] = t0;
     save_index = 1;
   }
+  /* SaveAt(dense=True): buffers full of inf, dense_ts[0] = t0 (_integrate.py:324-327,
+   * 1315-1323) */
+  const int drec = dense_rec_of(d);
+  double *dts = NULL, *dinf = NULL;
+  if (io->dense_ts) {
+    dts = io->dense_ts + bidx * (int64_t)(d->max_steps + 1);
+    dinf = io->dense_info + bidx * (int64_t)d->max_steps * drec;
+    for (int i = 0; i <= d->max_steps; i++) dts[i] = INFINITY;
+    for (int64_t i = 0; i < (int64_t)d->max_steps * drec; i++) dinf[i] = INFINITY;
+    dts[0] = t0;
+  }
   int first_step = 1;
   double f0[64];
   memset(f0, 0, sizeof f0);
@@ -891,6 +916,21 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
         tso[save_index] = dir * io->ts[ts_index];
         ts_index++; save_index++;
       }
+      /* _integrate.py:493-527: SaveAt(steps=n) saves (tnext, y1) of every n-th
+       * accepted step, after the ts of the step */
+      if (d->save_steps > 0 && (num_acc + 1) % d->save_steps == 0) {
+        for (int n = 0; n < D; n++) ys[(int64_t)save_index * D + n] = so.y1[n];
+        tso[save_index] = tnext;
+        save_index++;
+      }
+      /* _integrate.py:529-540: the step's dense info and its end time */
+      if (dts) {
+        dts[num_acc + 1] = tnext;
+        double *r = dinf + (int64_t)num_acc * drec;
+        memcpy(r, y, sizeof(double) * D);
+        memcpy(r + D, so.y1, sizeof(double) * D);
+        for (int j = 0; j < tab->s; j++) memcpy(r + (2 + j) * D, so.k[j], sizeof(double) * D);
+      }
       if (tape) tape_push(tape, D, tprev, tnext, y, lo, save_index);
       memcpy(y, so.y1, sizeof(double) * D);
       if (tab->fsal) { memcpy(f0, so.fsal_f, sizeof(double) * D); first_step = 0; }
@@ -909,8 +949,11 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
       save_index++;
     }
   }
-  /* _integrate.py:847-877: the t1 save goes to the next free slot */
-  if (d->save_t1) {
+  /* _integrate.py:847-877: the t1 save goes to the next free slot, unless
+   * SaveAt(steps=n) saved it: always for n = 1, for n > 1 when the accepted
+   * steps are a multiple of n */
+  int t1_via_steps = d->save_steps == 0 ? 0 : (d->save_steps == 1 ? 1 : (num_acc % d->save_steps == 0));
+  if (d->save_t1 && !t1_via_steps) {
     for (int n = 0; n < D; n++) ys[(int64_t)save_index * D + n] = y[n];
     tso[save_index] = tprev;
     if (tape) tape->t1_slot = save_index;
@@ -919,6 +962,7 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
   if (result == ORC_SUCCESSFUL && tprev < t1) result = ORC_MAX_STEPS_REACHED;
   for (int i = 0; i < n_save; i++) tso[i] *= dir;
   io->result[bidx] = result;
+  if (io->dense_n) io->dense_n[bidx] = num_acc + 1;
   io->stats[bidx * 3 + 0] = num_steps;
   io->stats[bidx * 3 + 1] = num_acc;
   io->stats[bidx * 3 + 2] = num_rej;
@@ -926,15 +970,18 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
 
 static void validate_desc(const orc_desc *d) { (void)d; init_tableaus(); }
 
-int orc_solve(const orc_desc *d, int64_t B, const double *t0, const double *t1,
-              const double *dt0, int64_t time_stride, const double *y0,
-              const double *args, int64_t args_stride, const double *params,
-              const double *ts, orc_vf_cb cb, void *cb_ctx, double *ys_out,
-              double *ts_out, int32_t *result, int32_t *stats, int nthreads) {
+int orc_solve_dense(const orc_desc *d, int64_t B, const double *t0, const double *t1,
+                    const double *dt0, int64_t time_stride, const double *y0,
+                    const double *args, int64_t args_stride, const double *params,
+                    const double *ts, orc_vf_cb cb, void *cb_ctx, double *ys_out,
+                    double *ts_out, int32_t *result, int32_t *stats, double *dense_ts,
+                    double *dense_info, int32_t *dense_n, int nthreads) {
   validate_desc(d);
   if (d->dim > 64 || d->dim < 1) return -1;
+  if (d->save_steps < 0) return -1;
+  if ((dense_ts != NULL) != (d->save_dense != 0)) return -1;
   SolveIO io = {d, t0, t1, dt0, time_stride, y0, args, args_stride, params, ts,
-                cb, cb_ctx, ys_out, ts_out, result, stats};
+                cb, cb_ctx, ys_out, ts_out, result, stats, dense_ts, dense_info, dense_n};
 #ifdef _OPENMP
   if (nthreads > 0 && d->field != ORC_CALLBACK) {
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
@@ -944,6 +991,140 @@ int orc_solve(const orc_desc *d, int64_t B, const double *t0, const double *t1,
 #endif
   (void)nthreads;
   for (int64_t b = 0; b < B; b++) solve_one(&io, b, NULL);
+  return 0;
+}
+
+int orc_solve(const orc_desc *d, int64_t B, const double *t0, const double *t1,
+              const double *dt0, int64_t time_stride, const double *y0,
+              const double *args, int64_t args_stride, const double *params,
+              const double *ts, orc_vf_cb cb, void *cb_ctx, double *ys_out,
+              double *ts_out, int32_t *result, int32_t *stats, int nthreads) {
+  if (d->save_dense) return -1;
+  return orc_solve_dense(d, B, t0, t1, dt0, time_stride, y0, args, args_stride, params,
+                         ts, cb, cb_ctx, ys_out, ts_out, result, stats, NULL, NULL, NULL,
+                         nthreads);
+}
+
+/* ------------------------------------------------------------------------ */
+/* DenseInterpolation.evaluate / derivative (_global_interpolation.py:315-393) */
+/* over the dense outputs of orc_solve_dense.                                 */
+/* ------------------------------------------------------------------------ */
+/* d/dtheta of the interp_linear_coeffs coefficients. */
+static void interp_deriv_coeffs(int solver, int s, double t, double *ay0, double *ay1,
+                                double g[7]) {
+  for (int j = 0; j < 7; j++) g[j] = 0.0;
+  double t2 = t * t, t3 = t2 * t;
+  switch (solver) {
+    case ORC_TSIT5: {
+      /* product rule on the factored weights of tsit5_weights */
+      double q, dq;
+      *ay0 = 0.0; *ay1 = 0.0;
+      q = t2 - 1.4364028541716351 * t + 0.7139816917074209; dq = 2 * t - 1.4364028541716351;
+      g[0] = -1.0530884977290216 * ((t - 1.3299890189751412) * q + t * q +
+                                     t * (t - 1.3299890189751412) * dq);
+      q = t2 - 2.1966568338249754 * t + 1.2949852507374631; dq = 2 * t - 2.1966568338249754;
+      g[1] = 0.1017 * (2 * t * q + t2 * dq);
+      q = t2 - 2.38535645472061657 * t + 1.57803468208092486; dq = 2 * t - 2.38535645472061657;
+      g[2] = 2.490627285651252793 * (2 * t * q + t2 * dq);
+      {
+        static const double C[4] = {-16.54810288924490272, 47.37952196281928122,
+                                    -34.87065786149660974, 2.5};
+        static const double A[4] = {1.21712927295533244, 1.203071208372362603, 1.2, 1.0};
+        static const double Bq[4] = {0.61620406037800089, 0.658047292653547382,
+                                     0.666666666666666667, 0.6};
+        for (int m = 0; m < 4; m++) {
+          double u = t - A[m], v = t - Bq[m];
+          g[3 + m] = C[m] * (v * t2 + u * t2 + u * v * 2 * t);
+        }
+      }
+      break;
+    }
+    case ORC_DOPRI5: {
+      double M = 64 * t3 - 96 * t2 + 32 * t;
+      *ay0 = -32 * t3 + 54 * t2 - 22 * t + M;
+      *ay1 = -32 * t3 + 42 * t2 - 10 * t;
+      for (int j = 0; j < 7; j++) g[j] = M * DOPRI5_CMID[j];
+      g[0] += -8 * t3 + 15 * t2 - 8 * t + 1;
+      g[6] += 8 * t3 - 9 * t2 + 2 * t;
+      break;
+    }
+    case ORC_HEUN:
+      *ay0 = 6 * t2 - 6 * t;
+      *ay1 = -6 * t2 + 6 * t;
+      g[0] = 3 * t2 - 4 * t + 1;
+      g[s - 1] = 3 * t2 - 2 * t;
+      break;
+    default:
+      *ay0 = -1.0; *ay1 = 1.0;
+      break;
+  }
+}
+
+/* searchsorted(ts, t, side) over the whole buffer (unused entries are +inf). */
+static int64_t search_sorted(const double *ts, int64_t n, double t, int left) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) / 2;
+    int go_right = left ? (ts[mid] < t) : (ts[mid] <= t);
+    if (go_right) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+int orc_dense_evaluate(const orc_desc *d, int64_t B, const double *t0, const double *t1,
+                       int64_t time_stride, const double *y0, const double *dense_ts,
+                       const double *dense_info, const int32_t *dense_n, int64_t Q,
+                       const double *q, int64_t q_stride, int left, int order,
+                       double *out) {
+  validate_desc(d);
+  const Tableau *tab = tableau_of(d->solver);
+  const int D = d->dim, s = tab->s, drec = dense_rec_of(d);
+  const int64_t L = d->max_steps + 1;
+  for (int64_t b = 0; b < B; b++) {
+    const double a0 = t0[b * time_stride], a1 = t1[b * time_stride];
+    const int dir = (a0 < a1) ? 1 : -1;
+    const double *ts = dense_ts + b * L;
+    const int64_t size = dense_n[b];
+    for (int64_t m = 0; m < Q; m++) {
+      double *o = out + (b * Q + m) * D;
+      const double t = q[b * q_stride + m] * dir;
+      /* trivial solve: y0 at t0 (_global_interpolation.py:344-345); the
+       * derivative of the constant there is zero */
+      if (size == 1 && t == a0 * dir) {
+        for (int n = 0; n < D; n++) o[n] = order ? 0.0 : y0[b * D + n];
+        continue;
+      }
+      if (size <= 1 || t < ts[0] || t > ts[size - 1]) {  /* _nan_if_out_of_bounds */
+        for (int n = 0; n < D; n++) o[n] = NAN;
+        continue;
+      }
+      int64_t idx = search_sorted(ts, L, t, left) - 1; /* _interpret_t */
+      if (idx < 0) idx = 0;
+      if (idx > size - 2) idx = size - 2;
+      const double *r = dense_info + (b * (L - 1) + idx) * drec;
+      StepOut so;
+      so.dim = D;
+      so.tprev = ts[idx];
+      so.tnext = ts[idx + 1];
+      memcpy(so.y0, r, sizeof(double) * D);
+      memcpy(so.y1, r + D, sizeof(double) * D);
+      for (int j = 0; j < s; j++) memcpy(so.k[j], r + (2 + j) * D, sizeof(double) * D);
+      for (int j = s; j < 7; j++) memset(so.k[j], 0, sizeof(double) * D);
+      if (!order) {
+        interp_eval(d->solver, &so, s, t, o);
+      } else {
+        /* d/dt = (d/dtheta) / (t1 - t0), back in the caller's direction */
+        double th = linear_rescale(so.tprev, t, so.tnext), ay0, ay1, g[7];
+        interp_deriv_coeffs(d->solver, s, th, &ay0, &ay1, g);
+        const double span = so.tnext - so.tprev;
+        for (int n = 0; n < D; n++) {
+          double v = ay0 * so.y0[n] + ay1 * so.y1[n];
+          for (int j = 0; j < s; j++) v += g[j] * so.k[j][n];
+          o[n] = span == 0.0 ? 0.0 : dir * v / span;
+        }
+      }
+    }
+  }
   return 0;
 }
 
@@ -1013,6 +1194,7 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
                        double *grad_args, double *grad_params, int nthreads) {
   validate_desc(d);
   if (d->dim > 64 || d->dim < 1) return -1;
+  if (d->save_steps || d->save_dense) return -2; /* forward outputs only */
   const Tableau *tab = tableau_of(d->solver);
   const int D = d->dim;
   const int n_save = n_save_of(d);
@@ -1337,6 +1519,7 @@ int orc_backsolve(const orc_desc *d, int64_t B, const double *t0, const double *
   validate_desc(d);
   if (d->dim > 64 || d->dim < 1) return -1;
   if (d->field == ORC_CALLBACK || d->diffusion != ORC_DIFF_NONE) return -2;
+  if (d->save_steps || d->save_dense) return -2;
   const int64_t N = 2 * (int64_t)d->dim + d->n_args + n_params;
   BsIO io = {d, t0, t1, dt0, time_stride, ts_saved, ys, grad_ys, args, args_stride,
              params, n_params, grad_y0, grad_args, result, stats};

@@ -526,3 +526,133 @@ def test_vbt_conditional_bridge():
     resid = (ws - s * w1) / np.sqrt(s * (1 - s))
     assert scipy.stats.kstest(resid, "norm").pvalue > 1e-3
     assert abs(np.corrcoef(resid, w1)[0, 1]) < 0.03
+
+
+# ---------------------------------------------------------------------------
+# SaveAt(steps=n) and SaveAt(dense=True)
+# ---------------------------------------------------------------------------
+
+def test_saveat_steps_decay():
+    # test/test_saveat_solution.py:116-180: shapes (max_steps // n, plus a t1
+    # slot only when max_steps % n != 0) and the analytic values at the saved ts
+    for steps, t1, n in ((1, 0, 4096), (2, 0, 2048), (2, 1, 2048), (3, 1, 1366)):
+        d = _decay(save_steps=steps, save_t1=t1)
+        assert O.n_saves(d) == n
+        r = O.solve(d, 0.1, 1.1, None, [[2.1]], params=[[-0.5]])
+        assert r["ys"].shape == (1, n, 1) and r["result"][0] == 0
+        ts = r["ts"][0]
+        fin = np.isfinite(ts)
+        assert fin.sum() >= 1 and np.all(np.isinf(ts[~fin])) and np.all(ts[~fin] > 0)
+        assert np.all(np.diff(ts[fin]) > 0)
+        np.testing.assert_allclose(r["ys"][0, fin, 0], 2.1 * np.exp(-0.5 * (ts[fin] - 0.1)),
+                                   rtol=1e-5, atol=1e-8)
+        assert np.all(np.isinf(r["ys"][0, ~fin, 0]))
+        nacc = r["stats"][0, 1]
+        assert fin.sum() == nacc // steps + (t1 and nacc % steps != 0)
+        assert ts[fin][-1] == 1.1 or (steps > 1 and nacc % steps != 0 and not t1)
+
+
+@pytest.mark.parametrize("with_7", [True, False])
+def test_saveat_steps_skip(with_7):
+    # test/test_saveat_solution.py:198-247: Euler on the unit grid 0..7 (or
+    # 0..6); the reference's StepTo(ts) grid is ConstantStepSize(dt0=1) here
+    t1 = 7.0 if with_7 else 6.0
+    cases = [((2, 0, 0), [2, 4, 6], [2, 4, 6]),
+             ((2, 1, 0), [2, 4, 6, 7], [2, 4, 6]),
+             ((2, 1, 1), [0, 2, 4, 6, 7], [0, 2, 4, 6]),
+             ((3, 0, 0), [3, 6], [3, 6]),
+             ((3, 1, 0), [3, 6, 7], [3, 6]),
+             ((3, 1, 1), [0, 3, 6, 7], [0, 3, 6])]
+    for (steps, st1, st0), want7, want6 in cases:
+        d = O.make_desc(solver=O.EULER, controller=O.CONSTANT, field=O.LINEAR, dim=1,
+                        save_steps=steps, save_t1=st1, save_t0=st0, max_steps=10)
+        r = O.solve(d, 0.0, t1, 1.0, [[1.0]], params=[[-0.5]])
+        ts = r["ts"][0]
+        assert list(ts[np.isfinite(ts)]) == (want7 if with_7 else want6)
+
+
+def test_saveat_steps_vs_ts():
+    # test/test_saveat_solution.py:250-279: steps=2 with t0 saves the same
+    # points as ts=[0, 2, 4, 6] on the unit grid
+    d = O.make_desc(solver=O.EULER, controller=O.CONSTANT, field=O.LINEAR, dim=1,
+                    save_steps=2, save_t0=1, save_t1=0, max_steps=6)
+    r = O.solve(d, 0.0, 6.0, 1.0, [[1.0]], params=[[-0.5]])
+    d2 = O.make_desc(solver=O.EULER, controller=O.CONSTANT, field=O.LINEAR, dim=1,
+                     n_ts=4, save_t1=0, max_steps=6)
+    r2 = O.solve(d2, 0.0, 6.0, 1.0, [[1.0]], params=[[-0.5]], ts=[0.0, 2.0, 4.0, 6.0])
+    assert np.array_equal(r["ts"], r2["ts"]) and np.array_equal(r["ys"], r2["ys"])
+
+
+def test_saveat_t0_eq_t1_steps():
+    # test/test_saveat_solution.py:323-368 (the steps=1 sub): y0 at t0 and the
+    # three ts, then max_steps infs
+    d = O.make_desc(solver=O.DOPRI5, controller=O.CONSTANT, field=O.LINEAR, dim=1,
+                    save_t0=1, n_ts=3, save_t1=0, save_steps=1, max_steps=256)
+    r = O.solve(d, 1.0, 1.0, 0.1, [[2.0]], params=[[1.0]], ts=[1.0, 1.0, 1.0])
+    assert r["ys"].shape == (1, 4 + 256, 1)
+    assert np.all(r["ys"][0, :4, 0] == 2.0) and np.all(np.isinf(r["ys"][0, 4:, 0]))
+
+
+def test_dense_decay():
+    # test/test_saveat_solution.py:182-195: evaluate(0.2), evaluate(0.8),
+    # evaluate(0.2, 0.8) as the difference, derivative(0.2)
+    d = _decay(save_dense=1, save_t1=1)
+    r = O.solve(d, 0.1, 1.1, None, [[2.1]], params=[[-0.5]])
+    assert r["dense_n"][0] == r["stats"][0, 1] + 1
+    assert r["dense_ts"][0, 0] == 0.1 and r["dense_ts"][0, r["dense_n"][0] - 1] == 1.1
+    assert np.all(np.isinf(r["dense_ts"][0, r["dense_n"][0]:]))
+    v = O.dense_evaluate(d, 0.1, 1.1, [[2.1]], r, [0.2, 0.8])
+    assert tree_allclose(v[0, 0, 0], 2.1 * math.exp(-0.05))
+    assert tree_allclose(v[0, 1, 0], 2.1 * math.exp(-0.35))
+    g = O.dense_evaluate(d, 0.1, 1.1, [[2.1]], r, [0.2], order=1)
+    assert tree_allclose(g[0, 0, 0], -0.5 * 2.1 * math.exp(-0.05))
+    # outside [t0, t1]: NaN (_global_interpolation.py:367-378)
+    o = O.dense_evaluate(d, 0.1, 1.1, [[2.1]], r, [0.0, 1.2])
+    assert np.all(np.isnan(o))
+
+
+def test_dense_trivial():
+    # test/test_saveat_solution.py:431-447: t0 == t1 evaluates to y0 at t0
+    d = _decay(save_dense=1)
+    r = O.solve(d, 2.0, 2.0, None, [[2.1]], params=[[-0.5]])
+    assert r["dense_n"][0] == 1
+    v = O.dense_evaluate(d, 2.0, 2.0, [[2.1]], r, [2.0, 2.5])
+    assert v[0, 0, 0] == 2.1 and np.isnan(v[0, 1, 0])
+
+
+@pytest.mark.parametrize("solver", SOLVERS)
+def test_dense_matches_saveat_ts_and_derivative(solver):
+    # The dense interpolant at the ts equals SaveAt(ts) (both evaluate the
+    # step's local interpolation, _integrate.py:456-487 and
+    # _global_interpolation.py:339-353); the derivative matches the vector
+    # field to the interpolant's accuracy, and a central difference of the
+    # interpolant, left and right limits, and reverse time
+    A = np.array([[-0.3, 1.0], [-1.0, -0.3]])
+    ctrl = (dict(controller=O.CONSTANT) if solver == O.EULER else
+            dict(rtol=1e-6, atol=1e-8) if solver == O.HEUN else dict(rtol=1e-8, atol=1e-10))
+    dt0 = 0.01 if solver == O.EULER else None
+    for t0, t1 in ((0.0, 3.0), (3.0, 0.0)):
+        ts = np.linspace(t0, t1, 9)[1:-1]
+        d = O.make_desc(solver=solver, field=O.LINEAR, dim=2, save_dense=1, save_t1=0,
+                        n_ts=len(ts), **ctrl)
+        r = O.solve(d, t0, t1, None if dt0 is None else math.copysign(dt0, t1 - t0),
+                    [[1.0, 0.5]], params=A, ts=ts)
+        assert r["result"][0] == 0
+        v = O.dense_evaluate(d, t0, t1, [[1.0, 0.5]], r, ts)
+        np.testing.assert_allclose(v[0], r["ys"][0], rtol=1e-13, atol=1e-14)
+        # derivative away from the step boundaries (Euler's interpolant has a
+        # kink at each one)
+        tq = ts + math.copysign(0.0031, t1 - t0)
+        g = O.dense_evaluate(d, t0, t1, [[1.0, 0.5]], r, tq, order=1)
+        h = 1e-6
+        fd = (O.dense_evaluate(d, t0, t1, [[1.0, 0.5]], r, tq + h) -
+              O.dense_evaluate(d, t0, t1, [[1.0, 0.5]], r, tq - h)) / (2 * h)
+        np.testing.assert_allclose(g, fd, rtol=1e-5, atol=1e-7)
+        vq = O.dense_evaluate(d, t0, t1, [[1.0, 0.5]], r, tq)
+        tol = 0.05 if solver == O.EULER else 1e-4
+        np.testing.assert_allclose(g[0], vq[0] @ A.T, rtol=tol, atol=tol * 1e-1)
+        # at a step boundary the left and right limits use the two neighbouring steps
+        kb = r["dense_ts"][0, 3] * (1 if t1 > t0 else -1)
+        lv = O.dense_evaluate(d, t0, t1, [[1.0, 0.5]], r, [kb], left=True)
+        rv = O.dense_evaluate(d, t0, t1, [[1.0, 0.5]], r, [kb], left=False)
+        np.testing.assert_allclose(lv, rv, rtol=1e-12, atol=1e-13)
