@@ -10,7 +10,7 @@ from ._core import (
     RESULTS, SaveAt, Solution, Tsit5, VanDerPol, VirtualBrownianTree, adjoint_rms_seminorm,
     rms_norm,
 )
-from ._integrate import diffeqsolve, lower, oracle_fields
+from ._integrate import DenseInterpolation, diffeqsolve, lower, oracle_fields
 
 __version__ = "0.1.0"
 

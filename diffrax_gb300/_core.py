@@ -262,17 +262,25 @@ class PIDController(AbstractStepSizeController):
 
 
 class SaveAt:
-    def __init__(self, *, t0: bool = False, t1: bool = False, ts=None, steps: bool = False,
+    """diffrax/_saveat.py:69-105.  ``steps`` is a bool or an int n (save every
+    n-th accepted step); ``dense=True`` records the solution's dense output
+    (``Solution.evaluate`` / ``Solution.derivative``)."""
+
+    def __init__(self, *, t0: bool = False, t1: bool = False, ts=None, steps=False,
                  dense: bool = False, solver_state: bool = False,
                  controller_state: bool = False, made_jump: bool = False):
-        if steps or dense:
-            raise NotImplementedError("SaveAt(steps=...) and SaveAt(dense=...) are not "
-                                      "supported by this library")
         if solver_state or controller_state or made_jump:
             raise NotImplementedError("saving solver/controller state is not supported")
-        if not (t0 or t1 or ts is not None):
+        # SubSaveAt.__init__: steps=True means every step (_saveat.py:40-43)
+        if isinstance(steps, bool):
+            steps = 1 if steps else 0
+        steps = int(steps)
+        if steps < 0:
+            raise ValueError("SaveAt(steps=n) needs n >= 0")
+        if not (t0 or t1 or ts is not None or steps or dense):
             raise ValueError("Empty saveat -- nothing will be saved.")
         self.t0, self.t1, self.ts = bool(t0), bool(t1), ts
+        self.steps, self.dense = steps, bool(dense)
 
 
 # ---------------------------------------------------------------------------
@@ -341,3 +349,19 @@ class Solution:
     ys: Any        # [B, n_save, dim]
     stats: dict    # num_steps / num_accepted_steps / num_rejected_steps: [B] int32
     result: Any    # [B] int32 RESULTS codes
+    interpolation: Any = None  # DenseInterpolation under SaveAt(dense=True)
+
+    def evaluate(self, t0, t1=None, left: bool = True):
+        """y(t0) of every trajectory from the dense output, or y(t1) - y(t0)
+        (diffrax/_solution.py:128-152).  t0 is a scalar ([B, dim] out), [Q]
+        times shared by the batch or [B, Q] per trajectory ([B, Q, dim] out)."""
+        if self.interpolation is None:
+            raise ValueError("Dense solution has not been saved; pass SaveAt(dense=True).")
+        return self.interpolation.evaluate(t0, t1, left)
+
+    def derivative(self, t, left: bool = True):
+        """dy/dt of the numerical solution (diffrax/_solution.py:154-201);
+        shapes as evaluate."""
+        if self.interpolation is None:
+            raise ValueError("Dense solution has not been saved; pass SaveAt(dense=True).")
+        return self.interpolation.derivative(t, left)

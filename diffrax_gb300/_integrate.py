@@ -65,7 +65,8 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
              factormin=0.2, factormax=10.0, dtmin=None, dtmax=None, force_dtmin=1,
              error_order=0.0, mlp_depth=0, mlp_widths=(), diffusion=0, vbt_t0=0.0,
              vbt_t1=1.0, vbt_tol=1e-3, seed=0, norm=0, adjoint=0, checkpoints=0,
-             schedule=SCHEDULES[schedule], mlp_precision=0, pad1=0)
+             schedule=SCHEDULES[schedule], mlp_precision=0,
+             save_steps=int(saveat.steps), save_dense=int(saveat.dense), pad2=0)
     if hasattr(drift, "lower_fields"):
         f.update(drift.lower_fields(dim))
     if isinstance(stepsize_controller, PIDController):
@@ -266,6 +267,34 @@ class Lowered:
             return ys, ts_out, res, stats, ws
         return ys, ts_out, res, stats
 
+    def run_forward_dense(self, stream=None):
+        """Forward solve under SaveAt(dense=True): the saved outputs plus the
+        dense buffers (step times, per-step records, entry counts)."""
+        dev = self.device
+        B, D, n_save = self.B, self.dim, self.n_save
+        L = int(self.fields["max_steps"]) + 1
+        stages = {0: 1, 1: 2, 2: 7, 3: 7}[self.fields["solver"]]
+        ys = torch.empty((B, n_save, D), dtype=self.dtype, device=dev)
+        ts_out = torch.empty((B, n_save), dtype=torch.float64, device=dev)
+        res = torch.empty((B,), dtype=torch.int32, device=dev)
+        stats = torch.empty((B, 3), dtype=torch.int32, device=dev)
+        dense_ts = torch.empty((B, L), dtype=torch.float64, device=dev)
+        dense_info = torch.empty((B, L - 1, (2 + stages) * D), dtype=self.dtype, device=dev)
+        dense_n = torch.empty((B,), dtype=torch.int32, device=dev)
+        ws_bytes = self.problem.workspace_size(B)
+        ws = torch.empty((max(ws_bytes, 1),), dtype=torch.uint8, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev).cuda_stream
+        p = lambda t: None if t is None or t.numel() == 0 else t.data_ptr()  # noqa: E731
+        rc = self.problem.lib.gbdx_solve_fwd_dense(
+            self.problem.handle, B, p(self.t0), p(self.t1), p(self.dt0), self.tstride,
+            p(self.y0), p(self.args), self.args_stride, p(self.params), p(self.save_ts),
+            p(ys), p(ts_out), p(res), p(stats), p(dense_ts), p(dense_info), p(dense_n),
+            p(ws), ws_bytes, stream)
+        _lib.check(rc, "gbdx_solve_fwd_dense")
+        interp = DenseInterpolation(self, dense_ts, dense_info, dense_n)
+        return ys, ts_out, res, stats, interp
+
     def run_backward(self, ws, grad_ys, y0, params, stream=None):
         """dL/dy0 and dL/dparams from the tape the forward left in `ws`."""
         dev = self.device
@@ -308,6 +337,63 @@ class Lowered:
         return grad_y0, grad_params[:n_params], res, stats
 
 
+class DenseInterpolation:
+    """Batched diffrax.DenseInterpolation (diffrax/_global_interpolation.py:315-393)
+    over a dense solve: ``ts`` [B, max_steps + 1] step times in the loop's
+    direction-flipped time (+inf where unused), ``ts_size`` [B] entries used,
+    ``infos`` [B, max_steps, (2 + stages) dim] per-step (y0, y1, k_0..k_{s-1}),
+    ``direction`` [B].  Evaluation runs on the GPU (gbdx_dense_evaluate)."""
+
+    def __init__(self, low: "Lowered", ts, infos, ts_size):
+        self._low = low
+        self.ts, self.infos, self.ts_size = ts, infos, ts_size
+        self.direction = torch.where(low.t0 < low.t1, 1, -1).to(torch.int32)
+        self.t0_if_trivial = low.t0 * self.direction
+        self.y0_if_trivial = low.y0
+
+    def _query(self, t):
+        low = self._low
+        q = torch.as_tensor(t, dtype=torch.float64).to(low.device)
+        if q.dim() == 0:
+            return q.reshape(1).contiguous(), 1, 0, True
+        if q.dim() == 1:
+            return q.contiguous(), int(q.numel()), 0, False
+        if q.dim() == 2 and q.shape[0] == low.B:
+            return q.contiguous(), int(q.shape[1]), int(q.shape[1]), False
+        raise ValueError("query times must be a scalar, [Q] or [batch, Q]")
+
+    def _run(self, t, left, order):
+        low = self._low
+        q, Q, qstride, scalar = self._query(t)
+        out = torch.empty((low.B, Q, low.dim), dtype=low.dtype, device=low.device)
+        stream = torch.cuda.current_stream(low.device).cuda_stream
+        rc = low.problem.lib.gbdx_dense_evaluate(
+            low.problem.handle, low.B, low.t0.data_ptr(), low.t1.data_ptr(), low.tstride,
+            low.y0.data_ptr(), self.ts.data_ptr(), self.infos.data_ptr(),
+            self.ts_size.data_ptr(), Q, q.data_ptr(), qstride, int(bool(left)), order,
+            out.data_ptr(), stream)
+        _lib.check(rc, "gbdx_dense_evaluate")
+        return out[:, 0] if scalar else out
+
+    def evaluate(self, t0, t1=None, left: bool = True):
+        if t1 is not None:
+            return self.evaluate(t1, left=left) - self.evaluate(t0, left=left)
+        return self._run(t0, left, 0)
+
+    def derivative(self, t, left: bool = True):
+        return self._run(t, left, 1)
+
+    @property
+    def t0(self):
+        first = torch.where(self.ts_size == 1, self.t0_if_trivial, self.ts[:, 0])
+        return first * self.direction
+
+    @property
+    def t1(self):
+        last = self.ts.gather(1, (self.ts_size.long() - 1).clamp(min=0)[:, None])[:, 0]
+        return torch.where(self.ts_size == 1, self.t0_if_trivial, last) * self.direction
+
+
 def _raise_on_failure(result: torch.Tensor):
     if _capturing():
         return
@@ -345,14 +431,23 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     low = Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
                   adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule,
                   want_grad=want_grad)
-    if want_grad:
+    interp = None
+    if saveat.dense or saveat.steps:
+        if want_grad:
+            raise NotImplementedError("gradients through SaveAt(steps=...) or "
+                                      "SaveAt(dense=True) are not supported")
+    if saveat.dense:
+        ys, ts_out, res, stats, interp = low.run_forward_dense()
+    elif want_grad:
         ys, ts_out, res, stats = solve_with_grad(low, y0, args)
     else:
         ys, ts_out, res, stats = low.run_forward()
+    if low.n_save == 0:  # SaveAt(dense=True) alone saves no ys (_integrate.py:1527-1539)
+        ys = ts_out = None
     sol = Solution(t0=t0, t1=t1, ts=ts_out, ys=ys,
                    stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],
                               num_rejected_steps=stats[:, 2], max_steps=max_steps),
-                   result=res)
+                   result=res, interpolation=interp)
     # the lowered solve; after a backward pass under BacksolveAdjoint it holds
     # the backward's RESULTS codes and step counts (bwd_result, bwd_stats)
     sol.lowered = low

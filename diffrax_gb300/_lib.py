@@ -32,13 +32,13 @@ class ProblemDesc(_c.Structure):
         ("norm", i32), ("schedule", i32),
         ("dtype", i32), ("kernel", i32), ("adjoint", i32), ("checkpoints", i32),
         ("block_threads", i32), ("ctas_per_sm", i32), ("mlp_precision", i32),
-        ("pad1", i32),
+        ("save_steps", i32), ("save_dense", i32), ("pad2", i32),
     ]
 
 
-# The leading block shared with the oracle descriptor (the oracle ignores the
-# schedule slot).
-ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:29]
+# The fields the oracle descriptor shares: the leading block (up to the
+# backsolve norm) and the SaveAt(steps/dense) selectors.
+ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:29] + ["save_steps", "save_dense"]
 
 _lock = threading.Lock()
 _LIB = None
@@ -69,6 +69,12 @@ def load():
         lib.gbdx_solve_fwd.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, i64, vp, vp, vp,
                                        vp, vp, vp, vp, _c.c_size_t, vp]
         lib.gbdx_solve_fwd.restype = i32
+        lib.gbdx_solve_fwd_dense.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, i64, vp, vp,
+                                             vp, vp, vp, vp, vp, vp, vp, vp, _c.c_size_t, vp]
+        lib.gbdx_solve_fwd_dense.restype = i32
+        lib.gbdx_dense_evaluate.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, vp, i64, vp, i64,
+                                            i32, i32, vp, vp]
+        lib.gbdx_dense_evaluate.restype = i32
         lib.gbdx_solve_bwd.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, i64, vp, vp, vp, vp,
                                        vp, vp, _c.c_size_t, vp]
         lib.gbdx_solve_bwd.restype = i32

@@ -202,8 +202,14 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   if (d.dim < 1) return fail(GBDX_ERR_INVALID, "state dimension must be positive");
   if (d.max_steps < 1) return fail(GBDX_ERR_INVALID, "max_steps must be a positive integer");
   if (d.n_ts < 0) return fail(GBDX_ERR_INVALID, "negative number of SaveAt(ts=...) points");
-  const int n_save = (d.save_t0 ? 1 : 0) + d.n_ts + (d.save_t1 ? 1 : 0);
-  if (n_save < 1) return fail(GBDX_ERR_INVALID, "SaveAt must save at least one point");
+  if (d.save_steps < 0) return fail(GBDX_ERR_INVALID, "SaveAt(steps=n) needs n >= 0");
+  // Output length (_integrate.py:1273-1293): SaveAt(steps=n) reserves
+  // max_steps // n slots, and the t1 slot only when n does not divide max_steps.
+  int n_save = (d.save_t0 ? 1 : 0) + d.n_ts;
+  if (d.save_steps > 0) n_save += d.max_steps / d.save_steps;
+  if (d.save_t1 && (d.save_steps == 0 || d.max_steps % d.save_steps != 0)) n_save += 1;
+  if (n_save < 1 && !d.save_dense)
+    return fail(GBDX_ERR_INVALID, "Empty saveat -- nothing will be saved.");
   const bool sde = d.diffusion != GBDX_DIFF_NONE;
   // pid.py:437-447: adaptive stepping needs an error estimate.
   if (d.controller == GBDX_PID && d.solver == GBDX_EULER)
@@ -235,10 +241,21 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   p->bs = gbdx::BsEntry{nullptr, nullptr, 0, 0, 0, 0};
   p->mlp = false;
   p->rows_per_cta = 1;
+  const bool xo = d.save_steps > 0 || d.save_dense;
+  if (xo && (d.field == GBDX_MLP || sde || d.adjoint != GBDX_ADJ_NONE)) {
+    delete p;
+    return fail(GBDX_ERR_UNSUPPORTED,
+                "SaveAt(steps=...) and SaveAt(dense=True) are available for forward solves "
+                "of the analytic ODE fields");
+  }
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
                d.field == GBDX_ORNSTEIN_UHLENBECK)) {
-    p->ode = d.dtype == GBDX_F32 ? gbdx::find_ode_entry_f32(d.solver, d.field, d.dim)
-                                 : gbdx::find_ode_entry_f64(d.solver, d.field, d.dim);
+    if (xo)
+      p->ode = d.dtype == GBDX_F32 ? gbdx::find_ode_entry_f32_xo(d.solver, d.field, d.dim)
+                                   : gbdx::find_ode_entry_f64_xo(d.solver, d.field, d.dim);
+    else
+      p->ode = d.dtype == GBDX_F32 ? gbdx::find_ode_entry_f32(d.solver, d.field, d.dim)
+                                   : gbdx::find_ode_entry_f64(d.solver, d.field, d.dim);
     if (!p->ode.launch) {
       delete p;
       return fail(GBDX_ERR_UNSUPPORTED, "no kernel for field %d with state dimension %d",
@@ -481,17 +498,19 @@ static int start_queue(const gbdx_problem *problem, gbdx::SolveParams &P, void *
   return GBDX_OK;
 }
 
-int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
-                   const double *t1, const double *dt0, int64_t time_stride,
-                   const void *y0, const void *args, int64_t args_stride,
-                   const void *params, const double *save_ts, void *ys_out,
-                   double *ts_out, int32_t *result_out, int32_t *stats_out,
-                   void *workspace, size_t workspace_bytes, void *stream) {
-  if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
+}  // extern "C"
+
+// The forward solve behind gbdx_solve_fwd and gbdx_solve_fwd_dense.
+static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
+                     const double *t1, const double *dt0, int64_t time_stride, const void *y0,
+                     const void *args, int64_t args_stride, const void *params,
+                     const double *save_ts, void *ys_out, double *ts_out, int32_t *result_out,
+                     int32_t *stats_out, double *dense_ts, void *dense_info, int32_t *dense_n,
+                     void *workspace, size_t workspace_bytes, void *stream) {
   const gbdx_problem_desc &d = problem->d;
   if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
   if (batch == 0) return GBDX_OK;
-  if (!ys_out || !ts_out || !result_out || !stats_out)
+  if ((problem->n_save > 0 && (!ys_out || !ts_out)) || !result_out || !stats_out)
     return fail(GBDX_ERR_INVALID, "null output pointer");
   gbdx::SolveParams P;
   WsLayout L;
@@ -502,7 +521,24 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   P.ts_out = ts_out;
   P.result_out = result_out;
   P.stats_out = stats_out;
+  P.save_steps = d.save_steps;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (d.save_dense) {
+    // The reference's dense buffers start full of +inf (_integrate.py:1315-1323);
+    // the solve overwrites the recorded steps.
+    const int stages = d.solver == GBDX_EULER ? 1 : d.solver == GBDX_HEUN ? 2 : 7;
+    const int64_t rec = int64_t(2 + stages) * d.dim;
+    cudaError_t e = gbdx::launch_fill_inf_f64(dense_ts, batch * (int64_t(d.max_steps) + 1), s);
+    if (e == cudaSuccess) {
+      const int64_t n = batch * int64_t(d.max_steps) * rec;
+      e = d.dtype == GBDX_F32 ? gbdx::launch_fill_inf_f32(static_cast<float *>(dense_info), n, s)
+                              : gbdx::launch_fill_inf_f64(static_cast<double *>(dense_info), n, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "dense buffer fill");
+    P.dense_ts = dense_ts;
+    P.dense_info = dense_info;
+    P.dense_n = dense_n;
+  }
 
   gbdx::LaunchCfg cfg;
   cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;
@@ -539,6 +575,82 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   }
   cudaError_t e = problem->ode.launch(P, cfg, s);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return GBDX_OK;
+}
+
+extern "C" {
+
+int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
+                   const double *t1, const double *dt0, int64_t time_stride,
+                   const void *y0, const void *args, int64_t args_stride,
+                   const void *params, const double *save_ts, void *ys_out,
+                   double *ts_out, int32_t *result_out, int32_t *stats_out,
+                   void *workspace, size_t workspace_bytes, void *stream) {
+  if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
+  if (problem->d.save_dense)
+    return fail(GBDX_ERR_INVALID,
+                "the problem saves the dense output: solve it with gbdx_solve_fwd_dense");
+  return solve_fwd(problem, batch, t0, t1, dt0, time_stride, y0, args, args_stride, params,
+                   save_ts, ys_out, ts_out, result_out, stats_out, nullptr, nullptr, nullptr,
+                   workspace, workspace_bytes, stream);
+}
+
+int gbdx_solve_fwd_dense(const gbdx_problem *problem, int64_t batch, const double *t0,
+                         const double *t1, const double *dt0, int64_t time_stride,
+                         const void *y0, const void *args, int64_t args_stride,
+                         const void *params, const double *save_ts, void *ys_out,
+                         double *ts_out, int32_t *result_out, int32_t *stats_out,
+                         double *dense_ts, void *dense_info, int32_t *dense_n,
+                         void *workspace, size_t workspace_bytes, void *stream) {
+  if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
+  if (!problem->d.save_dense)
+    return fail(GBDX_ERR_INVALID, "the problem was not created with SaveAt(dense=True)");
+  if (batch > 0 && (!dense_ts || !dense_info || !dense_n))
+    return fail(GBDX_ERR_INVALID, "null dense output pointer");
+  return solve_fwd(problem, batch, t0, t1, dt0, time_stride, y0, args, args_stride, params,
+                   save_ts, ys_out, ts_out, result_out, stats_out, dense_ts, dense_info,
+                   dense_n, workspace, workspace_bytes, stream);
+}
+
+int gbdx_dense_evaluate(const gbdx_problem *problem, int64_t batch, const double *t0,
+                        const double *t1, int64_t time_stride, const void *y0,
+                        const double *dense_ts, const void *dense_info,
+                        const int32_t *dense_n, int64_t Q, const double *query,
+                        int64_t query_stride, int left, int order, void *out, void *stream) {
+  if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
+  const gbdx_problem_desc &d = problem->d;
+  if (!d.save_dense)
+    return fail(GBDX_ERR_INVALID, "the problem was not created with SaveAt(dense=True)");
+  if (batch < 0 || Q < 0) return fail(GBDX_ERR_INVALID, "negative batch or query count");
+  if (time_stride != 0 && time_stride != 1)
+    return fail(GBDX_ERR_INVALID, "time_stride must be 0 or 1");
+  if (query_stride != 0 && query_stride != Q)
+    return fail(GBDX_ERR_INVALID, "query_stride must be 0 (shared) or Q (per trajectory)");
+  if (order != 0 && order != 1)
+    return fail(GBDX_ERR_INVALID, "order must be 0 (evaluate) or 1 (derivative)");
+  if (batch == 0 || Q == 0) return GBDX_OK;
+  if (!t0 || !t1 || !y0 || !dense_ts || !dense_info || !dense_n || !query || !out)
+    return fail(GBDX_ERR_INVALID, "null pointer argument");
+  gbdx::DenseEvalArgs A;
+  A.batch = batch;
+  A.Q = Q;
+  A.q_stride = query_stride;
+  A.time_stride = time_stride;
+  A.dim = d.dim;
+  A.max_steps = d.max_steps;
+  A.left = left ? 1 : 0;
+  A.order = order;
+  A.t0 = t0;
+  A.t1 = t1;
+  A.query = query;
+  A.dense_ts = dense_ts;
+  A.y0 = y0;
+  A.dense_info = dense_info;
+  A.dense_n = dense_n;
+  A.out = out;
+  cudaError_t e = gbdx::launch_dense_evaluate(d.solver, d.dtype, A,
+                                              reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "dense evaluation launch");
   return GBDX_OK;
 }
 

@@ -313,6 +313,11 @@ struct SolveParams {
   int32_t *tape_n;            // [batch] accepted steps
   int32_t *tape_stride;       // [batch] accepted steps between checkpoints
   int checkpoints;
+  // SaveAt(steps=n) and SaveAt(dense=True) (the extended-output kernels)
+  int save_steps;             // n > 0: save (tnext, y1) of every n-th accepted step
+  double *dense_ts;           // [batch, max_steps + 1] step times (direction-flipped)
+  void *dense_info;           // [batch, max_steps, (2 + stages) dim]: y0, y1, k_j
+  int32_t *dense_n;           // [batch] accepted steps + 1
 };
 
 // BacksolveAdjoint backward arguments.

@@ -25,6 +25,22 @@ struct OdeEntry {
 
 OdeEntry find_ode_entry_f32(int solver, int field, int dim);
 OdeEntry find_ode_entry_f64(int solver, int field, int dim);
+// The same kernels with SaveAt(steps=n) / SaveAt(dense=True) outputs.
+OdeEntry find_ode_entry_f32_xo(int solver, int field, int dim);
+OdeEntry find_ode_entry_f64_xo(int solver, int field, int dim);
+// Fill n doubles (or floats) with +inf on stream s.
+cudaError_t launch_fill_inf_f64(double *p, int64_t n, cudaStream_t s);
+cudaError_t launch_fill_inf_f32(float *p, int64_t n, cudaStream_t s);
+// DenseInterpolation.evaluate / .derivative over a dense solve's outputs.
+struct DenseEvalArgs {
+  int64_t batch, Q, q_stride, time_stride;
+  int dim, max_steps, left, order;
+  const double *t0, *t1, *query, *dense_ts;
+  const void *y0, *dense_info;
+  const int32_t *dense_n;
+  void *out;
+};
+cudaError_t launch_dense_evaluate(int solver, int dtype, const DenseEvalArgs &A, cudaStream_t s);
 using BwdLaunchFn = cudaError_t (*)(const SolveParams &, const BwdParams &, int grid,
                                     cudaStream_t);
 using BwdOccFn = cudaError_t (*)(int *ctas_per_sm);

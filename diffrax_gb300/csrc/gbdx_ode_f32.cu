@@ -3,6 +3,6 @@
 
 namespace gbdx {
 OdeEntry find_ode_entry_f32(int solver, int field, int dim) {
-  return find_ode_entry_t<float>(solver, field, dim);
+  return find_ode_entry_t<float, false>(solver, field, dim);
 }
 }  // namespace gbdx

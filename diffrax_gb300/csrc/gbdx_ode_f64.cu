@@ -3,6 +3,6 @@
 
 namespace gbdx {
 OdeEntry find_ode_entry_f64(int solver, int field, int dim) {
-  return find_ode_entry_t<double>(solver, field, dim);
+  return find_ode_entry_t<double, false>(solver, field, dim);
 }
 }  // namespace gbdx

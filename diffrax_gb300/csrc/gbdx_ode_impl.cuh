@@ -8,28 +8,29 @@
 
 namespace gbdx {
 
-template <int SOLVER, class FIELD, class T>
+// XO selects the extended-output kernels (SaveAt(steps=n), SaveAt(dense=True)).
+template <int SOLVER, class FIELD, class T, bool XO>
 cudaError_t launch_ode(const SolveParams &P, const LaunchCfg &cfg, cudaStream_t s) {
   if (P.batch <= 0) return cudaSuccess;
   if (cfg.kernel == GBDX_KERNEL_PLAIN) {
     const int64_t blocks = (P.batch + 127) / 128;
-    plain_kernel<SOLVER, FIELD, T><<<(unsigned)blocks, 128, 0, s>>>(P);
+    plain_kernel<SOLVER, FIELD, T, XO><<<(unsigned)blocks, 128, 0, s>>>(P);
   } else {
-    fused_kernel<SOLVER, FIELD, T><<<cfg.grid, cfg.block, 0, s>>>(P);
+    fused_kernel<SOLVER, FIELD, T, XO><<<cfg.grid, cfg.block, 0, s>>>(P);
   }
   return cudaGetLastError();
 }
 
-template <int SOLVER, class FIELD, class T>
+template <int SOLVER, class FIELD, class T, bool XO>
 cudaError_t occupancy_ode(int block, int *ctas_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      ctas_per_sm, fused_kernel<SOLVER, FIELD, T>, block, 0);
+      ctas_per_sm, fused_kernel<SOLVER, FIELD, T, XO>, block, 0);
 }
 
-template <class T>
+template <class T, bool XO>
 OdeEntry find_ode_entry_t(int solver, int field, int dim) {
 #define GBDX_ENTRY(S, F) \
-  OdeEntry { &launch_ode<S, F, T>, &occupancy_ode<S, F, T> }
+  OdeEntry { &launch_ode<S, F, T, XO>, &occupancy_ode<S, F, T, XO> }
 #define GBDX_SOLVERS(F)                                        \
   switch (solver) {                                            \
     case GBDX_EULER: return GBDX_ENTRY(GBDX_EULER, F);         \

@@ -52,8 +52,10 @@ __device__ __forceinline__ T tsit5_w(int j, T t) {
 // hardware conversion (shortest latency; the fused kernel, whose time is set
 // by the step latency of its longest trajectories) or the integer-pipe one
 // (no FP64-pipe issue; the plain kernel, which keeps every trajectory
-// resident and is bound by FP64 issue).  Both give the same value.
-template <int SOLVER, class FIELD, class T, bool LAT = false>
+// resident and is bound by FP64 issue).  Both give the same value.  XO
+// (extended outputs) adds SaveAt(steps=n) and SaveAt(dense=True)
+// (_integrate.py:492-540); the kernels without them keep the shorter step.
+template <int SOLVER, class FIELD, class T, bool LAT = false, bool XO = false>
 struct Traj {
   using TB = Tab<SOLVER>;
   static constexpr int D = FIELD::D;
@@ -79,6 +81,7 @@ struct Traj {
   int sc, nc;  // ConstantStepSize state (constant.py:41-57)
   double t0s, t1s;
   int first, dir, save_index, ts_index, nsteps, nacc, nrej, result;
+  int sdown;  // XO: accepted steps left until the next SaveAt(steps=n) save
   int64_t idx;
   T wb[FIELD::SDE ? D : 1];  // SDE: W(tprev) of every component (FP32 fields only)
 
@@ -158,6 +161,12 @@ struct Traj {
       for (int n = 0; n < D; n++) o[n] = y[n];
       P.ts_out[idx * P.n_save] = a * dir;
       save_index = 1;
+    }
+    if constexpr (XO) {
+      sdown = P.save_steps;
+      // dense_ts[0] = t0 in the loop's time (_integrate.py:1315-1323); the
+      // rest of the buffers was filled with +inf before the launch.
+      if (P.dense_ts) P.dense_ts[i * (P.max_steps + 1)] = a;
     }
   }
 
@@ -386,6 +395,34 @@ struct Traj {
         ts_index++;
         save_index++;
       }
+      if constexpr (XO) {
+        // SaveAt(steps=n): (tnext, y1) of every n-th accepted step, after the
+        // step's ts saves (_integrate.py:492-527).
+        if (P.save_steps > 0 && --sdown == 0) {
+          sdown = P.save_steps;
+          T *o = ys_row(P, save_index);
+#pragma unroll
+          for (int n = 0; n < D; n++) o[n] = y1[n];
+          P.ts_out[idx * P.n_save + save_index] = dir > 0 ? tnext : -tnext;
+          save_index++;
+        }
+        // SaveAt(dense=True): the step's end time and (y0, y1, k_0..k_{S-1})
+        // (_integrate.py:529-540).
+        if (P.dense_ts) {
+          P.dense_ts[idx * (P.max_steps + 1) + nacc + 1] = tnext;
+          T *r = reinterpret_cast<T *>(P.dense_info) +
+                 (idx * P.max_steps + nacc) * int64_t((2 + S) * D);
+#pragma unroll
+          for (int n = 0; n < D; n++) {
+            r[n] = y[n];
+            r[D + n] = y1[n];
+          }
+#pragma unroll
+          for (int j = 0; j < S; j++)
+#pragma unroll
+            for (int n = 0; n < D; n++) r[(2 + j) * D + n] = k[j][n];
+        }
+      }
 #pragma unroll
       for (int n = 0; n < D; n++) y[n] = y1[n];
       if constexpr (FIELD::TAPE) {
@@ -456,7 +493,12 @@ struct Traj {
         save_index++;
       }
     }
-    if (P.save_t1) {
+    // The t1 value is already saved when SaveAt(steps=n) saved the last step:
+    // always for n = 1, for n > 1 when n divides the accepted steps
+    // (_integrate.py:847-877).
+    bool t1_via_steps = false;
+    if constexpr (XO) t1_via_steps = P.save_steps > 0 && sdown == P.save_steps;
+    if (P.save_t1 && !t1_via_steps) {
       T *o = ys_row(P, save_index);
 #pragma unroll
       for (int n = 0; n < D; n++) o[n] = y[n];
@@ -467,7 +509,10 @@ struct Traj {
       T *o = ys_row(P, m);
 #pragma unroll
       for (int n = 0; n < D; n++) o[n] = T(INFINITY);
-      P.ts_out[idx * P.n_save + m] = INFINITY;
+      P.ts_out[idx * P.n_save + m] = dir > 0 ? INFINITY : -INFINITY;  // direction * inf
+    }
+    if constexpr (XO) {
+      if (P.dense_n) P.dense_n[idx] = nacc + 1;
     }
     int r = result;
     if (r == GBDX_SUCCESSFUL && tprev < t1) r = GBDX_MAX_STEPS_REACHED;  // :883
@@ -487,11 +532,11 @@ struct Traj {
 // ---------------------------------------------------------------------------
 // K0: the plain form -- one trajectory per thread, one launch, no refill.
 // ---------------------------------------------------------------------------
-template <int SOLVER, class FIELD, class T>
+template <int SOLVER, class FIELD, class T, bool XO = false>
 __global__ void __launch_bounds__(128) plain_kernel(SolveParams P) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= P.batch) return;
-  Traj<SOLVER, FIELD, T> tr;
+  Traj<SOLVER, FIELD, T, false, XO> tr;
   tr.init(P, i);
   while (tr.running(P)) tr.step(P);
   tr.finish(P);
@@ -503,9 +548,9 @@ __global__ void __launch_bounds__(128) plain_kernel(SolveParams P) {
 // from a device counter (one warp-aggregated atomicAdd per refill), so warps
 // never idle on the longest lane of a fixed group.
 // ---------------------------------------------------------------------------
-template <int SOLVER, class FIELD, class T>
+template <int SOLVER, class FIELD, class T, bool XO = false>
 __global__ void __launch_bounds__(256) fused_kernel(SolveParams P) {
-  Traj<SOLVER, FIELD, T, true> tr;
+  Traj<SOLVER, FIELD, T, true, XO> tr;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   bool active = false;

@@ -16,6 +16,11 @@
  *   gbdx_solve_fwd        <- jax.vmap(diffeqsolve) forward:
  *                            AbstractAdjoint.loop (diffrax/_adjoint.py:121-143)
  *                            driving loop() (diffrax/_integrate.py:302-885)
+ *   gbdx_solve_fwd_dense  <- the same with SaveAt(dense=True): the dense_ts /
+ *                            dense_infos buffers of loop()
+ *                            (diffrax/_integrate.py:529-540, 1315-1323)
+ *   gbdx_dense_evaluate   <- DenseInterpolation.evaluate / .derivative
+ *                            (diffrax/_global_interpolation.py:315-393)
  *   gbdx_solve_bwd        <- the VJP of that solve under
  *                            RecursiveCheckpointAdjoint (diffrax/_adjoint.py:179-312)
  *   gbdx_backsolve_bwd    <- BacksolveAdjoint's backward pass
@@ -103,7 +108,10 @@ typedef struct gbdx_problem_desc {
   int32_t block_threads; /* 0 = autotuned */
   int32_t ctas_per_sm;   /* 0 = autotuned */
   int32_t mlp_precision; /* gbdx_mlp_precision of the MLP field's products */
-  int32_t pad1;
+  int32_t save_steps;    /* SaveAt(steps=n): save every n-th accepted step; 0 = off */
+  int32_t save_dense;    /* SaveAt(dense=True): record the dense output (solve with
+                            gbdx_solve_fwd_dense) */
+  int32_t pad2;
 } gbdx_problem_desc;
 
 typedef struct gbdx_problem gbdx_problem;
@@ -114,7 +122,9 @@ typedef struct gbdx_problem gbdx_problem;
 int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out);
 int gbdx_problem_destroy(gbdx_problem *problem);
 
-/* Number of saved points per trajectory: save_t0 + n_ts + save_t1. */
+/* Number of saved points per trajectory (diffrax/_integrate.py:1273-1293):
+ * save_t0 + n_ts + max_steps / save_steps (when save_steps > 0) + save_t1
+ * (unless save_steps divides max_steps, when the t1 value is a step save). */
 int gbdx_num_saves(const gbdx_problem *problem);
 
 /* Device workspace (bytes) a forward solve over `batch` trajectories needs. */
@@ -190,6 +200,48 @@ int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double 
                        const void *params, void *grad_y0, void *grad_params,
                        int32_t *result_out, int32_t *stats_out, void *workspace,
                        size_t workspace_bytes, void *stream);
+
+/*
+ * Forward solve with SaveAt(dense=True) (the problem's save_dense set): the
+ * arguments of gbdx_solve_fwd plus the dense output of every trajectory, as the
+ * reference's loop records it (diffrax/_integrate.py:529-540, 1315-1323):
+ *   dense_ts   : device f64 [batch, max_steps + 1]: t0 then the end time of every
+ *                accepted step, in the direction-flipped time of the loop
+ *                (time runs forward; t * sign(t1 - t0)); +inf where unused.
+ *   dense_info : device [batch, max_steps, (2 + stages) * dim] in desc.dtype: per
+ *                accepted step (y0, y1, k_0 .. k_{stages-1}), each dim long, with
+ *                k_j the stage increments f_j * control; +inf where unused.
+ *                stages = 1 Euler, 2 Heun, 7 Dopri5 and Tsit5.
+ *   dense_n    : device int32 [batch]: accepted steps + 1 (entries of dense_ts).
+ * With n_saves = 0 (SaveAt(dense=True) alone) ys_out and ts_out may be NULL.
+ * Analytic fields only.
+ */
+int gbdx_solve_fwd_dense(const gbdx_problem *problem, int64_t batch, const double *t0,
+                         const double *t1, const double *dt0, int64_t time_stride,
+                         const void *y0, const void *args, int64_t args_stride,
+                         const void *params, const double *save_ts, void *ys_out,
+                         double *ts_out, int32_t *result_out, int32_t *stats_out,
+                         double *dense_ts, void *dense_info, int32_t *dense_n,
+                         void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * DenseInterpolation.evaluate (order 0) and .derivative (order 1) of a dense
+ * solve (diffrax/_global_interpolation.py:315-393 with the solver's local
+ * interpolant, diffrax/_solver/tsit5.py:103-156,
+ * diffrax/_local_interpolation.py:29-139): out[b, q] = y_b(t) or dy_b/dt at
+ * t = query[b * query_stride + q] in the caller's time (query_stride 0: one
+ * set of Q times shared by the batch; Q: Q times per trajectory).
+ *   t0, t1, time_stride : the solve's (only the direction sign(t1 - t0) is read).
+ *   y0                  : device [batch, dim], the solve's initial state.
+ *   dense_ts, dense_info, dense_n : gbdx_solve_fwd_dense's outputs.
+ *   left    : which side's step a query on a step boundary takes (1 = left).
+ *   out     : device [batch, Q, dim] in desc.dtype; NaN outside [t0, t1].
+ */
+int gbdx_dense_evaluate(const gbdx_problem *problem, int64_t batch, const double *t0,
+                        const double *t1, int64_t time_stride, const void *y0,
+                        const double *dense_ts, const void *dense_info,
+                        const int32_t *dense_n, int64_t Q, const double *query,
+                        int64_t query_stride, int left, int order, void *out, void *stream);
 
 /*
  * Forward solve for callers that cannot allocate device memory.  It has no

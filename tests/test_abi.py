@@ -55,7 +55,8 @@ def test_problem_create_and_queries():
     (dict(solver=0), "error estimates"),          # adaptive Euler (pid.py:437-447)
     (dict(solver=9), "unknown solver"),
     (dict(max_steps=0), "max_steps"),
-    (dict(save_t1=0), "at least one"),
+    (dict(save_t1=0), "Empty saveat"),
+    (dict(save_steps=-1), "steps"),
     (dict(dtype=7), "dtype"),
 ])
 def test_problem_validation(bad, msg):
@@ -99,7 +100,7 @@ def test_saveat_validation():
     with pytest.raises(ValueError):
         dfx.SaveAt()
     with pytest.raises(NotImplementedError):
-        dfx.SaveAt(dense=True)
+        dfx.SaveAt(t1=True, solver_state=True)
 
 
 def test_backsolve_kwargs_validation():
@@ -139,3 +140,47 @@ def test_no_cpu_fallback():
         dfx.diffeqsolve(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(), 0.0, 1.0, None,
                         torch.zeros(4, 2), torch.ones(1),
                         stepsize_controller=dfx.PIDController(rtol=1e-6, atol=1e-9))
+
+
+@pytest.mark.parametrize("steps, t0, t1, n_ts, max_steps", [
+    (1, 0, 1, 0, 4096), (2, 0, 1, 0, 4096), (3, 1, 1, 5, 4096), (3, 0, 0, 0, 10),
+    (7, 1, 1, 0, 10), (0, 1, 1, 3, 100)])
+def test_saveat_steps_output_length(steps, t0, t1, n_ts, max_steps):
+    # _integrate.py:1273-1293, as the oracle restates it
+    import oracle as O
+    f = _fields(save_steps=steps, save_t0=t0, save_t1=t1, n_ts=n_ts, max_steps=max_steps)
+    assert _lib.Problem(f).n_save == O.n_saves(O.make_desc(**dfx.oracle_fields(f)))
+
+
+def test_saveat_steps_dense_scope():
+    # forward solves of the analytic fields only; a dense problem is solved by
+    # gbdx_solve_fwd_dense and evaluated by gbdx_dense_evaluate (no kernel
+    # runs: the calls fail validation first)
+    with pytest.raises(_lib.GbdxError, match="analytic"):
+        _lib.Problem(_fields(save_steps=1, adjoint=1, checkpoints=8))
+    assert _lib.Problem(_fields(save_dense=1, save_t1=0)).n_save == 0
+    lib = _lib.load()
+    p = _lib.Problem(_fields(save_dense=1))
+    z = [None] * 16
+    assert lib.gbdx_solve_fwd(p.handle, 1, *z[:3], 0, *z[:2], 0, *z[:7], 0, None) == -1
+    assert "gbdx_solve_fwd_dense" in _lib.last_error()
+    q = _lib.Problem(_fields(save_steps=2))
+    assert lib.gbdx_solve_fwd_dense(q.handle, 1, *z[:3], 0, *z[:2], 0, *z[:10], 0, None) == -1
+    assert "dense" in _lib.last_error()
+    assert lib.gbdx_dense_evaluate(p.handle, 1, None, None, 0, None, None, None, None, 3,
+                                   None, 5, 1, 0, None, None) == -1
+    assert "query_stride" in _lib.last_error()
+
+
+def test_saveat_steps_dense_python_surface():
+    with pytest.raises(ValueError, match="Empty saveat"):
+        dfx.SaveAt()
+    assert dfx.SaveAt(steps=True).steps == 1 and dfx.SaveAt(steps=4).steps == 4
+    assert dfx.SaveAt(dense=True).dense
+    f = dfx.lower(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(),
+                  dfx.PIDController(rtol=1e-6, atol=1e-9), dfx.SaveAt(steps=3, dense=True),
+                  dim=2, dtype=torch.float32, max_steps=64, n_ts=0)
+    assert f["save_steps"] == 3 and f["save_dense"] == 1
+    sol = dfx.Solution(t0=0.0, t1=1.0, ts=None, ys=None, stats={}, result=None)
+    with pytest.raises(ValueError, match="dense=True"):
+        sol.evaluate(0.5)
