@@ -11,6 +11,8 @@ import dataclasses
 import enum
 from typing import Any, Optional, Sequence
 
+import numpy as np
+
 # ---------------------------------------------------------------------------
 # Registered vector fields.  A field is a vector_field(t, y, args) that the
 # library knows how to evaluate on the GPU.
@@ -254,6 +256,45 @@ class PIDController(AbstractStepSizeController):
     safety: float = 0.9
     error_order: Optional[float] = None
     norm: Any = rms_norm
+
+
+class ClipStepSizeController(AbstractStepSizeController):
+    """diffrax/_step_size_controller/clip.py:120-427: steps exactly to
+    ``step_ts`` and to just before / just after ``jump_ts`` (where FSAL solvers
+    evaluate the vector field afresh).  Wraps a PIDController;
+    ``store_rejected_steps`` (revisiting rejected steps of SDE solves) is not
+    available."""
+
+    def __init__(self, controller, step_ts=None, jump_ts=None, store_rejected_steps=None):
+        if not isinstance(controller, PIDController):
+            if isinstance(controller, ClipStepSizeController):
+                raise NotImplementedError("nested ClipStepSizeController wrappers are not "
+                                          "supported; pass all step_ts/jump_ts to one")
+            raise ValueError("Can only apply `ClipStepSizeController` to adaptive step size "
+                             f"controllers, but got {controller}.")
+        if store_rejected_steps is not None:
+            if store_rejected_steps <= 0:
+                raise ValueError("`store_rejected_steps must either be `None` or a "
+                                 "non-negative integer.")
+            raise NotImplementedError("store_rejected_steps is not supported")
+        self.controller = controller
+        sort = lambda x: None if x is None else np.sort(  # noqa: E731
+            np.asarray(x, dtype=np.float64).reshape(-1))
+        self.step_ts = sort(step_ts)
+        self.jump_ts = sort(jump_ts)
+        self.store_rejected_steps = None
+
+    @property
+    def rtol(self):
+        return self.controller.rtol
+
+    @property
+    def atol(self):
+        return self.controller.atol
+
+    @property
+    def norm(self):
+        return self.controller.norm
 
 
 # ---------------------------------------------------------------------------

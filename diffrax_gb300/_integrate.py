@@ -15,7 +15,8 @@ import torch
 
 from . import _lib
 from ._core import (
-    RESULT_MESSAGES, RESULTS, AbstractField, BacksolveAdjoint, ConstantStepSize, ControlTerm,
+    RESULT_MESSAGES, RESULTS, AbstractField, BacksolveAdjoint, ClipStepSizeController,
+    ConstantStepSize, ControlTerm,
     Euler, MultiTerm, ODETerm, OrnsteinUhlenbeck, PIDController,
     RecursiveCheckpointAdjoint, SaveAt, Solution, VirtualBrownianTree, adjoint_rms_seminorm,
 )
@@ -66,9 +67,15 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
              error_order=0.0, mlp_depth=0, mlp_widths=(), diffusion=0, vbt_t0=0.0,
              vbt_t1=1.0, vbt_tol=1e-3, seed=0, norm=0, adjoint=0, checkpoints=0,
              schedule=SCHEDULES[schedule], mlp_precision=0,
-             save_steps=int(saveat.steps), save_dense=int(saveat.dense), pad2=0)
+             save_steps=int(saveat.steps), save_dense=int(saveat.dense), n_step_ts=0,
+             n_jump_ts=0, pad3=0)
     if hasattr(drift, "lower_fields"):
         f.update(drift.lower_fields(dim))
+    if isinstance(stepsize_controller, ClipStepSizeController):
+        clip = stepsize_controller
+        f.update(n_step_ts=0 if clip.step_ts is None else int(clip.step_ts.size),
+                 n_jump_ts=0 if clip.jump_ts is None else int(clip.jump_ts.size))
+        stepsize_controller = clip.controller
     if isinstance(stepsize_controller, PIDController):
         c = stepsize_controller
         f.update(controller=1, rtol=float(c.rtol), atol=float(c.atol),
@@ -177,8 +184,16 @@ class Lowered:
         ts = saveat.ts
         if ts is not None:
             ts = torch.as_tensor(ts, dtype=torch.float64).to(dev).reshape(-1).contiguous()
-        self.save_ts = ts
         n_ts = 0 if ts is None else int(ts.numel())
+        # the solve's times: SaveAt ts, then a ClipStepSizeController's sorted
+        # step_ts and jump_ts (include/gbdx.h)
+        clip_parts = []
+        if isinstance(stepsize_controller, ClipStepSizeController):
+            clip_parts = [torch.as_tensor(v, dtype=torch.float64).to(dev)
+                          for v in (stepsize_controller.step_ts, stepsize_controller.jump_ts)
+                          if v is not None]
+        self.save_ts = (torch.cat(([ts] if ts is not None else []) + clip_parts).contiguous()
+                        if clip_parts else ts)
         # The adjoint shapes the problem only when a gradient will be taken:
         # a plain forward solve records no tape.
         self.adjoint = adjoint if want_grad else None

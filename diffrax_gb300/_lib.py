@@ -32,13 +32,15 @@ class ProblemDesc(_c.Structure):
         ("norm", i32), ("schedule", i32),
         ("dtype", i32), ("kernel", i32), ("adjoint", i32), ("checkpoints", i32),
         ("block_threads", i32), ("ctas_per_sm", i32), ("mlp_precision", i32),
-        ("save_steps", i32), ("save_dense", i32), ("pad2", i32),
+        ("save_steps", i32), ("save_dense", i32), ("n_step_ts", i32), ("n_jump_ts", i32),
+        ("pad3", i32),
     ]
 
 
 # The fields the oracle descriptor shares: the leading block (up to the
-# backsolve norm) and the SaveAt(steps/dense) selectors.
-ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:29] + ["save_steps", "save_dense"]
+# backsolve norm), the SaveAt(steps/dense) selectors and the clip counts.
+ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:29] + [
+    "save_steps", "save_dense", "n_step_ts", "n_jump_ts"]
 
 _lock = threading.Lock()
 _LIB = None

@@ -241,12 +241,23 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   p->bs = gbdx::BsEntry{nullptr, nullptr, 0, 0, 0, 0};
   p->mlp = false;
   p->rows_per_cta = 1;
-  const bool xo = d.save_steps > 0 || d.save_dense;
+  if (d.n_step_ts < 0 || d.n_jump_ts < 0) {
+    delete p;
+    return fail(GBDX_ERR_INVALID, "negative number of step_ts or jump_ts");
+  }
+  const bool clip = d.n_step_ts > 0 || d.n_jump_ts > 0;
+  // clip.py:195-199
+  if (clip && d.controller != GBDX_PID) {
+    delete p;
+    return fail(GBDX_ERR_INVALID,
+                "Can only apply `ClipStepSizeController` to adaptive step size controllers.");
+  }
+  const bool xo = d.save_steps > 0 || d.save_dense || clip;
   if (xo && (d.field == GBDX_MLP || sde || d.adjoint != GBDX_ADJ_NONE)) {
     delete p;
     return fail(GBDX_ERR_UNSUPPORTED,
-                "SaveAt(steps=...) and SaveAt(dense=True) are available for forward solves "
-                "of the analytic ODE fields");
+                "SaveAt(steps=...), SaveAt(dense=True) and ClipStepSizeController are "
+                "available for forward solves of the analytic ODE fields");
   }
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
                d.field == GBDX_ORNSTEIN_UHLENBECK)) {
@@ -405,7 +416,8 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
     return fail(GBDX_ERR_INVALID,
                 "Constant step size solvers cannot select step size automatically; please "
                 "pass a value for `dt0`.");
-  if (d.n_ts > 0 && !save_ts) return fail(GBDX_ERR_INVALID, "SaveAt(ts=...) without ts");
+  if (d.n_ts + d.n_step_ts + d.n_jump_ts > 0 && !save_ts)
+    return fail(GBDX_ERR_INVALID, "SaveAt(ts=...) or step_ts/jump_ts without times");
   if (d.n_args > 0 && !args) return fail(GBDX_ERR_INVALID, "field arguments missing");
   if (problem->mlp && !params) return fail(GBDX_ERR_INVALID, "MLP parameters missing");
   const int rc = ws_layout(problem, batch, L);
@@ -425,6 +437,10 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
   P.args_stride = args_stride;
   P.params = params;
   P.save_ts = save_ts;
+  P.n_step_ts = d.n_step_ts;
+  P.n_jump_ts = d.n_jump_ts;
+  P.step_ts = save_ts ? save_ts + d.n_ts : nullptr;
+  P.jump_ts = save_ts ? save_ts + d.n_ts + d.n_step_ts : nullptr;
   P.controller = d.controller;
   P.rtol = d.rtol;
   P.atol = d.atol;

@@ -224,6 +224,13 @@ __device__ __forceinline__ double next_up(double x) {
   return from_order_key(k);
 }
 
+// nextafter(x, -inf) for non-NaN x (+inf gives the largest finite double).
+__device__ __forceinline__ double next_down(double x) {
+  long long k = order_key(x) - 1;
+  if (k == -1) k = -2;  // from +0 the next value down is -denorm_min
+  return from_order_key(k);
+}
+
 // t1 minus 100 ULP (_integrate.py:319-322): 100 applications of
 // nextafter(., -inf), the threshold above which tnext snaps to t1.
 __device__ __forceinline__ double t1_clip_floor(double t1) {
@@ -318,6 +325,10 @@ struct SolveParams {
   double *dense_ts;           // [batch, max_steps + 1] step times (direction-flipped)
   void *dense_info;           // [batch, max_steps, (2 + stages) dim]: y0, y1, k_j
   int32_t *dense_n;           // [batch] accepted steps + 1
+  // ClipStepSizeController(step_ts, jump_ts) around the PID controller (the
+  // extended-output kernels): caller-time times sorted increasing
+  const double *step_ts, *jump_ts;
+  int n_step_ts, n_jump_ts;
 };
 
 // BacksolveAdjoint backward arguments.

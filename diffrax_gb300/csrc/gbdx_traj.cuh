@@ -48,6 +48,23 @@ __device__ __forceinline__ T tsit5_w(int j, T t) {
   }
 }
 
+// ClipStepSizeController (diffrax/_step_size_controller/clip.py) works in the
+// loop's direction-flipped time, where the caller's sorted times become
+// sort(ts * direction) (clip.py:203-213).  clip_get is the i-th of those, +inf
+// past the end (_get_t, clip.py:55-62); clip_find the first index whose time
+// is strictly greater than t, searched from a hint (_find_idx_with_hint,
+// clip.py:102-118).
+__device__ __forceinline__ double clip_get(const double *ts, int n, int i, int dir) {
+  if (i >= n) return INFINITY;
+  return dir > 0 ? __ldg(ts + i) : -__ldg(ts + n - 1 - i);
+}
+__device__ __forceinline__ int clip_find(const double *ts, int n, int dir, double t, int hint) {
+  int i = hint;
+  while (i < n && clip_get(ts, n, i, dir) <= t) i++;
+  while (i > 0 && clip_get(ts, n, i - 1, dir) > t) i--;
+  return i;
+}
+
 // LAT selects the form of the FP32 copy of dt for the FP32-state kernels: the
 // hardware conversion (shortest latency; the fused kernel, whose time is set
 // by the step latency of its longest trajectories) or the integer-pipe one
@@ -82,6 +99,7 @@ struct Traj {
   double t0s, t1s;
   int first, dir, save_index, ts_index, nsteps, nacc, nrej, result;
   int sdown;  // XO: accepted steps left until the next SaveAt(steps=n) save
+  int sidx, jidx;  // XO: ClipStepSizeController step / jump indices (hints)
   int64_t idx;
   T wb[FIELD::SDE ? D : 1];  // SDE: W(tprev) of every component (FP32 fields only)
 
@@ -115,6 +133,7 @@ struct Traj {
       if (P.has_dtmax) h = fmin(h, P.dtmax);
       if (P.has_dtmin) h = fmax(h, P.dtmin);
       tn = a + h;
+      if constexpr (XO) tn = clip_init(P, a, tn);
       h1 = F32 ? T(0) : T(1);
       h2 = h1;
       at_dtmin = 0;
@@ -168,6 +187,55 @@ struct Traj {
       // rest of the buffers was filled with +inf before the launch.
       if (P.dense_ts) P.dense_ts[i * (P.max_steps + 1)] = a;
     }
+  }
+
+  // ClipStepSizeController.init (clip.py:215-276): the first step ends no
+  // later than the first step time after t0, and just before the first jump.
+  __device__ double clip_init(const SolveParams &P, double a, double tn) {
+    sidx = jidx = 0;
+    if (P.n_step_ts > 0) {
+      sidx = clip_find(P.step_ts, P.n_step_ts, dir, a, 0);
+      tn = fmin(tn, clip_get(P.step_ts, P.n_step_ts, sidx, dir));
+    }
+    if (P.n_jump_ts > 0) {
+      jidx = clip_find(P.jump_ts, P.n_jump_ts, dir, a, 0);
+      tn = fmin(tn, next_down(clip_get(P.jump_ts, P.n_jump_ts, jidx, dir)));
+    }
+    return tn;
+  }
+
+  // ClipStepSizeController.adapt_step_size after the PID controller
+  // (clip.py:330-389).  A step that ended at x or just before x, for x a
+  // jump time, restarts past x (_bump_next_t0, clip.py:79-99: the sorted
+  // times equal to nt0 or to nextafter(nt0) sit just below and at the first
+  // index above nt0); the next step ends no later than the next step time and
+  // just before the next jump.  Returns made_jump.
+  __device__ bool clip_adapt(const SolveParams &P, double &nt0, double &nt1) {
+    bool made = false;
+    if (P.n_step_ts > 0) {
+      const int n = P.n_step_ts;
+      const int i = clip_find(P.step_ts, n, dir, nt0, sidx);
+      const double n1 = next_up(nt0);
+      double b0 = nt0;
+      if (i < n && clip_get(P.step_ts, n, i, dir) == n1) b0 = next_up(n1);
+      if (i > 0 && clip_get(P.step_ts, n, i - 1, dir) == nt0) b0 = n1;
+      sidx = clip_find(P.step_ts, n, dir, b0, i);
+      nt1 = fmin(nt1, clip_get(P.step_ts, n, sidx, dir));
+    }
+    if (P.n_jump_ts > 0) {
+      const int n = P.n_jump_ts;
+      const int i = clip_find(P.jump_ts, n, dir, nt0, jidx);
+      const double n1 = next_up(nt0);
+      const bool m1 = i < n && clip_get(P.jump_ts, n, i, dir) == n1;
+      const bool m2 = i > 0 && clip_get(P.jump_ts, n, i - 1, dir) == nt0;
+      if (m1) nt0 = next_up(n1);
+      if (m2) nt0 = n1;
+      made = m1 || m2;
+      nt1 = fmax(next_up(nt0), nt1);  // never an empty interval (clip.py:354-372)
+      jidx = clip_find(P.jump_ts, n, dir, nt0, i);
+      nt1 = fmin(nt1, next_down(clip_get(P.jump_ts, n, jidx, dir)));
+    }
+    return made;
   }
 
   // One loop iteration.
@@ -366,6 +434,13 @@ struct Traj {
       nt1 = tn;
       dt_next = F32 ? tn - nt0 : 0.0;
     }
+    bool made_jump = false;
+    if constexpr (XO) {
+      if (P.controller == GBDX_PID && (P.n_step_ts > 0 || P.n_jump_ts > 0)) {
+        made_jump = clip_adapt(P, nt0, nt1);
+        dt_next = nt1 - nt0;
+      }
+    }
     // Book-keeping (_integrate.py:410-413).  tprev and tnext never exceed t1
     // (tnext starts at min(t0 + dt0, t1) and is clipped), so the minimum with
     // t1 is the identity; FP32 mode skips it and defers the clip to the next
@@ -441,6 +516,12 @@ struct Traj {
 #pragma unroll
         for (int n = 0; n < D; n++) f0[n] = flast[n];
         first = 0;
+      }
+      // after a jump the FSAL solvers evaluate the first stage afresh
+      // (runge_kutta.py:684-700); a rejected step keeps the flag
+      // (_integrate.py:425)
+      if constexpr (XO) {
+        if (made_jump) first = 1;
       }
       nacc++;
     } else {

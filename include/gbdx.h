@@ -111,7 +111,12 @@ typedef struct gbdx_problem_desc {
   int32_t save_steps;    /* SaveAt(steps=n): save every n-th accepted step; 0 = off */
   int32_t save_dense;    /* SaveAt(dense=True): record the dense output (solve with
                             gbdx_solve_fwd_dense) */
-  int32_t pad2;
+  /* ClipStepSizeController(PIDController(...), step_ts, jump_ts)
+   * (diffrax/_step_size_controller/clip.py:120-427; store_rejected_steps is not
+   * available): the numbers of step and jump times, passed after the n_ts
+   * SaveAt times in the solve's save_ts array.  PID controller only. */
+  int32_t n_step_ts, n_jump_ts;
+  int32_t pad3;
 } gbdx_problem_desc;
 
 typedef struct gbdx_problem gbdx_problem;
@@ -139,7 +144,10 @@ size_t gbdx_workspace_size(const gbdx_problem *problem, int64_t batch);
  *                 (args_stride 0) in desc.dtype; NULL when n_args == 0.
  *   params      : device MLP / linear / diffusion parameters in desc.dtype
  *                 (layout in gbdx_param_count); NULL for analytic fields.
- *   save_ts     : device f64 [n_ts], increasing, inside [t0, t1].
+ *   save_ts     : device f64 [n_ts + n_step_ts + n_jump_ts]: the SaveAt(ts)
+ *                 times (monotone in the direction of integration, inside
+ *                 [t0, t1]), then the step_ts and the jump_ts of a
+ *                 ClipStepSizeController, each sorted increasing.
  *   ys_out      : device [batch, n_saves, dim] in desc.dtype (unsaved = +inf).
  *   ts_out      : device f64 [batch, n_saves].
  *   result_out  : device int32 [batch] gbdx_result codes.

@@ -21,7 +21,7 @@ from .build import build_oracle, oracle_lib_path
 
 __all__ = [
     "OracleDesc", "load", "solve", "grad_recursive", "vbt_increments", "normal4",
-    "dense_evaluate", "n_saves", "STAGES",
+    "dense_evaluate", "n_saves", "STAGES", "clip_times", "clip_find", "clip_adapt",
     "EULER", "HEUN", "DOPRI5", "TSIT5", "CONSTANT", "PID",
     "LOTKA_VOLTERRA", "VAN_DER_POL", "ORNSTEIN_UHLENBECK", "MLP", "LINEAR", "CALLBACK",
     "DIFF_NONE", "DIFF_OU", "DIFF_TANH_DIAG", "RESULT_NAMES",
@@ -53,7 +53,8 @@ class OracleDesc(ctypes.Structure):
         ("vbt_t0", ctypes.c_double), ("vbt_t1", ctypes.c_double),
         ("vbt_tol", ctypes.c_double), ("seed", ctypes.c_uint64),
         ("norm", ctypes.c_int32), ("save_steps", ctypes.c_int32),
-        ("save_dense", ctypes.c_int32), ("pad_", ctypes.c_int32),
+        ("save_dense", ctypes.c_int32), ("n_step_ts", ctypes.c_int32),
+        ("n_jump_ts", ctypes.c_int32), ("pad_", ctypes.c_int32),
     ]
 
 
@@ -63,7 +64,8 @@ _DEFAULTS = dict(solver=TSIT5, controller=PID, field=LOTKA_VOLTERRA, dim=2,
                  dtmax=math.nan, force_dtmin=1, error_order=0.0, n_ts=0,
                  save_t0=0, save_t1=1, max_steps=4096, n_args=0, mlp_depth=0,
                  mlp_widths=(), diffusion=DIFF_NONE, vbt_t0=0.0, vbt_t1=1.0,
-                 vbt_tol=1e-3, seed=0, norm=0, save_steps=0, save_dense=0)
+                 vbt_tol=1e-3, seed=0, norm=0, save_steps=0, save_dense=0,
+                 n_step_ts=0, n_jump_ts=0)
 
 STAGES = {EULER: 1, HEUN: 2, DOPRI5: 7, TSIT5: 7}
 
@@ -123,6 +125,12 @@ def load():
     lib.orc_dense_evaluate.argtypes = [ctypes.POINTER(OracleDesc), i64, dp, dp, i64, dp, dp,
                                        dp, ip, i64, dp, i64, ctypes.c_int, ctypes.c_int, dp]
     lib.orc_dense_evaluate.restype = ctypes.c_int
+    lib.orc_clip_find.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+    lib.orc_clip_find.restype = ctypes.c_int
+    lib.orc_clip_adapt.argtypes = [dp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(ctypes.c_double)]
+    lib.orc_clip_adapt.restype = ctypes.c_int
     lib.orc_grad_recursive.argtypes = [ctypes.POINTER(OracleDesc), i64, dp, dp, dp, i64,
                                        dp, dp, i64, dp, i64, dp, dp, dp, dp, ip, ip, dp,
                                        dp, dp, ctypes.c_int]
@@ -188,11 +196,25 @@ def _prep(desc, B, t0, t1, dt0, y0, args, params, ts):
     return t0, t1, dt0, time_stride, y0, args_arr, args_stride, params.reshape(-1), ts
 
 
+def clip_times(desc: OracleDesc, ts=None, step_ts=None, jump_ts=None):
+    """The solve's times array: SaveAt ts, then ClipStepSizeController step_ts
+    and jump_ts (each sorted increasing), with the descriptor's counts set."""
+    parts = [np.zeros(0) if ts is None else np.asarray(ts, np.float64).reshape(-1)]
+    for name, v in (("n_step_ts", step_ts), ("n_jump_ts", jump_ts)):
+        v = np.zeros(0) if v is None else np.sort(np.asarray(v, np.float64).reshape(-1))
+        setattr(desc, name, int(v.size))
+        parts.append(v)
+    return np.concatenate(parts)
+
+
 def solve(desc: OracleDesc, t0, t1, dt0, y0, args=None, params=None, ts=None,
-          nthreads: int = 1, callback=None):
+          nthreads: int = 1, callback=None, step_ts=None, jump_ts=None):
     """Run the oracle.  Returns dict(ys [B,n_save,D], ts [B,n_save], result [B],
-    stats [B,3] = (num_steps, num_accepted, num_rejected))."""
+    stats [B,3] = (num_steps, num_accepted, num_rejected)).  step_ts / jump_ts
+    wrap the PID controller in ClipStepSizeController (clip.py)."""
     lib = load()
+    if step_ts is not None or jump_ts is not None:
+        ts = clip_times(desc, ts, step_ts, jump_ts)
     y0 = np.asarray(y0, dtype=np.float64)
     B = y0.shape[0] if y0.ndim == 2 else 1
     t0, t1, dt0, tstride, y0, args_arr, astride, params, ts = _prep(
@@ -233,6 +255,29 @@ def solve(desc: OracleDesc, t0, t1, dt0, y0, args=None, params=None, ts=None,
     if dense:
         out.update(dense_ts=dense["ts"], dense_info=dense["info"], dense_n=dense["n"])
     return out
+
+
+def clip_find(ts, t, hint, direction=1) -> int:
+    """_find_idx_with_hint (clip.py:102-118) in the direction-flipped time."""
+    lib = load()
+    a = _f64(np.sort(np.asarray(ts, np.float64)))
+    return int(lib.orc_clip_find(_dptr(a), int(a.size), int(direction), float(t), int(hint)))
+
+
+def clip_adapt(step_ts, jump_ts, next_t0, next_t1, idx=(0, 0), direction=1):
+    """ClipStepSizeController.adapt_step_size after the inner controller
+    proposed (next_t0, next_t1) (clip.py:330-389).  Returns (next_t0, next_t1,
+    made_jump, (step_index, jump_index))."""
+    lib = load()
+    st = _f64(np.sort(np.asarray([] if step_ts is None else step_ts, np.float64)))
+    jt = _f64(np.sort(np.asarray([] if jump_ts is None else jump_ts, np.float64)))
+    ix = np.asarray(idx, dtype=np.int32).copy()
+    a, b = ctypes.c_double(next_t0), ctypes.c_double(next_t1)
+    mj = lib.orc_clip_adapt(_dptr(st) if st.size else None, int(st.size),
+                            _dptr(jt) if jt.size else None, int(jt.size), int(direction),
+                            ix.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                            ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value, bool(mj), (int(ix[0]), int(ix[1]))
 
 
 def dense_evaluate(desc: OracleDesc, t0, t1, y0, sol, query, left=True, order=0):

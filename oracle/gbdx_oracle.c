@@ -16,6 +16,8 @@
  *                           diffrax/_local_interpolation.py:29-139
  *   PID controller ........ diffrax/_step_size_controller/pid.py:316-567
  *   constant step size .... diffrax/_step_size_controller/constant.py:20-104
+ *   clip controller ....... diffrax/_step_size_controller/clip.py:36-427
+ *                           (step_ts, jump_ts; no store_rejected_steps)
  *   terms ................. diffrax/_term.py:174-226, 271-555, 666-764
  *   virtual Brownian tree . diffrax/_brownian/tree.py:245-354, 366-448,
  *                           607-621, 626-773 (BrownianIncrement branch)
@@ -78,6 +80,10 @@ typedef struct {
   int32_t norm;           /* used by the backsolve adjoint only */
   int32_t save_steps;     /* SaveAt(steps=n): every n-th accepted step; 0 = off */
   int32_t save_dense;     /* SaveAt(dense=True) */
+  /* ClipStepSizeController(step_ts, jump_ts) around the PID controller: the
+   * times follow the n_ts SaveAt times in the solve's `ts` array, each group
+   * sorted increasing in the caller's time */
+  int32_t n_step_ts, n_jump_ts;
   int32_t pad_;
 } orc_desc;
 
@@ -737,6 +743,83 @@ static int constant_adapt(double t1, CtrlState *cs, double *next_t0, double *nex
   return 1;
 }
 
+/* ClipStepSizeController (clip.py).  `ts` holds n times sorted increasing in
+ * the caller's time; the controller works in the loop's direction-flipped
+ * time, where the sorted array is sort(ts * direction) (clip.py:203-213). */
+static double clip_get(const double *ts, int n, int i, int dir) {
+  /* _get_t (clip.py:55-62): ts[i], +inf past the end */
+  if (i >= n) return INFINITY;
+  return dir > 0 ? ts[i] : -ts[n - 1 - i];
+}
+
+/* _find_idx_with_hint (clip.py:102-118): the first index whose time is
+ * strictly greater than t, by a linear search from the hint. */
+static int clip_find(const double *ts, int n, int dir, double t, int hint) {
+  int i = hint;
+  while (i < n && clip_get(ts, n, i, dir) <= t) i++;
+  while (i > 0 && clip_get(ts, n, i - 1, dir) > t) i--;
+  return i;
+}
+
+/* _bump_next_t0 (clip.py:79-99): a step that ended at prevbefore(x) or at x
+ * for x in ts restarts after x (two nextafters, or one). */
+static double clip_bump(const double *ts, int n, int dir, double t, int *made_jump) {
+  double n1 = nextafter(t, INFINITY);
+  int mj1 = 0, mj2 = 0;
+  for (int i = 0; i < n; i++) {
+    double v = clip_get(ts, n, i, dir);
+    mj1 |= (v == n1);
+    mj2 |= (v == t);
+  }
+  double out = mj1 ? nextafter(n1, INFINITY) : t;
+  if (mj2) out = n1;
+  *made_jump = mj1 | mj2;
+  return out;
+}
+
+typedef struct {
+  const double *step_ts, *jump_ts;
+  int n_step, n_jump, step_index, jump_index;
+} ClipState;
+
+/* ClipStepSizeController.init (clip.py:215-276): the first step end clipped
+ * to the first step time after t0 and to just before the first jump. */
+static double clip_init(ClipState *c, int dir, double t0, double tnext) {
+  if (c->n_step) {
+    c->step_index = clip_find(c->step_ts, c->n_step, dir, t0, 0);
+    double v = clip_get(c->step_ts, c->n_step, c->step_index, dir);
+    tnext = v < tnext ? v : tnext;
+  }
+  if (c->n_jump) {
+    c->jump_index = clip_find(c->jump_ts, c->n_jump, dir, t0, 0);
+    double v = nextafter(clip_get(c->jump_ts, c->n_jump, c->jump_index, dir), -INFINITY);
+    tnext = v < tnext ? v : tnext;
+  }
+  return tnext;
+}
+
+/* ClipStepSizeController.adapt_step_size after the inner controller
+ * (clip.py:330-389).  Returns made_jump. */
+static int clip_adapt(ClipState *c, int dir, double *next_t0, double *next_t1) {
+  int made_jump = 0, mj;
+  if (c->n_step) {
+    double b0 = clip_bump(c->step_ts, c->n_step, dir, *next_t0, &mj);
+    c->step_index = clip_find(c->step_ts, c->n_step, dir, b0, c->step_index);
+    double v = clip_get(c->step_ts, c->n_step, c->step_index, dir);
+    if (v < *next_t1) *next_t1 = v;
+  }
+  if (c->n_jump) {
+    *next_t0 = clip_bump(c->jump_ts, c->n_jump, dir, *next_t0, &mj);
+    double lo = nextafter(*next_t0, INFINITY);
+    if (lo > *next_t1) *next_t1 = lo;
+    made_jump |= mj;
+    c->jump_index = clip_find(c->jump_ts, c->n_jump, dir, *next_t0, c->jump_index);
+    double v = nextafter(clip_get(c->jump_ts, c->n_jump, c->jump_index, dir), -INFINITY);
+    if (v < *next_t1) *next_t1 = v;
+  }
+  return made_jump;
+}
+
 static double error_order_of(const orc_desc *d, const Tableau *tab) {
   if (d->error_order > 0) return d->error_order;
   if (d->diffusion != ORC_DIFF_NONE) return tab->strong_order + 0.5;
@@ -830,9 +913,12 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
   memcpy(y, io->y0 + bidx * D, sizeof(double) * D);
   if (tape) { tape->dir = dir; tape->t0_eq_t1 = (t0 == t1); }
 
-  /* controller init (pid.py:316-392, constant.py:30-57) */
+  /* controller init (pid.py:316-392, constant.py:30-57, clip.py:215-276) */
   CtrlState cs;
   memset(&cs, 0, sizeof cs);
+  ClipState clip = {io->ts + d->n_ts, io->ts + d->n_ts + d->n_step_ts, d->n_step_ts,
+                    d->n_jump_ts, 0, 0};
+  const int clipping = d->n_step_ts > 0 || d->n_jump_ts > 0;
   double tnext;
   if (d->controller == ORC_PID) {
     /* The terms are already wrapped when init runs (_integrate.py:1172-1176,
@@ -842,6 +928,7 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
     if (!isnan(d->dtmin)) h = h > d->dtmin ? h : d->dtmin;
     tnext = t0 + h;
     cs.prev_inv = 1.0; cs.prev_prev_inv = 1.0; cs.at_dtmin = 0;
+    if (clipping) tnext = clip_init(&clip, dir, t0, tnext);
   } else {
     cs.steps_completed = 1;
     cs.num_steps = (int)ceil((t1 - t0) / nextafter(dt0, INFINITY));
@@ -872,6 +959,7 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
     dts[0] = t0;
   }
   int first_step = 1;
+  int made_jump = 0; /* _integrate.py:1309, 425 */
   double f0[64];
   memset(f0, 0, sizeof f0);
   int result = ORC_SUCCESSFUL;
@@ -885,7 +973,8 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
       vbt_increment(d, (uint32_t)bidx, dir * tprev, dir * tnext, dw);
       dwp = dw;
     }
-    rk_step(&F, tab, dir, tprev, tnext, y, !first_step, f0, dwp, &so);
+    /* FSAL reuse unless first step or just after a jump (runge_kutta.py:684-700) */
+    rk_step(&F, tab, dir, tprev, tnext, y, !(first_step || made_jump), f0, dwp, &so);
     for (int n = 0; n < D; n++)
       if (isnan(so.err[n])) so.err[n] = INFINITY; /* _integrate.py:386 */
     int keep, cres = ORC_SUCCESSFUL;
@@ -902,6 +991,10 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
       }
       double scaled = rms_norm(sc, D);
       keep = pid_adapt(d, eord, tprev, tnext, scaled, &cs, &nt0, &nt1, &cres);
+      if (clipping) {
+        int mj = clip_adapt(&clip, dir, &nt0, &nt1);
+        if (keep) made_jump = mj; /* a rejected step keeps the old flag (:425) */
+      }
     } else {
       keep = constant_adapt(tnext, &cs, &nt0, &nt1);
     }
@@ -1128,6 +1221,22 @@ int orc_dense_evaluate(const orc_desc *d, int64_t B, const double *t0, const dou
   return 0;
 }
 
+/* The ClipStepSizeController helpers on their own (clip.py:55-118, 330-389),
+ * for known-answer checks: _find_idx_with_hint, and adapt_step_size after the
+ * inner controller proposed (next_t0, next_t1); idx = {step_index, jump_index}. */
+int orc_clip_find(const double *ts, int n, int dir, double t, int hint) {
+  return clip_find(ts, n, dir, t, hint);
+}
+
+int orc_clip_adapt(const double *step_ts, int n_step, const double *jump_ts, int n_jump,
+                   int dir, int *idx, double *next_t0, double *next_t1) {
+  ClipState c = {step_ts, jump_ts, n_step, n_jump, idx[0], idx[1]};
+  int mj = clip_adapt(&c, dir, next_t0, next_t1);
+  idx[0] = c.step_index;
+  idx[1] = c.jump_index;
+  return mj;
+}
+
 /* Brownian increments of the oracle's tree, for checking the kernels' tree. */
 int orc_vbt_increments(const orc_desc *d, int64_t n, const uint32_t *traj,
                        const double *ta, const double *tb, double *dw) {
@@ -1194,7 +1303,8 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
                        double *grad_args, double *grad_params, int nthreads) {
   validate_desc(d);
   if (d->dim > 64 || d->dim < 1) return -1;
-  if (d->save_steps || d->save_dense) return -2; /* forward outputs only */
+  if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts)
+    return -2; /* forward outputs only */
   const Tableau *tab = tableau_of(d->solver);
   const int D = d->dim;
   const int n_save = n_save_of(d);
@@ -1519,7 +1629,7 @@ int orc_backsolve(const orc_desc *d, int64_t B, const double *t0, const double *
   validate_desc(d);
   if (d->dim > 64 || d->dim < 1) return -1;
   if (d->field == ORC_CALLBACK || d->diffusion != ORC_DIFF_NONE) return -2;
-  if (d->save_steps || d->save_dense) return -2;
+  if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts) return -2;
   const int64_t N = 2 * (int64_t)d->dim + d->n_args + n_params;
   BsIO io = {d, t0, t1, dt0, time_stride, ts_saved, ys, grad_ys, args, args_stride,
              params, n_params, grad_y0, grad_args, result, stats};

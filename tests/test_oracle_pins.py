@@ -656,3 +656,112 @@ def test_dense_matches_saveat_ts_and_derivative(solver):
         lv = O.dense_evaluate(d, t0, t1, [[1.0, 0.5]], r, [kb], left=True)
         rv = O.dense_evaluate(d, t0, t1, [[1.0, 0.5]], r, [kb], left=False)
         np.testing.assert_allclose(lv, rv, rtol=1e-12, atol=1e-13)
+
+
+# ---------------------------------------------------------------------------
+# ClipStepSizeController(step_ts, jump_ts) (clip.py)
+# ---------------------------------------------------------------------------
+
+def test_clip_find_idx_with_hint():
+    # test/test_adaptive_stepsize_controller.py:284-292: the first index
+    # strictly greater than t, whatever the hint
+    ts = np.arange(5.0)
+    for hint in (0, 2, 3, 5):
+        assert O.clip_find(ts, 2.5, hint) == 3
+        assert O.clip_find(ts, 2.0, hint) == 3
+        assert O.clip_find(ts, 1.9, hint) == 2
+    # backwards in time the array is sort(-ts) = [-4, ..., 0]
+    assert O.clip_find(ts, -2.5, 0, direction=-1) == 2
+
+
+def test_clip_adapt_known_answers():
+    # clip.py:330-389 on one wrapper with jump_ts=[3, 13], step_ts=[23]
+    # (the inner wrapper of test/test_adaptive_stepsize_controller.py:255-281)
+    pb = lambda x: np.nextafter(x, -np.inf)  # noqa: E731
+    na = lambda x: np.nextafter(x, np.inf)  # noqa: E731
+    t0, t1, mj, idx = O.clip_adapt([23.0], [3.0, 13.0], 1.0, 11.0)
+    assert (t0, t1, mj) == (1.0, pb(3.0), False)
+    # a step that ended just before the jump restarts after it (two ulps on)
+    t0, t1, mj, idx = O.clip_adapt([23.0], [3.0, 13.0], t1, t1 + 10.0, idx)
+    assert t0 == na(3.0) and mj and t1 == min(pb(3.0) + 10.0, pb(13.0))
+    # and a step that ended exactly on the jump restarts one ulp on
+    t0, t1, mj, idx = O.clip_adapt([23.0], [3.0, 13.0], 13.0, 14.0, idx)
+    assert t0 == na(13.0) and mj and t1 == 14.0
+    t0, t1, mj, idx = O.clip_adapt([23.0], [3.0, 13.0], 20.0, 30.0, idx)
+    assert (t0, t1, mj) == (20.0, 23.0, False)
+    # step_ts: a step that ended on a step time clips to the next one
+    t0, t1, mj, idx = O.clip_adapt([2.0, 13.0], None, 2.0, 40.0)
+    assert (t0, t1, mj) == (2.0, 13.0, False)
+    # never an empty interval after a bump (clip.py:354-372)
+    t0, t1, mj, idx = O.clip_adapt(None, [0.98], pb(0.98), pb(0.98))
+    assert t0 == na(0.98) and t1 == na(t0) and mj
+
+
+def _clip_desc(**kw):
+    return O.make_desc(**dict(dict(solver=O.DOPRI5, controller=O.PID, rtol=1e-4, atol=1e-6,
+                                   save_steps=1, save_t1=0), **kw))
+
+
+@pytest.mark.parametrize("backwards", [False, True])
+def test_clip_step_ts(backwards):
+    # test/test_adaptive_stepsize_controller.py:18-41: y' = -0.2 y, Dopri5,
+    # PID(1e-4, 1e-6), step_ts=[3, 4], SaveAt(steps=True): 3 and 4 are steps
+    t0, t1 = (5.0, 0.0) if backwards else (0.0, 5.0)
+    d = _clip_desc(field=O.LINEAR, dim=1)
+    r = O.solve(d, t0, t1, None, [[1.0]], params=[[-0.2]], step_ts=[3, 4])
+    assert r["result"][0] == 0
+    assert 3.0 in r["ts"][0] and 4.0 in r["ts"][0]
+    r0 = O.solve(_clip_desc(field=O.LINEAR, dim=1), t0, t1, None, [[1.0]], params=[[-0.2]])
+    assert 3.0 not in r0["ts"][0]
+
+
+def _forced(t, y):
+    # test/test_adaptive_stepsize_controller.py:47-51: a damped oscillator
+    # whose forcing flips sign at t = 7.5
+    x, v = y
+    force = 10.0 if t < 7.5 else -10.0
+    return np.array([v, -4 * np.pi ** 2 * x - 4 * np.pi * 0.05 * v + force])
+
+
+@pytest.mark.parametrize("backwards", [False, True])
+def test_clip_jump_ts(backwards):
+    # test/test_adaptive_stepsize_controller.py:44-88
+    t0, t1 = (15.0, 0.0) if backwards else (0.0, 15.0)
+
+    def run(**kw):
+        d = _clip_desc(field=O.CALLBACK, dim=2)
+        return O.solve(d, t0, t1, None, [[1.5, 0.0]], callback=_forced, **kw)
+
+    no_jump, jump = run(), run(jump_ts=[7.5])
+    assert no_jump["stats"][0, 0] > jump["stats"][0, 0]
+    assert jump["result"][0] == 0
+    assert run(jump_ts=[7.5], step_ts=[7.5])["result"][0] == 0
+    r = run(jump_ts=[7.5], step_ts=[3.5, 8])
+    assert r["result"][0] == 0
+    assert 3.5 in r["ts"][0] and 8.0 in r["ts"][0]
+    # the solve steps to just before the jump and restarts just after it
+    ts = np.abs(r["ts"][0][np.isfinite(r["ts"][0])])
+    if backwards:
+        assert np.nextafter(7.5, np.inf) in ts and np.nextafter(7.5, -np.inf) not in ts
+    else:
+        assert np.nextafter(7.5, -np.inf) in ts and 7.5 not in ts
+
+
+def test_clip_jump_at_t1():
+    # test/test_adaptive_stepsize_controller.py:322-343 (here in FP64 time):
+    # a jump at t1 still ends the solve exactly at t1
+    d = O.make_desc(solver=O.HEUN, controller=O.PID, rtol=1e-6, atol=1e-6, field=O.LINEAR,
+                    dim=1, n_ts=1, save_t1=0, max_steps=1 << 16)
+    r = O.solve(d, 0.0, 1e3, 0.01, [[1.0]], params=[[-1.0]], ts=[1e3], jump_ts=[1e3])
+    assert r["result"][0] == 0 and r["ts"][0, 0] == 1e3
+
+
+def test_clip_t0_just_before_jump():
+    # test/test_adaptive_stepsize_controller.py:346-371 (without its event): a
+    # solve starting at prevbefore(jump) takes a zero-length first step, then
+    # restarts past the jump and finishes
+    d = O.make_desc(solver=O.HEUN, controller=O.PID, rtol=1e-6, atol=1e-6, field=O.LINEAR,
+                    dim=4, save_t1=1, max_steps=100)
+    r = O.solve(d, np.nextafter(0.98, -np.inf), 1.2, None, np.zeros((1, 4)),
+                params=np.zeros((4, 4)), jump_ts=[0.98])
+    assert r["result"][0] == 0 and r["ts"][0, 0] == 1.2
