@@ -24,7 +24,8 @@ __all__ = [
     "dense_evaluate", "n_saves", "STAGES", "clip_times", "clip_find", "clip_adapt",
     "EULER", "HEUN", "DOPRI5", "TSIT5", "CONSTANT", "PID",
     "LOTKA_VOLTERRA", "VAN_DER_POL", "ORNSTEIN_UHLENBECK", "MLP", "LINEAR", "CALLBACK",
-    "DIFF_NONE", "DIFF_OU", "DIFF_TANH_DIAG", "RESULT_NAMES",
+    "DIFF_NONE", "DIFF_OU", "DIFF_TANH_DIAG", "RESULT_NAMES", "EV_LINEAR", "EV_LINEAR_BOOL",
+    "EV_STEADY", "EV_EITHER", "EV_UP", "EV_DOWN",
 ]
 
 EULER, HEUN, DOPRI5, TSIT5 = 0, 1, 2, 3
@@ -32,8 +33,11 @@ CONSTANT, PID = 0, 1
 LOTKA_VOLTERRA, VAN_DER_POL, ORNSTEIN_UHLENBECK, MLP, LINEAR, CALLBACK = 0, 1, 2, 3, 4, 5
 DIFF_NONE, DIFF_OU, DIFF_TANH_DIAG = 0, 1, 2
 NORM_RMS, NORM_ADJOINT_SEMI = 0, 1
+EV_LINEAR, EV_LINEAR_BOOL, EV_STEADY = 0, 1, 2
+EV_EITHER, EV_UP, EV_DOWN = 0, 1, 2
 RESULT_NAMES = {0: "successful", 1: "max_steps_reached", 2: "dt_min_reached",
-                3: "event_occurred", 4: "max_steps_rejected", 5: "internal_error"}
+                3: "event_occurred", 4: "max_steps_rejected", 5: "internal_error",
+                6: "nonlinear_max_steps_reached"}
 
 
 class OracleDesc(ctypes.Structure):
@@ -54,7 +58,10 @@ class OracleDesc(ctypes.Structure):
         ("vbt_tol", ctypes.c_double), ("seed", ctypes.c_uint64),
         ("norm", ctypes.c_int32), ("save_steps", ctypes.c_int32),
         ("save_dense", ctypes.c_int32), ("n_step_ts", ctypes.c_int32),
-        ("n_jump_ts", ctypes.c_int32), ("pad_", ctypes.c_int32),
+        ("n_jump_ts", ctypes.c_int32), ("n_event", ctypes.c_int32),
+        ("event_root", ctypes.c_int32), ("ev_kind", ctypes.c_int32 * 4),
+        ("ev_dir", ctypes.c_int32 * 4), ("newton_rtol", ctypes.c_double),
+        ("newton_atol", ctypes.c_double), ("ev_coef", ctypes.c_double * 24),
     ]
 
 
@@ -65,7 +72,8 @@ _DEFAULTS = dict(solver=TSIT5, controller=PID, field=LOTKA_VOLTERRA, dim=2,
                  save_t0=0, save_t1=1, max_steps=4096, n_args=0, mlp_depth=0,
                  mlp_widths=(), diffusion=DIFF_NONE, vbt_t0=0.0, vbt_t1=1.0,
                  vbt_tol=1e-3, seed=0, norm=0, save_steps=0, save_dense=0,
-                 n_step_ts=0, n_jump_ts=0)
+                 n_step_ts=0, n_jump_ts=0, n_event=0, event_root=0, ev_kind=(), ev_dir=(),
+                 newton_rtol=1e-5, newton_atol=1e-5, ev_coef=())
 
 STAGES = {EULER: 1, HEUN: 2, DOPRI5: 7, TSIT5: 7}
 
@@ -91,6 +99,11 @@ def make_desc(**kw) -> OracleDesc:
         if k == "mlp_widths":
             arr = (ctypes.c_int32 * 9)(*([int(x) for x in v] + [0] * (9 - len(v))))
             d.mlp_widths = arr
+        elif k in ("ev_kind", "ev_dir"):
+            setattr(d, k, (ctypes.c_int32 * 4)(*([int(x) for x in v] + [0] * (4 - len(v)))))
+        elif k == "ev_coef":
+            v = [float(x) for x in v]
+            setattr(d, k, (ctypes.c_double * 24)(*(v + [0.0] * (24 - len(v)))))
         elif k in ("dtmin", "dtmax") and v is None:
             setattr(d, k, math.nan)
         else:
@@ -120,7 +133,7 @@ def load():
                               i64, dp, dp, VF_CB, ctypes.c_void_p, dp, dp, ip, ip,
                               ctypes.c_int]
     lib.orc_solve.restype = ctypes.c_int
-    lib.orc_solve_dense.argtypes = lib.orc_solve.argtypes[:-1] + [dp, dp, ip, ctypes.c_int]
+    lib.orc_solve_dense.argtypes = lib.orc_solve.argtypes[:-1] + [dp, dp, ip, ip, ctypes.c_int]
     lib.orc_solve_dense.restype = ctypes.c_int
     lib.orc_dense_evaluate.argtypes = [ctypes.POINTER(OracleDesc), i64, dp, dp, i64, dp, dp,
                                        dp, ip, i64, dp, i64, ctypes.c_int, ctypes.c_int, dp]
@@ -241,17 +254,21 @@ def solve(desc: OracleDesc, t0, t1, dt0, y0, args=None, params=None, ts=None,
             ov[:] = callback(t, yv.copy())
         keep = cb = VF_CB(_cb)
     ip = ctypes.POINTER(ctypes.c_int32)
+    ev = np.full(B, -1, dtype=np.int32) if desc.n_event else None
     rc = lib.orc_solve_dense(ctypes.byref(desc), B, _dptr(t0), _dptr(t1), _dptr(dt0), tstride,
                              _dptr(y0), _dptr(args_arr), astride, _dptr(params), _dptr(ts), cb,
                              None, _dptr(ys), _dptr(ts_out), res.ctypes.data_as(ip),
                              stats.ctypes.data_as(ip),
                              _dptr(dense["ts"]) if dense else None,
                              _dptr(dense["info"]) if dense else None,
-                             dense["n"].ctypes.data_as(ip) if dense else None, int(nthreads))
+                             dense["n"].ctypes.data_as(ip) if dense else None,
+                             ev.ctypes.data_as(ip) if ev is not None else None, int(nthreads))
     del keep
     if rc != 0:
         raise ValueError(f"oracle rejected the problem (code {rc})")
     out = dict(ys=ys, ts=ts_out, result=res, stats=stats)
+    if ev is not None:
+        out["event_index"] = ev
     if dense:
         out.update(dense_ts=dense["ts"], dense_info=dense["info"], dense_n=dense["n"])
     return out

@@ -18,6 +18,10 @@
  *   constant step size .... diffrax/_step_size_controller/constant.py:20-104
  *   clip controller ....... diffrax/_step_size_controller/clip.py:36-427
  *                           (step_ts, jump_ts; no store_rejected_steps)
+ *   events ................ diffrax/_event.py:13-175 (registered conditions),
+ *                           diffrax/_integrate.py:542-633 (detection),
+ *                           686-821 (root find and unsave), 847-877, with
+ *                           optimistix.Newton (cauchy termination) restated
  *   terms ................. diffrax/_term.py:174-226, 271-555, 666-764
  *   virtual Brownian tree . diffrax/_brownian/tree.py:245-354, 366-448,
  *                           607-621, 626-773 (BrownianIncrement branch)
@@ -49,6 +53,12 @@ enum {
 };
 enum { ORC_DIFF_NONE = 0, ORC_DIFF_OU = 1, ORC_DIFF_TANH_DIAG = 2 };
 enum { ORC_NORM_RMS = 0, ORC_NORM_ADJOINT_SEMI = 1 };
+/* Registered event conditions: a linear form w.y + wt t + c of the state and
+ * the loop's time (real-valued, or its sign as a boolean), and
+ * steady_state_event (boolean, _event.py:120-175). */
+enum { ORC_EV_LINEAR = 0, ORC_EV_LINEAR_BOOL = 1, ORC_EV_STEADY = 2 };
+enum { ORC_EV_EITHER = 0, ORC_EV_UP = 1, ORC_EV_DOWN = 2 };
+#define ORC_MAX_EVENTS 4
 
 /* RESULTS codes (diffrax/_solution.py:13-31): successful must be 0. */
 enum {
@@ -57,7 +67,8 @@ enum {
   ORC_DT_MIN_REACHED = 2,
   ORC_EVENT_OCCURRED = 3,
   ORC_MAX_STEPS_REJECTED = 4,
-  ORC_INTERNAL_ERROR = 5
+  ORC_INTERNAL_ERROR = 5,
+  ORC_EVENT_ROOT_MAX_STEPS = 6 /* the event's root find did not converge */
 };
 
 typedef void (*orc_vf_cb)(double t, const double *y, double *out, int dim,
@@ -84,7 +95,15 @@ typedef struct {
    * times follow the n_ts SaveAt times in the solve's `ts` array, each group
    * sorted increasing in the caller's time */
   int32_t n_step_ts, n_jump_ts;
-  int32_t pad_;
+  /* Event(cond_fn=[...], root_finder, direction): n_event conditions of kind
+   * ev_kind (ORC_EV_*) and direction ev_dir (ORC_EV_EITHER/UP/DOWN); linear:
+   * ev_coef[6 i + n] = w_n (n < dim <= 4), [6 i + 4] = wt, [6 i + 5] = c;
+   * steady state: [6 i] = rtol, [6 i + 1] = atol.  event_root = 1 finds the
+   * event time by Newton's method with newton_rtol / newton_atol. */
+  int32_t n_event, event_root;
+  int32_t ev_kind[ORC_MAX_EVENTS], ev_dir[ORC_MAX_EVENTS];
+  double newton_rtol, newton_atol;
+  double ev_coef[6 * ORC_MAX_EVENTS];
 } orc_desc;
 
 /* ------------------------------------------------------------------------ */
@@ -737,6 +756,8 @@ static int constant_adapt(double t1, CtrlState *cs, double *next_t0, double *nex
   int sc = cs->steps_completed + 1;
   double t1n = cs->t0_sim + (cs->t1_sim - cs->t0_sim) * ((double)sc / (double)cs->num_steps);
   if (sc == cs->num_steps) t1n = cs->t1_sim;
+  /* an infinite t1 (num_steps = -1) keeps adding dt0 (constant.py:48-55, 94-97) */
+  if (cs->num_steps < 0) t1n = t1 + cs->t1_sim;
   cs->steps_completed = sc;
   *next_t0 = t1;
   *next_t1 = t1n;
@@ -781,6 +802,9 @@ typedef struct {
   const double *step_ts, *jump_ts;
   int n_step, n_jump, step_index, jump_index;
 } ClipState;
+
+/* jnp.sign, with NaN for NaN */
+static double ev_sign(double x) { return isnan(x) ? NAN : (double)((x > 0) - (x < 0)); }
 
 /* ClipStepSizeController.init (clip.py:215-276): the first step end clipped
  * to the first step time after t0 and to just before the first jump. */
@@ -827,6 +851,88 @@ static double error_order_of(const orc_desc *d, const Tableau *tab) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Events (_event.py, _integrate.py:542-633, 686-821).                       */
+/* ------------------------------------------------------------------------ */
+static void interp_eval(int solver, const StepOut *so, int s, double t, double *out);
+static void interp_deriv_coeffs(int solver, int s, double t, double *ay0, double *ay1,
+                                double g[7]);
+
+/* Value of condition i at the loop's time t (the direction-flipped time the
+ * reference passes to cond_fn) and state y; booleans are 0 / 1. */
+static double ev_value(const Field *F, int dir, int i, double t, const double *y) {
+  const orc_desc *d = F->d;
+  const double *c = d->ev_coef + 6 * i;
+  if (d->ev_kind[i] == ORC_EV_STEADY) {
+    /* norm(vf) < atol + rtol norm(y) with the PID's rms_norm; the wrapped
+     * field is dir * f(dir * t, y), of the same norm (_event.py:164-175) */
+    double f[64];
+    field_drift(F, dir * t, y, f);
+    return rms_norm(f, d->dim) < c[1] + c[0] * rms_norm(y, d->dim) ? 1.0 : 0.0;
+  }
+  double v = 0.0;
+  for (int n = 0; n < d->dim; n++) v += c[n] * y[n];
+  v += c[4] * t;
+  v += c[5];
+  if (d->ev_kind[i] == ORC_EV_LINEAR_BOOL) return v > 0 ? 1.0 : 0.0;
+  return v;
+}
+
+/* Whether condition i triggers between values old and new (_integrate.py:585-602). */
+static int ev_triggered(const orc_desc *d, int i, double old_v, double new_v) {
+  if (d->ev_kind[i] != ORC_EV_LINEAR) return new_v != 0.0;
+  double so = ev_sign(old_v), sn = ev_sign(new_v);
+  switch (d->ev_dir[i]) {
+    case ORC_EV_UP: return so <= 0 && sn > 0;
+    case ORC_EV_DOWN: return so > 0 && sn <= 0;
+    default: return so != sn || isnan(so) || isnan(sn);
+  }
+}
+
+/* The event's root find (_integrate.py:704-779): optimistix.Newton with
+ * cauchy_termination on g(t) = cond_i(t, interp(t)) over the last step's
+ * interval [so->tprev, so->tnext] from t = so->tnext, each iterate clipped to
+ * the interval; it stops once the step was below atol + rtol |t| and |g| at
+ * the previous iterate below atol, from the second iteration on, or after 256
+ * iterations (not converged).  A boolean condition has its root at the end of
+ * the step.  Returns the root; *ok = 0 if it did not converge. */
+static double ev_root(const Field *F, const Tableau *tab, int i, const StepOut *so, int *ok) {
+  const orc_desc *d = F->d;
+  const int D = d->dim;
+  *ok = 1;
+  if (d->ev_kind[i] != ORC_EV_LINEAR) return so->tnext;
+  const double *c = d->ev_coef + 6 * i;
+  const double lo = so->tprev, hi = so->tnext, span = hi - lo;
+  double y = hi;
+  for (int step = 1; step <= 256; step++) {
+    double yv[64], ay0, ay1, g[7];
+    interp_eval(d->solver, so, tab->s, y, yv);
+    double f = 0.0;
+    for (int n = 0; n < D; n++) f += c[n] * yv[n];
+    f += c[4] * y;
+    f += c[5];
+    /* g'(t) = w . dinterp/dt + wt, dinterp/dt = (d/dtheta) / span */
+    interp_deriv_coeffs(d->solver, tab->s, linear_rescale(lo, y, hi), &ay0, &ay1, g);
+    double fp = 0.0;
+    for (int n = 0; n < D; n++) {
+      double v = ay0 * so->y0[n] + ay1 * so->y1[n];
+      for (int j = 0; j < tab->s; j++) v += g[j] * so->k[j][n];
+      fp += c[n] * (span == 0.0 ? 0.0 : v / span);
+    }
+    fp += c[4];
+    double diff = f / fp;
+    double ny = y - diff;
+    if (ny < lo) ny = lo;
+    if (ny > hi) ny = hi;
+    if (isnan(ny)) { *ok = 0; return y; }
+    double diffsize = fabs(diff) / (d->newton_atol + d->newton_rtol * fabs(ny));
+    y = ny;
+    if (step >= 2 && diffsize < 1.0 && fabs(f) < d->newton_atol) return y;
+  }
+  *ok = 0;
+  return y;
+}
+
+/* ------------------------------------------------------------------------ */
 /* The per-trajectory solve loop (_integrate.py:302-885, init 1036-1305).    */
 /* ------------------------------------------------------------------------ */
 typedef struct {
@@ -849,6 +955,8 @@ typedef struct {
    * [B, max_steps, (2 + s) dim] (+inf where unused), and steps + 1 [B] */
   double *dense_ts, *dense_info;
   int32_t *dense_n;
+  /* Event: the index of the condition that ended the solve, -1 if none [B] */
+  int32_t *event_index;
 } SolveIO;
 
 /* A record of one accepted step, kept for the discretise-then-optimise VJP. */
@@ -931,8 +1039,8 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
     if (clipping) tnext = clip_init(&clip, dir, t0, tnext);
   } else {
     cs.steps_completed = 1;
-    cs.num_steps = (int)ceil((t1 - t0) / nextafter(dt0, INFINITY));
-    cs.t0_sim = t0; cs.t1_sim = t1;
+    cs.num_steps = isfinite(t1) ? (int)ceil((t1 - t0) / nextafter(dt0, INFINITY)) : -1;
+    cs.t0_sim = t0; cs.t1_sim = isfinite(t1) ? t1 : dt0;
     tnext = t0 + dt0;
   }
   tnext = tnext < t1 ? tnext : t1;
@@ -966,6 +1074,16 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
   int num_steps = 0, num_acc = 0, num_rej = 0;
   StepOut so;
   double dw[64];
+  /* Event values at (t0, y0) (_integrate.py:1333-1426): a boolean condition
+   * that already holds ends the solve before its first step. */
+  double ev_val[ORC_MAX_EVENTS];
+  int ev_idx = -1, ev_have = 0;
+  StepOut ev_so; /* the step over which the event fired */
+  for (int i = 0; i < d->n_event; i++) {
+    ev_val[i] = ev_value(&F, dir, i, t0, y);
+    if (ev_idx < 0 && d->ev_kind[i] != ORC_EV_LINEAR && ev_val[i] != 0.0) ev_idx = i;
+  }
+  if (ev_idx >= 0) result = ORC_EVENT_OCCURRED;
   while (tprev < t1 && result == ORC_SUCCESSFUL) {
     if (num_steps >= d->max_steps) break;
     const double *dwp = NULL;
@@ -1033,11 +1151,49 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
     if (keep) num_acc++; else num_rej++;
     tprev = nt0;
     tnext = nt1;
+    /* _integrate.py:542-633: every condition at the new (tprev, y); the first
+     * that triggered (in order) ends the solve */
+    if (d->n_event) {
+      int fired = -1;
+      for (int i = 0; i < d->n_event; i++) {
+        double v = ev_value(&F, dir, i, tprev, y);
+        if (fired < 0 && ev_triggered(d, i, ev_val[i], v)) fired = i;
+        ev_val[i] = v;
+      }
+      if (fired >= 0) {
+        ev_idx = fired;
+        ev_so = so;
+        ev_have = 1;
+        result = ORC_EVENT_OCCURRED;
+      }
+    }
+  }
+  /* _integrate.py:686-821: with a root finder the final time is the event's
+   * root inside the last step and y there its interpolant (y itself when no
+   * step was taken); every save after it is deleted */
+  double tfinal = tprev, yf[64];
+  const double *yfinal = y;
+  const int ev_root_finder = d->n_event > 0 && d->event_root;
+  if (ev_root_finder && ev_idx >= 0) {
+    if (ev_have) {
+      int ok = 1;
+      tfinal = ev_root(&F, tab, ev_idx, &ev_so, &ok);
+      interp_eval(d->solver, &ev_so, tab->s, tfinal, yf);
+      yfinal = yf;
+      if (!ok) result = ORC_EVENT_ROOT_MAX_STEPS;
+    }
+    for (int i = 0; i < n_save; i++) {
+      if (tso[i] > tfinal) {
+        if (tso[i] < INFINITY) save_index--;
+        tso[i] = INFINITY;
+        for (int n = 0; n < D; n++) ys[(int64_t)i * D + n] = INFINITY;
+      }
+    }
   }
   /* _integrate.py:823-845: t0 == t1 fills the ts outputs with y0 */
   if (t0 == t1) {
     for (int i = 0; i < d->n_ts; i++) {
-      for (int n = 0; n < D; n++) ys[(int64_t)save_index * D + n] = y[n];
+      for (int n = 0; n < D; n++) ys[(int64_t)save_index * D + n] = yfinal[n];
       tso[save_index] = t0;
       save_index++;
     }
@@ -1046,9 +1202,13 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
    * SaveAt(steps=n) saved it: always for n = 1, for n > 1 when the accepted
    * steps are a multiple of n */
   int t1_via_steps = d->save_steps == 0 ? 0 : (d->save_steps == 1 ? 1 : (num_acc % d->save_steps == 0));
-  if (d->save_t1 && !t1_via_steps) {
-    for (int n = 0; n < D; n++) ys[(int64_t)save_index * D + n] = y[n];
-    tso[save_index] = tprev;
+  /* with an event root finder the final value is saved whenever steps saved
+   * the t1 value, since that save was deleted above (:866-872) */
+  const int save_final = ev_root_finder ? (d->save_t1 || t1_via_steps)
+                                        : (d->save_t1 && !t1_via_steps);
+  if (save_final) {
+    for (int n = 0; n < D; n++) ys[(int64_t)save_index * D + n] = yfinal[n];
+    tso[save_index] = tfinal;
     if (tape) tape->t1_slot = save_index;
     save_index++;
   }
@@ -1056,6 +1216,7 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
   for (int i = 0; i < n_save; i++) tso[i] *= dir;
   io->result[bidx] = result;
   if (io->dense_n) io->dense_n[bidx] = num_acc + 1;
+  if (io->event_index) io->event_index[bidx] = ev_idx;
   io->stats[bidx * 3 + 0] = num_steps;
   io->stats[bidx * 3 + 1] = num_acc;
   io->stats[bidx * 3 + 2] = num_rej;
@@ -1068,13 +1229,18 @@ int orc_solve_dense(const orc_desc *d, int64_t B, const double *t0, const double
                     const double *args, int64_t args_stride, const double *params,
                     const double *ts, orc_vf_cb cb, void *cb_ctx, double *ys_out,
                     double *ts_out, int32_t *result, int32_t *stats, double *dense_ts,
-                    double *dense_info, int32_t *dense_n, int nthreads) {
+                    double *dense_info, int32_t *dense_n, int32_t *event_index,
+                    int nthreads) {
   validate_desc(d);
   if (d->dim > 64 || d->dim < 1) return -1;
   if (d->save_steps < 0) return -1;
   if ((dense_ts != NULL) != (d->save_dense != 0)) return -1;
+  if (d->n_event < 0 || d->n_event > ORC_MAX_EVENTS) return -1;
+  for (int i = 0; i < d->n_event; i++)
+    if (d->ev_kind[i] != ORC_EV_STEADY && d->dim > 4) return -1;
   SolveIO io = {d, t0, t1, dt0, time_stride, y0, args, args_stride, params, ts,
-                cb, cb_ctx, ys_out, ts_out, result, stats, dense_ts, dense_info, dense_n};
+                cb, cb_ctx, ys_out, ts_out, result, stats, dense_ts, dense_info, dense_n,
+                event_index};
 #ifdef _OPENMP
   if (nthreads > 0 && d->field != ORC_CALLBACK) {
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
@@ -1095,7 +1261,7 @@ int orc_solve(const orc_desc *d, int64_t B, const double *t0, const double *t1,
   if (d->save_dense) return -1;
   return orc_solve_dense(d, B, t0, t1, dt0, time_stride, y0, args, args_stride, params,
                          ts, cb, cb_ctx, ys_out, ts_out, result, stats, NULL, NULL, NULL,
-                         nthreads);
+                         NULL, nthreads);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1303,7 +1469,7 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
                        double *grad_args, double *grad_params, int nthreads) {
   validate_desc(d);
   if (d->dim > 64 || d->dim < 1) return -1;
-  if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts)
+  if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts || d->n_event)
     return -2; /* forward outputs only */
   const Tableau *tab = tableau_of(d->solver);
   const int D = d->dim;
@@ -1629,7 +1795,7 @@ int orc_backsolve(const orc_desc *d, int64_t B, const double *t0, const double *
   validate_desc(d);
   if (d->dim > 64 || d->dim < 1) return -1;
   if (d->field == ORC_CALLBACK || d->diffusion != ORC_DIFF_NONE) return -2;
-  if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts) return -2;
+  if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts || d->n_event) return -2;
   const int64_t N = 2 * (int64_t)d->dim + d->n_args + n_params;
   BsIO io = {d, t0, t1, dt0, time_stride, ts_saved, ys, grad_ys, args, args_stride,
              params, n_params, grad_y0, grad_args, result, stats};

@@ -765,3 +765,135 @@ def test_clip_t0_just_before_jump():
     r = O.solve(d, np.nextafter(0.98, -np.inf), 1.2, None, np.zeros((1, 4)),
                 params=np.zeros((4, 4)), jump_ts=[0.98])
     assert r["result"][0] == 0 and r["ts"][0, 0] == 1.2
+
+
+# ---------------------------------------------------------------------------
+# Events (_event.py, _integrate.py:542-633, 686-877), restating
+# test/test_event.py with the registered conditions: a linear form
+# w.y + wt t + c (real-valued, or "> 0" as a boolean) and steady_state_event.
+# ---------------------------------------------------------------------------
+
+def _event_desc(conds, root=False, dim=1, **kw):
+    """conds: list of (kind, coef[6], direction)."""
+    base = dict(solver=O.TSIT5, controller=O.CONSTANT, dim=dim, save_t1=1,
+                n_event=len(conds), event_root=int(root), ev_kind=[c[0] for c in conds],
+                ev_coef=sum([list(c[1]) for c in conds], []), ev_dir=[c[2] for c in conds],
+                newton_rtol=1e-5, newton_atol=1e-5)
+    base.update(kw)
+    return O.make_desc(**base)
+
+
+def _lin(w=(0, 0, 0, 0), wt=0.0, c=0.0, kind=O.EV_LINEAR, direction=O.EV_EITHER):
+    return (kind, list(w) + [0.0] * (4 - len(w)) + [wt, c], direction)
+
+
+def _const_field(v):
+    return lambda t, y: np.asarray(v, dtype=np.float64)
+
+
+def test_event_steady_state():
+    # test/test_event.py:106-121: tolerances from the PID controller
+    d = _event_desc([(O.EV_STEADY, [1e-3, 1e-6, 0, 0, 0, 0], 0)], controller=O.PID,
+                    rtol=1e-3, atol=1e-6, field=O.LINEAR)
+    r = O.solve(d, 0.0, np.inf, 1.0, [[1.0]], params=[[-1.0]])
+    assert r["event_index"][0] == 0 and r["result"][0] == 3
+    assert abs(r["ys"][0, 0, 0]) < 1e-5
+
+
+def test_event_no_step():
+    # test/test_event.py:124-143: a boolean condition true at t0 ends the
+    # solve before its first step
+    d = _event_desc([_lin(w=(0, -1), kind=O.EV_LINEAR_BOOL)], dim=2, field=O.CALLBACK)
+    r = O.solve(d, 0.0, 10.0, 1.0, [[1.0, -0.1]], callback=_const_field([1.0, 1.0]))
+    assert r["stats"][0, 0] == 0 and r["event_index"][0] == 0
+    assert np.array_equal(r["ys"][0, -1], [1.0, -0.1]) and r["ts"][0, -1] == 0.0
+
+
+def test_event_continuous_terminate():
+    # test/test_event.py:146-178: t > 10 as a boolean ends with y > 10; t - 10
+    # as a real condition ends at t >= 10 (no root finder)
+    d = _event_desc([_lin(wt=1.0, c=-10.0, kind=O.EV_LINEAR_BOOL)], field=O.LINEAR)
+    r = O.solve(d, 0.0, np.inf, 1.0, [[1.0]], params=[[1.0]])
+    assert r["ys"][0, 0, 0] > 10 and r["result"][0] == 3
+    d = _event_desc([_lin(wt=1.0, c=-10.0)], field=O.LINEAR)
+    r = O.solve(d, 0.0, np.inf, 1.0, [[1.0]], params=[[1.0]])
+    assert r["ts"][0, 0] >= 10
+
+
+def test_event_time_and_value():
+    # test/test_event.py:181-216: with Newton(1e-5, 1e-5) the event time of
+    # y = e^t crossing e is 1 (rtol 1e-4), and y' = 1 from -10 stops at y = 0
+    d = _event_desc([_lin(w=(1,), c=-math.e)], root=True, field=O.LINEAR)
+    r = O.solve(d, 0.0, np.inf, 1.0, [[1.0]], params=[[1.0]])
+    assert tree_allclose(r["ts"][0, 0], 1.0, rtol=1e-4)
+    d = _event_desc([_lin(w=(1,))], root=True, field=O.CALLBACK)
+    r = O.solve(d, 0.0, np.inf, 1.0, [[-10.0]], callback=_const_field([1.0]))
+    assert tree_allclose(r["ys"][0, 0, 0], 0.0, rtol=1e-5, atol=1e-8)
+    assert tree_allclose(r["ts"][0, 0], 10.0, rtol=1e-5)
+
+
+def test_event_none_and_two_conditions():
+    # test/test_event.py:219-262
+    d = _event_desc([_lin(w=(1,))], root=True, field=O.CALLBACK)
+    r = O.solve(d, 0.0, 5.0, 1.0, [[-10.0]], callback=_const_field([1.0]))
+    assert r["event_index"][0] == -1 and r["result"][0] == 0
+    assert tree_allclose(r["ts"][0, 0], 5.0)
+    d = _event_desc([_lin(wt=1.0, c=-10.0), _lin(w=(1,), c=5.0)], root=True, field=O.CALLBACK)
+    r = O.solve(d, 0.0, np.inf, 1.0, [[-10.0]], callback=_const_field([1.0]))
+    assert r["event_index"][0] == 1
+    assert tree_allclose(r["ts"][0, 0], 5.0, rtol=1e-5)
+
+
+def test_event_directions():
+    # _integrate.py:585-597: up-crossings only, down-crossings only
+    for direction, fires in ((O.EV_UP, True), (O.EV_DOWN, False), (O.EV_EITHER, True)):
+        d = _event_desc([_lin(w=(1,), direction=direction)], root=True, field=O.CALLBACK)
+        r = O.solve(d, 0.0, 20.0, 1.0, [[-10.0]], callback=_const_field([1.0]))
+        assert (r["event_index"][0] == 0) == fires
+
+
+@pytest.mark.parametrize("steps", (1, 2, 3, 4, 5))
+def test_event_save_all_steps(steps):
+    # test/test_event.py:566-612: y' = (1, 1), event x = thr, every step saved;
+    # the save after the event time is replaced by the event's (t, y)
+    thr = steps - 0.5
+    for t0_save, t1_save, n in ((0, 0, steps), (0, 1, steps), (1, 1, steps + 1)):
+        d = _event_desc([_lin(w=(1, 0), c=-thr)], root=True, dim=2, field=O.CALLBACK,
+                        save_steps=1, save_t0=t0_save, save_t1=t1_save, max_steps=4096)
+        r = O.solve(d, 0.0, 10.0, 1.0, [[0.0, -thr]], callback=_const_field([1.0, 1.0]))
+        ts, ys = r["ts"][0], r["ys"][0]
+        assert np.isfinite(ts).sum() == n and np.isfinite(ys[:, 0]).sum() == n
+        assert tree_allclose(ts[n - 1], thr, atol=1e-5)
+        assert tree_allclose(ys[n - 1], [thr, 0.0], atol=1e-5)
+
+
+@pytest.mark.parametrize("steps", (1, 2, 3, 4, 5))
+def test_event_save_ts(steps):
+    # test/test_event.py:615-666: ts saves after the event time are deleted;
+    # with t1 (or steps) the last save is the event's
+    thr = steps - 0.5
+    ts_save = [0.5, 3.5, 5.5]
+    cases = [(dict(), False), (dict(save_t1=1), True), (dict(save_t0=1), False),
+             (dict(save_steps=1), True)]
+    for extra, save_final in cases:
+        kw = dict(save_t1=0, save_t0=0, n_ts=3, max_steps=4096)
+        kw.update(extra)
+        d = _event_desc([_lin(w=(1, 0), c=-thr)], root=True, dim=2, field=O.CALLBACK, **kw)
+        r = O.solve(d, 0.0, 10.0, 1.0, [[0.0, -thr]], ts=ts_save,
+                    callback=_const_field([1.0, 1.0]))
+        ts, ys = r["ts"][0], r["ys"][0]
+        fin = np.isfinite(ts)
+        if save_final:
+            assert tree_allclose(ts[fin][-1], thr, atol=1e-5)
+            assert tree_allclose(ys[fin][-1], [thr, 0.0], atol=1e-5)
+        else:
+            assert np.all(ts[fin] <= thr)
+
+
+def test_event_constant_step_infinite_t1():
+    # constant.py:48-55, 94-97: with t1 = inf the grid keeps adding dt0; the
+    # condition t - 3 changes sign (to 0) on reaching t = 3
+    d = _event_desc([_lin(wt=1.0, c=-3.0)], field=O.CALLBACK, save_steps=1, save_t1=0)
+    r = O.solve(d, 0.0, np.inf, 0.5, [[0.0]], callback=_const_field([1.0]))
+    ts = r["ts"][0]
+    assert list(ts[np.isfinite(ts)]) == [0.5, 1.0, 1.5, 2.0, 2.5, 3.0]
