@@ -8,7 +8,7 @@ from ._core import (
     BacksolveAdjoint, ClipStepSizeController, ConstantStepSize, ControlTerm, Dopri5, Euler, Heun, LotkaVolterra,
     MLPField, MultiTerm, ODETerm, OrnsteinUhlenbeck, TanhDiagonalDiffusion, PIDController, RecursiveCheckpointAdjoint,
     RESULTS, SaveAt, Solution, Tsit5, VanDerPol, VirtualBrownianTree, adjoint_rms_seminorm,
-    rms_norm,
+    rms_norm, Event, LinearCondition, Newton, SteadyStateCondition, steady_state_event,
 )
 from ._integrate import DenseInterpolation, diffeqsolve, lower, oracle_fields
 

@@ -298,6 +298,84 @@ class ClipStepSizeController(AbstractStepSizeController):
 
 
 # ---------------------------------------------------------------------------
+# Events (diffrax/_event.py).  The kernels evaluate registered conditions; a
+# condition sees the loop's time (t * sign(t1 - t0), as the reference's
+# cond_fn does) and the state.
+# ---------------------------------------------------------------------------
+
+
+class LinearCondition:
+    """A registered event condition: ``sum_n y_coeffs[n] y[n] + t_coeff t +
+    offset`` (at most 4 state coefficients).  Real-valued: the event fires when
+    it changes sign (``Event.direction`` picks up- or down-crossings).  With
+    ``boolean=True`` it is the condition ``value > 0`` and fires when true.
+    Examples: ``LinearCondition([1, 0])`` is the reference's ``cond_fn = y[0]``;
+    ``LinearCondition([], t_coeff=1, offset=-10, boolean=True)`` is
+    ``t > 10``."""
+
+    def __init__(self, y_coeffs=(), t_coeff: float = 0.0, offset: float = 0.0,
+                 boolean: bool = False):
+        w = [float(x) for x in np.asarray(y_coeffs, dtype=np.float64).reshape(-1)]
+        if len(w) > 4:
+            raise ValueError("a LinearCondition takes at most 4 state coefficients")
+        self.y_coeffs, self.t_coeff, self.offset = w, float(t_coeff), float(offset)
+        self.boolean = bool(boolean)
+
+
+class SteadyStateCondition:
+    """steady_state_event (diffrax/_event.py:120-175): fires once
+    ``rms(f(t, y)) < atol + rtol * rms(y)``; unset tolerances default to the
+    adaptive step size controller's."""
+
+    def __init__(self, rtol=None, atol=None, norm=None):
+        if norm is not None and norm is not rms_norm:
+            raise NotImplementedError("steady_state_event takes the rms_norm only")
+        self.rtol, self.atol = rtol, atol
+
+
+def steady_state_event(rtol=None, atol=None, norm=None):
+    """diffrax/_event.py:120-175."""
+    return SteadyStateCondition(rtol, atol, norm)
+
+
+class Newton:
+    """The root finder of an event (optimistix.Newton(rtol, atol, norm)): Newton's
+    method with Cauchy termination on the last step's interpolant."""
+
+    def __init__(self, rtol: float, atol: float, norm=None):
+        self.rtol, self.atol = float(rtol), float(atol)
+
+
+class Event:
+    """diffrax/_event.py:13-51.  ``cond_fn`` is one registered condition or a
+    list of them (at most 4); ``direction`` is None / True / False, or a list of
+    them (True: up-crossings only, False: down-crossings only)."""
+
+    def __init__(self, cond_fn, root_finder=None, direction=None):
+        single = not isinstance(cond_fn, (list, tuple))
+        conds = [cond_fn] if single else list(cond_fn)
+        if direction in (None, False, True):
+            dirs = [direction] * len(conds)
+        else:
+            dirs = list(direction)
+            if single or len(dirs) != len(conds):
+                raise ValueError("Missmatch in the structure of `cond_fn` and `direction`.")
+        if any(x not in (None, False, True) for x in dirs):
+            raise ValueError("`direction` must be a `None`, `bool`, or a PyTree of "
+                             "`None | bool`s with the same structure as `cond_fn`.")
+        for c in conds:
+            if not isinstance(c, (LinearCondition, SteadyStateCondition)):
+                raise NotImplementedError("event conditions must be registered conditions "
+                                          "(LinearCondition, steady_state_event)")
+        if not 1 <= len(conds) <= 4:
+            raise ValueError("an Event takes 1 to 4 conditions")
+        if root_finder is not None and not isinstance(root_finder, Newton):
+            raise NotImplementedError("the event root finder must be Newton(rtol, atol)")
+        self.cond_fn, self.root_finder, self.direction = cond_fn, root_finder, direction
+        self._conds, self._dirs, self._single = conds, dirs, single
+
+
+# ---------------------------------------------------------------------------
 # SaveAt (diffrax/_saveat.py:14-105).
 # ---------------------------------------------------------------------------
 
@@ -365,6 +443,7 @@ class RESULTS(enum.IntEnum):
     event_occurred = 3
     max_steps_rejected = 4
     internal_error = 5
+    nonlinear_max_steps_reached = 6
 
 
 RESULT_MESSAGES = {
@@ -377,6 +456,8 @@ RESULT_MESSAGES = {
                             "occurred.",
     RESULTS.max_steps_rejected: "Maximum number of rejected steps was reached.",
     RESULTS.internal_error: "An internal error occurred.",
+    RESULTS.nonlinear_max_steps_reached: "The maximum number of steps was reached in the "
+                                         "nonlinear solver.",
 }
 
 
@@ -391,6 +472,7 @@ class Solution:
     stats: dict    # num_steps / num_accepted_steps / num_rejected_steps: [B] int32
     result: Any    # [B] int32 RESULTS codes
     interpolation: Any = None  # DenseInterpolation under SaveAt(dense=True)
+    event_mask: Any = None     # Event: [B] bool per condition (cond_fn's structure)
 
     def evaluate(self, t0, t1=None, left: bool = True):
         """y(t0) of every trajectory from the dense output, or y(t1) - y(t0)

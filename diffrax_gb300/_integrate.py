@@ -8,6 +8,7 @@ diffrax/_integrate.py:888-1543.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from typing import Any, Optional
 
@@ -16,7 +17,7 @@ import torch
 from . import _lib
 from ._core import (
     RESULT_MESSAGES, RESULTS, AbstractField, BacksolveAdjoint, ClipStepSizeController,
-    ConstantStepSize, ControlTerm,
+    ConstantStepSize, ControlTerm, Event, LinearCondition, SteadyStateCondition,
     Euler, MultiTerm, ODETerm, OrnsteinUhlenbeck, PIDController,
     RecursiveCheckpointAdjoint, SaveAt, Solution, VirtualBrownianTree, adjoint_rms_seminorm,
 )
@@ -50,9 +51,42 @@ def _split_terms(terms):
     raise TypeError(f"unsupported terms {terms!r}")
 
 
+def _lower_event(event: Event, controller, dim: int) -> dict:
+    """Descriptor fields of an Event (include/gbdx.h: GBDX_EV_*)."""
+    kinds, dirs, coef = [], [], []
+    inner = controller.controller if isinstance(controller, ClipStepSizeController) \
+        else controller
+    for c, d in zip(event._conds, event._dirs):
+        dirs.append(0 if d is None else (1 if d else 2))
+        if isinstance(c, LinearCondition):
+            if len(c.y_coeffs) > dim:
+                raise ValueError(f"the condition has {len(c.y_coeffs)} state coefficients "
+                                 f"for a state of dimension {dim}")
+            kinds.append(1 if c.boolean else 0)
+            coef += c.y_coeffs + [0.0] * (4 - len(c.y_coeffs)) + [c.t_coeff, c.offset]
+        else:
+            rtol, atol = c.rtol, c.atol
+            if rtol is None or atol is None:
+                if not isinstance(inner, PIDController):
+                    raise ValueError(
+                        "The `rtol`, `atol`, and `norm` for `steady_state_event` default to "
+                        "the values used with an adaptive step size controller (such as "
+                        "`diffrax.PIDController`). Either use an adaptive step size "
+                        "controller, or specify these tolerances manually.")
+                rtol = inner.rtol if rtol is None else rtol
+                atol = inner.atol if atol is None else atol
+            kinds.append(2)
+            coef += [float(rtol), float(atol), 0.0, 0.0, 0.0, 0.0]
+    rf = event.root_finder
+    return dict(n_event=len(kinds), event_root=int(rf is not None), ev_kind=kinds,
+                ev_dir=dirs, ev_coef=coef, newton_rtol=rf.rtol if rf else 1e-5,
+                newton_atol=rf.atol if rf else 1e-5)
+
+
 def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype,
           max_steps: int, n_ts: int, adjoint=None, kernel: str = "auto",
-          block_threads: int = 0, ctas_per_sm: int = 0, schedule: str = "auto") -> dict:
+          block_threads: int = 0, ctas_per_sm: int = 0, schedule: str = "auto",
+          event: Optional[Event] = None) -> dict:
     """Descriptor fields (gbdx_problem_desc) for one solve."""
     drift, diff, bm = _split_terms(terms)
     if not isinstance(drift, AbstractField):
@@ -68,7 +102,10 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
              vbt_t1=1.0, vbt_tol=1e-3, seed=0, norm=0, adjoint=0, checkpoints=0,
              schedule=SCHEDULES[schedule], mlp_precision=0,
              save_steps=int(saveat.steps), save_dense=int(saveat.dense), n_step_ts=0,
-             n_jump_ts=0, pad3=0)
+             n_jump_ts=0, n_event=0, event_root=0, ev_kind=(), ev_dir=(), pad3=0,
+             newton_rtol=1e-5, newton_atol=1e-5, ev_coef=())
+    if event is not None:
+        f.update(_lower_event(event, stepsize_controller, int(dim)))
     if hasattr(drift, "lower_fields"):
         f.update(drift.lower_fields(dim))
     if isinstance(stepsize_controller, ClipStepSizeController):
@@ -168,7 +205,7 @@ class Lowered:
 
     def __init__(self, terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
                  adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule="auto",
-                 want_grad=False):
+                 want_grad=False, event=None):
         dev = _device()
         if not isinstance(y0, torch.Tensor):
             y0 = torch.as_tensor(y0)
@@ -202,7 +239,7 @@ class Lowered:
                             dtype=self.dtype, max_steps=max_steps, n_ts=n_ts,
                             adjoint=None if backsolve else self.adjoint, kernel=kernel,
                             block_threads=block_threads, ctas_per_sm=ctas_per_sm,
-                            schedule=schedule)
+                            schedule=schedule, event=event)
         drift = _split_terms(terms)[0]
         self.drift = drift
         self.problem = _lib.get_problem(self.fields)
@@ -282,33 +319,40 @@ class Lowered:
             return ys, ts_out, res, stats, ws
         return ys, ts_out, res, stats
 
-    def run_forward_dense(self, stream=None):
-        """Forward solve under SaveAt(dense=True): the saved outputs plus the
-        dense buffers (step times, per-step records, entry counts)."""
+    def run_forward_ex(self, stream=None):
+        """Forward solve through gbdx_solve_fwd_ex: the saved outputs plus the
+        dense buffers (SaveAt(dense=True)) and the index of the event condition
+        that ended each trajectory (-1 for none)."""
         dev = self.device
         B, D, n_save = self.B, self.dim, self.n_save
-        L = int(self.fields["max_steps"]) + 1
-        stages = {0: 1, 1: 2, 2: 7, 3: 7}[self.fields["solver"]]
         ys = torch.empty((B, n_save, D), dtype=self.dtype, device=dev)
         ts_out = torch.empty((B, n_save), dtype=torch.float64, device=dev)
         res = torch.empty((B,), dtype=torch.int32, device=dev)
         stats = torch.empty((B, 3), dtype=torch.int32, device=dev)
-        dense_ts = torch.empty((B, L), dtype=torch.float64, device=dev)
-        dense_info = torch.empty((B, L - 1, (2 + stages) * D), dtype=self.dtype, device=dev)
-        dense_n = torch.empty((B,), dtype=torch.int32, device=dev)
+        p = lambda t: None if t is None or t.numel() == 0 else t.data_ptr()  # noqa: E731
+        ex = _lib.FwdExtras()
+        interp = ev = None
+        if self.fields["save_dense"]:
+            L = int(self.fields["max_steps"]) + 1
+            stages = {0: 1, 1: 2, 2: 7, 3: 7}[self.fields["solver"]]
+            dense_ts = torch.empty((B, L), dtype=torch.float64, device=dev)
+            dense_info = torch.empty((B, L - 1, (2 + stages) * D), dtype=self.dtype, device=dev)
+            dense_n = torch.empty((B,), dtype=torch.int32, device=dev)
+            ex.dense_ts, ex.dense_info, ex.dense_n = p(dense_ts), p(dense_info), p(dense_n)
+            interp = DenseInterpolation(self, dense_ts, dense_info, dense_n)
+        if self.fields["n_event"]:
+            ev = torch.empty((B,), dtype=torch.int32, device=dev)
+            ex.event_index = p(ev)
         ws_bytes = self.problem.workspace_size(B)
         ws = torch.empty((max(ws_bytes, 1),), dtype=torch.uint8, device=dev)
         if stream is None:
             stream = torch.cuda.current_stream(dev).cuda_stream
-        p = lambda t: None if t is None or t.numel() == 0 else t.data_ptr()  # noqa: E731
-        rc = self.problem.lib.gbdx_solve_fwd_dense(
+        rc = self.problem.lib.gbdx_solve_fwd_ex(
             self.problem.handle, B, p(self.t0), p(self.t1), p(self.dt0), self.tstride,
             p(self.y0), p(self.args), self.args_stride, p(self.params), p(self.save_ts),
-            p(ys), p(ts_out), p(res), p(stats), p(dense_ts), p(dense_info), p(dense_n),
-            p(ws), ws_bytes, stream)
-        _lib.check(rc, "gbdx_solve_fwd_dense")
-        interp = DenseInterpolation(self, dense_ts, dense_info, dense_n)
-        return ys, ts_out, res, stats, interp
+            p(ys), p(ts_out), p(res), p(stats), ctypes.byref(ex), p(ws), ws_bytes, stream)
+        _lib.check(rc, "gbdx_solve_fwd_ex")
+        return ys, ts_out, res, stats, interp, ev
 
     def run_backward(self, ws, grad_ys, y0, params, stream=None):
         """dL/dy0 and dL/dparams from the tape the forward left in `ws`."""
@@ -412,7 +456,8 @@ class DenseInterpolation:
 def _raise_on_failure(result: torch.Tensor):
     if _capturing():
         return
-    bad = result != 0
+    # successful and event_occurred are both fine (is_okay, _solution.py:52-54)
+    bad = (result != 0) & (result != int(RESULTS.event_occurred))
     if bool(bad.any()):
         code = int(result[bad][0].item())
         n = int(bad.sum().item())
@@ -437,22 +482,19 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     "index", "longest_first") sets the order in which the fused kernel takes
     trajectories (results do not depend on it).
     """
-    if event is not None:
-        raise NotImplementedError("events are not supported")
     if solver_state is not None or controller_state is not None or made_jump is not None:
         raise NotImplementedError("resuming from solver/controller state is not supported")
     from ._autograd import needs_grad, solve_with_grad
     want_grad = needs_grad(terms, y0, args)
+    if want_grad and (saveat.dense or saveat.steps or event is not None):
+        raise NotImplementedError("gradients through SaveAt(steps=...), SaveAt(dense=True) "
+                                  "or events are not supported")
     low = Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
                   adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule,
-                  want_grad=want_grad)
-    interp = None
-    if saveat.dense or saveat.steps:
-        if want_grad:
-            raise NotImplementedError("gradients through SaveAt(steps=...) or "
-                                      "SaveAt(dense=True) are not supported")
-    if saveat.dense:
-        ys, ts_out, res, stats, interp = low.run_forward_dense()
+                  want_grad=want_grad, event=event)
+    interp = ev = None
+    if saveat.dense or event is not None:
+        ys, ts_out, res, stats, interp, ev = low.run_forward_ex()
     elif want_grad:
         ys, ts_out, res, stats = solve_with_grad(low, y0, args)
     else:
@@ -463,6 +505,9 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
                    stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],
                               num_rejected_steps=stats[:, 2], max_steps=max_steps),
                    result=res, interpolation=interp)
+    if event is not None:
+        masks = [ev == i for i in range(len(event._conds))]
+        sol.event_mask = masks[0] if event._single else masks
     # the lowered solve; after a backward pass under BacksolveAdjoint it holds
     # the backward's RESULTS codes and step counts (bwd_result, bwd_stats)
     sol.lowered = low

@@ -33,14 +33,21 @@ class ProblemDesc(_c.Structure):
         ("dtype", i32), ("kernel", i32), ("adjoint", i32), ("checkpoints", i32),
         ("block_threads", i32), ("ctas_per_sm", i32), ("mlp_precision", i32),
         ("save_steps", i32), ("save_dense", i32), ("n_step_ts", i32), ("n_jump_ts", i32),
-        ("pad3", i32),
+        ("n_event", i32), ("event_root", i32), ("ev_kind", i32 * 4), ("ev_dir", i32 * 4),
+        ("pad3", i32), ("newton_rtol", f64), ("newton_atol", f64), ("ev_coef", f64 * 24),
     ]
+
+
+class FwdExtras(_c.Structure):
+    """Mirror of gbdx_fwd_extras."""
+    _fields_ = [("dense_ts", vp), ("dense_info", vp), ("dense_n", vp), ("event_index", vp)]
 
 
 # The fields the oracle descriptor shares: the leading block (up to the
 # backsolve norm), the SaveAt(steps/dense) selectors and the clip counts.
 ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:29] + [
-    "save_steps", "save_dense", "n_step_ts", "n_jump_ts"]
+    "save_steps", "save_dense", "n_step_ts", "n_jump_ts", "n_event", "event_root", "ev_kind",
+    "ev_dir", "newton_rtol", "newton_atol", "ev_coef"]
 
 _lock = threading.Lock()
 _LIB = None
@@ -71,9 +78,10 @@ def load():
         lib.gbdx_solve_fwd.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, i64, vp, vp, vp,
                                        vp, vp, vp, vp, _c.c_size_t, vp]
         lib.gbdx_solve_fwd.restype = i32
-        lib.gbdx_solve_fwd_dense.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, i64, vp, vp,
-                                             vp, vp, vp, vp, vp, vp, vp, vp, _c.c_size_t, vp]
-        lib.gbdx_solve_fwd_dense.restype = i32
+        lib.gbdx_solve_fwd_ex.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, i64, vp, vp,
+                                          vp, vp, vp, vp, _c.POINTER(FwdExtras), vp,
+                                          _c.c_size_t, vp]
+        lib.gbdx_solve_fwd_ex.restype = i32
         lib.gbdx_dense_evaluate.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, vp, i64, vp, i64,
                                             i32, i32, vp, vp]
         lib.gbdx_dense_evaluate.restype = i32
@@ -114,6 +122,11 @@ def make_desc(fields: dict) -> ProblemDesc:
     for k, v in fields.items():
         if k == "mlp_widths":
             d.mlp_widths = (i32 * 9)(*([int(x) for x in v] + [0] * (9 - len(v))))
+        elif k in ("ev_kind", "ev_dir"):
+            setattr(d, k, (i32 * 4)(*([int(x) for x in v] + [0] * (4 - len(v)))))
+        elif k == "ev_coef":
+            v = [float(x) for x in v]
+            setattr(d, k, (f64 * 24)(*(v + [0.0] * (24 - len(v)))))
         elif k in ("dtmin", "dtmax") and v is None:
             setattr(d, k, math.nan)
         else:

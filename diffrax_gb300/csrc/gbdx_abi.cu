@@ -252,12 +252,31 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     return fail(GBDX_ERR_INVALID,
                 "Can only apply `ClipStepSizeController` to adaptive step size controllers.");
   }
-  const bool xo = d.save_steps > 0 || d.save_dense || clip;
+  if (d.n_event < 0 || d.n_event > GBDX_MAX_EVENTS) {
+    delete p;
+    return fail(GBDX_ERR_INVALID, "an event has 0 to %d conditions", GBDX_MAX_EVENTS);
+  }
+  for (int e = 0; e < d.n_event; e++) {
+    if (d.ev_kind[e] < GBDX_EV_LINEAR || d.ev_kind[e] > GBDX_EV_STEADY ||
+        d.ev_dir[e] < GBDX_EV_EITHER || d.ev_dir[e] > GBDX_EV_DOWN) {
+      delete p;
+      return fail(GBDX_ERR_INVALID, "unknown event condition kind or direction");
+    }
+    if (d.ev_kind[e] != GBDX_EV_STEADY && d.dim > 4) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED, "linear event conditions take a state of dim <= 4");
+    }
+  }
+  if (d.n_event > 0 && d.event_root && !(d.newton_rtol >= 0 && d.newton_atol > 0)) {
+    delete p;
+    return fail(GBDX_ERR_INVALID, "the root finder needs rtol >= 0 and atol > 0");
+  }
+  const bool xo = d.save_steps > 0 || d.save_dense || clip || d.n_event > 0;
   if (xo && (d.field == GBDX_MLP || sde || d.adjoint != GBDX_ADJ_NONE)) {
     delete p;
     return fail(GBDX_ERR_UNSUPPORTED,
-                "SaveAt(steps=...), SaveAt(dense=True) and ClipStepSizeController are "
-                "available for forward solves of the analytic ODE fields");
+                "SaveAt(steps=...), SaveAt(dense=True), ClipStepSizeController and events "
+                "are available for forward solves of the analytic ODE fields");
   }
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
                d.field == GBDX_ORNSTEIN_UHLENBECK)) {
@@ -441,6 +460,15 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
   P.n_jump_ts = d.n_jump_ts;
   P.step_ts = save_ts ? save_ts + d.n_ts : nullptr;
   P.jump_ts = save_ts ? save_ts + d.n_ts + d.n_step_ts : nullptr;
+  P.n_event = d.n_event;
+  P.event_root = d.event_root ? 1 : 0;
+  for (int e = 0; e < GBDX_MAX_EVENTS; e++) {
+    P.ev_kind[e] = d.ev_kind[e];
+    P.ev_dir[e] = d.ev_dir[e];
+  }
+  memcpy(P.ev_coef, d.ev_coef, sizeof P.ev_coef);
+  P.newton_rtol = d.newton_rtol;
+  P.newton_atol = d.newton_atol;
   P.controller = d.controller;
   P.rtol = d.rtol;
   P.atol = d.atol;
@@ -516,13 +544,16 @@ static int start_queue(const gbdx_problem *problem, gbdx::SolveParams &P, void *
 
 }  // extern "C"
 
-// The forward solve behind gbdx_solve_fwd and gbdx_solve_fwd_dense.
+// The forward solve behind gbdx_solve_fwd and gbdx_solve_fwd_ex.
 static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                      const double *t1, const double *dt0, int64_t time_stride, const void *y0,
                      const void *args, int64_t args_stride, const void *params,
                      const double *save_ts, void *ys_out, double *ts_out, int32_t *result_out,
-                     int32_t *stats_out, double *dense_ts, void *dense_info, int32_t *dense_n,
-                     void *workspace, size_t workspace_bytes, void *stream) {
+                     int32_t *stats_out, const gbdx_fwd_extras *ex, void *workspace,
+                     size_t workspace_bytes, void *stream) {
+  double *dense_ts = ex ? ex->dense_ts : nullptr;
+  void *dense_info = ex ? ex->dense_info : nullptr;
+  int32_t *dense_n = ex ? ex->dense_n : nullptr;
   const gbdx_problem_desc &d = problem->d;
   if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
   if (batch == 0) return GBDX_OK;
@@ -555,6 +586,7 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
     P.dense_info = dense_info;
     P.dense_n = dense_n;
   }
+  if (d.n_event > 0) P.event_index = ex ? ex->event_index : nullptr;
 
   gbdx::LaunchCfg cfg;
   cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;
@@ -603,29 +635,31 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    double *ts_out, int32_t *result_out, int32_t *stats_out,
                    void *workspace, size_t workspace_bytes, void *stream) {
   if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
-  if (problem->d.save_dense)
+  if (problem->d.save_dense || problem->d.n_event > 0)
     return fail(GBDX_ERR_INVALID,
-                "the problem saves the dense output: solve it with gbdx_solve_fwd_dense");
+                "the problem saves the dense output or has an event: solve it with "
+                "gbdx_solve_fwd_ex");
   return solve_fwd(problem, batch, t0, t1, dt0, time_stride, y0, args, args_stride, params,
-                   save_ts, ys_out, ts_out, result_out, stats_out, nullptr, nullptr, nullptr,
-                   workspace, workspace_bytes, stream);
+                   save_ts, ys_out, ts_out, result_out, stats_out, nullptr, workspace,
+                   workspace_bytes, stream);
 }
 
-int gbdx_solve_fwd_dense(const gbdx_problem *problem, int64_t batch, const double *t0,
-                         const double *t1, const double *dt0, int64_t time_stride,
-                         const void *y0, const void *args, int64_t args_stride,
-                         const void *params, const double *save_ts, void *ys_out,
-                         double *ts_out, int32_t *result_out, int32_t *stats_out,
-                         double *dense_ts, void *dense_info, int32_t *dense_n,
-                         void *workspace, size_t workspace_bytes, void *stream) {
+int gbdx_solve_fwd_ex(const gbdx_problem *problem, int64_t batch, const double *t0,
+                      const double *t1, const double *dt0, int64_t time_stride,
+                      const void *y0, const void *args, int64_t args_stride,
+                      const void *params, const double *save_ts, void *ys_out,
+                      double *ts_out, int32_t *result_out, int32_t *stats_out,
+                      const gbdx_fwd_extras *extras, void *workspace, size_t workspace_bytes,
+                      void *stream) {
   if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
-  if (!problem->d.save_dense)
-    return fail(GBDX_ERR_INVALID, "the problem was not created with SaveAt(dense=True)");
-  if (batch > 0 && (!dense_ts || !dense_info || !dense_n))
-    return fail(GBDX_ERR_INVALID, "null dense output pointer");
+  if (problem->d.save_dense && batch > 0 &&
+      (!extras || !extras->dense_ts || !extras->dense_info || !extras->dense_n))
+    return fail(GBDX_ERR_INVALID,
+                "the problem saves the dense output: dense_ts, dense_info and dense_n are "
+                "required");
   return solve_fwd(problem, batch, t0, t1, dt0, time_stride, y0, args, args_stride, params,
-                   save_ts, ys_out, ts_out, result_out, stats_out, dense_ts, dense_info,
-                   dense_n, workspace, workspace_bytes, stream);
+                   save_ts, ys_out, ts_out, result_out, stats_out, extras, workspace,
+                   workspace_bytes, stream);
 }
 
 int gbdx_dense_evaluate(const gbdx_problem *problem, int64_t batch, const double *t0,

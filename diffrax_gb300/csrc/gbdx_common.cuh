@@ -329,6 +329,12 @@ struct SolveParams {
   // extended-output kernels): caller-time times sorted increasing
   const double *step_ts, *jump_ts;
   int n_step_ts, n_jump_ts;
+  // Event (the extended-output kernels): conditions, root finder, output
+  int n_event, event_root;
+  int ev_kind[GBDX_MAX_EVENTS], ev_dir[GBDX_MAX_EVENTS];
+  double newton_rtol, newton_atol;
+  double ev_coef[6 * GBDX_MAX_EVENTS];
+  int32_t *event_index;       // [batch] condition that ended the solve, -1 none
 };
 
 // BacksolveAdjoint backward arguments.

@@ -37,37 +37,6 @@ cudaError_t fill_inf(T *p, int64_t n, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// d/dtheta of the Tsit5 dense-output weights b_j(theta) of tsit5_w (product
-// rule on the same factored polynomials).
-template <class T>
-__device__ __forceinline__ T tsit5_dw(int j, T t) {
-  auto quad = [](T c, T a, T e, T t) {  // c t^2 (t^2 - a t + e)
-    const T q = t * t - a * t + e;
-    return c * (T(2) * t * q + t * t * (T(2) * t - a));
-  };
-  auto cub = [](T c, T a, T b, T t) {  // c (t - a)(t - b) t^2
-    const T u = t - a, v = t - b;
-    return c * (v * t * t + u * t * t + T(2) * t * u * v);
-  };
-  switch (j) {
-    case 0: {  // c t (t - a)(t^2 - p t + q)
-      const T c = T(-1.0530884977290216), a = T(1.3299890189751412);
-      const T p = T(1.4364028541716351), q = T(0.7139816917074209);
-      const T g = t * t - p * t + q;
-      return c * ((t - a) * g + t * g + t * (t - a) * (T(2) * t - p));
-    }
-    case 1: return quad(T(0.1017), T(2.1966568338249754), T(1.2949852507374631), t);
-    case 2:
-      return quad(T(2.490627285651252793), T(2.38535645472061657), T(1.57803468208092486), t);
-    case 3:
-      return cub(T(-16.54810288924490272), T(1.21712927295533244), T(0.61620406037800089), t);
-    case 4:
-      return cub(T(47.37952196281928122), T(1.203071208372362603), T(0.658047292653547382), t);
-    case 5: return cub(T(-34.87065786149660974), T(1.2), T(0.666666666666666667), t);
-    default: return cub(T(2.5), T(1), T(0.6), t);
-  }
-}
-
 // Value (ORDER 0) or d/dtheta (ORDER 1) of the local interpolant of one step,
 // component n of the record r = (y0, y1, k_0 .. k_{S-1}).
 template <int SOLVER, class T>

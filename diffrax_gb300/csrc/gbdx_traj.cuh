@@ -48,6 +48,37 @@ __device__ __forceinline__ T tsit5_w(int j, T t) {
   }
 }
 
+// d/dtheta of the Tsit5 dense-output weights b_j(theta) of tsit5_w (product
+// rule on the same factored polynomials).
+template <class T>
+__device__ __forceinline__ T tsit5_dw(int j, T t) {
+  auto quad = [](T c, T a, T e, T t) {  // c t^2 (t^2 - a t + e)
+    const T q = t * t - a * t + e;
+    return c * (T(2) * t * q + t * t * (T(2) * t - a));
+  };
+  auto cub = [](T c, T a, T b, T t) {  // c (t - a)(t - b) t^2
+    const T u = t - a, v = t - b;
+    return c * (v * t * t + u * t * t + T(2) * t * u * v);
+  };
+  switch (j) {
+    case 0: {  // c t (t - a)(t^2 - p t + q)
+      const T c = T(-1.0530884977290216), a = T(1.3299890189751412);
+      const T p = T(1.4364028541716351), q = T(0.7139816917074209);
+      const T g = t * t - p * t + q;
+      return c * ((t - a) * g + t * g + t * (t - a) * (T(2) * t - p));
+    }
+    case 1: return quad(T(0.1017), T(2.1966568338249754), T(1.2949852507374631), t);
+    case 2:
+      return quad(T(2.490627285651252793), T(2.38535645472061657), T(1.57803468208092486), t);
+    case 3:
+      return cub(T(-16.54810288924490272), T(1.21712927295533244), T(0.61620406037800089), t);
+    case 4:
+      return cub(T(47.37952196281928122), T(1.203071208372362603), T(0.658047292653547382), t);
+    case 5: return cub(T(-34.87065786149660974), T(1.2), T(0.666666666666666667), t);
+    default: return cub(T(2.5), T(1), T(0.6), t);
+  }
+}
+
 // ClipStepSizeController (diffrax/_step_size_controller/clip.py) works in the
 // loop's direction-flipped time, where the caller's sorted times become
 // sort(ts * direction) (clip.py:203-213).  clip_get is the i-th of those, +inf
@@ -100,6 +131,11 @@ struct Traj {
   int first, dir, save_index, ts_index, nsteps, nacc, nrej, result;
   int sdown;  // XO: accepted steps left until the next SaveAt(steps=n) save
   int sidx, jidx;  // XO: ClipStepSizeController step / jump indices (hints)
+  // XO events: the conditions' last values, the condition that fired (-1
+  // none) and, with a root finder, the event time
+  double evv[GBDX_MAX_EVENTS];
+  int evi;
+  double tfin;
   int64_t idx;
   T wb[FIELD::SDE ? D : 1];  // SDE: W(tprev) of every component (FP32 fields only)
 
@@ -140,9 +176,12 @@ struct Traj {
     } else {
       double h = P.dt0[ti] * dir;
       sc = 1;
-      nc = (int)ceil((b - a) / next_up(h));
+      // an infinite t1 is marked by nc = -1: the grid keeps adding dt0
+      // (constant.py:48-55, 94-97)
+      const bool fin = isfinite(b);
+      nc = fin ? (int)ceil((b - a) / next_up(h)) : -1;
       t0s = a;
-      t1s = b;
+      t1s = fin ? b : h;
       tn = a + h;
     }
     tnext = fmin(tn, b);
@@ -186,7 +225,121 @@ struct Traj {
       // dense_ts[0] = t0 in the loop's time (_integrate.py:1315-1323); the
       // rest of the buffers was filled with +inf before the launch.
       if (P.dense_ts) P.dense_ts[i * (P.max_steps + 1)] = a;
+      // Event values at (t0, y0) (_integrate.py:1333-1426): a boolean
+      // condition that already holds ends the solve before its first step.
+      evi = -1;
+      tfin = a;
+      if (P.n_event > 0) {
+        T f[D];
+        FIELD::vf(P, args, y, f);
+        for (int e = 0; e < P.n_event; e++) {
+          evv[e] = ev_value(P, e, a, y, f);
+          if (evi < 0 && P.ev_kind[e] != GBDX_EV_LINEAR && evv[e] != 0.0) evi = e;
+        }
+        if (evi >= 0) result = GBDX_EVENT_OCCURRED;
+      }
     }
+  }
+
+  // Value of event condition e at the loop's time t and state yv, with f the
+  // field there (steady_state_event); booleans are 0 / 1 (_event.py:120-175).
+  __device__ double ev_value(const SolveParams &P, int e, double t, const T *yv,
+                             const T *f) const {
+    const double *c = P.ev_coef + 6 * e;
+    if (P.ev_kind[e] == GBDX_EV_STEADY) {
+      double sf = 0.0, sy = 0.0;
+#pragma unroll
+      for (int n = 0; n < D; n++) {
+        sf += double(f[n]) * double(f[n]);
+        sy += double(yv[n]) * double(yv[n]);
+      }
+      return sqrt(sf / D) < c[1] + c[0] * sqrt(sy / D) ? 1.0 : 0.0;
+    }
+    double v = 0.0;
+#pragma unroll
+    for (int n = 0; n < (D < 4 ? D : 4); n++) v += c[n] * double(yv[n]);
+    v += c[4] * t;
+    v += c[5];
+    if (P.ev_kind[e] == GBDX_EV_LINEAR_BOOL) return v > 0 ? 1.0 : 0.0;
+    return v;
+  }
+
+  // Whether condition e triggers between its values vo and vn: a boolean when
+  // it holds, a real value on the chosen sign change (_integrate.py:585-602).
+  __device__ static bool ev_trig(const SolveParams &P, int e, double vo, double vn) {
+    if (P.ev_kind[e] != GBDX_EV_LINEAR) return vn != 0.0;
+    const double so = isnan(vo) ? vo : double((vo > 0) - (vo < 0));
+    const double sn = isnan(vn) ? vn : double((vn > 0) - (vn < 0));
+    if (P.ev_dir[e] == GBDX_EV_UP) return so <= 0 && sn > 0;
+    if (P.ev_dir[e] == GBDX_EV_DOWN) return so > 0 && sn <= 0;
+    return so != sn;
+  }
+
+  // d/dtheta of the local interpolant inside the step, component n.
+  __device__ __forceinline__ T interp_d(T th, int n, const T (&k)[S][D], const T (&y1)[D]) const {
+    if constexpr (SOLVER == GBDX_TSIT5) {
+      T acc = T(0);
+#pragma unroll
+      for (int j = 0; j < 7; j++) acc += tsit5_dw<T>(j, th) * k[j < S ? j : 0][n];
+      return acc;
+    } else if constexpr (SOLVER == GBDX_DOPRI5) {
+      T cm = T(0);
+#pragma unroll
+      for (int j = 0; j < S; j++) cm += T(Tab<GBDX_DOPRI5>::cmid(j < 7 ? j : 0)) * k[j][n];
+      const T y0 = y[n], yy1 = y1[n], ymid = y0 + cm;
+      const T fa = k[0][n], fb = k[S - 1][n];
+      const T a = T(2) * (fb - fa) - T(8) * (yy1 + y0) + T(16) * ymid;
+      const T b = T(5) * fa - T(3) * fb + T(18) * y0 + T(14) * yy1 - T(32) * ymid;
+      const T c = fb - T(4) * fa - T(11) * y0 - T(5) * yy1 + T(16) * ymid;
+      return ((T(4) * a * th + T(3) * b) * th + T(2) * c) * th + fa;
+    } else if constexpr (SOLVER == GBDX_HEUN) {
+      const T y0 = y[n], yy1 = y1[n], ka = k[0][n], kb = k[S - 1][n];
+      const T a = ka + kb + T(2) * y0 - T(2) * yy1;
+      const T b = T(-2) * ka - kb - T(3) * y0 + T(3) * yy1;
+      return (T(3) * a * th + T(2) * b) * th + ka;
+    } else {
+      return y1[n] - y[n];
+    }
+  }
+
+  // The event's root find (_integrate.py:704-779): Newton's method (the
+  // restated optimistix.Newton with cauchy termination) on
+  // g(t) = w . interp(t) + wt t + c over the step [tp, tn] from t = tn, each
+  // iterate clipped to the step; it stops once the step was below
+  // atol + rtol |t| and |g| at the previous iterate below atol, from the
+  // second iteration on, or fails after 256 iterations.  A boolean condition's
+  // root is the end of the step.  y holds the step's y0.
+  __device__ double ev_root(const SolveParams &P, int e, const T (&k)[S][D], const T (&y1)[D],
+                            double tp, double tn, bool &ok) const {
+    ok = true;
+    if (P.ev_kind[e] != GBDX_EV_LINEAR) return tn;
+    const double *c = P.ev_coef + 6 * e;
+    const double span = tn - tp;
+    double t = tn;
+    for (int it = 1; it <= 256; it++) {
+      const T th = T(span == 0.0 ? 0.0 : (t - tp) / span);
+      double g = 0.0, gp = 0.0;
+#pragma unroll
+      for (int n = 0; n < (D < 4 ? D : 4); n++) {
+        g += c[n] * double(interp(th, n, k, y1));
+        gp += c[n] * (span == 0.0 ? 0.0 : double(interp_d(th, n, k, y1)) / span);
+      }
+      g += c[4] * t;
+      g += c[5];
+      gp += c[4];
+      const double diff = g / gp;
+      double nt = t - diff;
+      nt = fmax(fmin(nt, tn), tp);
+      if (isnan(nt)) {
+        ok = false;
+        return t;
+      }
+      const double size = fabs(diff) / (P.newton_atol + P.newton_rtol * fabs(nt));
+      t = nt;
+      if (it >= 2 && size < 1.0 && fabs(g) < P.newton_atol) return t;
+    }
+    ok = false;
+    return t;
   }
 
   // ClipStepSizeController.init (clip.py:215-276): the first step ends no
@@ -429,6 +582,7 @@ struct Traj {
       const int s2 = sc + 1;
       double tn = t0s + (t1s - t0s) * (double(s2) / double(nc));
       if (s2 == nc) tn = t1s;
+      if (nc < 0) tn = tnext + t1s;
       sc = s2;
       nt0 = tnext;
       nt1 = tn;
@@ -455,12 +609,52 @@ struct Traj {
     }
 
     if (keep) {
+      // Events at the new state (_integrate.py:542-633): the first condition
+      // (in order) that triggers ends the solve; with a root finder the final
+      // time is the root inside this step, and the saves after it are not
+      // made (the reference deletes them, :796-821).
+      double tsave = tnext;
+      T yfin[XO ? D : 1];
+      if constexpr (XO) {
+        if (P.n_event > 0) {
+          T fn[D];
+          if constexpr (TB::FSAL) {
+#pragma unroll
+            for (int n = 0; n < D; n++) fn[n] = flast[n];
+          } else {
+            bool steady = false;
+            for (int e = 0; e < P.n_event; e++) steady |= P.ev_kind[e] == GBDX_EV_STEADY;
+            if (steady) FIELD::vf(P, args, y1, fn);
+          }
+          int fired = -1;
+          for (int e = 0; e < P.n_event; e++) {
+            const double v = ev_value(P, e, tnext, y1, fn);
+            if (fired < 0 && ev_trig(P, e, evv[e], v)) fired = e;
+            evv[e] = v;
+          }
+          if (fired >= 0) {
+            evi = fired;
+            result = GBDX_EVENT_OCCURRED;
+            tfin = tnext;
+            if (P.event_root) {
+              bool ok = true;
+              tfin = ev_root(P, fired, k, y1, tprev, tnext, ok);
+              if (!ok) result = GBDX_NONLINEAR_MAX_STEPS;
+              const double span = tnext - tprev;
+              const T th = T(span == 0.0 ? 0.0 : (tfin - tprev) / span);
+#pragma unroll
+              for (int n = 0; n < D; n++) yfin[n] = interp(th, n, k, y1);
+              tsave = tfin;
+            }
+          }
+        }
+      }
       // SaveAt(ts): every ts <= tnext of the step just taken, interpolated
       // inside [tprev, tnext] (_integrate.py:456-487).
       while (ts_index < P.n_ts) {
         const double tsv = __ldg(P.save_ts + ts_index);
         const double tsd = dir > 0 ? tsv : -tsv;
-        if (order_key(tsd) > order_key(tnext)) break;  // save times are never NaN
+        if (order_key(tsd) > order_key(tsave)) break;  // save times are never NaN
         const double thd = (tprev == tnext) ? 0.0 : (tsd - tprev) / (tnext - tprev);
         const T th = T(thd);
         T *o = ys_row(P, save_index);
@@ -475,11 +669,13 @@ struct Traj {
         // step's ts saves (_integrate.py:492-527).
         if (P.save_steps > 0 && --sdown == 0) {
           sdown = P.save_steps;
-          T *o = ys_row(P, save_index);
+          if (order_key(tnext) <= order_key(tsave)) {  // not past an event's root
+            T *o = ys_row(P, save_index);
 #pragma unroll
-          for (int n = 0; n < D; n++) o[n] = y1[n];
-          P.ts_out[idx * P.n_save + save_index] = dir > 0 ? tnext : -tnext;
-          save_index++;
+            for (int n = 0; n < D; n++) o[n] = y1[n];
+            P.ts_out[idx * P.n_save + save_index] = dir > 0 ? tnext : -tnext;
+            save_index++;
+          }
         }
         // SaveAt(dense=True): the step's end time and (y0, y1, k_0..k_{S-1})
         // (_integrate.py:529-540).
@@ -500,6 +696,12 @@ struct Traj {
       }
 #pragma unroll
       for (int n = 0; n < D; n++) y[n] = y1[n];
+      if constexpr (XO) {
+        if (evi >= 0 && P.event_root) {
+#pragma unroll
+          for (int n = 0; n < D; n++) y[n] = yfin[n];
+        }
+      }
       if constexpr (FIELD::TAPE) {
         if (P.tape_t) {
           P.tape_t[idx * (P.max_steps + 1) + nacc + 1] = tnext;
@@ -577,13 +779,22 @@ struct Traj {
     // The t1 value is already saved when SaveAt(steps=n) saved the last step:
     // always for n = 1, for n > 1 when n divides the accepted steps
     // (_integrate.py:847-877).
-    bool t1_via_steps = false;
-    if constexpr (XO) t1_via_steps = P.save_steps > 0 && sdown == P.save_steps;
-    if (P.save_t1 && !t1_via_steps) {
+    // With an event root finder the final value is saved whenever the steps
+    // saved the t1 value, as that save fell after the event (:860-872); the
+    // final time is then the event's.
+    bool t1_via_steps = false, save_final = P.save_t1;
+    double tf = tprev;
+    if constexpr (XO) {
+      t1_via_steps = P.save_steps > 0 && sdown == P.save_steps;
+      const bool root = P.n_event > 0 && P.event_root;
+      save_final = root ? (P.save_t1 || t1_via_steps) : (P.save_t1 && !t1_via_steps);
+      if (root && evi >= 0) tf = tfin;
+    }
+    if (save_final) {
       T *o = ys_row(P, save_index);
 #pragma unroll
       for (int n = 0; n < D; n++) o[n] = y[n];
-      P.ts_out[idx * P.n_save + save_index] = tprev * dir;
+      P.ts_out[idx * P.n_save + save_index] = tf * dir;
       save_index++;
     }
     for (int m = save_index; m < P.n_save; m++) {
@@ -594,6 +805,7 @@ struct Traj {
     }
     if constexpr (XO) {
       if (P.dense_n) P.dense_n[idx] = nacc + 1;
+      if (P.event_index) P.event_index[idx] = evi;
     }
     int r = result;
     if (r == GBDX_SUCCESSFUL && tprev < t1) r = GBDX_MAX_STEPS_REACHED;  // :883

@@ -16,9 +16,10 @@
  *   gbdx_solve_fwd        <- jax.vmap(diffeqsolve) forward:
  *                            AbstractAdjoint.loop (diffrax/_adjoint.py:121-143)
  *                            driving loop() (diffrax/_integrate.py:302-885)
- *   gbdx_solve_fwd_dense  <- the same with SaveAt(dense=True): the dense_ts /
- *                            dense_infos buffers of loop()
- *                            (diffrax/_integrate.py:529-540, 1315-1323)
+ *   gbdx_solve_fwd_ex     <- the same with SaveAt(dense=True) (the dense_ts /
+ *                            dense_infos buffers of loop(),
+ *                            diffrax/_integrate.py:529-540, 1315-1323) and
+ *                            events (event_mask, diffrax/_integrate.py:542-821)
  *   gbdx_dense_evaluate   <- DenseInterpolation.evaluate / .derivative
  *                            (diffrax/_global_interpolation.py:315-393)
  *   gbdx_solve_bwd        <- the VJP of that solve under
@@ -72,8 +73,21 @@ enum gbdx_result {
   GBDX_DT_MIN_REACHED = 2,
   GBDX_EVENT_OCCURRED = 3,
   GBDX_MAX_STEPS_REJECTED = 4,
-  GBDX_INTERNAL_ERROR = 5
+  GBDX_INTERNAL_ERROR = 5,
+  GBDX_NONLINEAR_MAX_STEPS = 6 /* the event's root find did not converge */
 };
+
+/* Registered event conditions (diffrax/_event.py:13-175).  A condition is
+ * evaluated at the loop's time t (time runs forward: t * sign(t1 - t0), the
+ * time the reference hands to cond_fn) and state y:
+ *   LINEAR       value = sum_n w_n y_n + wt t + c  (real-valued; dim <= 4)
+ *   LINEAR_BOOL  value > 0 of the same form      (boolean)
+ *   STEADY       rms(f(t, y)) < atol + rtol rms(y) (steady_state_event)  */
+enum gbdx_event_kind { GBDX_EV_LINEAR = 0, GBDX_EV_LINEAR_BOOL = 1, GBDX_EV_STEADY = 2 };
+/* Event direction of a real-valued condition: either sign change, up-crossings
+ * only (direction=True), down-crossings only (direction=False). */
+enum gbdx_event_dir { GBDX_EV_EITHER = 0, GBDX_EV_UP = 1, GBDX_EV_DOWN = 2 };
+#define GBDX_MAX_EVENTS 4
 
 enum gbdx_status {
   GBDX_OK = 0,
@@ -110,14 +124,46 @@ typedef struct gbdx_problem_desc {
   int32_t mlp_precision; /* gbdx_mlp_precision of the MLP field's products */
   int32_t save_steps;    /* SaveAt(steps=n): save every n-th accepted step; 0 = off */
   int32_t save_dense;    /* SaveAt(dense=True): record the dense output (solve with
-                            gbdx_solve_fwd_dense) */
+                            gbdx_solve_fwd_ex) */
   /* ClipStepSizeController(PIDController(...), step_ts, jump_ts)
    * (diffrax/_step_size_controller/clip.py:120-427; store_rejected_steps is not
    * available): the numbers of step and jump times, passed after the n_ts
    * SaveAt times in the solve's save_ts array.  PID controller only. */
   int32_t n_step_ts, n_jump_ts;
+  /* Event(cond_fn=[...], root_finder, direction) (diffrax/_event.py:13-51,
+   * diffrax/_integrate.py:542-633, 686-877): n_event conditions (0 = none,
+   * at most GBDX_MAX_EVENTS) of kind ev_kind (gbdx_event_kind) and direction
+   * ev_dir (gbdx_event_dir).  Coefficients of condition i: LINEAR(_BOOL)
+   * ev_coef[6 i + n] = w_n (n < dim), [6 i + 4] = wt, [6 i + 5] = c; STEADY
+   * [6 i] = rtol, [6 i + 1] = atol.  event_root = 1 locates the event time by
+   * Newton's method (optimistix.Newton(newton_rtol, newton_atol)) on the last
+   * step's interpolant.  Forward solves of the analytic fields; solve with
+   * gbdx_solve_fwd_ex to read which condition fired. */
+  int32_t n_event, event_root;
+  int32_t ev_kind[GBDX_MAX_EVENTS], ev_dir[GBDX_MAX_EVENTS];
   int32_t pad3;
+  double newton_rtol, newton_atol;
+  double ev_coef[6 * GBDX_MAX_EVENTS];
 } gbdx_problem_desc;
+
+/* Optional outputs of gbdx_solve_fwd_ex (NULL where not wanted). */
+typedef struct gbdx_fwd_extras {
+  /* SaveAt(dense=True) (diffrax/_integrate.py:529-540, 1315-1323):
+   *   dense_ts   : device f64 [batch, max_steps + 1]: t0 then the end time of
+   *                every accepted step, in the loop's direction-flipped time
+   *                (t * sign(t1 - t0)); +inf where unused.
+   *   dense_info : device [batch, max_steps, (2 + stages) * dim] in desc.dtype:
+   *                per accepted step (y0, y1, k_0 .. k_{stages-1}), each dim
+   *                long, with k_j the stage increments f_j * control; +inf
+   *                where unused.  stages = 1 Euler, 2 Heun, 7 Dopri5 and Tsit5.
+   *   dense_n    : device int32 [batch]: accepted steps + 1. */
+  double *dense_ts;
+  void *dense_info;
+  int32_t *dense_n;
+  /* Event: device int32 [batch], the index of the condition that ended the
+   * solve (the reference's event_mask), -1 where none did. */
+  int32_t *event_index;
+} gbdx_fwd_extras;
 
 typedef struct gbdx_problem gbdx_problem;
 
@@ -210,27 +256,19 @@ int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double 
                        size_t workspace_bytes, void *stream);
 
 /*
- * Forward solve with SaveAt(dense=True) (the problem's save_dense set): the
- * arguments of gbdx_solve_fwd plus the dense output of every trajectory, as the
- * reference's loop records it (diffrax/_integrate.py:529-540, 1315-1323):
- *   dense_ts   : device f64 [batch, max_steps + 1]: t0 then the end time of every
- *                accepted step, in the direction-flipped time of the loop
- *                (time runs forward; t * sign(t1 - t0)); +inf where unused.
- *   dense_info : device [batch, max_steps, (2 + stages) * dim] in desc.dtype: per
- *                accepted step (y0, y1, k_0 .. k_{stages-1}), each dim long, with
- *                k_j the stage increments f_j * control; +inf where unused.
- *                stages = 1 Euler, 2 Heun, 7 Dopri5 and Tsit5.
- *   dense_n    : device int32 [batch]: accepted steps + 1 (entries of dense_ts).
- * With n_saves = 0 (SaveAt(dense=True) alone) ys_out and ts_out may be NULL.
- * Analytic fields only.
+ * Forward solve with the optional outputs of gbdx_fwd_extras: the arguments of
+ * gbdx_solve_fwd plus `extras`.  Problems with save_dense or events must be
+ * solved here (dense_ts, dense_info and dense_n are then required; event_index
+ * may be NULL).  With n_saves = 0 (SaveAt(dense=True) alone) ys_out and ts_out
+ * may be NULL.
  */
-int gbdx_solve_fwd_dense(const gbdx_problem *problem, int64_t batch, const double *t0,
-                         const double *t1, const double *dt0, int64_t time_stride,
-                         const void *y0, const void *args, int64_t args_stride,
-                         const void *params, const double *save_ts, void *ys_out,
-                         double *ts_out, int32_t *result_out, int32_t *stats_out,
-                         double *dense_ts, void *dense_info, int32_t *dense_n,
-                         void *workspace, size_t workspace_bytes, void *stream);
+int gbdx_solve_fwd_ex(const gbdx_problem *problem, int64_t batch, const double *t0,
+                      const double *t1, const double *dt0, int64_t time_stride,
+                      const void *y0, const void *args, int64_t args_stride,
+                      const void *params, const double *save_ts, void *ys_out,
+                      double *ts_out, int32_t *result_out, int32_t *stats_out,
+                      const gbdx_fwd_extras *extras, void *workspace,
+                      size_t workspace_bytes, void *stream);
 
 /*
  * DenseInterpolation.evaluate (order 0) and .derivative (order 1) of a dense
@@ -241,7 +279,7 @@ int gbdx_solve_fwd_dense(const gbdx_problem *problem, int64_t batch, const doubl
  * set of Q times shared by the batch; Q: Q times per trajectory).
  *   t0, t1, time_stride : the solve's (only the direction sign(t1 - t0) is read).
  *   y0                  : device [batch, dim], the solve's initial state.
- *   dense_ts, dense_info, dense_n : gbdx_solve_fwd_dense's outputs.
+ *   dense_ts, dense_info, dense_n : gbdx_solve_fwd_ex's dense outputs.
  *   left    : which side's step a query on a step boundary takes (1 = left).
  *   out     : device [batch, Q, dim] in desc.dtype; NaN outside [t0, t1].
  */

@@ -153,9 +153,9 @@ def test_saveat_steps_output_length(steps, t0, t1, n_ts, max_steps):
 
 
 def test_saveat_steps_dense_scope():
-    # forward solves of the analytic fields only; a dense problem is solved by
-    # gbdx_solve_fwd_dense and evaluated by gbdx_dense_evaluate (no kernel
-    # runs: the calls fail validation first)
+    # forward solves of the analytic fields only; a dense or event problem is
+    # solved by gbdx_solve_fwd_ex and evaluated by gbdx_dense_evaluate (no
+    # kernel runs: the calls fail validation first)
     with pytest.raises(_lib.GbdxError, match="analytic"):
         _lib.Problem(_fields(save_steps=1, adjoint=1, checkpoints=8))
     assert _lib.Problem(_fields(save_dense=1, save_t1=0)).n_save == 0
@@ -163,13 +163,48 @@ def test_saveat_steps_dense_scope():
     p = _lib.Problem(_fields(save_dense=1))
     z = [None] * 16
     assert lib.gbdx_solve_fwd(p.handle, 1, *z[:3], 0, *z[:2], 0, *z[:7], 0, None) == -1
-    assert "gbdx_solve_fwd_dense" in _lib.last_error()
-    q = _lib.Problem(_fields(save_steps=2))
-    assert lib.gbdx_solve_fwd_dense(q.handle, 1, *z[:3], 0, *z[:2], 0, *z[:10], 0, None) == -1
-    assert "dense" in _lib.last_error()
+    assert "gbdx_solve_fwd_ex" in _lib.last_error()
+    assert lib.gbdx_solve_fwd_ex(p.handle, 1, *z[:3], 0, *z[:2], 0, *z[:7], None, 0,
+                                 None) == -1
+    assert "dense_ts" in _lib.last_error()
     assert lib.gbdx_dense_evaluate(p.handle, 1, None, None, 0, None, None, None, None, 3,
                                    None, 5, 1, 0, None, None) == -1
     assert "query_stride" in _lib.last_error()
+    q = _lib.Problem(_fields(n_event=1, ev_kind=[0], ev_coef=[1, 0, 0, 0, 0, 0]))
+    assert lib.gbdx_solve_fwd(q.handle, 1, *z[:3], 0, *z[:2], 0, *z[:7], 0, None) == -1
+
+
+@pytest.mark.parametrize("bad, msg", [
+    (dict(n_event=5), "conditions"),
+    (dict(n_event=1, ev_kind=[7]), "kind"),
+    (dict(n_event=1, ev_dir=[3]), "direction"),
+    (dict(n_event=1, event_root=1, newton_atol=0.0), "root finder"),
+])
+def test_event_validation(bad, msg):
+    with pytest.raises(ValueError, match=msg):
+        _lib.Problem(_fields(**bad))
+
+
+def test_event_python_surface():
+    with pytest.raises(ValueError, match="Missmatch"):
+        dfx.Event([dfx.LinearCondition([1])], direction=[True, False])
+    with pytest.raises(NotImplementedError):
+        dfx.Event(lambda t, y, args, **kw: y)
+    ev = dfx.Event([dfx.LinearCondition([1, 0], offset=-1.0),
+                    dfx.LinearCondition([], t_coeff=1.0, offset=-3.0, boolean=True),
+                    dfx.steady_state_event()], dfx.Newton(1e-6, 1e-7), direction=True)
+    f = dfx.lower(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(),
+                  dfx.PIDController(rtol=1e-6, atol=1e-9), dfx.SaveAt(t1=True), dim=2,
+                  dtype=torch.float32, max_steps=64, n_ts=0, event=ev)
+    assert f["n_event"] == 3 and f["ev_kind"] == [0, 1, 2] and f["ev_dir"] == [1, 1, 1]
+    assert f["ev_coef"][:6] == [1.0, 0.0, 0.0, 0.0, 0.0, -1.0]
+    assert f["ev_coef"][12:14] == [1e-6, 1e-9] and f["event_root"] == 1
+    assert _lib.Problem(f).n_save == 1
+    # steady_state_event without an adaptive controller needs its tolerances
+    with pytest.raises(ValueError, match="steady_state_event"):
+        dfx.lower(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(), dfx.ConstantStepSize(),
+                  dfx.SaveAt(t1=True), dim=2, dtype=torch.float32, max_steps=64, n_ts=0,
+                  event=dfx.Event(dfx.steady_state_event()))
 
 
 def test_saveat_steps_dense_python_surface():
