@@ -5,7 +5,7 @@ executed by hand-written sm_103a kernels in libgbdx.so (see include/gbdx.h).
 """
 from ._core import (
     AbstractAdjoint, AbstractField, AbstractSolver, AbstractStepSizeController, AbstractTerm,
-    BacksolveAdjoint, ClipStepSizeController, ConstantStepSize, ControlTerm, Dopri5, Euler, Heun, LotkaVolterra,
+    BacksolveAdjoint, ClipStepSizeController, ConstantStepSize, ControlTerm, Dopri5, Dopri8, Euler, Heun, LotkaVolterra,
     MLPField, MultiTerm, ODETerm, OrnsteinUhlenbeck, TanhDiagonalDiffusion, PIDController, RecursiveCheckpointAdjoint,
     RESULTS, SaveAt, Solution, Tsit5, VanDerPol, VirtualBrownianTree, adjoint_rms_seminorm,
     rms_norm, Event, LinearCondition, Newton, SteadyStateCondition, steady_state_event,

@@ -218,6 +218,11 @@ class Tsit5(AbstractSolver):
     solver_id, _order = 3, 5
 
 
+class Dopri8(AbstractSolver):
+    """diffrax/_solver/dopri8.py:306-353 (analytic fields)."""
+    solver_id, _order = 4, 8
+
+
 # ---------------------------------------------------------------------------
 # Step size controllers.
 # ---------------------------------------------------------------------------

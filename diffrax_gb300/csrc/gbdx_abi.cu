@@ -182,6 +182,7 @@ static int solver_order(int solver) {
   switch (solver) {
     case GBDX_EULER: return 1;
     case GBDX_HEUN: return 2;
+    case GBDX_DOPRI8: return 8;
     default: return 5;
   }
 }
@@ -193,7 +194,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   if (!desc || !out) return fail(GBDX_ERR_INVALID, "null descriptor or output handle");
   *out = nullptr;
   const gbdx_problem_desc &d = *desc;
-  if (d.solver < GBDX_EULER || d.solver > GBDX_TSIT5)
+  if (d.solver < GBDX_EULER || d.solver > GBDX_DOPRI8)
     return fail(GBDX_ERR_INVALID, "unknown solver %d", d.solver);
   if (d.controller != GBDX_CONSTANT && d.controller != GBDX_PID)
     return fail(GBDX_ERR_INVALID, "unknown step size controller %d", d.controller);
@@ -293,6 +294,10 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     }
   } else if (d.field == GBDX_MLP) {
     const int *w = d.mlp_widths;
+    if (d.solver == GBDX_DOPRI8) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED, "Dopri8 is available for the analytic fields");
+    }
     if (d.mlp_depth != 3 || w[0] != d.dim || w[3] != d.dim || w[1] != w[2]) {
       delete p;
       return fail(GBDX_ERR_UNSUPPORTED,
@@ -573,7 +578,10 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
   if (d.save_dense) {
     // The reference's dense buffers start full of +inf (_integrate.py:1315-1323);
     // the solve overwrites the recorded steps.
-    const int stages = d.solver == GBDX_EULER ? 1 : d.solver == GBDX_HEUN ? 2 : 7;
+    const int stages = d.solver == GBDX_EULER    ? 1
+                       : d.solver == GBDX_HEUN   ? 2
+                       : d.solver == GBDX_DOPRI8 ? 14
+                                                 : 7;
     const int64_t rec = int64_t(2 + stages) * d.dim;
     cudaError_t e = gbdx::launch_fill_inf_f64(dense_ts, batch * (int64_t(d.max_steps) + 1), s);
     if (e == cudaSuccess) {

@@ -169,6 +169,69 @@ struct Tab<GBDX_EULER> {
   __host__ __device__ static constexpr double e(int) { return 0.0; }
 };
 
+
+// Dopri8 (dopri8.py:18-189): Prince and Dormand's 8(7) pair with 14 stages,
+// FSAL and SSAL (the last stage is evaluated at y1), and the Bogacki--Shampine
+// dense output y(theta) = y0 + sum_j theta P_j(theta) k_j (dopri8.py:192-303,
+// P_j of degree 5, highest power first).  Published method constants, written
+// as the exact rational quotients.
+template <>
+struct Tab<GBDX_DOPRI8> {
+  static constexpr int S = 14;
+  static constexpr bool FSAL = true, SSAL = true;
+  static constexpr int ORDER = 8;
+  static constexpr double STRONG_ORDER = 0.0;
+  __host__ __device__ static constexpr double c(int i) {
+    constexpr double v[14] = {0.0, (1.0 / 18.0), (1.0 / 12.0), (1.0 / 8.0), (5.0 / 16.0), (3.0 / 8.0), (59.0 / 400.0), (93.0 / 200.0), (5490023248.0 / 9719169821.0), (13.0 / 20.0), (1201146811.0 / 1299019798.0), 1.0, 1.0, 1.0};
+    return v[i];
+  }
+  __host__ __device__ static constexpr double a(int i, int j) {
+    constexpr double v[13][14] = {
+        {(1.0 / 18.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {(1.0 / 48.0), (1.0 / 16.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {(1.0 / 32.0), 0.0, (3.0 / 32.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {(5.0 / 16.0), 0.0, (-75.0 / 64.0), (75.0 / 64.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {(3.0 / 80.0), 0.0, 0.0, (3.0 / 16.0), (3.0 / 20.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {(29443841.0 / 614563906.0), 0.0, 0.0, (77736538.0 / 692538347.0), (-28693883.0 / 1125000000.0), (23124283.0 / 1800000000.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {(16016141.0 / 946692911.0), 0.0, 0.0, (61564180.0 / 158732637.0), (22789713.0 / 633445777.0), (545815736.0 / 2771057229.0), (-180193667.0 / 1043307555.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {(39632708.0 / 573591083.0), 0.0, 0.0, (-433636366.0 / 683701615.0), (-421739975.0 / 2616292301.0), (100302831.0 / 723423059.0), (790204164.0 / 839813087.0), (800635310.0 / 3783071287.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {(246121993.0 / 1340847787.0), 0.0, 0.0, (-37695042795.0 / 15268766246.0), (-309121744.0 / 1061227803.0), (-12992083.0 / 490766935.0), (6005943493.0 / 2108947869.0), (393006217.0 / 1396673457.0), (123872331.0 / 1001029789.0), 0.0, 0.0, 0.0, 0.0, 0.0},
+        {(-1028468189.0 / 846180014.0), 0.0, 0.0, (8478235783.0 / 508512852.0), (1311729495.0 / 1432422823.0), (-10304129995.0 / 1701304382.0), (-48777925059.0 / 3047939560.0), (15336726248.0 / 1032824649.0), (-45442868181.0 / 3398467696.0), (3065993473.0 / 597172653.0), 0.0, 0.0, 0.0, 0.0},
+        {(185892177.0 / 718116043.0), 0.0, 0.0, (-3185094517.0 / 667107341.0), (-477755414.0 / 1098053517.0), (-703635378.0 / 230739211.0), (5731566787.0 / 1027545527.0), (5232866602.0 / 850066563.0), (-4093664535.0 / 808688257.0), (3962137247.0 / 1805957418.0), (65686358.0 / 487910083.0), 0.0, 0.0, 0.0},
+        {(403863854.0 / 491063109.0), 0.0, 0.0, (-5068492393.0 / 434740067.0), (-411421997.0 / 543043805.0), (652783627.0 / 914296604.0), (11173962825.0 / 925320556.0), (-13158990841.0 / 6184727034.0), (3936647629.0 / 1978049680.0), (-160528059.0 / 685178525.0), (248638103.0 / 1413531060.0), 0.0, 0.0, 0.0},
+        {(14005451.0 / 335480064.0), 0.0, 0.0, 0.0, 0.0, (-59238493.0 / 1068277825.0), (181606767.0 / 758867731.0), (561292985.0 / 797845732.0), (-1041891430.0 / 1371343529.0), (760417239.0 / 1151165299.0), (118820643.0 / 751138087.0), (-528747749.0 / 2220607170.0), (1.0 / 4.0), 0.0},
+    };
+    return i == 0 ? 0.0 : v[i - 1][j];
+  }
+  __host__ __device__ static constexpr double b(int j) {
+    constexpr double v[14] = {(14005451.0 / 335480064.0), 0.0, 0.0, 0.0, 0.0, (-59238493.0 / 1068277825.0), (181606767.0 / 758867731.0), (561292985.0 / 797845732.0), (-1041891430.0 / 1371343529.0), (760417239.0 / 1151165299.0), (118820643.0 / 751138087.0), (-528747749.0 / 2220607170.0), (1.0 / 4.0), 0.0};
+    return v[j];
+  }
+  __host__ __device__ static constexpr double e(int j) {
+    constexpr double v[14] = {((14005451.0 / 335480064.0) - (13451932.0 / 455176623.0)), 0.0, 0.0, 0.0, 0.0, ((-59238493.0 / 1068277825.0) - (-808719846.0 / 976000145.0)), ((181606767.0 / 758867731.0) - (1757004468.0 / 5645159321.0)), ((561292985.0 / 797845732.0) - (656045339.0 / 265891186.0)), ((-1041891430.0 / 1371343529.0) - (-3867574721.0 / 1518517206.0)), ((760417239.0 / 1151165299.0) - (465885868.0 / 322736535.0)), ((118820643.0 / 751138087.0) - (53011238.0 / 667516719.0)), ((-528747749.0 / 2220607170.0) - (2.0 / 45.0)), (1.0 / 4.0), 0.0};
+    return v[j];
+  }
+  __host__ __device__ static constexpr double p(int j, int m) {
+    constexpr double v[14][6] = {
+        {-6.34483493928604, 22.139650499809406, -30.061056828966645, 19.999006933368396, -6.6910181737837595, 1.0},
+        {0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+        {-39.61079198522025, 116.44221495503422, -121.49996277313346, 52.227353279294555, -7.6142658045872675, 0.0},
+        {20.376121380879145, -67.14513188259572, 83.17210046398478, -46.89191641810936, 10.728139263042886, 0.0},
+        {7.334709882679536, -16.56722435274965, 9.572450755599366, -0.18908932250105956, 0.5526637063753649, 0.0},
+        {32.88017743524592, -89.9916014847245, 87.84060576772056, -35.70759759462221, 4.218656262566515, 0.0},
+        {-10.158899052642676, 22.623748964853284, -17.415210777076297, 6.273644808324035, -0.6627209125361597, 0.0},
+        {-12.540126809878256, 32.23623401673554, -28.590328951479098, 10.316088127245076, -1.2636789001135462, 0.0},
+        {29.555300148451604, -82.10203154883598, 81.66309505843414, -34.76507698666118, 5.410603789859042, 0.0},
+        {-41.79234864243906, 116.26621857911195, -114.93752913770093, 47.745797107822554, -7.032137906794574, 0.0},
+        {20.300692582210083, -53.90207774663854, 50.255836422617605, -19.008209934160803, 2.3537586759714983, 0.0},
+    };
+    return v[j][m];
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Precision helpers.
 // ---------------------------------------------------------------------------

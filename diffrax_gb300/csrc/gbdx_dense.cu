@@ -44,7 +44,12 @@ __device__ __forceinline__ T local_interp(const T *r, int D, int n, T th, int or
   constexpr int S = Tab<SOLVER>::S;
   const T y0 = r[n], y1 = r[D + n];
   auto k = [&](int j) { return r[(2 + j) * D + n]; };
-  if constexpr (SOLVER == GBDX_TSIT5) {
+  if constexpr (SOLVER == GBDX_DOPRI8) {
+    T acc = T(0);
+#pragma unroll
+    for (int j = 0; j < S; j++) acc += (order ? dopri8_dw<T>(j, th) : dopri8_w<T>(j, th)) * k(j);
+    return order ? acc : y0 + acc;
+  } else if constexpr (SOLVER == GBDX_TSIT5) {
     T acc = T(0);
 #pragma unroll
     for (int j = 0; j < 7; j++) acc += (order ? tsit5_dw<T>(j, th) : tsit5_w<T>(j, th)) * k(j);
@@ -137,6 +142,7 @@ cudaError_t dense_eval_t(int solver, const DenseEvalArgs &A, cudaStream_t s) {
     case GBDX_HEUN: dense_eval_kernel<GBDX_HEUN, T><<<blocks, 256, 0, s>>>(A); break;
     case GBDX_DOPRI5: dense_eval_kernel<GBDX_DOPRI5, T><<<blocks, 256, 0, s>>>(A); break;
     case GBDX_TSIT5: dense_eval_kernel<GBDX_TSIT5, T><<<blocks, 256, 0, s>>>(A); break;
+    case GBDX_DOPRI8: dense_eval_kernel<GBDX_DOPRI8, T><<<blocks, 256, 0, s>>>(A); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

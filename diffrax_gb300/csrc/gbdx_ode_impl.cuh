@@ -37,6 +37,7 @@ OdeEntry find_ode_entry_t(int solver, int field, int dim) {
     case GBDX_HEUN: return GBDX_ENTRY(GBDX_HEUN, F);           \
     case GBDX_DOPRI5: return GBDX_ENTRY(GBDX_DOPRI5, F);       \
     case GBDX_TSIT5: return GBDX_ENTRY(GBDX_TSIT5, F);         \
+    case GBDX_DOPRI8: return GBDX_ENTRY(GBDX_DOPRI8, F);       \
     default: return OdeEntry{nullptr, nullptr};                \
   }
   if (field == GBDX_LOTKA_VOLTERRA && dim == 2) { GBDX_SOLVERS(LotkaVolterra<T>) }

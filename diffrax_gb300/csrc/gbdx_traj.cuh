@@ -48,6 +48,25 @@ __device__ __forceinline__ T tsit5_w(int j, T t) {
   }
 }
 
+// Dopri8 dense-output weights theta P_j(theta) and their theta-derivative
+// P_j + theta P_j' (Tab<GBDX_DOPRI8>::p, dopri8.py:192-303).
+template <class T>
+__device__ __forceinline__ T dopri8_w(int j, T t) {
+  using TB = Tab<GBDX_DOPRI8>;
+  const T p = ((((T(TB::p(j, 0)) * t + T(TB::p(j, 1))) * t + T(TB::p(j, 2))) * t +
+                T(TB::p(j, 3))) * t + T(TB::p(j, 4))) * t + T(TB::p(j, 5));
+  return t * p;
+}
+template <class T>
+__device__ __forceinline__ T dopri8_dw(int j, T t) {
+  using TB = Tab<GBDX_DOPRI8>;
+  const T p = ((((T(TB::p(j, 0)) * t + T(TB::p(j, 1))) * t + T(TB::p(j, 2))) * t +
+                T(TB::p(j, 3))) * t + T(TB::p(j, 4))) * t + T(TB::p(j, 5));
+  const T dp = (((T(5 * TB::p(j, 0)) * t + T(4 * TB::p(j, 1))) * t + T(3 * TB::p(j, 2))) * t +
+                T(2 * TB::p(j, 3))) * t + T(TB::p(j, 4));
+  return p + t * dp;
+}
+
 // d/dtheta of the Tsit5 dense-output weights b_j(theta) of tsit5_w (product
 // rule on the same factored polynomials).
 template <class T>
@@ -277,7 +296,12 @@ struct Traj {
 
   // d/dtheta of the local interpolant inside the step, component n.
   __device__ __forceinline__ T interp_d(T th, int n, const T (&k)[S][D], const T (&y1)[D]) const {
-    if constexpr (SOLVER == GBDX_TSIT5) {
+    if constexpr (SOLVER == GBDX_DOPRI8) {
+      T acc = T(0);
+#pragma unroll
+      for (int j = 0; j < S; j++) acc += dopri8_dw<T>(j, th) * k[j][n];
+      return acc;
+    } else if constexpr (SOLVER == GBDX_TSIT5) {
       T acc = T(0);
 #pragma unroll
       for (int j = 0; j < 7; j++) acc += tsit5_dw<T>(j, th) * k[j < S ? j : 0][n];
@@ -737,7 +761,12 @@ struct Traj {
 
   // Dense output inside the step, component n.  y holds y0 of the step.
   __device__ __forceinline__ T interp(T th, int n, const T (&k)[S][D], const T (&y1)[D]) const {
-    if constexpr (SOLVER == GBDX_TSIT5) {
+    if constexpr (SOLVER == GBDX_DOPRI8) {
+      T acc = T(0);
+#pragma unroll
+      for (int j = 0; j < S; j++) acc += dopri8_w<T>(j, th) * k[j][n];
+      return y[n] + acc;
+    } else if constexpr (SOLVER == GBDX_TSIT5) {
       T acc = T(0);
 #pragma unroll
       for (int j = 0; j < 7; j++) acc += tsit5_w<T>(j, th) * k[j < S ? j : 0][n];

@@ -38,8 +38,15 @@
 extern "C" {
 #endif
 
-/* Solvers (diffrax/_solver/{euler,heun,dopri5,tsit5}.py). */
-enum gbdx_solver { GBDX_EULER = 0, GBDX_HEUN = 1, GBDX_DOPRI5 = 2, GBDX_TSIT5 = 3 };
+/* Solvers (diffrax/_solver/{euler,heun,dopri5,tsit5,dopri8}.py); Dopri8 on the
+ * analytic fields. */
+enum gbdx_solver {
+  GBDX_EULER = 0,
+  GBDX_HEUN = 1,
+  GBDX_DOPRI5 = 2,
+  GBDX_TSIT5 = 3,
+  GBDX_DOPRI8 = 4
+};
 /* Step size controllers (diffrax/_step_size_controller/{constant,pid}.py). */
 enum gbdx_controller { GBDX_CONSTANT = 0, GBDX_PID = 1 };
 /* Registered vector fields. */

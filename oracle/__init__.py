@@ -22,13 +22,13 @@ from .build import build_oracle, oracle_lib_path
 __all__ = [
     "OracleDesc", "load", "solve", "grad_recursive", "vbt_increments", "normal4",
     "dense_evaluate", "n_saves", "STAGES", "clip_times", "clip_find", "clip_adapt",
-    "EULER", "HEUN", "DOPRI5", "TSIT5", "CONSTANT", "PID",
+    "EULER", "HEUN", "DOPRI5", "TSIT5", "DOPRI8", "CONSTANT", "PID",
     "LOTKA_VOLTERRA", "VAN_DER_POL", "ORNSTEIN_UHLENBECK", "MLP", "LINEAR", "CALLBACK",
     "DIFF_NONE", "DIFF_OU", "DIFF_TANH_DIAG", "RESULT_NAMES", "EV_LINEAR", "EV_LINEAR_BOOL",
     "EV_STEADY", "EV_EITHER", "EV_UP", "EV_DOWN",
 ]
 
-EULER, HEUN, DOPRI5, TSIT5 = 0, 1, 2, 3
+EULER, HEUN, DOPRI5, TSIT5, DOPRI8 = 0, 1, 2, 3, 4
 CONSTANT, PID = 0, 1
 LOTKA_VOLTERRA, VAN_DER_POL, ORNSTEIN_UHLENBECK, MLP, LINEAR, CALLBACK = 0, 1, 2, 3, 4, 5
 DIFF_NONE, DIFF_OU, DIFF_TANH_DIAG = 0, 1, 2
@@ -75,7 +75,7 @@ _DEFAULTS = dict(solver=TSIT5, controller=PID, field=LOTKA_VOLTERRA, dim=2,
                  n_step_ts=0, n_jump_ts=0, n_event=0, event_root=0, ev_kind=(), ev_dir=(),
                  newton_rtol=1e-5, newton_atol=1e-5, ev_coef=())
 
-STAGES = {EULER: 1, HEUN: 2, DOPRI5: 7, TSIT5: 7}
+STAGES = {EULER: 1, HEUN: 2, DOPRI5: 7, TSIT5: 7, DOPRI8: 14}
 
 
 def n_saves(desc) -> int:

@@ -11,8 +11,8 @@
  *
  *   solve loop ............ diffrax/_integrate.py:302-885, 1036-1305
  *   explicit RK step ...... diffrax/_solver/runge_kutta.py:446-1203
- *   tableaus .............. diffrax/_solver/{tsit5,dopri5,heun,euler}.py
- *   interpolants .......... diffrax/_solver/tsit5.py:103-156,
+ *   tableaus .............. diffrax/_solver/{tsit5,dopri5,dopri8,heun,euler}.py
+ *   interpolants .......... diffrax/_solver/tsit5.py:103-156, dopri8.py:192-303,
  *                           diffrax/_local_interpolation.py:29-139
  *   PID controller ........ diffrax/_step_size_controller/pid.py:316-567
  *   constant step size .... diffrax/_step_size_controller/constant.py:20-104
@@ -41,7 +41,8 @@
 #include <omp.h>
 #endif
 
-enum { ORC_EULER = 0, ORC_HEUN = 1, ORC_DOPRI5 = 2, ORC_TSIT5 = 3 };
+enum { ORC_EULER = 0, ORC_HEUN = 1, ORC_DOPRI5 = 2, ORC_TSIT5 = 3, ORC_DOPRI8 = 4 };
+#define ORC_MAX_S 14 /* most stages of a tableau (Dopri8) */
 enum { ORC_CONSTANT = 0, ORC_PID = 1 };
 enum {
   ORC_LOTKA_VOLTERRA = 0,
@@ -114,13 +115,53 @@ typedef struct {
 typedef struct {
   int s;          /* stages */
   int fsal, ssal; /* runge_kutta.py:143-165 */
-  double a[7][7]; /* a[i][j], j < i */
-  double b[7], e[7], c[7];
+  double a[ORC_MAX_S][ORC_MAX_S]; /* a[i][j], j < i */
+  double b[ORC_MAX_S], e[ORC_MAX_S], c[ORC_MAX_S];
   int order;      /* ODE order; error_order for ODEs (base.py:97-120) */
   double strong_order;
 } Tableau;
 
-static Tableau TSIT5, DOPRI5, HEUN, EULER;
+static Tableau TSIT5, DOPRI5, DOPRI8, HEUN, EULER;
+/* Dopri8 (dopri8.py:18-189): Prince and Dormand's 8(7) pair, 14 stages,
+ * FSAL and SSAL; published method constants as exact rational quotients. */
+static const double DOPRI8_A[13][ORC_MAX_S] = {
+    {(1.0 / 18.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {(1.0 / 48.0), (1.0 / 16.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {(1.0 / 32.0), 0.0, (3.0 / 32.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {(5.0 / 16.0), 0.0, (-75.0 / 64.0), (75.0 / 64.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {(3.0 / 80.0), 0.0, 0.0, (3.0 / 16.0), (3.0 / 20.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {(29443841.0 / 614563906.0), 0.0, 0.0, (77736538.0 / 692538347.0), (-28693883.0 / 1125000000.0), (23124283.0 / 1800000000.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {(16016141.0 / 946692911.0), 0.0, 0.0, (61564180.0 / 158732637.0), (22789713.0 / 633445777.0), (545815736.0 / 2771057229.0), (-180193667.0 / 1043307555.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {(39632708.0 / 573591083.0), 0.0, 0.0, (-433636366.0 / 683701615.0), (-421739975.0 / 2616292301.0), (100302831.0 / 723423059.0), (790204164.0 / 839813087.0), (800635310.0 / 3783071287.0), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {(246121993.0 / 1340847787.0), 0.0, 0.0, (-37695042795.0 / 15268766246.0), (-309121744.0 / 1061227803.0), (-12992083.0 / 490766935.0), (6005943493.0 / 2108947869.0), (393006217.0 / 1396673457.0), (123872331.0 / 1001029789.0), 0.0, 0.0, 0.0, 0.0, 0.0},
+    {(-1028468189.0 / 846180014.0), 0.0, 0.0, (8478235783.0 / 508512852.0), (1311729495.0 / 1432422823.0), (-10304129995.0 / 1701304382.0), (-48777925059.0 / 3047939560.0), (15336726248.0 / 1032824649.0), (-45442868181.0 / 3398467696.0), (3065993473.0 / 597172653.0), 0.0, 0.0, 0.0, 0.0},
+    {(185892177.0 / 718116043.0), 0.0, 0.0, (-3185094517.0 / 667107341.0), (-477755414.0 / 1098053517.0), (-703635378.0 / 230739211.0), (5731566787.0 / 1027545527.0), (5232866602.0 / 850066563.0), (-4093664535.0 / 808688257.0), (3962137247.0 / 1805957418.0), (65686358.0 / 487910083.0), 0.0, 0.0, 0.0},
+    {(403863854.0 / 491063109.0), 0.0, 0.0, (-5068492393.0 / 434740067.0), (-411421997.0 / 543043805.0), (652783627.0 / 914296604.0), (11173962825.0 / 925320556.0), (-13158990841.0 / 6184727034.0), (3936647629.0 / 1978049680.0), (-160528059.0 / 685178525.0), (248638103.0 / 1413531060.0), 0.0, 0.0, 0.0},
+    {(14005451.0 / 335480064.0), 0.0, 0.0, 0.0, 0.0, (-59238493.0 / 1068277825.0), (181606767.0 / 758867731.0), (561292985.0 / 797845732.0), (-1041891430.0 / 1371343529.0), (760417239.0 / 1151165299.0), (118820643.0 / 751138087.0), (-528747749.0 / 2220607170.0), (1.0 / 4.0), 0.0},
+};
+static const double DOPRI8_B[ORC_MAX_S] = {(14005451.0 / 335480064.0), 0.0, 0.0, 0.0, 0.0, (-59238493.0 / 1068277825.0), (181606767.0 / 758867731.0), (561292985.0 / 797845732.0), (-1041891430.0 / 1371343529.0), (760417239.0 / 1151165299.0), (118820643.0 / 751138087.0), (-528747749.0 / 2220607170.0), (1.0 / 4.0), 0.0};
+static const double DOPRI8_E[ORC_MAX_S] = {((14005451.0 / 335480064.0) - (13451932.0 / 455176623.0)), 0.0, 0.0, 0.0, 0.0, ((-59238493.0 / 1068277825.0) - (-808719846.0 / 976000145.0)), ((181606767.0 / 758867731.0) - (1757004468.0 / 5645159321.0)), ((561292985.0 / 797845732.0) - (656045339.0 / 265891186.0)), ((-1041891430.0 / 1371343529.0) - (-3867574721.0 / 1518517206.0)), ((760417239.0 / 1151165299.0) - (465885868.0 / 322736535.0)), ((118820643.0 / 751138087.0) - (53011238.0 / 667516719.0)), ((-528747749.0 / 2220607170.0) - (2.0 / 45.0)), (1.0 / 4.0), 0.0};
+static const double DOPRI8_C[ORC_MAX_S] = {0.0, (1.0 / 18.0), (1.0 / 12.0), (1.0 / 8.0), (5.0 / 16.0), (3.0 / 8.0), (59.0 / 400.0), (93.0 / 200.0), (5490023248.0 / 9719169821.0), (13.0 / 20.0), (1201146811.0 / 1299019798.0), 1.0, 1.0, 1.0};
+/* Bogacki--Shampine dense output of Dopri8 (dopri8.py:192-303):
+ * y(theta) = y0 + sum_j theta * P_j(theta) k_j with P_j the degree-5
+ * polynomial of row j (highest power first). */
+static const double DOPRI8_P[ORC_MAX_S][6] = {
+    {-6.34483493928604, 22.139650499809406, -30.061056828966645, 19.999006933368396, -6.6910181737837595, 1.0},
+    {0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {-39.61079198522025, 116.44221495503422, -121.49996277313346, 52.227353279294555, -7.6142658045872675, 0.0},
+    {20.376121380879145, -67.14513188259572, 83.17210046398478, -46.89191641810936, 10.728139263042886, 0.0},
+    {7.334709882679536, -16.56722435274965, 9.572450755599366, -0.18908932250105956, 0.5526637063753649, 0.0},
+    {32.88017743524592, -89.9916014847245, 87.84060576772056, -35.70759759462221, 4.218656262566515, 0.0},
+    {-10.158899052642676, 22.623748964853284, -17.415210777076297, 6.273644808324035, -0.6627209125361597, 0.0},
+    {-12.540126809878256, 32.23623401673554, -28.590328951479098, 10.316088127245076, -1.2636789001135462, 0.0},
+    {29.555300148451604, -82.10203154883598, 81.66309505843414, -34.76507698666118, 5.410603789859042, 0.0},
+    {-41.79234864243906, 116.26621857911195, -114.93752913770093, 47.745797107822554, -7.032137906794574, 0.0},
+    {20.300692582210083, -53.90207774663854, 50.255836422617605, -19.008209934160803, 2.3537586759714983, 0.0},
+};
+
 
 static void init_tableaus(void) {
   static int done = 0;
@@ -189,6 +230,16 @@ static void init_tableaus(void) {
   DOPRI5.e[5] = 11.0 / 84 - 649.0 / 6300;
   DOPRI5.e[6] = -1.0 / 60.0;
 
+  memset(&DOPRI8, 0, sizeof DOPRI8);
+  DOPRI8.s = 14; DOPRI8.fsal = 1; DOPRI8.ssal = 1; DOPRI8.order = 8;
+  for (int i = 1; i < 14; i++)
+    for (int j = 0; j < i; j++) DOPRI8.a[i][j] = DOPRI8_A[i - 1][j];
+  for (int j = 0; j < 14; j++) {
+    DOPRI8.b[j] = DOPRI8_B[j];
+    DOPRI8.e[j] = DOPRI8_E[j];
+    DOPRI8.c[j] = DOPRI8_C[j];
+  }
+
   memset(&HEUN, 0, sizeof HEUN);
   HEUN.s = 2; HEUN.fsal = 0; HEUN.ssal = 0; HEUN.order = 2; HEUN.strong_order = 0.5;
   HEUN.c[1] = 1.0; HEUN.a[1][0] = 1.0;
@@ -204,6 +255,7 @@ static const Tableau *tableau_of(int solver) {
     case ORC_EULER: return &EULER;
     case ORC_HEUN: return &HEUN;
     case ORC_DOPRI5: return &DOPRI5;
+    case ORC_DOPRI8: return &DOPRI8;
     default: return &TSIT5;
   }
 }
@@ -533,8 +585,8 @@ static void field_diffusion_vjp(const Field *F, const double *y, const double *d
 /* ------------------------------------------------------------------------ */
 typedef struct {
   int dim;
-  double k[7][64];
-  double ystage[7][64];
+  double k[ORC_MAX_S][64];
+  double ystage[ORC_MAX_S][64];
   double y0[64], y1[64], err[64];
   double fsal_f[64];
   double dw[64];
@@ -616,15 +668,33 @@ static void tsit5_weights(double t, double w[7]) {
   w[6] = 2.5 * (t - 1) * (t - 0.6) * t * t;
 }
 
+/* Dopri8 dense-output weights theta P_j(theta), or their theta-derivative
+ * P_j + theta P_j' (deriv = 1). */
+static void dopri8_weights(double t, double w[ORC_MAX_S], int deriv) {
+  for (int j = 0; j < 14; j++) {
+    const double *c = DOPRI8_P[j];
+    double p = ((((c[0] * t + c[1]) * t + c[2]) * t + c[3]) * t + c[4]) * t + c[5];
+    if (deriv) {
+      double dp = (((5 * c[0] * t + 4 * c[1]) * t + 3 * c[2]) * t + 2 * c[3]) * t + c[4];
+      w[j] = p + t * dp;
+    } else {
+      w[j] = t * p;
+    }
+  }
+}
+
 /* Coefficients of the interpolant as a linear map of (y0, y1, k_j):
  * out = ay0 * y0 + ay1 * y1 + sum_j g[j] k_j.  Used by the VJP. */
 static void interp_linear_coeffs(int solver, int s, double th, double *ay0,
-                                 double *ay1, double g[7]) {
-  for (int j = 0; j < 7; j++) g[j] = 0.0;
+                                 double *ay1, double g[ORC_MAX_S]) {
+  for (int j = 0; j < ORC_MAX_S; j++) g[j] = 0.0;
   double t2 = th * th, t3 = t2 * th, t4 = t3 * th;
   switch (solver) {
     case ORC_TSIT5:
       *ay0 = 1.0; *ay1 = 0.0; tsit5_weights(th, g);
+      break;
+    case ORC_DOPRI8:
+      *ay0 = 1.0; *ay1 = 0.0; dopri8_weights(th, g, 0);
       break;
     case ORC_DOPRI5: {
       /* _local_interpolation.py:109-127 expanded in the monomials. */
@@ -659,6 +729,16 @@ static void interp_eval(int solver, const StepOut *so, int s, double t, double *
       for (int n = 0; n < D; n++) {
         double acc = 0.0;
         for (int j = 0; j < 7; j++) acc += w[j] * so->k[j][n];
+        out[n] = so->y0[n] + acc;
+      }
+      break;
+    }
+    case ORC_DOPRI8: {
+      double w[ORC_MAX_S];
+      dopri8_weights(th, w, 0);
+      for (int n = 0; n < D; n++) {
+        double acc = 0.0;
+        for (int j = 0; j < 14; j++) acc += w[j] * so->k[j][n];
         out[n] = so->y0[n] + acc;
       }
       break;
@@ -855,7 +935,7 @@ static double error_order_of(const orc_desc *d, const Tableau *tab) {
 /* ------------------------------------------------------------------------ */
 static void interp_eval(int solver, const StepOut *so, int s, double t, double *out);
 static void interp_deriv_coeffs(int solver, int s, double t, double *ay0, double *ay1,
-                                double g[7]);
+                                double g[ORC_MAX_S]);
 
 /* Value of condition i at the loop's time t (the direction-flipped time the
  * reference passes to cond_fn) and state y; booleans are 0 / 1. */
@@ -904,7 +984,7 @@ static double ev_root(const Field *F, const Tableau *tab, int i, const StepOut *
   const double lo = so->tprev, hi = so->tnext, span = hi - lo;
   double y = hi;
   for (int step = 1; step <= 256; step++) {
-    double yv[64], ay0, ay1, g[7];
+    double yv[64], ay0, ay1, g[ORC_MAX_S];
     interp_eval(d->solver, so, tab->s, y, yv);
     double f = 0.0;
     for (int n = 0; n < D; n++) f += c[n] * yv[n];
@@ -1270,10 +1350,14 @@ int orc_solve(const orc_desc *d, int64_t B, const double *t0, const double *t1,
 /* ------------------------------------------------------------------------ */
 /* d/dtheta of the interp_linear_coeffs coefficients. */
 static void interp_deriv_coeffs(int solver, int s, double t, double *ay0, double *ay1,
-                                double g[7]) {
-  for (int j = 0; j < 7; j++) g[j] = 0.0;
+                                double g[ORC_MAX_S]) {
+  for (int j = 0; j < ORC_MAX_S; j++) g[j] = 0.0;
   double t2 = t * t, t3 = t2 * t;
   switch (solver) {
+    case ORC_DOPRI8:
+      *ay0 = 0.0; *ay1 = 0.0;
+      dopri8_weights(t, g, 1);
+      break;
     case ORC_TSIT5: {
       /* product rule on the factored weights of tsit5_weights */
       double q, dq;
@@ -1368,12 +1452,12 @@ int orc_dense_evaluate(const orc_desc *d, int64_t B, const double *t0, const dou
       memcpy(so.y0, r, sizeof(double) * D);
       memcpy(so.y1, r + D, sizeof(double) * D);
       for (int j = 0; j < s; j++) memcpy(so.k[j], r + (2 + j) * D, sizeof(double) * D);
-      for (int j = s; j < 7; j++) memset(so.k[j], 0, sizeof(double) * D);
+      for (int j = s; j < ORC_MAX_S; j++) memset(so.k[j], 0, sizeof(double) * D);
       if (!order) {
         interp_eval(d->solver, &so, s, t, o);
       } else {
         /* d/dt = (d/dtheta) / (t1 - t0), back in the caller's direction */
-        double th = linear_rescale(so.tprev, t, so.tnext), ay0, ay1, g[7];
+        double th = linear_rescale(so.tprev, t, so.tnext), ay0, ay1, g[ORC_MAX_S];
         interp_deriv_coeffs(d->solver, s, th, &ay0, &ay1, g);
         const double span = so.tnext - so.tprev;
         for (int n = 0; n < D; n++) {
@@ -1426,14 +1510,14 @@ int orc_normal4(uint64_t seed, uint32_t traj, uint32_t node, uint32_t kind, uint
 /* recomputation schedule, not the values, so the oracle tapes every step.   */
 /* ------------------------------------------------------------------------ */
 static void step_vjp(const Field *F, const Tableau *tab, int dir, const StepOut *so,
-                     const double *gy1_in, double kbar[7][64], double *gy0,
+                     const double *gy1_in, double kbar[ORC_MAX_S][64], double *gy0,
                      double *gargs, double *gP) {
   const orc_desc *d = F->d;
   const int D = d->dim;
   const double control = dir * (so->tnext - so->tprev);
   double gy1[64];
   memcpy(gy1, gy1_in, sizeof(double) * D);
-  double ybar[7][64];
+  double ybar[ORC_MAX_S][64];
   memset(ybar, 0, sizeof ybar);
   if (tab->ssal) {
     for (int n = 0; n < D; n++) ybar[tab->s - 1][n] += gy1[n];
@@ -1518,7 +1602,7 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
         dwp = dw;
       }
       rk_step(&F, tab, tape.dir, st->tprev, st->tnext, ystart, 0, f0dummy, dwp, &so);
-      double kbar[7][64];
+      double kbar[ORC_MAX_S][64];
       memset(kbar, 0, sizeof kbar);
       double gy0[64], gy1[64];
       memset(gy0, 0, sizeof gy0);
@@ -1526,7 +1610,7 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
       for (int m = st->save_lo; m < st->save_hi; m++) {
         double tsv = ts_out[b * n_save + m] * tape.dir;
         double th = linear_rescale(st->tprev, tsv, st->tnext);
-        double ay0, ay1, g[7];
+        double ay0, ay1, g[ORC_MAX_S];
         interp_linear_coeffs(d->solver, tab->s, th, &ay0, &ay1, g);
         const double *go = gys + (int64_t)m * D;
         for (int n = 0; n < D; n++) {
@@ -1574,12 +1658,12 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
 /* ------------------------------------------------------------------------ */
 typedef struct {
   int64_t N;       /* augmented size 2D + n_args + n_params */
-  double *k[7], *zs, *z1, *err, *fsal, *f, *sc;
+  double *k[ORC_MAX_S], *zs, *z1, *err, *fsal, *f, *sc;
 } AugWork;
 
 static void aug_alloc(AugWork *w, int64_t N) {
   w->N = N;
-  for (int i = 0; i < 7; i++) w->k[i] = (double *)calloc((size_t)N, sizeof(double));
+  for (int i = 0; i < ORC_MAX_S; i++) w->k[i] = (double *)calloc((size_t)N, sizeof(double));
   w->zs = (double *)calloc((size_t)N, sizeof(double));
   w->z1 = (double *)calloc((size_t)N, sizeof(double));
   w->err = (double *)calloc((size_t)N, sizeof(double));
@@ -1589,7 +1673,7 @@ static void aug_alloc(AugWork *w, int64_t N) {
 }
 
 static void aug_free(AugWork *w) {
-  for (int i = 0; i < 7; i++) free(w->k[i]);
+  for (int i = 0; i < ORC_MAX_S; i++) free(w->k[i]);
   free(w->zs); free(w->z1); free(w->err); free(w->fsal); free(w->f); free(w->sc);
 }
 

@@ -17,8 +17,8 @@ import scipy.stats
 import oracle as O
 from conftest import tree_allclose
 
-SOLVERS = [O.EULER, O.HEUN, O.DOPRI5, O.TSIT5]
-ORDERS = {O.EULER: 1, O.HEUN: 2, O.DOPRI5: 5, O.TSIT5: 5}
+SOLVERS = [O.EULER, O.HEUN, O.DOPRI5, O.TSIT5, O.DOPRI8]
+ORDERS = {O.EULER: 1, O.HEUN: 2, O.DOPRI5: 5, O.TSIT5: 5, O.DOPRI8: 8}
 
 
 def _decay(**kw):
@@ -262,7 +262,7 @@ def _detest_problems():
 
 
 @pytest.mark.skipif(not os.path.exists(REF_DETEST), reason="reference tree absent")
-@pytest.mark.parametrize("solver", [O.HEUN, O.DOPRI5, O.TSIT5])
+@pytest.mark.parametrize("solver", [O.HEUN, O.DOPRI5, O.TSIT5, O.DOPRI8])
 def test_detest_against_scipy(solver):
     ns, names = _detest_problems()
     assert len(names) == 25
