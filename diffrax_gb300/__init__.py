@@ -11,6 +11,7 @@ from ._core import (
     rms_norm, Event, LinearCondition, Newton, SteadyStateCondition, steady_state_event,
 )
 from ._integrate import DenseInterpolation, diffeqsolve, lower, oracle_fields
+from ._tune import GraphedSolve, autotune_launch, tuned_shapes
 
 __version__ = "0.1.0"
 

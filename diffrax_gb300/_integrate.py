@@ -472,7 +472,8 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
                 max_steps: Optional[int] = 4096, throw: bool = True,
                 progress_meter: Any = None, solver_state=None, controller_state=None,
                 made_jump=None, kernel: str = "auto", block_threads: int = 0,
-                ctas_per_sm: int = 0, schedule: str = "auto") -> Solution:
+                ctas_per_sm: int = 0, schedule: str = "auto",
+                autotune: bool = False) -> Solution:
     """Batched diffrax.diffeqsolve on the GPU (diffrax/_integrate.py:888-1543).
 
     Extra keyword arguments select the GB300 execution policy: ``kernel`` is
@@ -480,7 +481,9 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     trajectory per thread); ``block_threads`` / ``ctas_per_sm`` override the
     autotuned launch shape of the fused kernel; ``schedule`` ("auto",
     "index", "longest_first") sets the order in which the fused kernel takes
-    trajectories (results do not depend on it).
+    trajectories (results do not depend on it); ``autotune=True`` times a few
+    launch shapes on this problem and batch the first time it is seen and
+    keeps the fastest (diffrax_gb300._tune).
     """
     if solver_state is not None or controller_state is not None or made_jump is not None:
         raise NotImplementedError("resuming from solver/controller state is not supported")
@@ -489,6 +492,14 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     if want_grad and (saveat.dense or saveat.steps or event is not None):
         raise NotImplementedError("gradients through SaveAt(steps=...), SaveAt(dense=True) "
                                   "or events are not supported")
+    if autotune and not want_grad and block_threads == 0 and ctas_per_sm == 0:
+        from ._tune import autotune_launch
+
+        def factory(bt, cps):
+            return Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
+                           adjoint, max_steps, kernel, bt, cps, schedule, event=event)
+        base = factory(0, 0)
+        block_threads, ctas_per_sm = autotune_launch(factory, base.B, base.fields)
     low = Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
                   adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule,
                   want_grad=want_grad, event=event)

@@ -1,0 +1,183 @@
+"""Launch-shape autotuner and CUDA-graph replay of repeated solves.
+
+The fused kernels take their launch shape from the problem descriptor
+(``block_threads``: trajectories per CTA of the analytic-field kernels;
+``ctas_per_sm``: resident CTAs, i.e. row tiles of the MLP kernels, per SM);
+0 selects the built-in heuristic.  ``autotune_launch`` times a small set of shapes
+on the actual problem and batch with CUDA events and keeps the fastest, per
+problem and batch size class, for the life of the process.  The analytic-field
+kernels give bit-identical results for every shape (every trajectory runs the
+same arithmetic in one thread); the MLP kernels sum each row's error norm with
+shared-memory atomics, whose order, and so the last bit of a norm, may change
+with the shape.
+
+``GraphedSolve`` captures one forward solve in a CUDA graph and replays it on
+new inputs of the same shapes, so a solve repeated inside a training or
+serving loop costs one graph launch.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+from ._core import RESULT_MESSAGES, RESULTS, SaveAt, Solution
+from ._integrate import Lowered, _raise_on_failure
+
+_LAUNCH_KEYS = ("block_threads", "ctas_per_sm")
+_TUNED: dict = {}
+
+
+def _key(fields: dict, batch: int):
+    """The problem minus its launch shape, and the batch's power-of-two class."""
+    items = []
+    for k, v in sorted(fields.items()):
+        if k in _LAUNCH_KEYS:
+            continue
+        items.append((k, tuple(v) if isinstance(v, (list, tuple)) else v))
+    return tuple(items), 1 << max(0, math.ceil(math.log2(max(batch, 1))))
+
+
+def candidates(fields: dict, batch: int) -> list:
+    """(block_threads, ctas_per_sm) shapes worth timing for this problem."""
+    if fields.get("field") == 3:  # MLP fields: 256 threads per CTA, one row tile each
+        return [(0, c) for c in (1, 2, 3, 4)]
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    out = [(0, 0)]
+    for block in (32, 64, 128, 256):
+        for per_sm in (1, 2, 4, 8, 16, 32):
+            lanes = block * per_sm * sms
+            if lanes > 2 * batch or block * per_sm > 2048:
+                continue
+            out.append((block, per_sm))
+    return out
+
+
+def autotune_launch(low_factory, batch: int, fields: dict, reps: int = 3,
+                    verbose: bool = False):
+    """Time every candidate launch shape of the problem and return the fastest
+    (block_threads, ctas_per_sm); cached per problem and batch class.
+
+    ``low_factory(block_threads, ctas_per_sm)`` builds the Lowered solve."""
+    key = _key(fields, batch)
+    hit = _TUNED.get(key)
+    if hit is not None:
+        return hit
+    best, best_ms = (0, 0), math.inf
+    stream = torch.cuda.current_stream()
+    for shape in candidates(fields, batch):
+        low = low_factory(*shape)
+        low.run_forward()  # warm-up (and first-use set-up)
+        ms = math.inf
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            low.run_forward()
+            e1.record(stream)
+            e1.synchronize()
+            ms = min(ms, e0.elapsed_time(e1))
+        if verbose:
+            print(f"autotune {shape}: {ms:.4f} ms")
+        if ms < best_ms:
+            best, best_ms = shape, ms
+    _TUNED[key] = best
+    return best
+
+
+def tuned_shapes() -> dict:
+    """The shapes chosen so far (problem key -> (block_threads, ctas_per_sm))."""
+    return dict(_TUNED)
+
+
+class GraphedSolve:
+    """A forward solve captured once as a CUDA graph and replayed on new inputs.
+
+    The constructor takes the arguments of ``diffeqsolve`` (forward solves: no
+    gradient); ``y0``, ``args`` and per-trajectory ``t0`` / ``t1`` / ``dt0``
+    fix the shapes.  ``__call__(y0=None, args=None, t0=None, t1=None,
+    dt0=None)`` copies the given inputs into the captured buffers, replays the
+    graph and returns a Solution whose tensors are the graph's output buffers:
+    the next call overwrites them (clone what must be kept).  ``autotune=True``
+    picks the launch shape before capture.
+    """
+
+    def __init__(self, terms, solver, t0, t1, dt0, y0, args=None, *,
+                 saveat: SaveAt = SaveAt(t1=True), stepsize_controller=None,
+                 max_steps: int = 4096, throw: bool = True, kernel: str = "auto",
+                 schedule: str = "auto", autotune: bool = False, event=None):
+        from ._core import ConstantStepSize
+        if stepsize_controller is None:
+            stepsize_controller = ConstantStepSize()
+        if saveat.dense:
+            raise NotImplementedError("GraphedSolve replays solves without dense output")
+        dev = torch.device("cuda", torch.cuda.current_device())
+
+        def own(x, dtype=None):
+            if x is None:
+                return None
+            t = torch.as_tensor(x)
+            t = t.to(device=dev, dtype=dtype or t.dtype)
+            return t.clone().contiguous()  # the graph reads these buffers
+
+        y0 = own(y0)
+        if y0.dtype not in (torch.float32, torch.float64):
+            y0 = y0.to(torch.float64)
+        t0 = own(t0, torch.float64) if isinstance(t0, torch.Tensor) else t0
+        t1 = own(t1, torch.float64) if isinstance(t1, torch.Tensor) else t1
+        dt0 = own(dt0, torch.float64) if isinstance(dt0, torch.Tensor) else dt0
+        args = own(args, y0.dtype)
+        self.throw, self.max_steps = throw, max_steps
+
+        def factory(block_threads, ctas_per_sm):
+            return Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
+                           None, max_steps, kernel, block_threads, ctas_per_sm, schedule,
+                           event=event)
+
+        shape = (0, 0)
+        if autotune:
+            base = factory(0, 0)
+            shape = autotune_launch(factory, base.B, base.fields)
+        self.shape = shape
+        low = factory(*shape)
+        self.low = low
+        self._event = event
+        run = low.run_forward_ex if event is not None else low.run_forward
+        run()  # warm-up outside the capture (first-use set-up of the library)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._outs = run()
+        torch.cuda.synchronize()
+
+    def _copy_in(self, name, value):
+        dst = getattr(self.low, name)
+        if dst is None:
+            raise ValueError(f"the captured solve has no {name} input")
+        src = torch.as_tensor(value).to(device=dst.device, dtype=dst.dtype)
+        if src.numel() != dst.numel():
+            raise ValueError(f"{name} must keep the captured shape {tuple(dst.shape)}")
+        dst.copy_(src.reshape(dst.shape))
+
+    def __call__(self, y0=None, args=None, t0=None, t1=None, dt0=None) -> Solution:
+        for name, v in (("y0", y0), ("args", args), ("t0", t0), ("t1", t1), ("dt0", dt0)):
+            if v is not None:
+                self._copy_in(name, v)
+        self.graph.replay()
+        outs = self._outs
+        ys, ts, res, stats = outs[:4]
+        sol = Solution(t0=self.low.t0, t1=self.low.t1, ts=ts, ys=ys,
+                       stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],
+                                  num_rejected_steps=stats[:, 2], max_steps=self.max_steps),
+                       result=res)
+        if self._event is not None:
+            ev = outs[5]
+            masks = [ev == i for i in range(len(self._event._conds))]
+            sol.event_mask = masks[0] if self._event._single else masks
+        if self.throw:
+            _raise_on_failure(res)
+        return sol
+
+
+__all__ = ["autotune_launch", "candidates", "tuned_shapes", "GraphedSolve", "RESULTS",
+           "RESULT_MESSAGES"]

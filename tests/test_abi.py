@@ -219,3 +219,13 @@ def test_saveat_steps_dense_python_surface():
     sol = dfx.Solution(t0=0.0, t1=1.0, ts=None, ys=None, stats={}, result=None)
     with pytest.raises(ValueError, match="dense=True"):
         sol.evaluate(0.5)
+
+
+def test_autotune_cache_key_ignores_launch_shape():
+    from diffrax_gb300 import _tune
+    f = _fields()
+    k1 = _tune._key(dict(f, block_threads=64, ctas_per_sm=2), 5000)
+    k2 = _tune._key(dict(f, block_threads=0, ctas_per_sm=0), 8000)
+    assert k1 == k2 and k1[1] == 8192
+    assert _tune._key(f, 9000) != k2
+    assert _tune.candidates(dict(f, field=3), 1024) == [(0, 1), (0, 2), (0, 3), (0, 4)]
