@@ -292,6 +292,19 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       return fail(GBDX_ERR_UNSUPPORTED, "no kernel for field %d with state dimension %d",
                   d.field, d.dim);
     }
+  } else if (sde && d.field == GBDX_ORNSTEIN_UHLENBECK && d.diffusion == GBDX_DIFF_OU) {
+    if (d.dtype != GBDX_F32) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED,
+                  "the Ornstein-Uhlenbeck SDE runs with FP32 state (FP32 Brownian tree)");
+    }
+    p->ode = gbdx::find_ode_sde_entry_f32(d.solver, d.dim);
+    if (!p->ode.launch) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED,
+                  "no SDE kernel for state dimension %d (the Ornstein-Uhlenbeck SDE takes "
+                  "dim 2 or 4) or solver %d", d.dim, d.solver);
+    }
   } else if (d.field == GBDX_MLP) {
     const int *w = d.mlp_widths;
     if (d.solver == GBDX_DOPRI8) {

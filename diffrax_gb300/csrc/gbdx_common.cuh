@@ -343,6 +343,21 @@ struct OrnsteinUhlenbeck {
   }
 };
 
+// Ornstein-Uhlenbeck SDE: the drift above with the diagonal diffusion sigma of
+// a ControlTerm driven by the virtual Brownian tree (dy = theta (mu - y) dt +
+// sigma dW, _term.py:271-555 with a diagonal operator).  Brownian values come
+// in pairs of components, so D is even.
+template <class T, int D_>
+struct OrnsteinUhlenbeckSDE : OrnsteinUhlenbeck<T, D_> {
+  static_assert(D_ % 2 == 0, "the Brownian tree draws components in pairs");
+  static constexpr bool SDE = true;
+  __device__ static __forceinline__ void sigma(const SolveParams &, const T *a, const T *,
+                                               T *s) {
+#pragma unroll
+    for (int i = 0; i < D_; i++) s[i] = a[2];
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Kernel parameters shared by every analytic-field launch.
 // ---------------------------------------------------------------------------

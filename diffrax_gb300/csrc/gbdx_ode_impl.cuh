@@ -55,4 +55,25 @@ OdeEntry find_ode_entry_t(int solver, int field, int dim) {
   return OdeEntry{nullptr, nullptr};
 }
 
+// The Ornstein-Uhlenbeck SDE (FP32 state: the tree's values are FP32).
+inline OdeEntry find_ode_sde_entry_t(int solver, int dim) {
+#define GBDX_ENTRY(S, F) \
+  OdeEntry { &launch_ode<S, F, float, false>, &occupancy_ode<S, F, float, false> }
+#define GBDX_SOLVERS(F)                                        \
+  switch (solver) {                                            \
+    case GBDX_EULER: return GBDX_ENTRY(GBDX_EULER, F);         \
+    case GBDX_HEUN: return GBDX_ENTRY(GBDX_HEUN, F);           \
+    case GBDX_DOPRI5: return GBDX_ENTRY(GBDX_DOPRI5, F);       \
+    case GBDX_TSIT5: return GBDX_ENTRY(GBDX_TSIT5, F);         \
+    default: return OdeEntry{nullptr, nullptr};                \
+  }
+  using OU2 = OrnsteinUhlenbeckSDE<float, 2>;
+  using OU4 = OrnsteinUhlenbeckSDE<float, 4>;
+  if (dim == 2) { GBDX_SOLVERS(OU2) }
+  if (dim == 4) { GBDX_SOLVERS(OU4) }
+#undef GBDX_SOLVERS
+#undef GBDX_ENTRY
+  return OdeEntry{nullptr, nullptr};
+}
+
 }  // namespace gbdx

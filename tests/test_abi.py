@@ -229,3 +229,21 @@ def test_autotune_cache_key_ignores_launch_shape():
     assert k1 == k2 and k1[1] == 8192
     assert _tune._key(f, 9000) != k2
     assert _tune.candidates(dict(f, field=3), 1024) == [(0, 1), (0, 2), (0, 3), (0, 4)]
+
+
+def test_ou_sde_scope():
+    # the Ornstein-Uhlenbeck SDE runs on the analytic kernels in FP32 state
+    # with an even state dimension (the tree draws component pairs)
+    bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (2,), key=0)
+    terms = dfx.MultiTerm(dfx.ODETerm(dfx.OrnsteinUhlenbeck()),
+                          dfx.ControlTerm(dfx.OrnsteinUhlenbeck(), bm))
+
+    def fields(dim, dtype):
+        return dfx.lower(terms, dfx.Heun(), dfx.ConstantStepSize(), dfx.SaveAt(t1=True),
+                         dim=dim, dtype=dtype, max_steps=100, n_ts=0)
+    assert _lib.Problem(fields(2, torch.float32)).n_save == 1
+    assert _lib.Problem(fields(4, torch.float32)).n_save == 1
+    with pytest.raises(_lib.GbdxError, match="FP32"):
+        _lib.Problem(fields(2, torch.float64))
+    with pytest.raises(_lib.GbdxError, match="dim 2 or 4"):
+        _lib.Problem(fields(3, torch.float32))
