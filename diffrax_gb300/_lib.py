@@ -85,6 +85,8 @@ def load():
         lib.gbdx_dense_evaluate.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, vp, i64, vp, i64,
                                             i32, i32, vp, vp]
         lib.gbdx_dense_evaluate.restype = i32
+        lib.gbdx_selftest_tcgen05.argtypes = [vp, vp, vp, vp, vp]
+        lib.gbdx_selftest_tcgen05.restype = i32
         lib.gbdx_solve_bwd.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, i64, vp, vp, vp, vp,
                                        vp, vp, _c.c_size_t, vp]
         lib.gbdx_solve_bwd.restype = i32

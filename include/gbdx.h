@@ -318,6 +318,16 @@ int gbdx_solve_fwd_noalloc(const gbdx_problem *problem, int64_t batch, const dou
                            double *ts_out, int32_t *result_out, int32_t *stats_out,
                            void *stream);
 
+/*
+ * Diagnostic of the fifth-generation tensor-core path on the current GPU (no
+ * counterpart in the reference): one CTA computes D = A B^T for A, B device
+ * FP32 [128, 64] rounded to BF16, with tcgen05.mma (operands in shared memory,
+ * FP32 accumulator in tensor memory), into D device FP32 [128, 128];
+ * status (device int32) is 0, or 1 if the products did not complete.
+ */
+int gbdx_selftest_tcgen05(const float *A, const float *B, float *D, int32_t *status,
+                          void *stream);
+
 /* Number of parameters of the MLP / linear field plus diffusion, in the flat
  * layout [W_0 (out x in, row-major), b_0, W_1, b_1, ..., W_sigma, b_sigma]. */
 int64_t gbdx_param_count(const gbdx_problem *problem);
