@@ -22,7 +22,7 @@ from ._core import (
     RecursiveCheckpointAdjoint, SaveAt, Solution, VirtualBrownianTree, adjoint_rms_seminorm,
 )
 
-KERNELS = {"auto": 0, "plain": 1, "fused": 2}
+KERNELS = {"auto": 0, "plain": 1, "fused": 2, "tc": 3}
 SCHEDULES = {"auto": 0, "index": 1, "longest_first": 2}
 
 
@@ -477,8 +477,8 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     """Batched diffrax.diffeqsolve on the GPU (diffrax/_integrate.py:888-1543).
 
     Extra keyword arguments select the GB300 execution policy: ``kernel`` is
-    "fused" (persistent work-stealing integrator, the default) or "plain" (one
-    trajectory per thread); ``block_threads`` / ``ctas_per_sm`` override the
+    "fused" (persistent work-stealing integrator, the default), "plain" (one
+    trajectory per thread) or "tc" (MLP-field forward on tcgen05 tensor cores); ``block_threads`` / ``ctas_per_sm`` override the
     autotuned launch shape of the fused kernel; ``schedule`` ("auto",
     "index", "longest_first") sets the order in which the fused kernel takes
     trajectories (results do not depend on it); ``autotune=True`` times a few

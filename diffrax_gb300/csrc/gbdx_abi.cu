@@ -51,8 +51,9 @@ struct gbdx_problem {
   gbdx::OdeEntry ode;
   gbdx::BwdEntry bwd;  // RecursiveCheckpointAdjoint backward (MLP fields)
   gbdx::BsEntry bs;    // BacksolveAdjoint backward (MLP fields)
-  bool mlp;            // MLP-field row-tile integrator (256 threads per CTA)
+  bool mlp;            // MLP-field row-tile integrator
   int rows_per_cta;
+  int mlp_block;       // threads per CTA of the MLP integrator
 };
 
 namespace {
@@ -201,6 +202,10 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   if (d.dtype != GBDX_F32 && d.dtype != GBDX_F64)
     return fail(GBDX_ERR_INVALID, "unknown dtype %d", d.dtype);
   if (d.dim < 1) return fail(GBDX_ERR_INVALID, "state dimension must be positive");
+  if (d.kernel < GBDX_KERNEL_AUTO || d.kernel > GBDX_KERNEL_TC)
+    return fail(GBDX_ERR_INVALID, "unknown kernel family %d", d.kernel);
+  if (d.kernel == GBDX_KERNEL_TC && d.field != GBDX_MLP)
+    return fail(GBDX_ERR_UNSUPPORTED, "the tensor-core (TC) kernel integrates MLP fields");
   if (d.max_steps < 1) return fail(GBDX_ERR_INVALID, "max_steps must be a positive integer");
   if (d.n_ts < 0) return fail(GBDX_ERR_INVALID, "negative number of SaveAt(ts=...) points");
   if (d.save_steps < 0) return fail(GBDX_ERR_INVALID, "SaveAt(steps=n) needs n >= 0");
@@ -242,6 +247,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   p->bs = gbdx::BsEntry{nullptr, nullptr, 0, 0, 0, 0};
   p->mlp = false;
   p->rows_per_cta = 1;
+  p->mlp_block = 256;
   if (d.n_step_ts < 0 || d.n_jump_ts < 0) {
     delete p;
     return fail(GBDX_ERR_INVALID, "negative number of step_ts or jump_ts");
@@ -327,6 +333,27 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     }
     const bool precise = d.mlp_precision == GBDX_MLP_FP32;
     const int D = d.dim, H = w[1];
+    if (d.kernel == GBDX_KERNEL_TC) {
+      // the tcgen05 forward: BF16 products, no gradient tape
+      if (precise || d.adjoint != GBDX_ADJ_NONE) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED,
+                    "the tensor-core (TC) kernel runs BF16 forward solves without an adjoint");
+      }
+      p->ode = gbdx::find_mlp_tc_entry(d.solver, D, H, sde);
+      if (!p->ode.launch) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED,
+                    "the tensor-core (TC) kernel takes 64 -> 128 -> 128 -> 64 ODE fields with "
+                    "Tsit5 (got dim %d, width %d, solver %d%s)", D, H, d.solver,
+                    sde ? ", SDE" : "");
+      }
+      p->mlp = true;
+      p->rows_per_cta = 128;
+      p->mlp_block = 256;
+      *out = p;
+      return GBDX_OK;
+    }
     if (d.kernel == GBDX_KERNEL_PLAIN) {
       // The plain form: one trajectory per thread, FP32 CUDA-core products.
       if (d.adjoint == GBDX_ADJ_BACKSOLVE) {
@@ -611,7 +638,7 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
 
   gbdx::LaunchCfg cfg;
   cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;
-  cfg.block = problem->mlp ? 256 : (d.block_threads > 0 ? d.block_threads : 64);
+  cfg.block = problem->mlp ? problem->mlp_block : (d.block_threads > 0 ? d.block_threads : 64);
   if (cfg.block % 32 != 0 || cfg.block > 256)
     return fail(GBDX_ERR_INVALID, "block_threads must be a multiple of 32 up to 256");
   cfg.grid = 1;

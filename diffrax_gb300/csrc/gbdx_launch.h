@@ -88,6 +88,8 @@ BwdEntry find_mlp_plain_bwd_entry(int solver, int D, int H, bool sde);
 cudaError_t launch_reduce_columns(const float *dP, int64_t n_params, int64_t batch, float *out,
                                   cudaStream_t s);
 OdeEntry find_mlp_entry_d64h128(int solver, bool precise, bool sde);
+// The MLP forward on tcgen05 (128 trajectories per CTA, one per thread).
+OdeEntry find_mlp_tc_entry(int solver, int D, int H, bool sde);
 OdeEntry find_mlp_entry_d64h256(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d32h64(int solver, bool precise, bool sde);
 

@@ -1,0 +1,618 @@
+// gbdx_mlp_tc.cu -- MLP-field integrator on the fifth-generation tensor cores
+// (tcgen05.mma, accumulators and Runge--Kutta stages in tensor memory).
+//
+// A CTA of 256 threads integrates a tile of 128 trajectories, two threads per
+// trajectory: threads r and r + 128 own TMEM lane r, i.e. row r of every
+// product, and split its columns; each keeps the row's controller state and
+// both take the same decisions, so the only exchange is the two halves of the
+// error norm.  Per RK stage the MLP field
+// D -> H -> H -> D (tanh hidden, identity output) is three tile products
+//   acc[128 x N] = A[128 x K] W[N x K]^T
+// issued by one thread as tcgen05.mma (kind::f16, BF16 operands in shared
+// memory, FP32 accumulator in TMEM), each operand held as a hi/lo BF16 pair
+// (hi.hi + lo.hi + hi.lo: ~16 significant bits, the smooth field the
+// adaptive controller needs).  Completion is signalled through an mbarrier
+// (bounded waits).  TMEM (512 columns x 128 lanes x 32 bit) holds the stage
+// vectors: columns [64 j, 64 j + 64) the stage j = 0..5 of the current step
+// (stage 0 as the unscaled FSAL field value f0, stages 1..5 as k_j = h f_j),
+// columns [384, 512) the product accumulator, whose first 64 columns after the
+// last stage hold the last stage's field (k_6, the next step's f0).
+//
+// Reference semantics as the other integrators: the loop body
+// (diffrax/_integrate.py:365-662), the explicit RK step
+// (diffrax/_solver/runge_kutta.py:446-1203, tsit5.py), the PID controller
+// (diffrax/_step_size_controller/pid.py:394-567), SaveAt(t0/ts/t1).
+#include <cuda_bf16.h>
+
+#include "gbdx_launch.h"
+#include "gbdx_mma.cuh"
+#include "gbdx_tc.cuh"
+#include "gbdx_traj.cuh"
+
+namespace gbdx {
+namespace {
+
+constexpr int kD = 64, kH = 128, kM = 128;
+constexpr int kThreads = 256;                // two threads per row
+constexpr int kDH = kD / 2;                  // state components per thread
+constexpr uint32_t kAcc = 384;               // first accumulator column
+constexpr uint32_t kWait = 1u << 24;         // polls of a completion barrier
+
+struct TcSmem {
+  __nv_bfloat16 w0h[kH * kD], w0l[kH * kD];  // layer 0: N = H rows, K = D
+  __nv_bfloat16 w1h[kH * kH], w1l[kH * kH];  // layer 1: N = H, K = H
+  __nv_bfloat16 w2h[kD * kH], w2l[kD * kH];  // layer 2: N = D, K = H
+  __nv_bfloat16 ah[kM * kH], al[kM * kH];    // activations: M rows, K <= H
+  float b0[kH], b1[kH], b2[kD];
+  float pa[2][kM], pb[2][kM];                // per-half error norm parts
+  int pn[2][kM];                             // per-half NaN flags of y1
+  unsigned long long qidx[kM];               // refill: queue slot of each row
+  uint64_t bar;
+  uint32_t slot;
+  int err;
+};
+
+// Per-row state in registers (the row_init / row_control rules of the
+// row-tile integrator: FP32 log-domain PID, FP64 times).
+struct Row {
+  double tprev, tnext, t1, floor1, dtc, tp_old, tn_old, t0s, t1s;
+  long long idx;
+  float hist1, hist2;
+  int active, first, keep, dir, save_index, ts_index, nsteps, nacc, nrej, result, sc, nc;
+  int at_dtmin;
+};
+
+__device__ __forceinline__ bool running(const Row &R, int max_steps) {
+  return R.active && order_key(R.tprev) < order_key(R.t1) && R.result == GBDX_SUCCESSFUL &&
+         R.nsteps < max_steps;
+}
+
+__device__ void init_row(Row &R, int64_t i, const SolveParams &P) {
+  const int64_t ti = i * P.time_stride;
+  double a = P.t0[ti], b = P.t1[ti];
+  const int dir = (a < b) ? 1 : -1;
+  a *= dir;
+  b *= dir;
+  R.idx = i;
+  R.dir = dir;
+  R.t1 = b;
+  double tn;
+  if (P.controller == GBDX_PID) {
+    double h = P.dt0 ? P.dt0[ti] * dir : 0.01;
+    if (P.has_dtmax) h = fmin(h, P.dtmax);
+    if (P.has_dtmin) h = fmax(h, P.dtmin);
+    tn = a + h;
+    R.hist1 = R.hist2 = 0.f;
+  } else {
+    const double h = P.dt0[ti] * dir;
+    R.sc = 1;
+    R.nc = (int)ceil((b - a) / next_up(h));
+    R.t0s = a;
+    R.t1s = b;
+    tn = a + h;
+  }
+  R.tnext = fmin(tn, b);
+  R.dtc = R.tnext - a;
+  R.tprev = a;
+  R.floor1 = t1_clip_floor(b);
+  R.first = 1;
+  R.keep = 0;
+  R.save_index = 0;
+  R.ts_index = 0;
+  R.nsteps = R.nacc = R.nrej = 0;
+  R.result = GBDX_SUCCESSFUL;
+  R.active = 1;
+  R.at_dtmin = 0;
+  if (P.save_t0) {
+    P.ts_out[i * P.n_save] = a * dir;
+    R.save_index = 1;
+  }
+}
+
+// pid.py:466-567 / constant.py:59-104 / _integrate.py:410-413 for one row,
+// given acc = the sum of squared scaled errors over the D components.
+__device__ void control_row(Row &R, float acc, const SolveParams &P) {
+  const double dt = R.dtc;
+  bool keep;
+  double nt0, nt1, dtn;
+  if (P.controller == GBDX_PID) {
+    keep = acc < float(kD);
+    const float lg = 0.5f * (log2f(float(kD)) - __log2f(acc));
+    float ex = 0.f;
+    if (P.c1_f != 0.f) ex += P.c1_f * lg;
+    if (P.c2_f != 0.f) ex += P.c2_f * R.hist1;
+    if (P.c3_f != 0.f) ex += P.c3_f * R.hist2;
+    float factor = P.safety_f * exp2f(ex);
+    const float hnew = isinf(lg) ? 0.f : lg;
+    if (P.has_dtmin) keep = keep || R.at_dtmin;
+    const float fmn = keep ? 1.f : P.factormin_f;
+    const float fmx = keep ? P.factormax_f : P.safety_f;
+    factor = fminf(fmaxf(factor, fmn), fmx);
+    dtn = dt * double(factor);
+    if (P.has_dtmax) dtn = fmin(dtn, P.dtmax);
+    if (P.has_dtmin) {
+      if (!P.force_dtmin && dtn < P.dtmin && R.result == GBDX_SUCCESSFUL)
+        R.result = GBDX_DT_MIN_REACHED;
+      if (R.at_dtmin && factor == 1.f) dtn = P.dtmin;
+      R.at_dtmin = dtn <= P.dtmin;
+      dtn = fmax(dtn, P.dtmin);
+    }
+    nt0 = keep ? R.tnext : R.tprev;
+    nt1 = nt0 + dtn;
+    if (keep) {
+      R.hist2 = R.hist1;
+      R.hist1 = hnew;
+    }
+  } else {
+    keep = true;
+    const int s2 = R.sc + 1;
+    double tn = R.t0s + (R.t1s - R.t0s) * (double(s2) / double(R.nc));
+    if (s2 == R.nc) tn = R.t1s;
+    R.sc = s2;
+    nt0 = R.tnext;
+    nt1 = tn;
+    dtn = tn - nt0;
+  }
+  if (order_key(nt1) > order_key(R.floor1)) {
+    nt1 = keep ? R.t1 : nt0 + 0.5 * (R.t1 - nt0);
+    dtn = nt1 - nt0;
+  }
+  R.keep = keep;
+  R.tp_old = R.tprev;
+  R.tn_old = R.tnext;
+  if (keep) {
+    R.nacc++;
+    R.first = 0;
+  } else {
+    R.nrej++;
+  }
+  R.nsteps++;
+  R.tprev = nt0;
+  R.tnext = nt1;
+  R.dtc = dtn;
+}
+
+// 16 values of this thread's row as hi/lo BF16 into the K-major operand tile
+// (two 16-byte runs per half).
+__device__ __forceinline__ void put16(TcSmem &sm, int row, int col, int K, const float (&v)[16]) {
+  uint32_t hi[8], lo[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(v[2 * j] - hf.x, v[2 * j + 1] - hf.y);
+    hi[j] = *reinterpret_cast<const uint32_t *>(&h);
+    lo[j] = *reinterpret_cast<const uint32_t *>(&l);
+  }
+  unsigned char *bh = reinterpret_cast<unsigned char *>(sm.ah);
+  unsigned char *bl = reinterpret_cast<unsigned char *>(sm.al);
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const uint32_t off = tc::kmajor_offset(row, col + 8 * half, K);
+    *reinterpret_cast<uint4 *>(bh + off) =
+        make_uint4(hi[4 * half], hi[4 * half + 1], hi[4 * half + 2], hi[4 * half + 3]);
+    *reinterpret_cast<uint4 *>(bl + off) =
+        make_uint4(lo[4 * half], lo[4 * half + 1], lo[4 * half + 2], lo[4 * half + 3]);
+  }
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};"
+      :: "r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])),
+         "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])),
+         "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+         "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])),
+         "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])),
+         "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+      : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// Everyone's operand writes are visible to the tensor core, then one thread
+// issues acc = A W^T as three hi/lo products per K = 16 slice and commits to
+// the barrier; all wait (bounded).  Returns false on a timeout.
+__device__ __forceinline__ bool layer(TcSmem &sm, uint32_t tmem, const __nv_bfloat16 *wh,
+                                      const __nv_bfloat16 *wl, int K, int N, uint32_t &phase) {
+  tc::fence_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc::fence_after_sync();
+    const uint32_t idesc = tc::idesc_bf16_f32(kM, N);
+    const uint32_t ah = tc::smem_u32(sm.ah), al = tc::smem_u32(sm.al);
+    const uint32_t bh = tc::smem_u32(wh), bl = tc::smem_u32(wl);
+    const uint32_t sbo = uint32_t(K) * 16u;
+    for (int kk = 0; kk < K / 16; kk++) {
+      const uint32_t o = 256u * kk;
+      const uint64_t dah = tc::smem_desc(ah + o, 128u, sbo), dal = tc::smem_desc(al + o, 128u, sbo);
+      const uint64_t dbh = tc::smem_desc(bh + o, 128u, sbo), dbl = tc::smem_desc(bl + o, 128u, sbo);
+      tc::mma_bf16(tmem + kAcc, dah, dbh, idesc, kk > 0 ? 1u : 0u);
+      tc::mma_bf16(tmem + kAcc, dal, dbh, idesc, 1u);
+      tc::mma_bf16(tmem + kAcc, dah, dbl, idesc, 1u);
+    }
+    tc::mma_commit(&sm.bar);
+  }
+  const bool ok = tc::mbar_wait(&sm.bar, phase, kWait);
+  phase ^= 1u;
+  tc::fence_after_sync();
+  return ok;
+}
+
+// Hidden layer epilogue: tanh(acc + b) of this thread's half of its row's
+// columns as the next product's operand (K = H).
+__device__ __forceinline__ void hidden_epilogue(TcSmem &sm, uint32_t lane_addr, const float *b,
+                                                int row, int half) {
+#pragma unroll 1
+  for (int c = half * (kH / 2); c < (half + 1) * (kH / 2); c += 16) {
+    float v[16];
+    tc::tmem_ld16(lane_addr + kAcc + c, v);
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = tanhf(v[j] + b[c + j]);
+    put16(sm, row, c, kH, v);
+  }
+}
+
+// The field at the operand already written (K = D): three layers; the output
+// f - b2 is left in accumulator columns [0, D).
+__device__ __forceinline__ bool mlp_eval(TcSmem &sm, uint32_t tmem, uint32_t lane_addr, int row,
+                                         int half, uint32_t &phase) {
+  bool ok = layer(sm, tmem, sm.w0h, sm.w0l, kD, kH, phase);
+  hidden_epilogue(sm, lane_addr, sm.b0, row, half);
+  ok &= layer(sm, tmem, sm.w1h, sm.w1l, kH, kH, phase);
+  hidden_epilogue(sm, lane_addr, sm.b1, row, half);
+  ok &= layer(sm, tmem, sm.w2h, sm.w2l, kH, kD, phase);
+  return ok;
+}
+
+// Stage I's input y + sum_{s<I} a_Is k_s of this thread's half row (y first,
+// the newest stage last; k_0 = h f0) as the first product's operand.
+template <int SOLVER, int I>
+__device__ __forceinline__ void stage_input(TcSmem &sm, uint32_t lane_addr, const float (&y)[kDH],
+                                            float h, int row, int col0) {
+  using TB = Tab<SOLVER>;
+#pragma unroll 1
+  for (int c = 0; c < kDH; c += 16) {
+    float yi[16], kv[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) yi[j] = y[c + j];
+#pragma unroll
+    for (int s = 0; s < I; s++) {
+      if (TB::a(I, s) == 0.0) continue;
+      tc::tmem_ld16(lane_addr + 64u * s + col0 + c, kv);
+      const float a = float(TB::a(I, s));
+#pragma unroll
+      for (int j = 0; j < 16; j++) yi[j] = fmaf(a, s == 0 ? kv[j] * h : kv[j], yi[j]);
+    }
+    put16(sm, row, col0 + c, kD, yi);
+  }
+}
+
+// Two threads integrate each row: thread t handles row t % 128 and the half
+// t / 128 of its columns.  Both keep the row's controller state and take the
+// same decisions (the controller is deterministic in the combined error norm,
+// the only value they exchange).
+template <int SOLVER>
+__global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
+  using TB = Tab<SOLVER>;
+  static_assert(TB::S == 7 && TB::FSAL && TB::SSAL, "seven-stage FSAL/SSAL tableau");
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcSmem &sm = *reinterpret_cast<TcSmem *>(smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & (kM - 1), half = tid >> 7, col0 = half * kDH;
+  const float *W = P.mlp;
+  constexpr int OW0 = 0, OB0 = OW0 + kH * kD, OW1 = OB0 + kH, OB1 = OW1 + kH * kH,
+                OW2 = OB1 + kH, OB2 = OW2 + kD * kH;
+
+  // weights as hi/lo BF16 in the K-major operand layout, biases
+  for (int i = tid; i < kH * kD; i += kThreads) {
+    const int n = i / kD, k = i % kD;
+    const uint32_t o = tc::kmajor_offset(n, k, kD) / 2;
+    split_store(W[OW0 + i], sm.w0h + o, sm.w0l + o);
+  }
+  for (int i = tid; i < kH * kH; i += kThreads) {
+    const int n = i / kH, k = i % kH;
+    const uint32_t o = tc::kmajor_offset(n, k, kH) / 2;
+    split_store(W[OW1 + i], sm.w1h + o, sm.w1l + o);
+  }
+  for (int i = tid; i < kD * kH; i += kThreads) {
+    const int n = i / kH, k = i % kH;
+    const uint32_t o = tc::kmajor_offset(n, k, kH) / 2;
+    split_store(W[OW2 + i], sm.w2h + o, sm.w2l + o);
+  }
+  for (int i = tid; i < kH; i += kThreads) {
+    sm.b0[i] = W[OB0 + i];
+    sm.b1[i] = W[OB1 + i];
+  }
+  for (int i = tid; i < kD; i += kThreads) sm.b2[i] = W[OB2 + i];
+  if (warp == 0) tc::tmem_alloc(&sm.slot, 512);
+  if (tid == 0) {
+    tc::mbar_init(&sm.bar, 1);
+    sm.err = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = sm.slot;
+  // this thread's TMEM lane: warps w and w + 4 share lanes 32 (w % 4) ...
+  const uint32_t lane_addr = tmem + (uint32_t((warp & 3) * 32) << 16);
+  uint32_t phase = 0;
+
+  Row R;
+  float y[kDH];
+  R.active = 0;
+  R.idx = 0;
+  // Take the next trajectory from the queue for rows that need one (`want`):
+  // the row's first thread draws the index, both threads load it.
+  auto refill = [&](bool want) {
+    if (want && half == 0) sm.qidx[row] = atomicAdd(P.queue, 1ull);
+    __syncthreads();
+    if (!want) return;
+    const unsigned long long q = sm.qidx[row];
+    if (q < (unsigned long long)P.batch) {
+      init_row(R, P.order ? (int64_t)P.order[q] : (int64_t)q, P);
+      const float *y0 = reinterpret_cast<const float *>(P.y0) + R.idx * kD + col0;
+#pragma unroll
+      for (int n = 0; n < kDH; n++) y[n] = y0[n];
+      if (P.save_t0) {
+        float *o = reinterpret_cast<float *>(P.ys_out) + R.idx * P.n_save * kD + col0;
+#pragma unroll
+        for (int n = 0; n < kDH; n++) o[n] = y[n];
+      }
+    } else {
+      R.active = 0;
+#pragma unroll
+      for (int n = 0; n < kDH; n++) y[n] = 0.f;
+    }
+  };
+  refill(true);
+
+  while (true) {
+    const bool live = running(R, P.max_steps);
+    const float h = live ? float(R.dir > 0 ? R.dtc : -R.dtc) : 0.f;
+    // stage 0: a fresh evaluation when some row starts (FSAL otherwise;
+    // runge_kutta.py:684-700).  Re-evaluating at y reproduces the FSAL value
+    // of the other rows bit for bit.
+    if (__syncthreads_or(live && R.first)) {
+#pragma unroll 1
+      for (int c = 0; c < kDH; c += 16) {
+        float v[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] = y[c + j];
+        put16(sm, row, col0 + c, kD, v);
+      }
+      if (!mlp_eval(sm, tmem, lane_addr, row, half, phase)) sm.err = 1;
+#pragma unroll
+      for (int c = col0; c < col0 + kDH; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr + kAcc + c, v);
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] += sm.b2[c + j];
+        tmem_st16(lane_addr + c, v);  // slot 0: f0
+      }
+    }
+    // stages 1..6
+#pragma unroll 1
+    for (int i = 1; i < 7; i++) {
+      switch (i) {
+        case 1: stage_input<SOLVER, 1>(sm, lane_addr, y, h, row, col0); break;
+        case 2: stage_input<SOLVER, 2>(sm, lane_addr, y, h, row, col0); break;
+        case 3: stage_input<SOLVER, 3>(sm, lane_addr, y, h, row, col0); break;
+        case 4: stage_input<SOLVER, 4>(sm, lane_addr, y, h, row, col0); break;
+        case 5: stage_input<SOLVER, 5>(sm, lane_addr, y, h, row, col0); break;
+        default: stage_input<SOLVER, 6>(sm, lane_addr, y, h, row, col0); break;
+      }
+      if (!mlp_eval(sm, tmem, lane_addr, row, half, phase)) sm.err = 1;
+      if (i < 6) {
+#pragma unroll
+        for (int c = col0; c < col0 + kDH; c += 16) {
+          float v[16];
+          tc::tmem_ld16(lane_addr + kAcc + c, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) v[j] = (v[j] + sm.b2[c + j]) * h;
+          tmem_st16(lane_addr + 64u * i + c, v);  // k_i
+        }
+      }
+    }
+    // y1 (SSAL: the last stage's input), error estimate and this half's part of
+    // the scaled error norm, both against max(|y0|, |y1|) and (for a row whose
+    // y1 has a NaN, pid.py:466-492) against |y0|
+    float pa = 0.f, pb = 0.f;
+    bool nanf = false;
+#pragma unroll 1
+    for (int c = 0; c < kDH; c += 16) {
+      float y1[16], er[16], kv[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        y1[j] = y[c + j];
+        er[j] = 0.f;
+      }
+#pragma unroll
+      for (int s = 0; s < 7; s++) {
+        if (s < 6) {
+          tc::tmem_ld16(lane_addr + 64u * s + col0 + c, kv);
+        } else {
+          tc::tmem_ld16(lane_addr + kAcc + col0 + c, kv);
+        }
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const float k =
+              s == 0 ? kv[j] * h : s == 6 ? (kv[j] + sm.b2[col0 + c + j]) * h : kv[j];
+          if (s < 6) y1[j] = fmaf(float(TB::a(6, s)), k, y1[j]);
+          if (TB::e(s) != 0.0) er[j] = fmaf(float(TB::e(s)), k, er[j]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        nanf |= isnan(y1[j]);
+        const float e = isnan(er[j]) ? INFINITY : er[j];
+        const float a0 = fabsf(y[c + j]);
+        const float sa = __fdividef(e, fmaf(fmaxf(a0, fabsf(y1[j])), P.rtol_f, P.atol_f));
+        const float sb = __fdividef(e, fmaf(a0, P.rtol_f, P.atol_f));
+        pa = fmaf(sa, sa, pa);
+        pb = fmaf(sb, sb, pb);
+      }
+    }
+    sm.pa[half][row] = pa;
+    sm.pb[half][row] = pb;
+    sm.pn[half][row] = nanf ? 1 : 0;
+    __syncthreads();
+    const bool rownan = sm.pn[0][row] | sm.pn[1][row];
+    const float acc = rownan ? sm.pb[0][row] + sm.pb[1][row] : sm.pa[0][row] + sm.pa[1][row];
+    if (live) control_row(R, acc, P);
+    const bool kept = live && R.keep;
+    // SaveAt(ts) inside the step just taken (_integrate.py:456-487)
+    while (true) {
+      bool pend = false;
+      double tsv = 0.0;
+      float th = 0.f;
+      if (kept && R.ts_index < P.n_ts) {
+        tsv = __ldg(P.save_ts + R.ts_index);
+        const double tsd = R.dir * tsv;
+        if (order_key(tsd) <= order_key(R.tn_old)) {
+          pend = true;
+          const double tp = R.tp_old, tn = R.tn_old;
+          th = float(tp == tn ? 0.0 : (tsd - tp) / (tn - tp));
+        }
+      }
+      if (!__any_sync(0xffffffffu, pend)) break;
+      float *o = reinterpret_cast<float *>(P.ys_out) +
+                 (R.idx * P.n_save + (pend ? R.save_index : 0)) * kD + col0;
+#pragma unroll 1
+      for (int c = 0; c < kDH; c += 16) {
+        float v[16], kv[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] = 0.f;
+#pragma unroll
+        for (int s = 0; s < 7; s++) {
+          if (s < 6) tc::tmem_ld16(lane_addr + 64u * s + col0 + c, kv);
+          else tc::tmem_ld16(lane_addr + kAcc + col0 + c, kv);
+          const float w = tsit5_w<float>(s, th);
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const float k =
+                s == 0 ? kv[j] * h : s == 6 ? (kv[j] + sm.b2[col0 + c + j]) * h : kv[j];
+            v[j] = fmaf(w, k, v[j]);
+          }
+        }
+        if (pend) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) o[c + j] = y[c + j] + v[j];
+        }
+      }
+      if (pend) {
+        if (half == 0) P.ts_out[R.idx * P.n_save + R.save_index] = tsv;
+        R.ts_index++;
+        R.save_index++;
+      }
+    }
+    // accept: y = y1, f0 = the last stage's field (FSAL); a rejected row
+    // keeps both
+#pragma unroll 1
+    for (int c = 0; c < kDH; c += 16) {
+      float y1[16], kv[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++) y1[j] = y[c + j];
+#pragma unroll
+      for (int s = 0; s < 6; s++) {
+        tc::tmem_ld16(lane_addr + 64u * s + col0 + c, kv);
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const float k = s == 0 ? kv[j] * h : kv[j];
+          y1[j] = fmaf(float(TB::a(6, s)), k, y1[j]);
+        }
+      }
+      float f0[16];
+      tc::tmem_ld16(lane_addr + col0 + c, f0);
+      tc::tmem_ld16(lane_addr + kAcc + col0 + c, kv);
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        if (kept) {
+          y[c + j] = y1[j];
+          f0[j] = kv[j] + sm.b2[col0 + c + j];
+        }
+      }
+      tmem_st16(lane_addr + col0 + c, f0);
+    }
+    // finished rows: t1 save, unused slots, results; then refill
+    const bool fin = R.active && !running(R, P.max_steps);
+    if (fin) {
+      const int64_t i = R.idx;
+      const int dir = R.dir;
+      const double t0 = P.t0[i * P.time_stride] * dir;
+      float *o = reinterpret_cast<float *>(P.ys_out) + i * P.n_save * kD + col0;
+      int si = R.save_index;
+      if (t0 == R.t1) {
+        for (int m = 0; m < P.n_ts; m++, si++) {
+          if (half == 0) P.ts_out[i * P.n_save + si] = t0 * dir;
+          for (int n = 0; n < kDH; n++) o[si * kD + n] = y[n];
+        }
+      }
+      if (P.save_t1) {
+        if (half == 0) P.ts_out[i * P.n_save + si] = R.tprev * dir;
+        for (int n = 0; n < kDH; n++) o[si * kD + n] = y[n];
+        si++;
+      }
+      for (int m = si; m < P.n_save; m++) {
+        if (half == 0) P.ts_out[i * P.n_save + m] = dir > 0 ? INFINITY : -INFINITY;
+        for (int n = 0; n < kDH; n++) o[m * kD + n] = INFINITY;
+      }
+      if (half == 0) {
+        int res = R.result;
+        if (sm.err) res = GBDX_INTERNAL_ERROR;
+        if (res == GBDX_SUCCESSFUL && order_key(R.tprev) < order_key(R.t1))
+          res = GBDX_MAX_STEPS_REACHED;
+        P.result_out[i] = res;
+        P.stats_out[i * 3 + 0] = R.nsteps;
+        P.stats_out[i * 3 + 1] = R.nacc;
+        P.stats_out[i * 3 + 2] = R.nrej;
+      }
+      R.active = 0;
+    }
+    const bool err = sm.err != 0;
+    refill(fin && !err);
+    if (err && R.active) {
+      // a product did not complete: end every row with an internal error
+      if (half == 0) P.result_out[R.idx] = GBDX_INTERNAL_ERROR;
+      R.active = 0;
+    }
+    if (!__syncthreads_or(R.active)) break;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+template <int SOLVER>
+cudaError_t launch_tc(const SolveParams &P, const LaunchCfg &cfg, cudaStream_t s) {
+  auto k = mlp_tc_kernel<SOLVER>;
+  cudaError_t e =
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(TcSmem)));
+  if (e != cudaSuccess) return e;
+  if (P.batch <= 0) return cudaSuccess;
+  k<<<cfg.grid, kThreads, sizeof(TcSmem), s>>>(P);
+  return cudaGetLastError();
+}
+
+template <int SOLVER>
+cudaError_t occupancy_tc(int, int *ctas) {
+  auto k = mlp_tc_kernel<SOLVER>;
+  cudaError_t e =
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(TcSmem)));
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, k, kThreads, sizeof(TcSmem));
+  // one CTA per SM: it holds all 512 TMEM columns
+  if (e == cudaSuccess && *ctas > 1) *ctas = 1;
+  return e;
+}
+
+}  // namespace
+
+OdeEntry find_mlp_tc_entry(int solver, int D, int H, bool sde) {
+  if (sde || D != kD || H != kH) return OdeEntry{nullptr, nullptr};
+  if (solver == GBDX_TSIT5) return OdeEntry{&launch_tc<GBDX_TSIT5>, &occupancy_tc<GBDX_TSIT5>};
+  return OdeEntry{nullptr, nullptr};
+}
+
+}  // namespace gbdx

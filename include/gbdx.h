@@ -61,8 +61,16 @@ enum gbdx_field {
 enum gbdx_diffusion { GBDX_DIFF_NONE = 0, GBDX_DIFF_OU = 1, GBDX_DIFF_TANH_DIAG = 2 };
 enum gbdx_dtype { GBDX_F32 = 0, GBDX_F64 = 1 };
 /* Kernel family: PLAIN is one trajectory per thread launched once per
- * trajectory; FUSED is the persistent work-stealing integrator. */
-enum gbdx_kernel { GBDX_KERNEL_AUTO = 0, GBDX_KERNEL_PLAIN = 1, GBDX_KERNEL_FUSED = 2 };
+ * trajectory; FUSED is the persistent work-stealing integrator; TC is the
+ * MLP-field forward on the fifth-generation tensor cores (tcgen05.mma with the
+ * accumulators and the Runge--Kutta stages in tensor memory; 64 -> 128 -> 128
+ * -> 64 fields, Tsit5, BF16 products, forward solves). */
+enum gbdx_kernel {
+  GBDX_KERNEL_AUTO = 0,
+  GBDX_KERNEL_PLAIN = 1,
+  GBDX_KERNEL_FUSED = 2,
+  GBDX_KERNEL_TC = 3
+};
 enum gbdx_adjoint { GBDX_ADJ_NONE = 0, GBDX_ADJ_RECURSIVE = 1, GBDX_ADJ_BACKSOLVE = 2 };
 enum gbdx_norm { GBDX_NORM_RMS = 0, GBDX_NORM_ADJOINT_SEMI = 1 };
 /* Work order of the fused kernels.  AUTO hands out trajectories by decreasing

@@ -247,3 +247,23 @@ def test_ou_sde_scope():
         _lib.Problem(fields(2, torch.float64))
     with pytest.raises(_lib.GbdxError, match="dim 2 or 4"):
         _lib.Problem(fields(3, torch.float32))
+
+
+def test_tc_kernel_scope():
+    # kernel="tc": BF16 forward solves of 64 -> 128 -> 128 -> 64 MLP fields
+    # with Tsit5; anything else is rejected at problem creation
+    W = [torch.zeros(128, 64), torch.zeros(128, 128), torch.zeros(64, 128)]
+    b = [torch.zeros(128), torch.zeros(128), torch.zeros(64)]
+    term = dfx.ODETerm(dfx.MLPField(W, b))
+    pid = dfx.PIDController(rtol=1e-5, atol=1e-7)
+
+    def fields(solver, **kw):
+        return dfx.lower(term, solver, pid, dfx.SaveAt(t1=True), dim=64, dtype=torch.float32,
+                         max_steps=64, n_ts=0, kernel="tc", **kw)
+    assert _lib.Problem(fields(dfx.Tsit5())).n_save == 1
+    with pytest.raises(_lib.GbdxError, match="Tsit5"):
+        _lib.Problem(fields(dfx.Dopri5()))
+    with pytest.raises(_lib.GbdxError, match="adjoint"):
+        _lib.Problem(fields(dfx.Tsit5(), adjoint=dfx.RecursiveCheckpointAdjoint(8)))
+    with pytest.raises(_lib.GbdxError, match="MLP"):
+        _lib.Problem(_fields(kernel=3))
