@@ -365,8 +365,9 @@ def profile_backsolve(dev, B, seminorm, n):
 
 def profile_neural(dev, which, B, n):
     """n fused solves of a neural workload at batch B, for ncu: the forward of
-    the neural ODE (64-128-128-64), its forward + RecursiveCheckpointAdjoint
-    backward, the wide neural ODE forward or the neural SDE forward."""
+    the neural ODE (64-128-128-64, row-tile or tcgen05 kernel), its forward +
+    RecursiveCheckpointAdjoint backward, the wide neural ODE forward or the
+    neural SDE forward."""
     import torch
     import diffrax_gb300 as dfx
     from diffrax_gb300._integrate import Lowered
@@ -392,8 +393,8 @@ def profile_neural(dev, which, B, n):
         saveat = dfx.SaveAt(ts=np.linspace(0, 1, 32)) if wide else dfx.SaveAt(t1=True)
     grad = which == "neural_ode_grad"
     low = Lowered(terms, solver, 0.0, 1.0, dt0, y0, None, saveat, ctrl,
-                  dfx.RecursiveCheckpointAdjoint(checkpoints=64), 4096, "fused", 0, 0,
-                  want_grad=grad)
+                  dfx.RecursiveCheckpointAdjoint(checkpoints=64), 4096,
+                  "tc" if which == "neural_ode_tc" else "fused", 0, 0, want_grad=grad)
     for _ in range(n):
         if grad:
             ys, _, res, _, ws = low.run_forward(keep_workspace=True)
@@ -500,6 +501,33 @@ def workload_neural(dev, flush, steps, warmup, kind):
     out["cpu_baseline_forward"] = _oracle_rate(
         lambda: O.solve(desc, 0.0, 1.0, dt0, y0[:512].astype(np.float64), params=params, ts=ts,
                         nthreads=cores), 512, cores)
+    if kind == "ode":
+        # The same forward on the fifth-generation tensor cores (tcgen05.mma,
+        # TMEM accumulators; 128 trajectories per CTA), at this batch (64
+        # tiles) and at a batch filling every SM with one tile (152 x 128),
+        # beside the mma.sync row-tile kernel at that batch.
+        tc = lowered("tc", False)
+        ms_t = _events_time(tc.run_forward, steps, warmup, flush)
+        ys_t = tc.run_forward()[0]
+        e_t = _rel_per_traj(ys_t[:n_chk].double().cpu().numpy(), ref["ys"])
+        alg_t = B * out["mean_attempted_steps"] * evals * fl_eval / (ms_t / 1e3) / 1e12
+        out["tc_forward"] = {"traj_per_s": B / (ms_t / 1e3), "ms": ms_t,
+                             "max_rel_err_vs_fp64_oracle": float(e_t.max()),
+                             "roofline": {"bound": "tensor", "achieved": alg_t,
+                                          "frac": alg_t / peaks.get("bf16_tflops", 1900.0),
+                                          "unit": "TFLOP/s", "peak_source": src}}
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        Bf = 128 * sms
+        yf = torch.tensor(np.random.default_rng(seed + 2).standard_normal((Bf, D)),
+                          dtype=torch.float32, device=dev)
+        full = {}
+        for kern in ("fused", "tc"):
+            lo = Lowered(terms_for("bf16"), solver, 0.0, 1.0, dt0, yf, None, saveat, ctrl, None,
+                         4096, kern, 0, 0)
+            ms_k = _events_time(lo.run_forward, steps, warmup, flush)
+            full[kern] = {"traj_per_s": Bf / (ms_k / 1e3), "ms": ms_k}
+        full["tc_over_fused"] = full["fused"]["ms"] / full["tc"]["ms"]
+        out[f"forward_batch_{Bf}"] = full
     if kind == "wide":
         out.update(workload_backsolve(dev, flush, steps, warmup, terms_for, solver, ctrl,
                                       saveat, ts, y0, y0_d, params, desc, B, D))
@@ -555,7 +583,8 @@ def main():
                     help="skip the other configurations")
     ap.add_argument("--profile", default=None,
                     choices=["fused", "plain", "backsolve", "backsolve_seminorm", "neural_ode",
-                             "neural_ode_grad", "neural_ode_wide", "neural_sde"],
+                             "neural_ode_tc", "neural_ode_grad", "neural_ode_wide",
+                             "neural_sde"],
                     help="run warmup + steps eager solves of one kernel only (for ncu); "
                          "backsolve*: forward + backward of the wide neural ODE at --batch")
     args = ap.parse_args()

@@ -350,7 +350,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       }
       p->mlp = true;
       p->rows_per_cta = 128;
-      p->mlp_block = 256;
+      p->mlp_block = 512;  // four threads per trajectory
       *out = p;
       return GBDX_OK;
     }
@@ -639,7 +639,7 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
   gbdx::LaunchCfg cfg;
   cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;
   cfg.block = problem->mlp ? problem->mlp_block : (d.block_threads > 0 ? d.block_threads : 64);
-  if (cfg.block % 32 != 0 || cfg.block > 256)
+  if (!problem->mlp && (cfg.block % 32 != 0 || cfg.block > 256))
     return fail(GBDX_ERR_INVALID, "block_threads must be a multiple of 32 up to 256");
   cfg.grid = 1;
   if (cfg.kernel == GBDX_KERNEL_FUSED) {

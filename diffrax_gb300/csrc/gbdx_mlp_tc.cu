@@ -1,11 +1,11 @@
 // gbdx_mlp_tc.cu -- MLP-field integrator on the fifth-generation tensor cores
 // (tcgen05.mma, accumulators and Runge--Kutta stages in tensor memory).
 //
-// A CTA of 256 threads integrates a tile of 128 trajectories, two threads per
-// trajectory: threads r and r + 128 own TMEM lane r, i.e. row r of every
-// product, and split its columns; each keeps the row's controller state and
-// both take the same decisions, so the only exchange is the two halves of the
-// error norm.  Per RK stage the MLP field
+// A CTA of 512 threads integrates a tile of 128 trajectories, four threads per
+// trajectory: threads r, r + 128, r + 256, r + 384 own TMEM lane r, i.e. row r
+// of every product, and split its columns; each keeps the row's controller
+// state and all take the same decisions, so the only exchange is the four
+// parts of the error norm.  Per RK stage the MLP field
 // D -> H -> H -> D (tanh hidden, identity output) is three tile products
 //   acc[128 x N] = A[128 x K] W[N x K]^T
 // issued by one thread as tcgen05.mma (kind::f16, BF16 operands in shared
@@ -33,8 +33,10 @@ namespace gbdx {
 namespace {
 
 constexpr int kD = 64, kH = 128, kM = 128;
-constexpr int kThreads = 256;                // two threads per row
-constexpr int kDH = kD / 2;                  // state components per thread
+constexpr int kSplit = 4;                    // threads per row
+constexpr int kThreads = kM * kSplit;
+constexpr int kDH = kD / kSplit;             // state components per thread
+constexpr int kHH = kH / kSplit;             // hidden columns per thread
 constexpr uint32_t kAcc = 384;               // first accumulator column
 constexpr uint32_t kWait = 1u << 24;         // polls of a completion barrier
 
@@ -44,8 +46,8 @@ struct TcSmem {
   __nv_bfloat16 w2h[kD * kH], w2l[kD * kH];  // layer 2: N = D, K = H
   __nv_bfloat16 ah[kM * kH], al[kM * kH];    // activations: M rows, K <= H
   float b0[kH], b1[kH], b2[kD];
-  float pa[2][kM], pb[2][kM];                // per-half error norm parts
-  int pn[2][kM];                             // per-half NaN flags of y1
+  float pa[kSplit][kM], pb[kSplit][kM];      // per-part error norm parts
+  int pn[kSplit][kM];                        // per-part NaN flags of y1
   unsigned long long qidx[kM];               // refill: queue slot of each row
   uint64_t bar;
   uint32_t slot;
@@ -240,12 +242,12 @@ __device__ __forceinline__ bool layer(TcSmem &sm, uint32_t tmem, const __nv_bflo
   return ok;
 }
 
-// Hidden layer epilogue: tanh(acc + b) of this thread's half of its row's
+// Hidden layer epilogue: tanh(acc + b) of this thread's part of its row's
 // columns as the next product's operand (K = H).
 __device__ __forceinline__ void hidden_epilogue(TcSmem &sm, uint32_t lane_addr, const float *b,
-                                                int row, int half) {
-#pragma unroll 1
-  for (int c = half * (kH / 2); c < (half + 1) * (kH / 2); c += 16) {
+                                                int row, int part) {
+#pragma unroll
+  for (int c = part * kHH; c < (part + 1) * kHH; c += 16) {
     float v[16];
     tc::tmem_ld16(lane_addr + kAcc + c, v);
 #pragma unroll
@@ -257,22 +259,22 @@ __device__ __forceinline__ void hidden_epilogue(TcSmem &sm, uint32_t lane_addr, 
 // The field at the operand already written (K = D): three layers; the output
 // f - b2 is left in accumulator columns [0, D).
 __device__ __forceinline__ bool mlp_eval(TcSmem &sm, uint32_t tmem, uint32_t lane_addr, int row,
-                                         int half, uint32_t &phase) {
+                                         int part, uint32_t &phase) {
   bool ok = layer(sm, tmem, sm.w0h, sm.w0l, kD, kH, phase);
-  hidden_epilogue(sm, lane_addr, sm.b0, row, half);
+  hidden_epilogue(sm, lane_addr, sm.b0, row, part);
   ok &= layer(sm, tmem, sm.w1h, sm.w1l, kH, kH, phase);
-  hidden_epilogue(sm, lane_addr, sm.b1, row, half);
+  hidden_epilogue(sm, lane_addr, sm.b1, row, part);
   ok &= layer(sm, tmem, sm.w2h, sm.w2l, kH, kD, phase);
   return ok;
 }
 
-// Stage I's input y + sum_{s<I} a_Is k_s of this thread's half row (y first,
+// Stage I's input y + sum_{s<I} a_Is k_s of this thread's part of its row (y first,
 // the newest stage last; k_0 = h f0) as the first product's operand.
 template <int SOLVER, int I>
 __device__ __forceinline__ void stage_input(TcSmem &sm, uint32_t lane_addr, const float (&y)[kDH],
                                             float h, int row, int col0) {
   using TB = Tab<SOLVER>;
-#pragma unroll 1
+#pragma unroll
   for (int c = 0; c < kDH; c += 16) {
     float yi[16], kv[16];
 #pragma unroll
@@ -289,10 +291,10 @@ __device__ __forceinline__ void stage_input(TcSmem &sm, uint32_t lane_addr, cons
   }
 }
 
-// Two threads integrate each row: thread t handles row t % 128 and the half
-// t / 128 of its columns.  Both keep the row's controller state and take the
-// same decisions (the controller is deterministic in the combined error norm,
-// the only value they exchange).
+// kSplit threads integrate each row: thread t handles row t % 128 and the
+// part t / 128 of its columns.  Each keeps the row's controller state and all
+// take the same decisions (the controller is deterministic in the combined
+// error norm, the only value they exchange).
 template <int SOLVER>
 __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
   using TB = Tab<SOLVER>;
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TcSmem &sm = *reinterpret_cast<TcSmem *>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int row = tid & (kM - 1), half = tid >> 7, col0 = half * kDH;
+  const int row = tid & (kM - 1), part = tid >> 7, col0 = part * kDH;
   const float *W = P.mlp;
   constexpr int OW0 = 0, OB0 = OW0 + kH * kD, OW1 = OB0 + kH, OB1 = OW1 + kH * kH,
                 OW2 = OB1 + kH, OB2 = OW2 + kD * kH;
@@ -346,7 +348,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
   // Take the next trajectory from the queue for rows that need one (`want`):
   // the row's first thread draws the index, both threads load it.
   auto refill = [&](bool want) {
-    if (want && half == 0) sm.qidx[row] = atomicAdd(P.queue, 1ull);
+    if (want && part == 0) sm.qidx[row] = atomicAdd(P.queue, 1ull);
     __syncthreads();
     if (!want) return;
     const unsigned long long q = sm.qidx[row];
@@ -375,14 +377,14 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
     // runge_kutta.py:684-700).  Re-evaluating at y reproduces the FSAL value
     // of the other rows bit for bit.
     if (__syncthreads_or(live && R.first)) {
-#pragma unroll 1
+#pragma unroll
       for (int c = 0; c < kDH; c += 16) {
         float v[16];
 #pragma unroll
         for (int j = 0; j < 16; j++) v[j] = y[c + j];
         put16(sm, row, col0 + c, kD, v);
       }
-      if (!mlp_eval(sm, tmem, lane_addr, row, half, phase)) sm.err = 1;
+      if (!mlp_eval(sm, tmem, lane_addr, row, part, phase)) sm.err = 1;
 #pragma unroll
       for (int c = col0; c < col0 + kDH; c += 16) {
         float v[16];
@@ -403,7 +405,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
         case 5: stage_input<SOLVER, 5>(sm, lane_addr, y, h, row, col0); break;
         default: stage_input<SOLVER, 6>(sm, lane_addr, y, h, row, col0); break;
       }
-      if (!mlp_eval(sm, tmem, lane_addr, row, half, phase)) sm.err = 1;
+      if (!mlp_eval(sm, tmem, lane_addr, row, part, phase)) sm.err = 1;
       if (i < 6) {
 #pragma unroll
         for (int c = col0; c < col0 + kDH; c += 16) {
@@ -415,12 +417,12 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
         }
       }
     }
-    // y1 (SSAL: the last stage's input), error estimate and this half's part of
+    // y1 (SSAL: the last stage's input), error estimate and this thread's part of
     // the scaled error norm, both against max(|y0|, |y1|) and (for a row whose
     // y1 has a NaN, pid.py:466-492) against |y0|
     float pa = 0.f, pb = 0.f;
     bool nanf = false;
-#pragma unroll 1
+#pragma unroll
     for (int c = 0; c < kDH; c += 16) {
       float y1[16], er[16], kv[16];
 #pragma unroll
@@ -454,12 +456,19 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
         pb = fmaf(sb, sb, pb);
       }
     }
-    sm.pa[half][row] = pa;
-    sm.pb[half][row] = pb;
-    sm.pn[half][row] = nanf ? 1 : 0;
+    sm.pa[part][row] = pa;
+    sm.pb[part][row] = pb;
+    sm.pn[part][row] = nanf ? 1 : 0;
     __syncthreads();
-    const bool rownan = sm.pn[0][row] | sm.pn[1][row];
-    const float acc = rownan ? sm.pb[0][row] + sm.pb[1][row] : sm.pa[0][row] + sm.pa[1][row];
+    bool rownan = false;
+    float acc_a = 0.f, acc_b = 0.f;
+#pragma unroll
+    for (int q = 0; q < kSplit; q++) {  // the same order in every thread of the row
+      rownan |= sm.pn[q][row] != 0;
+      acc_a += sm.pa[q][row];
+      acc_b += sm.pb[q][row];
+    }
+    const float acc = rownan ? acc_b : acc_a;
     if (live) control_row(R, acc, P);
     const bool kept = live && R.keep;
     // SaveAt(ts) inside the step just taken (_integrate.py:456-487)
@@ -479,7 +488,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
       if (!__any_sync(0xffffffffu, pend)) break;
       float *o = reinterpret_cast<float *>(P.ys_out) +
                  (R.idx * P.n_save + (pend ? R.save_index : 0)) * kD + col0;
-#pragma unroll 1
+#pragma unroll
       for (int c = 0; c < kDH; c += 16) {
         float v[16], kv[16];
 #pragma unroll
@@ -502,14 +511,14 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
         }
       }
       if (pend) {
-        if (half == 0) P.ts_out[R.idx * P.n_save + R.save_index] = tsv;
+        if (part == 0) P.ts_out[R.idx * P.n_save + R.save_index] = tsv;
         R.ts_index++;
         R.save_index++;
       }
     }
     // accept: y = y1, f0 = the last stage's field (FSAL); a rejected row
     // keeps both
-#pragma unroll 1
+#pragma unroll
     for (int c = 0; c < kDH; c += 16) {
       float y1[16], kv[16];
 #pragma unroll
@@ -545,20 +554,20 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
       int si = R.save_index;
       if (t0 == R.t1) {
         for (int m = 0; m < P.n_ts; m++, si++) {
-          if (half == 0) P.ts_out[i * P.n_save + si] = t0 * dir;
+          if (part == 0) P.ts_out[i * P.n_save + si] = t0 * dir;
           for (int n = 0; n < kDH; n++) o[si * kD + n] = y[n];
         }
       }
       if (P.save_t1) {
-        if (half == 0) P.ts_out[i * P.n_save + si] = R.tprev * dir;
+        if (part == 0) P.ts_out[i * P.n_save + si] = R.tprev * dir;
         for (int n = 0; n < kDH; n++) o[si * kD + n] = y[n];
         si++;
       }
       for (int m = si; m < P.n_save; m++) {
-        if (half == 0) P.ts_out[i * P.n_save + m] = dir > 0 ? INFINITY : -INFINITY;
+        if (part == 0) P.ts_out[i * P.n_save + m] = dir > 0 ? INFINITY : -INFINITY;
         for (int n = 0; n < kDH; n++) o[m * kD + n] = INFINITY;
       }
-      if (half == 0) {
+      if (part == 0) {
         int res = R.result;
         if (sm.err) res = GBDX_INTERNAL_ERROR;
         if (res == GBDX_SUCCESSFUL && order_key(R.tprev) < order_key(R.t1))
@@ -574,7 +583,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
     refill(fin && !err);
     if (err && R.active) {
       // a product did not complete: end every row with an internal error
-      if (half == 0) P.result_out[R.idx] = GBDX_INTERNAL_ERROR;
+      if (part == 0) P.result_out[R.idx] = GBDX_INTERNAL_ERROR;
       R.active = 0;
     }
     if (!__syncthreads_or(R.active)) break;
