@@ -492,14 +492,15 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     if want_grad and (saveat.dense or saveat.steps or event is not None):
         raise NotImplementedError("gradients through SaveAt(steps=...), SaveAt(dense=True) "
                                   "or events are not supported")
-    if autotune and not want_grad and block_threads == 0 and ctas_per_sm == 0:
+    if (autotune and not want_grad and block_threads == 0 and ctas_per_sm == 0
+            and kernel in ("auto", "fused")):
         from ._tune import autotune_launch
 
-        def factory(bt, cps):
+        def factory(kern, bt, cps):
             return Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
-                           adjoint, max_steps, kernel, bt, cps, schedule, event=event)
-        base = factory(0, 0)
-        block_threads, ctas_per_sm = autotune_launch(factory, base.B, base.fields)
+                           adjoint, max_steps, kern, bt, cps, schedule, event=event)
+        base = factory(kernel, 0, 0)
+        kernel, block_threads, ctas_per_sm = autotune_launch(factory, base.B, base.fields)
     low = Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
                   adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule,
                   want_grad=want_grad, event=event)

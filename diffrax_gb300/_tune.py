@@ -38,32 +38,50 @@ def _key(fields: dict, batch: int):
     return tuple(items), 1 << max(0, math.ceil(math.log2(max(batch, 1))))
 
 
+def tc_eligible(fields: dict) -> bool:
+    """Whether the tcgen05 forward (kernel "tc") serves this problem: BF16
+    forward solves of 64 -> 128 -> 128 -> 64 MLP ODE fields with Tsit5."""
+    return (fields.get("field") == 3 and fields.get("solver") == 3 and
+            tuple(fields.get("mlp_widths", ())) == (64, 128, 128, 64) and
+            fields.get("mlp_precision", 0) == 0 and fields.get("adjoint", 0) == 0 and
+            fields.get("diffusion", 0) == 0 and not fields.get("save_steps") and
+            not fields.get("save_dense") and not fields.get("n_event") and
+            not fields.get("n_step_ts") and not fields.get("n_jump_ts"))
+
+
 def candidates(fields: dict, batch: int) -> list:
-    """(block_threads, ctas_per_sm) shapes worth timing for this problem."""
-    if fields.get("field") == 3:  # MLP fields: 256 threads per CTA, one row tile each
-        return [(0, c) for c in (1, 2, 3, 4)]
+    """(kernel, block_threads, ctas_per_sm) shapes worth timing for this
+    problem: the launch shape of the fused kernels and, for the MLP fields,
+    the tile shape (32-row mma.sync tiles, or 128-row tcgen05 tiles)."""
+    kernel = fields.get("kernel", 0)
+    if fields.get("field") == 3:  # MLP fields: one row tile per CTA
+        out = [("fused", 0, c) for c in (1, 2, 3, 4)]
+        if kernel == 0 and tc_eligible(fields):
+            out.append(("tc", 0, 1))
+        return out
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    out = [(0, 0)]
+    out = [("fused", 0, 0)]
     for block in (32, 64, 128, 256):
         for per_sm in (1, 2, 4, 8, 16, 32):
             lanes = block * per_sm * sms
             if lanes > 2 * batch or block * per_sm > 2048:
                 continue
-            out.append((block, per_sm))
+            out.append(("fused", block, per_sm))
     return out
 
 
 def autotune_launch(low_factory, batch: int, fields: dict, reps: int = 3,
                     verbose: bool = False):
-    """Time every candidate launch shape of the problem and return the fastest
-    (block_threads, ctas_per_sm); cached per problem and batch class.
+    """Time every candidate shape of the problem and return the fastest
+    (kernel, block_threads, ctas_per_sm); cached per problem and batch class.
 
-    ``low_factory(block_threads, ctas_per_sm)`` builds the Lowered solve."""
+    ``low_factory(kernel, block_threads, ctas_per_sm)`` builds the Lowered
+    solve."""
     key = _key(fields, batch)
     hit = _TUNED.get(key)
     if hit is not None:
         return hit
-    best, best_ms = (0, 0), math.inf
+    best, best_ms = ("fused", 0, 0), math.inf
     stream = torch.cuda.current_stream()
     for shape in candidates(fields, batch):
         low = low_factory(*shape)
@@ -86,7 +104,8 @@ def autotune_launch(low_factory, batch: int, fields: dict, reps: int = 3,
 
 
 def tuned_shapes() -> dict:
-    """The shapes chosen so far (problem key -> (block_threads, ctas_per_sm))."""
+    """The shapes chosen so far (problem key -> (kernel, block_threads,
+    ctas_per_sm))."""
     return dict(_TUNED)
 
 
@@ -129,14 +148,14 @@ class GraphedSolve:
         args = own(args, y0.dtype)
         self.throw, self.max_steps = throw, max_steps
 
-        def factory(block_threads, ctas_per_sm):
+        def factory(kern, block_threads, ctas_per_sm):
             return Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
-                           None, max_steps, kernel, block_threads, ctas_per_sm, schedule,
+                           None, max_steps, kern, block_threads, ctas_per_sm, schedule,
                            event=event)
 
-        shape = (0, 0)
+        shape = (kernel, 0, 0)
         if autotune:
-            base = factory(0, 0)
+            base = factory(kernel, 0, 0)
             shape = autotune_launch(factory, base.B, base.fields)
         self.shape = shape
         low = factory(*shape)

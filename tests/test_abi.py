@@ -228,7 +228,16 @@ def test_autotune_cache_key_ignores_launch_shape():
     k2 = _tune._key(dict(f, block_threads=0, ctas_per_sm=0), 8000)
     assert k1 == k2 and k1[1] == 8192
     assert _tune._key(f, 9000) != k2
-    assert _tune.candidates(dict(f, field=3), 1024) == [(0, 1), (0, 2), (0, 3), (0, 4)]
+    assert _tune.candidates(dict(f, field=3), 1024) == [("fused", 0, c) for c in (1, 2, 3, 4)]
+    # the 64-128-128-64 Tsit5 BF16 forward may also take the tcgen05 tiles
+    W = [torch.zeros(128, 64), torch.zeros(128, 128), torch.zeros(64, 128)]
+    b = [torch.zeros(128), torch.zeros(128), torch.zeros(64)]
+    mlp = dfx.lower(dfx.ODETerm(dfx.MLPField(W, b)), dfx.Tsit5(),
+                    dfx.PIDController(rtol=1e-5, atol=1e-7), dfx.SaveAt(t1=True), dim=64,
+                    dtype=torch.float32, max_steps=64, n_ts=0)
+    assert _tune.tc_eligible(mlp) and ("tc", 0, 1) in _tune.candidates(mlp, 8192)
+    assert ("tc", 0, 1) not in _tune.candidates(dict(mlp, kernel=2), 8192)
+    assert not _tune.tc_eligible(dict(mlp, solver=2))
 
 
 def test_ou_sde_scope():

@@ -60,8 +60,11 @@ def test_autotune_mlp_row_tiles():
     sol = dfx.diffeqsolve(term, dfx.Tsit5(), 0.0, 1.0, None, y0, stepsize_controller=pid,
                           autotune=True)
     # the MLP kernels sum each row's error norm with shared-memory atomics,
-    # whose order (and last bit) may change with the launch shape: equal to
-    # the solve's accuracy, not bit for bit
+    # whose order (and last bit) may change with the launch shape, and the
+    # tuner may pick the tcgen05 tiles: equal to the solve's accuracy, not bit
+    # for bit
+    chosen = [v for v in _tune.tuned_shapes().values() if v[0] in ("fused", "tc")]
+    assert chosen
     err = (sol.ys - ref.ys).abs().max() / ref.ys.abs().max()
     assert float(err) < 1e-4
 
@@ -75,8 +78,8 @@ def test_graphed_solve_replays_new_inputs():
         y0n, mun, t1n = vdp_inputs(4096, seed)
         sol = g(y0=y0n, args=mun, t1=t1n)
         ref = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1n, None, y0n, mun,
-                              stepsize_controller=PID, block_threads=g.shape[0],
-                              ctas_per_sm=g.shape[1])
+                              stepsize_controller=PID, kernel=g.shape[0],
+                              block_threads=g.shape[1], ctas_per_sm=g.shape[2])
         assert torch.equal(sol.ys, ref.ys) and torch.equal(sol.ts, ref.ts)
         assert torch.equal(sol.stats["num_accepted_steps"], ref.stats["num_accepted_steps"])
     # the inputs given to the constructor were copied, not aliased
