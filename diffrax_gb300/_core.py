@@ -155,21 +155,42 @@ class MultiTerm(AbstractTerm):
         self.terms = tuple(terms)
 
 
+class AbstractBrownianIncrement:
+    """The quantities a Brownian path returns over an interval
+    (diffrax/_custom_types.py)."""
+
+
+class BrownianIncrement(AbstractBrownianIncrement):
+    """W only."""
+
+
+class SpaceTimeLevyArea(AbstractBrownianIncrement):
+    """W and the space-time Levy area H = (1/h) int (W_{s,r} - (r-s)/h W_{s,t}) dr."""
+
+
 class VirtualBrownianTree:
     """Brownian motion on [t0, t1] discretised to `tol`, evaluated by binary
-    bridge descent (diffrax/_brownian/tree.py:177-354, BrownianIncrement).
+    bridge descent (diffrax/_brownian/tree.py:177-354): with
+    ``levy_area=BrownianIncrement`` the midpoint rule of W alone
+    (tree.py:752-768), with ``levy_area=SpaceTimeLevyArea`` the joint rule of
+    W and the space-time Levy area (tree.py:727-750, 562-603), which ShARK
+    needs and Euler / Heun also accept (they use its W).
 
     `key` is an integer seed of this library's counter-based generator
     (Philox4x32-10); trajectory b of a batch uses its own independent path.
     """
 
     def __init__(self, t0: float, t1: float, tol: float, shape: Sequence[int] | int,
-                 key: int = 0):
+                 key: int = 0, levy_area: type = BrownianIncrement):
         if not t0 < t1:
             raise ValueError("t0 must be strictly less than t1")
+        if levy_area not in (BrownianIncrement, SpaceTimeLevyArea):
+            raise ValueError(f"levy_area must be BrownianIncrement or SpaceTimeLevyArea, "
+                             f"got {levy_area!r}")
         self.t0, self.t1, self.tol = float(t0), float(t1), float(tol)
         self.shape = (shape,) if isinstance(shape, int) else tuple(shape)
         self.key = int(key)
+        self.levy_area = levy_area
 
 
 # ---------------------------------------------------------------------------
@@ -221,6 +242,14 @@ class Tsit5(AbstractSolver):
 class Dopri8(AbstractSolver):
     """diffrax/_solver/dopri8.py:306-353 (analytic fields)."""
     solver_id, _order = 4, 8
+
+
+class ShARK(AbstractSolver):
+    """Shifted Additive-noise Runge-Kutta (diffrax/_solver/shark.py:38-80):
+    two drift evaluations per step, strong order 1.5 for additive noise;
+    needs a VirtualBrownianTree with levy_area=SpaceTimeLevyArea."""
+    solver_id, _order, _strong_order = 5, 2, 1.5
+    minimal_levy_area = SpaceTimeLevyArea
 
 
 # ---------------------------------------------------------------------------

@@ -18,7 +18,7 @@ from . import _lib
 from ._core import (
     RESULT_MESSAGES, RESULTS, AbstractField, BacksolveAdjoint, ClipStepSizeController,
     ConstantStepSize, ControlTerm, Event, LinearCondition, SteadyStateCondition,
-    Euler, MultiTerm, ODETerm, OrnsteinUhlenbeck, PIDController,
+    Euler, MultiTerm, ShARK, SpaceTimeLevyArea, ODETerm, OrnsteinUhlenbeck, PIDController,
     RecursiveCheckpointAdjoint, SaveAt, Solution, VirtualBrownianTree, adjoint_rms_seminorm,
 )
 
@@ -102,7 +102,7 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
              vbt_t1=1.0, vbt_tol=1e-3, seed=0, norm=0, adjoint=0, checkpoints=0,
              schedule=SCHEDULES[schedule], mlp_precision=0,
              save_steps=int(saveat.steps), save_dense=int(saveat.dense), n_step_ts=0,
-             n_jump_ts=0, n_event=0, event_root=0, ev_kind=(), ev_dir=(), pad3=0,
+             n_jump_ts=0, n_event=0, event_root=0, ev_kind=(), ev_dir=(), levy_area=0,
              newton_rtol=1e-5, newton_atol=1e-5, ev_coef=())
     if event is not None:
         f.update(_lower_event(event, stepsize_controller, int(dim)))
@@ -140,7 +140,15 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
             f["diffusion"] = vf.diffusion_id
         else:
             raise NotImplementedError("unsupported diffusion")
-        f.update(vbt_t0=bm.t0, vbt_t1=bm.t1, vbt_tol=bm.tol, seed=bm.key)
+        levy = getattr(bm, "levy_area", None) is SpaceTimeLevyArea
+        f.update(vbt_t0=bm.t0, vbt_t1=bm.t1, vbt_tol=bm.tol, seed=bm.key,
+                 levy_area=int(levy))
+        if isinstance(solver, ShARK) and not levy:
+            # srk.py:374-379
+            raise ValueError("The Brownian increment BrownianIncrement does not have the "
+                             "minimal Levy Area SpaceTimeLevyArea.")
+    elif isinstance(solver, ShARK):
+        raise ValueError("ShARK solves SDEs: terms must be MultiTerm(ODETerm, ControlTerm)")
     if isinstance(adjoint, RecursiveCheckpointAdjoint):
         cp = adjoint.checkpoints
         if cp is None:

@@ -34,7 +34,7 @@ class ProblemDesc(_c.Structure):
         ("block_threads", i32), ("ctas_per_sm", i32), ("mlp_precision", i32),
         ("save_steps", i32), ("save_dense", i32), ("n_step_ts", i32), ("n_jump_ts", i32),
         ("n_event", i32), ("event_root", i32), ("ev_kind", i32 * 4), ("ev_dir", i32 * 4),
-        ("pad3", i32), ("newton_rtol", f64), ("newton_atol", f64), ("ev_coef", f64 * 24),
+        ("levy_area", i32), ("newton_rtol", f64), ("newton_atol", f64), ("ev_coef", f64 * 24),
     ]
 
 
@@ -47,7 +47,7 @@ class FwdExtras(_c.Structure):
 # backsolve norm), the SaveAt(steps/dense) selectors and the clip counts.
 ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:29] + [
     "save_steps", "save_dense", "n_step_ts", "n_jump_ts", "n_event", "event_root", "ev_kind",
-    "ev_dir", "newton_rtol", "newton_atol", "ev_coef"]
+    "ev_dir", "levy_area", "newton_rtol", "newton_atol", "ev_coef"]
 
 _lock = threading.Lock()
 _LIB = None

@@ -184,10 +184,12 @@ static int solver_order(int solver) {
     case GBDX_EULER: return 1;
     case GBDX_HEUN: return 2;
     case GBDX_DOPRI8: return 8;
+    case GBDX_SHARK: return 2;
     default: return 5;
   }
 }
 static double solver_strong_order(int solver) {
+  if (solver == GBDX_SHARK) return 1.5;
   return (solver == GBDX_EULER || solver == GBDX_HEUN) ? 0.5 : 0.0;
 }
 
@@ -195,7 +197,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   if (!desc || !out) return fail(GBDX_ERR_INVALID, "null descriptor or output handle");
   *out = nullptr;
   const gbdx_problem_desc &d = *desc;
-  if (d.solver < GBDX_EULER || d.solver > GBDX_DOPRI8)
+  if (d.solver < GBDX_EULER || d.solver > GBDX_SHARK)
     return fail(GBDX_ERR_INVALID, "unknown solver %d", d.solver);
   if (d.controller != GBDX_CONSTANT && d.controller != GBDX_PID)
     return fail(GBDX_ERR_INVALID, "unknown step size controller %d", d.controller);
@@ -217,6 +219,14 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   if (n_save < 1 && !d.save_dense)
     return fail(GBDX_ERR_INVALID, "Empty saveat -- nothing will be saved.");
   const bool sde = d.diffusion != GBDX_DIFF_NONE;
+  if (d.levy_area != GBDX_LEVY_NONE && d.levy_area != GBDX_LEVY_SPACE_TIME)
+    return fail(GBDX_ERR_INVALID, "unknown levy_area %d", d.levy_area);
+  if (d.levy_area != GBDX_LEVY_NONE && !sde)
+    return fail(GBDX_ERR_INVALID, "levy_area belongs to the Brownian tree of an SDE");
+  // srk.py:374-379: ShARK takes the space-time Levy area of an SDE's tree
+  if (d.solver == GBDX_SHARK && (!sde || d.levy_area != GBDX_LEVY_SPACE_TIME))
+    return fail(GBDX_ERR_INVALID,
+                "ShARK solves SDEs whose Brownian tree has levy_area=SpaceTimeLevyArea");
   // pid.py:437-447: adaptive stepping needs an error estimate.
   if (d.controller == GBDX_PID && d.solver == GBDX_EULER)
     return fail(GBDX_ERR_INVALID,
@@ -304,7 +314,9 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       return fail(GBDX_ERR_UNSUPPORTED,
                   "the Ornstein-Uhlenbeck SDE runs with FP32 state (FP32 Brownian tree)");
     }
-    p->ode = gbdx::find_ode_sde_entry_f32(d.solver, d.dim);
+    p->ode = d.levy_area == GBDX_LEVY_SPACE_TIME
+                 ? gbdx::find_ode_sde_levy_entry_f32(d.solver, d.dim)
+                 : gbdx::find_ode_sde_entry_f32(d.solver, d.dim);
     if (!p->ode.launch) {
       delete p;
       return fail(GBDX_ERR_UNSUPPORTED,
@@ -316,6 +328,11 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     if (d.solver == GBDX_DOPRI8) {
       delete p;
       return fail(GBDX_ERR_UNSUPPORTED, "Dopri8 is available for the analytic fields");
+    }
+    if (d.levy_area != GBDX_LEVY_NONE) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED,
+                  "the space-time Levy area tree (and ShARK) drive the Ornstein-Uhlenbeck SDE");
     }
     if (d.mlp_depth != 3 || w[0] != d.dim || w[3] != d.dim || w[1] != w[2]) {
       delete p;

@@ -157,6 +157,23 @@ struct Tab<GBDX_HEUN> {
   __host__ __device__ static constexpr double e(int j) { return j == 0 ? 0.5 : -0.5; }
 };
 
+// ShARK (shark.py:10-35): the drift rows of the additive-noise stochastic
+// Runge--Kutta tableau; the W and H coefficients (a^W = (0, 5/6), a^H =
+// (1, 1), b^W = 1, b^H = 0) enter in Traj::step.
+template <>
+struct Tab<GBDX_SHARK> {
+  static constexpr int S = 2;
+  static constexpr bool FSAL = false, SSAL = false;
+  static constexpr int ORDER = 2;
+  static constexpr double STRONG_ORDER = 1.5;
+  __host__ __device__ static constexpr double c(int i) { return i == 0 ? 0.0 : 5.0 / 6.0; }
+  __host__ __device__ static constexpr double a(int i, int j) {
+    return (i == 1 && j == 0) ? 5.0 / 6.0 : 0.0;
+  }
+  __host__ __device__ static constexpr double b(int j) { return j == 0 ? 0.4 : 0.6; }
+  __host__ __device__ static constexpr double e(int j) { return j == 0 ? -0.6 : 0.6; }
+};
+
 template <>
 struct Tab<GBDX_EULER> {
   static constexpr int S = 1;
@@ -346,16 +363,28 @@ struct OrnsteinUhlenbeck {
 // Ornstein-Uhlenbeck SDE: the drift above with the diagonal diffusion sigma of
 // a ControlTerm driven by the virtual Brownian tree (dy = theta (mu - y) dt +
 // sigma dW, _term.py:271-555 with a diagonal operator).  Brownian values come
-// in pairs of components, so D is even.
-template <class T, int D_>
+// in pairs of components, so D is even.  LEVY_ selects the tree with
+// space-time Levy area (levy_area=SpaceTimeLevyArea), which ShARK needs.
+template <class T, int D_, bool LEVY_ = false>
 struct OrnsteinUhlenbeckSDE : OrnsteinUhlenbeck<T, D_> {
   static_assert(D_ % 2 == 0, "the Brownian tree draws components in pairs");
   static constexpr bool SDE = true;
+  static constexpr bool LEVY = LEVY_;
   __device__ static __forceinline__ void sigma(const SolveParams &, const T *a, const T *,
                                                T *s) {
 #pragma unroll
     for (int i = 0; i < D_; i++) s[i] = a[2];
   }
+};
+
+// Whether a field's Brownian tree carries the space-time Levy area.
+template <class F, class = void>
+struct FieldLevy {
+  static constexpr bool value = false;
+};
+template <class F>
+struct FieldLevy<F, decltype(void(F::LEVY))> {
+  static constexpr bool value = F::LEVY;
 };
 
 // ---------------------------------------------------------------------------

@@ -56,6 +56,7 @@ OdeEntry find_ode_entry_t(int solver, int field, int dim) {
 }
 
 // The Ornstein-Uhlenbeck SDE (FP32 state: the tree's values are FP32).
+template <bool LEVY>
 inline OdeEntry find_ode_sde_entry_t(int solver, int dim) {
 #define GBDX_ENTRY(S, F) \
   OdeEntry { &launch_ode<S, F, float, false>, &occupancy_ode<S, F, float, false> }
@@ -65,10 +66,13 @@ inline OdeEntry find_ode_sde_entry_t(int solver, int dim) {
     case GBDX_HEUN: return GBDX_ENTRY(GBDX_HEUN, F);           \
     case GBDX_DOPRI5: return GBDX_ENTRY(GBDX_DOPRI5, F);       \
     case GBDX_TSIT5: return GBDX_ENTRY(GBDX_TSIT5, F);         \
+    case GBDX_SHARK:                                           \
+      if constexpr (LEVY) return GBDX_ENTRY(GBDX_SHARK, F);    \
+      return OdeEntry{nullptr, nullptr};                       \
     default: return OdeEntry{nullptr, nullptr};                \
   }
-  using OU2 = OrnsteinUhlenbeckSDE<float, 2>;
-  using OU4 = OrnsteinUhlenbeckSDE<float, 4>;
+  using OU2 = OrnsteinUhlenbeckSDE<float, 2, LEVY>;
+  using OU4 = OrnsteinUhlenbeckSDE<float, 4, LEVY>;
   if (dim == 2) { GBDX_SOLVERS(OU2) }
   if (dim == 4) { GBDX_SOLVERS(OU4) }
 #undef GBDX_SOLVERS

@@ -3,5 +3,7 @@
 #include "gbdx_ode_impl.cuh"
 
 namespace gbdx {
-OdeEntry find_ode_sde_entry_f32(int solver, int dim) { return find_ode_sde_entry_t(solver, dim); }
+OdeEntry find_ode_sde_entry_f32(int solver, int dim) {
+  return find_ode_sde_entry_t<false>(solver, dim);
+}
 }  // namespace gbdx

@@ -129,6 +129,8 @@ struct Traj {
   static constexpr int S = TB::S;
   static constexpr int NA = FIELD::NARGS > 0 ? FIELD::NARGS : 1;
   static constexpr bool F32 = sizeof(T) == 4;
+  static constexpr bool LEVY = FieldLevy<FIELD>::value;
+  static_assert(SOLVER != GBDX_SHARK || LEVY, "ShARK needs the space-time Levy area");
 
   T y[D];
   T f0[D];  // FSAL: f(t_n, y_n) from the last stage of the previous step
@@ -157,6 +159,10 @@ struct Traj {
   double tfin;
   int64_t idx;
   T wb[FIELD::SDE ? D : 1];  // SDE: W(tprev) of every component (FP32 fields only)
+  // Levy area tree: wb holds W_unit(r) and hb bar H_unit(r) at the unit time
+  // rb of tprev (unscaled, for Chen's relation)
+  T hb[LEVY ? D : 1];
+  float rb;
 
   __device__ __forceinline__ bool running(const SolveParams &P) const {
     return live && result == GBDX_SUCCESSFUL && nsteps < P.max_steps;
@@ -210,7 +216,18 @@ struct Traj {
     live = a < b;
     tprev = a;
     floor1 = t1_clip_floor(b);
-    if constexpr (FIELD::SDE) {
+    if constexpr (LEVY) {
+      rb = float((a * dir - P.vbt_t0) * P.vbt_inv_len);
+#pragma unroll
+      for (int n = 0; n < D; n += 2) {
+        float2 w, hh;
+        vbt_levy_pair(P, i, rb, n, w, hh);
+        wb[n] = w.x;
+        wb[n + 1] = w.y;
+        hb[n] = hh.x;
+        hb[n + 1] = hh.y;
+      }
+    } else if constexpr (FIELD::SDE) {
 #pragma unroll
       for (int n = 0; n < D; n += 2) {
         const float2 w = vbt_w_pair(P, i, a * dir, n);
@@ -429,7 +446,35 @@ struct Traj {
     T k[S][D];
     T f[D], yi[D], y1[D], err[D], flast[D];
     T dw[FIELD::SDE ? D : 1], wn[FIELD::SDE ? D : 1], sg[FIELD::SDE ? D : 1];
-    if constexpr (FIELD::SDE) {
+    T dh[LEVY ? D : 1], hn[LEVY ? D : 1];
+    float rn = 0.f;
+    if constexpr (LEVY) {
+      // (W, H) over the loop's step from the tree's values at its two ends
+      // by Chen's relation (_levy_diff, tree.py:94-126), scaled by sqrt(T)
+      // (tree.py:303-323).  The WrapTerm evaluates the forward real interval
+      // and multiplies W and H by the direction (_term.py:742-745): W_b - W_a
+      // either way, and H is dir times the relation's value for (a, b).
+      rn = float((tnext * dir - P.vbt_t0) * P.vbt_inv_len);
+      const float su = rn - rb;
+      const float inv = fabsf(su) < 1.1920929e-7f ? 0.f : 1.0f / su;
+      const float sq = P.vbt_sqrt_len, sqh = dir > 0 ? sq : -sq;
+#pragma unroll
+      for (int n = 0; n < D; n += 2) {
+        float2 w, hh;
+        vbt_levy_pair(P, idx, rn, n, w, hh);
+        wn[n] = w.x;
+        wn[n + 1] = w.y;
+        hn[n] = hh.x;
+        hn[n + 1] = hh.y;
+      }
+#pragma unroll
+      for (int n = 0; n < D; n++) {
+        const float u_bb_s = rn * wb[n] - rb * wn[n];
+        const float bhh_su = hn[n] - hb[n] - 0.5f * u_bb_s;
+        dw[n] = sq * (wn[n] - wb[n]);
+        dh[n] = sqh * (inv * bhh_su);
+      }
+    } else if constexpr (FIELD::SDE) {
       // Brownian increment over [tprev, tnext] (ControlTerm, _term.py:420-427)
 #pragma unroll
       for (int n = 0; n < D; n += 2) {
@@ -440,73 +485,106 @@ struct Traj {
         dw[n + 1] = w.y - wb[n + 1];
       }
     }
-    // Stage 0: FSAL reuse except on the first step (runge_kutta.py:684-700).
-    if (TB::FSAL && !first) {
-#pragma unroll
-      for (int n = 0; n < D; n++) f[n] = f0[n];
-    } else {
-      FIELD::vf(P, args, y, f);
-    }
-    if constexpr (FIELD::SDE) {
+    if constexpr (SOLVER == GBDX_SHARK) {
+      // ShARK, the additive-noise branch of AbstractSRK.step (srk.py:335-671):
+      //   z_0 = y0 + g H,  z_1 = y0 + 5/6 h f_0 + g (5/6 W + H),
+      //   y1 = y0 + h (0.4 f_0 + 0.6 f_1) + g W,  err = h (0.6 f_1 - 0.6 f_0),
+      // with g = g(t0) (the Ornstein-Uhlenbeck diffusion is constant, so the
+      // correction 0.5 (g(t1) - g(t0)) (W - 2H) of srk.py:607-618 is zero).
+      // The drift's control is the loop's step t1 - t0 (srk.py:364, given to
+      // vf_prod, which the WrapTerm does not flip).
+      const T hl = dir > 0 ? h : -h;
+      T gw[D], gh[D];
       FIELD::sigma(P, args, y, sg);
 #pragma unroll
-      for (int n = 0; n < D; n++) k[0][n] = f[n] * h + sg[n] * dw[n];
-    } else {
-#pragma unroll
-      for (int n = 0; n < D; n++) k[0][n] = f[n] * h;
-    }
-#pragma unroll
-    for (int i = 1; i < S; i++) {
-#pragma unroll
       for (int n = 0; n < D; n++) {
-        if constexpr (F32) {
-          // y0 first, newest stage last: only one FMA waits on k_{i-1}.
-          T acc = y[n];
-#pragma unroll
-          for (int j = 0; j < i; j++)
-            if (TB::a(i, j) != 0.0) acc = fmaf(T(TB::a(i, j)), k[j][n], acc);
-          yi[n] = acc;
-        } else {
-          // Reference order: increment first, then y0 (runge_kutta.py:866-871).
-          T inc = T(0);
-#pragma unroll
-          for (int j = 0; j < i; j++)
-            if (TB::a(i, j) != 0.0) inc += T(TB::a(i, j)) * k[j][n];
-          yi[n] = y[n] + inc;
-        }
+        gw[n] = sg[n] * dw[n];
+        gh[n] = sg[n] * dh[n];
+        yi[n] = y[n] + gh[n];
       }
       FIELD::vf(P, args, yi, f);
+#pragma unroll
+      for (int n = 0; n < D; n++) {
+        k[0][n] = f[n] * hl;
+        yi[n] = (y[n] + T(5.0 / 6.0) * k[0][n]) + (T(5.0 / 6.0) * gw[n] + gh[n]);
+      }
+      FIELD::vf(P, args, yi, f);
+#pragma unroll
+      for (int n = 0; n < D; n++) {
+        k[1][n] = f[n] * hl;
+        y1[n] = (y[n] + (T(0.4) * k[0][n] + T(0.6) * k[1][n])) + gw[n];
+        const T e = T(-0.6) * k[0][n] + T(0.6) * k[1][n];
+        err[n] = is_nan_(e) ? T(INFINITY) : e;
+      }
+    } else {
+      // Stage 0: FSAL reuse except on the first step (runge_kutta.py:684-700).
+      if (TB::FSAL && !first) {
+#pragma unroll
+        for (int n = 0; n < D; n++) f[n] = f0[n];
+      } else {
+        FIELD::vf(P, args, y, f);
+      }
       if constexpr (FIELD::SDE) {
-        FIELD::sigma(P, args, yi, sg);
+        FIELD::sigma(P, args, y, sg);
 #pragma unroll
-        for (int n = 0; n < D; n++) k[i][n] = f[n] * h + sg[n] * dw[n];
+        for (int n = 0; n < D; n++) k[0][n] = f[n] * h + sg[n] * dw[n];
       } else {
 #pragma unroll
-        for (int n = 0; n < D; n++) k[i][n] = f[n] * h;
+        for (int n = 0; n < D; n++) k[0][n] = f[n] * h;
       }
-      if (i == S - 1) {
 #pragma unroll
-        for (int n = 0; n < D; n++) flast[n] = f[n];
+      for (int i = 1; i < S; i++) {
+#pragma unroll
+        for (int n = 0; n < D; n++) {
+          if constexpr (F32) {
+            // y0 first, newest stage last: only one FMA waits on k_{i-1}.
+            T acc = y[n];
+#pragma unroll
+            for (int j = 0; j < i; j++)
+              if (TB::a(i, j) != 0.0) acc = fmaf(T(TB::a(i, j)), k[j][n], acc);
+            yi[n] = acc;
+          } else {
+            // Reference order: increment first, then y0 (runge_kutta.py:866-871).
+            T inc = T(0);
+#pragma unroll
+            for (int j = 0; j < i; j++)
+              if (TB::a(i, j) != 0.0) inc += T(TB::a(i, j)) * k[j][n];
+            yi[n] = y[n] + inc;
+          }
+        }
+        FIELD::vf(P, args, yi, f);
+        if constexpr (FIELD::SDE) {
+          FIELD::sigma(P, args, yi, sg);
+#pragma unroll
+          for (int n = 0; n < D; n++) k[i][n] = f[n] * h + sg[n] * dw[n];
+        } else {
+#pragma unroll
+          for (int n = 0; n < D; n++) k[i][n] = f[n] * h;
+        }
+        if (i == S - 1) {
+#pragma unroll
+          for (int n = 0; n < D; n++) flast[n] = f[n];
+        }
       }
-    }
-    // y1 (SSAL: the last stage's input, runge_kutta.py:1177-1185) and the
-    // embedded error estimate (:1186-1197).
+      // y1 (SSAL: the last stage's input, runge_kutta.py:1177-1185) and the
+      // embedded error estimate (:1186-1197).
 #pragma unroll
-    for (int n = 0; n < D; n++) {
-      if constexpr (TB::SSAL) {
-        y1[n] = yi[n];
-      } else {
-        T inc = T(0);
+      for (int n = 0; n < D; n++) {
+        if constexpr (TB::SSAL) {
+          y1[n] = yi[n];
+        } else {
+          T inc = T(0);
 #pragma unroll
-        for (int j = 0; j < S; j++) inc += T(TB::b(j)) * k[j][n];
-        y1[n] = y[n] + inc;
+          for (int j = 0; j < S; j++) inc += T(TB::b(j)) * k[j][n];
+          y1[n] = y[n] + inc;
+        }
+        T e = T(0);
+#pragma unroll
+        for (int j = 0; j < S; j++)
+          if (TB::e(j) != 0.0) e += T(TB::e(j)) * k[j][n];
+        err[n] = is_nan_(e) ? T(INFINITY) : e;
       }
-      T e = T(0);
-#pragma unroll
-      for (int j = 0; j < S; j++)
-        if (TB::e(j) != 0.0) e += T(TB::e(j)) * k[j][n];
-      err[n] = is_nan_(e) ? T(INFINITY) : e;
-    }
+    }  // explicit RK stages
 
     if constexpr (F32) {
       if (pend) {
@@ -737,6 +815,11 @@ struct Traj {
       if constexpr (FIELD::SDE) {
 #pragma unroll
         for (int n = 0; n < D; n++) wb[n] = wn[n];
+      }
+      if constexpr (LEVY) {
+#pragma unroll
+        for (int n = 0; n < D; n++) hb[n] = hn[n];
+        rb = rn;
       }
       if (TB::FSAL) {
 #pragma unroll

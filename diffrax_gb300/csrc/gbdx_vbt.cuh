@@ -1,4 +1,5 @@
-// gbdx_vbt.cuh -- device virtual Brownian tree (BrownianIncrement).
+// gbdx_vbt.cuh -- device virtual Brownian tree (BrownianIncrement, and
+// SpaceTimeLevyArea in vbt_levy_pair).
 //
 // W(t) on [vbt_t0, vbt_t0 + T] by binary bridge descent from a counter-based
 // generator, as VirtualBrownianTree._evaluate_leaf (diffrax/_brownian/
@@ -30,7 +31,7 @@ __device__ __forceinline__ void philox4x32_10(uint32_t (&c)[4], uint32_t k0, uin
   }
 }
 
-enum { kVbtRoot = 0, kVbtMid = 1, kVbtLeaf = 2 };
+enum { kVbtRoot = 0, kVbtMid = 1, kVbtLeaf = 2, kVbtRootH = 3, kVbtMidH = 4, kVbtLeafH = 5 };
 
 // Normals of dimensions (col, col + 1), col even, for one tree node.
 __device__ __forceinline__ float2 vbt_normal_pair(uint64_t seed, uint32_t traj, uint32_t node,
@@ -209,6 +210,76 @@ static __device__ __noinline__ float4 vbt_w_quad(const SolveParams &P, int64_t t
   const float sq = P.vbt_sqrt_len;
   return make_float4(sq * (ws[0] + f * wsu[0] + bb * z.x), sq * (ws[1] + f * wsu[1] + bb * z.y),
                      sq * (ws[2] + f * wsu[2] + bb * z.z), sq * (ws[3] + f * wsu[3] + bb * z.w));
+}
+
+// The tree with space-time Levy area: W_unit(r) and bar H_unit(r) = r H_{0,r}
+// at unit time r for dimensions (col, col + 1), col even, unscaled (the caller
+// combines two points by Chen's relation and scales by sqrt(T)).  The descent
+// carries W and bar H of each dyadic interval: root W_1 ~ N(0, 1), bar H_1 ~
+// N(0, 1/12) (tree.py:389-394); midpoint rule tree.py:727-750; final bridge
+// tree.py:562-603.  The kVbt*H draws feed bar H, the others W, as in the
+// FP64 oracle.
+static __device__ __noinline__ void vbt_levy_pair(const SolveParams &P, int64_t traj, float r, int col,
+                                                  float2 &w_r, float2 &bhh_r) {
+  const float tol = float(P.vbt_tol_unit);
+  const uint32_t tj = uint32_t(traj);
+  const float2 z0 = vbt_normal_pair(P.seed, tj, 0u, kVbtRoot, col);
+  const float2 n0 = vbt_normal_pair(P.seed, tj, 0u, kVbtRootH, col);
+  float ws[2] = {0.f, 0.f}, wsu[2] = {z0.x, z0.y};
+  float hs[2] = {0.f, 0.f};
+  const float inv_sqrt12 = 0.28867513459481287f;
+  float hsu[2] = {n0.x * inv_sqrt12, n0.y * inv_sqrt12};
+  float s = 0.f, su = 1.f;
+  uint32_t node = 1;
+  while (su > tol) {  // while 2^-level > tol (tree.py:406-409)
+    const float st = 0.5f * su, t_mid = s + st;
+    const float2 z1 = vbt_normal_pair(P.seed, tj, node, kVbtMid, col);
+    const float2 z2 = vbt_normal_pair(P.seed, tj, node, kVbtMidH, col);
+    const float zs = 0.25f * sqrtf(su), ns = sqrtf(su * (1.0f / 12.0f));
+    const float c3 = 1.5f / su, q = 0.25f * su;
+    const bool right = r > t_mid;
+    const float zz1[2] = {z1.x, z1.y}, zz2[2] = {z2.x, z2.y};
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      const float z = zz1[i] * zs, n = zz2[i] * ns;
+      const float wt1 = 0.5f * wsu[i], wt2 = c3 * hsu[i] + z;
+      const float ht1 = 0.125f * hsu[i] - q * z, ht2 = q * n;
+      if (right) {
+        const float w_t = ws[i] + (wt1 + wt2);
+        hs[i] = hs[i] + (ht1 + ht2) + 0.5f * (t_mid * ws[i] - s * w_t);
+        ws[i] = w_t;
+        wsu[i] = wt1 - wt2;
+        hsu[i] = ht1 - ht2;
+      } else {
+        wsu[i] = wt1 + wt2;
+        hsu[i] = ht1 + ht2;
+      }
+    }
+    if (right) s = t_mid;
+    node = 2 * node + (right ? 1u : 0u);
+    su = st;
+  }
+  const float sr = fmaxf(r - s, 0.f), ru = fmaxf(su - sr, 0.f);
+  const float2 x1 = vbt_normal_pair(P.seed, tj, node, kVbtLeaf, col);
+  const float2 x2 = vbt_normal_pair(P.seed, tj, node, kVbtLeafH, col);
+  const float sr3 = sr * sr * sr, ru3 = ru * ru * ru, su3 = su * su * su;
+  const float dd = sqrtf(sr3 + ru3);
+  const float sr_ru_half = sqrtf(sr * ru);
+  const float d_prime = 1.0f / (2.0f * su * dd);
+  const float a = d_prime * sr3 * sr_ru_half, b = d_prime * ru3 * sr_ru_half;
+  const float c = sqrtf(3.0f * sr3 * ru3) / (6.0f * dd);
+  const float fw = sr / su, fh = 6.0f * sr * ru / su3, fx = 2.0f * (a + b) / su, fb = sr3 / su3;
+  const float xx1[2] = {x1.x, x1.y}, xx2[2] = {x2.x, x2.y};
+  float wo[2], ho[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    const float w_sr = fw * wsu[i] + fh * hsu[i] + fx * xx1[i];
+    wo[i] = ws[i] + w_sr;
+    const float bhh_sr = fb * hsu[i] - a * xx1[i] + c * xx2[i];
+    ho[i] = hs[i] + bhh_sr + 0.5f * (r * ws[i] - s * wo[i]);
+  }
+  w_r = make_float2(wo[0], wo[1]);
+  bhh_r = make_float2(ho[0], ho[1]);
 }
 
 }  // namespace gbdx

@@ -38,15 +38,20 @@
 extern "C" {
 #endif
 
-/* Solvers (diffrax/_solver/{euler,heun,dopri5,tsit5,dopri8}.py); Dopri8 on the
- * analytic fields. */
+/* Solvers (diffrax/_solver/{euler,heun,dopri5,tsit5,dopri8,shark}.py); Dopri8
+ * on the analytic fields; ShARK (the additive-noise stochastic Runge--Kutta
+ * method, srk.py:335-671) on the Ornstein--Uhlenbeck SDE with a space-time
+ * Levy area tree. */
 enum gbdx_solver {
   GBDX_EULER = 0,
   GBDX_HEUN = 1,
   GBDX_DOPRI5 = 2,
   GBDX_TSIT5 = 3,
-  GBDX_DOPRI8 = 4
+  GBDX_DOPRI8 = 4,
+  GBDX_SHARK = 5
 };
+/* Levy area drawn by the virtual Brownian tree (diffrax/_custom_types.py). */
+enum gbdx_levy_area { GBDX_LEVY_NONE = 0, GBDX_LEVY_SPACE_TIME = 1 };
 /* Step size controllers (diffrax/_step_size_controller/{constant,pid}.py). */
 enum gbdx_controller { GBDX_CONSTANT = 0, GBDX_PID = 1 };
 /* Registered vector fields. */
@@ -156,7 +161,10 @@ typedef struct gbdx_problem_desc {
    * gbdx_solve_fwd_ex to read which condition fired. */
   int32_t n_event, event_root;
   int32_t ev_kind[GBDX_MAX_EVENTS], ev_dir[GBDX_MAX_EVENTS];
-  int32_t pad3;
+  /* The VirtualBrownianTree's levy_area (gbdx_levy_area): SPACE_TIME draws the
+   * space-time Levy area H beside W (diffrax/_brownian/tree.py:562-603,
+   * 727-750); GBDX_SHARK needs it, Euler and Heun use its W. */
+  int32_t levy_area;
   double newton_rtol, newton_atol;
   double ev_coef[6 * GBDX_MAX_EVENTS];
 } gbdx_problem_desc;

@@ -20,7 +20,8 @@ import numpy as np
 from .build import build_oracle, oracle_lib_path
 
 __all__ = [
-    "OracleDesc", "load", "solve", "grad_recursive", "vbt_increments", "normal4",
+    "OracleDesc", "load", "solve", "grad_recursive", "vbt_increments", "vbt_levy_increments",
+    "vbt_levy_points", "normal4", "SHARK",
     "dense_evaluate", "n_saves", "STAGES", "clip_times", "clip_find", "clip_adapt",
     "EULER", "HEUN", "DOPRI5", "TSIT5", "DOPRI8", "CONSTANT", "PID",
     "LOTKA_VOLTERRA", "VAN_DER_POL", "ORNSTEIN_UHLENBECK", "MLP", "LINEAR", "CALLBACK",
@@ -28,7 +29,7 @@ __all__ = [
     "EV_STEADY", "EV_EITHER", "EV_UP", "EV_DOWN",
 ]
 
-EULER, HEUN, DOPRI5, TSIT5, DOPRI8 = 0, 1, 2, 3, 4
+EULER, HEUN, DOPRI5, TSIT5, DOPRI8, SHARK = 0, 1, 2, 3, 4, 5
 CONSTANT, PID = 0, 1
 LOTKA_VOLTERRA, VAN_DER_POL, ORNSTEIN_UHLENBECK, MLP, LINEAR, CALLBACK = 0, 1, 2, 3, 4, 5
 DIFF_NONE, DIFF_OU, DIFF_TANH_DIAG = 0, 1, 2
@@ -60,7 +61,8 @@ class OracleDesc(ctypes.Structure):
         ("save_dense", ctypes.c_int32), ("n_step_ts", ctypes.c_int32),
         ("n_jump_ts", ctypes.c_int32), ("n_event", ctypes.c_int32),
         ("event_root", ctypes.c_int32), ("ev_kind", ctypes.c_int32 * 4),
-        ("ev_dir", ctypes.c_int32 * 4), ("newton_rtol", ctypes.c_double),
+        ("ev_dir", ctypes.c_int32 * 4), ("levy_area", ctypes.c_int32),
+        ("newton_rtol", ctypes.c_double),
         ("newton_atol", ctypes.c_double), ("ev_coef", ctypes.c_double * 24),
     ]
 
@@ -73,9 +75,9 @@ _DEFAULTS = dict(solver=TSIT5, controller=PID, field=LOTKA_VOLTERRA, dim=2,
                  mlp_widths=(), diffusion=DIFF_NONE, vbt_t0=0.0, vbt_t1=1.0,
                  vbt_tol=1e-3, seed=0, norm=0, save_steps=0, save_dense=0,
                  n_step_ts=0, n_jump_ts=0, n_event=0, event_root=0, ev_kind=(), ev_dir=(),
-                 newton_rtol=1e-5, newton_atol=1e-5, ev_coef=())
+                 levy_area=0, newton_rtol=1e-5, newton_atol=1e-5, ev_coef=())
 
-STAGES = {EULER: 1, HEUN: 2, DOPRI5: 7, TSIT5: 7, DOPRI8: 14}
+STAGES = {EULER: 1, HEUN: 2, DOPRI5: 7, TSIT5: 7, DOPRI8: 14, SHARK: 2}
 
 
 def n_saves(desc) -> int:
@@ -153,6 +155,10 @@ def load():
     lib.orc_backsolve.restype = ctypes.c_int
     lib.orc_vbt_increments.argtypes = [ctypes.POINTER(OracleDesc), i64,
                                        ctypes.POINTER(ctypes.c_uint32), dp, dp, dp]
+    lib.orc_vbt_levy_increments.argtypes = [ctypes.POINTER(OracleDesc), i64,
+                                            ctypes.POINTER(ctypes.c_uint32), dp, dp, dp, dp]
+    lib.orc_vbt_levy_points.argtypes = [ctypes.POINTER(OracleDesc), i64,
+                                        ctypes.POINTER(ctypes.c_uint32), dp, dp, dp]
     lib.orc_normal4.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.c_uint32, ctypes.c_uint32, dp]
     lib.orc_desc_size.restype = ctypes.c_int
@@ -401,6 +407,34 @@ def vbt_increments(desc: OracleDesc, traj, ta, tb):
                            traj.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
                            _dptr(ta), _dptr(tb), _dptr(out))
     return out
+
+
+def vbt_levy_increments(desc: OracleDesc, traj, ta, tb):
+    """(W, H) of [ta, tb] from the oracle's tree with space-time Levy area
+    (VirtualBrownianTree.evaluate(ta, tb, use_levy=True))."""
+    lib = load()
+    traj = np.ascontiguousarray(traj, dtype=np.uint32)
+    ta = _f64(ta)
+    tb = _f64(tb)
+    w = np.empty((traj.size, desc.dim))
+    h = np.empty((traj.size, desc.dim))
+    lib.orc_vbt_levy_increments(ctypes.byref(desc), traj.size,
+                                traj.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                _dptr(ta), _dptr(tb), _dptr(w), _dptr(h))
+    return w, h
+
+
+def vbt_levy_points(desc: OracleDesc, traj, r):
+    """W(r) and bar H(r) = r H_{0,r} of the Levy area tree on the unit interval."""
+    lib = load()
+    traj = np.ascontiguousarray(traj, dtype=np.uint32)
+    r = _f64(r)
+    w = np.empty((traj.size, desc.dim))
+    h = np.empty((traj.size, desc.dim))
+    lib.orc_vbt_levy_points(ctypes.byref(desc), traj.size,
+                            traj.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                            _dptr(r), _dptr(w), _dptr(h))
+    return w, h
 
 
 def normal4(seed, traj, node, kind, q):

@@ -23,8 +23,11 @@
  *                           686-821 (root find and unsave), 847-877, with
  *                           optimistix.Newton (cauchy termination) restated
  *   terms ................. diffrax/_term.py:174-226, 271-555, 666-764
- *   virtual Brownian tree . diffrax/_brownian/tree.py:245-354, 366-448,
- *                           607-621, 626-773 (BrownianIncrement branch)
+ *   virtual Brownian tree . diffrax/_brownian/tree.py:94-126, 245-354, 366-448,
+ *                           562-621, 626-773 (BrownianIncrement and
+ *                           SpaceTimeLevyArea branches)
+ *   ShARK ................. diffrax/_solver/shark.py:10-35 with the additive-
+ *                           noise step of diffrax/_solver/srk.py:335-671
  *   gradients ............. diffrax/_adjoint.py:179-312 (discretise-then-
  *                           optimise: exact VJP of the accepted-step map with
  *                           the controller under stop_gradient, pid.py:374,
@@ -33,6 +36,7 @@
  *
  * Built with -ffp-contract=off so that x86-64 and aarch64 give identical bits.
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -41,7 +45,8 @@
 #include <omp.h>
 #endif
 
-enum { ORC_EULER = 0, ORC_HEUN = 1, ORC_DOPRI5 = 2, ORC_TSIT5 = 3, ORC_DOPRI8 = 4 };
+enum { ORC_EULER = 0, ORC_HEUN = 1, ORC_DOPRI5 = 2, ORC_TSIT5 = 3, ORC_DOPRI8 = 4,
+       ORC_SHARK = 5 };
 #define ORC_MAX_S 14 /* most stages of a tableau (Dopri8) */
 enum { ORC_CONSTANT = 0, ORC_PID = 1 };
 enum {
@@ -103,6 +108,8 @@ typedef struct {
    * event time by Newton's method with newton_rtol / newton_atol. */
   int32_t n_event, event_root;
   int32_t ev_kind[ORC_MAX_EVENTS], ev_dir[ORC_MAX_EVENTS];
+  /* the tree's Levy area: 0 = BrownianIncrement, 1 = SpaceTimeLevyArea */
+  int32_t levy_area;
   double newton_rtol, newton_atol;
   double ev_coef[6 * ORC_MAX_EVENTS];
 } orc_desc;
@@ -121,7 +128,7 @@ typedef struct {
   double strong_order;
 } Tableau;
 
-static Tableau TSIT5, DOPRI5, DOPRI8, HEUN, EULER;
+static Tableau TSIT5, DOPRI5, DOPRI8, HEUN, EULER, SHARK;
 /* Dopri8 (dopri8.py:18-189): Prince and Dormand's 8(7) pair, 14 stages,
  * FSAL and SSAL; published method constants as exact rational quotients. */
 static const double DOPRI8_A[13][ORC_MAX_S] = {
@@ -247,6 +254,13 @@ static void init_tableaus(void) {
 
   memset(&EULER, 0, sizeof EULER);
   EULER.s = 1; EULER.order = 1; EULER.strong_order = 0.5; EULER.b[0] = 1.0;
+
+  /* ShARK (shark.py:10-35): the drift rows; the W and H coefficients of the
+   * additive-noise stages are in shark_step. */
+  memset(&SHARK, 0, sizeof SHARK);
+  SHARK.s = 2; SHARK.order = 2; SHARK.strong_order = 1.5;
+  SHARK.c[1] = 5.0 / 6.0; SHARK.a[1][0] = 5.0 / 6.0;
+  SHARK.b[0] = 0.4; SHARK.b[1] = 0.6; SHARK.e[0] = -0.6; SHARK.e[1] = 0.6;
   done = 1;
 }
 
@@ -256,6 +270,7 @@ static const Tableau *tableau_of(int solver) {
     case ORC_HEUN: return &HEUN;
     case ORC_DOPRI5: return &DOPRI5;
     case ORC_DOPRI8: return &DOPRI8;
+    case ORC_SHARK: return &SHARK;
     default: return &TSIT5;
   }
 }
@@ -357,6 +372,111 @@ static void vbt_increment(const orc_desc *d, uint32_t traj, double ta, double tb
   vbt_eval_unit(d->seed, traj, tol_unit, rb, d->dim, wb);
   double sq = sqrt(T);
   for (int i = 0; i < d->dim; i++) dw[i] = sq * (wb[i] - wa[i]);
+}
+
+/* The tree with space-time Levy area (levy_area = SpaceTimeLevyArea): the
+ * descent carries W and bar H (bar H_{s,u} = (u - s) H_{s,u}) of each dyadic
+ * interval.  Root: W_1 ~ N(0, 1), bar H_1 ~ N(0, 1/12) (tree.py:389-394);
+ * midpoint rule tree.py:727-750 (Foster's thesis, Theorem 6.1.4 bridge);
+ * final bridge to r tree.py:562-603.  Draws: VBT_ROOT / VBT_MID / VBT_LEAF
+ * feed W (z1, x1), the _H kinds feed bar H (z2, x2). */
+enum { VBT_ROOT_H = 3, VBT_MID_H = 4, VBT_LEAF_H = 5 };
+
+static void vbt_levy_eval_unit(uint64_t seed, uint32_t traj, double tol_unit, double r,
+                               int dim, double *w_r, double *bhh_r) {
+  double ws[64], wsu[64], hs[64], hsu[64], z1[64], z2[64];
+  int level = 0;
+  double s = 0.0;
+  uint32_t node = 1;
+  normals(seed, traj, 0, VBT_ROOT, dim, z1);
+  normals(seed, traj, 0, VBT_ROOT_H, dim, z2);
+  for (int i = 0; i < dim; i++) {
+    ws[i] = 0.0; wsu[i] = z1[i];
+    hs[i] = 0.0; hsu[i] = z2[i] / sqrt(12.0);
+  }
+  while (ldexp(1.0, -level) > tol_unit) {
+    double su = ldexp(1.0, -level);
+    double st = su / 2;
+    double t = s + st;
+    double root_su = sqrt(su);
+    normals(seed, traj, node, VBT_MID, dim, z1);
+    normals(seed, traj, node, VBT_MID_H, dim, z2);
+    int right = r > t;
+    for (int i = 0; i < dim; i++) {
+      double z = z1[i] * (root_su / 4);
+      double n = z2[i] * sqrt(su / 12);
+      double w_term1 = wsu[i] / 2;
+      double w_term2 = (3 / (2 * su)) * hsu[i] + z;
+      double w_st = w_term1 + w_term2, w_tu = w_term1 - w_term2;
+      double h_term1 = hsu[i] / 8 - su / 4 * z;
+      double h_term2 = (su / 4) * n;
+      double h_st = h_term1 + h_term2, h_tu = h_term1 - h_term2;
+      double w_t = ws[i] + w_st;
+      double h_t = hs[i] + h_st + 0.5 * (t * ws[i] - s * w_t);
+      if (right) { ws[i] = w_t; wsu[i] = w_tu; hs[i] = h_t; hsu[i] = h_tu; }
+      else { wsu[i] = w_st; hsu[i] = h_st; }
+    }
+    if (right) s = t;
+    node = 2 * node + (uint32_t)right;
+    level++;
+  }
+  double su = ldexp(1.0, -level);
+  double sr = r - s; if (sr < 0) sr = 0;
+  double ru = su - sr; if (ru < 0) ru = 0;
+  normals(seed, traj, node, VBT_LEAF, dim, z1);
+  normals(seed, traj, node, VBT_LEAF_H, dim, z2);
+  double sr3 = pow(sr, 3), ru3 = pow(ru, 3), su3 = pow(su, 3);
+  double sr_ru_half = sqrt(sr * ru);
+  double dd = sqrt(sr3 + ru3);
+  double d_prime = 1 / (2 * su * dd);
+  double a = d_prime * sr3 * sr_ru_half;
+  double b = d_prime * ru3 * sr_ru_half;
+  double c = sqrt(3 * sr3 * ru3) / (6 * dd);
+  for (int i = 0; i < dim; i++) {
+    double w_sr = sr / su * wsu[i] + 6 * sr * ru / su3 * hsu[i] + 2 * (a + b) / su * z1[i];
+    w_r[i] = ws[i] + w_sr;
+    double bhh_sr = sr3 / su3 * hsu[i] - a * z1[i] + c * z2[i];
+    bhh_r[i] = hs[i] + bhh_sr + 0.5 * (r * ws[i] - s * w_r[i]);
+  }
+}
+
+/* VirtualBrownianTree.evaluate(ta, tb, use_levy=True) (tree.py:325-354):
+ * (W, H) of [ta, tb] from the two point values by Chen's relation
+ * (_levy_diff, tree.py:94-126), then scaled by sqrt(T). */
+static void vbt_levy_increment(const orc_desc *d, uint32_t traj, double ta, double tb,
+                               double *dw, double *dh) {
+  double T = d->vbt_t1 - d->vbt_t0;
+  double tol_unit = d->vbt_tol / T;
+  double ra = (ta - d->vbt_t0) / T, rb = (tb - d->vbt_t0) / T;
+  double wa[64], wb[64], ha[64], hb[64];
+  vbt_levy_eval_unit(d->seed, traj, tol_unit, ra, d->dim, wa, ha);
+  vbt_levy_eval_unit(d->seed, traj, tol_unit, rb, d->dim, wb, hb);
+  double su = rb - ra;
+  double inv = fabs(su) < DBL_EPSILON ? 0.0 : 1 / su;
+  double sq = sqrt(T);
+  for (int i = 0; i < d->dim; i++) {
+    double u_bb_s = rb * wa[i] - ra * wb[i];
+    double bhh_su = hb[i] - ha[i] - 0.5 * u_bb_s;
+    dw[i] = sq * (wb[i] - wa[i]);
+    dh[i] = sq * (inv * bhh_su);
+  }
+}
+
+/* The Brownian increment of the loop's step [tprev, tnext] (direction-
+ * flipped time).  The WrapTerm (_term.py:742-745) evaluates the forward real
+ * interval and multiplies the whole increment (W and H) by the direction. */
+static void step_increment(const orc_desc *d, uint32_t traj, int dir, double tprev,
+                           double tnext, double *dw, double *dh) {
+  if (!d->levy_area) {
+    vbt_increment(d, traj, dir * tprev, dir * tnext, dw);
+    return;
+  }
+  if (dir > 0) {
+    vbt_levy_increment(d, traj, tprev, tnext, dw, dh);
+  } else {
+    vbt_levy_increment(d, traj, -tnext, -tprev, dw, dh);
+    for (int i = 0; i < d->dim; i++) { dw[i] = -dw[i]; dh[i] = -dh[i]; }
+  }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -644,6 +764,45 @@ static void rk_step(const Field *F, const Tableau *tab, int dir, double tprev,
     double e = 0.0;
     for (int j = 0; j < tab->s; j++) e += tab->e[j] * so->k[j][n];
     so->err[n] = e;
+  }
+}
+
+/* One ShARK step (shark.py:10-35) by the additive-noise branch of
+ * AbstractSRK.step (srk.py:335-671):
+ *   z_j = y0 + sum_i a_ji h f_i + g (a^W_j W + a^H_j H),  a^W = (0, 5/6),
+ *         a^H = (1, 1), c = (0, 5/6), a_10 = 5/6;
+ *   y1  = y0 + h (0.4 f_0 + 0.6 f_1) + g W;  error = h (-0.6 f_0 + 0.6 f_1).
+ * g = g(t0) (the diffusion does not depend on y; the Ornstein-Uhlenbeck and
+ * the registered diffusions do not depend on t either, so the correction
+ * 0.5 (g(t1) - g(t0)) (W - 2H) of srk.py:607-618 is zero).  The drift's
+ * control is the loop's step t1 - t0 (srk.py:364, passed to vf_prod, which
+ * the WrapTerm does not flip), not dir * (t1 - t0) as for the RK solvers. */
+static void shark_step(const Field *F, int dir, double tprev, double tnext,
+                       const double *y0, const double *dw, const double *dh, StepOut *so) {
+  const int D = F->d->dim;
+  const double h = tnext - tprev;
+  double g[64], gw[64], gh[64], z[64], f[64];
+  so->dim = D;
+  so->tprev = tprev; so->tnext = tnext;
+  memcpy(so->y0, y0, sizeof(double) * D);
+  memcpy(so->dw, dw, sizeof(double) * D);
+  field_diffusion(F, y0, g);
+  for (int n = 0; n < D; n++) { gw[n] = g[n] * dw[n]; gh[n] = g[n] * dh[n]; }
+  /* stage 0 at t0: z_0 = y0 + g H */
+  for (int n = 0; n < D; n++) z[n] = (y0[n] + 0.0) + (0.0 * gw[n] + 1.0 * gh[n]);
+  memcpy(so->ystage[0], z, sizeof(double) * D);
+  field_drift(F, dir * tprev, z, f);
+  for (int n = 0; n < D; n++) so->k[0][n] = f[n] * h;
+  /* stage 1 at t0 + 5/6 h */
+  for (int n = 0; n < D; n++)
+    z[n] = (y0[n] + SHARK.a[1][0] * so->k[0][n]) + (5.0 / 6.0 * gw[n] + 1.0 * gh[n]);
+  memcpy(so->ystage[1], z, sizeof(double) * D);
+  field_drift(F, dir * (tprev + SHARK.c[1] * h), z, f);
+  for (int n = 0; n < D; n++) so->k[1][n] = f[n] * h;
+  for (int n = 0; n < D; n++) {
+    double drift = SHARK.b[0] * so->k[0][n] + SHARK.b[1] * so->k[1][n];
+    so->y1[n] = (y0[n] + drift) + (1.0 * gw[n] + 0.0 * gh[n]);
+    so->err[n] = SHARK.e[0] * so->k[0][n] + SHARK.e[1] * so->k[1][n];
   }
 }
 
@@ -1153,7 +1312,7 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
   int result = ORC_SUCCESSFUL;
   int num_steps = 0, num_acc = 0, num_rej = 0;
   StepOut so;
-  double dw[64];
+  double dw[64], dh[64];
   /* Event values at (t0, y0) (_integrate.py:1333-1426): a boolean condition
    * that already holds ends the solve before its first step. */
   double ev_val[ORC_MAX_EVENTS];
@@ -1168,11 +1327,15 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
     if (num_steps >= d->max_steps) break;
     const double *dwp = NULL;
     if (d->diffusion != ORC_DIFF_NONE) {
-      vbt_increment(d, (uint32_t)bidx, dir * tprev, dir * tnext, dw);
+      step_increment(d, (uint32_t)bidx, dir, tprev, tnext, dw, dh);
       dwp = dw;
     }
-    /* FSAL reuse unless first step or just after a jump (runge_kutta.py:684-700) */
-    rk_step(&F, tab, dir, tprev, tnext, y, !(first_step || made_jump), f0, dwp, &so);
+    if (d->solver == ORC_SHARK) {
+      shark_step(&F, dir, tprev, tnext, y, dw, dh, &so);
+    } else {
+      /* FSAL reuse unless first step or just after a jump (runge_kutta.py:684-700) */
+      rk_step(&F, tab, dir, tprev, tnext, y, !(first_step || made_jump), f0, dwp, &so);
+    }
     for (int n = 0; n < D; n++)
       if (isnan(so.err[n])) so.err[n] = INFINITY; /* _integrate.py:386 */
     int keep, cres = ORC_SUCCESSFUL;
@@ -1318,6 +1481,10 @@ int orc_solve_dense(const orc_desc *d, int64_t B, const double *t0, const double
   if (d->n_event < 0 || d->n_event > ORC_MAX_EVENTS) return -1;
   for (int i = 0; i < d->n_event; i++)
     if (d->ev_kind[i] != ORC_EV_STEADY && d->dim > 4) return -1;
+  if (d->levy_area != 0 && d->levy_area != 1) return -1;
+  /* ShARK takes the SpaceTimeLevyArea of an SDE's tree (srk.py:374-379) */
+  if (d->solver == ORC_SHARK && (d->diffusion == ORC_DIFF_NONE || !d->levy_area)) return -1;
+  if (d->solver == ORC_SHARK && d->save_dense) return -2;
   SolveIO io = {d, t0, t1, dt0, time_stride, y0, args, args_stride, params, ts,
                 cb, cb_ctx, ys_out, ts_out, result, stats, dense_ts, dense_info, dense_n,
                 event_index};
@@ -1494,6 +1661,24 @@ int orc_vbt_increments(const orc_desc *d, int64_t n, const uint32_t *traj,
   return 0;
 }
 
+/* (W, H) increments of the oracle's space-time Levy area tree over [ta, tb]. */
+int orc_vbt_levy_increments(const orc_desc *d, int64_t n, const uint32_t *traj,
+                            const double *ta, const double *tb, double *dw, double *dh) {
+  for (int64_t i = 0; i < n; i++)
+    vbt_levy_increment(d, traj[i], ta[i], tb[i], dw + i * d->dim, dh + i * d->dim);
+  return 0;
+}
+
+/* W(t) and bar H(t) = t H_{0,t} of the Levy area tree on the unit interval. */
+int orc_vbt_levy_points(const orc_desc *d, int64_t n, const uint32_t *traj,
+                        const double *r, double *w, double *bhh) {
+  double tol_unit = d->vbt_tol / (d->vbt_t1 - d->vbt_t0);
+  for (int64_t i = 0; i < n; i++)
+    vbt_levy_eval_unit(d->seed, traj[i], tol_unit, r[i], d->dim, w + i * d->dim,
+                       bhh + i * d->dim);
+  return 0;
+}
+
 int orc_normal4(uint64_t seed, uint32_t traj, uint32_t node, uint32_t kind, uint32_t q,
                 double *z) {
   normal4(seed, traj, node, kind, q, z);
@@ -1555,6 +1740,7 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
   if (d->dim > 64 || d->dim < 1) return -1;
   if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts || d->n_event)
     return -2; /* forward outputs only */
+  if (d->levy_area || d->solver == ORC_SHARK) return -2;
   const Tableau *tab = tableau_of(d->solver);
   const int D = d->dim;
   const int n_save = n_save_of(d);
@@ -1880,6 +2066,7 @@ int orc_backsolve(const orc_desc *d, int64_t B, const double *t0, const double *
   if (d->dim > 64 || d->dim < 1) return -1;
   if (d->field == ORC_CALLBACK || d->diffusion != ORC_DIFF_NONE) return -2;
   if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts || d->n_event) return -2;
+  if (d->levy_area || d->solver == ORC_SHARK) return -2;
   const int64_t N = 2 * (int64_t)d->dim + d->n_args + n_params;
   BsIO io = {d, t0, t1, dt0, time_stride, ts_saved, ys, grad_ys, args, args_stride,
              params, n_params, grad_y0, grad_args, result, stats};

@@ -276,3 +276,45 @@ def test_tc_kernel_scope():
         _lib.Problem(fields(dfx.Tsit5(), adjoint=dfx.RecursiveCheckpointAdjoint(8)))
     with pytest.raises(_lib.GbdxError, match="MLP"):
         _lib.Problem(_fields(kernel=3))
+
+
+def test_shark_and_levy_tree_scope():
+    # ShARK needs an SDE whose tree has the space-time Levy area
+    # (srk.py:374-379); the Levy area tree drives the Ornstein-Uhlenbeck SDE
+    # kernels (Euler, Heun, Dopri5, Tsit5 use its W).
+    def terms(levy):
+        bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (2,), key=0, levy_area=levy)
+        return dfx.MultiTerm(dfx.ODETerm(dfx.OrnsteinUhlenbeck()),
+                             dfx.ControlTerm(dfx.OrnsteinUhlenbeck(), bm))
+
+    def fields(solver, levy, ctrl=None):
+        return dfx.lower(terms(levy), solver, ctrl or dfx.ConstantStepSize(),
+                         dfx.SaveAt(t1=True), dim=2, dtype=torch.float32, max_steps=100,
+                         n_ts=0)
+    f = fields(dfx.ShARK(), dfx.SpaceTimeLevyArea)
+    assert f["solver"] == 5 and f["levy_area"] == 1
+    assert _lib.Problem(f).n_save == 1
+    assert _lib.Problem(fields(dfx.ShARK(), dfx.SpaceTimeLevyArea,
+                               dfx.PIDController(rtol=1e-3, atol=1e-3))).n_save == 1
+    assert _lib.Problem(fields(dfx.Heun(), dfx.SpaceTimeLevyArea)).n_save == 1
+    assert fields(dfx.Heun(), dfx.BrownianIncrement)["levy_area"] == 0
+    with pytest.raises(ValueError, match="minimal Levy Area"):
+        fields(dfx.ShARK(), dfx.BrownianIncrement)
+    with pytest.raises(ValueError, match="SDE"):
+        dfx.lower(dfx.ODETerm(dfx.OrnsteinUhlenbeck()), dfx.ShARK(), dfx.ConstantStepSize(),
+                  dfx.SaveAt(t1=True), dim=2, dtype=torch.float32, max_steps=100, n_ts=0)
+    with pytest.raises(ValueError, match="levy_area"):
+        dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (2,), levy_area=int)
+    # the C ABI checks the same
+    with pytest.raises(ValueError, match="levy_area=SpaceTimeLevyArea"):
+        _lib.Problem(dict(f, levy_area=0))
+    with pytest.raises(ValueError, match="unknown levy_area"):
+        _lib.Problem(dict(f, levy_area=2))
+    g = dfx.lower(dfx.ODETerm(dfx.OrnsteinUhlenbeck()), dfx.Heun(), dfx.ConstantStepSize(),
+                  dfx.SaveAt(t1=True), dim=2, dtype=torch.float32, max_steps=100, n_ts=0)
+    with pytest.raises(ValueError, match="Brownian tree of an SDE"):
+        _lib.Problem(dict(g, levy_area=1))
+    with pytest.raises(_lib.GbdxError, match="analytic ODE fields"):
+        _lib.Problem(dfx.lower(terms(dfx.SpaceTimeLevyArea), dfx.ShARK(),
+                               dfx.ConstantStepSize(), dfx.SaveAt(dense=True), dim=2,
+                               dtype=torch.float32, max_steps=100, n_ts=0))

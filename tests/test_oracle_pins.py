@@ -528,6 +528,142 @@ def test_vbt_conditional_bridge():
     assert abs(np.corrcoef(resid, w1)[0, 1]) < 0.03
 
 
+# --- the tree with space-time Levy area (test/test_brownian.py) ------------
+
+def test_levy_tree_statistics():
+    # test/test_brownian.py:120-175: over [0, 5] with tol 2^-5, W ~ N(0, 5),
+    # H ~ N(0, 5/12), and W and H uncorrelated.
+    d = O.make_desc(dim=1, vbt_t0=0.0, vbt_t1=5.0, vbt_tol=2 ** -5, seed=5678)
+    n = 200000
+    traj = np.arange(n, dtype=np.uint32)
+    w, h = O.vbt_levy_increments(d, traj, np.zeros(n), np.full(n, 5.0))
+    w, h = w[:, 0], h[:, 0]
+    assert scipy.stats.kstest(h, scipy.stats.norm(0, math.sqrt(5 / 12)).cdf).pvalue > 0.1
+    assert scipy.stats.kstest(w, scipy.stats.norm(0, math.sqrt(5)).cdf).pvalue > 0.1
+    assert abs(np.mean(h * w)) < 0.01
+
+
+def _true_cond_stats_wh(w_s, h_s, w_u, h_u, s, r, u):
+    # Law of (W_r, H_r) given (W_s, H_s, W_u, H_u), H = H_{0,.}: Foster's
+    # bridge as the reference's test writes it (test/test_brownian.py:183-211).
+    su, sr, ru = u - s, r - s, u - r
+    sr3, ru3, su2 = sr ** 3, ru ** 3, su ** 2
+    sr_ru_half = math.sqrt(sr * ru)
+    dd = math.sqrt(sr3 + ru3)
+    a = sr3 * sr_ru_half / (2 * su * dd)
+    b = ru3 * sr_ru_half / (2 * su * dd)
+    c = sr ** 1.5 * ru ** 1.5 / (math.sqrt(12) * dd)
+    h_su = (u * h_u - s * h_s - u / 2 * w_s + s / 2 * w_u) / su
+    w_mean = w_s + (sr / su) * (w_u - w_s) + (6 * sr * ru / su2) * h_su
+    w_std = 2 * (a + b) / su
+    h_mean = (s / r) * h_s + (sr3 / (r * su2)) * h_su + 0.5 * w_s - s / (2 * r) * w_mean
+    h_std = math.sqrt((c / r) ** 2 + ((a * u + s * b) / (r * su)) ** 2)
+    return w_mean, w_std, h_mean, h_std
+
+
+def test_levy_tree_conditional_statistics():
+    # test/test_brownian.py:276-490 (SpaceTimeLevyArea, use_levy=True):
+    # evaluate(t0, t_i) on many paths at sorted times at least 2^-8 apart; the
+    # middle of each consecutive triple, normalised by its conditional law
+    # given the outer two, is N(0, 1) (KS at 0.1 with a Bonferroni correction).
+    t0, t1 = 0.0, 8.7
+    d = O.make_desc(dim=1, vbt_t0=t0, vbt_t1=t1, vbt_tol=2 ** -10, seed=5680)
+    rng = np.random.default_rng(5680)
+    ts = np.sort(rng.uniform(t0 + 0.1, t1 - 0.1, 40))
+    keep = [ts[0]]
+    for t in ts[1:]:
+        if t >= keep[-1] + 2 ** -8:
+            keep.append(t)
+    ts = np.array(keep)
+    n = 20000
+    traj = np.arange(n, dtype=np.uint32)
+    vals = [O.vbt_levy_increments(d, traj, np.full(n, t0), np.full(n, t)) for t in ts]
+    pw1, pw2, ph = [], [], []
+    for i in range(1, len(ts) - 1):
+        s, r, u = ts[i - 1] - t0, ts[i] - t0, ts[i + 1] - t0
+        (w_s, h_s), (w_r, h_r), (w_u, h_u) = [(v[0][:, 0], v[1][:, 0]) for v in vals[i - 1:i + 2]]
+        w_mean1 = w_s + (w_u - w_s) * (r - s) / (u - s)
+        w_std1 = math.sqrt((u - r) * (r - s) / (u - s))
+        pw1.append(scipy.stats.kstest((w_r - w_mean1) / w_std1, "norm").pvalue)
+        w_mean, w_std, h_mean, h_std = _true_cond_stats_wh(w_s, h_s, w_u, h_u, s, r, u)
+        pw2.append(scipy.stats.kstest((w_r - w_mean) / w_std, "norm").pvalue)
+        ph.append(scipy.stats.kstest((h_r - h_mean) / h_std, "norm").pvalue)
+    m = len(pw1)
+    assert m >= 10
+    assert min(pw1) > 0.1 / m and min(pw2) > 0.1 / m and min(ph) > 0.1 / m
+
+
+def test_levy_tree_reverse_time():
+    # test/test_brownian.py:679-695: increments over reversed intervals are
+    # the negated forward ones (W); H of [b, a] by Chen's relation equals H
+    # of [a, b].
+    d = O.make_desc(dim=1, vbt_t0=0.0, vbt_t1=5.0, vbt_tol=2 ** -5, seed=5678)
+    rng = np.random.default_rng(1)
+    ts = rng.uniform(0, 5, 100)
+    traj = np.zeros(99, dtype=np.uint32)
+    wf, hf = O.vbt_levy_increments(d, traj, ts[:-1], ts[1:])
+    wb, hb = O.vbt_levy_increments(d, traj, ts[1:], ts[:-1])
+    assert np.allclose(wf, -wb, atol=1e-13)
+    assert np.allclose(hf, hb, atol=1e-9)
+
+
+def _nonlinear_additive_sde(solver, level, n=100, t0=0.3, t1=5.3):
+    # An additive-noise SDE in the spirit of the reference's get_time_sde
+    # (test/helpers.py:452-491): a bounded nonlinear drift with cubic damping
+    # and a constant diffusion, on a Levy area tree with tol 2^-14; steps of
+    # (t1 - t0) / 2^level land on every SaveAt time of the coarsest level.
+    d = O.make_desc(solver=solver, controller=O.CONSTANT, field=O.CALLBACK, dim=2, n_ts=3,
+                    save_t1=0, diffusion=O.DIFF_OU, vbt_t0=t0, vbt_t1=t1, vbt_tol=2 ** -14,
+                    seed=5678, levy_area=1, n_args=3)
+
+    def drift(t, y):
+        return (0.5 * np.sin(3 * y[::-1]) - 0.5 * y ** 3) / ((y * y).sum() + 1.0)
+
+    y0 = np.tile([0.7, -0.4], (n, 1))
+    r = O.solve(d, t0, t1, (t1 - t0) / 2 ** level, y0, args=[0.0, 0.0, 1.0],
+                ts=np.linspace(t0, t1, 3), callback=drift)
+    assert (r["result"] == 0).all()
+    return r["ys"], r["stats"][:, 0].mean()
+
+
+def _path_l2_dist(a, b):
+    # test/helpers.py:97-116: sqrt(mean over paths of sup over the saves of
+    # the squared distance)
+    return math.sqrt(np.mean(np.max(((a - b) ** 2).sum(-1), axis=1)))
+
+
+def test_shark_strong_order():
+    # test/test_sde1.py:42-91 (ShARK, additive noise, theoretical order 1.5):
+    # levels 1..7 against ShARK itself at level 9, order by a log-log fit,
+    # within 0.4 of 1.5.
+    ref, _ = _nonlinear_additive_sde(O.SHARK, 9)
+    errs, steps = [], []
+    for level in range(1, 8):
+        ys, n = _nonlinear_additive_sde(O.SHARK, level)
+        errs.append(_path_l2_dist(ys, ref))
+        steps.append(n)
+    order = np.polyfit(np.log(1 / np.array(steps)), np.log(errs), 1)[0]
+    assert -0.4 < order - 1.5 < 0.4, order
+
+
+def test_shark_limit_is_heuns_limit():
+    # test/test_sde1.py:118-190: ShARK and Heun (both Stratonovich; the noise
+    # is additive) converge to the same solution on the same tree: Heun's
+    # distance to ShARK at a fine level shrinks as Heun refines.
+    ref, _ = _nonlinear_additive_sde(O.SHARK, 9)
+    e = [_path_l2_dist(_nonlinear_additive_sde(O.HEUN, lv)[0], ref) for lv in (7, 9, 11)]
+    assert e[0] > 2.5 * e[1] > 6 * e[2], e
+    assert e[2] < 2e-3, e
+
+
+def test_shark_needs_levy_area():
+    # srk.py:374-379: a tree without the space-time Levy area is rejected.
+    d = O.make_desc(solver=O.SHARK, controller=O.CONSTANT, field=O.ORNSTEIN_UHLENBECK, dim=2,
+                    diffusion=O.DIFF_OU, levy_area=0, n_args=3)
+    with pytest.raises(ValueError):
+        O.solve(d, 0.0, 1.0, 0.1, np.zeros((1, 2)), args=[1.0, 0.0, 1.0])
+
+
 # ---------------------------------------------------------------------------
 # SaveAt(steps=n) and SaveAt(dense=True)
 # ---------------------------------------------------------------------------
