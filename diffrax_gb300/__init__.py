@@ -9,7 +9,7 @@ from ._core import (
     MLPField, MultiTerm, ODETerm, OrnsteinUhlenbeck, TanhDiagonalDiffusion, PIDController, RecursiveCheckpointAdjoint,
     RESULTS, SaveAt, Solution, Tsit5, VanDerPol, VirtualBrownianTree, adjoint_rms_seminorm,
     rms_norm, Event, LinearCondition, Newton, SteadyStateCondition, steady_state_event,
-    AbstractBrownianIncrement, BrownianIncrement, ShARK, SpaceTimeLevyArea,
+    AbstractBrownianIncrement, BrownianIncrement, SEA, ShARK, SpaceTimeLevyArea, SRA1,
 )
 from ._integrate import DenseInterpolation, diffeqsolve, lower, oracle_fields
 from ._tune import GraphedSolve, autotune_launch, tuned_shapes

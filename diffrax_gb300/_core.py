@@ -252,6 +252,22 @@ class ShARK(AbstractSolver):
     minimal_levy_area = SpaceTimeLevyArea
 
 
+class SRA1(AbstractSolver):
+    """Roessler's SRA1 for additive noise (diffrax/_solver/sra1.py:37-68):
+    two drift evaluations per step, strong order 1.5; needs a
+    VirtualBrownianTree with levy_area=SpaceTimeLevyArea."""
+    solver_id, _order, _strong_order = 6, 2, 1.5
+    minimal_levy_area = SpaceTimeLevyArea
+
+
+class SEA(AbstractSolver):
+    """Shifted Euler for additive noise (diffrax/_solver/sea.py:37-69): one
+    drift evaluation per step, strong order 1, no error estimate (constant
+    steps); needs a VirtualBrownianTree with levy_area=SpaceTimeLevyArea."""
+    solver_id, _order, _strong_order = 7, 1, 1.0
+    minimal_levy_area = SpaceTimeLevyArea
+
+
 # ---------------------------------------------------------------------------
 # Step size controllers.
 # ---------------------------------------------------------------------------

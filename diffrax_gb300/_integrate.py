@@ -18,7 +18,7 @@ from . import _lib
 from ._core import (
     RESULT_MESSAGES, RESULTS, AbstractField, BacksolveAdjoint, ClipStepSizeController,
     ConstantStepSize, ControlTerm, Event, LinearCondition, SteadyStateCondition,
-    Euler, MultiTerm, ShARK, SpaceTimeLevyArea, ODETerm, OrnsteinUhlenbeck, PIDController,
+    Euler, MultiTerm, SpaceTimeLevyArea, ODETerm, OrnsteinUhlenbeck, PIDController,
     RecursiveCheckpointAdjoint, SaveAt, Solution, VirtualBrownianTree, adjoint_rms_seminorm,
 )
 
@@ -143,12 +143,13 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
         levy = getattr(bm, "levy_area", None) is SpaceTimeLevyArea
         f.update(vbt_t0=bm.t0, vbt_t1=bm.t1, vbt_tol=bm.tol, seed=bm.key,
                  levy_area=int(levy))
-        if isinstance(solver, ShARK) and not levy:
+        if getattr(solver, "minimal_levy_area", None) is SpaceTimeLevyArea and not levy:
             # srk.py:374-379
             raise ValueError("The Brownian increment BrownianIncrement does not have the "
                              "minimal Levy Area SpaceTimeLevyArea.")
-    elif isinstance(solver, ShARK):
-        raise ValueError("ShARK solves SDEs: terms must be MultiTerm(ODETerm, ControlTerm)")
+    elif getattr(solver, "minimal_levy_area", None) is not None:
+        raise ValueError(f"{type(solver).__name__} solves SDEs: terms must be "
+                         "MultiTerm(ODETerm, ControlTerm)")
     if isinstance(adjoint, RecursiveCheckpointAdjoint):
         cp = adjoint.checkpoints
         if cp is None:

@@ -185,11 +185,14 @@ static int solver_order(int solver) {
     case GBDX_HEUN: return 2;
     case GBDX_DOPRI8: return 8;
     case GBDX_SHARK: return 2;
+    case GBDX_SRA1: return 2;
+    case GBDX_SEA: return 1;
     default: return 5;
   }
 }
 static double solver_strong_order(int solver) {
-  if (solver == GBDX_SHARK) return 1.5;
+  if (solver == GBDX_SHARK || solver == GBDX_SRA1) return 1.5;
+  if (solver == GBDX_SEA) return 1.0;
   return (solver == GBDX_EULER || solver == GBDX_HEUN) ? 0.5 : 0.0;
 }
 
@@ -197,7 +200,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   if (!desc || !out) return fail(GBDX_ERR_INVALID, "null descriptor or output handle");
   *out = nullptr;
   const gbdx_problem_desc &d = *desc;
-  if (d.solver < GBDX_EULER || d.solver > GBDX_SHARK)
+  if (d.solver < GBDX_EULER || d.solver > GBDX_SEA)
     return fail(GBDX_ERR_INVALID, "unknown solver %d", d.solver);
   if (d.controller != GBDX_CONSTANT && d.controller != GBDX_PID)
     return fail(GBDX_ERR_INVALID, "unknown step size controller %d", d.controller);
@@ -223,12 +226,13 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     return fail(GBDX_ERR_INVALID, "unknown levy_area %d", d.levy_area);
   if (d.levy_area != GBDX_LEVY_NONE && !sde)
     return fail(GBDX_ERR_INVALID, "levy_area belongs to the Brownian tree of an SDE");
-  // srk.py:374-379: ShARK takes the space-time Levy area of an SDE's tree
-  if (d.solver == GBDX_SHARK && (!sde || d.levy_area != GBDX_LEVY_SPACE_TIME))
+  // srk.py:374-379: the SRKs take the space-time Levy area of an SDE's tree
+  if (gbdx::is_srk(d.solver) && (!sde || d.levy_area != GBDX_LEVY_SPACE_TIME))
     return fail(GBDX_ERR_INVALID,
-                "ShARK solves SDEs whose Brownian tree has levy_area=SpaceTimeLevyArea");
+                "ShARK, SRA1 and SEA solve SDEs whose Brownian tree has "
+                "levy_area=SpaceTimeLevyArea");
   // pid.py:437-447: adaptive stepping needs an error estimate.
-  if (d.controller == GBDX_PID && d.solver == GBDX_EULER)
+  if (d.controller == GBDX_PID && (d.solver == GBDX_EULER || d.solver == GBDX_SEA))
     return fail(GBDX_ERR_INVALID,
                 "Cannot use adaptive step sizes with a solver that does not provide error "
                 "estimates.");

@@ -157,9 +157,14 @@ struct Tab<GBDX_HEUN> {
   __host__ __device__ static constexpr double e(int j) { return j == 0 ? 0.5 : -0.5; }
 };
 
-// ShARK (shark.py:10-35): the drift rows of the additive-noise stochastic
-// Runge--Kutta tableau; the W and H coefficients (a^W = (0, 5/6), a^H =
-// (1, 1), b^W = 1, b^H = 0) enter in Traj::step.
+// The additive-noise stochastic Runge--Kutta tableaus (srk.py
+// StochasticButcherTableau with AdditiveCoeffs): the drift rows, and the W
+// and H coefficients of each stage (aw, ah) and of the solution (bw, bh).
+__host__ __device__ constexpr bool is_srk(int solver) {
+  return solver == GBDX_SHARK || solver == GBDX_SRA1 || solver == GBDX_SEA;
+}
+
+// ShARK (shark.py:10-35)
 template <>
 struct Tab<GBDX_SHARK> {
   static constexpr int S = 2;
@@ -172,6 +177,43 @@ struct Tab<GBDX_SHARK> {
   }
   __host__ __device__ static constexpr double b(int j) { return j == 0 ? 0.4 : 0.6; }
   __host__ __device__ static constexpr double e(int j) { return j == 0 ? -0.6 : 0.6; }
+  __host__ __device__ static constexpr double aw(int j) { return j == 0 ? 0.0 : 5.0 / 6.0; }
+  __host__ __device__ static constexpr double ah(int) { return 1.0; }
+  static constexpr double BW = 1.0, BH = 0.0;
+};
+
+// SRA1 (sra1.py:10-34; Roessler 2010)
+template <>
+struct Tab<GBDX_SRA1> {
+  static constexpr int S = 2;
+  static constexpr bool FSAL = false, SSAL = false;
+  static constexpr int ORDER = 2;
+  static constexpr double STRONG_ORDER = 1.5;
+  __host__ __device__ static constexpr double c(int i) { return i == 0 ? 0.0 : 3.0 / 4.0; }
+  __host__ __device__ static constexpr double a(int i, int j) {
+    return (i == 1 && j == 0) ? 3.0 / 4.0 : 0.0;
+  }
+  __host__ __device__ static constexpr double b(int j) { return j == 0 ? 1.0 / 3.0 : 2.0 / 3.0; }
+  __host__ __device__ static constexpr double e(int j) { return j == 0 ? -2.0 / 3.0 : 2.0 / 3.0; }
+  __host__ __device__ static constexpr double aw(int j) { return j == 0 ? 0.0 : 3.0 / 4.0; }
+  __host__ __device__ static constexpr double ah(int j) { return j == 0 ? 0.0 : 1.5; }
+  static constexpr double BW = 1.0, BH = 0.0;
+};
+
+// SEA, the shifted Euler method (sea.py:10-34): one stage, no error estimate
+template <>
+struct Tab<GBDX_SEA> {
+  static constexpr int S = 1;
+  static constexpr bool FSAL = false, SSAL = false;
+  static constexpr int ORDER = 1;
+  static constexpr double STRONG_ORDER = 1.0;
+  __host__ __device__ static constexpr double c(int) { return 0.0; }
+  __host__ __device__ static constexpr double a(int, int) { return 0.0; }
+  __host__ __device__ static constexpr double b(int) { return 1.0; }
+  __host__ __device__ static constexpr double e(int) { return 0.0; }
+  __host__ __device__ static constexpr double aw(int) { return 0.5; }
+  __host__ __device__ static constexpr double ah(int) { return 1.0; }
+  static constexpr double BW = 1.0, BH = 0.0;
 };
 
 template <>

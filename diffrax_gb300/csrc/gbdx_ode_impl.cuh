@@ -69,6 +69,12 @@ inline OdeEntry find_ode_sde_entry_t(int solver, int dim) {
     case GBDX_SHARK:                                           \
       if constexpr (LEVY) return GBDX_ENTRY(GBDX_SHARK, F);    \
       return OdeEntry{nullptr, nullptr};                       \
+    case GBDX_SRA1:                                            \
+      if constexpr (LEVY) return GBDX_ENTRY(GBDX_SRA1, F);     \
+      return OdeEntry{nullptr, nullptr};                       \
+    case GBDX_SEA:                                             \
+      if constexpr (LEVY) return GBDX_ENTRY(GBDX_SEA, F);      \
+      return OdeEntry{nullptr, nullptr};                       \
     default: return OdeEntry{nullptr, nullptr};                \
   }
   using OU2 = OrnsteinUhlenbeckSDE<float, 2, LEVY>;

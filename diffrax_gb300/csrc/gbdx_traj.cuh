@@ -130,7 +130,7 @@ struct Traj {
   static constexpr int NA = FIELD::NARGS > 0 ? FIELD::NARGS : 1;
   static constexpr bool F32 = sizeof(T) == 4;
   static constexpr bool LEVY = FieldLevy<FIELD>::value;
-  static_assert(SOLVER != GBDX_SHARK || LEVY, "ShARK needs the space-time Levy area");
+  static_assert(!is_srk(SOLVER) || LEVY, "the SRKs need the space-time Levy area");
 
   T y[D];
   T f0[D];  // FSAL: f(t_n, y_n) from the last stage of the previous step
@@ -485,10 +485,11 @@ struct Traj {
         dw[n + 1] = w.y - wb[n + 1];
       }
     }
-    if constexpr (SOLVER == GBDX_SHARK) {
-      // ShARK, the additive-noise branch of AbstractSRK.step (srk.py:335-671):
-      //   z_0 = y0 + g H,  z_1 = y0 + 5/6 h f_0 + g (5/6 W + H),
-      //   y1 = y0 + h (0.4 f_0 + 0.6 f_1) + g W,  err = h (0.6 f_1 - 0.6 f_0),
+    if constexpr (is_srk(SOLVER)) {
+      // ShARK / SRA1 / SEA, the additive-noise branch of AbstractSRK.step
+      // (srk.py:335-671):
+      //   z_j = (y0 + sum_i a_ji h f_i) + g (aw_j W + ah_j H),
+      //   y1 = (y0 + sum_j b_j h f_j) + g (bw W + bh H),  err = sum_j e_j h f_j,
       // with g = g(t0) (the Ornstein-Uhlenbeck diffusion is constant, so the
       // correction 0.5 (g(t1) - g(t0)) (W - 2H) of srk.py:607-618 is zero).
       // The drift's control is the loop's step t1 - t0 (srk.py:364, given to
@@ -500,20 +501,36 @@ struct Traj {
       for (int n = 0; n < D; n++) {
         gw[n] = sg[n] * dw[n];
         gh[n] = sg[n] * dh[n];
-        yi[n] = y[n] + gh[n];
       }
-      FIELD::vf(P, args, yi, f);
+#pragma unroll
+      for (int j = 0; j < S; j++) {
+#pragma unroll
+        for (int n = 0; n < D; n++) {
+          T drift = T(0);
+#pragma unroll
+          for (int i = 0; i < j; i++)
+            if (TB::a(j, i) != 0.0) drift += T(TB::a(j, i)) * k[i][n];
+          T noise = T(0);
+          if (TB::aw(j) != 0.0) noise += T(TB::aw(j)) * gw[n];
+          if (TB::ah(j) != 0.0) noise += T(TB::ah(j)) * gh[n];
+          yi[n] = (y[n] + drift) + noise;
+        }
+        FIELD::vf(P, args, yi, f);
+#pragma unroll
+        for (int n = 0; n < D; n++) k[j][n] = f[n] * hl;
+      }
 #pragma unroll
       for (int n = 0; n < D; n++) {
-        k[0][n] = f[n] * hl;
-        yi[n] = (y[n] + T(5.0 / 6.0) * k[0][n]) + (T(5.0 / 6.0) * gw[n] + gh[n]);
-      }
-      FIELD::vf(P, args, yi, f);
+        T drift = T(0), e = T(0);
 #pragma unroll
-      for (int n = 0; n < D; n++) {
-        k[1][n] = f[n] * hl;
-        y1[n] = (y[n] + (T(0.4) * k[0][n] + T(0.6) * k[1][n])) + gw[n];
-        const T e = T(-0.6) * k[0][n] + T(0.6) * k[1][n];
+        for (int j = 0; j < S; j++) {
+          drift += T(TB::b(j)) * k[j][n];
+          if (TB::e(j) != 0.0) e += T(TB::e(j)) * k[j][n];
+        }
+        T noise = T(0);
+        if (TB::BW != 0.0) noise += T(TB::BW) * gw[n];
+        if (TB::BH != 0.0) noise += T(TB::BH) * gh[n];
+        y1[n] = (y[n] + drift) + noise;
         err[n] = is_nan_(e) ? T(INFINITY) : e;
       }
     } else {

@@ -38,17 +38,19 @@
 extern "C" {
 #endif
 
-/* Solvers (diffrax/_solver/{euler,heun,dopri5,tsit5,dopri8,shark}.py); Dopri8
- * on the analytic fields; ShARK (the additive-noise stochastic Runge--Kutta
- * method, srk.py:335-671) on the Ornstein--Uhlenbeck SDE with a space-time
- * Levy area tree. */
+/* Solvers (diffrax/_solver/{euler,heun,dopri5,tsit5,dopri8,shark,sra1,sea}.py);
+ * Dopri8 on the analytic fields; ShARK, SRA1 and SEA (the additive-noise
+ * stochastic Runge--Kutta methods, srk.py:335-671) on the Ornstein--Uhlenbeck
+ * SDE with a space-time Levy area tree (SEA: constant steps). */
 enum gbdx_solver {
   GBDX_EULER = 0,
   GBDX_HEUN = 1,
   GBDX_DOPRI5 = 2,
   GBDX_TSIT5 = 3,
   GBDX_DOPRI8 = 4,
-  GBDX_SHARK = 5
+  GBDX_SHARK = 5,
+  GBDX_SRA1 = 6,
+  GBDX_SEA = 7
 };
 /* Levy area drawn by the virtual Brownian tree (diffrax/_custom_types.py). */
 enum gbdx_levy_area { GBDX_LEVY_NONE = 0, GBDX_LEVY_SPACE_TIME = 1 };

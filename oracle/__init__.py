@@ -21,7 +21,7 @@ from .build import build_oracle, oracle_lib_path
 
 __all__ = [
     "OracleDesc", "load", "solve", "grad_recursive", "vbt_increments", "vbt_levy_increments",
-    "vbt_levy_points", "normal4", "SHARK",
+    "vbt_levy_points", "normal4", "SHARK", "SRA1", "SEA",
     "dense_evaluate", "n_saves", "STAGES", "clip_times", "clip_find", "clip_adapt",
     "EULER", "HEUN", "DOPRI5", "TSIT5", "DOPRI8", "CONSTANT", "PID",
     "LOTKA_VOLTERRA", "VAN_DER_POL", "ORNSTEIN_UHLENBECK", "MLP", "LINEAR", "CALLBACK",
@@ -29,7 +29,7 @@ __all__ = [
     "EV_STEADY", "EV_EITHER", "EV_UP", "EV_DOWN",
 ]
 
-EULER, HEUN, DOPRI5, TSIT5, DOPRI8, SHARK = 0, 1, 2, 3, 4, 5
+EULER, HEUN, DOPRI5, TSIT5, DOPRI8, SHARK, SRA1, SEA = 0, 1, 2, 3, 4, 5, 6, 7
 CONSTANT, PID = 0, 1
 LOTKA_VOLTERRA, VAN_DER_POL, ORNSTEIN_UHLENBECK, MLP, LINEAR, CALLBACK = 0, 1, 2, 3, 4, 5
 DIFF_NONE, DIFF_OU, DIFF_TANH_DIAG = 0, 1, 2
@@ -77,7 +77,7 @@ _DEFAULTS = dict(solver=TSIT5, controller=PID, field=LOTKA_VOLTERRA, dim=2,
                  n_step_ts=0, n_jump_ts=0, n_event=0, event_root=0, ev_kind=(), ev_dir=(),
                  levy_area=0, newton_rtol=1e-5, newton_atol=1e-5, ev_coef=())
 
-STAGES = {EULER: 1, HEUN: 2, DOPRI5: 7, TSIT5: 7, DOPRI8: 14, SHARK: 2}
+STAGES = {EULER: 1, HEUN: 2, DOPRI5: 7, TSIT5: 7, DOPRI8: 14, SHARK: 2, SRA1: 2, SEA: 1}
 
 
 def n_saves(desc) -> int:

@@ -26,8 +26,9 @@
  *   virtual Brownian tree . diffrax/_brownian/tree.py:94-126, 245-354, 366-448,
  *                           562-621, 626-773 (BrownianIncrement and
  *                           SpaceTimeLevyArea branches)
- *   ShARK ................. diffrax/_solver/shark.py:10-35 with the additive-
- *                           noise step of diffrax/_solver/srk.py:335-671
+ *   additive-noise SRKs ... diffrax/_solver/{shark,sra1,sea}.py:10-35 with
+ *                           the additive-noise step of diffrax/_solver/srk.py:
+ *                           335-671
  *   gradients ............. diffrax/_adjoint.py:179-312 (discretise-then-
  *                           optimise: exact VJP of the accepted-step map with
  *                           the controller under stop_gradient, pid.py:374,
@@ -46,7 +47,9 @@
 #endif
 
 enum { ORC_EULER = 0, ORC_HEUN = 1, ORC_DOPRI5 = 2, ORC_TSIT5 = 3, ORC_DOPRI8 = 4,
-       ORC_SHARK = 5 };
+       ORC_SHARK = 5, ORC_SRA1 = 6, ORC_SEA = 7 };
+/* the additive-noise stochastic Runge-Kutta methods (srk.py) */
+#define ORC_IS_SRK(s) ((s) == ORC_SHARK || (s) == ORC_SRA1 || (s) == ORC_SEA)
 #define ORC_MAX_S 14 /* most stages of a tableau (Dopri8) */
 enum { ORC_CONSTANT = 0, ORC_PID = 1 };
 enum {
@@ -126,9 +129,14 @@ typedef struct {
   double b[ORC_MAX_S], e[ORC_MAX_S], c[ORC_MAX_S];
   int order;      /* ODE order; error_order for ODEs (base.py:97-120) */
   double strong_order;
+  /* additive-noise SRK (srk.py AdditiveCoeffs): stage j adds
+   * g (aw[j] W + ah[j] H), the solution g (bw W + bh H); has_err = 0 when the
+   * tableau has no b_error */
+  double aw[ORC_MAX_S], ah[ORC_MAX_S], bw, bh;
+  int has_err;
 } Tableau;
 
-static Tableau TSIT5, DOPRI5, DOPRI8, HEUN, EULER, SHARK;
+static Tableau TSIT5, DOPRI5, DOPRI8, HEUN, EULER, SHARK, SRA1, SEA;
 /* Dopri8 (dopri8.py:18-189): Prince and Dormand's 8(7) pair, 14 stages,
  * FSAL and SSAL; published method constants as exact rational quotients. */
 static const double DOPRI8_A[13][ORC_MAX_S] = {
@@ -255,12 +263,26 @@ static void init_tableaus(void) {
   memset(&EULER, 0, sizeof EULER);
   EULER.s = 1; EULER.order = 1; EULER.strong_order = 0.5; EULER.b[0] = 1.0;
 
-  /* ShARK (shark.py:10-35): the drift rows; the W and H coefficients of the
-   * additive-noise stages are in shark_step. */
+  /* ShARK (shark.py:10-35) */
   memset(&SHARK, 0, sizeof SHARK);
-  SHARK.s = 2; SHARK.order = 2; SHARK.strong_order = 1.5;
+  SHARK.s = 2; SHARK.order = 2; SHARK.strong_order = 1.5; SHARK.has_err = 1;
   SHARK.c[1] = 5.0 / 6.0; SHARK.a[1][0] = 5.0 / 6.0;
   SHARK.b[0] = 0.4; SHARK.b[1] = 0.6; SHARK.e[0] = -0.6; SHARK.e[1] = 0.6;
+  SHARK.aw[0] = 0.0; SHARK.aw[1] = 5.0 / 6.0; SHARK.ah[0] = 1.0; SHARK.ah[1] = 1.0;
+  SHARK.bw = 1.0; SHARK.bh = 0.0;
+
+  /* SRA1 (sra1.py:10-34, Roessler 2010) */
+  memset(&SRA1, 0, sizeof SRA1);
+  SRA1.s = 2; SRA1.order = 2; SRA1.strong_order = 1.5; SRA1.has_err = 1;
+  SRA1.c[1] = 3.0 / 4.0; SRA1.a[1][0] = 3.0 / 4.0;
+  SRA1.b[0] = 1.0 / 3.0; SRA1.b[1] = 2.0 / 3.0; SRA1.e[0] = -2.0 / 3.0; SRA1.e[1] = 2.0 / 3.0;
+  SRA1.aw[0] = 0.0; SRA1.aw[1] = 3.0 / 4.0; SRA1.ah[0] = 0.0; SRA1.ah[1] = 1.5;
+  SRA1.bw = 1.0; SRA1.bh = 0.0;
+
+  /* SEA, the shifted Euler method (sea.py:10-34): no error estimate */
+  memset(&SEA, 0, sizeof SEA);
+  SEA.s = 1; SEA.order = 1; SEA.strong_order = 1.0; SEA.has_err = 0;
+  SEA.b[0] = 1.0; SEA.aw[0] = 0.5; SEA.ah[0] = 1.0; SEA.bw = 1.0; SEA.bh = 0.0;
   done = 1;
 }
 
@@ -271,6 +293,8 @@ static const Tableau *tableau_of(int solver) {
     case ORC_DOPRI5: return &DOPRI5;
     case ORC_DOPRI8: return &DOPRI8;
     case ORC_SHARK: return &SHARK;
+    case ORC_SRA1: return &SRA1;
+    case ORC_SEA: return &SEA;
     default: return &TSIT5;
   }
 }
@@ -767,42 +791,45 @@ static void rk_step(const Field *F, const Tableau *tab, int dir, double tprev,
   }
 }
 
-/* One ShARK step (shark.py:10-35) by the additive-noise branch of
- * AbstractSRK.step (srk.py:335-671):
- *   z_j = y0 + sum_i a_ji h f_i + g (a^W_j W + a^H_j H),  a^W = (0, 5/6),
- *         a^H = (1, 1), c = (0, 5/6), a_10 = 5/6;
- *   y1  = y0 + h (0.4 f_0 + 0.6 f_1) + g W;  error = h (-0.6 f_0 + 0.6 f_1).
+/* One step of an additive-noise stochastic Runge--Kutta method (ShARK,
+ * SRA1, SEA) by the additive-noise branch of AbstractSRK.step
+ * (srk.py:335-671):
+ *   z_j = (y0 + sum_i a_ji h f_i) + g (aw_j W + ah_j H),  f_j = f(t0 + c_j h, z_j),
+ *   y1  = (y0 + sum_j b_j h f_j) + g (bw W + bh H),  error = sum_j e_j h f_j.
  * g = g(t0) (the diffusion does not depend on y; the Ornstein-Uhlenbeck and
  * the registered diffusions do not depend on t either, so the correction
  * 0.5 (g(t1) - g(t0)) (W - 2H) of srk.py:607-618 is zero).  The drift's
  * control is the loop's step t1 - t0 (srk.py:364, passed to vf_prod, which
  * the WrapTerm does not flip), not dir * (t1 - t0) as for the RK solvers. */
-static void shark_step(const Field *F, int dir, double tprev, double tnext,
-                       const double *y0, const double *dw, const double *dh, StepOut *so) {
+static void srk_step(const Field *F, const Tableau *tab, int dir, double tprev, double tnext,
+                     const double *y0, const double *dw, const double *dh, StepOut *so) {
   const int D = F->d->dim;
   const double h = tnext - tprev;
-  double g[64], gw[64], gh[64], z[64], f[64];
+  double g[64], gw[64], gh[64], f[64];
   so->dim = D;
   so->tprev = tprev; so->tnext = tnext;
   memcpy(so->y0, y0, sizeof(double) * D);
   memcpy(so->dw, dw, sizeof(double) * D);
   field_diffusion(F, y0, g);
   for (int n = 0; n < D; n++) { gw[n] = g[n] * dw[n]; gh[n] = g[n] * dh[n]; }
-  /* stage 0 at t0: z_0 = y0 + g H */
-  for (int n = 0; n < D; n++) z[n] = (y0[n] + 0.0) + (0.0 * gw[n] + 1.0 * gh[n]);
-  memcpy(so->ystage[0], z, sizeof(double) * D);
-  field_drift(F, dir * tprev, z, f);
-  for (int n = 0; n < D; n++) so->k[0][n] = f[n] * h;
-  /* stage 1 at t0 + 5/6 h */
-  for (int n = 0; n < D; n++)
-    z[n] = (y0[n] + SHARK.a[1][0] * so->k[0][n]) + (5.0 / 6.0 * gw[n] + 1.0 * gh[n]);
-  memcpy(so->ystage[1], z, sizeof(double) * D);
-  field_drift(F, dir * (tprev + SHARK.c[1] * h), z, f);
-  for (int n = 0; n < D; n++) so->k[1][n] = f[n] * h;
+  for (int j = 0; j < tab->s; j++) {
+    double *z = so->ystage[j];
+    for (int n = 0; n < D; n++) {
+      double drift = 0.0;
+      for (int i = 0; i < j; i++) drift += tab->a[j][i] * so->k[i][n];
+      z[n] = (y0[n] + drift) + (tab->aw[j] * gw[n] + tab->ah[j] * gh[n]);
+    }
+    field_drift(F, dir * (tprev + tab->c[j] * h), z, f);
+    for (int n = 0; n < D; n++) so->k[j][n] = f[n] * h;
+  }
   for (int n = 0; n < D; n++) {
-    double drift = SHARK.b[0] * so->k[0][n] + SHARK.b[1] * so->k[1][n];
-    so->y1[n] = (y0[n] + drift) + (1.0 * gw[n] + 0.0 * gh[n]);
-    so->err[n] = SHARK.e[0] * so->k[0][n] + SHARK.e[1] * so->k[1][n];
+    double drift = 0.0, e = 0.0;
+    for (int j = 0; j < tab->s; j++) {
+      drift += tab->b[j] * so->k[j][n];
+      e += tab->e[j] * so->k[j][n];
+    }
+    so->y1[n] = (y0[n] + drift) + (tab->bw * gw[n] + tab->bh * gh[n]);
+    so->err[n] = e;
   }
 }
 
@@ -1330,8 +1357,8 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
       step_increment(d, (uint32_t)bidx, dir, tprev, tnext, dw, dh);
       dwp = dw;
     }
-    if (d->solver == ORC_SHARK) {
-      shark_step(&F, dir, tprev, tnext, y, dw, dh, &so);
+    if (ORC_IS_SRK(d->solver)) {
+      srk_step(&F, tab, dir, tprev, tnext, y, dw, dh, &so);
     } else {
       /* FSAL reuse unless first step or just after a jump (runge_kutta.py:684-700) */
       rk_step(&F, tab, dir, tprev, tnext, y, !(first_step || made_jump), f0, dwp, &so);
@@ -1482,9 +1509,11 @@ int orc_solve_dense(const orc_desc *d, int64_t B, const double *t0, const double
   for (int i = 0; i < d->n_event; i++)
     if (d->ev_kind[i] != ORC_EV_STEADY && d->dim > 4) return -1;
   if (d->levy_area != 0 && d->levy_area != 1) return -1;
-  /* ShARK takes the SpaceTimeLevyArea of an SDE's tree (srk.py:374-379) */
-  if (d->solver == ORC_SHARK && (d->diffusion == ORC_DIFF_NONE || !d->levy_area)) return -1;
-  if (d->solver == ORC_SHARK && d->save_dense) return -2;
+  /* the SRKs take the SpaceTimeLevyArea of an SDE's tree (srk.py:374-379) */
+  if (ORC_IS_SRK(d->solver) && (d->diffusion == ORC_DIFF_NONE || !d->levy_area)) return -1;
+  if (ORC_IS_SRK(d->solver) && d->save_dense) return -2;
+  /* pid.py:437-447: adaptive steps need an error estimate */
+  if (d->controller == ORC_PID && d->solver == ORC_SEA) return -1;
   SolveIO io = {d, t0, t1, dt0, time_stride, y0, args, args_stride, params, ts,
                 cb, cb_ctx, ys_out, ts_out, result, stats, dense_ts, dense_info, dense_n,
                 event_index};
@@ -1740,7 +1769,7 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
   if (d->dim > 64 || d->dim < 1) return -1;
   if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts || d->n_event)
     return -2; /* forward outputs only */
-  if (d->levy_area || d->solver == ORC_SHARK) return -2;
+  if (d->levy_area || ORC_IS_SRK(d->solver)) return -2;
   const Tableau *tab = tableau_of(d->solver);
   const int D = d->dim;
   const int n_save = n_save_of(d);
@@ -2066,7 +2095,7 @@ int orc_backsolve(const orc_desc *d, int64_t B, const double *t0, const double *
   if (d->dim > 64 || d->dim < 1) return -1;
   if (d->field == ORC_CALLBACK || d->diffusion != ORC_DIFF_NONE) return -2;
   if (d->save_steps || d->save_dense || d->n_step_ts || d->n_jump_ts || d->n_event) return -2;
-  if (d->levy_area || d->solver == ORC_SHARK) return -2;
+  if (d->levy_area || ORC_IS_SRK(d->solver)) return -2;
   const int64_t N = 2 * (int64_t)d->dim + d->n_args + n_params;
   BsIO io = {d, t0, t1, dt0, time_stride, ts_saved, ys, grad_ys, args, args_stride,
              params, n_params, grad_y0, grad_args, result, stats};

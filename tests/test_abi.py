@@ -300,6 +300,16 @@ def test_shark_and_levy_tree_scope():
     assert fields(dfx.Heun(), dfx.BrownianIncrement)["levy_area"] == 0
     with pytest.raises(ValueError, match="minimal Levy Area"):
         fields(dfx.ShARK(), dfx.BrownianIncrement)
+    for solver, sid in ((dfx.SRA1(), 6), (dfx.SEA(), 7)):
+        g = fields(solver, dfx.SpaceTimeLevyArea)
+        assert g["solver"] == sid and _lib.Problem(g).n_save == 1
+        with pytest.raises(ValueError, match="minimal Levy Area"):
+            fields(solver, dfx.BrownianIncrement)
+    assert _lib.Problem(fields(dfx.SRA1(), dfx.SpaceTimeLevyArea,
+                               dfx.PIDController(rtol=1e-3, atol=1e-3))).n_save == 1
+    with pytest.raises(ValueError, match="error estimates"):
+        _lib.Problem(fields(dfx.SEA(), dfx.SpaceTimeLevyArea,
+                            dfx.PIDController(rtol=1e-3, atol=1e-3)))
     with pytest.raises(ValueError, match="SDE"):
         dfx.lower(dfx.ODETerm(dfx.OrnsteinUhlenbeck()), dfx.ShARK(), dfx.ConstantStepSize(),
                   dfx.SaveAt(t1=True), dim=2, dtype=torch.float32, max_steps=100, n_ts=0)

@@ -1,5 +1,6 @@
-"""ShARK and the virtual Brownian tree with space-time Levy area on the
-analytic-field kernels (diffrax/_solver/shark.py, the additive-noise branch of
+"""The additive-noise SRKs (ShARK, SRA1, SEA) and the virtual Brownian tree
+with space-time Levy area on the analytic-field kernels
+(diffrax/_solver/{shark,sra1,sea}.py, the additive-noise branch of
 diffrax/_solver/srk.py:335-671, diffrax/_brownian/tree.py:94-126, 562-603,
 727-750), against the FP64 oracle fed the identical integer stream, and
 against the Ornstein-Uhlenbeck process's known law."""
@@ -69,7 +70,8 @@ def test_device_levy_tree_matches_oracle():
 
 
 @pytest.mark.parametrize("kernel", ["plain", "fused"])
-@pytest.mark.parametrize("solver, dim", [("shark", 2), ("shark", 4), ("heun", 2), ("euler", 4)])
+@pytest.mark.parametrize("solver, dim", [("shark", 2), ("shark", 4), ("sra1", 2), ("sea", 4),
+                                         ("heun", 2), ("euler", 4)])
 def test_levy_tree_solvers_match_oracle_on_the_same_path(kernel, solver, dim):
     rng = np.random.default_rng(61)
     B = 2048
@@ -77,7 +79,8 @@ def test_levy_tree_solvers_match_oracle_on_the_same_path(kernel, solver, dim):
     args = np.array([1.5, 0.5, 0.6])
     bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (dim,), key=9,
                                  levy_area=dfx.SpaceTimeLevyArea)
-    s = {"shark": dfx.ShARK(), "heun": dfx.Heun(), "euler": dfx.Euler()}[solver]
+    s = {"shark": dfx.ShARK(), "sra1": dfx.SRA1(), "sea": dfx.SEA(), "heun": dfx.Heun(),
+         "euler": dfx.Euler()}[solver]
     saveat = dfx.SaveAt(ts=np.linspace(0.0, 1.0, 11), t1=True)
     sol, r = solve_pair(s, dfx.ConstantStepSize(), 0.0, 1.0, 0.02, y0, args, bm, kernel, saveat)
     assert (sol.result.cpu().numpy() == 0).all()
@@ -107,8 +110,9 @@ def test_shark_reverse_time_matches_oracle():
     assert err < 5e-5, err
 
 
-def test_shark_adaptive_matches_oracle():
-    # ShARK with a PID controller (error order strong_order + 1/2 = 2,
+@pytest.mark.parametrize("solver", [dfx.ShARK(), dfx.SRA1()])
+def test_srk_adaptive_matches_oracle(solver):
+    # ShARK / SRA1 with a PID controller (error order strong_order + 1/2 = 2,
     # base.py:292-301).  As for Heun, FP32 step factors part the step
     # sequences from the FP64 oracle's after a while on a Brownian path:
     # compare the step counts and solutions statistically.
@@ -118,7 +122,7 @@ def test_shark_adaptive_matches_oracle():
     args = np.array([2.0, -0.3, 0.2])
     bm = dfx.VirtualBrownianTree(0.0, 2.0, 1e-4, (2,), key=13,
                                  levy_area=dfx.SpaceTimeLevyArea)
-    sol, r = solve_pair(dfx.ShARK(), dfx.PIDController(rtol=1e-3, atol=1e-4), 0.0, 2.0, 0.01,
+    sol, r = solve_pair(solver, dfx.PIDController(rtol=1e-3, atol=1e-4), 0.0, 2.0, 0.01,
                         y0, args, bm, "fused", max_steps=16384)
     assert (sol.result.cpu().numpy() == 0).all()
     n_gpu = sol.stats["num_steps"].cpu().numpy().mean()

@@ -632,34 +632,44 @@ def _path_l2_dist(a, b):
     return math.sqrt(np.mean(np.max(((a - b) ** 2).sum(-1), axis=1)))
 
 
-def test_shark_strong_order():
-    # test/test_sde1.py:42-91 (ShARK, additive noise, theoretical order 1.5):
-    # levels 1..7 against ShARK itself at level 9, order by a log-log fit,
-    # within 0.4 of 1.5.
-    ref, _ = _nonlinear_additive_sde(O.SHARK, 9)
+@pytest.mark.parametrize("solver, theoretical", [(O.SHARK, 1.5), (O.SRA1, 1.5), (O.SEA, 1.0)])
+def test_additive_srk_strong_order(solver, theoretical):
+    # test/test_sde1.py:16-91 (ShARK, SRA1 and SEA on additive noise, orders
+    # 1.5, 1.5, 1.0): levels 1..7 against the solver itself at level 9, order
+    # by a log-log fit, within 0.4 of the theoretical order.
+    ref, _ = _nonlinear_additive_sde(solver, 9)
     errs, steps = [], []
     for level in range(1, 8):
-        ys, n = _nonlinear_additive_sde(O.SHARK, level)
+        ys, n = _nonlinear_additive_sde(solver, level)
         errs.append(_path_l2_dist(ys, ref))
         steps.append(n)
     order = np.polyfit(np.log(1 / np.array(steps)), np.log(errs), 1)[0]
-    assert -0.4 < order - 1.5 < 0.4, order
+    assert -0.4 < order - theoretical < 0.4, order
 
 
-def test_shark_limit_is_heuns_limit():
-    # test/test_sde1.py:118-190: ShARK and Heun (both Stratonovich; the noise
-    # is additive) converge to the same solution on the same tree: Heun's
-    # distance to ShARK at a fine level shrinks as Heun refines.
+def test_additive_srk_limit_is_heuns_limit():
+    # test/test_sde1.py:118-190: the SRKs and Heun (all Stratonovich; the
+    # noise is additive) converge to the same solution on the same tree:
+    # Heun's distance to ShARK at a fine level shrinks as Heun refines, and
+    # SRA1 and SEA at fine levels are as close to ShARK as Heun is.
     ref, _ = _nonlinear_additive_sde(O.SHARK, 9)
     e = [_path_l2_dist(_nonlinear_additive_sde(O.HEUN, lv)[0], ref) for lv in (7, 9, 11)]
     assert e[0] > 2.5 * e[1] > 6 * e[2], e
     assert e[2] < 2e-3, e
+    assert _path_l2_dist(_nonlinear_additive_sde(O.SRA1, 9)[0], ref) < 2e-3
+    assert _path_l2_dist(_nonlinear_additive_sde(O.SEA, 11)[0], ref) < 2e-3
 
 
-def test_shark_needs_levy_area():
-    # srk.py:374-379: a tree without the space-time Levy area is rejected.
-    d = O.make_desc(solver=O.SHARK, controller=O.CONSTANT, field=O.ORNSTEIN_UHLENBECK, dim=2,
-                    diffusion=O.DIFF_OU, levy_area=0, n_args=3)
+def test_srk_needs_levy_area():
+    # srk.py:374-379: a tree without the space-time Levy area is rejected;
+    # SEA has no error estimate for adaptive steps (pid.py:437-447).
+    for solver in (O.SHARK, O.SRA1, O.SEA):
+        d = O.make_desc(solver=solver, controller=O.CONSTANT, field=O.ORNSTEIN_UHLENBECK,
+                        dim=2, diffusion=O.DIFF_OU, levy_area=0, n_args=3)
+        with pytest.raises(ValueError):
+            O.solve(d, 0.0, 1.0, 0.1, np.zeros((1, 2)), args=[1.0, 0.0, 1.0])
+    d = O.make_desc(solver=O.SEA, controller=O.PID, field=O.ORNSTEIN_UHLENBECK, dim=2,
+                    diffusion=O.DIFF_OU, levy_area=1, n_args=3)
     with pytest.raises(ValueError):
         O.solve(d, 0.0, 1.0, 0.1, np.zeros((1, 2)), args=[1.0, 0.0, 1.0])
 
