@@ -10,8 +10,10 @@ CUDA graph.  Inputs are seeded synthetic draws of exactly that distribution.
 
 One step = one solve of the whole batch.  `value` is trajectories/s with
 inputs resident in HBM (fused kernel K1); `e2e` is the same metric through the
-public diffeqsolve call with pinned host inputs copied in and results copied
-out every step.  The plain one-trajectory-per-thread kernel K0 is timed the
+public API for a repeated solve, GraphedSolve (one solve captured as a CUDA
+graph, the counterpart of a jitted diffeqsolve), with pinned host inputs copied
+in and results copied out every step; `e2e_eager` the same through a fresh
+diffeqsolve call every step.  The plain one-trajectory-per-thread kernel K0 is timed the
 same way and reported beside it, together with the max relative error of both
 against the FP64 oracle and the oracle's own throughput on the host cores.
 
@@ -693,28 +695,43 @@ def main():
     ys_h = torch.empty((B, 1, 2), dtype=torch.float32).pin_memory()
     res_h = torch.empty((B,), dtype=torch.int32).pin_memory()
 
-    def e2e_step():
+    def eager_step():
         sol = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1_h, None, y0_h, mu_h,
                               stepsize_controller=pid, throw=False)
         ys_h.copy_(sol.ys, non_blocking=True)
         res_h.copy_(sol.result, non_blocking=True)
         torch.cuda.synchronize()
-    for _ in range(args.warmup):
-        e2e_step()
-    barrier()
-    e2e_t = []
-    for _ in range(args.steps):
-        flush.fill_(1.0)
+
+    graphed = dfx.GraphedSolve(term, dfx.Dopri5(), 0.0, t1_h, None, y0_h, mu_h,
+                               stepsize_controller=pid, throw=False)
+
+    def graphed_step():
+        sol = graphed(y0=y0_h, args=mu_h, t1=t1_h)
+        ys_h.copy_(sol.ys, non_blocking=True)
+        res_h.copy_(sol.result, non_blocking=True)
         torch.cuda.synchronize()
-        t = time.perf_counter()
-        e2e_step()
-        e2e_t.append(time.perf_counter() - t)
-    e2e_s = statistics.mean(e2e_t)
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    h2d = B * (2 * 4 + 4 + 8) + 8
+
+    def wall_time(step):
+        for _ in range(args.warmup):
+            step()
+        barrier()
+        ts_ = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            step()
+            ts_.append(time.perf_counter() - t)
+        s_ = statistics.mean(ts_)
+        if world > 1:
+            t = torch.tensor([s_], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            s_ = float(t.item())
+        return s_
+    e2e_s = wall_time(graphed_step)
+    e2e_ok = bool((res_h == 0).all()) and bool(torch.equal(ys_h, ys.cpu()))
+    eager_s = wall_time(eager_step)
+    h2d = B * (2 * 4 + 4 + 8)  # y0, mu, t1 (t0 = 0 is a cached device scalar)
     d2h = B * (2 * 4 + 4)
 
     others = {}
@@ -790,7 +807,11 @@ def main():
                        "saveat": "t1", "kernel": "fused persistent (CUDA graph)",
                        "l2": "256 MB buffer written between timed solves"},
             "e2e": {"value": B * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h, "api": "GraphedSolve",
+                    "results_equal_device_run": e2e_ok},
+            "e2e_eager": {"value": B * world / eager_s, "unit": UNIT,
+                          "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                          "api": "diffeqsolve"},
             # per timed solve: the four longest-first work-order kernels and
             # the integrator (one graph replay)
             "gpu_launches": 5 * args.steps,

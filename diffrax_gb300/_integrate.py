@@ -171,19 +171,53 @@ def _device():
     return torch.device("cuda", torch.cuda.current_device())
 
 
+def _to_dev(x: torch.Tensor, dev, dtype=None) -> torch.Tensor:
+    """x on the device.  A host tensor in page-locked memory is copied
+    asynchronously on the current stream (the solve that reads it is queued
+    behind the copy, so the host does not wait for it); other tensors as by
+    Tensor.to."""
+    nb = x.device.type == "cpu" and x.is_pinned()
+    return x.to(device=dev, dtype=dtype or x.dtype, non_blocking=nb)
+
+
+# Device copies of scalar times (value, device, length) -> FP64 array, so that
+# a repeated solve with Python-number times neither copies from the host nor
+# launches a fill.  The kernels only read them; entries made during a CUDA
+# graph capture are not kept (their memory belongs to the graph).
+_SCALAR_TIMES: dict = {}
+
+
+def _scalar_time(x, n: int, dev) -> torch.Tensor:
+    key = (float(x), dev.index, n)
+    t = _SCALAR_TIMES.get(key)
+    if t is None:
+        t = torch.full((n,), float(x), dtype=torch.float64, device=dev)
+        if not _capturing():
+            if len(_SCALAR_TIMES) >= 32:
+                _SCALAR_TIMES.clear()
+            _SCALAR_TIMES[key] = t
+    return t
+
+
 def _time_arrays(t0, t1, dt0, B, dev):
-    def as_t(x):
-        if isinstance(x, torch.Tensor):
-            return x.to(device=dev, dtype=torch.float64).reshape(-1)
-        return torch.tensor([float(x)], dtype=torch.float64, device=dev)
-    vals = [as_t(t0), as_t(t1)] + ([as_t(dt0)] if dt0 is not None else [])
-    if all(v.numel() == 1 for v in vals):
-        return vals[0], vals[1], (vals[2] if dt0 is not None else None), 0
-    out = [v.expand(B).contiguous() if v.numel() == 1 else v.contiguous() for v in vals]
-    for v in out:
-        if v.numel() != B:
+    """t0, t1, dt0 as FP64 device arrays: one entry each (stride 0) when all
+    are scalars, else B entries each (stride 1)."""
+    xs = [t0, t1] + ([dt0] if dt0 is not None else [])
+    tens = [_to_dev(x, dev, torch.float64).reshape(-1) if isinstance(x, torch.Tensor) else None
+            for x in xs]
+    per_traj = any(t is not None and t.numel() != 1 for t in tens)
+    n = B if per_traj else 1
+    out = []
+    for x, t in zip(xs, tens):
+        if t is None:
+            out.append(_scalar_time(x, n, dev))
+        elif t.numel() == 1 and n > 1:
+            out.append(t.expand(n).contiguous())
+        elif t.numel() != n:
             raise ValueError("t0, t1 and dt0 must be scalars or have one entry per trajectory")
-    return out[0], out[1], (out[2] if dt0 is not None else None), 1
+        else:
+            out.append(t.contiguous())
+    return out[0], out[1], (out[2] if dt0 is not None else None), int(per_traj)
 
 
 def _capturing() -> bool:
@@ -224,7 +258,7 @@ class Lowered:
             raise ValueError("y0 must be [batch, dim] (vmapped semantics)")
         self.dtype = y0.dtype
         self.B, self.dim = int(y0.shape[0]), int(y0.shape[1])
-        self.y0 = y0.to(dev).contiguous()
+        self.y0 = _to_dev(y0, dev).contiguous()
         if max_steps is None:
             raise NotImplementedError("max_steps=None is not supported")
         ts = saveat.ts
@@ -278,7 +312,7 @@ class Lowered:
         if na:
             if args is None:
                 raise ValueError(f"{type(drift).__name__} needs args with {na} entries")
-            a = torch.as_tensor(args).to(device=dev, dtype=self.dtype)
+            a = _to_dev(torch.as_tensor(args), dev, self.dtype)
             if a.numel() == na:
                 a = a.reshape(na).contiguous()
                 self.args_stride = 0
@@ -493,6 +527,10 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     trajectories (results do not depend on it); ``autotune=True`` times a few
     launch shapes on this problem and batch the first time it is seen and
     keeps the fastest (diffrax_gb300._tune).
+
+    Inputs may live on the host: those in page-locked memory are copied to the
+    device asynchronously, so they must not be modified until the solution's
+    tensors have been read.
     """
     if solver_state is not None or controller_state is not None or made_jump is not None:
         raise NotImplementedError("resuming from solver/controller state is not supported")

@@ -118,7 +118,8 @@ class GraphedSolve:
     dt0=None)`` copies the given inputs into the captured buffers, replays the
     graph and returns a Solution whose tensors are the graph's output buffers:
     the next call overwrites them (clone what must be kept).  ``autotune=True``
-    picks the launch shape before capture.
+    picks the launch shape before capture.  Inputs in page-locked host memory
+    are copied asynchronously: keep them unmodified until the outputs are read.
     """
 
     def __init__(self, terms, solver, t0, t1, dt0, y0, args=None, *,
@@ -142,9 +143,15 @@ class GraphedSolve:
         y0 = own(y0)
         if y0.dtype not in (torch.float32, torch.float64):
             y0 = y0.to(torch.float64)
-        t0 = own(t0, torch.float64) if isinstance(t0, torch.Tensor) else t0
-        t1 = own(t1, torch.float64) if isinstance(t1, torch.Tensor) else t1
-        dt0 = own(dt0, torch.float64) if isinstance(dt0, torch.Tensor) else dt0
+        # every time becomes a buffer of this solve (a Python number too: the
+        # calls overwrite the captured times in place)
+        t0 = own(torch.tensor([float(t0)]) if not isinstance(t0, torch.Tensor) else t0,
+                 torch.float64)
+        t1 = own(torch.tensor([float(t1)]) if not isinstance(t1, torch.Tensor) else t1,
+                 torch.float64)
+        if dt0 is not None:
+            dt0 = own(torch.tensor([float(dt0)]) if not isinstance(dt0, torch.Tensor) else dt0,
+                      torch.float64)
         args = own(args, y0.dtype)
         self.throw, self.max_steps = throw, max_steps
 
@@ -173,10 +180,12 @@ class GraphedSolve:
         dst = getattr(self.low, name)
         if dst is None:
             raise ValueError(f"the captured solve has no {name} input")
-        src = torch.as_tensor(value).to(device=dst.device, dtype=dst.dtype)
+        src = torch.as_tensor(value)
         if src.numel() != dst.numel():
             raise ValueError(f"{name} must keep the captured shape {tuple(dst.shape)}")
-        dst.copy_(src.reshape(dst.shape))
+        # a page-locked host source is copied asynchronously, ahead of the
+        # replay on the same stream
+        dst.copy_(src.reshape(dst.shape), non_blocking=src.device.type == "cpu" and src.is_pinned())
 
     def __call__(self, y0=None, args=None, t0=None, t1=None, dt0=None) -> Solution:
         for name, v in (("y0", y0), ("args", args), ("t0", t0), ("t1", t1), ("dt0", dt0)):
