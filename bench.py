@@ -410,6 +410,137 @@ def profile_neural(dev, which, B, n):
         sys.exit(1)
 
 
+RESULT_NAMES_BENCH = {0: "successful", 1: "max_steps_reached", 2: "dt_min_reached",
+                      3: "event_occurred", 4: "max_steps_rejected", 5: "internal_error",
+                      6: "nonlinear_max_steps_reached"}
+
+
+def workload_next_rows(dev, flush, steps, warmup):
+    """The solve features beyond the headline path, each timed on the device
+    (CUDA events, L2 flushed) beside the same solve without it, with its
+    parity against the FP64 oracle on the first 256 trajectories.
+
+    ODE rows: Van der Pol, Dopri5 + PID(1e-6, 1e-9, p=.3, i=.4), mu ~
+    LogU[0.1, 10], (x0, y0) ~ U[-2, 2]^2, t in [0, 10], batch 16384, FP32
+    state, max_steps 1024: SaveAt(steps=3), SaveAt(dense=True) (+ evaluation
+    at 64 times), ClipStepSizeController(step_ts = 101-point grid, jump_ts =
+    2.5, 5, 7.5), Event(x crosses 0 upwards, Newton(1e-5, 1e-5) root), Dopri8.
+    SDE rows: Ornstein-Uhlenbeck dim 2 (theta 1.5, mu 0.5, sigma 0.6) on
+    [0, 1], dt 0.01, tree tol 1e-3, batch 16384: Heun on the W-only tree,
+    Heun / ShARK / SRA1 / SEA on the space-time Levy area tree."""
+    import torch
+    import diffrax_gb300 as dfx
+    import oracle as O
+    from diffrax_gb300._integrate import Lowered, oracle_fields
+    B, n_chk, t1 = 16384, 256, 10.0
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(7)
+    mu = np.exp(rng.uniform(np.log(0.1), np.log(10.0), B))
+    y0 = rng.uniform(-2, 2, (B, 2))
+    y0_d = torch.tensor(y0, dtype=torch.float32, device=dev)
+    mu_d = torch.tensor(mu[:, None], dtype=torch.float32, device=dev)
+    pid = dfx.PIDController(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4)
+    term = dfx.ODETerm(dfx.VanDerPol())
+    out = {"workload": "vdp_dopri5_pid_t10_b16384 and ou_sde_dt0.01_b16384",
+           "ode": {}, "sde": {}}
+
+    def ode_row(solver, saveat, ctrl, event=None):
+        low = Lowered(term, solver, 0.0, t1, None, y0_d, mu_d, saveat, ctrl, None, 1024,
+                      "fused", 0, 0, event=event)
+        ex = saveat.dense or event is not None
+        run = low.run_forward_ex if ex else low.run_forward
+        ms = _events_time(run, steps, warmup, flush)
+        outs = run()
+        ts_ = np.asarray(saveat.ts) if saveat.ts is not None else None
+        d = O.make_desc(**oracle_fields(low.fields))
+        kw = {}
+        if isinstance(ctrl, dfx.ClipStepSizeController):
+            kw = dict(step_ts=ctrl.step_ts, jump_ts=ctrl.jump_ts)
+        r = O.solve(d, 0.0, t1, None, y0[:n_chk], args=mu[:n_chk, None], ts=ts_,
+                    nthreads=cores, **kw)
+        res = outs[2].cpu().numpy()
+        codes, counts = np.unique(res, return_counts=True)
+        row = {"traj_per_s": B / (ms / 1e3), "ms": ms,
+               "mean_attempted_steps": float(outs[3][:, 0].float().mean().item()),
+               "results": {RESULT_NAMES_BENCH.get(int(c), str(c)): int(n)
+                           for c, n in zip(codes, counts)}}
+        # the final value (the last written save: saves are compacted and the
+        # slots after them hold inf) against the oracle's
+        def final(ys_, ts_):
+            k = np.isfinite(ts_).sum(axis=1) - 1
+            return ys_[np.arange(ys_.shape[0]), k]
+        last = final(outs[0][:n_chk].double().cpu().numpy(), outs[1][:n_chk].cpu().numpy())
+        ref_last = final(r["ys"], r["ts"])
+        e = np.abs(last - ref_last).max(axis=1) / np.abs(ref_last).max()
+        row["t1_rel_err_vs_fp64_oracle"] = {"median": float(np.median(e)), "max": float(e.max())}
+        return low, outs, r, row
+
+    base = ode_row(dfx.Dopri5(), dfx.SaveAt(t1=True), pid)[3]
+    out["ode"]["base_saveat_t1"] = base
+    for name, solver, saveat, ctrl, event in (
+            ("saveat_steps3", dfx.Dopri5(), dfx.SaveAt(steps=3, t1=True), pid, None),
+            ("saveat_dense", dfx.Dopri5(), dfx.SaveAt(dense=True, t1=True), pid, None),
+            ("clip_controller", dfx.Dopri5(), dfx.SaveAt(t1=True),
+             dfx.ClipStepSizeController(pid, step_ts=np.linspace(0.0, t1, 101),
+                                        jump_ts=np.array([2.5, 5.0, 7.5])), None),
+            ("event_x_up_newton", dfx.Dopri5(), dfx.SaveAt(t1=True), pid,
+             dfx.Event(dfx.LinearCondition([1.0, 0.0]), dfx.Newton(1e-5, 1e-5),
+                       direction=True)),
+            ("dopri8", dfx.Dopri8(), dfx.SaveAt(t1=True), pid, None)):
+        low, outs, r, row = ode_row(solver, saveat, ctrl, event)
+        row["time_over_base"] = row["ms"] / base["ms"]
+        if saveat.dense:
+            interp = outs[4]
+            q = torch.linspace(0.0, t1, 64, dtype=torch.float64, device=dev)
+            ms_q = _events_time(lambda: interp.evaluate(q), steps, warmup, flush)
+            yq = interp.evaluate(q)[:n_chk].double().cpu().numpy()
+            d = O.make_desc(**oracle_fields(low.fields))
+            rq = O.dense_evaluate(d, 0.0, t1, y0[:n_chk], r, q.cpu().numpy())
+            eq = np.abs(yq - rq).max(axis=(1, 2)) / np.abs(rq).max()
+            row["dense_bytes"] = int(outs[4].infos.numel() * outs[4].infos.element_size())
+            row["evaluate_64_times"] = {
+                "ms": ms_q, "rel_err_vs_fp64_oracle": {"median": float(np.median(eq)),
+                                                       "max": float(eq.max())}}
+        if event is not None:
+            ev = outs[5][:n_chk].cpu().numpy()
+            row["event_fired_frac"] = float((outs[5] >= 0).float().mean().item())
+            row["event_index_agrees_with_oracle"] = float((ev == r["event_index"]).mean())
+            tg = outs[1][:n_chk, -1].cpu().numpy()
+            row["event_time_abs_diff"] = {"median": float(np.median(np.abs(tg - r["ts"][:, -1]))),
+                                          "max": float(np.abs(tg - r["ts"][:, -1]).max())}
+        out["ode"][name] = row
+
+    # SDE rows
+    ys0 = rng.uniform(-2, 2, (B, 2))
+    ys0_d = torch.tensor(ys0, dtype=torch.float32, device=dev)
+    sargs = np.array([1.5, 0.5, 0.6])
+    sargs_d = torch.tensor(sargs, dtype=torch.float32, device=dev)
+    sde_base = None
+    for name, solver, levy in (("heun_w_tree", dfx.Heun(), dfx.BrownianIncrement),
+                               ("heun_levy_tree", dfx.Heun(), dfx.SpaceTimeLevyArea),
+                               ("shark", dfx.ShARK(), dfx.SpaceTimeLevyArea),
+                               ("sra1", dfx.SRA1(), dfx.SpaceTimeLevyArea),
+                               ("sea", dfx.SEA(), dfx.SpaceTimeLevyArea)):
+        bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (2,), key=5, levy_area=levy)
+        terms = dfx.MultiTerm(dfx.ODETerm(dfx.OrnsteinUhlenbeck()),
+                              dfx.ControlTerm(dfx.OrnsteinUhlenbeck(), bm))
+        low = Lowered(terms, solver, 0.0, 1.0, 0.01, ys0_d, sargs_d, dfx.SaveAt(t1=True),
+                      dfx.ConstantStepSize(), None, 4096, "fused", 0, 0)
+        ms = _events_time(low.run_forward, steps, warmup, flush)
+        ys_ = low.run_forward()[0][:n_chk, 0].double().cpu().numpy()
+        r = O.solve(O.make_desc(**oracle_fields(low.fields)), 0.0, 1.0, 0.01, ys0[:n_chk],
+                    args=sargs, nthreads=cores)
+        e = np.abs(ys_ - r["ys"][:, 0]).max(axis=1) / np.abs(r["ys"][:, 0]).max()
+        row = {"traj_per_s": B / (ms / 1e3), "ms": ms,
+               "t1_rel_err_vs_fp64_oracle": {"median": float(np.median(e)), "max": float(e.max())},
+               "steps": 100}
+        if sde_base is None:
+            sde_base = ms
+        row["time_over_heun_w_tree"] = ms / sde_base
+        out["sde"][name] = row
+    return out
+
+
 def workload_neural(dev, flush, steps, warmup, kind):
     """Neural ODE (64-128-128-64, Tsit5 PID(1e-5, 1e-7), batch 8192, t1 save,
     RecursiveCheckpointAdjoint(64), loss mean y(t1)^2), the wide neural ODE
@@ -741,6 +872,7 @@ def main():
             others["neural_ode"] = workload_neural(dev, flush, 5, 3, "ode")
             others["neural_ode_wide"] = workload_neural(dev, flush, 5, 3, "wide")
             others["neural_sde"] = workload_neural(dev, flush, 5, 3, "sde")
+            others["next_rows"] = workload_next_rows(dev, flush, 10, 3)
         except Exception as exc:  # report, never hide the headline line
             others["error"] = f"{type(exc).__name__}: {exc}"
 

@@ -656,6 +656,18 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
     P.dense_n = dense_n;
   }
   if (d.n_event > 0) P.event_index = ex ? ex->event_index : nullptr;
+  if (d.save_steps > 0 && problem->n_save > 0) {
+    // SaveAt(steps=n) reserves max_steps / n slots per trajectory, most of
+    // them unused: fill them all in one pass before the solve
+    cudaError_t e =
+        d.dtype == GBDX_F32
+            ? gbdx::launch_fill_saves_f32(static_cast<float *>(ys_out), ts_out, batch,
+                                          problem->n_save, d.dim, t0, t1, time_stride, s)
+            : gbdx::launch_fill_saves_f64(static_cast<double *>(ys_out), ts_out, batch,
+                                          problem->n_save, d.dim, t0, t1, time_stride, s);
+    if (e != cudaSuccess) return cuda_fail(e, "save buffer fill");
+    P.saves_prefilled = 1;
+  }
 
   gbdx::LaunchCfg cfg;
   cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;

@@ -455,6 +455,7 @@ struct SolveParams {
   // conversions)
   float rtol_f, atol_f, safety_f, factormin_f, factormax_f, c1_f, c2_f, c3_f;
   int n_ts, save_t0, save_t1, n_save, max_steps;
+  int saves_prefilled;        // the unused save slots were filled before the launch
   unsigned long long *queue;  // work-stealing counter (fused kernel)
   const int32_t *order;       // optional work order: queue slot -> trajectory
   // MLP fields and SDEs

@@ -37,6 +37,41 @@ cudaError_t fill_inf(T *p, int64_t n, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// The save buffers of a solve with many save slots (SaveAt(steps=n)): every
+// slot starts as the reference's unused save, ys = +inf and ts = direction *
+// inf (_integrate.py:1273-1293); the solve overwrites the slots it saves.  One
+// coalesced pass here replaces the per-trajectory fill loop at the end of each
+// trajectory, which runs on one lane of a warp at a time.
+template <class T>
+__global__ void fill_saves_kernel(T *ys, double *ts, int64_t batch, int n_save, int dim,
+                                  const double *t0, const double *t1, int64_t time_stride) {
+  const int64_t n = batch * n_save;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t b = i / n_save;
+    const int64_t ti = b * time_stride;
+    ts[i] = __ldg(t0 + ti) < __ldg(t1 + ti) ? INFINITY : -INFINITY;
+    for (int c = 0; c < dim; c++) ys[i * dim + c] = T(INFINITY);
+  }
+}
+
+template <class T>
+cudaError_t fill_saves(T *ys, double *ts, int64_t batch, int n_save, int dim, const double *t0,
+                       const double *t1, int64_t time_stride, cudaStream_t s) {
+  const int64_t n = batch * int64_t(n_save);
+  if (n <= 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  int64_t blocks = (n + 255) / 256;
+  const int64_t cap = int64_t(sms) * 8;
+  if (blocks > cap) blocks = cap;
+  fill_saves_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(ys, ts, batch, n_save, dim, t0, t1,
+                                                        time_stride);
+  return cudaGetLastError();
+}
+
 // Value (ORDER 0) or d/dtheta (ORDER 1) of the local interpolant of one step,
 // component n of the record r = (y0, y1, k_0 .. k_{S-1}).
 template <int SOLVER, class T>
@@ -152,6 +187,16 @@ cudaError_t dense_eval_t(int solver, const DenseEvalArgs &A, cudaStream_t s) {
 
 cudaError_t launch_fill_inf_f64(double *p, int64_t n, cudaStream_t s) { return fill_inf(p, n, s); }
 cudaError_t launch_fill_inf_f32(float *p, int64_t n, cudaStream_t s) { return fill_inf(p, n, s); }
+cudaError_t launch_fill_saves_f32(float *ys, double *ts, int64_t batch, int n_save, int dim,
+                                  const double *t0, const double *t1, int64_t time_stride,
+                                  cudaStream_t s) {
+  return fill_saves(ys, ts, batch, n_save, dim, t0, t1, time_stride, s);
+}
+cudaError_t launch_fill_saves_f64(double *ys, double *ts, int64_t batch, int n_save, int dim,
+                                  const double *t0, const double *t1, int64_t time_stride,
+                                  cudaStream_t s) {
+  return fill_saves(ys, ts, batch, n_save, dim, t0, t1, time_stride, s);
+}
 
 cudaError_t launch_dense_evaluate(int solver, int dtype, const DenseEvalArgs &A, cudaStream_t s) {
   return dtype == GBDX_F32 ? dense_eval_t<float>(solver, A, s) : dense_eval_t<double>(solver, A, s);

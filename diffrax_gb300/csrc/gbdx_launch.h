@@ -36,6 +36,13 @@ OdeEntry find_ode_entry_f64_xo(int solver, int field, int dim);
 // Fill n doubles (or floats) with +inf on stream s.
 cudaError_t launch_fill_inf_f64(double *p, int64_t n, cudaStream_t s);
 cudaError_t launch_fill_inf_f32(float *p, int64_t n, cudaStream_t s);
+// ys = +inf, ts = direction * inf over all [batch, n_save] save slots.
+cudaError_t launch_fill_saves_f32(float *ys, double *ts, int64_t batch, int n_save, int dim,
+                                  const double *t0, const double *t1, int64_t time_stride,
+                                  cudaStream_t s);
+cudaError_t launch_fill_saves_f64(double *ys, double *ts, int64_t batch, int n_save, int dim,
+                                  const double *t0, const double *t1, int64_t time_stride,
+                                  cudaStream_t s);
 // DenseInterpolation.evaluate / .derivative over a dense solve's outputs.
 struct DenseEvalArgs {
   int64_t batch, Q, q_stride, time_stride;

@@ -104,14 +104,24 @@ __device__ __forceinline__ T tsit5_dw(int j, T t) {
 // past the end (_get_t, clip.py:55-62); clip_find the first index whose time
 // is strictly greater than t, searched from a hint (_find_idx_with_hint,
 // clip.py:102-118).
+// The comparisons run on order keys (integer pipes; GB300 issues FP64
+// compares at ~1/64 of the FP32 rate), with -0 keyed as +0 so that key
+// equality and order are the FP64 ones; the sign flip is an integer XOR.
+__device__ __forceinline__ long long ckey(double x) {
+  const long long k = order_key(x);
+  return k == -1 ? 0 : k;
+}
 __device__ __forceinline__ double clip_get(const double *ts, int n, int i, int dir) {
   if (i >= n) return INFINITY;
-  return dir > 0 ? __ldg(ts + i) : -__ldg(ts + n - 1 - i);
+  if (dir > 0) return __ldg(ts + i);
+  return __longlong_as_double(__double_as_longlong(__ldg(ts + n - 1 - i)) ^
+                              (long long)0x8000000000000000ULL);
 }
 __device__ __forceinline__ int clip_find(const double *ts, int n, int dir, double t, int hint) {
+  const long long kt = ckey(t);
   int i = hint;
-  while (i < n && clip_get(ts, n, i, dir) <= t) i++;
-  while (i > 0 && clip_get(ts, n, i - 1, dir) > t) i--;
+  while (i < n && ckey(clip_get(ts, n, i, dir)) <= kt) i++;
+  while (i > 0 && ckey(clip_get(ts, n, i - 1, dir)) > kt) i--;
   return i;
 }
 
@@ -268,9 +278,14 @@ struct Traj {
       if (P.n_event > 0) {
         T f[D];
         FIELD::vf(P, args, y, f);
-        for (int e = 0; e < P.n_event; e++) {
-          evv[e] = ev_value(P, e, a, y, f);
-          if (evi < 0 && P.ev_kind[e] != GBDX_EV_LINEAR && evv[e] != 0.0) evi = e;
+        // unrolled over the condition slots: constant indices keep evv in
+        // registers and the parameter arrays in the constant bank
+#pragma unroll
+        for (int e = 0; e < GBDX_MAX_EVENTS; e++) {
+          if (e < P.n_event) {
+            evv[e] = ev_value(P, e, a, y, f);
+            if (evi < 0 && P.ev_kind[e] != GBDX_EV_LINEAR && evv[e] != 0.0) evi = e;
+          }
         }
         if (evi >= 0) result = GBDX_EVENT_OCCURRED;
       }
@@ -279,9 +294,9 @@ struct Traj {
 
   // Value of event condition e at the loop's time t and state yv, with f the
   // field there (steady_state_event); booleans are 0 / 1 (_event.py:120-175).
-  __device__ double ev_value(const SolveParams &P, int e, double t, const T *yv,
+  __device__ __forceinline__ double ev_value(const SolveParams &P, int e, double t, const T *yv,
                              const T *f) const {
-    const double *c = P.ev_coef + 6 * e;
+    const int c0 = 6 * e;  // coefficients P.ev_coef[c0 ..]
     if (P.ev_kind[e] == GBDX_EV_STEADY) {
       double sf = 0.0, sy = 0.0;
 #pragma unroll
@@ -289,20 +304,21 @@ struct Traj {
         sf += double(f[n]) * double(f[n]);
         sy += double(yv[n]) * double(yv[n]);
       }
-      return sqrt(sf / D) < c[1] + c[0] * sqrt(sy / D) ? 1.0 : 0.0;
+      return sqrt(sf / D) < P.ev_coef[c0 + 1] + P.ev_coef[c0 + 0] * sqrt(sy / D) ? 1.0 : 0.0;
     }
     double v = 0.0;
 #pragma unroll
-    for (int n = 0; n < (D < 4 ? D : 4); n++) v += c[n] * double(yv[n]);
-    v += c[4] * t;
-    v += c[5];
+    for (int n = 0; n < (D < 4 ? D : 4); n++) v += P.ev_coef[c0 + n] * double(yv[n]);
+    v += P.ev_coef[c0 + 4] * t;
+    v += P.ev_coef[c0 + 5];
     if (P.ev_kind[e] == GBDX_EV_LINEAR_BOOL) return v > 0 ? 1.0 : 0.0;
     return v;
   }
 
   // Whether condition e triggers between its values vo and vn: a boolean when
   // it holds, a real value on the chosen sign change (_integrate.py:585-602).
-  __device__ static bool ev_trig(const SolveParams &P, int e, double vo, double vn) {
+  __device__ __forceinline__ static bool ev_trig(const SolveParams &P, int e, double vo,
+                                                 double vn) {
     if (P.ev_kind[e] != GBDX_EV_LINEAR) return vn != 0.0;
     const double so = isnan(vo) ? vo : double((vo > 0) - (vo < 0));
     const double sn = isnan(vn) ? vn : double((vn > 0) - (vn < 0));
@@ -350,11 +366,11 @@ struct Traj {
   // atol + rtol |t| and |g| at the previous iterate below atol, from the
   // second iteration on, or fails after 256 iterations.  A boolean condition's
   // root is the end of the step.  y holds the step's y0.
-  __device__ double ev_root(const SolveParams &P, int e, const T (&k)[S][D], const T (&y1)[D],
-                            double tp, double tn, bool &ok) const {
+  __device__ __forceinline__ double ev_root(const SolveParams &P, int kind, const double (&cf)[6],
+                                            const T (&k)[S][D], const T (&y1)[D], double tp,
+                                            double tn, bool &ok) const {
     ok = true;
-    if (P.ev_kind[e] != GBDX_EV_LINEAR) return tn;
-    const double *c = P.ev_coef + 6 * e;
+    if (kind != GBDX_EV_LINEAR) return tn;
     const double span = tn - tp;
     double t = tn;
     for (int it = 1; it <= 256; it++) {
@@ -362,12 +378,12 @@ struct Traj {
       double g = 0.0, gp = 0.0;
 #pragma unroll
       for (int n = 0; n < (D < 4 ? D : 4); n++) {
-        g += c[n] * double(interp(th, n, k, y1));
-        gp += c[n] * (span == 0.0 ? 0.0 : double(interp_d(th, n, k, y1)) / span);
+        g += cf[n] * double(interp(th, n, k, y1));
+        gp += cf[n] * (span == 0.0 ? 0.0 : double(interp_d(th, n, k, y1)) / span);
       }
-      g += c[4] * t;
-      g += c[5];
-      gp += c[4];
+      g += cf[4] * t;
+      g += cf[5];
+      gp += cf[4];
       const double diff = g / gp;
       double nt = t - diff;
       nt = fmax(fmin(nt, tn), tp);
@@ -389,11 +405,13 @@ struct Traj {
     sidx = jidx = 0;
     if (P.n_step_ts > 0) {
       sidx = clip_find(P.step_ts, P.n_step_ts, dir, a, 0);
-      tn = fmin(tn, clip_get(P.step_ts, P.n_step_ts, sidx, dir));
+      const double st = clip_get(P.step_ts, P.n_step_ts, sidx, dir);
+      if (ckey(st) < ckey(tn)) tn = st;
     }
     if (P.n_jump_ts > 0) {
       jidx = clip_find(P.jump_ts, P.n_jump_ts, dir, a, 0);
-      tn = fmin(tn, next_down(clip_get(P.jump_ts, P.n_jump_ts, jidx, dir)));
+      const double jt = next_down(clip_get(P.jump_ts, P.n_jump_ts, jidx, dir));
+      if (ckey(jt) < ckey(tn)) tn = jt;
     }
     return tn;
   }
@@ -404,30 +422,33 @@ struct Traj {
   // times equal to nt0 or to nextafter(nt0) sit just below and at the first
   // index above nt0); the next step ends no later than the next step time and
   // just before the next jump.  Returns made_jump.
-  __device__ bool clip_adapt(const SolveParams &P, double &nt0, double &nt1) {
+  __device__ __forceinline__ bool clip_adapt(const SolveParams &P, double &nt0, double &nt1) {
     bool made = false;
     if (P.n_step_ts > 0) {
       const int n = P.n_step_ts;
       const int i = clip_find(P.step_ts, n, dir, nt0, sidx);
       const double n1 = next_up(nt0);
       double b0 = nt0;
-      if (i < n && clip_get(P.step_ts, n, i, dir) == n1) b0 = next_up(n1);
-      if (i > 0 && clip_get(P.step_ts, n, i - 1, dir) == nt0) b0 = n1;
+      if (i < n && ckey(clip_get(P.step_ts, n, i, dir)) == ckey(n1)) b0 = next_up(n1);
+      if (i > 0 && ckey(clip_get(P.step_ts, n, i - 1, dir)) == ckey(nt0)) b0 = n1;
       sidx = clip_find(P.step_ts, n, dir, b0, i);
-      nt1 = fmin(nt1, clip_get(P.step_ts, n, sidx, dir));
+      const double st = clip_get(P.step_ts, n, sidx, dir);
+      if (ckey(st) < ckey(nt1)) nt1 = st;
     }
     if (P.n_jump_ts > 0) {
       const int n = P.n_jump_ts;
       const int i = clip_find(P.jump_ts, n, dir, nt0, jidx);
       const double n1 = next_up(nt0);
-      const bool m1 = i < n && clip_get(P.jump_ts, n, i, dir) == n1;
-      const bool m2 = i > 0 && clip_get(P.jump_ts, n, i - 1, dir) == nt0;
+      const bool m1 = i < n && ckey(clip_get(P.jump_ts, n, i, dir)) == ckey(n1);
+      const bool m2 = i > 0 && ckey(clip_get(P.jump_ts, n, i - 1, dir)) == ckey(nt0);
       if (m1) nt0 = next_up(n1);
       if (m2) nt0 = n1;
       made = m1 || m2;
-      nt1 = fmax(next_up(nt0), nt1);  // never an empty interval (clip.py:354-372)
+      const double lo = next_up(nt0);  // never an empty interval (clip.py:354-372)
+      if (ckey(lo) > ckey(nt1)) nt1 = lo;
       jidx = clip_find(P.jump_ts, n, dir, nt0, i);
-      nt1 = fmin(nt1, next_down(clip_get(P.jump_ts, n, jidx, dir)));
+      const double jt = next_down(clip_get(P.jump_ts, n, jidx, dir));
+      if (ckey(jt) < ckey(nt1)) nt1 = jt;
     }
     return made;
   }
@@ -742,14 +763,19 @@ struct Traj {
             for (int n = 0; n < D; n++) fn[n] = flast[n];
           } else {
             bool steady = false;
-            for (int e = 0; e < P.n_event; e++) steady |= P.ev_kind[e] == GBDX_EV_STEADY;
+#pragma unroll
+            for (int e = 0; e < GBDX_MAX_EVENTS; e++)
+              steady |= e < P.n_event && P.ev_kind[e] == GBDX_EV_STEADY;
             if (steady) FIELD::vf(P, args, y1, fn);
           }
           int fired = -1;
-          for (int e = 0; e < P.n_event; e++) {
-            const double v = ev_value(P, e, tnext, y1, fn);
-            if (fired < 0 && ev_trig(P, e, evv[e], v)) fired = e;
-            evv[e] = v;
+#pragma unroll
+          for (int e = 0; e < GBDX_MAX_EVENTS; e++) {
+            if (e < P.n_event) {
+              const double v = ev_value(P, e, tnext, y1, fn);
+              if (fired < 0 && ev_trig(P, e, evv[e], v)) fired = e;
+              evv[e] = v;
+            }
           }
           if (fired >= 0) {
             evi = fired;
@@ -757,7 +783,19 @@ struct Traj {
             tfin = tnext;
             if (P.event_root) {
               bool ok = true;
-              tfin = ev_root(P, fired, k, y1, tprev, tnext, ok);
+              // the fired condition's kind and coefficients, selected with
+              // constant indices
+              int kind = GBDX_EV_LINEAR;
+              double cf[6];
+#pragma unroll
+              for (int e = 0; e < GBDX_MAX_EVENTS; e++) {
+                if (e == fired) {
+                  kind = P.ev_kind[e];
+#pragma unroll
+                  for (int n = 0; n < 6; n++) cf[n] = P.ev_coef[6 * e + n];
+                }
+              }
+              tfin = ev_root(P, kind, cf, k, y1, tprev, tnext, ok);
               if (!ok) result = GBDX_NONLINEAR_MAX_STEPS;
               const double span = tnext - tprev;
               const T th = T(span == 0.0 ? 0.0 : (tfin - tprev) / span);
@@ -926,11 +964,13 @@ struct Traj {
       P.ts_out[idx * P.n_save + save_index] = tf * dir;
       save_index++;
     }
-    for (int m = save_index; m < P.n_save; m++) {
-      T *o = ys_row(P, m);
+    if (!P.saves_prefilled) {
+      for (int m = save_index; m < P.n_save; m++) {
+        T *o = ys_row(P, m);
 #pragma unroll
-      for (int n = 0; n < D; n++) o[n] = T(INFINITY);
-      P.ts_out[idx * P.n_save + m] = dir > 0 ? INFINITY : -INFINITY;  // direction * inf
+        for (int n = 0; n < D; n++) o[n] = T(INFINITY);
+        P.ts_out[idx * P.n_save + m] = dir > 0 ? INFINITY : -INFINITY;  // direction * inf
+      }
     }
     if constexpr (XO) {
       if (P.dense_n) P.dense_n[idx] = nacc + 1;
