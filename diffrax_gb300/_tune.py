@@ -120,12 +120,22 @@ class GraphedSolve:
     the next call overwrites them (clone what must be kept).  ``autotune=True``
     picks the launch shape before capture.  Inputs in page-locked host memory
     are copied asynchronously: keep them unmodified until the outputs are read.
+
+    ``host_io=True`` serves a host-side caller with one graph launch per solve:
+    the inputs given as page-locked host tensors become the solve's staging
+    buffers, copied to the device inside the graph, and the outputs (ys, ts,
+    result, stats, and the event index) are copied into page-locked host
+    tensors inside it too.  A call then writes any new inputs into the staging
+    buffers (or the caller writes them there itself), replays the graph,
+    waits for it, and returns a Solution of host tensors (overwritten by the
+    next call).
     """
 
     def __init__(self, terms, solver, t0, t1, dt0, y0, args=None, *,
                  saveat: SaveAt = SaveAt(t1=True), stepsize_controller=None,
                  max_steps: int = 4096, throw: bool = True, kernel: str = "auto",
-                 schedule: str = "auto", autotune: bool = False, event=None):
+                 schedule: str = "auto", autotune: bool = False, event=None,
+                 host_io: bool = False):
         from ._core import ConstantStepSize
         if stepsize_controller is None:
             stepsize_controller = ConstantStepSize()
@@ -140,6 +150,15 @@ class GraphedSolve:
             t = t.to(device=dev, dtype=dtype or t.dtype)
             return t.clone().contiguous()  # the graph reads these buffers
 
+        # host_io: the page-locked host inputs stay bound as staging buffers
+        self._host_in = {}
+        if host_io:
+            for name, v in (("y0", y0), ("args", args), ("t0", t0), ("t1", t1), ("dt0", dt0)):
+                if isinstance(v, torch.Tensor) and v.device.type == "cpu":
+                    if not v.is_pinned():
+                        raise ValueError(f"host_io needs page-locked host tensors ({name}: "
+                                         "use Tensor.pin_memory())")
+                    self._host_in[name] = v
         y0 = own(y0)
         if y0.dtype not in (torch.float32, torch.float64):
             y0 = y0.to(torch.float64)
@@ -169,11 +188,32 @@ class GraphedSolve:
         self.low = low
         self._event = event
         run = low.run_forward_ex if event is not None else low.run_forward
-        run()  # warm-up outside the capture (first-use set-up of the library)
+        for name, h in self._host_in.items():
+            dst = getattr(low, name)
+            if h.numel() != dst.numel() or h.dtype != dst.dtype:
+                raise ValueError(f"host_io: {name} must be a {dst.dtype} tensor of "
+                                 f"{dst.numel()} entries")
+        warm = run()  # warm-up outside the capture (first-use set-up of the library)
+        self.host_io = bool(host_io)
+        self._host_out = []
+        if host_io:
+            self._host_out = [None if o is None else torch.empty(o.shape, dtype=o.dtype,
+                                                                  pin_memory=True)
+                              for o in warm]
         torch.cuda.synchronize()
+
+        def staged():
+            for name, h in self._host_in.items():
+                dst = getattr(low, name)
+                dst.copy_(h.reshape(dst.shape), non_blocking=True)
+            outs = run()
+            for o, h in zip(outs, self._host_out):
+                if h is not None and o is not None and isinstance(o, torch.Tensor):
+                    h.copy_(o, non_blocking=True)
+            return outs
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
-            self._outs = run()
+            self._outs = staged()
         torch.cuda.synchronize()
 
     def _copy_in(self, name, value):
@@ -189,10 +229,21 @@ class GraphedSolve:
 
     def __call__(self, y0=None, args=None, t0=None, t1=None, dt0=None) -> Solution:
         for name, v in (("y0", y0), ("args", args), ("t0", t0), ("t1", t1), ("dt0", dt0)):
-            if v is not None:
+            if v is None:
+                continue
+            h = self._host_in.get(name)
+            if h is None:
                 self._copy_in(name, v)
+            elif v is not h:
+                src = torch.as_tensor(v)
+                if src.numel() != h.numel():
+                    raise ValueError(f"{name} must keep the captured shape {tuple(h.shape)}")
+                h.copy_(src.reshape(h.shape))  # into the staging buffer
         self.graph.replay()
         outs = self._outs
+        if self.host_io:
+            torch.cuda.current_stream().synchronize()
+            outs = [h if h is not None else o for o, h in zip(outs, self._host_out)]
         ys, ts, res, stats = outs[:4]
         sol = Solution(t0=self.low.t0, t1=self.low.t1, ts=ts, ys=ys,
                        stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],

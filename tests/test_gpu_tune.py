@@ -97,3 +97,27 @@ def test_graphed_solve_with_event():
     ref = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1n, None, y0n, mun, stepsize_controller=PID,
                           event=ev, throw=False)
     assert torch.equal(sol.ys, ref.ys) and torch.equal(sol.event_mask, ref.event_mask)
+
+
+def test_graphed_solve_host_io():
+    # host_io: the page-locked inputs are the graph's staging buffers and the
+    # outputs land in page-locked host tensors, one graph launch per solve
+    term = dfx.ODETerm(dfx.VanDerPol())
+    y0, mu, t1 = vdp_inputs(4096, 7)
+    y0_h, mu_h, t1_h = (x.cpu().pin_memory() for x in (y0, mu, t1))
+    g = dfx.GraphedSolve(term, dfx.Dopri5(), 0.0, t1_h, None, y0_h, mu_h,
+                         stepsize_controller=PID, throw=False, host_io=True)
+    sol = g()
+    ref = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1, None, y0, mu, stepsize_controller=PID)
+    assert sol.ys.device.type == "cpu" and sol.ys.is_pinned()
+    assert torch.equal(sol.ys, ref.ys.cpu()) and torch.equal(sol.result, ref.result.cpu())
+    # new inputs written into the staging buffers by the caller, or passed
+    y0n, mun, t1n = vdp_inputs(4096, 8)
+    y0_h.copy_(y0n.cpu())
+    sol = g(args=mun.cpu(), t1=t1n.cpu())
+    ref = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1n, None, y0n, mun, stepsize_controller=PID)
+    assert torch.equal(sol.ys, ref.ys.cpu())
+    assert torch.equal(sol.stats["num_steps"], ref.stats["num_steps"].cpu())
+    with pytest.raises(ValueError, match="page-locked"):
+        dfx.GraphedSolve(term, dfx.Dopri5(), 0.0, t1.cpu(), None, y0.cpu(), mu.cpu(),
+                         stepsize_controller=PID, host_io=True)
