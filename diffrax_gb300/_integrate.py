@@ -377,7 +377,7 @@ class Lowered:
         interp = ev = None
         if self.fields["save_dense"]:
             L = int(self.fields["max_steps"]) + 1
-            stages = {0: 1, 1: 2, 2: 7, 3: 7, 4: 14}[self.fields["solver"]]
+            stages = {0: 1, 1: 2, 2: 7, 3: 7, 4: 14, 5: 2, 6: 2, 7: 1}[self.fields["solver"]]
             dense_ts = torch.empty((B, L), dtype=torch.float64, device=dev)
             dense_info = torch.empty((B, L - 1, (2 + stages) * D), dtype=self.dtype, device=dev)
             dense_n = torch.empty((B,), dtype=torch.int32, device=dev)

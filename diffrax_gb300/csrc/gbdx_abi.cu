@@ -190,6 +190,18 @@ static int solver_order(int solver) {
     default: return 5;
   }
 }
+// Stages of a solver: the k vectors of its dense-output record.
+static int solver_stages(int solver) {
+  switch (solver) {
+    case GBDX_EULER: return 1;
+    case GBDX_HEUN: return 2;
+    case GBDX_DOPRI8: return 14;
+    case GBDX_SHARK: return 2;
+    case GBDX_SRA1: return 2;
+    case GBDX_SEA: return 1;
+    default: return 7;
+  }
+}
 static double solver_strong_order(int solver) {
   if (solver == GBDX_SHARK || solver == GBDX_SRA1) return 1.5;
   if (solver == GBDX_SEA) return 1.0;
@@ -293,11 +305,13 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     return fail(GBDX_ERR_INVALID, "the root finder needs rtol >= 0 and atol > 0");
   }
   const bool xo = d.save_steps > 0 || d.save_dense || clip || d.n_event > 0;
-  if (xo && (d.field == GBDX_MLP || sde || d.adjoint != GBDX_ADJ_NONE)) {
+  if (xo && (d.field == GBDX_MLP || d.adjoint != GBDX_ADJ_NONE ||
+             (sde && d.diffusion != GBDX_DIFF_OU))) {
     delete p;
     return fail(GBDX_ERR_UNSUPPORTED,
                 "SaveAt(steps=...), SaveAt(dense=True), ClipStepSizeController and events "
-                "are available for forward solves of the analytic ODE fields");
+                "are available for forward solves of the analytic fields (ODEs and the "
+                "Ornstein-Uhlenbeck SDE)");
   }
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
                d.field == GBDX_ORNSTEIN_UHLENBECK)) {
@@ -319,8 +333,10 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
                   "the Ornstein-Uhlenbeck SDE runs with FP32 state (FP32 Brownian tree)");
     }
     p->ode = d.levy_area == GBDX_LEVY_SPACE_TIME
-                 ? gbdx::find_ode_sde_levy_entry_f32(d.solver, d.dim)
-                 : gbdx::find_ode_sde_entry_f32(d.solver, d.dim);
+                 ? (xo ? gbdx::find_ode_sde_levy_entry_f32_xo(d.solver, d.dim)
+                       : gbdx::find_ode_sde_levy_entry_f32(d.solver, d.dim))
+                 : (xo ? gbdx::find_ode_sde_entry_f32_xo(d.solver, d.dim)
+                       : gbdx::find_ode_sde_entry_f32(d.solver, d.dim));
     if (!p->ode.launch) {
       delete p;
       return fail(GBDX_ERR_UNSUPPORTED,
@@ -639,10 +655,7 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
   if (d.save_dense) {
     // The reference's dense buffers start full of +inf (_integrate.py:1315-1323);
     // the solve overwrites the recorded steps.
-    const int stages = d.solver == GBDX_EULER    ? 1
-                       : d.solver == GBDX_HEUN   ? 2
-                       : d.solver == GBDX_DOPRI8 ? 14
-                                                 : 7;
+    const int stages = solver_stages(d.solver);
     const int64_t rec = int64_t(2 + stages) * d.dim;
     cudaError_t e = gbdx::launch_fill_inf_f64(dense_ts, batch * (int64_t(d.max_steps) + 1), s);
     if (e == cudaSuccess) {

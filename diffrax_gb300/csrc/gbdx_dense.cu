@@ -178,6 +178,10 @@ cudaError_t dense_eval_t(int solver, const DenseEvalArgs &A, cudaStream_t s) {
     case GBDX_DOPRI5: dense_eval_kernel<GBDX_DOPRI5, T><<<blocks, 256, 0, s>>>(A); break;
     case GBDX_TSIT5: dense_eval_kernel<GBDX_TSIT5, T><<<blocks, 256, 0, s>>>(A); break;
     case GBDX_DOPRI8: dense_eval_kernel<GBDX_DOPRI8, T><<<blocks, 256, 0, s>>>(A); break;
+    // the additive-noise SRKs interpolate linearly (srk.py:268, 670)
+    case GBDX_SHARK: dense_eval_kernel<GBDX_SHARK, T><<<blocks, 256, 0, s>>>(A); break;
+    case GBDX_SRA1: dense_eval_kernel<GBDX_SRA1, T><<<blocks, 256, 0, s>>>(A); break;
+    case GBDX_SEA: dense_eval_kernel<GBDX_SEA, T><<<blocks, 256, 0, s>>>(A); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

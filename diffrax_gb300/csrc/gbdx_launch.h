@@ -30,6 +30,9 @@ OdeEntry find_ode_sde_entry_f32(int solver, int dim);
 // The Ornstein-Uhlenbeck SDE driven by the space-time Levy area tree (Euler,
 // Heun, Dopri5, Tsit5 use its W; ShARK also its H).
 OdeEntry find_ode_sde_levy_entry_f32(int solver, int dim);
+// The same with the extended outputs (SaveAt(steps), dense, clip, events).
+OdeEntry find_ode_sde_entry_f32_xo(int solver, int dim);
+OdeEntry find_ode_sde_levy_entry_f32_xo(int solver, int dim);
 // The same kernels with SaveAt(steps=n) / SaveAt(dense=True) outputs.
 OdeEntry find_ode_entry_f32_xo(int solver, int field, int dim);
 OdeEntry find_ode_entry_f64_xo(int solver, int field, int dim);

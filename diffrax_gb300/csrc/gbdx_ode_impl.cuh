@@ -56,10 +56,10 @@ OdeEntry find_ode_entry_t(int solver, int field, int dim) {
 }
 
 // The Ornstein-Uhlenbeck SDE (FP32 state: the tree's values are FP32).
-template <bool LEVY>
+template <bool LEVY, bool XO = false>
 inline OdeEntry find_ode_sde_entry_t(int solver, int dim) {
 #define GBDX_ENTRY(S, F) \
-  OdeEntry { &launch_ode<S, F, float, false>, &occupancy_ode<S, F, float, false> }
+  OdeEntry { &launch_ode<S, F, float, XO>, &occupancy_ode<S, F, float, XO> }
 #define GBDX_SOLVERS(F)                                        \
   switch (solver) {                                            \
     case GBDX_EULER: return GBDX_ENTRY(GBDX_EULER, F);         \

@@ -159,8 +159,9 @@ typedef struct gbdx_problem_desc {
    * ev_coef[6 i + n] = w_n (n < dim), [6 i + 4] = wt, [6 i + 5] = c; STEADY
    * [6 i] = rtol, [6 i + 1] = atol.  event_root = 1 locates the event time by
    * Newton's method (optimistix.Newton(newton_rtol, newton_atol)) on the last
-   * step's interpolant.  Forward solves of the analytic fields; solve with
-   * gbdx_solve_fwd_ex to read which condition fired. */
+   * step's interpolant.  Forward solves of the analytic fields (ODEs and the
+   * Ornstein--Uhlenbeck SDE); solve with gbdx_solve_fwd_ex to read which
+   * condition fired. */
   int32_t n_event, event_root;
   int32_t ev_kind[GBDX_MAX_EVENTS], ev_dir[GBDX_MAX_EVENTS];
   /* The VirtualBrownianTree's levy_area (gbdx_levy_area): SPACE_TIME draws the

@@ -1511,7 +1511,6 @@ int orc_solve_dense(const orc_desc *d, int64_t B, const double *t0, const double
   if (d->levy_area != 0 && d->levy_area != 1) return -1;
   /* the SRKs take the SpaceTimeLevyArea of an SDE's tree (srk.py:374-379) */
   if (ORC_IS_SRK(d->solver) && (d->diffusion == ORC_DIFF_NONE || !d->levy_area)) return -1;
-  if (ORC_IS_SRK(d->solver) && d->save_dense) return -2;
   /* pid.py:437-447: adaptive steps need an error estimate */
   if (d->controller == ORC_PID && d->solver == ORC_SEA) return -1;
   SolveIO io = {d, t0, t1, dt0, time_stride, y0, args, args_stride, params, ts,
