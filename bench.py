@@ -365,6 +365,34 @@ def profile_backsolve(dev, B, seminorm, n):
         sys.exit(1)
 
 
+def profile_saveat_steps(dev, n):
+    """`--profile saveat_steps`: n rounds of the SaveAt(t1) and the
+    SaveAt(steps=3) solves of the Van der Pol rows of workload_next_rows
+    (batch 16384, t in [0, 10]), alternating, for a launch-by-launch
+    comparison of the plain and the extended-output fused kernels."""
+    import torch
+    import diffrax_gb300 as dfx
+    from diffrax_gb300._integrate import Lowered
+    B = 16384
+    rng = np.random.default_rng(7)
+    mu = np.exp(rng.uniform(np.log(0.1), np.log(10.0), B))
+    y0 = rng.uniform(-2, 2, (B, 2))
+    y0_d = torch.tensor(y0, dtype=torch.float32, device=dev)
+    mu_d = torch.tensor(mu[:, None], dtype=torch.float32, device=dev)
+    pid = dfx.PIDController(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4)
+    lows = [Lowered(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(), 0.0, 10.0, None, y0_d, mu_d,
+                    sa, pid, None, 1024, "fused", 0, 0)
+            for sa in (dfx.SaveAt(t1=True), dfx.SaveAt(steps=3, t1=True))]
+    ok = True
+    for _ in range(n):
+        for low in lows:
+            ok = ok and bool((low.run_forward()[2] == 0).all().item())
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "saveat_steps", "rounds": n, "all_successful": ok}))
+    if not ok:
+        sys.exit(1)
+
+
 def profile_neural(dev, which, B, n):
     """n fused solves of a neural workload at batch B, for ncu: the forward of
     the neural ODE (64-128-128-64, row-tile or tcgen05 kernel), its forward +
@@ -717,7 +745,7 @@ def main():
     ap.add_argument("--profile", default=None,
                     choices=["fused", "plain", "backsolve", "backsolve_seminorm", "neural_ode",
                              "neural_ode_tc", "neural_ode_grad", "neural_ode_wide",
-                             "neural_sde"],
+                             "neural_sde", "saveat_steps"],
                     help="run warmup + steps eager solves of one kernel only (for ncu); "
                          "backsolve*: forward + backward of the wide neural ODE at --batch")
     args = ap.parse_args()
@@ -796,6 +824,9 @@ def main():
         return
     if args.profile and args.profile.startswith("neural"):
         profile_neural(dev, args.profile, B, args.warmup + args.steps)
+        return
+    if args.profile == "saveat_steps":
+        profile_saveat_steps(dev, args.warmup + args.steps)
         return
     if args.profile:
         low = lowered(args.profile)
