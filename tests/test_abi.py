@@ -328,3 +328,34 @@ def test_shark_and_levy_tree_scope():
     assert _lib.Problem(dfx.lower(terms(dfx.SpaceTimeLevyArea), dfx.ShARK(),
                                   dfx.ConstantStepSize(), dfx.SaveAt(dense=True), dim=2,
                                   dtype=torch.float32, max_steps=100, n_ts=0)).n_save == 0
+
+
+def test_sde_extended_output_scope():
+    # SaveAt(steps / dense), the clip controller and events serve the
+    # Ornstein-Uhlenbeck SDE on either tree; the MLP SDE keeps SaveAt(ts / t0 / t1)
+    pid = dfx.PIDController(rtol=1e-3, atol=1e-3)
+    for levy, solver in ((dfx.BrownianIncrement, dfx.Heun()),
+                         (dfx.SpaceTimeLevyArea, dfx.ShARK())):
+        bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (2,), key=0, levy_area=levy)
+        terms = dfx.MultiTerm(dfx.ODETerm(dfx.OrnsteinUhlenbeck()),
+                              dfx.ControlTerm(dfx.OrnsteinUhlenbeck(), bm))
+        for saveat, ctrl, event in (
+                (dfx.SaveAt(steps=2, t1=True), dfx.ConstantStepSize(), None),
+                (dfx.SaveAt(dense=True), dfx.ConstantStepSize(), None),
+                (dfx.SaveAt(t1=True), dfx.ClipStepSizeController(pid, step_ts=[0.5]), None),
+                (dfx.SaveAt(t1=True), dfx.ConstantStepSize(),
+                 dfx.Event(dfx.LinearCondition([1.0, 0.0]), dfx.Newton(1e-5, 1e-5)))):
+            f = dfx.lower(terms, solver, ctrl, saveat, dim=2, dtype=torch.float32,
+                          max_steps=64, n_ts=0, event=event)
+            p = _lib.Problem(f)
+            assert p.n_save == (32 if saveat.steps else (0 if saveat.dense else 1))
+    W = [torch.zeros(8, 4), torch.zeros(8, 8), torch.zeros(4, 8)]
+    b = [torch.zeros(8), torch.zeros(8), torch.zeros(4)]
+    bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (4,), key=0)
+    terms = dfx.MultiTerm(dfx.ODETerm(dfx.MLPField(W, b)),
+                          dfx.ControlTerm(dfx.TanhDiagonalDiffusion(torch.zeros(4, 4),
+                                                                    torch.zeros(4)), bm))
+    f = dfx.lower(terms, dfx.Heun(), dfx.ConstantStepSize(), dfx.SaveAt(steps=2, t1=True),
+                  dim=4, dtype=torch.float32, max_steps=64, n_ts=0)
+    with pytest.raises(_lib.GbdxError, match="Ornstein-Uhlenbeck SDE"):
+        _lib.Problem(f)

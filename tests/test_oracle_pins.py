@@ -660,6 +660,28 @@ def test_additive_srk_limit_is_heuns_limit():
     assert _path_l2_dist(_nonlinear_additive_sde(O.SEA, 11)[0], ref) < 2e-3
 
 
+@pytest.mark.parametrize("solver, levy", [(O.HEUN, 0), (O.SHARK, 1)])
+def test_sde_extended_outputs_agree(solver, levy):
+    # On one Brownian path and a constant-step grid: SaveAt(steps=1) saves the
+    # step ends, SaveAt(ts=grid) interpolates to the same points, and the dense
+    # output evaluated there gives them again (_integrate.py:456-540).
+    kw = dict(solver=solver, controller=O.CONSTANT, field=O.ORNSTEIN_UHLENBECK, dim=2,
+              diffusion=O.DIFF_OU, vbt_t0=0.0, vbt_t1=1.0, vbt_tol=1e-3, seed=23,
+              levy_area=levy, n_args=3, max_steps=20, save_t1=0)
+    rng = np.random.default_rng(5)
+    y0 = rng.uniform(-1, 1, (16, 2))
+    args = [1.5, 0.5, 0.6]
+    grid = np.linspace(0.05, 1.0, 20)
+    a = O.solve(O.make_desc(save_steps=1, **kw), 0.0, 1.0, 0.05, y0, args=args)
+    b = O.solve(O.make_desc(n_ts=20, **kw), 0.0, 1.0, 0.05, y0, args=args, ts=grid)
+    assert np.allclose(a["ts"], grid[None, :], rtol=0, atol=1e-15)
+    assert np.allclose(a["ys"], b["ys"], rtol=1e-12, atol=1e-12)
+    d = O.make_desc(save_dense=1, save_t1=1, **{k: v for k, v in kw.items() if k != "save_t1"})
+    c = O.solve(d, 0.0, 1.0, 0.05, y0, args=args)
+    q = O.dense_evaluate(d, 0.0, 1.0, y0, c, grid)
+    assert np.allclose(q, a["ys"], rtol=1e-12, atol=1e-12)
+
+
 def test_srk_needs_levy_area():
     # srk.py:374-379: a tree without the space-time Levy area is rejected;
     # SEA has no error estimate for adaptive steps (pid.py:437-447).
