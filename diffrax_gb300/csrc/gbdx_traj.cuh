@@ -1,7 +1,8 @@
 // gbdx_traj.cuh -- one trajectory of a vmapped diffeqsolve, held in registers.
 //
 // Traj<SOLVER, FIELD, T>::step() is one iteration of the reference's outer
-// while-loop body (diffrax/_integrate.py:365-662): an explicit RK step, the
+// while-loop body (diffrax/_integrate.py:365-662): an explicit RK step (or,
+// for the additive-noise SRKs, the stochastic step of srk.py:335-671), the
 // NaN->inf error guard (:386), the controller (pid.py:394-567 or
 // constant.py:59-104), clip-to-end (:410-413, 278-284), the keep/reject select
 // (:422-430), the step counters (:433-437) and the SaveAt(ts) loop (:456-487).
