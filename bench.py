@@ -75,16 +75,11 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "fused_kernel_vdp_dopri5.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except OSError:
-        pass
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the fused kernel on this workload, from an ncu capture of the same command
+# (bench.py --profile fused); not measured in a bench run (a run under ncu is
+# never timed).
+NCU_TRAFFIC_BYTES_PER_LAUNCH = 2119936.0
 
 
 class ClockSampler:
@@ -149,8 +144,9 @@ def run_reference(args):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    sample = args.ref_sample
-    mu, y0, t1 = vdp_inputs(sample, args.seed)
+    sample = args.ref_sample if args.ref_sample > 0 else args.batch
+    mu, y0, t1 = vdp_inputs(args.batch, args.seed)
+    mu, y0, t1 = mu[:sample], y0[:sample], t1[:sample]
     for _ in range(args.warmup):
         oracle_solve(mu, y0, t1, cores)
     times = []
@@ -164,7 +160,8 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "batch_per_step": sample,
+        "config": {"workload": WORKLOAD, "batch_per_gpu": args.batch,
+                   "batch_per_step": sample,
                    "note": "Diffrax (JAX) is not installable offline; this is the FP64 C "
                            "restatement of its solve loop with OpenMP over trajectories"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -252,87 +249,6 @@ def workload_lotka_volterra(dev, flush, steps, warmup):
         O.make_desc(solver=O.TSIT5, controller=O.PID, field=O.LOTKA_VOLTERRA, dim=2, rtol=1e-6,
                     atol=1e-8, n_ts=100, save_t1=0, n_args=4),
         0.0, 140.0, 0.1, y0, args=args, ts=ts, nthreads=cores), B, cores)
-    return out
-
-
-def workload_backsolve(dev, flush, steps, warmup, terms_for, solver, ctrl, saveat, ts, y0,
-                       y0_d, params, desc, B, D):
-    """Forward + BacksolveAdjoint backward of loss = sum over the saved points of
-    mean(y^2): the reference's default rms_norm (a_theta in the error norm,
-    streamed from HBM) and adjoint_rms_seminorm.  Width 256 holds BF16
-    weights, so the oracle runs with the same BF16-rounded weights."""
-    import torch
-    import diffrax_gb300 as dfx
-    import oracle as O
-    from diffrax_gb300._integrate import Lowered
-    cores = os.cpu_count() or 1
-    p_bf16 = torch.tensor(params, dtype=torch.float32).to(torch.bfloat16).double().numpy()
-    # biases stay FP32 (only the weight matrices are BF16 operands)
-    widths = [64, 256, 256, 64]
-    off = 0
-    for i in range(3):
-        n_w = widths[i] * widths[i + 1]
-        p_bf16[off + n_w:off + n_w + widths[i + 1]] = params[off + n_w:off + n_w + widths[i + 1]]
-        off += n_w + widths[i + 1]
-    out = {}
-    for name, adj in (("rms_norm", dfx.BacksolveAdjoint()),
-                      ("seminorm", dfx.BacksolveAdjoint(stepsize_controller=dfx.PIDController(
-                          rtol=ctrl.rtol, atol=ctrl.atol, norm=dfx.adjoint_rms_seminorm)))):
-        low = Lowered(terms_for("bf16"), solver, 0.0, 1.0, None, y0_d, None, saveat, ctrl, adj,
-                      4096, "fused", 0, 0, want_grad=True)
-
-        def fwd_bwd():
-            ys_, ts_, _, _ = low.run_forward()
-            gys = ys_ * (2.0 / (B * D))
-            return low.run_backsolve(ts_, ys_, gys, low.params)
-        ms = _events_time(fwd_bwd, steps, warmup, flush)
-        gy0, gp, res, st = fwd_bwd()
-        n_g = 32
-        ys_, ts_, _, _ = low.run_forward()
-        ys_g = ys_[:n_g].double().cpu().numpy()
-        bdesc = O.make_desc(**dfx.oracle_fields(low.bwd_fields))
-        # the oracle gradient of the first n_g trajectories, from the same saves
-        gys = 2.0 * ys_g / (B * D)
-        t = time.perf_counter()
-        r = O.backsolve(bdesc, 0.0, 1.0, None, ts_[:n_g].cpu().numpy(), ys_g, gys,
-                        params=p_bf16, nthreads=cores)
-        dt_cpu = time.perf_counter() - t
-        gy0_g = gy0[:n_g].double().cpu().numpy()
-        ent = {"grads_per_s": B / (ms / 1e3), "ms": ms, "unit": "trajectory gradients/s",
-               "mean_backward_steps": float(st[:, 0].float().mean().item()),
-               "backward_failures": int((res != 0).sum().item()),
-               "dL_dy0_max_rel_err_vs_fp64_oracle": float(
-                   np.abs(gy0_g - r["grad_y0"]).max() / np.abs(r["grad_y0"]).max()),
-               "oracle_mean_backward_steps": float(r["stats"][:, 0].mean()),
-               "cpu_baseline": {"value": n_g / dt_cpu, "unit": "trajectory gradients/s",
-                                "cores": cores, "kind": "port",
-                                "sample": f"{n_g} trajectories backward only, FP64 oracle, "
-                                          f"{dt_cpu:.2f} s"}}
-        if name == "rms_norm":
-            peaks, src = measured_peaks()
-            n_par = int(low.params.numel())
-            stream = float(st[:, 0].double().sum().item()) * 2 * 4 * n_par
-            ent["roofline"] = {
-                "bound": "hbm", "achieved": stream / (ms / 1e3) / 1e9,
-                "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
-                "frac": stream / (ms / 1e3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
-                "peak_source": src,
-                "work": "a_theta double buffer: 8 bytes per parameter per trajectory-step "
-                        "(read a_theta0, write the candidate); timed region = forward + "
-                        "backward"}
-            # the plain form: one trajectory per thread, FP32 CUDA cores
-            plow = Lowered(terms_for("bf16"), solver, 0.0, 1.0, None, y0_d, None, saveat, ctrl,
-                           adj, 4096, "plain", 0, 0, want_grad=True)
-
-            def fwd_bwd_plain():
-                ys_, ts_, _, _ = plow.run_forward()
-                gys_ = ys_ * (2.0 / (B * D))
-                return plow.run_backsolve(ts_, ys_, gys_, plow.params)
-            ms_p = _events_time(fwd_bwd_plain, 1, 0, flush)  # one ~40 s solve
-            ent["plain_forward_adjoint"] = {"grads_per_s": B / (ms_p / 1e3), "ms": ms_p}
-            ent["fused_over_plain"] = ms_p / ms
-            ent["a_theta_stream_bytes"] = stream
-        out[f"backsolve_{name}"] = ent
     return out
 
 
@@ -459,7 +375,7 @@ def workload_next_rows(dev, flush, steps, warmup):
     import torch
     import diffrax_gb300 as dfx
     import oracle as O
-    from diffrax_gb300._integrate import Lowered, oracle_fields
+    from diffrax_gb300._integrate import Lowered
     B, n_chk, t1 = 16384, 256, 10.0
     cores = os.cpu_count() or 1
     rng = np.random.default_rng(7)
@@ -480,7 +396,7 @@ def workload_next_rows(dev, flush, steps, warmup):
         ms = _events_time(run, steps, warmup, flush)
         outs = run()
         ts_ = np.asarray(saveat.ts) if saveat.ts is not None else None
-        d = O.make_desc(**oracle_fields(low.fields))
+        d = O.make_desc(**O.oracle_fields(low.fields))
         kw = {}
         if isinstance(ctrl, dfx.ClipStepSizeController):
             kw = dict(step_ts=ctrl.step_ts, jump_ts=ctrl.jump_ts)
@@ -522,7 +438,7 @@ def workload_next_rows(dev, flush, steps, warmup):
             q = torch.linspace(0.0, t1, 64, dtype=torch.float64, device=dev)
             ms_q = _events_time(lambda: interp.evaluate(q), steps, warmup, flush)
             yq = interp.evaluate(q)[:n_chk].double().cpu().numpy()
-            d = O.make_desc(**oracle_fields(low.fields))
+            d = O.make_desc(**O.oracle_fields(low.fields))
             rq = O.dense_evaluate(d, 0.0, t1, y0[:n_chk], r, q.cpu().numpy())
             eq = np.abs(yq - rq).max(axis=(1, 2)) / np.abs(rq).max()
             row["dense_bytes"] = int(outs[4].infos.numel() * outs[4].infos.element_size())
@@ -556,7 +472,7 @@ def workload_next_rows(dev, flush, steps, warmup):
                       dfx.ConstantStepSize(), None, 4096, "fused", 0, 0)
         ms = _events_time(low.run_forward, steps, warmup, flush)
         ys_ = low.run_forward()[0][:n_chk, 0].double().cpu().numpy()
-        r = O.solve(O.make_desc(**oracle_fields(low.fields)), 0.0, 1.0, 0.01, ys0[:n_chk],
+        r = O.solve(O.make_desc(**O.oracle_fields(low.fields)), 0.0, 1.0, 0.01, ys0[:n_chk],
                     args=sargs, nthreads=cores)
         e = np.abs(ys_ - r["ys"][:, 0]).max(axis=1) / np.abs(r["ys"][:, 0]).max()
         row = {"traj_per_s": B / (ms / 1e3), "ms": ms,
@@ -569,165 +485,421 @@ def workload_next_rows(dev, flush, steps, warmup):
     return out
 
 
+def _per_row_max(a, b):
+    """max over rows of max|a - b| / max|b| within the row."""
+    return float(_rel_per_traj(a, b).max())
+
+
+def _vec_rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+class _NeuralCase:
+    """One neural workload: its inputs, its Lowered solves per kernel form and
+    precision, and the FP64 oracle on a subset of its trajectories."""
+
+    def __init__(self, dev, kind):
+        import torch
+        import diffrax_gb300 as dfx
+        self.dev, self.kind = dev, kind
+        self.cores = os.cpu_count() or 1
+        if kind == "ode":
+            self.widths, self.B, seed = [64, 128, 128, 64], 8192, 21
+            self.solver, self.ctrl, self.dt0 = (dfx.Tsit5(),
+                                                dfx.PIDController(rtol=1e-5, atol=1e-7), None)
+            self.ts, self.sde = None, False
+            self.adjoint = dfx.RecursiveCheckpointAdjoint(checkpoints=64)
+            self.name = "neural_ode_64_128_tsit5_pid_b8192_recursive64"
+        elif kind == "wide":
+            self.widths, self.B, seed = [64, 256, 256, 64], 16384, 22
+            self.solver, self.ctrl, self.dt0 = (dfx.Tsit5(),
+                                                dfx.PIDController(rtol=1e-5, atol=1e-7), None)
+            self.ts, self.sde = np.linspace(0.0, 1.0, 32), False
+            self.adjoint = dfx.BacksolveAdjoint()
+            self.name = "neural_ode_64_256_tsit5_pid_b16384_ts32_backsolve"
+        else:
+            self.widths, self.B, seed = [32, 64, 64, 32], 32768, 23
+            self.solver, self.ctrl, self.dt0 = dfx.Heun(), dfx.ConstantStepSize(), 0.01
+            self.ts, self.sde = None, True
+            # the default checkpoint count (ceil(log2(max_steps)))
+            self.adjoint = dfx.RecursiveCheckpointAdjoint()
+            self.name = "neural_sde_32_64_heun_dt0.01_vbt1e-3_b32768_recursive"
+        self.saveat = dfx.SaveAt(ts=self.ts) if self.ts is not None else dfx.SaveAt(t1=True)
+        w, D = self.widths, self.widths[0]
+        self.D, self.seed = D, seed
+        Ws, bs = _mlp_np(w, seed)
+        rng = np.random.default_rng(seed + 1)
+        self.y0 = rng.standard_normal((self.B, D)).astype(np.float32)
+        params = [np.concatenate([W.reshape(-1), b]) for W, b in zip(Ws, bs)]
+        self.tW = [torch.tensor(W, device=dev) for W in Ws]
+        self.tb = [torch.tensor(b, device=dev) for b in bs]
+        if self.sde:
+            Wsig = (rng.standard_normal((D, D)) / np.sqrt(D)).astype(np.float32)
+            bsig = np.zeros(D, np.float32)
+            self.tWs, self.tbs = torch.tensor(Wsig, device=dev), torch.tensor(bsig, device=dev)
+            params += [Wsig.reshape(-1), bsig]
+        self.params = np.concatenate(params).astype(np.float64)
+        # the BF16 weight values the width-256 tensor-core kernels hold (biases FP32)
+        p16 = torch.tensor(self.params, dtype=torch.float32).to(torch.bfloat16).double().numpy()
+        off = 0
+        for i in range(len(w) - 1):
+            n_w = w[i] * w[i + 1]
+            p16[off + n_w:off + n_w + w[i + 1]] = self.params[off + n_w:off + n_w + w[i + 1]]
+            off += n_w + w[i + 1]
+        self.params_bf16 = p16
+        self.y0_d = torch.tensor(self.y0, device=dev)
+        self.fl_eval = 2 * sum(w[i] * w[i + 1] for i in range(len(w) - 1)) + (
+            2 * D * D if self.sde else 0)
+        self.evals = 2 if self.sde else 6
+
+    def terms(self, prec):
+        import diffrax_gb300 as dfx
+        field = dfx.MLPField(self.tW, self.tb, precision=prec)
+        if not self.sde:
+            return dfx.ODETerm(field)
+        bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (self.D,), key=self.seed)
+        return dfx.MultiTerm(dfx.ODETerm(field), dfx.ControlTerm(
+            dfx.TanhDiagonalDiffusion(self.tWs, self.tbs), bm))
+
+    def lowered(self, kern, grad, prec="bf16", n=None, adjoint=None):
+        from diffrax_gb300._integrate import Lowered
+        y0 = self.y0_d if n is None else self.y0_d[:n].contiguous()
+        return Lowered(self.terms(prec), self.solver, 0.0, 1.0, self.dt0, y0, None,
+                       self.saveat, self.ctrl, adjoint or self.adjoint, 4096, kern, 0, 0,
+                       want_grad=grad)
+
+    def desc(self, fields):
+        import oracle as O
+        return O.make_desc(**O.oracle_fields(fields))
+
+    def oracle_forward(self, n, params=None):
+        import oracle as O
+        low = self.lowered("fused", False, n=1)
+        return O.solve(self.desc(low.fields), 0.0, 1.0, self.dt0,
+                       self.y0[:n].astype(np.float64),
+                       params=self.params if params is None else params, ts=self.ts,
+                       nthreads=self.cores)
+
+    def grad_ys(self, ys):
+        """Cotangent of loss = mean(y^2) over the whole batch (and over the
+        saved points: sum)."""
+        return 2.0 * ys / (self.B * self.D)
+
+
+def _neural_forward(case, flush, steps, warmup, n_chk=256):
+    """The forward solve in the fused (BF16 tensor-core) and plain (FP32
+    one-trajectory-per-thread) forms, each with its error against the FP64
+    oracle on the first n_chk trajectories; when the fused form's error is
+    above the plain form's, the fused kernel's FP32 mode is timed too (the
+    comparison at equal accuracy)."""
+    peaks, src = measured_peaks()
+    ref = case.oracle_forward(n_chk)
+    out = {}
+    for form, kern, prec, reps in (("fused", "fused", "bf16", steps),
+                                   ("plain", "plain", "fp32", max(2, steps // 4))):
+        low = case.lowered(kern, False, prec)
+        ms = _events_time(low.run_forward, reps, min(warmup, 1) if form == "plain" else warmup,
+                          flush)
+        ys, _, res, st = low.run_forward()
+        e = _rel_per_traj(ys[:n_chk].double().cpu().numpy(), ref["ys"])
+        out[form] = {"traj_per_s": case.B / (ms / 1e3), "ms": ms,
+                     "max_rel_err_vs_fp64_oracle": float(e.max()),
+                     "median_rel_err_vs_fp64_oracle": float(np.median(e)),
+                     "mean_attempted_steps": float(st[:, 0].float().mean().item()),
+                     "all_successful": bool((res == 0).all().item())}
+    f = out["fused"]
+    alg = case.B * f["mean_attempted_steps"] * case.evals * case.fl_eval / (f["ms"] / 1e3) / 1e12
+    peak = peaks.get("bf16_tflops", 1900.0)
+    f["roofline"] = {
+        "bound": "tensor", "achieved": alg, "peak": peak, "unit": "TFLOP/s",
+        "frac": alg / peak, "peak_source": src,
+        "work": f"{case.fl_eval} flop per field evaluation x {case.evals} evaluations per "
+                f"attempted step (algorithmic; hi/lo operands execute 2-3x that)"}
+    out["fused_over_plain"] = out["plain"]["ms"] / f["ms"]
+    out["fused_err_le_plain_err"] = (f["max_rel_err_vs_fp64_oracle"]
+                                     <= out["plain"]["max_rel_err_vs_fp64_oracle"])
+    if not out["fused_err_le_plain_err"]:
+        low = case.lowered("fused", False, "fp32")
+        ms = _events_time(low.run_forward, steps, warmup, flush)
+        ys = low.run_forward()[0]
+        e = _rel_per_traj(ys[:n_chk].double().cpu().numpy(), ref["ys"])
+        out["fused_fp32"] = {"traj_per_s": case.B / (ms / 1e3), "ms": ms,
+                             "max_rel_err_vs_fp64_oracle": float(e.max()),
+                             "median_rel_err_vs_fp64_oracle": float(np.median(e))}
+        out["fused_fp32_over_plain"] = out["plain"]["ms"] / ms
+        out["fused_fp32_err_le_plain_err"] = (float(e.max())
+                                              <= out["plain"]["max_rel_err_vs_fp64_oracle"])
+    if case.kind == "wide":
+        # the fused form's error against the oracle holding the same BF16 weights
+        refb = case.oracle_forward(n_chk, params=case.params_bf16)
+        low = case.lowered("fused", False, "bf16")
+        ys = low.run_forward()[0]
+        f["max_rel_err_vs_fp64_oracle_same_bf16_weights"] = float(
+            _rel_per_traj(ys[:n_chk].double().cpu().numpy(), refb["ys"]).max())
+    cpu_n = 512
+    out["cpu_baseline"] = _oracle_rate(lambda: case.oracle_forward(cpu_n), cpu_n, case.cores)
+    return out
+
+
+def _recursive_grad(case, flush, steps, warmup, n_g=64):
+    """Forward + RecursiveCheckpointAdjoint backward of loss = mean(y(t1)^2):
+    gradients/s of the fused and plain forms over the whole batch, and each
+    form's dL/dy0 and dL/dtheta against the FP64 oracle's discretise-then-
+    optimise gradient on the first n_g trajectories (end to end: each side's
+    cotangent comes from its own forward)."""
+    import torch
+    import oracle as O
+    ref_f = case.oracle_forward(n_g)
+    low1 = case.lowered("fused", True, n=1)
+    r = O.grad_recursive(case.desc(low1.fields), 0.0, 1.0, case.dt0,
+                         case.y0[:n_g].astype(np.float64), case.grad_ys(ref_f["ys"]),
+                         params=case.params, ts=case.ts, nthreads=case.cores)
+    out = {}
+
+    def run(kern, prec, n=None):
+        low = case.lowered(kern, True, prec, n=n)
+
+        def fwd_bwd():
+            ys_, _, _, _, ws = low.run_forward(keep_workspace=True)
+            return low.run_backward(ws, case.grad_ys(ys_), low.y0, low.params)
+        return low, fwd_bwd
+
+    def errs(kern, prec):
+        _, fb = run(kern, prec, n_g)
+        gy0, gp = fb()
+        return (_per_row_max(gy0.double().cpu().numpy(), r["grad_y0"]),
+                _vec_rel(gp.double().cpu().numpy(), r["grad_params"]))
+
+    forms = [("fused", "fused", "bf16", steps, warmup),
+             ("plain", "plain", "fp32", max(2, steps // 2), 1)]
+    for form, kern, prec, reps, wu in forms:
+        _, fb = run(kern, prec)
+        ms = _events_time(fb, reps, wu, flush)
+        e0, ep = errs(kern, prec)
+        out[form] = {"grads_per_s": case.B / (ms / 1e3), "ms": ms,
+                     "unit": "trajectory gradients/s",
+                     "dL_dy0_max_rel_err_vs_fp64_oracle": e0,
+                     "dL_dtheta_rel_err_vs_fp64_oracle": ep}
+    f, p = out["fused"], out["plain"]
+    out["fused_over_plain"] = p["ms"] / f["ms"]
+    out["fused_err_le_plain_err"] = (
+        f["dL_dy0_max_rel_err_vs_fp64_oracle"] <= p["dL_dy0_max_rel_err_vs_fp64_oracle"] and
+        f["dL_dtheta_rel_err_vs_fp64_oracle"] <= p["dL_dtheta_rel_err_vs_fp64_oracle"])
+    if not out["fused_err_le_plain_err"]:
+        _, fb = run("fused", "fp32")
+        ms = _events_time(fb, steps, warmup, flush)
+        e0, ep = errs("fused", "fp32")
+        out["fused_fp32"] = {"grads_per_s": case.B / (ms / 1e3), "ms": ms,
+                             "dL_dy0_max_rel_err_vs_fp64_oracle": e0,
+                             "dL_dtheta_rel_err_vs_fp64_oracle": ep}
+        out["fused_fp32_over_plain"] = p["ms"] / ms
+        out["fused_fp32_err_le_plain_err"] = (
+            e0 <= p["dL_dy0_max_rel_err_vs_fp64_oracle"] and
+            ep <= p["dL_dtheta_rel_err_vs_fp64_oracle"])
+    out["oracle_fp64_grad_norm"] = float(np.linalg.norm(r["grad_params"]))
+    t = time.perf_counter()
+    O.grad_recursive(case.desc(low1.fields), 0.0, 1.0, case.dt0,
+                     case.y0[:n_g].astype(np.float64), case.grad_ys(ref_f["ys"]),
+                     params=case.params, ts=case.ts, nthreads=case.cores)
+    dt = time.perf_counter() - t
+    out["cpu_baseline"] = {"value": n_g / dt, "unit": "trajectory gradients/s",
+                           "cores": case.cores, "kind": "port",
+                           "sample": f"{n_g} trajectories forward + backward, FP64 oracle, "
+                                     f"{dt:.2f} s"}
+    return out
+
+
+def _backsolve_grad(case, flush, steps, warmup, n_g=32):
+    """Forward + BacksolveAdjoint backward of loss = sum over the saved points
+    of mean(y^2), under the reference's default rms_norm (a_theta in the error
+    norm, streamed from HBM) and under adjoint_rms_seminorm.  Gradients/s of
+    the fused and plain forms over the whole batch; each form's dL/dy0 and
+    dL/dtheta against the FP64 oracle (forward with the config's FP32 weights,
+    backsolve from its own saves) on the first n_g trajectories."""
+    import diffrax_gb300 as dfx
+    import oracle as O
+    ref_f = case.oracle_forward(n_g)
+    out = {}
+    for name, adj in (("rms_norm", dfx.BacksolveAdjoint()),
+                      ("seminorm", dfx.BacksolveAdjoint(stepsize_controller=dfx.PIDController(
+                          rtol=case.ctrl.rtol, atol=case.ctrl.atol,
+                          norm=dfx.adjoint_rms_seminorm)))):
+        bdesc = case.desc(case.lowered("fused", True, n=1, adjoint=adj).bwd_fields)
+        t = time.perf_counter()
+        r = O.backsolve(bdesc, 0.0, 1.0, None, ref_f["ts"], ref_f["ys"],
+                        case.grad_ys(ref_f["ys"]), params=case.params, nthreads=case.cores)
+        dt_cpu = time.perf_counter() - t
+
+        def run(kern, prec, n=None):
+            low = case.lowered(kern, True, prec, n=n, adjoint=adj)
+
+            def fwd_bwd():
+                ys_, ts_, _, _ = low.run_forward()
+                return low.run_backsolve(ts_, ys_, case.grad_ys(ys_), low.params)
+            return low, fwd_bwd
+
+        def errs(kern, prec):
+            low, fb = run(kern, prec, n_g)
+            gy0, gp, res, _ = fb()
+            return (_per_row_max(gy0.double().cpu().numpy(), r["grad_y0"]),
+                    _vec_rel(gp.double().cpu().numpy(), r["grad_params"]), low)
+
+        ent = {}
+        forms = [("fused", "fused", "bf16", steps, warmup)]
+        if name == "rms_norm":
+            forms.append(("plain", "plain", "fp32", 1, 0))  # one ~40 s solve
+        for form, kern, prec, reps, wu in forms:
+            low, fb = run(kern, prec)
+            ms = _events_time(fb, reps, wu, flush)
+            gy0, gp, res, st = fb()
+            e0, ep, _ = errs(kern, prec)
+            ent[form] = {"grads_per_s": case.B / (ms / 1e3), "ms": ms,
+                         "unit": "trajectory gradients/s",
+                         "mean_backward_steps": float(st[:, 0].float().mean().item()),
+                         "backward_failures": int((res != 0).sum().item()),
+                         "dL_dy0_max_rel_err_vs_fp64_oracle": e0,
+                         "dL_dtheta_rel_err_vs_fp64_oracle": ep}
+            if form == "fused" and name == "rms_norm":
+                peaks, src = measured_peaks()
+                n_par = int(low.params.numel())
+                stream = float(st[:, 0].double().sum().item()) * 2 * 4 * n_par
+                peak = peaks.get("hbm_gbs", 6800.0)
+                ent["roofline"] = {
+                    "bound": "hbm", "achieved": stream / (ms / 1e3) / 1e9, "peak": peak,
+                    "unit": "GB/s", "frac": stream / (ms / 1e3) / 1e9 / peak,
+                    "peak_source": src, "a_theta_stream_bytes": stream,
+                    "work": "a_theta double buffer: 8 bytes per parameter per "
+                            "trajectory-step (read a_theta0, write the candidate); timed "
+                            "region = forward + backward"}
+        if "plain" in ent:
+            f, p = ent["fused"], ent["plain"]
+            ent["fused_over_plain"] = p["ms"] / f["ms"]
+            ent["fused_err_le_plain_err"] = (
+                f["dL_dy0_max_rel_err_vs_fp64_oracle"] <= p["dL_dy0_max_rel_err_vs_fp64_oracle"]
+                and f["dL_dtheta_rel_err_vs_fp64_oracle"]
+                <= p["dL_dtheta_rel_err_vs_fp64_oracle"])
+            if not ent["fused_err_le_plain_err"]:
+                low, fb = run("fused", "fp32")
+                ms = _events_time(fb, max(2, steps // 2), 1, flush)
+                e0, ep, _ = errs("fused", "fp32")
+                ent["fused_fp32"] = {"grads_per_s": case.B / (ms / 1e3), "ms": ms,
+                                     "dL_dy0_max_rel_err_vs_fp64_oracle": e0,
+                                     "dL_dtheta_rel_err_vs_fp64_oracle": ep}
+                ent["fused_fp32_over_plain"] = p["ms"] / ms
+                ent["fused_fp32_err_le_plain_err"] = (
+                    e0 <= p["dL_dy0_max_rel_err_vs_fp64_oracle"] and
+                    ep <= p["dL_dtheta_rel_err_vs_fp64_oracle"])
+        ent["oracle_mean_backward_steps"] = float(r["stats"][:, 0].mean())
+        ent["cpu_baseline"] = {"value": n_g / dt_cpu, "unit": "trajectory gradients/s",
+                               "cores": case.cores, "kind": "port",
+                               "sample": f"{n_g} trajectories backward only, FP64 oracle, "
+                                         f"{dt_cpu:.2f} s"}
+        out[f"backsolve_{name}"] = ent
+    return out
+
+
 def workload_neural(dev, flush, steps, warmup, kind):
     """Neural ODE (64-128-128-64, Tsit5 PID(1e-5, 1e-7), batch 8192, t1 save,
     RecursiveCheckpointAdjoint(64), loss mean y(t1)^2), the wide neural ODE
-    forward (64-256-256-64, batch 16384, 32 ts) or the neural SDE (drift
-    32-64-64-32, diffusion 0.1 tanh(W y + b), Heun dt 0.01, VBT tol 1e-3,
-    batch 32768, RecursiveCheckpointAdjoint)."""
+    (64-256-256-64, batch 16384, 32 ts, BacksolveAdjoint, loss sum over the
+    saves of mean y^2) or the neural SDE (drift 32-64-64-32, diffusion
+    0.1 tanh(W y + b), Heun dt 0.01, VBT tol 1e-3, batch 32768,
+    RecursiveCheckpointAdjoint, loss mean y(t1)^2): forward and gradient
+    throughput of the fused and plain forms with their errors against the
+    FP64 oracle."""
     import torch
-    import diffrax_gb300 as dfx
-    import oracle as O
-    from diffrax_gb300._integrate import Lowered
-    cores = os.cpu_count() or 1
-    if kind == "ode":
-        widths, B, seed = [64, 128, 128, 64], 8192, 21
-        solver, ctrl, dt0 = dfx.Tsit5(), dfx.PIDController(rtol=1e-5, atol=1e-7), None
-        saveat, ts, cps, sde = dfx.SaveAt(t1=True), None, 64, False
-        name = "neural_ode_64_128_tsit5_pid_b8192_recursive64"
-    elif kind == "wide":
-        widths, B, seed = [64, 256, 256, 64], 16384, 22
-        solver, ctrl, dt0 = dfx.Tsit5(), dfx.PIDController(rtol=1e-5, atol=1e-7), None
-        ts = np.linspace(0.0, 1.0, 32)
-        saveat, cps, sde = dfx.SaveAt(ts=ts), 64, False
-        name = "neural_ode_64_256_tsit5_pid_b16384_ts32_forward"
-    else:
-        widths, B, seed = [32, 64, 64, 32], 32768, 23
-        solver, ctrl, dt0 = dfx.Heun(), dfx.ConstantStepSize(), 0.01
-        saveat, ts, cps, sde = dfx.SaveAt(t1=True), None, 16, True
-        name = "neural_sde_32_64_heun_dt0.01_vbt1e-3_b32768_recursive16"
-    D = widths[0]
-    Ws, bs = _mlp_np(widths, seed)
-    rng = np.random.default_rng(seed + 1)
-    y0 = rng.standard_normal((B, D)).astype(np.float32)
-    params = [np.concatenate([W.reshape(-1), b]) for W, b in zip(Ws, bs)]
-    tW = [torch.tensor(W, device=dev) for W in Ws]
-    tb = [torch.tensor(b, device=dev) for b in bs]
-    y0_d = torch.tensor(y0, device=dev)
-    out = {"workload": name}
-
-    def terms_for(prec):
-        field = dfx.MLPField(tW, tb, precision=prec)
-        if not sde:
-            return dfx.ODETerm(field)
-        bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (D,), key=seed)
-        return dfx.MultiTerm(dfx.ODETerm(field),
-                             dfx.ControlTerm(dfx.TanhDiagonalDiffusion(tWs, tbs), bm))
-    if sde:
-        Wsig = (rng.standard_normal((D, D)) / np.sqrt(D)).astype(np.float32)
-        bsig = np.zeros(D, np.float32)
-        tWs, tbs = torch.tensor(Wsig, device=dev), torch.tensor(bsig, device=dev)
-        params += [Wsig.reshape(-1), bsig]
-    params = np.concatenate(params).astype(np.float64)
-
-    def lowered(kern, grad, prec="bf16"):
-        return Lowered(terms_for(prec), solver, 0.0, 1.0, dt0, y0_d, None, saveat, ctrl,
-                       dfx.RecursiveCheckpointAdjoint(checkpoints=cps), 4096, kern, 0, 0,
-                       want_grad=grad)
-    fwd = lowered("fused", False)
-    ms_f = _events_time(fwd.run_forward, steps, warmup, flush)
-    ys = fwd.run_forward()[0]
-    out["fused_forward"] = {"traj_per_s": B / (ms_f / 1e3), "ms": ms_f}
-    plain = lowered("plain", False)
-    ms_p = _events_time(plain.run_forward, max(2, steps // 4), 1, flush)
-    out["plain_forward"] = {"traj_per_s": B / (ms_p / 1e3), "ms": ms_p}
-    out["fused_over_plain_forward"] = ms_p / ms_f
-    # accuracy of the BF16 tensor-core forward against the FP64 oracle
-    n_chk = 256
-    fields = dfx.lower(terms_for("bf16"), solver, ctrl, saveat, dim=D, dtype=torch.float32,
-                       max_steps=4096, n_ts=0 if ts is None else len(ts))
-    desc = O.make_desc(**dfx.oracle_fields(fields))
-    ref = O.solve(desc, 0.0, 1.0, dt0, y0[:n_chk].astype(np.float64), params=params, ts=ts,
-                  nthreads=cores)
-    e = _rel_per_traj(ys[:n_chk].double().cpu().numpy(), ref["ys"])
-    out["fused_forward"]["max_rel_err_vs_fp64_oracle"] = float(e.max())
-    out["fused_forward"]["median_rel_err_vs_fp64_oracle"] = float(np.median(e))
-    out["mean_attempted_steps"] = float(fwd.run_forward()[3][:, 0].float().mean().item())
-    # Tensor-core roofline of the fused forward: algorithmic field flops
-    # (2 sum in*out per evaluation, Tsit5/Dopri5 6 evaluations per attempted
-    # step, Heun 2) against the measured dense BF16 peak; the hi/lo operands
-    # execute 3x (2x with single-BF16 weights) as many tensor-core flops.
-    peaks, src = measured_peaks()
-    evals = 2 if kind == "sde" else 6
-    fl_eval = 2 * sum(widths[i] * widths[i + 1] for i in range(3))
-    if sde:
-        fl_eval += 2 * D * D
-    alg = B * out["mean_attempted_steps"] * evals * fl_eval / (ms_f / 1e3) / 1e12
-    mult = 3 if widths[1] <= 128 else 2
-    out["fused_forward"]["roofline"] = {
-        "bound": "tensor", "achieved": alg, "peak": peaks.get("bf16_tflops", 1900.0),
-        "unit": "TFLOP/s", "frac": alg / peaks.get("bf16_tflops", 1900.0), "peak_source": src,
-        "executed_tensor_tflops": alg * mult,
-        "work": f"{fl_eval} flop per field evaluation x {evals} evaluations per attempted step"}
-    out["cpu_baseline_forward"] = _oracle_rate(
-        lambda: O.solve(desc, 0.0, 1.0, dt0, y0[:512].astype(np.float64), params=params, ts=ts,
-                        nthreads=cores), 512, cores)
+    case = _NeuralCase(dev, kind)
+    out = {"workload": case.name, "forward": _neural_forward(case, flush, steps, warmup)}
     if kind == "ode":
         # The same forward on the fifth-generation tensor cores (tcgen05.mma,
         # TMEM accumulators; 128 trajectories per CTA), at this batch (64
         # tiles) and at a batch filling every SM with one tile (152 x 128),
         # beside the mma.sync row-tile kernel at that batch.
-        tc = lowered("tc", False)
+        import oracle as O
+        from diffrax_gb300._integrate import Lowered
+        n_chk = 256
+        ref = case.oracle_forward(n_chk)
+        tc = case.lowered("tc", False)
         ms_t = _events_time(tc.run_forward, steps, warmup, flush)
-        ys_t = tc.run_forward()[0]
+        ys_t, _, _, st_t = tc.run_forward()
         e_t = _rel_per_traj(ys_t[:n_chk].double().cpu().numpy(), ref["ys"])
-        alg_t = B * out["mean_attempted_steps"] * evals * fl_eval / (ms_t / 1e3) / 1e12
-        out["tc_forward"] = {"traj_per_s": B / (ms_t / 1e3), "ms": ms_t,
-                             "max_rel_err_vs_fp64_oracle": float(e_t.max()),
-                             "roofline": {"bound": "tensor", "achieved": alg_t,
-                                          "frac": alg_t / peaks.get("bf16_tflops", 1900.0),
-                                          "unit": "TFLOP/s", "peak_source": src}}
+        peaks, src = measured_peaks()
+        alg_t = (case.B * float(st_t[:, 0].float().mean().item()) * case.evals * case.fl_eval
+                 / (ms_t / 1e3) / 1e12)
+        out["forward"]["tc"] = {
+            "traj_per_s": case.B / (ms_t / 1e3), "ms": ms_t,
+            "max_rel_err_vs_fp64_oracle": float(e_t.max()),
+            "roofline": {"bound": "tensor", "achieved": alg_t,
+                         "frac": alg_t / peaks.get("bf16_tflops", 1900.0),
+                         "unit": "TFLOP/s", "peak_source": src}}
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         Bf = 128 * sms
-        yf = torch.tensor(np.random.default_rng(seed + 2).standard_normal((Bf, D)),
+        yf = torch.tensor(np.random.default_rng(case.seed + 2).standard_normal((Bf, case.D)),
                           dtype=torch.float32, device=dev)
         full = {}
         for kern in ("fused", "tc"):
-            lo = Lowered(terms_for("bf16"), solver, 0.0, 1.0, dt0, yf, None, saveat, ctrl, None,
-                         4096, kern, 0, 0)
+            lo = Lowered(case.terms("bf16"), case.solver, 0.0, 1.0, case.dt0, yf, None,
+                         case.saveat, case.ctrl, None, 4096, kern, 0, 0)
             ms_k = _events_time(lo.run_forward, steps, warmup, flush)
             full[kern] = {"traj_per_s": Bf / (ms_k / 1e3), "ms": ms_k}
         full["tc_over_fused"] = full["fused"]["ms"] / full["tc"]["ms"]
         out[f"forward_batch_{Bf}"] = full
     if kind == "wide":
-        out.update(workload_backsolve(dev, flush, steps, warmup, terms_for, solver, ctrl,
-                                      saveat, ts, y0, y0_d, params, desc, B, D))
-        return out
-    # forward + RecursiveCheckpointAdjoint backward of loss = mean(y(t1)^2)
-    grad = lowered("fused", True)
-
-    def fwd_bwd():
-        ys_, _, _, _, ws = grad.run_forward(keep_workspace=True)
-        gys = ys_ * (2.0 / ys_.numel())
-        return grad.run_backward(ws, gys, grad.y0, grad.params)
-    ms_g = _events_time(fwd_bwd, steps, warmup, flush)
-    out["fused_forward_adjoint"] = {"grads_per_s": B / (ms_g / 1e3), "ms": ms_g,
-                                    "unit": "trajectory gradients/s"}
-    gy0, gp = fwd_bwd()
-    n_g = 64
-    ys_g = grad.run_forward()[0][:n_g].double().cpu().numpy()
-    gys = 2.0 * ys_g / (B * D)
-    r = O.grad_recursive(desc, 0.0, 1.0, dt0, y0[:n_g].astype(np.float64), gys, params=params,
-                         ts=ts, nthreads=cores)
-    out["fused_forward_adjoint"]["dL_dy0_max_rel_err_vs_fp64_oracle"] = float(
-        np.abs(gy0[:n_g].double().cpu().numpy() - r["grad_y0"]).max()
-        / np.abs(r["grad_y0"]).max())
-    # the plain form: forward with the full tape + one-trajectory-per-thread
-    # backward on the CUDA cores (FP32)
-    pgrad = lowered("plain", True)
-
-    def fwd_bwd_plain():
-        ys_, _, _, _, ws = pgrad.run_forward(keep_workspace=True)
-        gys_ = ys_ * (2.0 / ys_.numel())
-        return pgrad.run_backward(ws, gys_, pgrad.y0, pgrad.params)
-    ms_pg = _events_time(fwd_bwd_plain, max(2, steps // 2), 1, flush)
-    out["plain_forward_adjoint"] = {"grads_per_s": B / (ms_pg / 1e3), "ms": ms_pg,
-                                    "unit": "trajectory gradients/s"}
-    out["fused_over_plain_forward_adjoint"] = ms_pg / ms_g
-    out["cpu_baseline_forward_adjoint"] = _oracle_rate(
-        lambda: O.grad_recursive(desc, 0.0, 1.0, dt0, y0[:n_g].astype(np.float64), gys,
-                                 params=params, ts=ts, nthreads=cores), n_g, cores)
+        out.update(_backsolve_grad(case, flush, steps, warmup))
+    else:
+        out["gradient"] = _recursive_grad(case, flush, steps, warmup)
     return out
+
+
+def _summary(others, vdp_ratio, vdp_err, vdp_plain_err):
+    """grads_per_s, fused_over_plain and errors (fused, plain) per config."""
+    def g(d, *keys):
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    def r3(x):
+        return None if x is None else float(f"{x:.3g}")
+    grads, ratio, errs = {}, {"c2_vdp_fwd": r3(vdp_ratio)}, {
+        "c2_vdp_fwd": [r3(vdp_err), r3(vdp_plain_err)]}
+    lv = others.get("lotka_volterra", {})
+    ratio["c1_lv_fwd"] = r3(g(lv, "fused_over_plain_f32"))
+    errs["c1_lv_fwd"] = [r3(g(lv, "fused_f32", "max_rel_err_vs_fp64_oracle")),
+                         r3(g(lv, "plain_f32", "max_rel_err_vs_fp64_oracle"))]
+    e0 = "dL_dy0_max_rel_err_vs_fp64_oracle"
+    for tag, key, gk in (("c3_node", "neural_ode", "gradient"),
+                         ("c4_wide", "neural_ode_wide", "backsolve_rms_norm"),
+                         ("c5_nsde", "neural_sde", "gradient")):
+        c = others.get(key, {})
+        fw = g(c, "forward")
+        ratio[f"{tag}_fwd"] = r3(g(fw, "fused_over_plain"))
+        errs[f"{tag}_fwd"] = [r3(g(fw, "fused", "max_rel_err_vs_fp64_oracle")),
+                              r3(g(fw, "plain", "max_rel_err_vs_fp64_oracle"))]
+        if g(fw, "fused_fp32") is not None:
+            ratio[f"{tag}_fwd_fp32"] = r3(g(fw, "fused_fp32_over_plain"))
+            errs[f"{tag}_fwd_fp32"] = r3(g(fw, "fused_fp32", "max_rel_err_vs_fp64_oracle"))
+        gr = g(c, gk)
+        grads[tag] = r3(g(gr, "fused", "grads_per_s"))
+        grads[f"{tag}_plain"] = r3(g(gr, "plain", "grads_per_s"))
+        ratio[f"{tag}_grad"] = r3(g(gr, "fused_over_plain"))
+        errs[f"{tag}_grad_dy0"] = [r3(g(gr, "fused", e0)), r3(g(gr, "plain", e0))]
+        errs[f"{tag}_grad_dtheta"] = [
+            r3(g(gr, "fused", "dL_dtheta_rel_err_vs_fp64_oracle")),
+            r3(g(gr, "plain", "dL_dtheta_rel_err_vs_fp64_oracle"))]
+        if g(gr, "fused_fp32") is not None:
+            grads[f"{tag}_fp32"] = r3(g(gr, "fused_fp32", "grads_per_s"))
+            ratio[f"{tag}_grad_fp32"] = r3(g(gr, "fused_fp32_over_plain"))
+            errs[f"{tag}_grad_fp32_dy0"] = r3(g(gr, "fused_fp32", e0))
+            errs[f"{tag}_grad_fp32_dtheta"] = r3(
+                g(gr, "fused_fp32", "dL_dtheta_rel_err_vs_fp64_oracle"))
+    grads["c4_wide_seminorm"] = r3(g(others.get("neural_ode_wide", {}), "backsolve_seminorm",
+                                     "fused", "grads_per_s"))
+    return {"grads_per_s": grads, "fused_over_plain": ratio,
+            "max_rel_err_fused_plain": errs}
 
 
 def main():
@@ -738,7 +910,8 @@ def main():
     ap.add_argument("--impl", default="gbdx", choices=["gbdx", "reference"])
     ap.add_argument("--batch", type=int, default=65536)
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--ref-sample", type=int, default=8192)
+    ap.add_argument("--ref-sample", type=int, default=0,
+                    help="trajectories per reference step (default: the whole batch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the other configurations")
@@ -899,16 +1072,31 @@ def main():
     d2h = B * (2 * 4 + 4)      # eager: ys, result
     d2h_graphed = B * (2 * 4 + 8 + 4 + 3 * 4)  # ys, ts, result, stats
 
+    # The kernel's own bound: no schedule finishes before its longest
+    # trajectory, whose steps depend on one another.  That trajectory alone
+    # (the same kernel, batch 1, CUDA events, median of the timed solves).
+    crit = None
+    if rank == 0:
+        k_long = int(stats[:, 0].argmax().item())
+        lone = Lowered(term, dfx.Dopri5(), 0.0, t1_d[k_long:k_long + 1].contiguous(), None,
+                       y0_d[k_long:k_long + 1].contiguous(), mu_d[k_long:k_long + 1].contiguous(),
+                       dfx.SaveAt(t1=True), pid, None, 4096, "fused", 0, 0)
+        ms_lone = _events_time(lone.run_forward, 20, 3, flush)
+        n_long = int(stats[k_long, 0].item())
+        crit = {"trajectory": k_long, "attempted_steps": n_long, "alone_ms": ms_lone,
+                "batch_ms": ms_fused, "frac": ms_lone / ms_fused}
+
     others = {}
     if rank == 0 and not args.headline_only:
-        try:
-            others["lotka_volterra"] = workload_lotka_volterra(dev, flush, 10, 3)
-            others["neural_ode"] = workload_neural(dev, flush, 5, 3, "ode")
-            others["neural_ode_wide"] = workload_neural(dev, flush, 5, 3, "wide")
-            others["neural_sde"] = workload_neural(dev, flush, 5, 3, "sde")
-            others["next_rows"] = workload_next_rows(dev, flush, 10, 3)
-        except Exception as exc:  # report, never hide the headline line
-            others["error"] = f"{type(exc).__name__}: {exc}"
+        for key, fn in (("lotka_volterra", lambda: workload_lotka_volterra(dev, flush, 10, 3)),
+                        ("neural_ode", lambda: workload_neural(dev, flush, 5, 3, "ode")),
+                        ("neural_ode_wide", lambda: workload_neural(dev, flush, 5, 3, "wide")),
+                        ("neural_sde", lambda: workload_neural(dev, flush, 5, 3, "sde")),
+                        ("next_rows", lambda: workload_next_rows(dev, flush, 10, 3))):
+            try:
+                others[key] = fn()
+            except Exception as exc:  # report, never hide the headline line
+                others[key] = {"error": f"{type(exc).__name__}: {exc}"}
 
     if rank == 0:
         peaks, src = measured_peaks()
@@ -916,28 +1104,34 @@ def main():
         fp32 = steps_total * FP32_FLOPS_PER_STEP / t_s / 1e12
         fp64 = steps_total * FP64_OPS_PER_STEP / t_s / 1e12
         gbs = B * BYTES_PER_TRAJ / t_s / 1e9
-        traffic = ncu_traffic()
-        # The fused kernel's own bound is step latency: the longest trajectory's
-        # dependent steps (each FP64 instruction holds an SM sub-partition's
-        # FP64 unit for ~64 cycles on GB300), not HBM (DRAM ~0.03 %): the HBM
-        # line is reported in the contract's form, with the compute rates
+        # The fused kernel's bound is the dependent-step latency of its longest
+        # trajectory (critical_path: that trajectory alone / the whole batch),
+        # not HBM (DRAM ~0.03 %) nor the FP32 pipe: the HBM line is kept in
+        # the contract's form, with the critical path and the compute rates
         # beside it.
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
+        sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+        if crit is not None:
+            crit["cycles_per_step_alone"] = (crit["alone_ms"] * 1e-3 * sm_mhz * 1e6
+                                             / max(crit["attempted_steps"], 1))
+            crit["sm_mhz"] = sm_mhz
         roofline = {
             "bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
-            "frac": gbs / hbm_peak, "traffic": traffic, "peak_source": src,
+            "frac": gbs / hbm_peak, "traffic": NCU_TRAFFIC_BYTES_PER_LAUNCH,
+            "traffic_source": "ncu capture of this kernel on this workload, not this run",
+            "peak_source": src,
             "work": f"{BYTES_PER_TRAJ} algorithmic bytes per trajectory x {B} per launch",
-            "limiter": "step latency of the longest trajectories (1031 dependent Dopri5 "
-                       "steps; each FP64 instruction holds an SM sub-partition's FP64 unit "
-                       "~64 cycles); see profiles/fused_kernel_vdp_dopri5.md",
-            "fp64": {"achieved": fp64, "peak": FP64_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
-                     "frac": fp64 / FP64_PEAK_TFLOPS_NOMINAL,
-                     "peak_source": "nominal GB300 FP64 rate"},
+            "binding": "critical_path",
+            "critical_path": crit,
             "fp32": {"achieved": fp32, "peak": FP32_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
                      "frac": fp32 / FP32_PEAK_TFLOPS_NOMINAL,
                      "work": f"{FP32_FLOPS_PER_STEP} FP32 flop per attempted step x "
                              f"{steps_total} attempted steps per launch",
-                     "peak_source": "nominal FP32 FMA rate at 2.07 GHz"},
+                     "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz), "
+                                    "not measured"},
+            "fp64": {"achieved": fp64, "peak": FP64_PEAK_TFLOPS_NOMINAL, "unit": "TFLOP/s",
+                     "frac": fp64 / FP64_PEAK_TFLOPS_NOMINAL,
+                     "peak_source": "nominal GB300 FP64 rate, not measured"},
         }
         # Accuracy of both kernels against the FP64 oracle on the same inputs.
         n_chk = min(B, 4096)
@@ -987,7 +1181,6 @@ def main():
             "plain": {"value": plain_value, "ms_per_step": ms_plain,
                       "max_rel_err_vs_fp64_oracle": plain_err[0],
                       "median_rel_err_vs_fp64_oracle": plain_err[1]},
-            "fused_over_plain": value / plain_value,
             "max_rel_err_vs_fp64_oracle": fused_err[0],
             "median_rel_err_vs_fp64_oracle": fused_err[1],
             "all_successful": ok,
@@ -995,6 +1188,9 @@ def main():
             "wall_s_timed_region": wall,
             "other_configs": others,
         }
+        # The whole metric in brief, last on the line: gradients/s, fused over
+        # plain and both forms' errors against the FP64 oracle per config.
+        line.update(_summary(others, value / plain_value, fused_err[0], plain_err[0]))
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

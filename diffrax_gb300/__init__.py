@@ -11,7 +11,7 @@ from ._core import (
     rms_norm, Event, LinearCondition, Newton, SteadyStateCondition, steady_state_event,
     AbstractBrownianIncrement, BrownianIncrement, SEA, ShARK, SpaceTimeLevyArea, SRA1,
 )
-from ._integrate import DenseInterpolation, diffeqsolve, lower, oracle_fields
+from ._integrate import DenseInterpolation, diffeqsolve, lower
 from ._tune import GraphedSolve, autotune_launch, tuned_shapes
 
 __version__ = "0.1.0"

@@ -75,6 +75,11 @@ class _BacksolveSolve(torch.autograd.Function):
         grad_y0, grad_params, res, stats = low.run_backsolve(ts, ys.detach(), grad_ys,
                                                              params.detach())
         low.bwd_result, low.bwd_stats = res, stats
+        if low.bwd_throw:
+            # a reverse solve that failed (max_steps, dtmin) gives no gradient:
+            # raise as the reference's backward diffeqsolve does with throw=True
+            from ._integrate import _raise_on_failure
+            _raise_on_failure(res)
         return (None, grad_y0 if ctx.needs_input_grad[1] else None,
                 grad_params.to(params.dtype) if ctx.needs_input_grad[2] else None)
 

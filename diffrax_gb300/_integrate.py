@@ -160,11 +160,6 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
     return f
 
 
-def oracle_fields(fields: dict) -> dict:
-    """The subset of a lowered descriptor that the FP64 oracle understands."""
-    return {k: v for k, v in fields.items() if k in _lib.ORACLE_FIELDS}
-
-
 def _device():
     if not torch.cuda.is_available():
         raise RuntimeError("diffrax_gb300 needs a CUDA device: there is no CPU path")
@@ -248,8 +243,11 @@ class Lowered:
 
     def __init__(self, terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
                  adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule="auto",
-                 want_grad=False, event=None):
+                 want_grad=False, event=None, throw=True):
         dev = _device()
+        # diffrax/_adjoint.py:623-634: the backward solve of BacksolveAdjoint
+        # takes the forward's `throw` unless its kwargs override it
+        self.throw = bool(throw)
         if not isinstance(y0, torch.Tensor):
             y0 = torch.as_tensor(y0)
         if y0.dtype not in (torch.float32, torch.float64):
@@ -300,6 +298,7 @@ class Lowered:
                                     max_steps=kw.get("max_steps", max_steps), n_ts=n_ts,
                                     adjoint=self.adjoint, kernel=kernel, schedule=schedule)
             self.bwd_problem = _lib.get_problem(self.bwd_fields)
+            self.bwd_throw = bool(kw.get("throw", throw))
             self.bwd_dt0 = self.dt0
             if kw.get("dt0") is not None:
                 self.bwd_dt0 = _time_arrays(t0, t1, kw["dt0"], self.B, dev)[2]
@@ -550,7 +549,7 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
         kernel, block_threads, ctas_per_sm = autotune_launch(factory, base.B, base.fields)
     low = Lowered(terms, solver, t0, t1, dt0, y0, args, saveat, stepsize_controller,
                   adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule,
-                  want_grad=want_grad, event=event)
+                  want_grad=want_grad, event=event, throw=throw)
     interp = ev = None
     if saveat.dense or event is not None:
         ys, ts_out, res, stats, interp, ev = low.run_forward_ex()

@@ -43,12 +43,6 @@ class FwdExtras(_c.Structure):
     _fields_ = [("dense_ts", vp), ("dense_info", vp), ("dense_n", vp), ("event_index", vp)]
 
 
-# The fields the oracle descriptor shares: the leading block (up to the
-# backsolve norm), the SaveAt(steps/dense) selectors and the clip counts.
-ORACLE_FIELDS = [f for f, _ in ProblemDesc._fields_][:29] + [
-    "save_steps", "save_dense", "n_step_ts", "n_jump_ts", "n_event", "event_root", "ev_kind",
-    "ev_dir", "levy_area", "newton_rtol", "newton_atol", "ev_coef"]
-
 _lock = threading.Lock()
 _LIB = None
 

@@ -56,6 +56,12 @@ struct gbdx_problem {
   int mlp_block;       // threads per CTA of the MLP integrator
 };
 
+namespace gbdx {
+// The adjoint the problem was created with (GBDX_ADJ_*), for the other
+// translation units of the library.
+int problem_adjoint(const gbdx_problem *p) { return p->d.adjoint; }
+}  // namespace gbdx
+
 namespace {
 
 // Workspace of one solve: the work counter, the work order, and (recursive

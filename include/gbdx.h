@@ -324,11 +324,14 @@ int gbdx_dense_evaluate(const gbdx_problem *problem, int64_t batch, const double
  * arguments without it and runs the same solve, using instead a fixed 4 MiB
  * scratch array that every GPU loading the library holds until the process
  * exits.  Batches whose workspace would exceed it (more than 1,047,360
- * trajectories on the fused kernels) are rejected with GBDX_ERR_WORKSPACE.
- * The first call on a device looks up the array's device address on that
- * device; make that first call before any stream capture.  All calls share the
- * one array (the solve clears what must start at zero), so calls that overlap
- * on the GPU race: serialise them on one stream.
+ * trajectories on the fused kernels) are rejected with GBDX_ERR_WORKSPACE,
+ * and problems created with an adjoint with GBDX_ERR_UNSUPPORTED (their tape
+ * must outlive the call in a workspace that gbdx_solve_bwd reads).
+ * The first call on a device (and the first after the device's context was
+ * replaced, e.g. by cudaDeviceReset) looks up the array's device address in
+ * that context; make that first call before any stream capture.  All calls
+ * share the one array (the solve clears what must start at zero), so calls
+ * that overlap on the GPU race: serialise them on one stream.
  */
 int gbdx_solve_fwd_noalloc(const gbdx_problem *problem, int64_t batch, const double *t0,
                            const double *t1, const double *dt0, int64_t time_stride,

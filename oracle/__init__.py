@@ -90,6 +90,13 @@ def n_saves(desc) -> int:
     return n
 
 
+def oracle_fields(fields: dict) -> dict:
+    """The subset of a lowered GPU descriptor (diffrax_gb300.lower) that the
+    oracle's descriptor holds: the problem definition without the GPU launch
+    policy (kernel family, launch shape, schedule, precision mode)."""
+    return {k: v for k, v in fields.items() if k in _DEFAULTS}
+
+
 def make_desc(**kw) -> OracleDesc:
     vals = dict(_DEFAULTS)
     unknown = set(kw) - set(vals)

@@ -149,7 +149,7 @@ def test_saveat_steps_output_length(steps, t0, t1, n_ts, max_steps):
     # _integrate.py:1273-1293, as the oracle restates it
     import oracle as O
     f = _fields(save_steps=steps, save_t0=t0, save_t1=t1, n_ts=n_ts, max_steps=max_steps)
-    assert _lib.Problem(f).n_save == O.n_saves(O.make_desc(**dfx.oracle_fields(f)))
+    assert _lib.Problem(f).n_save == O.n_saves(O.make_desc(**O.oracle_fields(f)))
 
 
 def test_saveat_steps_dense_scope():

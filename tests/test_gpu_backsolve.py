@@ -65,7 +65,7 @@ def backsolve_case(widths, solver, controller, ts, B, precision, seed=0, seminor
     low = sol.lowered
     g_params = torch.cat([t.grad.reshape(-1) for pair in zip(tW, tb) for t in pair])
     params = np.concatenate([np.concatenate([W.reshape(-1), b]) for W, b in zip(Ws, bs)])
-    d = O.make_desc(**dfx.oracle_fields(low.bwd_fields))
+    d = O.make_desc(**O.oracle_fields(low.bwd_fields))
     r = O.backsolve(d, 0.0, t1, dt0, sol.ts.cpu().numpy(), ys.detach().cpu().numpy(), G,
                     params=params, nthreads=8)
     return dict(g_y0=y0_t.grad.double().cpu().numpy(),
@@ -201,7 +201,7 @@ def test_backsolve_neural_ode_wide_finite_differences():
     widths = [64, 256, 256, 64]
     c = backsolve_case(widths, dfx.Tsit5(), PID, ts, 16, "bf16", seed=8, bf16_weights=True,
                        grad_ys=_c4_grad_ys)
-    d = O.make_desc(**dfx.oracle_fields(c["sol"].lowered.fields))
+    d = O.make_desc(**O.oracle_fields(c["sol"].lowered.fields))
     y0, P = c["y0"], c["params"]
     B, D = y0.shape
 
@@ -216,9 +216,11 @@ def test_backsolve_neural_ode_wide_finite_differences():
         v = rng.standard_normal(P.size)
         v /= np.linalg.norm(v)
         fd = (loss(P + eps * v) - loss(P - eps * v)) / (2 * eps)
-        errs.append(abs(fd - c["g_params"] @ v) / np.linalg.norm(c["g_params"]))
-    print(f"backsolve vs central differences: max rel err {max(errs):.2e}")
-    assert max(errs) < 1e-3
+        # relative to the directional derivative itself (|g.v| is ~|g|/sqrt(P))
+        errs.append(abs(fd - c["g_params"] @ v) / abs(fd))
+    print(f"backsolve vs central differences: per-direction rel err "
+          f"{' '.join(f'{e:.1e}' for e in errs)}")
+    assert max(errs) < 2e-3
 
 
 def test_backsolve_plain_kernel():
@@ -234,3 +236,29 @@ def test_backsolve_plain_kernel():
     assert np.all(c["result"] == 0)
     check_steps(c, False, 7)
     assert e0 < 1e-4 and ep < 1e-4
+
+
+@pytest.mark.parametrize("throw", [True, False])
+def test_backsolve_backward_failure(throw):
+    # The reverse solve of BacksolveAdjoint(max_steps=2) cannot cross five
+    # saved intervals.  With throw=True the backward raises, as the
+    # reference's backward diffeqsolve does (diffrax/_adjoint.py:623-634);
+    # with throw=False it returns and records max_steps_reached per trajectory.
+    dev = torch.device("cuda")
+    widths = [32, 64, 64, 32]
+    Ws, bs = mlp_params(widths, 3)
+    tW = [torch.tensor(W, dtype=torch.float32, device=dev, requires_grad=True) for W in Ws]
+    tb = [torch.tensor(b, dtype=torch.float32, device=dev) for b in bs]
+    y0 = torch.tensor(np.random.default_rng(4).standard_normal((8, 32)), dtype=torch.float32,
+                      device=dev)
+    sol = dfx.diffeqsolve(dfx.ODETerm(dfx.MLPField(tW, tb)), dfx.Tsit5(), 0.0, 1.0, None, y0,
+                          saveat=dfx.SaveAt(ts=TS6), stepsize_controller=PID,
+                          adjoint=dfx.BacksolveAdjoint(max_steps=2, throw=throw))
+    assert bool((sol.result == 0).all())
+    loss = (sol.ys ** 2).sum()
+    if throw:
+        with pytest.raises(RuntimeError, match="maximum number of solver steps"):
+            loss.backward()
+    else:
+        loss.backward()
+        assert bool((sol.lowered.bwd_result == int(dfx.RESULTS.max_steps_reached)).all())

@@ -39,7 +39,7 @@ def solve_pair(field, solver, controller, saveat, t0, t1, dt0, y0, args, dtype, 
     ts = None if saveat.ts is None else np.asarray(saveat.ts, dtype=np.float64)
     fields = dfx.lower(dfx.ODETerm(field), solver, controller, saveat, dim=y0.shape[1],
                        dtype=dtype, max_steps=max_steps, n_ts=0 if ts is None else ts.size)
-    d = O.make_desc(**dfx.oracle_fields(fields))
+    d = O.make_desc(**O.oracle_fields(fields))
     r = O.solve(d, t0, t1, dt0, y0, args=args, ts=ts, nthreads=8)
     return sol, r, d
 

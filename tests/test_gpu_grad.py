@@ -70,7 +70,7 @@ def grad_case(widths, solver, controller, saveat, t1, dt0, B, precision, checkpo
     ts = None if saveat.ts is None else np.asarray(saveat.ts, dtype=np.float64)
     fields = dfx.lower(terms, solver, controller, saveat, dim=D, dtype=torch.float32,
                        max_steps=max_steps, n_ts=0 if ts is None else ts.size)
-    d = O.make_desc(**dfx.oracle_fields(fields))
+    d = O.make_desc(**O.oracle_fields(fields))
     r = O.grad_recursive(d, 0.0, t1, dt0, y0, G, params=params, ts=ts, nthreads=8)
     steps = sol.stats["num_steps"].cpu().numpy()
     return g_y0, g_params, r, steps
@@ -168,3 +168,73 @@ def test_grad_plain_kernel(sde):
     e0, ep = rel(g_y0, r["grad_y0"]), rel(g_p, r["grad_params"])
     print(f"plain backward (sde={sde}): dL/dy0 rel {e0:.2e}, dL/dtheta rel {ep:.2e}")
     assert e0 < 1e-4 and ep < 1e-4
+
+
+def _loss_grad_case(widths, solver, controller, dt0, B, checkpoints, sde, seed, kernel,
+                    precision):
+    """dL/dy0 and dL/dtheta of loss = mean(y(t1)^2) through diffeqsolve and
+    backward(), against the FP64 oracle's gradient of the same loss (its
+    cotangent from its own forward)."""
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(seed + 100)
+    D = widths[0]
+    y0 = rng.standard_normal((B, D)).astype(np.float32).astype(np.float64)
+    Ws, bs = params_np(widths, seed, bias_scale=0.0)
+    tW = [torch.tensor(W, dtype=torch.float32, device=dev, requires_grad=True) for W in Ws]
+    tb = [torch.tensor(b, dtype=torch.float32, device=dev, requires_grad=True) for b in bs]
+    field = dfx.MLPField(tW, tb, precision=precision)
+    flat = [np.concatenate([W.reshape(-1), b]) for W, b in zip(Ws, bs)]
+    extra = []
+    if sde:
+        Wsig = (rng.standard_normal((D, D)) / np.sqrt(D)).astype(np.float32).astype(np.float64)
+        bsig = np.zeros(D)
+        tWs = torch.tensor(Wsig, dtype=torch.float32, device=dev, requires_grad=True)
+        tbs = torch.tensor(bsig, dtype=torch.float32, device=dev, requires_grad=True)
+        bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (D,), key=seed + 7)
+        terms = dfx.MultiTerm(dfx.ODETerm(field), dfx.ControlTerm(
+            dfx.TanhDiagonalDiffusion(tWs, tbs), bm))
+        flat += [Wsig.reshape(-1), bsig]
+        extra = [tWs, tbs]
+    else:
+        terms = dfx.ODETerm(field)
+    params = np.concatenate(flat)
+    y0_t = torch.tensor(y0, dtype=torch.float32, device=dev, requires_grad=True)
+    sol = dfx.diffeqsolve(terms, solver, 0.0, 1.0, dt0, y0_t, stepsize_controller=controller,
+                          adjoint=dfx.RecursiveCheckpointAdjoint(checkpoints=checkpoints),
+                          kernel=kernel)
+    loss = (sol.ys ** 2).mean()
+    loss.backward()
+    torch.cuda.synchronize()
+    g_params = torch.cat([t.grad.reshape(-1) for pair in zip(tW, tb) for t in pair] +
+                         [t.grad.reshape(-1) for t in extra]).double().cpu().numpy()
+    fields = dfx.lower(terms, solver, controller, dfx.SaveAt(t1=True), dim=D,
+                       dtype=torch.float32, max_steps=4096, n_ts=0)
+    d = O.make_desc(**O.oracle_fields(fields))
+    ref = O.solve(d, 0.0, 1.0, dt0, y0, params=params, nthreads=8)
+    G = 2.0 * ref["ys"] / ref["ys"].size
+    r = O.grad_recursive(d, 0.0, 1.0, dt0, y0, G, params=params, nthreads=8)
+    g_y0 = y0_t.grad.double().cpu().numpy()
+    e0 = float((np.abs(g_y0 - r["grad_y0"]).max(axis=1)
+                / np.abs(r["grad_y0"]).max(axis=1)).max())
+    return e0, rel(g_params, r["grad_params"])
+
+
+@pytest.mark.parametrize("sde", [False, True])
+def test_grad_product_precision_matches_plain_error(sde):
+    # The gradient workloads as specified, at a reduced batch: the neural ODE
+    # 64-128-128-64 with Tsit5 + PID(1e-5, 1e-7) and RecursiveCheckpointAdjoint(64),
+    # and the neural SDE 32-64-64-32 (diffusion 0.1 tanh(W y + b)) with Heun,
+    # dt 0.01, VBT tol 1e-3 and the default checkpoints.  The BF16 tensor-core
+    # form must be as accurate against the FP64 oracle as the plain FP32 form
+    # on the same inputs (within 2x: both solve in FP32 state and their FP32
+    # controllers take the same steps, which differ from the FP64 oracle's).
+    if sde:
+        args = ([32, 64, 64, 32], dfx.Heun(), dfx.ConstantStepSize(), 0.01, 128, None, True, 31)
+    else:
+        args = ([64, 128, 128, 64], dfx.Tsit5(), dfx.PIDController(rtol=1e-5, atol=1e-7), None,
+                128, 64, False, 32)
+    f0, fp = _loss_grad_case(*args, kernel="fused", precision="bf16")
+    p0, pp = _loss_grad_case(*args, kernel="plain", precision="fp32")
+    print(f"product-precision gradients (sde={sde}): fused BF16 dL/dy0 {f0:.2e} "
+          f"dL/dtheta {fp:.2e}; plain FP32 dL/dy0 {p0:.2e} dL/dtheta {pp:.2e}")
+    assert f0 <= 2 * p0 + 1e-6 and fp <= 2 * pp + 1e-6

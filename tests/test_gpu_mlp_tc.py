@@ -33,7 +33,7 @@ def oracle(field, params, y0, saveat, ctrl, t1=1.0):
     ts = None if saveat.ts is None else np.asarray(saveat.ts, dtype=np.float64)
     fields = dfx.lower(dfx.ODETerm(field), dfx.Tsit5(), ctrl, saveat, dim=64,
                        dtype=torch.float32, max_steps=4096, n_ts=0 if ts is None else ts.size)
-    d = O.make_desc(**dfx.oracle_fields(fields))
+    d = O.make_desc(**O.oracle_fields(fields))
     return O.solve(d, 0.0, t1, None, y0, params=params, ts=ts, nthreads=8)
 
 

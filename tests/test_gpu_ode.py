@@ -32,7 +32,7 @@ def run_both(field, solver, controller, saveat, t0, t1, dt0, y0, args, dtype, ke
     ts = None if saveat.ts is None else np.asarray(saveat.ts, dtype=np.float64)
     fields = dfx.lower(dfx.ODETerm(field), solver, controller, saveat, dim=y0.shape[1],
                        dtype=dtype, max_steps=max_steps, n_ts=0 if ts is None else ts.size)
-    d = O.make_desc(**dfx.oracle_fields(fields))
+    d = O.make_desc(**O.oracle_fields(fields))
     r = O.solve(d, t0, t1, dt0, y0, args=args, ts=ts, nthreads=8)
     return sol, r
 
@@ -122,8 +122,10 @@ def test_van_der_pol_uneven_fp64(kernel):
 
 @pytest.mark.parametrize("kernel", ["plain", "fused"])
 def test_van_der_pol_config2_fp32(kernel):
-    # Config 2 distribution; FP32 state with FP64 t/dt against the FP64 oracle.
-    mu, y0, t1 = vdp_inputs(8192, 3)
+    # The uneven Van der Pol workload at its full batch (65 536); FP32 state
+    # with FP64 t/dt against the FP64 oracle.  The largest errors sit on the
+    # stiff rows (mu near 10), where FP32 stage rounding moves the step ends.
+    mu, y0, t1 = vdp_inputs(65536, 3)
     sol, r = run_both(dfx.VanDerPol(), dfx.Dopri5(),
                       dfx.PIDController(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4),
                       dfx.SaveAt(t1=True), 0.0, t1, None, y0, mu[:, None], torch.float32,
@@ -132,8 +134,8 @@ def test_van_der_pol_config2_fp32(kernel):
     ys = sol.ys.cpu().numpy()
     per = np.abs(ys - r["ys"]).max(axis=(1, 2)) / np.abs(r["ys"]).max(axis=(1, 2))
     print(f"VdP config-2 FP32 {kernel}: median rel err {np.median(per):.2e} max {per.max():.2e}")
-    assert np.median(per) < 1e-4
-    assert np.quantile(per, 0.99) < 5e-3
+    assert np.median(per) < 5e-6
+    assert per.max() < 1e-3
     assert np.array_equal(sol.ts.cpu().numpy(), r["ts"])
 
 

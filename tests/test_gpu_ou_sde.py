@@ -27,7 +27,7 @@ def solve_pair(solver, ctrl, dt0, y0, args, bm, kernel, saveat=None, max_steps=4
     ts = None if saveat.ts is None else np.asarray(saveat.ts, dtype=np.float64)
     fields = dfx.lower(terms, solver, ctrl, saveat, dim=y0.shape[1], dtype=torch.float32,
                        max_steps=max_steps, n_ts=0 if ts is None else ts.size)
-    d = O.make_desc(**dfx.oracle_fields(fields))
+    d = O.make_desc(**O.oracle_fields(fields))
     r = O.solve(d, bm.t0, bm.t1, dt0, y0, args=args, ts=ts, nthreads=8)
     return sol, r
 

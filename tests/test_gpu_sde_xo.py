@@ -33,7 +33,7 @@ def _pair(solver, levy, saveat, ctrl, dt0, y0, max_steps=128, event=None, step_t
     fields = dfx.lower(terms, solver, ctrl, saveat, dim=y0.shape[1], dtype=torch.float32,
                        max_steps=max_steps, n_ts=0 if saveat.ts is None else len(saveat.ts),
                        event=event)
-    d = O.make_desc(**dfx.oracle_fields(fields))
+    d = O.make_desc(**O.oracle_fields(fields))
     ts = None if saveat.ts is None else np.asarray(saveat.ts, np.float64)
     r = O.solve(d, 0.0, 1.0, dt0, y0, args=ARGS, ts=ts, nthreads=8, step_ts=step_ts,
                 jump_ts=jump_ts)

@@ -175,7 +175,12 @@ def test_high_order_interpolants(solver):
 
 # --- DETEST against scipy DOP853 (test/test_detest.py:390-469) --------------
 
-REF_DETEST = "/root/reference/test/test_detest.py"
+# The reference tree: DIFFRAX_REFERENCE_DIR, else a checkout beside this
+# repository.  The test is skipped where neither exists.
+REF_DIR = os.environ.get("DIFFRAX_REFERENCE_DIR",
+                         os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(
+                             os.path.abspath(__file__)))), "reference"))
+REF_DETEST = os.path.join(REF_DIR, "test", "test_detest.py")
 
 
 class _At:

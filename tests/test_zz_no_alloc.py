@@ -67,7 +67,8 @@ def test_noalloc_matches_workspace_solve_on_repeated_calls():
     torch.cuda.synchronize()
     for _ in range(2):  # the second call reuses the array the first one left behind
         out = _noalloc_solve(fn, low)
-        assert torch.allclose(out[0], ref[0], rtol=1e-6, atol=0)
+        # the fused kernel is deterministic: the same solve gives the same bits
+        assert torch.equal(out[0], ref[0])
         assert torch.equal(out[1], ref[1])
         assert torch.equal(out[2], ref[2])
         assert torch.equal(out[3], ref[3])
@@ -81,7 +82,7 @@ def test_noalloc_second_problem_after_first():
         low = _problem(B, seed)
         ref = [t.clone() for t in low.run_forward()]
         out = _noalloc_solve(fn, low)
-        assert torch.allclose(out[0], ref[0], rtol=1e-6, atol=0)
+        assert torch.equal(out[0], ref[0])
         assert torch.equal(out[3], ref[3])
 
 
@@ -92,4 +93,23 @@ def test_noalloc_rejects_batches_beyond_the_array():
     rc = fn(low.problem.handle, 2_000_000, None, None, None, 1, None, None, 1, None, None,
             None, None, None, None, torch.cuda.current_stream().cuda_stream)
     assert rc == -4
-    assert "4 MiB" in _lib.last_error()
+    msg = _lib.last_error()
+    assert "4 MiB" in msg and "2000000 trajectories" in msg
+
+
+def test_noalloc_rejects_problems_with_an_adjoint():
+    # A gradient's tape must outlive the call in a workspace the backward
+    # reads, which the shared array cannot be.
+    fn = _bind(_lib.load())
+    dev = torch.device("cuda")
+    w = [64, 128, 128, 64]
+    field = dfx.MLPField([torch.zeros(w[i + 1], w[i], device=dev) for i in range(3)],
+                         [torch.zeros(w[i + 1], device=dev) for i in range(3)])
+    low = Lowered(dfx.ODETerm(field), dfx.Tsit5(), 0.0, 1.0, 0.1,
+                  torch.zeros(4, 64, device=dev), None, dfx.SaveAt(t1=True),
+                  dfx.ConstantStepSize(), dfx.RecursiveCheckpointAdjoint(), 16, "fused", 0, 0,
+                  want_grad=True)
+    rc = fn(low.problem.handle, 4, None, None, None, 0, None, None, 0, None, None,
+            None, None, None, None, torch.cuda.current_stream().cuda_stream)
+    assert rc != 0
+    assert "forward-only" in _lib.last_error()
