@@ -25,7 +25,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
 # The FP64-state kernels are the parity mode: no FMA contraction, so their
 # arithmetic rounds like the oracle's (built with -ffp-contract=off).
 PER_FILE_FLAGS = {"gbdx_ode_f64.cu": ["-fmad=false"], "gbdx_ode_f64_xo.cu": ["-fmad=false"],
-                  "gbdx_dense.cu": ["-fmad=false"]}
+                  "gbdx_dense.cu": ["-fmad=false"], "gbdx_ode_adj_f64.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:

@@ -414,6 +414,49 @@ class Lowered:
         return grad_y0, grad_params[:n_params]
 
 
+    def run_backward_args(self, ws, grad_ys, y0, args, stream=None):
+        """Analytic fields: dL/dy0 and dL/dargs from the tape the forward left
+        in `ws` (dL/dargs [B, n_args] for per-trajectory args, else [n_args])."""
+        dev = self.device
+        grad_ys = grad_ys.to(device=dev, dtype=self.dtype).contiguous()
+        grad_y0 = torch.empty((self.B, self.dim), dtype=self.dtype, device=dev)
+        na = self.drift.n_args
+        grad_args = torch.empty((self.B, na) if self.args_stride else (na,),
+                                dtype=self.dtype, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev).cuda_stream
+        p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        rc = self.problem.lib.gbdx_solve_bwd(
+            self.problem.handle, self.B, p(self.t0), p(self.t1), p(self.dt0), self.tstride,
+            p(y0), p(args), self.args_stride, None, p(self.save_ts), p(grad_ys),
+            p(grad_y0), p(grad_args), p(ws), ws.numel(), stream)
+        _lib.check(rc, "gbdx_solve_bwd")
+        return grad_y0, grad_args
+
+    def run_backsolve_args(self, ts_out, ys, grad_ys, args, stream=None):
+        """Analytic fields, BacksolveAdjoint: dL/dy0, dL/dargs and the
+        backward's RESULTS codes and step counts."""
+        dev = self.device
+        prob = self.bwd_problem
+        grad_ys = grad_ys.to(device=dev, dtype=self.dtype).contiguous()
+        grad_y0 = torch.empty((self.B, self.dim), dtype=self.dtype, device=dev)
+        na = self.drift.n_args
+        grad_args = torch.empty((self.B, na) if self.args_stride else (na,),
+                                dtype=self.dtype, device=dev)
+        res = torch.empty((self.B,), dtype=torch.int32, device=dev)
+        stats = torch.empty((self.B, 3), dtype=torch.int32, device=dev)
+        ws_bytes = prob.workspace_size(self.B)
+        ws = torch.empty((max(ws_bytes, 1),), dtype=torch.uint8, device=dev)
+        if stream is None:
+            stream = torch.cuda.current_stream(dev).cuda_stream
+        p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        rc = prob.lib.gbdx_backsolve_bwd_ex(
+            prob.handle, self.B, p(self.t0), p(self.t1), p(self.bwd_dt0), self.tstride,
+            p(ts_out.contiguous()), p(ys.contiguous()), p(grad_ys), p(args), self.args_stride,
+            None, p(grad_y0), p(grad_args), p(res), p(stats), p(ws), ws_bytes, stream)
+        _lib.check(rc, "gbdx_backsolve_bwd_ex")
+        return grad_y0, grad_args, res, stats
+
     def run_backsolve(self, ts_out, ys, grad_ys, params, stream=None):
         """BacksolveAdjoint backward from the forward's saved (ts, ys):
         dL/dy0, dL/dparams and the backward's RESULTS codes and step counts."""

@@ -87,6 +87,9 @@ def load():
         lib.gbdx_backsolve_bwd.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, vp, vp, vp, vp,
                                            vp, vp, vp, _c.c_size_t, vp]
         lib.gbdx_backsolve_bwd.restype = i32
+        lib.gbdx_backsolve_bwd_ex.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, vp, vp, i64,
+                                              vp, vp, vp, vp, vp, vp, _c.c_size_t, vp]
+        lib.gbdx_backsolve_bwd_ex.restype = i32
         lib.gbdx_last_error.argtypes = []
         lib.gbdx_last_error.restype = _c.c_char_p
         lib.gbdx_version.restype = i32

@@ -51,6 +51,7 @@ struct gbdx_problem {
   gbdx::OdeEntry ode;
   gbdx::BwdEntry bwd;  // RecursiveCheckpointAdjoint backward (MLP fields)
   gbdx::BsEntry bs;    // BacksolveAdjoint backward (MLP fields)
+  gbdx::AdjEntry adj;  // gradients of the analytic fields (y0 and args)
   bool mlp;            // MLP-field row-tile integrator
   int rows_per_cta;
   int mlp_block;       // threads per CTA of the MLP integrator
@@ -171,6 +172,26 @@ int ws_layout(const gbdx_problem *p, int64_t batch, WsLayout *L) {
     L->pcomp = off;
     off += up256(size_t(L->n_cta) * np * sizeof(float));
   }
+  if (d.adjoint == GBDX_ADJ_RECURSIVE && p->adj.rc_bwd) {
+    // the analytic fields: the full tape (time and state of every accepted
+    // step) and the per-trajectory args gradients
+    const size_t esz = d.dtype == GBDX_F32 ? 4 : 8, C = size_t(d.max_steps) + 1;
+    L->tape_t = off;
+    off += up256(B * C * sizeof(double));
+    L->tape_y = off;
+    off += up256(B * C * d.dim * esz);
+    L->tape_n = off;
+    off += up256(B * sizeof(int32_t));
+    L->tape_s = off;
+    off += up256(B * sizeof(int32_t));
+    L->scratch = off;
+    off += up256(B * size_t(p->adj.n_args) * esz);
+  } else if (d.adjoint == GBDX_ADJ_BACKSOLVE && p->adj.bs_bwd) {
+    const size_t esz = d.dtype == GBDX_F32 ? 4 : 8;
+    L->scratch = off;
+    off += up256(B * size_t(p->adj.n_args) * esz);
+    L->track = bs_tracks(d);
+  }
   L->total = off;
   return GBDX_OK;
 }
@@ -277,6 +298,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   p->ode = gbdx::OdeEntry{nullptr, nullptr};
   p->bwd = gbdx::BwdEntry{nullptr, nullptr};
   p->bs = gbdx::BsEntry{nullptr, nullptr, 0, 0, 0, 0};
+  p->adj = gbdx::AdjEntry{};
   p->mlp = false;
   p->rows_per_cta = 1;
   p->mlp_block = 256;
@@ -332,6 +354,21 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       return fail(GBDX_ERR_UNSUPPORTED, "no kernel for field %d with state dimension %d",
                   d.field, d.dim);
     }
+    if (d.adjoint != GBDX_ADJ_NONE) {
+      p->adj = d.dtype == GBDX_F32 ? gbdx::find_ode_adj_entry_f32(d.solver, d.field, d.dim, false)
+                                   : gbdx::find_ode_adj_entry_f64(d.solver, d.field, d.dim);
+      if (!p->adj.rc_bwd) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED,
+                    "gradients of the analytic fields take Euler, Heun, Dopri5 or Tsit5");
+      }
+      if (d.adjoint == GBDX_ADJ_RECURSIVE) p->ode = p->adj.fwd;
+      if (d.adjoint == GBDX_ADJ_BACKSOLVE && d.norm != GBDX_NORM_RMS &&
+          d.norm != GBDX_NORM_ADJOINT_SEMI) {
+        delete p;
+        return fail(GBDX_ERR_INVALID, "unknown norm %d", d.norm);
+      }
+    }
   } else if (sde && d.field == GBDX_ORNSTEIN_UHLENBECK && d.diffusion == GBDX_DIFF_OU) {
     if (d.dtype != GBDX_F32) {
       delete p;
@@ -348,6 +385,24 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       return fail(GBDX_ERR_UNSUPPORTED,
                   "no SDE kernel for state dimension %d (the Ornstein-Uhlenbeck SDE takes "
                   "dim 2 or 4) or solver %d", d.dim, d.solver);
+    }
+    if (d.adjoint == GBDX_ADJ_BACKSOLVE) {
+      delete p;
+      return fail(GBDX_ERR_UNSUPPORTED, "BacksolveAdjoint is available for ODEs");
+    }
+    if (d.adjoint == GBDX_ADJ_RECURSIVE) {
+      if (d.levy_area != GBDX_LEVY_NONE) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED,
+                    "gradients of the Ornstein-Uhlenbeck SDE take the W-only Brownian tree");
+      }
+      p->adj = gbdx::find_ode_adj_entry_f32(d.solver, d.field, d.dim, true);
+      if (!p->adj.rc_bwd) {
+        delete p;
+        return fail(GBDX_ERR_UNSUPPORTED,
+                    "gradients of the Ornstein-Uhlenbeck SDE take Euler or Heun");
+      }
+      p->ode = p->adj.fwd;
     }
   } else if (d.field == GBDX_MLP) {
     const int *w = d.mlp_widths;
@@ -594,7 +649,7 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
   // and square root of the tree's time scaling are done once here.
   P.vbt_inv_len = 1.0 / (d.vbt_t1 - d.vbt_t0);
   P.vbt_sqrt_len = float(sqrt(d.vbt_t1 - d.vbt_t0));
-  if (d.adjoint == GBDX_ADJ_RECURSIVE && problem->bwd.launch) {
+  if (d.adjoint == GBDX_ADJ_RECURSIVE && (problem->bwd.launch || problem->adj.rc_bwd)) {
     char *w = static_cast<char *>(workspace);
     P.tape_t = reinterpret_cast<double *>(w + L->tape_t);
     P.tape_y = reinterpret_cast<float *>(w + L->tape_y);
@@ -603,7 +658,7 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
     // An even slot count keeps the online thinning exact: when the slots
     // fill at step n = C s, n is a multiple of the doubled stride 2 s.  The
     // plain form tapes every accepted step.
-    P.checkpoints = d.kernel == GBDX_KERNEL_PLAIN
+    P.checkpoints = (d.kernel == GBDX_KERNEL_PLAIN || problem->adj.rc_bwd)
                         ? d.max_steps + 1
                         : (d.checkpoints >= 4 ? (d.checkpoints / 2) * 2 : 2);
   }
@@ -811,9 +866,10 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    void *grad_y0, void *grad_params, void *workspace,
                    size_t workspace_bytes, void *stream) {
   if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
-  if (problem->d.adjoint != GBDX_ADJ_RECURSIVE || !problem->bwd.launch)
+  if (problem->d.adjoint != GBDX_ADJ_RECURSIVE ||
+      (!problem->bwd.launch && !problem->adj.rc_bwd))
     return fail(GBDX_ERR_UNSUPPORTED,
-                "the problem was not created with RecursiveCheckpointAdjoint on an MLP field");
+                "the problem was not created with RecursiveCheckpointAdjoint");
   if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
   if (!grad_ys || !grad_y0 || !grad_params)
     return fail(GBDX_ERR_INVALID, "null gradient pointer");
@@ -823,6 +879,26 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    save_ts, workspace, workspace_bytes, &P, &L);
   if (rc != GBDX_OK) return rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (problem->adj.rc_bwd) {
+    // analytic fields: grad_params receives dL/dargs, per trajectory
+    // [batch, n_args] when args has a row per trajectory, else [n_args]
+    gbdx::AdjParams A;
+    memset(&A, 0, sizeof A);
+    A.grad_ys = grad_ys;
+    A.grad_y0 = grad_y0;
+    A.grad_args = args_stride != 0 ? grad_params : static_cast<char *>(workspace) + L.scratch;
+    cudaError_t e = problem->adj.rc_bwd(P, A, s);
+    if (e != cudaSuccess) return cuda_fail(e, "backward launch");
+    if (args_stride == 0) {
+      e = problem->d.dtype == GBDX_F32
+              ? gbdx::launch_reduce_arg_rows_f32(A.grad_args, batch, problem->adj.n_args,
+                                                 grad_params, s)
+              : gbdx::launch_reduce_arg_rows_f64(A.grad_args, batch, problem->adj.n_args,
+                                                 grad_params, s);
+      if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
+    }
+    return GBDX_OK;
+  }
   const int np = int(gbdx_param_count(problem));
   char *w = static_cast<char *>(workspace);
   gbdx::BwdParams Q;
@@ -859,11 +935,23 @@ int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double 
                        const void *params, void *grad_y0, void *grad_params,
                        int32_t *result_out, int32_t *stats_out, void *workspace,
                        size_t workspace_bytes, void *stream) {
+  return gbdx_backsolve_bwd_ex(problem, batch, t0, t1, dt0, time_stride, save_ts, ys, grad_ys,
+                               nullptr, 0, params, grad_y0, grad_params, result_out,
+                               stats_out, workspace, workspace_bytes, stream);
+}
+
+int gbdx_backsolve_bwd_ex(const gbdx_problem *problem, int64_t batch, const double *t0,
+                          const double *t1, const double *dt0, int64_t time_stride,
+                          const double *save_ts, const void *ys, const void *grad_ys,
+                          const void *args, int64_t args_stride, const void *params,
+                          void *grad_y0, void *grad_params, int32_t *result_out,
+                          int32_t *stats_out, void *workspace, size_t workspace_bytes,
+                          void *stream) {
   if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
   const gbdx_problem_desc &d = problem->d;
-  if (d.adjoint != GBDX_ADJ_BACKSOLVE || !problem->bs.launch)
+  if (d.adjoint != GBDX_ADJ_BACKSOLVE || (!problem->bs.launch && !problem->adj.bs_bwd))
     return fail(GBDX_ERR_UNSUPPORTED,
-                "the problem was not created with BacksolveAdjoint on an MLP field");
+                "the problem was not created with BacksolveAdjoint");
   if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
   if (!grad_ys || !grad_y0 || !grad_params || !ys || !result_out || !stats_out)
     return fail(GBDX_ERR_INVALID, "null pointer argument");
@@ -871,12 +959,33 @@ int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double 
   gbdx::SolveParams P;
   WsLayout L;
   // y0 is not read by the backward; the saved states stand in for the check.
-  int rc = prepare(problem, batch, t0, t1, dt0, time_stride, ys, nullptr, 0, params, save_ts,
-                   workspace, workspace_bytes, &P, &L);
+  int rc = prepare(problem, batch, t0, t1, dt0, time_stride, ys, args, args_stride, params,
+                   save_ts, workspace, workspace_bytes, &P, &L);
   if (rc != GBDX_OK) return rc;
   P.result_out = result_out;
   P.stats_out = stats_out;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (problem->adj.bs_bwd) {
+    // analytic fields: grad_params receives dL/dargs as in gbdx_solve_bwd
+    gbdx::AdjParams A;
+    memset(&A, 0, sizeof A);
+    A.grad_ys = grad_ys;
+    A.ys = ys;
+    A.grad_y0 = grad_y0;
+    A.grad_args = args_stride != 0 ? grad_params : static_cast<char *>(workspace) + L.scratch;
+    A.track_args = L.track ? 1 : 0;
+    cudaError_t e = problem->adj.bs_bwd(P, A, s);
+    if (e != cudaSuccess) return cuda_fail(e, "backsolve launch");
+    if (args_stride == 0) {
+      e = d.dtype == GBDX_F32
+              ? gbdx::launch_reduce_arg_rows_f32(A.grad_args, batch, problem->adj.n_args,
+                                                 grad_params, s)
+              : gbdx::launch_reduce_arg_rows_f64(A.grad_args, batch, problem->adj.n_args,
+                                                 grad_params, s);
+      if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
+    }
+    return GBDX_OK;
+  }
   const int np = int(gbdx_param_count(problem));
   const int D = d.dim, H = d.mlp_widths[1];
   char *w = static_cast<char *>(workspace);

@@ -378,6 +378,15 @@ struct LotkaVolterra {
     o[0] = a[0] * y[0] - a[1] * y[0] * y[1];
     o[1] = -a[2] * y[1] + a[3] * y[0] * y[1];
   }
+  // gy += (df/dy)^T g, ga += (df/da)^T g
+  __device__ static __forceinline__ void vjp(const T *a, const T *y, const T *g, T *gy, T *ga) {
+    gy[0] += g[0] * (a[0] - a[1] * y[1]) + g[1] * (a[3] * y[1]);
+    gy[1] += g[0] * (-a[1] * y[0]) + g[1] * (-a[2] + a[3] * y[0]);
+    ga[0] += g[0] * y[0];
+    ga[1] += -g[0] * y[0] * y[1];
+    ga[2] += -g[1] * y[1];
+    ga[3] += g[1] * y[0] * y[1];
+  }
 };
 
 template <class T>
@@ -389,6 +398,11 @@ struct VanDerPol {
     o[0] = y[1];
     o[1] = a[0] * (T(1) - y[0] * y[0]) * y[1] - y[0];
   }
+  __device__ static __forceinline__ void vjp(const T *a, const T *y, const T *g, T *gy, T *ga) {
+    gy[0] += g[1] * (T(-2) * a[0] * y[0] * y[1] - T(1));
+    gy[1] += g[0] + g[1] * a[0] * (T(1) - y[0] * y[0]);
+    ga[0] += g[1] * (T(1) - y[0] * y[0]) * y[1];
+  }
 };
 
 template <class T, int D_>
@@ -399,6 +413,14 @@ struct OrnsteinUhlenbeck {
   __device__ static __forceinline__ void vf(const SolveParams &, const T *a, const T *y, T *o) {
 #pragma unroll
     for (int i = 0; i < D; i++) o[i] = a[0] * (a[1] - y[i]);
+  }
+  __device__ static __forceinline__ void vjp(const T *a, const T *y, const T *g, T *gy, T *ga) {
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      gy[i] += -a[0] * g[i];
+      ga[0] += g[i] * (a[1] - y[i]);
+      ga[1] += g[i] * a[0];
+    }
   }
 };
 
@@ -416,6 +438,13 @@ struct OrnsteinUhlenbeckSDE : OrnsteinUhlenbeck<T, D_> {
                                                T *s) {
 #pragma unroll
     for (int i = 0; i < D_; i++) s[i] = a[2];
+  }
+  // VJP of y -> sigma(y) * dw (elementwise) with cotangent g: sigma is the
+  // constant a[2], so only ga[2] receives sum_i g_i dw_i.
+  __device__ static __forceinline__ void sigma_vjp(const T *, const T *, const T *dw,
+                                                   const T *g, T *, T *ga) {
+#pragma unroll
+    for (int i = 0; i < D_; i++) ga[2] += g[i] * dw[i];
   }
 };
 
@@ -498,6 +527,16 @@ struct BsParams {
   const uint2 *w0f, *w0v, *w2f, *w2v;  // B fragments (width 256)
   int track;             // the error norm runs over a_theta
   float n_norm;          // number of components in the error norm
+};
+
+// Arguments of the analytic-field backward kernels (device pointers in the
+// problem's dtype).
+struct AdjParams {
+  const void *grad_ys;  // [batch, n_save, D]
+  const void *ys;       // backsolve: the forward's saved states [batch, n_save, D]
+  void *grad_y0;        // [batch, D]
+  void *grad_args;      // [batch, n_args] per trajectory
+  int track_args;       // backsolve: the error norm covers a_args (rms_norm)
 };
 
 // Backward (RecursiveCheckpointAdjoint) arguments.

@@ -105,5 +105,22 @@ OdeEntry find_mlp_entry_d64h128(int solver, bool precise, bool sde);
 OdeEntry find_mlp_tc_entry(int solver, int D, int H, bool sde);
 OdeEntry find_mlp_entry_d64h256(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d32h64(int solver, bool precise, bool sde);
+// Gradients of the analytic-field solves (y0 and args): the forward with the
+// full tape, the RecursiveCheckpointAdjoint and BacksolveAdjoint backwards.
+struct AdjParams;
+using AdjLaunchFn = cudaError_t (*)(const SolveParams &, const AdjParams &, cudaStream_t);
+struct AdjEntry {
+  OdeEntry fwd{nullptr, nullptr};  // forward recording the tape
+  AdjLaunchFn rc_bwd = nullptr;    // RecursiveCheckpointAdjoint backward
+  AdjLaunchFn bs_bwd = nullptr;    // BacksolveAdjoint backward (ODEs)
+  int n_args = 0;
+};
+AdjEntry find_ode_adj_entry_f32(int solver, int field, int dim, bool sde);
+AdjEntry find_ode_adj_entry_f64(int solver, int field, int dim);
+// out[p] = compensated sum over the batch of rows[b][p] ([batch, n_args]).
+cudaError_t launch_reduce_arg_rows_f32(const void *rows, int64_t batch, int n_args, void *out,
+                                       cudaStream_t s);
+cudaError_t launch_reduce_arg_rows_f64(const void *rows, int64_t batch, int n_args, void *out,
+                                       cudaStream_t s);
 
 }  // namespace gbdx

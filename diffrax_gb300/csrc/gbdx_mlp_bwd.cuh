@@ -76,13 +76,17 @@ enum { kLoadNone = 0, kLoadCheckpoint = 1, kLoadScratch = 2 };
 template <class SH, bool PRECISE, bool SDE>
 struct BwdSmem;
 
+// The cotangents are hi/lo BF16 pairs like the forward's activations (~16
+// significant bits), so the gradient keeps the accuracy of the FP32 form.  The
+// layer-0 cotangent G1 is written into the storage of the layer-1 activations
+// A2 (hi and lo), which are dead once dW2 has been accumulated.
 template <class SH, bool SDE>
 struct BwdSmem<SH, false, SDE> {
+  static_assert(!SH::TIGHT, "G1 lives in the A2 storage of the untight layout");
   MlpSmem<SH, false, SDE> f;  // weights, biases, X, A1, A2 (forward recompute)
-  __nv_bfloat16 G3[SH::M][SH::PD];
-  __nv_bfloat16 Gs[SDE ? SH::M : 1][SH::PD];
-  __nv_bfloat16 G2[SH::M][SH::PH];
-  __nv_bfloat16 G1[SH::M][SH::PH];
+  __nv_bfloat16 G3[SH::M][SH::PD], G3l[SH::M][SH::PD];
+  __nv_bfloat16 Gs[SDE ? SH::M : 1][SH::PD], Gsl[SDE ? SH::M : 1][SH::PD];
+  __nv_bfloat16 G2[SH::M][SH::PH], G2l[SH::M][SH::PH];
   float db0[SH::H], db1[SH::H], db2[SH::D], dbs[SH::D];
   BwdRows<SH::M> rows;
 };
@@ -99,12 +103,13 @@ struct BwdSmem<SH, true, SDE> {
 };
 
 // dW[o][n] (at flat offset `off`, row length N) += G^T S over the tile's rows,
-// BF16 products, accumulated into this CTA's Kahan partials.
+// with G = Gh + Gl and S = Sh + Sl hi/lo BF16 pairs: the three BF16 products
+// Gh Sh + Gh Sl + Gl Sh, accumulated into this CTA's Kahan partials.
 template <class SH, int O, int N>
-__device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *G, int ldg,
-                                         const __nv_bfloat16 *S, const __nv_bfloat16 *Sl,
-                                         int lds, int off, float *psum, float *pcomp, int warp,
-                                         int lane) {
+__device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *G, const __nv_bfloat16 *Gl,
+                                         int ldg, const __nv_bfloat16 *S,
+                                         const __nv_bfloat16 *Sl, int lds, int off, float *psum,
+                                         float *pcomp, int warp, int lane) {
   constexpr int TILES = (O / 16) * (N / 8);
   static_assert(TILES % SH::WARPS == 0, "weight-gradient tile split");
   constexpr int T = TILES / SH::WARPS;
@@ -131,6 +136,7 @@ __device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *G, int ldg,
     for (int j = 0; j < CH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
     warp_tile_gemm_tt<SH::M, CH>(acc, G, ldg, ot * 16, S, lds, nt0 * 8, lane);
     warp_tile_gemm_tt<SH::M, CH>(acc, G, ldg, ot * 16, Sl, lds, nt0 * 8, lane);
+    warp_tile_gemm_tt<SH::M, CH>(acc, Gl, ldg, ot * 16, S, lds, nt0 * 8, lane);
 #pragma unroll
     for (int j = 0; j < CH; j++)
 #pragma unroll
@@ -170,10 +176,8 @@ struct MlpVjp {
         sm.G3[row][col] = G3r[e];
         if constexpr (SDE) sm.Gs[row][col] = gz;
       } else {
-        if ((e & 1) == 0) {
-          *reinterpret_cast<uint32_t *>(&sm.G3[row][col]) = pack_bf16x2(G3r[e], G3r[e + 1]);
-        }
-        if constexpr (SDE) sm.Gs[row][col] = __float2bfloat16_rn(gz);
+        if ((e & 1) == 0) store_split2(G3r[e], G3r[e + 1], &sm.G3[row][col], &sm.G3l[row][col]);
+        if constexpr (SDE) split_store(gz, &sm.Gs[row][col], &sm.Gsl[row][col]);
       }
       if (G3r[e] != 0.f) atomicAdd(&sm.db2[col], G3r[e]);
       if (SDE && gz != 0.f) atomicAdd(&sm.dbs[col], gz);
@@ -248,6 +252,8 @@ struct MlpVjp {
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         warp_tile_gemm_bt<D, SH::TPWH>(acc, &sm.G3[mt * 16][0], SH::PD, &sm.f.W2[0][0],
                                        SH::PH, nt0 * 8, lane);
+        warp_tile_gemm_bt<D, SH::TPWH>(acc, &sm.G3l[mt * 16][0], SH::PD, &sm.f.W2[0][0],
+                                       SH::PH, nt0 * 8, lane);
         if constexpr (SH::WSPLIT)
           warp_tile_gemm_bt<D, SH::TPWH>(acc, &sm.G3[mt * 16][0], SH::PD, sm.f.w2l(0),
                                          SH::PH, nt0 * 8, lane);
@@ -262,20 +268,25 @@ struct MlpVjp {
                              __bfloat162float(sm.f.a2l()[row][col + 1]);
             const float v0 = acc[j][2 * hr] * (1.f - a0 * a0);
             const float v1 = acc[j][2 * hr + 1] * (1.f - a1 * a1);
-            *reinterpret_cast<uint32_t *>(&sm.G2[row][col]) = pack_bf16x2(v0, v1);
+            store_split2(v0, v1, &sm.G2[row][col], &sm.G2l[row][col]);
             if (v0 != 0.f) atomicAdd(&sm.db1[col], v0);
             if (v1 != 0.f) atomicAdd(&sm.db1[col + 1], v1);
           }
       }
-      dw_tiles<SH, D, H>(&sm.G3[0][0], SH::PD, &sm.f.a2()[0][0], &sm.f.a2l()[0][0], SH::PH,
-                         SH::OW2, psum, pcomp, warp, lane);
+      dw_tiles<SH, D, H>(&sm.G3[0][0], &sm.G3l[0][0], SH::PD, &sm.f.a2()[0][0],
+                         &sm.f.a2l()[0][0], SH::PH, SH::OW2, psum, pcomp, warp, lane);
       __syncthreads();
+      // A2 is dead from here: G1 (hi/lo) takes its storage
+      __nv_bfloat16(*G1)[SH::PH] = sm.f.a2();
+      __nv_bfloat16(*G1l)[SH::PH] = sm.f.a2l();
       {  // 3. G1 = (G2 W1) * (1 - A1^2)
         const int t0 = warp * SH::TPWH, mt = t0 / SH::NTH, nt0 = t0 % SH::NTH;
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         warp_tile_gemm_bt<H, SH::TPWH>(acc, &sm.G2[mt * 16][0], SH::PH, &sm.f.W1[0][0],
+                                       SH::PH, nt0 * 8, lane);
+        warp_tile_gemm_bt<H, SH::TPWH>(acc, &sm.G2l[mt * 16][0], SH::PH, &sm.f.W1[0][0],
                                        SH::PH, nt0 * 8, lane);
         if constexpr (SH::WSPLIT)
           warp_tile_gemm_bt<H, SH::TPWH>(acc, &sm.G2[mt * 16][0], SH::PH, sm.f.w1l(0),
@@ -291,26 +302,30 @@ struct MlpVjp {
                              __bfloat162float(sm.f.A1l[row][col + 1]);
             const float v0 = acc[j][2 * hr] * (1.f - a0 * a0);
             const float v1 = acc[j][2 * hr + 1] * (1.f - a1 * a1);
-            *reinterpret_cast<uint32_t *>(&sm.G1[row][col]) = pack_bf16x2(v0, v1);
+            store_split2(v0, v1, &G1[row][col], &G1l[row][col]);
             if (v0 != 0.f) atomicAdd(&sm.db0[col], v0);
             if (v1 != 0.f) atomicAdd(&sm.db0[col + 1], v1);
           }
       }
-      dw_tiles<SH, H, H>(&sm.G2[0][0], SH::PH, &sm.f.A1[0][0], &sm.f.A1l[0][0], SH::PH,
-                         SH::OW1, psum, pcomp, warp, lane);
+      dw_tiles<SH, H, H>(&sm.G2[0][0], &sm.G2l[0][0], SH::PH, &sm.f.A1[0][0],
+                         &sm.f.A1l[0][0], SH::PH, SH::OW1, psum, pcomp, warp, lane);
       __syncthreads();
       {  // 4. gY = G1 W0 (+ Gs Ws), owned layout
         const int t0 = warp * SH::TPW, mt = t0 / SH::NT, nt0 = t0 % SH::NT;
         float acc[SH::TPW][4];
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        warp_tile_gemm_bt<H, SH::TPW>(acc, &sm.G1[mt * 16][0], SH::PH, &sm.f.W0[0][0], SH::PW0,
+        warp_tile_gemm_bt<H, SH::TPW>(acc, &G1[mt * 16][0], SH::PH, &sm.f.W0[0][0], SH::PW0,
+                                      nt0 * 8, lane);
+        warp_tile_gemm_bt<H, SH::TPW>(acc, &G1l[mt * 16][0], SH::PH, &sm.f.W0[0][0], SH::PW0,
                                       nt0 * 8, lane);
         if constexpr (SH::WSPLIT)
-          warp_tile_gemm_bt<H, SH::TPW>(acc, &sm.G1[mt * 16][0], SH::PH, sm.f.w0l(0),
+          warp_tile_gemm_bt<H, SH::TPW>(acc, &G1[mt * 16][0], SH::PH, sm.f.w0l(0),
                                         SH::PW0, nt0 * 8, lane);
         if constexpr (SDE) {
           warp_tile_gemm_bt<D, SH::TPW>(acc, &sm.Gs[mt * 16][0], SH::PD, &sm.f.Ws[0][0],
+                                        SH::PD, nt0 * 8, lane);
+          warp_tile_gemm_bt<D, SH::TPW>(acc, &sm.Gsl[mt * 16][0], SH::PD, &sm.f.Ws[0][0],
                                         SH::PD, nt0 * 8, lane);
           if constexpr (SH::WSPLIT)
             warp_tile_gemm_bt<D, SH::TPW>(acc, &sm.Gs[mt * 16][0], SH::PD, sm.f.wsl(0),
@@ -319,11 +334,11 @@ struct MlpVjp {
 #pragma unroll
         for (int e = 0; e < NE; e++) gY[e] = acc[e >> 2][e & 3];
       }
-      dw_tiles<SH, H, D>(&sm.G1[0][0], SH::PH, &sm.f.X[0][0], &sm.f.Xl[0][0], SH::PD, SH::OW0,
-                         psum, pcomp, warp, lane);
+      dw_tiles<SH, H, D>(&G1[0][0], &G1l[0][0], SH::PH, &sm.f.X[0][0], &sm.f.Xl[0][0], SH::PD,
+                         SH::OW0, psum, pcomp, warp, lane);
       if constexpr (SDE)
-        dw_tiles<SH, D, D>(&sm.Gs[0][0], SH::PD, &sm.f.X[0][0], &sm.f.Xl[0][0], SH::PD,
-                           SH::OWS, psum, pcomp, warp, lane);
+        dw_tiles<SH, D, D>(&sm.Gs[0][0], &sm.Gsl[0][0], SH::PD, &sm.f.X[0][0], &sm.f.Xl[0][0],
+                           SH::PD, SH::OWS, psum, pcomp, warp, lane);
     }
   }
 };

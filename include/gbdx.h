@@ -25,7 +25,7 @@
  *   gbdx_solve_bwd        <- the VJP of that solve under
  *                            RecursiveCheckpointAdjoint (diffrax/_adjoint.py:179-312)
  *   gbdx_backsolve_bwd    <- BacksolveAdjoint's backward pass
- *                            (diffrax/_adjoint.py:572-734, AdjointTerm
+ *   gbdx_backsolve_bwd_ex    (diffrax/_adjoint.py:572-734, AdjointTerm
  *                            diffrax/_term.py:767-910)
  */
 #ifndef GBDX_H_
@@ -235,15 +235,21 @@ int gbdx_solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    void *workspace, size_t workspace_bytes, void *stream);
 
 /*
- * Backward of a solve under RecursiveCheckpointAdjoint (MLP fields): the
+ * Backward of a solve under RecursiveCheckpointAdjoint: the
  * discretise-then-optimise VJP of the accepted-step map (the controller is
  * stop-gradient, as in the reference).  Call it after gbdx_solve_fwd on the
  * same problem, inputs and workspace: the forward recorded its accepted-step
- * time grid and state checkpoints there.
+ * time grid and state checkpoints there (every accepted state for the
+ * analytic fields).
  *   grad_ys     : device [batch, n_saves, dim] cotangent of ys (desc.dtype).
  *   grad_y0     : device [batch, dim] output, dL/dy0.
- *   grad_params : device [gbdx_param_count] output, dL/dparams summed over the
- *                 batch with compensated (Kahan) accumulation.
+ *   grad_params : MLP fields: device [gbdx_param_count] FP32 output,
+ *                 dL/dparams summed over the batch with compensated (Kahan)
+ *                 accumulation.  Analytic fields (Lotka-Volterra, Van der
+ *                 Pol, Ornstein-Uhlenbeck ODE and SDE; Euler, Heun, Dopri5,
+ *                 Tsit5): dL/dargs in desc.dtype, [batch, n_args] when args
+ *                 has a row per trajectory (args_stride = n_args), else
+ *                 [n_args] summed over the batch (compensated).
  */
 int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    const double *t1, const double *dt0, int64_t time_stride,
@@ -253,7 +259,7 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    size_t workspace_bytes, void *stream);
 
 /*
- * Backward of a solve under BacksolveAdjoint (MLP fields, ODEs): reverse-time
+ * Backward of a solve under BacksolveAdjoint (MLP field ODEs): reverse-time
  * solves of the augmented state (y, a, a_theta) between adjacent saved times
  * (diffrax/_adjoint.py:572-734) with the problem's solver and controller --
  * create the problem with adjoint = GBDX_ADJ_BACKSOLVE and the backward's
@@ -280,6 +286,27 @@ int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double 
                        const void *params, void *grad_y0, void *grad_params,
                        int32_t *result_out, int32_t *stats_out, void *workspace,
                        size_t workspace_bytes, void *stream);
+
+/*
+ * gbdx_backsolve_bwd with the field's args: the same backward pass
+ * (diffrax/_adjoint.py:572-734) for every field, including the analytic ones
+ * (Lotka-Volterra, Van der Pol, Ornstein-Uhlenbeck ODEs; Euler, Heun, Dopri5,
+ * Tsit5), whose augmented state is (y, a, a_args) -- AdjointTerm.vf
+ * (diffrax/_term.py:886-910) with the args as the differentiable leaves.
+ * GBDX_NORM_RMS runs the error norm over (y, a, a_args), GBDX_NORM_ADJOINT_SEMI
+ * over (y, a).  ys, grad_ys and grad_y0 are in desc.dtype.
+ *   args, args_stride : as for gbdx_solve_fwd (NULL, 0 for MLP fields).
+ *   grad_params : MLP fields as gbdx_backsolve_bwd; analytic fields dL/dargs,
+ *                 [batch, n_args] for per-trajectory args, else [n_args]
+ *                 summed over the batch (compensated).
+ */
+int gbdx_backsolve_bwd_ex(const gbdx_problem *problem, int64_t batch, const double *t0,
+                          const double *t1, const double *dt0, int64_t time_stride,
+                          const double *save_ts, const void *ys, const void *grad_ys,
+                          const void *args, int64_t args_stride, const void *params,
+                          void *grad_y0, void *grad_params, int32_t *result_out,
+                          int32_t *stats_out, void *workspace, size_t workspace_bytes,
+                          void *stream);
 
 /*
  * Forward solve with the optional outputs of gbdx_fwd_extras: the arguments of

@@ -1872,7 +1872,10 @@ int orc_grad_recursive(const orc_desc *d, int64_t B, const double *t0,
 /* ------------------------------------------------------------------------ */
 typedef struct {
   int64_t N;       /* augmented size 2D + n_args + n_params */
-  double *k[ORC_MAX_S], *zs, *z1, *err, *fsal, *f, *sc;
+  /* fsal: f at the current state (the solver state); fsal_new: f at the
+   * step's proposed state, committed to fsal only when the step is kept
+   * (_integrate.py:424 keeps the solver state of a rejected step) */
+  double *k[ORC_MAX_S], *zs, *z1, *err, *fsal, *fsal_new, *f, *sc;
 } AugWork;
 
 static void aug_alloc(AugWork *w, int64_t N) {
@@ -1882,13 +1885,15 @@ static void aug_alloc(AugWork *w, int64_t N) {
   w->z1 = (double *)calloc((size_t)N, sizeof(double));
   w->err = (double *)calloc((size_t)N, sizeof(double));
   w->fsal = (double *)calloc((size_t)N, sizeof(double));
+  w->fsal_new = (double *)calloc((size_t)N, sizeof(double));
   w->f = (double *)calloc((size_t)N, sizeof(double));
   w->sc = (double *)calloc((size_t)N, sizeof(double));
 }
 
 static void aug_free(AugWork *w) {
   for (int i = 0; i < ORC_MAX_S; i++) free(w->k[i]);
-  free(w->zs); free(w->z1); free(w->err); free(w->fsal); free(w->f); free(w->sc);
+  free(w->zs); free(w->z1); free(w->err); free(w->fsal); free(w->fsal_new); free(w->f);
+  free(w->sc);
 }
 
 /* AdjointTerm.vf at z (only the y and a_y parts of z enter). */
@@ -1921,7 +1926,7 @@ static void aug_step(const Field *F, const Tableau *tab, int dir, double tprev,
     } else {
       aug_vf(F, dir * ti, w->zs, w->f, N);
     }
-    if (tab->fsal && i == tab->s - 1) memcpy(w->fsal, w->f, sizeof(double) * (size_t)N);
+    if (tab->fsal && i == tab->s - 1) memcpy(w->fsal_new, w->f, sizeof(double) * (size_t)N);
     for (int64_t n = 0; n < N; n++) w->k[i][n] = w->f[n] * control;
   }
   for (int64_t n = 0; n < N; n++) {
@@ -2054,7 +2059,10 @@ static void backsolve_one(const BsIO *io, int64_t b, double *gP, AugWork *w) {
       if (nt1 > floor_te) nt1 = keep ? te : nt0 + 0.5 * (te - nt0);
       if (keep) {
         memcpy(z, w->z1, sizeof(double) * (size_t)N);
-        if (tab->fsal) have_f0 = 1;
+        if (tab->fsal) {
+          memcpy(w->fsal, w->fsal_new, sizeof(double) * (size_t)N);
+          have_f0 = 1;
+        }
       }
       if (seg_result == ORC_SUCCESSFUL) seg_result = cres;
       nsteps++;

@@ -437,6 +437,33 @@ def test_backsolve_against_recursive_and_exact(save_t0, save_t1, ts):
     assert tree_allclose(bs["grad_params"].reshape(2, 2), gA, atol=1e-5)
 
 
+@pytest.mark.parametrize("solver", ["TSIT5", "DOPRI5"])
+def test_backsolve_steps_equal_a_forward_solve_of_the_adjoint_system(solver):
+    # Under adjoint_rms_seminorm the error norm covers (y, a) only, and for
+    # y' = A y the (y, a) part of AdjointTerm.vf (_term.py:886-910) is the
+    # linear field z' = blockdiag(A, -A^T) z.  One backward segment (SaveAt(t1))
+    # must therefore take exactly the steps of a forward solve of that system
+    # from t1 to t0 with the same controller and dt0 -- including the retries
+    # after rejected steps, whose first stage is f at the unchanged state
+    # (the solver state of a rejected step is kept, _integrate.py:424).
+    kw = dict(solver=getattr(O, solver), controller=O.PID, rtol=1e-8, atol=1e-8, save_t1=1)
+    d = O.make_desc(field=O.LINEAR, dim=2, norm=O.NORM_ADJOINT_SEMI, **kw)
+    y0 = np.array([[0.9, 5.4]])
+    fwd = O.solve(d, 0.3, 9.5, 3.0, y0, params=_BS_A)
+    G = np.array([[[0.7, -1.3]]])
+    bs = O.backsolve(d, 0.3, 9.5, 3.0, fwd["ts"], fwd["ys"], G, params=_BS_A)
+    M = np.zeros((4, 4))
+    M[:2, :2] = _BS_A
+    M[2:, 2:] = -_BS_A.T
+    d4 = O.make_desc(field=O.LINEAR, dim=4, **kw)
+    z0 = np.concatenate([fwd["ys"][0, -1], G[0, -1]])[None]
+    aug = O.solve(d4, 9.5, 0.3, -3.0, z0, params=M)
+    assert bs["result"][0] == 0 and aug["result"][0] == 0
+    assert bs["stats"][0, 2] > 0  # the large dt0 forces rejections
+    assert np.array_equal(bs["stats"], aug["stats"])
+    assert np.allclose(bs["grad_y0"][0], aug["ys"][0, -1, 2:], rtol=1e-12, atol=0)
+
+
 def test_backsolve_seminorm():
     # adjoint_rms_seminorm (_misc.py:85-116) drops a_args and a_theta from the
     # error norm: fewer steps, same gradient to the tolerance.
