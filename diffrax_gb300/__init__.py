@@ -13,6 +13,7 @@ from ._core import (
 )
 from ._integrate import DenseInterpolation, diffeqsolve, lower
 from ._tune import GraphedSolve, autotune_launch, tuned_shapes
+from . import distributed
 
 __version__ = "0.1.0"
 

@@ -11,13 +11,21 @@ same arithmetic in one thread); the MLP kernels sum each row's error norm with
 shared-memory atomics, whose order, and so the last bit of a norm, may change
 with the shape.
 
+With ``GBDX_AUTOTUNE_CACHE`` set to a file path, the choices also persist
+across processes: they are read from that JSON file on first use and every
+new choice is written back, keyed by the GPU's name, the problem and the
+batch class.
+
 ``GraphedSolve`` captures one forward solve in a CUDA graph and replays it on
 new inputs of the same shapes, so a solve repeated inside a training or
 serving loop costs one graph launch.
 """
 from __future__ import annotations
 
+import json
 import math
+import os
+import tempfile
 
 import torch
 
@@ -70,14 +78,74 @@ def candidates(fields: dict, batch: int) -> list:
     return out
 
 
+_CACHE_ENV = "GBDX_AUTOTUNE_CACHE"
+_cache_loaded: set = set()
+
+
+def _cache_entry_key(device_name: str, key) -> str:
+    return json.dumps([device_name, [list(kv) for kv in key[0]], key[1]], sort_keys=True)
+
+
+def _device_name() -> str:
+    try:
+        return torch.cuda.get_device_name(torch.cuda.current_device())
+    except Exception:  # no device: the key still separates machines by name
+        return "unknown"
+
+
+def load_cache(path: str, device_name: str) -> int:
+    """Merge the choices recorded for `device_name` in the JSON file `path`
+    into this process's table; returns how many were read (0 when the file is
+    missing or unreadable)."""
+    try:
+        with open(path) as f:
+            data = json.load(f)
+    except (OSError, ValueError):
+        return 0
+    n = 0
+    for k, v in data.items():
+        try:
+            dev, items, cls = json.loads(k)
+        except (ValueError, TypeError):
+            continue
+        if dev != device_name:
+            continue
+        key = (tuple((a, tuple(b) if isinstance(b, list) else b) for a, b in items), cls)
+        _TUNED[key] = (str(v[0]), int(v[1]), int(v[2]))
+        n += 1
+    return n
+
+
+def save_cache(path: str, device_name: str) -> None:
+    """Write this process's choices for `device_name` into the JSON file
+    `path`, keeping the entries it already holds (atomic replace)."""
+    try:
+        with open(path) as f:
+            data = json.load(f)
+    except (OSError, ValueError):
+        data = {}
+    for key, shape in _TUNED.items():
+        data[_cache_entry_key(device_name, key)] = list(shape)
+    d = os.path.dirname(os.path.abspath(path))
+    fd, tmp = tempfile.mkstemp(dir=d, suffix=".tmp")
+    with os.fdopen(fd, "w") as f:
+        json.dump(data, f, indent=0, sort_keys=True)
+    os.replace(tmp, path)
+
+
 def autotune_launch(low_factory, batch: int, fields: dict, reps: int = 3,
                     verbose: bool = False):
     """Time every candidate shape of the problem and return the fastest
-    (kernel, block_threads, ctas_per_sm); cached per problem and batch class.
+    (kernel, block_threads, ctas_per_sm); cached per problem and batch class
+    (and in the GBDX_AUTOTUNE_CACHE file when that is set).
 
     ``low_factory(kernel, block_threads, ctas_per_sm)`` builds the Lowered
     solve."""
     key = _key(fields, batch)
+    path = os.environ.get(_CACHE_ENV)
+    if path and path not in _cache_loaded:
+        _cache_loaded.add(path)
+        load_cache(path, _device_name())
     hit = _TUNED.get(key)
     if hit is not None:
         return hit
@@ -100,6 +168,8 @@ def autotune_launch(low_factory, batch: int, fields: dict, reps: int = 3,
         if ms < best_ms:
             best, best_ms = shape, ms
     _TUNED[key] = best
+    if path:
+        save_cache(path, _device_name())
     return best
 
 

@@ -5,6 +5,7 @@
 // solve never allocates: scratch comes from the caller's workspace.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -35,6 +36,15 @@ int cuda_fail(cudaError_t e, const char *what) {
 }
 
 constexpr size_t kQueueBytes = 256;
+
+// An NVTX range over one C-ABI call, so a profiler's timeline shows which
+// solve issued which launches (no cost when no profiler is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 }  // namespace
 
@@ -694,6 +704,7 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
                      const double *save_ts, void *ys_out, double *ts_out, int32_t *result_out,
                      int32_t *stats_out, const gbdx_fwd_extras *ex, void *workspace,
                      size_t workspace_bytes, void *stream) {
+  NvtxRange nvtx("gbdx_solve_fwd");
   double *dense_ts = ex ? ex->dense_ts : nullptr;
   void *dense_info = ex ? ex->dense_info : nullptr;
   int32_t *dense_n = ex ? ex->dense_n : nullptr;
@@ -822,6 +833,7 @@ int gbdx_dense_evaluate(const gbdx_problem *problem, int64_t batch, const double
                         const double *dense_ts, const void *dense_info,
                         const int32_t *dense_n, int64_t Q, const double *query,
                         int64_t query_stride, int left, int order, void *out, void *stream) {
+  NvtxRange nvtx("gbdx_dense_evaluate");
   if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
   const gbdx_problem_desc &d = problem->d;
   if (!d.save_dense)
@@ -865,6 +877,7 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    const void *params, const double *save_ts, const void *grad_ys,
                    void *grad_y0, void *grad_params, void *workspace,
                    size_t workspace_bytes, void *stream) {
+  NvtxRange nvtx("gbdx_solve_bwd");
   if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
   if (problem->d.adjoint != GBDX_ADJ_RECURSIVE ||
       (!problem->bwd.launch && !problem->adj.rc_bwd))
@@ -947,6 +960,7 @@ int gbdx_backsolve_bwd_ex(const gbdx_problem *problem, int64_t batch, const doub
                           void *grad_y0, void *grad_params, int32_t *result_out,
                           int32_t *stats_out, void *workspace, size_t workspace_bytes,
                           void *stream) {
+  NvtxRange nvtx("gbdx_backsolve_bwd");
   if (!problem) return fail(GBDX_ERR_INVALID, "null problem");
   const gbdx_problem_desc &d = problem->d;
   if (d.adjoint != GBDX_ADJ_BACKSOLVE || (!problem->bs.launch && !problem->adj.bs_bwd))

@@ -13,8 +13,9 @@
 // A CTA of 8 warps integrates a tile of M trajectories ("rows") in lockstep,
 // as the forward kernel does; each row walks its own segments and refills
 // from the work counter after its last one.  Per RK stage the tile evaluates
-// f and the VJP a^T df/dy as chains of tensor-core products with hi/lo BF16
-// operands (or FP32 CUDA-core products in the parity mode) and records, per
+// f and the VJP a^T df/dy as chains of tensor-core products of the BF16
+// weights with hi/lo BF16 operands (or FP32 CUDA-core products in the parity
+// mode) and records, per
 // row, the vector pairs whose outer products are -a^T df/dtheta:
 //   (dz0, x) for W0/b0, (dz1, h1) for W1/b1, (a, h2) for W2/b2,
 // where x is the stage input, h1, h2 the hidden activations and dz0, dz1 the
@@ -48,11 +49,11 @@ struct BsShape {
   static constexpr int D = D_, H = H_;
   static constexpr int M = D_ >= 64 ? 16 : 32;  // rows per CTA
   static constexpr int THREADS = 256, WARPS = 8;
-  // Width 256: W1 stays in shared memory as BF16; W0 and W2 are read as
-  // pre-arranged BF16 fragments from global memory (L2).  Narrower fields
-  // keep all three as hi/lo BF16 pairs in shared memory.
+  // The weights are the model's BF16 values (as in the forward kernel).
+  // Width 256: W1 stays in shared memory; W0 and W2 are read as pre-arranged
+  // BF16 fragments from global memory (L2).  Narrower fields keep all three
+  // in shared memory.
   static constexpr bool GFRAG = H_ >= 256;
-  static constexpr bool WSPLIT = !GFRAG;
   static constexpr int PD = D + 8, PH = H + 8;
   static constexpr int MT = M / 16, NT = D / 8, NTH = H / 8;
   static constexpr int TPW = MT * NT / WARPS;    // output tiles per warp
@@ -85,9 +86,9 @@ template <class SH, bool GF>
 struct BsWeights;
 template <class SH>
 struct BsWeights<SH, false> {
-  __nv_bfloat16 W0[SH::H][SH::PD], W0l[SH::H][SH::PD];
-  __nv_bfloat16 W1[SH::H][SH::PH], W1l[SH::H][SH::PH];
-  __nv_bfloat16 W2[SH::D][SH::PH], W2l[SH::D][SH::PH];
+  __nv_bfloat16 W0[SH::H][SH::PD];
+  __nv_bfloat16 W1[SH::H][SH::PH];
+  __nv_bfloat16 W2[SH::D][SH::PH];
 };
 template <class SH>
 struct BsWeights<SH, true> {
@@ -183,11 +184,11 @@ struct BsField {
           sm.W1[i / H][i % H] = __float2bfloat16_rn(P[SH::OW1 + i]);
       } else {
         for (int i = tid; i < H * D; i += SH::THREADS)
-          split_store(P[SH::OW0 + i], &sm.W0[i / D][i % D], &sm.W0l[i / D][i % D]);
+          sm.W0[i / D][i % D] = __float2bfloat16_rn(P[SH::OW0 + i]);
         for (int i = tid; i < H * H; i += SH::THREADS)
-          split_store(P[SH::OW1 + i], &sm.W1[i / H][i % H], &sm.W1l[i / H][i % H]);
+          sm.W1[i / H][i % H] = __float2bfloat16_rn(P[SH::OW1 + i]);
         for (int i = tid; i < D * H; i += SH::THREADS)
-          split_store(P[SH::OW2 + i], &sm.W2[i / H][i % H], &sm.W2l[i / H][i % H]);
+          sm.W2[i / H][i % H] = __float2bfloat16_rn(P[SH::OW2 + i]);
       }
     }
   }
@@ -328,7 +329,7 @@ struct BsField {
                                   nth0, lane);
         else
           fwd_gemm<D, SH::TPWH>(acc, &sm.a.X[mth * 16][0], &sm.a.Xl[mth * 16][0], SH::PD,
-                                &sm.W0[nth0 * 8][0], &sm.W0l[nth0 * 8][0], SH::PD, lane);
+                                &sm.W0[nth0 * 8][0], nullptr, SH::PD, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
           const int col = (nth0 + j) * 8 + 2 * c, r0 = mth * 16 + g;
@@ -344,10 +345,8 @@ struct BsField {
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        const __nv_bfloat16 *w1l = nullptr;
-        if constexpr (SH::WSPLIT) w1l = &sm.W1l[nth0 * 8][0];
         fwd_gemm<H, SH::TPWH>(acc, &sm.a.R1[mth * 16][0], &sm.a.R1l[mth * 16][0], SH::PH,
-                              &sm.W1[nth0 * 8][0], w1l, SH::PH, lane);
+                              &sm.W1[nth0 * 8][0], nullptr, SH::PH, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
           const int col = (nth0 + j) * 8 + 2 * c, r0 = mth * 16 + g;
@@ -368,7 +367,7 @@ struct BsField {
                                  nto0, lane);
         else
           fwd_gemm<H, SH::TPW>(acc, &sm.a.R2[mto * 16][0], &sm.a.R2l[mto * 16][0], SH::PH,
-                               &sm.W2[nto0 * 8][0], &sm.W2l[nto0 * 8][0], SH::PH, lane);
+                               &sm.W2[nto0 * 8][0], nullptr, SH::PH, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) {
           int row, col;
@@ -386,7 +385,7 @@ struct BsField {
                                   nth0, lane);
         else
           vjp_gemm<D, SH::TPWH>(acc, &sm.a.G[mth * 16][0], &sm.a.Gl[mth * 16][0], SH::PD,
-                                &sm.W2[0][0], &sm.W2l[0][0], SH::PH, nth0 * 8, lane);
+                                &sm.W2[0][0], nullptr, SH::PH, nth0 * 8, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
@@ -404,10 +403,8 @@ struct BsField {
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        const __nv_bfloat16 *w1l = nullptr;
-        if constexpr (SH::WSPLIT) w1l = &sm.W1l[0][0];
         vjp_gemm<H, SH::TPWH>(acc, &sm.a.R2[mth * 16][0], &sm.a.R2l[mth * 16][0], SH::PH,
-                              &sm.W1[0][0], w1l, SH::PH, nth0 * 8, lane);
+                              &sm.W1[0][0], nullptr, SH::PH, nth0 * 8, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
@@ -430,7 +427,7 @@ struct BsField {
                                  nto0, lane);
         else
           vjp_gemm<H, SH::TPW>(acc, &sm.a.R1[mto * 16][0], &sm.a.R1l[mto * 16][0], SH::PH,
-                               &sm.W0[0][0], &sm.W0l[0][0], SH::PD, nto0 * 8, lane);
+                               &sm.W0[0][0], nullptr, SH::PD, nto0 * 8, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) GY[e] = acc[e >> 2][e & 3];
       }

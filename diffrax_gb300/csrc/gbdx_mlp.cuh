@@ -5,6 +5,11 @@
 // stage the tile evaluates the field as a chain of tensor-core products,
 //   F = W2 tanh(W1 tanh(W0 Y + b0) + b1) + b2        (eqx.nn.MLP semantics)
 // with the weights resident in shared memory as BF16 and FP32 accumulation.
+// The weights are the model's BF16 values (FP32 inputs are rounded to BF16);
+// the operands they multiply -- stage inputs, hidden activations -- are held
+// as sums of three BF16 pieces (24 significant bits), so every product is
+// exact up to the FP32 accumulation and the field is as accurate as an FP32
+// evaluation with the same weights.
 // The RK state of every (row, component) -- y, the stage increments k_i, the
 // FSAL vector and the error estimate -- lives in registers in the layout of
 // the last product's accumulator fragments, so all stage arithmetic is
@@ -42,9 +47,9 @@ struct MlpShape {
   static constexpr int TPW = MT * NT / WARPS;       // output tiles per warp
   static constexpr int TPWH = MT * NTH / WARPS;     // hidden tiles per warp
   static constexpr int NE = 4 * TPW;                // owned elements per thread
-  // Weights are held as BF16 hi/lo pairs when both halves fit in shared
-  // memory (width <= 128); at width 256 only the hi half (the BF16 weights).
-  static constexpr bool WSPLIT = H_ <= 128;
+  // BF16 pieces of each activation operand: three (24 bits) up to width 128;
+  // two (16 bits) at width 256, where the weights fill shared memory.
+  static constexpr int NP = H_ <= 128 ? 3 : 2;
   static_assert(MT * NT % WARPS == 0 && TPW >= 1, "tile split");
   static_assert(MT * NTH % WARPS == 0 && NTH % TPWH == 0, "hidden tile split");
   static_assert(NT % TPW == 0, "output tile split");
@@ -66,35 +71,27 @@ struct RowState {
 template <class SH, bool PRECISE, bool SDE>
 struct MlpSmem;
 
-// lo halves of the weights (present only when they fit)
-template <class SH, bool SDE, bool ON>
-struct WeightLo {
-  __nv_bfloat16 W0l[SH::H][SH::PW0];
-  __nv_bfloat16 W1l[SH::H][SH::PH];
-  __nv_bfloat16 W2l[SH::D][SH::PH];
-  __nv_bfloat16 Wsl[SDE ? SH::D : 1][SH::PD];
-};
-template <class SH, bool SDE>
-struct WeightLo<SH, SDE, false> {};
-
 // A2 storage (aliased onto A1 in the tight layout)
 template <class SH, bool OWN>
 struct Act2 {
   __nv_bfloat16 A2s[SH::M][SH::PH], A2ls[SH::M][SH::PH];
+  __nv_bfloat16 A2l2s[SH::NP == 3 ? SH::M : 1][SH::PH];
 };
 template <class SH>
 struct Act2<SH, false> {};
 
 template <class SH, bool SDE>
-struct MlpSmem<SH, false, SDE> : WeightLo<SH, SDE, SH::WSPLIT>, Act2<SH, !SH::TIGHT> {
+struct MlpSmem<SH, false, SDE> : Act2<SH, !SH::TIGHT> {
+  static constexpr int M3 = SH::NP == 3 ? SH::M : 1;
   __nv_bfloat16 W0[SH::H][SH::PW0];
   __nv_bfloat16 W1[SH::H][SH::PH];
   __nv_bfloat16 W2[SH::D][SH::PH];
   __nv_bfloat16 Ws[SDE ? SH::D : 1][SH::PD];
   float b0[SH::H], b1[SH::H], b2[SH::D], bs[SH::D];
-  // stage input and hidden activations as hi/lo BF16 pairs
-  __nv_bfloat16 X[SH::M][SH::PD], Xl[SH::M][SH::PD];
-  __nv_bfloat16 A1[SH::M][SH::PH], A1l[SH::M][SH::PH];
+  // stage input and hidden activations as BF16 pieces (the third piece only
+  // with NP == 3)
+  __nv_bfloat16 X[SH::M][SH::PD], Xl[SH::M][SH::PD], Xl2[M3][SH::PD];
+  __nv_bfloat16 A1[SH::M][SH::PH], A1l[SH::M][SH::PH], A1l2[M3][SH::PH];
   RowState<SH::M> rows;
   __device__ __nv_bfloat16 (*a2())[SH::PH] {
     if constexpr (SH::TIGHT) return A1; else return this->A2s;
@@ -102,18 +99,13 @@ struct MlpSmem<SH, false, SDE> : WeightLo<SH, SDE, SH::WSPLIT>, Act2<SH, !SH::TI
   __device__ __nv_bfloat16 (*a2l())[SH::PH] {
     if constexpr (SH::TIGHT) return A1l; else return this->A2ls;
   }
-  __device__ const __nv_bfloat16 *w0l(int r) const {
-    if constexpr (SH::WSPLIT) return &this->W0l[r][0]; else return nullptr;
+  __device__ __nv_bfloat16 (*a2l2())[SH::PH] {
+    if constexpr (SH::TIGHT) return A1l2; else return this->A2l2s;
   }
-  __device__ const __nv_bfloat16 *w1l(int r) const {
-    if constexpr (SH::WSPLIT) return &this->W1l[r][0]; else return nullptr;
-  }
-  __device__ const __nv_bfloat16 *w2l(int r) const {
-    if constexpr (SH::WSPLIT) return &this->W2l[r][0]; else return nullptr;
-  }
-  __device__ const __nv_bfloat16 *wsl(int r) const {
-    if constexpr (SH::WSPLIT && SDE) return &this->Wsl[r][0]; else return nullptr;
-  }
+  // the third pieces' rows (null with two pieces)
+  __device__ __nv_bfloat16 *xl2(int r) { return SH::NP == 3 ? &Xl2[r][0] : nullptr; }
+  __device__ __nv_bfloat16 *a1l2(int r) { return SH::NP == 3 ? &A1l2[r][0] : nullptr; }
+  __device__ __nv_bfloat16 *a2l2r(int r) { return SH::NP == 3 ? &a2l2()[r][0] : nullptr; }
 };
 
 template <class SH, bool SDE>
@@ -151,20 +143,16 @@ struct MlpField {
       if (SDE) sm.bs[i] = P[SH::OBS + i];
     }
     if constexpr (!PRECISE) {
-      constexpr bool WS = SH::WSPLIT;
+      // the model's BF16 weights
       for (int i = tid; i < H * D; i += SH::THREADS)
-        split_store(P[SH::OW0 + i], &sm.W0[i / D][i % D],
-                    WS ? const_cast<__nv_bfloat16 *>(sm.w0l(i / D)) + i % D : nullptr);
+        sm.W0[i / D][i % D] = __float2bfloat16_rn(P[SH::OW0 + i]);
       for (int i = tid; i < H * H; i += SH::THREADS)
-        split_store(P[SH::OW1 + i], &sm.W1[i / H][i % H],
-                    WS ? const_cast<__nv_bfloat16 *>(sm.w1l(i / H)) + i % H : nullptr);
+        sm.W1[i / H][i % H] = __float2bfloat16_rn(P[SH::OW1 + i]);
       for (int i = tid; i < D * H; i += SH::THREADS)
-        split_store(P[SH::OW2 + i], &sm.W2[i / H][i % H],
-                    WS ? const_cast<__nv_bfloat16 *>(sm.w2l(i / H)) + i % H : nullptr);
+        sm.W2[i / H][i % H] = __float2bfloat16_rn(P[SH::OW2 + i]);
       if constexpr (SDE)
         for (int i = tid; i < D * D; i += SH::THREADS)
-          split_store(P[SH::OWS + i], &sm.Ws[i / D][i % D],
-                      WS ? const_cast<__nv_bfloat16 *>(sm.wsl(i / D)) + i % D : nullptr);
+          sm.Ws[i / D][i % D] = __float2bfloat16_rn(P[SH::OWS + i]);
     }
   }
 
@@ -178,21 +166,21 @@ struct MlpField {
         sm.X[row][col] = Y[e];
         sm.X[row][col + 1] = Y[e + 1];
       } else {
-        store_split2(Y[e], Y[e + 1], &sm.X[row][col], &sm.Xl[row][col]);
+        __nv_bfloat16 *x2 = sm.xl2(row);
+        store_split3x2(Y[e], Y[e + 1], &sm.X[row][col], &sm.Xl[row][col],
+                       x2 ? x2 + col : nullptr);
       }
     }
   }
 
-  // acc += (Ah + Al)[rows, K] (Wh + Wl)[n, K]^T without the lo*lo term: three
-  // BF16 tensor-core products (two when the weights are not split).
+  // acc += (A0 + A1 [+ A2])[rows, K] W[n, K]^T: one BF16 tensor-core product
+  // per activation piece against the BF16 weights.
   template <int K, int NTW>
-  __device__ static __forceinline__ void split_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *Ah,
-                                                    const __nv_bfloat16 *Al, int lda,
-                                                    const __nv_bfloat16 *Wh,
-                                                    const __nv_bfloat16 *Wl, int ldw, int lane) {
-    warp_tile_gemm<K, NTW>(acc, Ah, lda, Wh, ldw, lane);
-    warp_tile_gemm<K, NTW>(acc, Al, lda, Wh, ldw, lane);
-    if constexpr (SH::WSPLIT) warp_tile_gemm<K, NTW>(acc, Ah, lda, Wl, ldw, lane);
+  __device__ static __forceinline__ void split_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *A0,
+                                                    const __nv_bfloat16 *A1,
+                                                    const __nv_bfloat16 *A2, int lda,
+                                                    const __nv_bfloat16 *W, int ldw, int lane) {
+    warp_tile_gemm_p<K, NTW, SH::NP>(acc, A0, A1, A2, lda, W, ldw, lane);
   }
 
   // F = MLP(X) and (SDE) sigma = 0.1 tanh(Ws X + bs), both in the owned layout.
@@ -241,16 +229,17 @@ struct MlpField {
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        split_gemm<D, SH::TPWH>(acc, &sm.X[mt * 16][0], &sm.Xl[mt * 16][0], SH::PD,
-                                &sm.W0[nt0 * 8][0], sm.w0l(nt0 * 8), SH::PW0, lane);
+        split_gemm<D, SH::TPWH>(acc, &sm.X[mt * 16][0], &sm.Xl[mt * 16][0], sm.xl2(mt * 16),
+                                SH::PD, &sm.W0[nt0 * 8][0], SH::PW0, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
           const int col = (nt0 + j) * 8 + 2 * c, r0 = mt * 16 + g;
           const float bb0 = sm.b0[col], bb1 = sm.b0[col + 1];
-          store_split2(tanhf(acc[j][0] + bb0), tanhf(acc[j][1] + bb1), &sm.A1[r0][col],
-                       &sm.A1l[r0][col]);
-          store_split2(tanhf(acc[j][2] + bb0), tanhf(acc[j][3] + bb1), &sm.A1[r0 + 8][col],
-                       &sm.A1l[r0 + 8][col]);
+          __nv_bfloat16 *p2a = sm.a1l2(r0), *p2b = sm.a1l2(r0 + 8);
+          store_split3x2(tanhf(acc[j][0] + bb0), tanhf(acc[j][1] + bb1), &sm.A1[r0][col],
+                         &sm.A1l[r0][col], p2a ? p2a + col : nullptr);
+          store_split3x2(tanhf(acc[j][2] + bb0), tanhf(acc[j][3] + bb1), &sm.A1[r0 + 8][col],
+                         &sm.A1l[r0 + 8][col], p2b ? p2b + col : nullptr);
         }
       }
       if constexpr (SDE) {  // diffusion product on the same operand
@@ -258,8 +247,8 @@ struct MlpField {
         float acc[SH::TPW][4];
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        split_gemm<D, SH::TPW>(acc, &sm.X[mt * 16][0], &sm.Xl[mt * 16][0], SH::PD,
-                               &sm.Ws[nt0 * 8][0], sm.wsl(nt0 * 8), SH::PD, lane);
+        split_gemm<D, SH::TPW>(acc, &sm.X[mt * 16][0], &sm.Xl[mt * 16][0], sm.xl2(mt * 16),
+                               SH::PD, &sm.Ws[nt0 * 8][0], SH::PD, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) {
           int row, col;
@@ -273,8 +262,8 @@ struct MlpField {
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        split_gemm<H, SH::TPWH>(acc, &sm.A1[mt * 16][0], &sm.A1l[mt * 16][0], SH::PH,
-                                &sm.W1[nt0 * 8][0], sm.w1l(nt0 * 8), SH::PH, lane);
+        split_gemm<H, SH::TPWH>(acc, &sm.A1[mt * 16][0], &sm.A1l[mt * 16][0], sm.a1l2(mt * 16),
+                                SH::PH, &sm.W1[nt0 * 8][0], SH::PH, lane);
         if constexpr (SH::TIGHT) __syncthreads();  // every warp has read A1
         auto A2 = sm.a2();
         auto A2l = sm.a2l();
@@ -282,10 +271,11 @@ struct MlpField {
         for (int j = 0; j < SH::TPWH; j++) {
           const int col = (nt0 + j) * 8 + 2 * c, r0 = mt * 16 + g;
           const float bb0 = sm.b1[col], bb1 = sm.b1[col + 1];
-          store_split2(tanhf(acc[j][0] + bb0), tanhf(acc[j][1] + bb1), &A2[r0][col],
-                       &A2l[r0][col]);
-          store_split2(tanhf(acc[j][2] + bb0), tanhf(acc[j][3] + bb1), &A2[r0 + 8][col],
-                       &A2l[r0 + 8][col]);
+          __nv_bfloat16 *p2a = sm.a2l2r(r0), *p2b = sm.a2l2r(r0 + 8);
+          store_split3x2(tanhf(acc[j][0] + bb0), tanhf(acc[j][1] + bb1), &A2[r0][col],
+                         &A2l[r0][col], p2a ? p2a + col : nullptr);
+          store_split3x2(tanhf(acc[j][2] + bb0), tanhf(acc[j][3] + bb1), &A2[r0 + 8][col],
+                         &A2l[r0 + 8][col], p2b ? p2b + col : nullptr);
         }
       }
       __syncthreads();
@@ -294,8 +284,8 @@ struct MlpField {
         float acc[SH::TPW][4];
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        split_gemm<H, SH::TPW>(acc, &sm.a2()[mt * 16][0], &sm.a2l()[mt * 16][0], SH::PH,
-                               &sm.W2[nt0 * 8][0], sm.w2l(nt0 * 8), SH::PH, lane);
+        split_gemm<H, SH::TPW>(acc, &sm.a2()[mt * 16][0], &sm.a2l()[mt * 16][0],
+                               sm.a2l2r(mt * 16), SH::PH, &sm.W2[nt0 * 8][0], SH::PH, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) {
           int row, col;

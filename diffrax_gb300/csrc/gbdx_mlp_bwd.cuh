@@ -76,17 +76,20 @@ enum { kLoadNone = 0, kLoadCheckpoint = 1, kLoadScratch = 2 };
 template <class SH, bool PRECISE, bool SDE>
 struct BwdSmem;
 
-// The cotangents are hi/lo BF16 pairs like the forward's activations (~16
-// significant bits), so the gradient keeps the accuracy of the FP32 form.  The
-// layer-0 cotangent G1 is written into the storage of the layer-1 activations
-// A2 (hi and lo), which are dead once dW2 has been accumulated.
+// The cotangents are held as three BF16 pieces like the forward's
+// activations (24 significant bits), so the gradient keeps the accuracy of an
+// FP32 evaluation with the same BF16 weights.  The layer-0 cotangent G1 is
+// written into the storage of the layer-1 activations A2 (all three pieces),
+// which are dead once dW2 has been accumulated.
 template <class SH, bool SDE>
 struct BwdSmem<SH, false, SDE> {
-  static_assert(!SH::TIGHT, "G1 lives in the A2 storage of the untight layout");
+  static_assert(!SH::TIGHT && SH::NP == 3,
+                "three-piece operands; G1 lives in the A2 storage of the untight layout");
   MlpSmem<SH, false, SDE> f;  // weights, biases, X, A1, A2 (forward recompute)
-  __nv_bfloat16 G3[SH::M][SH::PD], G3l[SH::M][SH::PD];
-  __nv_bfloat16 Gs[SDE ? SH::M : 1][SH::PD], Gsl[SDE ? SH::M : 1][SH::PD];
-  __nv_bfloat16 G2[SH::M][SH::PH], G2l[SH::M][SH::PH];
+  __nv_bfloat16 G3[SH::M][SH::PD], G3l[SH::M][SH::PD], G3l2[SH::M][SH::PD];
+  __nv_bfloat16 Gs[SDE ? SH::M : 1][SH::PD], Gsl[SDE ? SH::M : 1][SH::PD],
+      Gsl2[SDE ? SH::M : 1][SH::PD];
+  __nv_bfloat16 G2[SH::M][SH::PH], G2l[SH::M][SH::PH], G2l2[SH::M][SH::PH];
   float db0[SH::H], db1[SH::H], db2[SH::D], dbs[SH::D];
   BwdRows<SH::M> rows;
 };
@@ -103,13 +106,12 @@ struct BwdSmem<SH, true, SDE> {
 };
 
 // dW[o][n] (at flat offset `off`, row length N) += G^T S over the tile's rows,
-// with G = Gh + Gl and S = Sh + Sl hi/lo BF16 pairs: the three BF16 products
-// Gh Sh + Gh Sl + Gl Sh, accumulated into this CTA's Kahan partials.
+// with G and S held as three BF16 pieces each (warp_tile_gemm_tt3),
+// accumulated into this CTA's Kahan partials.
 template <class SH, int O, int N>
-__device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *G, const __nv_bfloat16 *Gl,
-                                         int ldg, const __nv_bfloat16 *S,
-                                         const __nv_bfloat16 *Sl, int lds, int off, float *psum,
-                                         float *pcomp, int warp, int lane) {
+__device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *const (&G)[3], int ldg,
+                                         const __nv_bfloat16 *const (&S)[3], int lds, int off,
+                                         float *psum, float *pcomp, int warp, int lane) {
   constexpr int TILES = (O / 16) * (N / 8);
   static_assert(TILES % SH::WARPS == 0, "weight-gradient tile split");
   constexpr int T = TILES / SH::WARPS;
@@ -134,9 +136,7 @@ __device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *G, const __nv_bflo
     float acc[CH][4];
 #pragma unroll
     for (int j = 0; j < CH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-    warp_tile_gemm_tt<SH::M, CH>(acc, G, ldg, ot * 16, S, lds, nt0 * 8, lane);
-    warp_tile_gemm_tt<SH::M, CH>(acc, G, ldg, ot * 16, Sl, lds, nt0 * 8, lane);
-    warp_tile_gemm_tt<SH::M, CH>(acc, Gl, ldg, ot * 16, S, lds, nt0 * 8, lane);
+    warp_tile_gemm_tt3<SH::M, CH>(acc, G, ldg, ot * 16, S, lds, nt0 * 8, lane);
 #pragma unroll
     for (int j = 0; j < CH; j++)
 #pragma unroll
@@ -176,8 +176,10 @@ struct MlpVjp {
         sm.G3[row][col] = G3r[e];
         if constexpr (SDE) sm.Gs[row][col] = gz;
       } else {
-        if ((e & 1) == 0) store_split2(G3r[e], G3r[e + 1], &sm.G3[row][col], &sm.G3l[row][col]);
-        if constexpr (SDE) split_store(gz, &sm.Gs[row][col], &sm.Gsl[row][col]);
+        if ((e & 1) == 0)
+          store_split3x2(G3r[e], G3r[e + 1], &sm.G3[row][col], &sm.G3l[row][col],
+                         &sm.G3l2[row][col]);
+        if constexpr (SDE) split_store3(gz, &sm.Gs[row][col], &sm.Gsl[row][col], &sm.Gsl2[row][col]);
       }
       if (G3r[e] != 0.f) atomicAdd(&sm.db2[col], G3r[e]);
       if (SDE && gz != 0.f) atomicAdd(&sm.dbs[col], gz);
@@ -245,100 +247,102 @@ struct MlpVjp {
         }
     } else {
       const int g = lane >> 2, c = lane & 3;
+      const __nv_bfloat16 *const G3p[3] = {&sm.G3[0][0], &sm.G3l[0][0], &sm.G3l2[0][0]};
+      const __nv_bfloat16 *const G2p[3] = {&sm.G2[0][0], &sm.G2l[0][0], &sm.G2l2[0][0]};
       {  // 2. G2 = (G3 W2) * (1 - A2^2), hidden-tile layout
         const int t0 = warp * SH::TPWH, mt = t0 / SH::NTH, nt0 = t0 % SH::NTH;
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        warp_tile_gemm_bt<D, SH::TPWH>(acc, &sm.G3[mt * 16][0], SH::PD, &sm.f.W2[0][0],
-                                       SH::PH, nt0 * 8, lane);
-        warp_tile_gemm_bt<D, SH::TPWH>(acc, &sm.G3l[mt * 16][0], SH::PD, &sm.f.W2[0][0],
-                                       SH::PH, nt0 * 8, lane);
-        if constexpr (SH::WSPLIT)
-          warp_tile_gemm_bt<D, SH::TPWH>(acc, &sm.G3[mt * 16][0], SH::PD, sm.f.w2l(0),
-                                         SH::PH, nt0 * 8, lane);
+        warp_tile_gemm_bt3<D, SH::TPWH>(acc, &sm.G3[mt * 16][0], &sm.G3l[mt * 16][0],
+                                        &sm.G3l2[mt * 16][0], SH::PD, &sm.f.W2[0][0], SH::PH,
+                                        nt0 * 8, lane);
+        auto A2 = sm.f.a2();
+        auto A2l = sm.f.a2l();
+        auto A2l2 = sm.f.a2l2();
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
           for (int hr = 0; hr < 2; hr++) {
             const int row = mt * 16 + g + hr * 8, col = (nt0 + j) * 8 + 2 * c;
-            const float a0 = __bfloat162float(sm.f.a2()[row][col]) +
-                             __bfloat162float(sm.f.a2l()[row][col]);
-            const float a1 = __bfloat162float(sm.f.a2()[row][col + 1]) +
-                             __bfloat162float(sm.f.a2l()[row][col + 1]);
+            const float a0 = __bfloat162float(A2[row][col]) + __bfloat162float(A2l[row][col]) +
+                             __bfloat162float(A2l2[row][col]);
+            const float a1 = __bfloat162float(A2[row][col + 1]) +
+                             __bfloat162float(A2l[row][col + 1]) +
+                             __bfloat162float(A2l2[row][col + 1]);
             const float v0 = acc[j][2 * hr] * (1.f - a0 * a0);
             const float v1 = acc[j][2 * hr + 1] * (1.f - a1 * a1);
-            store_split2(v0, v1, &sm.G2[row][col], &sm.G2l[row][col]);
+            store_split3x2(v0, v1, &sm.G2[row][col], &sm.G2l[row][col], &sm.G2l2[row][col]);
             if (v0 != 0.f) atomicAdd(&sm.db1[col], v0);
             if (v1 != 0.f) atomicAdd(&sm.db1[col + 1], v1);
           }
       }
-      dw_tiles<SH, D, H>(&sm.G3[0][0], &sm.G3l[0][0], SH::PD, &sm.f.a2()[0][0],
-                         &sm.f.a2l()[0][0], SH::PH, SH::OW2, psum, pcomp, warp, lane);
+      {
+        const __nv_bfloat16 *const A2p[3] = {&sm.f.a2()[0][0], &sm.f.a2l()[0][0],
+                                             &sm.f.a2l2()[0][0]};
+        dw_tiles<SH, D, H>(G3p, SH::PD, A2p, SH::PH, SH::OW2, psum, pcomp, warp, lane);
+      }
       __syncthreads();
-      // A2 is dead from here: G1 (hi/lo) takes its storage
+      // A2 is dead from here: G1 (three pieces) takes its storage
       __nv_bfloat16(*G1)[SH::PH] = sm.f.a2();
       __nv_bfloat16(*G1l)[SH::PH] = sm.f.a2l();
+      __nv_bfloat16(*G1l2)[SH::PH] = sm.f.a2l2();
       {  // 3. G1 = (G2 W1) * (1 - A1^2)
         const int t0 = warp * SH::TPWH, mt = t0 / SH::NTH, nt0 = t0 % SH::NTH;
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        warp_tile_gemm_bt<H, SH::TPWH>(acc, &sm.G2[mt * 16][0], SH::PH, &sm.f.W1[0][0],
-                                       SH::PH, nt0 * 8, lane);
-        warp_tile_gemm_bt<H, SH::TPWH>(acc, &sm.G2l[mt * 16][0], SH::PH, &sm.f.W1[0][0],
-                                       SH::PH, nt0 * 8, lane);
-        if constexpr (SH::WSPLIT)
-          warp_tile_gemm_bt<H, SH::TPWH>(acc, &sm.G2[mt * 16][0], SH::PH, sm.f.w1l(0),
-                                         SH::PH, nt0 * 8, lane);
+        warp_tile_gemm_bt3<H, SH::TPWH>(acc, &sm.G2[mt * 16][0], &sm.G2l[mt * 16][0],
+                                        &sm.G2l2[mt * 16][0], SH::PH, &sm.f.W1[0][0], SH::PH,
+                                        nt0 * 8, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
           for (int hr = 0; hr < 2; hr++) {
             const int row = mt * 16 + g + hr * 8, col = (nt0 + j) * 8 + 2 * c;
             const float a0 = __bfloat162float(sm.f.A1[row][col]) +
-                             __bfloat162float(sm.f.A1l[row][col]);
+                             __bfloat162float(sm.f.A1l[row][col]) +
+                             __bfloat162float(sm.f.A1l2[row][col]);
             const float a1 = __bfloat162float(sm.f.A1[row][col + 1]) +
-                             __bfloat162float(sm.f.A1l[row][col + 1]);
+                             __bfloat162float(sm.f.A1l[row][col + 1]) +
+                             __bfloat162float(sm.f.A1l2[row][col + 1]);
             const float v0 = acc[j][2 * hr] * (1.f - a0 * a0);
             const float v1 = acc[j][2 * hr + 1] * (1.f - a1 * a1);
-            store_split2(v0, v1, &G1[row][col], &G1l[row][col]);
+            store_split3x2(v0, v1, &G1[row][col], &G1l[row][col], &G1l2[row][col]);
             if (v0 != 0.f) atomicAdd(&sm.db0[col], v0);
             if (v1 != 0.f) atomicAdd(&sm.db0[col + 1], v1);
           }
       }
-      dw_tiles<SH, H, H>(&sm.G2[0][0], &sm.G2l[0][0], SH::PH, &sm.f.A1[0][0],
-                         &sm.f.A1l[0][0], SH::PH, SH::OW1, psum, pcomp, warp, lane);
+      {
+        const __nv_bfloat16 *const A1p[3] = {&sm.f.A1[0][0], &sm.f.A1l[0][0],
+                                             &sm.f.A1l2[0][0]};
+        dw_tiles<SH, H, H>(G2p, SH::PH, A1p, SH::PH, SH::OW1, psum, pcomp, warp, lane);
+      }
       __syncthreads();
       {  // 4. gY = G1 W0 (+ Gs Ws), owned layout
         const int t0 = warp * SH::TPW, mt = t0 / SH::NT, nt0 = t0 % SH::NT;
         float acc[SH::TPW][4];
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        warp_tile_gemm_bt<H, SH::TPW>(acc, &G1[mt * 16][0], SH::PH, &sm.f.W0[0][0], SH::PW0,
-                                      nt0 * 8, lane);
-        warp_tile_gemm_bt<H, SH::TPW>(acc, &G1l[mt * 16][0], SH::PH, &sm.f.W0[0][0], SH::PW0,
-                                      nt0 * 8, lane);
-        if constexpr (SH::WSPLIT)
-          warp_tile_gemm_bt<H, SH::TPW>(acc, &G1[mt * 16][0], SH::PH, sm.f.w0l(0),
-                                        SH::PW0, nt0 * 8, lane);
-        if constexpr (SDE) {
-          warp_tile_gemm_bt<D, SH::TPW>(acc, &sm.Gs[mt * 16][0], SH::PD, &sm.f.Ws[0][0],
-                                        SH::PD, nt0 * 8, lane);
-          warp_tile_gemm_bt<D, SH::TPW>(acc, &sm.Gsl[mt * 16][0], SH::PD, &sm.f.Ws[0][0],
-                                        SH::PD, nt0 * 8, lane);
-          if constexpr (SH::WSPLIT)
-            warp_tile_gemm_bt<D, SH::TPW>(acc, &sm.Gs[mt * 16][0], SH::PD, sm.f.wsl(0),
-                                          SH::PD, nt0 * 8, lane);
-        }
+        warp_tile_gemm_bt3<H, SH::TPW>(acc, &G1[mt * 16][0], &G1l[mt * 16][0],
+                                       &G1l2[mt * 16][0], SH::PH, &sm.f.W0[0][0], SH::PW0,
+                                       nt0 * 8, lane);
+        if constexpr (SDE)
+          warp_tile_gemm_bt3<D, SH::TPW>(acc, &sm.Gs[mt * 16][0], &sm.Gsl[mt * 16][0],
+                                         &sm.Gsl2[mt * 16][0], SH::PD, &sm.f.Ws[0][0], SH::PD,
+                                         nt0 * 8, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) gY[e] = acc[e >> 2][e & 3];
       }
-      dw_tiles<SH, H, D>(&G1[0][0], &G1l[0][0], SH::PH, &sm.f.X[0][0], &sm.f.Xl[0][0], SH::PD,
-                         SH::OW0, psum, pcomp, warp, lane);
-      if constexpr (SDE)
-        dw_tiles<SH, D, D>(&sm.Gs[0][0], &sm.Gsl[0][0], SH::PD, &sm.f.X[0][0], &sm.f.Xl[0][0],
-                           SH::PD, SH::OWS, psum, pcomp, warp, lane);
+      const __nv_bfloat16 *const Xp[3] = {&sm.f.X[0][0], &sm.f.Xl[0][0], &sm.f.Xl2[0][0]};
+      {
+        const __nv_bfloat16 *const G1p[3] = {&G1[0][0], &G1l[0][0], &G1l2[0][0]};
+        dw_tiles<SH, H, D>(G1p, SH::PH, Xp, SH::PD, SH::OW0, psum, pcomp, warp, lane);
+      }
+      if constexpr (SDE) {
+        const __nv_bfloat16 *const Gsp[3] = {&sm.Gs[0][0], &sm.Gsl[0][0], &sm.Gsl2[0][0]};
+        dw_tiles<SH, D, D>(Gsp, SH::PD, Xp, SH::PD, SH::OWS, psum, pcomp, warp, lane);
+      }
     }
   }
 };

@@ -9,9 +9,11 @@
 // D -> H -> H -> D (tanh hidden, identity output) is three tile products
 //   acc[128 x N] = A[128 x K] W[N x K]^T
 // issued by one thread as tcgen05.mma (kind::f16, BF16 operands in shared
-// memory, FP32 accumulator in TMEM), each operand held as a hi/lo BF16 pair
-// (hi.hi + lo.hi + hi.lo: ~16 significant bits, the smooth field the
-// adaptive controller needs).  Completion is signalled through an mbarrier
+// memory, FP32 accumulator in TMEM): the model's BF16 weights against the
+// activation operand held as three BF16 pieces (24 significant bits; one
+// product per piece), so the products are exact up to the FP32 accumulation
+// and the field is as smooth as an FP32 evaluation -- what the adaptive
+// controller needs.  Completion is signalled through an mbarrier
 // (bounded waits).  TMEM (512 columns x 128 lanes x 32 bit) holds the stage
 // vectors: columns [64 j, 64 j + 64) the stage j = 0..5 of the current step
 // (stage 0 as the unscaled FSAL field value f0, stages 1..5 as k_j = h f_j),
@@ -41,10 +43,11 @@ constexpr uint32_t kAcc = 384;               // first accumulator column
 constexpr uint32_t kWait = 1u << 24;         // polls of a completion barrier
 
 struct TcSmem {
-  __nv_bfloat16 w0h[kH * kD], w0l[kH * kD];  // layer 0: N = H rows, K = D
-  __nv_bfloat16 w1h[kH * kH], w1l[kH * kH];  // layer 1: N = H, K = H
-  __nv_bfloat16 w2h[kD * kH], w2l[kD * kH];  // layer 2: N = D, K = H
-  __nv_bfloat16 ah[kM * kH], al[kM * kH];    // activations: M rows, K <= H
+  __nv_bfloat16 w0[kH * kD];                 // layer 0: N = H rows, K = D (BF16 weights)
+  __nv_bfloat16 w1[kH * kH];                 // layer 1: N = H, K = H
+  __nv_bfloat16 w2[kD * kH];                 // layer 2: N = D, K = H
+  // activations as three BF16 pieces (24 significant bits): M rows, K <= H
+  __nv_bfloat16 ah[kM * kH], al[kM * kH], al2[kM * kH];
   float b0[kH], b1[kH], b2[kD];
   float pa[kSplit][kM], pb[kSplit][kM];      // per-part error norm parts
   int pn[kSplit][kM];                        // per-part NaN flags of y1
@@ -174,27 +177,32 @@ __device__ void control_row(Row &R, float acc, const SolveParams &P) {
   R.dtc = dtn;
 }
 
-// 16 values of this thread's row as hi/lo BF16 into the K-major operand tile
-// (two 16-byte runs per half).
+// 16 values of this thread's row as three BF16 pieces into the K-major
+// operand tiles (two 16-byte runs per piece and half).
 __device__ __forceinline__ void put16(TcSmem &sm, int row, int col, int K, const float (&v)[16]) {
-  uint32_t hi[8], lo[8];
+  uint32_t p0[8], p1[8], p2[8];
 #pragma unroll
   for (int j = 0; j < 8; j++) {
     const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
     const float2 hf = __bfloat1622float2(h);
-    const __nv_bfloat162 l = __floats2bfloat162_rn(v[2 * j] - hf.x, v[2 * j + 1] - hf.y);
-    hi[j] = *reinterpret_cast<const uint32_t *>(&h);
-    lo[j] = *reinterpret_cast<const uint32_t *>(&l);
+    const float r0 = v[2 * j] - hf.x, r1 = v[2 * j + 1] - hf.y;
+    const __nv_bfloat162 m = __floats2bfloat162_rn(r0, r1);
+    const float2 mf = __bfloat1622float2(m);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(r0 - mf.x, r1 - mf.y);
+    p0[j] = *reinterpret_cast<const uint32_t *>(&h);
+    p1[j] = *reinterpret_cast<const uint32_t *>(&m);
+    p2[j] = *reinterpret_cast<const uint32_t *>(&l);
   }
-  unsigned char *bh = reinterpret_cast<unsigned char *>(sm.ah);
-  unsigned char *bl = reinterpret_cast<unsigned char *>(sm.al);
+  unsigned char *b0 = reinterpret_cast<unsigned char *>(sm.ah);
+  unsigned char *b1 = reinterpret_cast<unsigned char *>(sm.al);
+  unsigned char *b2 = reinterpret_cast<unsigned char *>(sm.al2);
 #pragma unroll
   for (int half = 0; half < 2; half++) {
     const uint32_t off = tc::kmajor_offset(row, col + 8 * half, K);
-    *reinterpret_cast<uint4 *>(bh + off) =
-        make_uint4(hi[4 * half], hi[4 * half + 1], hi[4 * half + 2], hi[4 * half + 3]);
-    *reinterpret_cast<uint4 *>(bl + off) =
-        make_uint4(lo[4 * half], lo[4 * half + 1], lo[4 * half + 2], lo[4 * half + 3]);
+    const int q = 4 * half;
+    *reinterpret_cast<uint4 *>(b0 + off) = make_uint4(p0[q], p0[q + 1], p0[q + 2], p0[q + 3]);
+    *reinterpret_cast<uint4 *>(b1 + off) = make_uint4(p1[q], p1[q + 1], p1[q + 2], p1[q + 3]);
+    *reinterpret_cast<uint4 *>(b2 + off) = make_uint4(p2[q], p2[q + 1], p2[q + 2], p2[q + 3]);
   }
 }
 
@@ -213,26 +221,27 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) 
 }
 
 // Everyone's operand writes are visible to the tensor core, then one thread
-// issues acc = A W^T as three hi/lo products per K = 16 slice and commits to
-// the barrier; all wait (bounded).  Returns false on a timeout.
-__device__ __forceinline__ bool layer(TcSmem &sm, uint32_t tmem, const __nv_bfloat16 *wh,
-                                      const __nv_bfloat16 *wl, int K, int N, uint32_t &phase) {
+// issues acc = (A0 + A1 + A2) W^T as three products per K = 16 slice (one per
+// activation piece, all against the BF16 weights) and commits to the
+// barrier; all wait (bounded).  Returns false on a timeout.
+__device__ __forceinline__ bool layer(TcSmem &sm, uint32_t tmem, const __nv_bfloat16 *w, int K,
+                                      int N, uint32_t &phase) {
   tc::fence_async_smem();
   tc::fence_before_sync();
   __syncthreads();
   if (threadIdx.x == 0) {
     tc::fence_after_sync();
     const uint32_t idesc = tc::idesc_bf16_f32(kM, N);
-    const uint32_t ah = tc::smem_u32(sm.ah), al = tc::smem_u32(sm.al);
-    const uint32_t bh = tc::smem_u32(wh), bl = tc::smem_u32(wl);
+    const uint32_t a0 = tc::smem_u32(sm.ah), a1 = tc::smem_u32(sm.al),
+                   a2 = tc::smem_u32(sm.al2);
+    const uint32_t bw = tc::smem_u32(w);
     const uint32_t sbo = uint32_t(K) * 16u;
     for (int kk = 0; kk < K / 16; kk++) {
       const uint32_t o = 256u * kk;
-      const uint64_t dah = tc::smem_desc(ah + o, 128u, sbo), dal = tc::smem_desc(al + o, 128u, sbo);
-      const uint64_t dbh = tc::smem_desc(bh + o, 128u, sbo), dbl = tc::smem_desc(bl + o, 128u, sbo);
-      tc::mma_bf16(tmem + kAcc, dah, dbh, idesc, kk > 0 ? 1u : 0u);
-      tc::mma_bf16(tmem + kAcc, dal, dbh, idesc, 1u);
-      tc::mma_bf16(tmem + kAcc, dah, dbl, idesc, 1u);
+      const uint64_t db = tc::smem_desc(bw + o, 128u, sbo);
+      tc::mma_bf16(tmem + kAcc, tc::smem_desc(a0 + o, 128u, sbo), db, idesc, kk > 0 ? 1u : 0u);
+      tc::mma_bf16(tmem + kAcc, tc::smem_desc(a1 + o, 128u, sbo), db, idesc, 1u);
+      tc::mma_bf16(tmem + kAcc, tc::smem_desc(a2 + o, 128u, sbo), db, idesc, 1u);
     }
     tc::mma_commit(&sm.bar);
   }
@@ -260,11 +269,11 @@ __device__ __forceinline__ void hidden_epilogue(TcSmem &sm, uint32_t lane_addr, 
 // f - b2 is left in accumulator columns [0, D).
 __device__ __forceinline__ bool mlp_eval(TcSmem &sm, uint32_t tmem, uint32_t lane_addr, int row,
                                          int part, uint32_t &phase) {
-  bool ok = layer(sm, tmem, sm.w0h, sm.w0l, kD, kH, phase);
+  bool ok = layer(sm, tmem, sm.w0, kD, kH, phase);
   hidden_epilogue(sm, lane_addr, sm.b0, row, part);
-  ok &= layer(sm, tmem, sm.w1h, sm.w1l, kH, kH, phase);
+  ok &= layer(sm, tmem, sm.w1, kH, kH, phase);
   hidden_epilogue(sm, lane_addr, sm.b1, row, part);
-  ok &= layer(sm, tmem, sm.w2h, sm.w2l, kH, kD, phase);
+  ok &= layer(sm, tmem, sm.w2, kH, kD, phase);
   return ok;
 }
 
@@ -307,21 +316,18 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
   constexpr int OW0 = 0, OB0 = OW0 + kH * kD, OW1 = OB0 + kH, OB1 = OW1 + kH * kH,
                 OW2 = OB1 + kH, OB2 = OW2 + kD * kH;
 
-  // weights as hi/lo BF16 in the K-major operand layout, biases
+  // the BF16 weights in the K-major operand layout, biases
   for (int i = tid; i < kH * kD; i += kThreads) {
     const int n = i / kD, k = i % kD;
-    const uint32_t o = tc::kmajor_offset(n, k, kD) / 2;
-    split_store(W[OW0 + i], sm.w0h + o, sm.w0l + o);
+    sm.w0[tc::kmajor_offset(n, k, kD) / 2] = __float2bfloat16_rn(W[OW0 + i]);
   }
   for (int i = tid; i < kH * kH; i += kThreads) {
     const int n = i / kH, k = i % kH;
-    const uint32_t o = tc::kmajor_offset(n, k, kH) / 2;
-    split_store(W[OW1 + i], sm.w1h + o, sm.w1l + o);
+    sm.w1[tc::kmajor_offset(n, k, kH) / 2] = __float2bfloat16_rn(W[OW1 + i]);
   }
   for (int i = tid; i < kD * kH; i += kThreads) {
     const int n = i / kH, k = i % kH;
-    const uint32_t o = tc::kmajor_offset(n, k, kH) / 2;
-    split_store(W[OW2 + i], sm.w2h + o, sm.w2l + o);
+    sm.w2[tc::kmajor_offset(n, k, kH) / 2] = __float2bfloat16_rn(W[OW2 + i]);
   }
   for (int i = tid; i < kH; i += kThreads) {
     sm.b0[i] = W[OB0 + i];

@@ -105,6 +105,34 @@ __device__ __forceinline__ void split_store(float x, __nv_bfloat16 *hi, __nv_bfl
   if (lo) *lo = __float2bfloat16_rn(x - __bfloat162float(h));
 }
 
+// x ~ p0 + p1 + p2, three BF16 pieces (p0 = bf16(x), p1 = bf16(x - p0),
+// p2 = bf16(x - p0 - p1)): 24 significant bits, so a product with a BF16
+// value is exact up to the FP32 accumulation.  p2 may be null (two pieces).
+__device__ __forceinline__ void split_store3(float x, __nv_bfloat16 *p0, __nv_bfloat16 *p1,
+                                             __nv_bfloat16 *p2) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(x);
+  const float r = x - __bfloat162float(h);
+  const __nv_bfloat16 m = __float2bfloat16_rn(r);
+  *p0 = h;
+  *p1 = m;
+  if (p2) *p2 = __float2bfloat16_rn(r - __bfloat162float(m));
+}
+
+// Two adjacent values as three (or, p2 null, two) BF16x2 pieces.
+__device__ __forceinline__ void store_split3x2(float x0, float x1, __nv_bfloat16 *p0,
+                                               __nv_bfloat16 *p1, __nv_bfloat16 *p2) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+  const float2 hf = __bfloat1622float2(h);
+  const float r0 = x0 - hf.x, r1 = x1 - hf.y;
+  const __nv_bfloat162 m = __floats2bfloat162_rn(r0, r1);
+  *reinterpret_cast<__nv_bfloat162 *>(p0) = h;
+  *reinterpret_cast<__nv_bfloat162 *>(p1) = m;
+  if (p2) {
+    const float2 mf = __bfloat1622float2(m);
+    *reinterpret_cast<__nv_bfloat162 *>(p2) = __floats2bfloat162_rn(r0 - mf.x, r1 - mf.y);
+  }
+}
+
 // Two adjacent values as hi/lo BF16x2 words.
 __device__ __forceinline__ void store_split2(float x0, float x1, __nv_bfloat16 *hi,
                                              __nv_bfloat16 *lo) {
@@ -203,6 +231,122 @@ __device__ __forceinline__ void warp_tile_gemm_tt(float (&acc)[NTW][4], const __
         uint32_t b[2];
         ldsm_bt1(b, S, lds, kk * 16, n0 + j * 8, lane);
         mma_bf16(acc[j], a, b[0], b[1]);
+      }
+    }
+  }
+}
+
+// acc += (A0 + A1 [+ A2])[16 rows, K] W[8 n tiles, K]^T: an activation held as
+// NP BF16 pieces times single-BF16 weights, each W fragment loaded once for
+// all pieces.
+template <int K, int NTW, int NP>
+__device__ __forceinline__ void warp_tile_gemm_p(float (&acc)[NTW][4], const __nv_bfloat16 *A0,
+                                                 const __nv_bfloat16 *A1,
+                                                 const __nv_bfloat16 *A2, int lda,
+                                                 const __nv_bfloat16 *W, int ldw, int lane) {
+  static_assert(NP == 2 || NP == 3, "two or three pieces");
+#pragma unroll
+  for (int kk = 0; kk < K / 16; kk++) {
+    uint32_t a[NP][4];
+    ldsm_a(a[0], A0 + kk * 16, lda, lane);
+    ldsm_a(a[1], A1 + kk * 16, lda, lane);
+    if constexpr (NP == 3) ldsm_a(a[NP - 1], A2 + kk * 16, lda, lane);
+    if constexpr (NTW % 2 == 0) {
+#pragma unroll
+      for (int j = 0; j < NTW; j += 2) {
+        uint32_t b[4];
+        ldsm_b2(b, W + (j * 8) * ldw + kk * 16, ldw, lane);
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+          mma_bf16(acc[j], a[p], b[0], b[1]);
+          mma_bf16(acc[j + 1], a[p], b[2], b[3]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NTW; j++) {
+        uint32_t b[2];
+        ldsm_b1(b, W + (j * 8) * ldw + kk * 16, ldw, lane);
+#pragma unroll
+        for (int p = 0; p < NP; p++) mma_bf16(acc[j], a[p], b[0], b[1]);
+      }
+    }
+  }
+}
+
+// acc[j] += (A0 + A1 + A2)[16 rows, K] B[K, 8 (n0 + 8 j)] with B row-major
+// [k][n] (transposed loads): a cotangent in three pieces times the weights.
+template <int K, int NTW>
+__device__ __forceinline__ void warp_tile_gemm_bt3(float (&acc)[NTW][4],
+                                                   const __nv_bfloat16 *A0,
+                                                   const __nv_bfloat16 *A1,
+                                                   const __nv_bfloat16 *A2, int lda,
+                                                   const __nv_bfloat16 *B, int ldb, int n0,
+                                                   int lane) {
+#pragma unroll
+  for (int kk = 0; kk < K / 16; kk++) {
+    uint32_t a[3][4];
+    ldsm_a(a[0], A0 + kk * 16, lda, lane);
+    ldsm_a(a[1], A1 + kk * 16, lda, lane);
+    ldsm_a(a[2], A2 + kk * 16, lda, lane);
+    if constexpr (NTW % 2 == 0) {
+#pragma unroll
+      for (int j = 0; j < NTW; j += 2) {
+        uint32_t b[4];
+        ldsm_bt2(b, B, ldb, kk * 16, n0 + j * 8, lane);
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+          mma_bf16(acc[j], a[p], b[0], b[1]);
+          mma_bf16(acc[j + 1], a[p], b[2], b[3]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NTW; j++) {
+        uint32_t b[2];
+        ldsm_bt1(b, B, ldb, kk * 16, n0 + j * 8, lane);
+#pragma unroll
+        for (int p = 0; p < 3; p++) mma_bf16(acc[j], a[p], b[0], b[1]);
+      }
+    }
+  }
+}
+
+// acc[j] += (G0 + G1 + G2)^T (S0 + S1 + S2) over M rows (weight-gradient
+// tiles) to 24 significant bits: the six piece products whose size is at
+// least 2^-18 of the leading one (G0S0, G0S1, G1S0, G0S2, G2S0, G1S1).
+template <int M, int NTW>
+__device__ __forceinline__ void warp_tile_gemm_tt3(float (&acc)[NTW][4],
+                                                   const __nv_bfloat16 *const (&G)[3], int ldg,
+                                                   int o0, const __nv_bfloat16 *const (&S)[3],
+                                                   int lds, int n0, int lane) {
+  constexpr int PAIRS[6][2] = {{0, 0}, {0, 1}, {1, 0}, {0, 2}, {2, 0}, {1, 1}};
+#pragma unroll
+  for (int kk = 0; kk < M / 16; kk++) {
+    uint32_t a[3][4];
+#pragma unroll
+    for (int p = 0; p < 3; p++) ldsm_at(a[p], G[p], ldg, kk * 16, o0, lane);
+    if constexpr (NTW % 2 == 0) {
+#pragma unroll
+      for (int j = 0; j < NTW; j += 2) {
+        uint32_t b[3][4];
+#pragma unroll
+        for (int p = 0; p < 3; p++) ldsm_bt2(b[p], S[p], lds, kk * 16, n0 + j * 8, lane);
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+          mma_bf16(acc[j], a[PAIRS[q][0]], b[PAIRS[q][1]][0], b[PAIRS[q][1]][1]);
+          mma_bf16(acc[j + 1], a[PAIRS[q][0]], b[PAIRS[q][1]][2], b[PAIRS[q][1]][3]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NTW; j++) {
+        uint32_t b[3][2];
+#pragma unroll
+        for (int p = 0; p < 3; p++) ldsm_bt1(b[p], S[p], lds, kk * 16, n0 + j * 8, lane);
+#pragma unroll
+        for (int q = 0; q < 6; q++)
+          mma_bf16(acc[j], a[PAIRS[q][0]], b[PAIRS[q][1]][0], b[PAIRS[q][1]][1]);
       }
     }
   }

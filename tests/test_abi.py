@@ -359,3 +359,30 @@ def test_sde_extended_output_scope():
                   dim=4, dtype=torch.float32, max_steps=64, n_ts=0)
     with pytest.raises(_lib.GbdxError, match="Ornstein-Uhlenbeck SDE"):
         _lib.Problem(f)
+
+
+def test_autotune_cache_round_trip(tmp_path, monkeypatch):
+    # GBDX_AUTOTUNE_CACHE: choices written by one process are read by the next
+    # (keyed by GPU name, problem and batch class); other GPUs' entries and
+    # a corrupt file are ignored.
+    from diffrax_gb300 import _tune
+    fields = dfx.lower(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(),
+                       dfx.PIDController(rtol=1e-6, atol=1e-9), dfx.SaveAt(t1=True), dim=2,
+                       dtype=torch.float32, max_steps=4096, n_ts=0)
+    key = _tune._key(fields, 65536)
+    path = str(tmp_path / "tune.json")
+    monkeypatch.setattr(_tune, "_TUNED", {key: ("fused", 128, 4)})
+    _tune.save_cache(path, "GPU-A")
+    monkeypatch.setattr(_tune, "_TUNED", {})
+    assert _tune.load_cache(path, "GPU-B") == 0
+    assert _tune.load_cache(path, "GPU-A") == 1
+    assert _tune._TUNED[key] == ("fused", 128, 4)
+    # a second problem merges into the same file
+    f2 = dict(fields, rtol=1e-5)
+    k2 = _tune._key(f2, 1000)
+    _tune._TUNED[k2] = ("fused", 64, 2)
+    _tune.save_cache(path, "GPU-A")
+    monkeypatch.setattr(_tune, "_TUNED", {})
+    assert _tune.load_cache(path, "GPU-A") == 2
+    open(path, "w").write("{not json")
+    assert _tune.load_cache(path, "GPU-A") == 0

@@ -46,7 +46,13 @@ def grad_pair(field, solver, ctrl, saveat, t0, t1, dt0, y0, args, dtype, adjoint
         r = O.grad_recursive(d, t0, t1, dt0, y0, G, args=args, ts=ts, nthreads=8)
         same = sol.stats["num_steps"].cpu().numpy() == r["stats"][:, 0]
     ga = a_t.grad.double().cpu().numpy()
-    gr = r["grad_args"] if ga.ndim == 2 else r["grad_args"].sum(axis=0)
+    if ga.ndim == 2:
+        gr = r["grad_args"]
+    else:
+        # shared args: the batch sum; ra_scale is the sum of the per-trajectory
+        # magnitudes, the scale of the sum's rounding
+        gr = r["grad_args"].sum(axis=0)
+        sol.ra_scale = np.abs(r["grad_args"]).sum(axis=0)
     # same: trajectories whose (backward) step counts equal the oracle's
     return y0_t.grad.double().cpu().numpy(), ga, r["grad_y0"], gr, same, sol
 
@@ -67,14 +73,16 @@ def lv_case(B, seed):
 @pytest.mark.parametrize("adjoint", [dfx.RecursiveCheckpointAdjoint(), dfx.BacksolveAdjoint()])
 @pytest.mark.parametrize("solver", ["tsit5", "dopri5", "heun"])
 def test_lotka_volterra_grads_fp64_match_oracle(solver, adjoint):
-    # Per-trajectory args, PID(1e-8, 1e-8), saves at 5 times and t1.
+    # Per-trajectory args, PID(1e-8, 1e-8) (1e-6 for the second-order Heun),
+    # saves at 5 times and t1.
     B = 256
     y0, args = lv_case(B, 3)
     ts = np.array([1.0, 4.0, 7.5, 12.0, 19.0])
     saveat = dfx.SaveAt(ts=ts, t1=True)
     G = np.random.default_rng(4).standard_normal((B, 6, 2))
+    tol = 1e-6 if solver == "heun" else 1e-8
     gy, ga, ry, ra, same, sol = grad_pair(
-        dfx.LotkaVolterra(), SOLVERS[solver], dfx.PIDController(rtol=1e-8, atol=1e-8), saveat,
+        dfx.LotkaVolterra(), SOLVERS[solver], dfx.PIDController(rtol=tol, atol=tol), saveat,
         0.0, 20.0, 0.1, y0, args, torch.float64, adjoint, G)
     e_y, e_a = row_rel(gy, ry), row_rel(ga, ra)
     print(f"LV FP64 {solver} {type(adjoint).__name__}: same steps {same.mean():.3f}, "
@@ -115,24 +123,29 @@ def test_van_der_pol_shared_args_constant_steps(solver, dtype):
         dfx.VanDerPol(), SOLVERS[solver], dfx.ConstantStepSize(), dfx.SaveAt(t1=True), 0.0,
         3.0, 0.01, y0, args, dtype, dfx.RecursiveCheckpointAdjoint(), G)
     assert same.all()
-    e_y = row_rel(gy, ry).max()
-    e_a = float(np.abs(ga - ra).max() / np.abs(ra).max())
+    # FP64: per trajectory; FP32: against the batch's largest gradient (with
+    # random cotangents a few trajectories' dL/dy0 nearly cancel, and FP32
+    # rounding is then large relative to them)
+    e_y = row_rel(gy, ry).max() if dtype == torch.float64 else float(
+        np.abs(gy - ry).max() / np.abs(ry).max())
+    e_a = float((np.abs(ga - ra) / sol.ra_scale).max())
     print(f"VdP shared mu {solver} {dtype}: dL/dy0 {e_y:.2e}, dL/dmu {e_a:.2e}")
-    tol = 1e-10 if dtype == torch.float64 else 2e-4
+    tol = 1e-10 if dtype == torch.float64 else 2e-5
     assert e_y < tol and e_a < tol
 
 
 def test_van_der_pol_reverse_time_and_saves():
     # Integration from t0 = 4 back to t1 = 0 with saves on the way (the
-    # direction flip of _integrate.py:1157-1176), per-trajectory mu.
+    # direction flip of _integrate.py:1157-1176), per-trajectory mu.  In
+    # reverse time the limit cycle repels: the states start inside it.
     B = 128
     rng = np.random.default_rng(8)
-    y0 = rng.uniform(-2, 2, (B, 2))
+    y0 = rng.uniform(-1, 1, (B, 2))
     args = np.exp(rng.uniform(np.log(0.3), np.log(3.0), (B, 1)))
     saveat = dfx.SaveAt(ts=np.array([3.5, 2.0, 0.7]), t0=True, t1=True)
     G = rng.standard_normal((B, 5, 2))
     gy, ga, ry, ra, same, sol = grad_pair(
-        dfx.VanDerPol(), dfx.Dopri5(), dfx.PIDController(rtol=1e-9, atol=1e-9), saveat, 4.0,
+        dfx.VanDerPol(), dfx.Dopri5(), dfx.PIDController(rtol=1e-8, atol=1e-8), saveat, 4.0,
         0.0, None, y0, args, torch.float64, dfx.RecursiveCheckpointAdjoint(), G)
     e_y, e_a = row_rel(gy, ry), row_rel(ga, ra)
     assert same.mean() >= 0.9
@@ -157,7 +170,7 @@ def test_ou_sde_grads_match_oracle_on_the_same_path(solver):
         y0, args, torch.float32, dfx.RecursiveCheckpointAdjoint(), G, terms=terms)
     assert same.all()
     e_y = row_rel(gy, ry).max()
-    e_a = float(np.abs(ga - ra).max() / np.abs(ra).max())
+    e_a = float((np.abs(ga - ra) / sol.ra_scale).max())
     print(f"OU SDE {solver}: dL/dy0 {e_y:.2e}, dL/d(theta, mu, sigma) {e_a:.2e}")
     assert e_y < 1e-5 and e_a < 1e-4
 

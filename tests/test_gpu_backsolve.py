@@ -36,7 +36,9 @@ def mlp_params(widths, seed, bias_scale=0.1, bf16_weights=False):
 
 
 def backsolve_case(widths, solver, controller, ts, B, precision, seed=0, seminorm=False,
-                   t1=1.0, dt0=None, bf16_weights=False, grad_ys=None, y0=None, kernel="fused"):
+                   t1=1.0, dt0=None, bf16_weights=True, grad_ys=None, y0=None, kernel="fused"):
+    """The model's weights are BF16 values (bf16_weights); the FP32 modes and
+    the oracle see the same values."""
     dev = torch.device("cuda")
     rng = np.random.default_rng(seed + 100)
     D = widths[0]

@@ -50,8 +50,9 @@ def test_tc_matches_oracle_and_rowtile():
     print(f"tc: rel err vs FP64 oracle median {np.median(err):.2e} max {err.max():.2e}; "
           f"steps {sol.stats['num_steps'].float().mean():.2f} (row tile "
           f"{ref.stats['num_steps'].float().mean():.2f}, oracle {r['stats'][:, 0].mean():.2f})")
-    # the same hi/lo BF16 field as the row-tile kernel: FP32-state accuracy
-    assert err.max() < 1e-4
+    # BF16 weights and three-piece activations, as the row-tile kernel:
+    # FP32-state accuracy
+    assert err.max() < 2e-5
     assert np.array_equal(sol.ts.cpu().numpy(), r["ts"])
     steps = sol.stats["num_steps"].cpu().numpy()
     assert steps.mean() < 2.5 * r["stats"][:, 0].mean()
