@@ -320,12 +320,13 @@ def profile_saveat_steps(dev, n):
 def profile_neural(dev, which, B, n):
     """n fused solves of a neural workload at batch B, for ncu: the forward of
     the neural ODE (64-128-128-64, row-tile or tcgen05 kernel), its forward +
-    RecursiveCheckpointAdjoint backward, the wide neural ODE forward or the
-    neural SDE forward."""
+    RecursiveCheckpointAdjoint backward, the wide neural ODE forward, or the
+    neural SDE forward (and its forward + RecursiveCheckpointAdjoint
+    backward)."""
     import torch
     import diffrax_gb300 as dfx
     from diffrax_gb300._integrate import Lowered
-    wide, sde = which == "neural_ode_wide", which == "neural_sde"
+    wide, sde = which == "neural_ode_wide", which in ("neural_sde", "neural_sde_grad")
     widths = [64, 256, 256, 64] if wide else ([32, 64, 64, 32] if sde else [64, 128, 128, 64])
     D = widths[0]
     Ws, bs = _mlp_np(widths, 21)
@@ -335,8 +336,7 @@ def profile_neural(dev, which, B, n):
                          [torch.tensor(b, device=dev) for b in bs])
     if sde:
         rng = np.random.default_rng(25)
-        Wsig = torch.tensor((rng.standard_normal((D, D)) / np.sqrt(D)).astype(np.float32),
-                            device=dev)
+        Wsig = torch.tensor(_bf16_values(rng.standard_normal((D, D)) / np.sqrt(D)), device=dev)
         bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (D,), key=23)
         terms = dfx.MultiTerm(dfx.ODETerm(field), dfx.ControlTerm(
             dfx.TanhDiagonalDiffusion(Wsig, torch.zeros(D, device=dev)), bm))
@@ -345,9 +345,10 @@ def profile_neural(dev, which, B, n):
         terms = dfx.ODETerm(field)
         solver, ctrl, dt0 = dfx.Tsit5(), dfx.PIDController(rtol=1e-5, atol=1e-7), None
         saveat = dfx.SaveAt(ts=np.linspace(0, 1, 32)) if wide else dfx.SaveAt(t1=True)
-    grad = which == "neural_ode_grad"
-    low = Lowered(terms, solver, 0.0, 1.0, dt0, y0, None, saveat, ctrl,
-                  dfx.RecursiveCheckpointAdjoint(checkpoints=64), 4096,
+    grad = which in ("neural_ode_grad", "neural_sde_grad")
+    adjoint = dfx.RecursiveCheckpointAdjoint() if sde else \
+        dfx.RecursiveCheckpointAdjoint(checkpoints=64)
+    low = Lowered(terms, solver, 0.0, 1.0, dt0, y0, None, saveat, ctrl, adjoint, 4096,
                   "tc" if which == "neural_ode_tc" else "fused", 0, 0, want_grad=grad)
     for _ in range(n):
         if grad:
@@ -911,7 +912,7 @@ def main():
     ap.add_argument("--profile", default=None,
                     choices=["fused", "plain", "backsolve", "backsolve_seminorm", "neural_ode",
                              "neural_ode_tc", "neural_ode_grad", "neural_ode_wide",
-                             "neural_sde", "saveat_steps"],
+                             "neural_sde", "neural_sde_grad", "saveat_steps"],
                     help="run warmup + steps eager solves of one kernel only (for ncu); "
                          "backsolve*: forward + backward of the wide neural ODE at --batch")
     args = ap.parse_args()

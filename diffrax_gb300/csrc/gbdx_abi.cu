@@ -78,7 +78,8 @@ namespace {
 // Workspace of one solve: the work counter, the work order, and (recursive
 // adjoint) the tape the backward reads plus its scratch.
 struct WsLayout {
-  size_t order, tape_t, tape_y, tape_n, tape_s, scratch, psum, pcomp, total;
+  size_t order, ffrag, tape_t, tape_y, tape_n, tape_s, scratch, psum, pcomp, total;
+  bool has_ffrag;  // width-256 MLP forward: W0 / W2 fragments at ffrag
   size_t frag, rec, ath;  // backsolve: B fragments, stage records, a_theta
   int seg_max, n_cta;
   bool track;
@@ -98,6 +99,11 @@ int ws_layout(const gbdx_problem *p, int64_t batch, WsLayout *L) {
   L->order = off;
   if (d.kernel != GBDX_KERNEL_PLAIN && d.schedule != GBDX_SCHED_INDEX)
     off += up256(gbdx::schedule_workspace_bytes(int64_t(B)));
+  // The width-256 MLP integrator reads W0 and W2 as BF16 mma fragments.
+  L->ffrag = off;
+  L->has_ffrag = p->mlp && d.kernel != GBDX_KERNEL_TC && d.mlp_widths[1] >= 256 &&
+                 d.mlp_precision != GBDX_MLP_FP32;
+  if (L->has_ffrag) off += 2 * up256(size_t(d.dim) * d.mlp_widths[1] * 2);
   L->tape_t = L->tape_y = L->tape_n = L->tape_s = L->scratch = L->psum = L->pcomp = off;
   L->seg_max = 0;
   L->n_cta = 0;
@@ -754,6 +760,21 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
     P.saves_prefilled = 1;
   }
 
+  if (L.has_ffrag) {
+    // W0 (B[k][n] = W0[n][k], K = D, N = H) and W2 (K = H, N = D) as BF16
+    // mma fragments for this launch
+    const int D = d.dim, H = d.mlp_widths[1];
+    const float *W = static_cast<const float *>(params);
+    uint2 *f0 = reinterpret_cast<uint2 *>(static_cast<char *>(workspace) + L.ffrag);
+    uint2 *f2 = reinterpret_cast<uint2 *>(static_cast<char *>(workspace) + L.ffrag +
+                                          up256(size_t(D) * H * 2));
+    cudaError_t e = gbdx::launch_frag_prep(W, D, D, H, 1, f0, s);
+    if (e == cudaSuccess)
+      e = gbdx::launch_frag_prep(W + size_t(H) * D + H + size_t(H) * H + H, H, H, D, 1, f2, s);
+    if (e != cudaSuccess) return cuda_fail(e, "weight fragments");
+    P.w0f = f0;
+    P.w2f = f2;
+  }
   gbdx::LaunchCfg cfg;
   cfg.kernel = d.kernel == GBDX_KERNEL_PLAIN ? GBDX_KERNEL_PLAIN : GBDX_KERNEL_FUSED;
   cfg.block = problem->mlp ? problem->mlp_block : (d.block_threads > 0 ? d.block_threads : 64);

@@ -14,8 +14,8 @@
 // as the forward kernel does; each row walks its own segments and refills
 // from the work counter after its last one.  Per RK stage the tile evaluates
 // f and the VJP a^T df/dy as chains of tensor-core products of the BF16
-// weights with hi/lo BF16 operands (or FP32 CUDA-core products in the parity
-// mode) and records, per
+// weights with three-piece BF16 operands (24 significant bits; or FP32
+// CUDA-core products in the parity mode) and records, per
 // row, the vector pairs whose outer products are -a^T df/dtheta:
 //   (dz0, x) for W0/b0, (dz1, h1) for W1/b1, (a, h2) for W2/b2,
 // where x is the stage input, h1, h2 the hidden activations and dz0, dz1 the
@@ -98,14 +98,14 @@ struct BsWeights<SH, true> {
 template <class SH, bool PRECISE>
 struct BsSmem;
 
-// Stage operands (hi/lo BF16): X the stage input, G its cotangent a, R1 h1
-// then dz0, R2 h2 then dz1.
+// Stage operands as three BF16 pieces each (24 significant bits): X the
+// stage input, G its cotangent a, R1 h1 then dz0, R2 h2 then dz1.
 template <class SH>
 struct BsAct {
-  __nv_bfloat16 X[SH::M][SH::PD], Xl[SH::M][SH::PD];
-  __nv_bfloat16 G[SH::M][SH::PD], Gl[SH::M][SH::PD];
-  __nv_bfloat16 R1[SH::M][SH::PH], R1l[SH::M][SH::PH];
-  __nv_bfloat16 R2[SH::M][SH::PH], R2l[SH::M][SH::PH];
+  __nv_bfloat16 X[SH::M][SH::PD], Xl[SH::M][SH::PD], Xl2[SH::M][SH::PD];
+  __nv_bfloat16 G[SH::M][SH::PD], Gl[SH::M][SH::PD], Gl2[SH::M][SH::PD];
+  __nv_bfloat16 R1[SH::M][SH::PH], R1l[SH::M][SH::PH], R1l2[SH::M][SH::PH];
+  __nv_bfloat16 R2[SH::M][SH::PH], R2l[SH::M][SH::PH], R2l2[SH::M][SH::PH];
 };
 // Operands of the tensor-core parameter pass of one row and layer:
 // o-side vectors U0 = -h u0, A2 = sum_j b_j du_j, A3 = sum_j e_j du_j and the
@@ -147,26 +147,6 @@ struct BsSmem<SH, true> {
   BsRows<SH::M> rows;
 };
 
-// acc[j] += (Ah + Al)[16 rows, K] B[K, 8 (nt0 + j)] where the B fragments of
-// a fixed matrix are pre-arranged in global memory as [n8 tile][k16 tile][lane].
-template <int K, int NTW>
-__device__ __forceinline__ void gemm_gfrag(float (&acc)[NTW][4], const __nv_bfloat16 *Ah,
-                                           const __nv_bfloat16 *Al, int lda, const uint2 *frag,
-                                           int nt0, int lane) {
-#pragma unroll 4
-  for (int kk = 0; kk < K / 16; kk++) {
-    uint32_t ah[4], al[4];
-    ldsm_a(ah, Ah + kk * 16, lda, lane);
-    ldsm_a(al, Al + kk * 16, lda, lane);
-#pragma unroll
-    for (int j = 0; j < NTW; j++) {
-      const uint2 b = __ldg(frag + (size_t((nt0 + j) * (K / 16) + kk) << 5) + lane);
-      mma_bf16(acc[j], ah, b.x, b.y);
-      mma_bf16(acc[j], al, b.x, b.y);
-    }
-  }
-}
-
 template <class SH, bool PRECISE>
 struct BsField {
   using Sm = BsSmem<SH, PRECISE>;
@@ -206,34 +186,32 @@ struct BsField {
         sm.a.G[row][col] = A[e];
         sm.a.G[row][col + 1] = A[e + 1];
       } else {
-        store_split2(Y[e], Y[e + 1], &sm.a.X[row][col], &sm.a.Xl[row][col]);
-        store_split2(A[e], A[e + 1], &sm.a.G[row][col], &sm.a.Gl[row][col]);
+        store_split3x2(Y[e], Y[e + 1], &sm.a.X[row][col], &sm.a.Xl[row][col],
+                       &sm.a.Xl2[row][col]);
+        store_split3x2(A[e], A[e + 1], &sm.a.G[row][col], &sm.a.Gl[row][col],
+                       &sm.a.Gl2[row][col]);
       }
       *reinterpret_cast<float2 *>(rec + row * REC + SH::RX + col) = make_float2(Y[e], Y[e + 1]);
       *reinterpret_cast<float2 *>(rec + row * REC + SH::RG + col) = make_float2(A[e], A[e + 1]);
     }
   }
 
-  // acc += (Ah + Al) (Wh + Wl)^T over K (no lo*lo term), W row-major [n][k].
+  // acc += (A0 + A1 + A2) W^T over K, W the BF16 weights row-major [n][k].
   template <int K, int NTW>
-  __device__ static __forceinline__ void fwd_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *Ah,
-                                                  const __nv_bfloat16 *Al, int lda,
-                                                  const __nv_bfloat16 *Wh,
-                                                  const __nv_bfloat16 *Wl, int ldw, int lane) {
-    warp_tile_gemm<K, NTW>(acc, Ah, lda, Wh, ldw, lane);
-    warp_tile_gemm<K, NTW>(acc, Al, lda, Wh, ldw, lane);
-    if (Wl) warp_tile_gemm<K, NTW>(acc, Ah, lda, Wl, ldw, lane);
+  __device__ static __forceinline__ void fwd_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *A0,
+                                                  const __nv_bfloat16 *A1,
+                                                  const __nv_bfloat16 *A2, int lda,
+                                                  const __nv_bfloat16 *W, int ldw, int lane) {
+    warp_tile_gemm_p<K, NTW, 3>(acc, A0, A1, A2, lda, W, ldw, lane);
   }
-  // acc += (Ah + Al) (Wh + Wl) over K, W row-major [k][n] (transposed loads).
+  // acc += (A0 + A1 + A2) W over K, W row-major [k][n] (transposed loads).
   template <int K, int NTW>
-  __device__ static __forceinline__ void vjp_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *Ah,
-                                                  const __nv_bfloat16 *Al, int lda,
-                                                  const __nv_bfloat16 *Wh,
-                                                  const __nv_bfloat16 *Wl, int ldw, int n0,
+  __device__ static __forceinline__ void vjp_gemm(float (&acc)[NTW][4], const __nv_bfloat16 *A0,
+                                                  const __nv_bfloat16 *A1,
+                                                  const __nv_bfloat16 *A2, int lda,
+                                                  const __nv_bfloat16 *W, int ldw, int n0,
                                                   int lane) {
-    warp_tile_gemm_bt<K, NTW>(acc, Ah, lda, Wh, ldw, n0, lane);
-    warp_tile_gemm_bt<K, NTW>(acc, Al, lda, Wh, ldw, n0, lane);
-    if (Wl) warp_tile_gemm_bt<K, NTW>(acc, Ah, lda, Wl, ldw, n0, lane);
+    warp_tile_gemm_bt3<K, NTW>(acc, A0, A1, A2, lda, W, ldw, n0, lane);
   }
 
   // Hidden-tile epilogue helper: write v to R (split) and to the record.
@@ -245,9 +223,9 @@ struct BsField {
       R[row][col + 1] = v1;
     } else {
       if (which == 1)
-        store_split2(v0, v1, &sm.a.R1[row][col], &sm.a.R1l[row][col]);
+        store_split3x2(v0, v1, &sm.a.R1[row][col], &sm.a.R1l[row][col], &sm.a.R1l2[row][col]);
       else
-        store_split2(v0, v1, &sm.a.R2[row][col], &sm.a.R2l[row][col]);
+        store_split3x2(v0, v1, &sm.a.R2[row][col], &sm.a.R2l[row][col], &sm.a.R2l2[row][col]);
     }
     *reinterpret_cast<float2 *>(rec + row * REC + roff + col) = make_float2(v0, v1);
   }
@@ -325,11 +303,12 @@ struct BsField {
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         if constexpr (SH::GFRAG)
-          gemm_gfrag<D, SH::TPWH>(acc, &sm.a.X[mth * 16][0], &sm.a.Xl[mth * 16][0], SH::PD, Q.w0f,
-                                  nth0, lane);
+          gemm_gfrag_p<D, SH::TPWH, 3>(acc, &sm.a.X[mth * 16][0], &sm.a.Xl[mth * 16][0],
+                                       &sm.a.Xl2[mth * 16][0], SH::PD, Q.w0f, nth0, lane);
         else
-          fwd_gemm<D, SH::TPWH>(acc, &sm.a.X[mth * 16][0], &sm.a.Xl[mth * 16][0], SH::PD,
-                                &sm.W0[nth0 * 8][0], nullptr, SH::PD, lane);
+          fwd_gemm<D, SH::TPWH>(acc, &sm.a.X[mth * 16][0], &sm.a.Xl[mth * 16][0],
+                                &sm.a.Xl2[mth * 16][0], SH::PD, &sm.W0[nth0 * 8][0], SH::PD,
+                                lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
           const int col = (nth0 + j) * 8 + 2 * c, r0 = mth * 16 + g;
@@ -345,8 +324,9 @@ struct BsField {
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        fwd_gemm<H, SH::TPWH>(acc, &sm.a.R1[mth * 16][0], &sm.a.R1l[mth * 16][0], SH::PH,
-                              &sm.W1[nth0 * 8][0], nullptr, SH::PH, lane);
+        fwd_gemm<H, SH::TPWH>(acc, &sm.a.R1[mth * 16][0], &sm.a.R1l[mth * 16][0],
+                              &sm.a.R1l2[mth * 16][0], SH::PH, &sm.W1[nth0 * 8][0], SH::PH,
+                              lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
           const int col = (nth0 + j) * 8 + 2 * c, r0 = mth * 16 + g;
@@ -363,11 +343,12 @@ struct BsField {
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         if constexpr (SH::GFRAG)
-          gemm_gfrag<H, SH::TPW>(acc, &sm.a.R2[mto * 16][0], &sm.a.R2l[mto * 16][0], SH::PH, Q.w2f,
-                                 nto0, lane);
+          gemm_gfrag_p<H, SH::TPW, 3>(acc, &sm.a.R2[mto * 16][0], &sm.a.R2l[mto * 16][0],
+                                      &sm.a.R2l2[mto * 16][0], SH::PH, Q.w2f, nto0, lane);
         else
-          fwd_gemm<H, SH::TPW>(acc, &sm.a.R2[mto * 16][0], &sm.a.R2l[mto * 16][0], SH::PH,
-                               &sm.W2[nto0 * 8][0], nullptr, SH::PH, lane);
+          fwd_gemm<H, SH::TPW>(acc, &sm.a.R2[mto * 16][0], &sm.a.R2l[mto * 16][0],
+                               &sm.a.R2l2[mto * 16][0], SH::PH, &sm.W2[nto0 * 8][0], SH::PH,
+                               lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) {
           int row, col;
@@ -381,19 +362,23 @@ struct BsField {
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         if constexpr (SH::GFRAG)
-          gemm_gfrag<D, SH::TPWH>(acc, &sm.a.G[mth * 16][0], &sm.a.Gl[mth * 16][0], SH::PD, Q.w2v,
-                                  nth0, lane);
+          gemm_gfrag_p<D, SH::TPWH, 3>(acc, &sm.a.G[mth * 16][0], &sm.a.Gl[mth * 16][0],
+                                       &sm.a.Gl2[mth * 16][0], SH::PD, Q.w2v, nth0, lane);
         else
-          vjp_gemm<D, SH::TPWH>(acc, &sm.a.G[mth * 16][0], &sm.a.Gl[mth * 16][0], SH::PD,
-                                &sm.W2[0][0], nullptr, SH::PH, nth0 * 8, lane);
+          vjp_gemm<D, SH::TPWH>(acc, &sm.a.G[mth * 16][0], &sm.a.Gl[mth * 16][0],
+                                &sm.a.Gl2[mth * 16][0], SH::PD, &sm.W2[0][0], SH::PH, nth0 * 8,
+                                lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
           for (int hr = 0; hr < 2; hr++) {
             const int row = mth * 16 + g + hr * 8, col = (nth0 + j) * 8 + 2 * c;
-            const float a0 = __bfloat162float(sm.a.R2[row][col]) + __bfloat162float(sm.a.R2l[row][col]);
-            const float a1 =
-                __bfloat162float(sm.a.R2[row][col + 1]) + __bfloat162float(sm.a.R2l[row][col + 1]);
+            const float a0 = __bfloat162float(sm.a.R2[row][col]) +
+                             __bfloat162float(sm.a.R2l[row][col]) +
+                             __bfloat162float(sm.a.R2l2[row][col]);
+            const float a1 = __bfloat162float(sm.a.R2[row][col + 1]) +
+                             __bfloat162float(sm.a.R2l[row][col + 1]) +
+                             __bfloat162float(sm.a.R2l2[row][col + 1]);
             put_hidden(sm, 2, row, col, acc[j][2 * hr] * (1.f - a0 * a0),
                        acc[j][2 * hr + 1] * (1.f - a1 * a1), rec, SH::RZ1);
           }
@@ -403,16 +388,20 @@ struct BsField {
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        vjp_gemm<H, SH::TPWH>(acc, &sm.a.R2[mth * 16][0], &sm.a.R2l[mth * 16][0], SH::PH,
-                              &sm.W1[0][0], nullptr, SH::PH, nth0 * 8, lane);
+        vjp_gemm<H, SH::TPWH>(acc, &sm.a.R2[mth * 16][0], &sm.a.R2l[mth * 16][0],
+                              &sm.a.R2l2[mth * 16][0], SH::PH, &sm.W1[0][0], SH::PH, nth0 * 8,
+                              lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++)
 #pragma unroll
           for (int hr = 0; hr < 2; hr++) {
             const int row = mth * 16 + g + hr * 8, col = (nth0 + j) * 8 + 2 * c;
-            const float a0 = __bfloat162float(sm.a.R1[row][col]) + __bfloat162float(sm.a.R1l[row][col]);
-            const float a1 =
-                __bfloat162float(sm.a.R1[row][col + 1]) + __bfloat162float(sm.a.R1l[row][col + 1]);
+            const float a0 = __bfloat162float(sm.a.R1[row][col]) +
+                             __bfloat162float(sm.a.R1l[row][col]) +
+                             __bfloat162float(sm.a.R1l2[row][col]);
+            const float a1 = __bfloat162float(sm.a.R1[row][col + 1]) +
+                             __bfloat162float(sm.a.R1l[row][col + 1]) +
+                             __bfloat162float(sm.a.R1l2[row][col + 1]);
             put_hidden(sm, 1, row, col, acc[j][2 * hr] * (1.f - a0 * a0),
                        acc[j][2 * hr + 1] * (1.f - a1 * a1), rec, SH::RZ0);
           }
@@ -423,11 +412,12 @@ struct BsField {
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         if constexpr (SH::GFRAG)
-          gemm_gfrag<H, SH::TPW>(acc, &sm.a.R1[mto * 16][0], &sm.a.R1l[mto * 16][0], SH::PH, Q.w0v,
-                                 nto0, lane);
+          gemm_gfrag_p<H, SH::TPW, 3>(acc, &sm.a.R1[mto * 16][0], &sm.a.R1l[mto * 16][0],
+                                      &sm.a.R1l2[mto * 16][0], SH::PH, Q.w0v, nto0, lane);
         else
-          vjp_gemm<H, SH::TPW>(acc, &sm.a.R1[mto * 16][0], &sm.a.R1l[mto * 16][0], SH::PH,
-                               &sm.W0[0][0], nullptr, SH::PD, nto0 * 8, lane);
+          vjp_gemm<H, SH::TPW>(acc, &sm.a.R1[mto * 16][0], &sm.a.R1l[mto * 16][0],
+                               &sm.a.R1l2[mto * 16][0], SH::PH, &sm.W0[0][0], SH::PD, nto0 * 8,
+                               lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) GY[e] = acc[e >> 2][e & 3];
       }

@@ -489,6 +489,7 @@ struct SolveParams {
   const int32_t *order;       // optional work order: queue slot -> trajectory
   // MLP fields and SDEs
   const float *mlp;           // flat FP32 parameters (W0, b0, W1, b1, W2, b2, Ws, bs)
+  const uint2 *w0f, *w2f;     // width 256: W0 and W2 as BF16 mma B fragments (workspace)
   uint64_t seed;              // Brownian generator seed
   double vbt_t0, vbt_len, vbt_tol_unit;
   double vbt_inv_len;         // 1 / vbt_len

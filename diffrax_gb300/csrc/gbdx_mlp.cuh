@@ -37,19 +37,18 @@ struct MlpShape {
   static constexpr int D = D_, H = H_;
   static constexpr int M = (H_ >= 256) ? 16 : 32;  // rows per CTA
   static constexpr int THREADS = 256, WARPS = 8;
-  // Tight layout at width 256: the layer-1 output overwrites the layer-0
-  // activations (A2 aliases A1) and W0 is unpadded, so BF16 weights plus hi/lo
+  // Width 256: W0 and W2 are read as pre-arranged BF16 mma B fragments from
+  // global memory (L2-resident, 32 KB each), so that W1 and the three-piece
   // activations fit the 227 KB of shared memory.
-  static constexpr bool TIGHT = H_ >= 256;
+  static constexpr bool GFRAG = H_ >= 256;
   static constexpr int PD = D + 8, PH = H + 8;      // padded smem row strides (bf16)
-  static constexpr int PW0 = TIGHT ? D : D + 8;     // row stride of W0
+  static constexpr int PW0 = D + 8;                 // row stride of W0
   static constexpr int MT = M / 16, NT = D / 8, NTH = H / 8;
   static constexpr int TPW = MT * NT / WARPS;       // output tiles per warp
   static constexpr int TPWH = MT * NTH / WARPS;     // hidden tiles per warp
   static constexpr int NE = 4 * TPW;                // owned elements per thread
-  // BF16 pieces of each activation operand: three (24 bits) up to width 128;
-  // two (16 bits) at width 256, where the weights fill shared memory.
-  static constexpr int NP = H_ <= 128 ? 3 : 2;
+  // BF16 pieces of each activation operand (24 significant bits)
+  static constexpr int NP = 3;
   static_assert(MT * NT % WARPS == 0 && TPW >= 1, "tile split");
   static_assert(MT * NTH % WARPS == 0 && NTH % TPWH == 0, "hidden tile split");
   static_assert(NT % TPW == 0, "output tile split");
@@ -71,37 +70,24 @@ struct RowState {
 template <class SH, bool PRECISE, bool SDE>
 struct MlpSmem;
 
-// A2 storage (aliased onto A1 in the tight layout)
-template <class SH, bool OWN>
-struct Act2 {
-  __nv_bfloat16 A2s[SH::M][SH::PH], A2ls[SH::M][SH::PH];
-  __nv_bfloat16 A2l2s[SH::NP == 3 ? SH::M : 1][SH::PH];
-};
-template <class SH>
-struct Act2<SH, false> {};
-
 template <class SH, bool SDE>
-struct MlpSmem<SH, false, SDE> : Act2<SH, !SH::TIGHT> {
+struct MlpSmem<SH, false, SDE> {
   static constexpr int M3 = SH::NP == 3 ? SH::M : 1;
-  __nv_bfloat16 W0[SH::H][SH::PW0];
+  __nv_bfloat16 W0[SH::GFRAG ? 1 : SH::H][SH::PW0];  // (global fragments at width 256)
   __nv_bfloat16 W1[SH::H][SH::PH];
-  __nv_bfloat16 W2[SH::D][SH::PH];
+  __nv_bfloat16 W2[SH::GFRAG ? 1 : SH::D][SH::PH];
+  const uint2 *w0f, *w2f;                            // the fragments (width 256)
   __nv_bfloat16 Ws[SDE ? SH::D : 1][SH::PD];
   float b0[SH::H], b1[SH::H], b2[SH::D], bs[SH::D];
   // stage input and hidden activations as BF16 pieces (the third piece only
   // with NP == 3)
   __nv_bfloat16 X[SH::M][SH::PD], Xl[SH::M][SH::PD], Xl2[M3][SH::PD];
   __nv_bfloat16 A1[SH::M][SH::PH], A1l[SH::M][SH::PH], A1l2[M3][SH::PH];
+  __nv_bfloat16 A2s[SH::M][SH::PH], A2ls[SH::M][SH::PH], A2l2s[M3][SH::PH];
   RowState<SH::M> rows;
-  __device__ __nv_bfloat16 (*a2())[SH::PH] {
-    if constexpr (SH::TIGHT) return A1; else return this->A2s;
-  }
-  __device__ __nv_bfloat16 (*a2l())[SH::PH] {
-    if constexpr (SH::TIGHT) return A1l; else return this->A2ls;
-  }
-  __device__ __nv_bfloat16 (*a2l2())[SH::PH] {
-    if constexpr (SH::TIGHT) return A1l2; else return this->A2l2s;
-  }
+  __device__ __nv_bfloat16 (*a2())[SH::PH] { return A2s; }
+  __device__ __nv_bfloat16 (*a2l())[SH::PH] { return A2ls; }
+  __device__ __nv_bfloat16 (*a2l2())[SH::PH] { return A2l2s; }
   // the third pieces' rows (null with two pieces)
   __device__ __nv_bfloat16 *xl2(int r) { return SH::NP == 3 ? &Xl2[r][0] : nullptr; }
   __device__ __nv_bfloat16 *a1l2(int r) { return SH::NP == 3 ? &A1l2[r][0] : nullptr; }
@@ -132,8 +118,10 @@ struct MlpField {
   using Sm = MlpSmem<SH, PRECISE, SDE>;
   static constexpr int D = SH::D, H = SH::H, M = SH::M, NE = SH::NE;
 
-  // Stage the weights (BF16 mode) and biases into shared memory.
-  __device__ static void stage(Sm &sm, const float *P, int tid) {
+  // Stage the weights (BF16 mode) and biases into shared memory (at width 256
+  // only W1: W0 and W2 are the global fragments S.w0f, S.w2f).
+  __device__ static void stage(Sm &sm, const SolveParams &S, int tid) {
+    const float *P = S.mlp;
     for (int i = tid; i < H; i += SH::THREADS) {
       sm.b0[i] = P[SH::OB0 + i];
       sm.b1[i] = P[SH::OB1 + i];
@@ -144,12 +132,19 @@ struct MlpField {
     }
     if constexpr (!PRECISE) {
       // the model's BF16 weights
-      for (int i = tid; i < H * D; i += SH::THREADS)
-        sm.W0[i / D][i % D] = __float2bfloat16_rn(P[SH::OW0 + i]);
+      if constexpr (SH::GFRAG) {
+        if (tid == 0) {
+          sm.w0f = S.w0f;
+          sm.w2f = S.w2f;
+        }
+      } else {
+        for (int i = tid; i < H * D; i += SH::THREADS)
+          sm.W0[i / D][i % D] = __float2bfloat16_rn(P[SH::OW0 + i]);
+        for (int i = tid; i < D * H; i += SH::THREADS)
+          sm.W2[i / H][i % H] = __float2bfloat16_rn(P[SH::OW2 + i]);
+      }
       for (int i = tid; i < H * H; i += SH::THREADS)
         sm.W1[i / H][i % H] = __float2bfloat16_rn(P[SH::OW1 + i]);
-      for (int i = tid; i < D * H; i += SH::THREADS)
-        sm.W2[i / H][i % H] = __float2bfloat16_rn(P[SH::OW2 + i]);
       if constexpr (SDE)
         for (int i = tid; i < D * D; i += SH::THREADS)
           sm.Ws[i / D][i % D] = __float2bfloat16_rn(P[SH::OWS + i]);
@@ -229,8 +224,12 @@ struct MlpField {
         float acc[SH::TPWH][4];
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        split_gemm<D, SH::TPWH>(acc, &sm.X[mt * 16][0], &sm.Xl[mt * 16][0], sm.xl2(mt * 16),
-                                SH::PD, &sm.W0[nt0 * 8][0], SH::PW0, lane);
+        if constexpr (SH::GFRAG)
+          gemm_gfrag_p<D, SH::TPWH, SH::NP>(acc, &sm.X[mt * 16][0], &sm.Xl[mt * 16][0],
+                                            sm.xl2(mt * 16), SH::PD, sm.w0f, nt0, lane);
+        else
+          split_gemm<D, SH::TPWH>(acc, &sm.X[mt * 16][0], &sm.Xl[mt * 16][0], sm.xl2(mt * 16),
+                                  SH::PD, &sm.W0[nt0 * 8][0], SH::PW0, lane);
 #pragma unroll
         for (int j = 0; j < SH::TPWH; j++) {
           const int col = (nt0 + j) * 8 + 2 * c, r0 = mt * 16 + g;
@@ -264,7 +263,6 @@ struct MlpField {
         for (int j = 0; j < SH::TPWH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
         split_gemm<H, SH::TPWH>(acc, &sm.A1[mt * 16][0], &sm.A1l[mt * 16][0], sm.a1l2(mt * 16),
                                 SH::PH, &sm.W1[nt0 * 8][0], SH::PH, lane);
-        if constexpr (SH::TIGHT) __syncthreads();  // every warp has read A1
         auto A2 = sm.a2();
         auto A2l = sm.a2l();
 #pragma unroll
@@ -284,8 +282,12 @@ struct MlpField {
         float acc[SH::TPW][4];
 #pragma unroll
         for (int j = 0; j < SH::TPW; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        split_gemm<H, SH::TPW>(acc, &sm.a2()[mt * 16][0], &sm.a2l()[mt * 16][0],
-                               sm.a2l2r(mt * 16), SH::PH, &sm.W2[nt0 * 8][0], SH::PH, lane);
+        if constexpr (SH::GFRAG)
+          gemm_gfrag_p<H, SH::TPW, SH::NP>(acc, &sm.a2()[mt * 16][0], &sm.a2l()[mt * 16][0],
+                                           sm.a2l2r(mt * 16), SH::PH, sm.w2f, nt0, lane);
+        else
+          split_gemm<H, SH::TPW>(acc, &sm.a2()[mt * 16][0], &sm.a2l()[mt * 16][0],
+                                 sm.a2l2r(mt * 16), SH::PH, &sm.W2[nt0 * 8][0], SH::PH, lane);
 #pragma unroll
         for (int e = 0; e < NE; e++) {
           int row, col;
@@ -536,7 +538,7 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const float *W = P.mlp;
 
-  FLD::stage(sm, W, tid);
+  FLD::stage(sm, P, tid);
   if (tid < M) {
     const unsigned long long q = atomicAdd(P.queue, 1ull);
     if (q < (unsigned long long)P.batch) {

@@ -83,8 +83,8 @@ struct BwdSmem;
 // which are dead once dW2 has been accumulated.
 template <class SH, bool SDE>
 struct BwdSmem<SH, false, SDE> {
-  static_assert(!SH::TIGHT && SH::NP == 3,
-                "three-piece operands; G1 lives in the A2 storage of the untight layout");
+  static_assert(SH::NP == 3 && !SH::GFRAG,
+                "three-piece operands, weights in shared memory");
   MlpSmem<SH, false, SDE> f;  // weights, biases, X, A1, A2 (forward recompute)
   __nv_bfloat16 G3[SH::M][SH::PD], G3l[SH::M][SH::PD], G3l2[SH::M][SH::PD];
   __nv_bfloat16 Gs[SDE ? SH::M : 1][SH::PD], Gsl[SDE ? SH::M : 1][SH::PD],
@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
   float *pcomp = Q.part_comp + size_t(blockIdx.x) * Q.n_params;
   const int n_save = P.n_save;
 
-  FLD::stage(sm.f, W, tid);
+  FLD::stage(sm.f, P, tid);
   for (int i = tid; i < H; i += SH::THREADS) sm.db0[i] = sm.db1[i] = 0.f;
   for (int i = tid; i < D; i += SH::THREADS) sm.db2[i] = sm.dbs[i] = 0.f;
   if (tid < M) {

@@ -274,6 +274,29 @@ __device__ __forceinline__ void warp_tile_gemm_p(float (&acc)[NTW][4], const __n
   }
 }
 
+// acc[j] += (A0 + A1 [+ A2])[16 rows, K] B[K, 8 (nt0 + j)] where the B
+// fragments of a fixed BF16 matrix are pre-arranged in global memory as
+// [n8 tile][k16 tile][lane] (one 8-byte load per lane, L2-resident).
+template <int K, int NTW, int NP>
+__device__ __forceinline__ void gemm_gfrag_p(float (&acc)[NTW][4], const __nv_bfloat16 *A0,
+                                             const __nv_bfloat16 *A1, const __nv_bfloat16 *A2,
+                                             int lda, const uint2 *frag, int nt0, int lane) {
+  static_assert(NP == 2 || NP == 3, "two or three pieces");
+#pragma unroll 4
+  for (int kk = 0; kk < K / 16; kk++) {
+    uint32_t a[NP][4];
+    ldsm_a(a[0], A0 + kk * 16, lda, lane);
+    ldsm_a(a[1], A1 + kk * 16, lda, lane);
+    if constexpr (NP == 3) ldsm_a(a[NP - 1], A2 + kk * 16, lda, lane);
+#pragma unroll
+    for (int j = 0; j < NTW; j++) {
+      const uint2 b = __ldg(frag + (size_t((nt0 + j) * (K / 16) + kk) << 5) + lane);
+#pragma unroll
+      for (int p = 0; p < NP; p++) mma_bf16(acc[j], a[p], b.x, b.y);
+    }
+  }
+}
+
 // acc[j] += (A0 + A1 + A2)[16 rows, K] B[K, 8 (n0 + 8 j)] with B row-major
 // [k][n] (transposed loads): a cotangent in three pieces times the weights.
 template <int K, int NTW>
