@@ -88,21 +88,40 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, period_ms: int = 20):
         self.index = index
+        self.period_ms = period_ms
         self.proc = None
         self.path = None
+        self.first = 0
+
+    def _rows(self):
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        return rows
 
     def start(self):
+        """Starts nvidia-smi and returns once it has written its first sample,
+        so that the samples after this call fall inside the timed region."""
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-i", str(self.index), "-lms", "200"],
+                 "-i", str(self.index), "-lms", str(self.period_ms)],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        deadline = time.perf_counter() + 10.0
+        while time.perf_counter() < deadline and self.proc.poll() is None:
+            if self._rows():
+                break
+            time.sleep(0.005)
+        self.first = len(self._rows())
 
     def stop(self):
         if self.proc is None:
@@ -112,12 +131,12 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        rows = []
-        for line in open(self.path):
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
-                rows.append(parts)
+        every = self._rows()
         os.unlink(self.path)
+        # the samples written during the timed region; a region shorter than
+        # the sampling period keeps the sample nearest its start
+        rows = every[self.first:] or every[-1:]
+        in_region = len(every) - self.first
         if not rows:
             return None
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
@@ -127,7 +146,7 @@ class ClockSampler:
                           if r[5 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(rows)}
+                "samples": max(in_region, 0), "period_ms": self.period_ms}
 
 
 def dist_env():
@@ -617,7 +636,7 @@ def _neural_forward(case, flush, steps, warmup, n_chk=256):
         "bound": "tensor", "achieved": alg, "peak": peak, "unit": "TFLOP/s",
         "frac": alg / peak, "peak_source": src,
         "work": f"{case.fl_eval} flop per field evaluation x {case.evals} evaluations per "
-                f"attempted step (algorithmic; hi/lo operands execute 2-3x that)"}
+                f"attempted step (algorithmic; the three-piece operands execute 3x that)"}
     out["fused_over_plain"] = out["plain"]["ms"] / f["ms"]
     out["fused_err_le_plain_err"] = (f["max_rel_err_vs_fp64_oracle"]
                                      <= out["plain"]["max_rel_err_vs_fp64_oracle"])

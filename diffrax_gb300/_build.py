@@ -3,6 +3,11 @@
 Each CUDA translation unit under ``csrc/`` is compiled by its own ``nvcc``
 process (in parallel) and linked into ``diffrax_gb300/_lib/libgbdx.so``.  The
 library is rebuilt whenever a source or header is newer than it.
+
+``build(bounds=True)`` makes the bounds-checked variant
+``libgbdx_bounds.so`` from the same sources with ``-DGBDX_BOUNDS`` (every
+kernel index into a caller buffer checked; include/gbdx.h, GBDX_ERR_BOUNDS);
+``GBDX_BOUNDS=1`` in the environment makes the package load it.
 """
 from __future__ import annotations
 
@@ -18,6 +23,8 @@ CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(PKG, "_lib", "obj")
 LIB_PATH = os.path.join(OUT_DIR, "libgbdx.so")
+BOUNDS_LIB_PATH = os.path.join(OUT_DIR, "libgbdx_bounds.so")
+BOUNDS_OBJ_DIR = os.path.join(PKG, "_lib", "obj_bounds")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
@@ -45,24 +52,29 @@ def _deps() -> list[str]:
             glob.glob(os.path.join(ROOT, "include", "*.h")) + [os.path.abspath(__file__)])
 
 
-def is_stale() -> bool:
-    if not os.path.exists(LIB_PATH):
+def is_stale(bounds: bool = False) -> bool:
+    lib = BOUNDS_LIB_PATH if bounds else LIB_PATH
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB_PATH)
+    t = os.path.getmtime(lib)
     return any(os.path.getmtime(p) > t for p in _deps())
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile every translation unit and link libgbdx.so.  Returns its path."""
-    if not force and not is_stale():
-        return LIB_PATH
-    os.makedirs(OBJ_DIR, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, bounds: bool = False) -> str:
+    """Compile every translation unit and link libgbdx.so (libgbdx_bounds.so
+    with bounds=True).  Returns its path."""
+    lib_path = BOUNDS_LIB_PATH if bounds else LIB_PATH
+    obj_dir = BOUNDS_OBJ_DIR if bounds else OBJ_DIR
+    if not force and not is_stale(bounds):
+        return lib_path
+    os.makedirs(obj_dir, exist_ok=True)
     cc = nvcc()
     srcs = sources()
+    extra = ["-DGBDX_BOUNDS"] if bounds else []
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(OBJ_DIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [cc] + NVCC_FLAGS + PER_FILE_FLAGS.get(os.path.basename(src), []) + [
+        obj = os.path.join(obj_dir, os.path.basename(src)[:-3] + ".o")
+        cmd = [cc] + NVCC_FLAGS + extra + PER_FILE_FLAGS.get(os.path.basename(src), []) + [
             "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
@@ -73,13 +85,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    tmp = lib_path + f".tmp{os.getpid()}"
     cmd = [cc, "-shared", "-cudart", "shared"] + ARCH + ["-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"link of libgbdx.so failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+        raise RuntimeError(f"link of {os.path.basename(lib_path)} failed:\n{r.stdout}\n"
+                           f"{r.stderr}")
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -58,11 +58,13 @@ class MLPField(AbstractField):
     (tanh on the hidden layers, identity output; equinox/nn/_mlp.py semantics)
     given its weights as tensors.  weights[l] is [out, in] as in a Linear layer.
 
-    precision "bf16" runs the products on the tensor cores with BF16 operands
-    and FP32 accumulation.  Operands are split into hi/lo BF16 pairs (three
-    products per tile, ~16 significant bits) so the field stays smooth under
-    adaptive stepping; at width 256 the weights are held as single BF16 values.
-    "fp32" runs the products in FP32 on the CUDA cores (parity mode)."""
+    precision "bf16" runs the products on the tensor cores with FP32
+    accumulation: the weights are held as BF16 values and every activation
+    operand is split into three BF16 pieces (24 significant bits, three
+    products per tile), so the field equals an FP32 evaluation of the
+    BF16-rounded weights and stays smooth under adaptive stepping.  "fp32"
+    runs the products in FP32 on the CUDA cores with the FP32 weights (parity
+    mode)."""
     field_id = 3
     n_args = 0
 
@@ -433,20 +435,24 @@ class Event:
 class SaveAt:
     """diffrax/_saveat.py:69-105.  ``steps`` is a bool or an int n (save every
     n-th accepted step); ``dense=True`` records the solution's dense output
-    (``Solution.evaluate`` / ``Solution.derivative``)."""
+    (``Solution.evaluate`` / ``Solution.derivative``); ``solver_state``,
+    ``controller_state`` and ``made_jump`` keep the final states, which a
+    later ``diffeqsolve`` resumes from."""
 
     def __init__(self, *, t0: bool = False, t1: bool = False, ts=None, steps=False,
                  dense: bool = False, solver_state: bool = False,
                  controller_state: bool = False, made_jump: bool = False):
-        if solver_state or controller_state or made_jump:
-            raise NotImplementedError("saving solver/controller state is not supported")
+        self.solver_state, self.controller_state = bool(solver_state), bool(controller_state)
+        self.made_jump = bool(made_jump)
         # SubSaveAt.__init__: steps=True means every step (_saveat.py:40-43)
         if isinstance(steps, bool):
             steps = 1 if steps else 0
         steps = int(steps)
         if steps < 0:
             raise ValueError("SaveAt(steps=n) needs n >= 0")
-        if not (t0 or t1 or ts is not None or steps or dense):
+        # the states alone save no ys (subs = None, _saveat.py:91-93)
+        self.state_only = not (t0 or t1 or ts is not None or steps or dense)
+        if self.state_only and not (solver_state or controller_state or made_jump):
             raise ValueError("Empty saveat -- nothing will be saved.")
         self.t0, self.t1, self.ts = bool(t0), bool(t1), ts
         self.steps, self.dense = steps, bool(dense)
@@ -523,6 +529,13 @@ class Solution:
     result: Any    # [B] int32 RESULTS codes
     interpolation: Any = None  # DenseInterpolation under SaveAt(dense=True)
     event_mask: Any = None     # Event: [B] bool per condition (cond_fn's structure)
+    # SaveAt(solver_state=, controller_state=, made_jump=): PID (prev_inv
+    # [B], prev_prev_inv [B], at_dtmin [B] bool) or ConstantStepSize
+    # (steps_completed [B], num_steps [B], t0 [B], t1_or_dt0 [B]); FSAL
+    # solvers (first_step [B] bool, f0 [B, dim]), others None; made_jump [B]
+    solver_state: Any = None
+    controller_state: Any = None
+    made_jump: Any = None
 
     def evaluate(self, t0, t1=None, left: bool = True):
         """y(t0) of every trajectory from the dense output, or y(t1) - y(t0)

@@ -92,7 +92,8 @@ def lower(terms, solver, stepsize_controller, saveat: SaveAt, *, dim: int, dtype
     if not isinstance(drift, AbstractField):
         raise TypeError("the drift must be a registered vector field")
     f = dict(solver=solver.solver_id, field=drift.field_id, dim=int(dim),
-             n_ts=int(n_ts), save_t0=int(saveat.t0), save_t1=int(saveat.t1),
+             n_ts=int(n_ts), save_t0=int(saveat.t0),
+             save_t1=int(saveat.t1 or getattr(saveat, "state_only", False)),
              max_steps=int(max_steps), n_args=drift.n_args,
              dtype=0 if dtype == torch.float32 else 1, kernel=KERNELS[kernel],
              block_threads=int(block_threads), ctas_per_sm=int(ctas_per_sm),
@@ -361,10 +362,12 @@ class Lowered:
             return ys, ts_out, res, stats, ws
         return ys, ts_out, res, stats
 
-    def run_forward_ex(self, stream=None):
+    def run_forward_ex(self, stream=None, state_in=None, want_state=False):
         """Forward solve through gbdx_solve_fwd_ex: the saved outputs plus the
         dense buffers (SaveAt(dense=True)) and the index of the event condition
-        that ended each trajectory (-1 for none)."""
+        that ended each trajectory (-1 for none).  state_in ([B, GBDX_STATE_HEAD
+        + dim] f64, include/gbdx.h) resumes a solve; want_state leaves the
+        final record in self.state_record."""
         dev = self.device
         B, D, n_save = self.B, self.dim, self.n_save
         ys = torch.empty((B, n_save, D), dtype=self.dtype, device=dev)
@@ -385,6 +388,14 @@ class Lowered:
         if self.fields["n_event"]:
             ev = torch.empty((B,), dtype=torch.int32, device=dev)
             ex.event_index = p(ev)
+        self.state_record = None
+        if state_in is not None:
+            state_in = state_in.to(device=dev, dtype=torch.float64).contiguous()
+            ex.state_in = p(state_in)
+        if want_state:
+            self.state_record = torch.empty((B, STATE_HEAD + D), dtype=torch.float64,
+                                            device=dev)
+            ex.state_out = p(self.state_record)
         ws_bytes = self.problem.workspace_size(B)
         ws = torch.empty((max(ws_bytes, 1),), dtype=torch.uint8, device=dev)
         if stream is None:
@@ -538,6 +549,62 @@ class DenseInterpolation:
         return torch.where(self.ts_size == 1, self.t0_if_trivial, last) * self.direction
 
 
+# gbdx_fwd_extras' resume record: GBDX_STATE_HEAD doubles, then f0 (include/gbdx.h)
+STATE_HEAD = 7
+_FSAL_SOLVERS = (2, 3, 4)  # Dopri5, Tsit5, Dopri8
+
+
+def _state_record(low: "Lowered", solver_state, controller_state, made_jump):
+    """The [B, STATE_HEAD + dim] resume record from diffeqsolve's
+    solver_state / controller_state / made_jump (_integrate.py:1252-1271,
+    1309), in the layouts Solution documents."""
+    f = low.fields
+    if f["n_step_ts"] or f["n_jump_ts"] or f["field"] == 3:
+        raise NotImplementedError("resuming is supported for the analytic fields without "
+                                  "a ClipStepSizeController")
+    B, D, dev = low.B, low.dim, low.device
+    rec = torch.zeros((B, STATE_HEAD + D), dtype=torch.float64, device=dev)
+    rec[:, 5] = 1.0
+
+    def col(v):
+        return torch.as_tensor(v).to(device=dev, dtype=torch.float64).reshape(-1).expand(B)
+
+    if controller_state is not None:
+        cs = tuple(controller_state)
+        want = 3 if f["controller"] == 1 else 4
+        if len(cs) != want:
+            raise ValueError(f"controller_state must hold {want} entries for this controller")
+        for k, v in enumerate(cs):
+            rec[:, k] = col(v)
+        rec[:, 4] = 1.0
+    if solver_state is not None:
+        if f["solver"] not in _FSAL_SOLVERS:
+            raise ValueError("this solver has no solver state (None)")
+        first_step, f0 = solver_state
+        rec[:, 5] = col(first_step)
+        rec[:, STATE_HEAD:] = torch.as_tensor(f0).to(device=dev, dtype=torch.float64
+                                                     ).reshape(-1, D).expand(B, D)
+    if made_jump is not None:
+        rec[:, 6] = col(made_jump)
+    return rec
+
+
+def _split_state(low: "Lowered", rec: torch.Tensor, saveat: SaveAt, sol: "Solution"):
+    """Solution.solver_state / controller_state / made_jump from the final
+    record (_integrate.py:1489-1500)."""
+    f = low.fields
+    if saveat.controller_state:
+        if f["controller"] == 1:
+            sol.controller_state = (rec[:, 0], rec[:, 1], rec[:, 2] != 0)
+        else:
+            sol.controller_state = (rec[:, 0].to(torch.int32), rec[:, 1].to(torch.int32),
+                                    rec[:, 2], rec[:, 3])
+    if saveat.solver_state and f["solver"] in _FSAL_SOLVERS:
+        sol.solver_state = (rec[:, 5] != 0, rec[:, STATE_HEAD:].to(low.dtype))
+    if saveat.made_jump:
+        sol.made_jump = rec[:, 6] != 0
+
+
 def _raise_on_failure(result: torch.Tensor):
     if _capturing():
         return
@@ -574,13 +641,14 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     device asynchronously, so they must not be modified until the solution's
     tensors have been read.
     """
-    if solver_state is not None or controller_state is not None or made_jump is not None:
-        raise NotImplementedError("resuming from solver/controller state is not supported")
+    resume = solver_state is not None or controller_state is not None or made_jump is not None
+    keep_state = saveat.solver_state or saveat.controller_state or saveat.made_jump
     from ._autograd import needs_grad, solve_with_grad
     want_grad = needs_grad(terms, y0, args)
-    if want_grad and (saveat.dense or saveat.steps or event is not None):
-        raise NotImplementedError("gradients through SaveAt(steps=...), SaveAt(dense=True) "
-                                  "or events are not supported")
+    if want_grad and (saveat.dense or saveat.steps or event is not None or resume
+                      or keep_state):
+        raise NotImplementedError("gradients through SaveAt(steps=...), SaveAt(dense=True), "
+                                  "events or solver/controller states are not supported")
     if (autotune and not want_grad and block_threads == 0 and ctas_per_sm == 0
             and kernel in ("auto", "fused")):
         from ._tune import autotune_launch
@@ -594,13 +662,20 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
                   adjoint, max_steps, kernel, block_threads, ctas_per_sm, schedule,
                   want_grad=want_grad, event=event, throw=throw)
     interp = ev = None
-    if saveat.dense or event is not None:
-        ys, ts_out, res, stats, interp, ev = low.run_forward_ex()
+    if saveat.dense or event is not None or resume or keep_state:
+        rec = None
+        if resume:
+            rec = _state_record(low, solver_state, controller_state, made_jump)
+        elif keep_state:
+            _state_record(low, None, None, None)  # the same support check
+        ys, ts_out, res, stats, interp, ev = low.run_forward_ex(state_in=rec,
+                                                                want_state=keep_state)
     elif want_grad:
         ys, ts_out, res, stats = solve_with_grad(low, y0, args)
     else:
         ys, ts_out, res, stats = low.run_forward()
-    if low.n_save == 0:  # SaveAt(dense=True) alone saves no ys (_integrate.py:1527-1539)
+    if low.n_save == 0 or saveat.state_only:
+        # SaveAt(dense=True) or the states alone save no ys (_integrate.py:1527-1539)
         ys = ts_out = None
     sol = Solution(t0=t0, t1=t1, ts=ts_out, ys=ys,
                    stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],
@@ -609,6 +684,8 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     if event is not None:
         masks = [ev == i for i in range(len(event._conds))]
         sol.event_mask = masks[0] if event._single else masks
+    if keep_state:
+        _split_state(low, low.state_record, saveat, sol)
     # the lowered solve; after a backward pass under BacksolveAdjoint it holds
     # the backward's RESULTS codes and step counts (bwd_result, bwd_stats)
     sol.lowered = low

@@ -40,24 +40,32 @@ class ProblemDesc(_c.Structure):
 
 class FwdExtras(_c.Structure):
     """Mirror of gbdx_fwd_extras."""
-    _fields_ = [("dense_ts", vp), ("dense_info", vp), ("dense_n", vp), ("event_index", vp)]
+    _fields_ = [("dense_ts", vp), ("dense_info", vp), ("dense_n", vp), ("event_index", vp),
+                ("state_in", vp), ("state_out", vp)]
 
 
 _lock = threading.Lock()
 _LIB = None
 
 
+def bounds_requested() -> bool:
+    """GBDX_BOUNDS=1 selects the bounds-checked library (libgbdx_bounds.so)."""
+    return os.environ.get("GBDX_BOUNDS", "0") not in ("", "0")
+
+
 def load():
-    """Build (when stale) and load libgbdx.so; raise loudly on failure."""
+    """Build (when stale) and load libgbdx.so -- libgbdx_bounds.so under
+    GBDX_BOUNDS=1; raise loudly on failure."""
     global _LIB
     with _lock:
         if _LIB is not None:
             return _LIB
-        path = _build.LIB_PATH
-        if _build.is_stale():
-            path = _build.build()
+        bounds = bounds_requested()
+        path = _build.BOUNDS_LIB_PATH if bounds else _build.LIB_PATH
+        if _build.is_stale(bounds):
+            path = _build.build(bounds=bounds)
         if not os.path.exists(path):
-            raise RuntimeError(f"libgbdx.so is missing at {path}")
+            raise RuntimeError(f"{os.path.basename(path)} is missing at {path}")
         lib = _c.CDLL(path)
         lib.gbdx_problem_create.argtypes = [_c.POINTER(ProblemDesc), _c.POINTER(vp)]
         lib.gbdx_problem_create.restype = i32
@@ -93,6 +101,10 @@ def load():
         lib.gbdx_last_error.argtypes = []
         lib.gbdx_last_error.restype = _c.c_char_p
         lib.gbdx_version.restype = i32
+        lib.gbdx_bounds_checked.argtypes = []
+        lib.gbdx_bounds_checked.restype = i32
+        if bool(lib.gbdx_bounds_checked()) != bounds:
+            raise RuntimeError(f"{os.path.basename(path)} is not the requested build")
         lib.gbdx_problem_desc_size.restype = _c.c_size_t
         if lib.gbdx_problem_desc_size() != _c.sizeof(ProblemDesc):
             raise RuntimeError("gbdx_problem_desc layout mismatch between Python and C")
@@ -108,11 +120,17 @@ class GbdxError(RuntimeError):
     pass
 
 
+class GbdxBoundsError(GbdxError, IndexError):
+    """A kernel index left its buffer (bounds-checked build, GBDX_ERR_BOUNDS)."""
+
+
 def check(rc: int, what: str):
     if rc != 0:
         msg = last_error()
         if rc == -1:
             raise ValueError(f"{what}: {msg}")
+        if rc == -5:
+            raise GbdxBoundsError(f"{what}: {msg}")
         raise GbdxError(f"{what} failed ({rc}): {msg}")
 
 

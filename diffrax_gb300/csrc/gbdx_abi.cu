@@ -78,7 +78,7 @@ namespace {
 // Workspace of one solve: the work counter, the work order, and (recursive
 // adjoint) the tape the backward reads plus its scratch.
 struct WsLayout {
-  size_t order, ffrag, tape_t, tape_y, tape_n, tape_s, scratch, psum, pcomp, total;
+  size_t order, ffrag, tape_t, tape_y, tape_n, tape_s, scratch, psum, pcomp, bounds, total;
   bool has_ffrag;  // width-256 MLP forward: W0 / W2 fragments at ffrag
   size_t frag, rec, ath;  // backsolve: B fragments, stage records, a_theta
   int seg_max, n_cta;
@@ -208,7 +208,63 @@ int ws_layout(const gbdx_problem *p, int64_t batch, WsLayout *L) {
     off += up256(B * size_t(p->adj.n_args) * esz);
     L->track = bs_tracks(d);
   }
+  L->bounds = off;
+#ifdef GBDX_BOUNDS
+  off += GBDX_BOUNDS_BYTES;
+#endif
   L->total = off;
+  return GBDX_OK;
+}
+
+// Bounds-checked builds: clear the launch's record before its kernels and
+// read it after them (include/gbdx.h, GBDX_ERR_BOUNDS).
+int bounds_clear(const gbdx::SolveParams &P, cudaStream_t s) {
+#ifdef GBDX_BOUNDS
+  cudaError_t e = cudaMemsetAsync(P.bounds, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return cuda_fail(e, "bounds record reset");
+#else
+  (void)P;
+  (void)s;
+#endif
+  return GBDX_OK;
+}
+
+const char *bounds_site_name(int site) {
+  switch (site) {
+    case GBDX_SITE_YS: return "ys";
+    case GBDX_SITE_TS: return "ts";
+    case GBDX_SITE_TAPE_T: return "tape times";
+    case GBDX_SITE_TAPE_Y: return "tape states";
+    case GBDX_SITE_DENSE_TS: return "dense_ts";
+    case GBDX_SITE_DENSE_INFO: return "dense_info";
+    case GBDX_SITE_STATE: return "state records";
+    case GBDX_SITE_SCRATCH: return "segment scratch";
+    case GBDX_SITE_GRAD_YS: return "grad_ys / saved ys";
+    default: return "unknown";
+  }
+}
+
+int bounds_report(const gbdx::SolveParams &P, cudaStream_t s, const char *call) {
+#ifdef GBDX_BOUNDS
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cap);
+  if (e != cudaSuccess) return cuda_fail(e, "bounds capture query");
+  if (cap != cudaStreamCaptureStatusNone) return GBDX_OK;
+  unsigned long long rec = 0;
+  e = cudaMemcpyAsync(&rec, P.bounds, sizeof rec, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "bounds record read");
+  if (rec != 0) {
+    long long idx = static_cast<long long>(rec << 8) >> 8;  // sign-extend 56 bits
+    const int site = int(rec >> 56);
+    return fail(GBDX_ERR_BOUNDS, "%s: index %lld outside the %s buffer (site %d)", call, idx,
+                bounds_site_name(site), site);
+  }
+#else
+  (void)P;
+  (void)s;
+  (void)call;
+#endif
   return GBDX_OK;
 }
 
@@ -217,6 +273,14 @@ int ws_layout(const gbdx_problem *p, int64_t batch, WsLayout *L) {
 extern "C" {
 
 int gbdx_version(void) { return 1; }
+
+int gbdx_bounds_checked(void) {
+#ifdef GBDX_BOUNDS
+  return 1;
+#else
+  return 0;
+#endif
+}
 
 size_t gbdx_problem_desc_size(void) { return sizeof(gbdx_problem_desc); }
 
@@ -349,13 +413,19 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     return fail(GBDX_ERR_INVALID, "the root finder needs rtol >= 0 and atol > 0");
   }
   const bool xo = d.save_steps > 0 || d.save_dense || clip || d.n_event > 0;
-  if (xo && (d.field == GBDX_MLP || d.adjoint != GBDX_ADJ_NONE ||
-             (sde && d.diffusion != GBDX_DIFF_OU))) {
+  // The MLP integrator (K2) records step saves and dense steps and runs the
+  // clip controller; the plain and tensor-core MLP kernels do not.
+  const bool xo_mlp = d.field == GBDX_MLP && d.n_event == 0 && d.adjoint == GBDX_ADJ_NONE &&
+                      d.kernel != GBDX_KERNEL_PLAIN && d.kernel != GBDX_KERNEL_TC;
+  if (xo && !xo_mlp &&
+      (d.field == GBDX_MLP || d.adjoint != GBDX_ADJ_NONE ||
+       (sde && d.diffusion != GBDX_DIFF_OU))) {
     delete p;
     return fail(GBDX_ERR_UNSUPPORTED,
                 "SaveAt(steps=...), SaveAt(dense=True), ClipStepSizeController and events "
                 "are available for forward solves of the analytic fields (ODEs and the "
-                "Ornstein-Uhlenbeck SDE)");
+                "Ornstein-Uhlenbeck SDE); all but events also for forward solves of the MLP "
+                "fields on the fused kernel");
   }
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
                d.field == GBDX_ORNSTEIN_UHLENBECK)) {
@@ -605,6 +675,10 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
                 workspace_bytes, L->total);
   gbdx::SolveParams &P = *out;
   memset(&P, 0, sizeof P);
+#ifdef GBDX_BOUNDS
+  P.bounds = reinterpret_cast<unsigned long long *>(static_cast<char *>(workspace) + L->bounds);
+  P.bounds_sink = static_cast<char *>(workspace) + L->bounds + 256;
+#endif
   P.batch = batch;
   P.t0 = t0;
   P.t1 = t1;
@@ -715,6 +789,11 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
   void *dense_info = ex ? ex->dense_info : nullptr;
   int32_t *dense_n = ex ? ex->dense_n : nullptr;
   const gbdx_problem_desc &d = problem->d;
+  const bool resume = ex && (ex->state_in || ex->state_out);
+  if (resume && (d.field == GBDX_MLP || d.n_step_ts > 0 || d.n_jump_ts > 0))
+    return fail(GBDX_ERR_UNSUPPORTED,
+                "solver and controller states are available for the analytic fields without "
+                "a ClipStepSizeController");
   if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
   if (batch == 0) return GBDX_OK;
   if ((problem->n_save > 0 && (!ys_out || !ts_out)) || !result_out || !stats_out)
@@ -730,6 +809,8 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
   P.stats_out = stats_out;
   P.save_steps = d.save_steps;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  rc = bounds_clear(P, s);
+  if (rc != GBDX_OK) return rc;
   if (d.save_dense) {
     // The reference's dense buffers start full of +inf (_integrate.py:1315-1323);
     // the solve overwrites the recorded steps.
@@ -747,6 +828,10 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
     P.dense_n = dense_n;
   }
   if (d.n_event > 0) P.event_index = ex ? ex->event_index : nullptr;
+  if (resume) {
+    P.state_in = ex->state_in;
+    P.state_out = ex->state_out;
+  }
   if (d.save_steps > 0 && problem->n_save > 0) {
     // SaveAt(steps=n) reserves max_steps / n slots per trajectory, most of
     // them unused: fill them all in one pass before the solve
@@ -810,7 +895,7 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
   }
   cudaError_t e = problem->ode.launch(P, cfg, s);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
-  return GBDX_OK;
+  return bounds_report(P, s, "gbdx_solve_fwd");
 }
 
 extern "C" {
@@ -913,6 +998,8 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                    save_ts, workspace, workspace_bytes, &P, &L);
   if (rc != GBDX_OK) return rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  rc = bounds_clear(P, s);
+  if (rc != GBDX_OK) return rc;
   if (problem->adj.rc_bwd) {
     // analytic fields: grad_params receives dL/dargs, per trajectory
     // [batch, n_args] when args has a row per trajectory, else [n_args]
@@ -931,7 +1018,7 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
                                                  grad_params, s);
       if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
     }
-    return GBDX_OK;
+    return bounds_report(P, s, "gbdx_solve_bwd");
   }
   const int np = int(gbdx_param_count(problem));
   char *w = static_cast<char *>(workspace);
@@ -943,7 +1030,7 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   Q.scratch = reinterpret_cast<float *>(w + L.scratch);
   Q.seg_max = L.seg_max;
   Q.n_params = np;
-  cudaError_t e = cudaMemsetAsync(w + L.psum, 0, L.total - L.psum, s);
+  cudaError_t e = cudaMemsetAsync(w + L.psum, 0, L.bounds - L.psum, s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient partial reset");
   const bool plain = problem->d.kernel == GBDX_KERNEL_PLAIN;
   if (batch > 0) {
@@ -960,7 +1047,7 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
     e = gbdx::launch_reduce_partials(Q.part_sum, Q.part_comp, batch > 0 ? L.n_cta : 0, np,
                                      static_cast<float *>(grad_params), s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
-  return GBDX_OK;
+  return bounds_report(P, s, "gbdx_solve_bwd");
 }
 
 int gbdx_backsolve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
@@ -1000,6 +1087,8 @@ int gbdx_backsolve_bwd_ex(const gbdx_problem *problem, int64_t batch, const doub
   P.result_out = result_out;
   P.stats_out = stats_out;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  rc = bounds_clear(P, s);
+  if (rc != GBDX_OK) return rc;
   if (problem->adj.bs_bwd) {
     // analytic fields: grad_params receives dL/dargs as in gbdx_solve_bwd
     gbdx::AdjParams A;
@@ -1019,7 +1108,7 @@ int gbdx_backsolve_bwd_ex(const gbdx_problem *problem, int64_t batch, const doub
                                                  grad_params, s);
       if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
     }
-    return GBDX_OK;
+    return bounds_report(P, s, "gbdx_backsolve_bwd");
   }
   const int np = int(gbdx_param_count(problem));
   const int D = d.dim, H = d.mlp_widths[1];
@@ -1041,7 +1130,7 @@ int gbdx_backsolve_bwd_ex(const gbdx_problem *problem, int64_t batch, const doub
     if (e != cudaSuccess) return cuda_fail(e, "plain backsolve launch");
     e = gbdx::launch_reduce_columns(Q.ath, np, batch, static_cast<float *>(grad_params), s);
     if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
-    return GBDX_OK;
+    return bounds_report(P, s, "gbdx_backsolve_bwd");
   }
   e = cudaMemsetAsync(w + L.psum, 0, L.ath - L.psum, s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient partial reset");
@@ -1079,7 +1168,7 @@ int gbdx_backsolve_bwd_ex(const gbdx_problem *problem, int64_t batch, const doub
     e = gbdx::launch_reduce_partials_frag(Q.psum, Q.pcomp, batch > 0 ? L.n_cta : 0, D, H,
                                           static_cast<float *>(grad_params), s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
-  return GBDX_OK;
+  return bounds_report(P, s, "gbdx_backsolve_bwd");
 }
 
 }  // extern "C"

@@ -62,6 +62,7 @@ struct BsShape {
   static_assert(MT * NT % WARPS == 0 && TPW >= 1, "tile split");
   static_assert(MT * NTH % WARPS == 0 && NTH % TPWH == 0, "hidden tile split");
   static_assert(NT % TPW == 0, "output tile split");
+  static_assert(NT <= 8, "error-norm partials: at most 8 column tiles");
   // flat parameter offsets (FP32, row-major [out][in]), as MlpShape
   static constexpr int OW0 = 0, OB0 = OW0 + H * D, OW1 = OB0 + H, OB1 = OW1 + H * H,
                        OW2 = OB1 + H, OB2 = OW2 + D * H, NP = OB2 + D;
@@ -80,6 +81,7 @@ struct BsRows {
   int seg[M], jold[M], trans[M], newtraj[M], done[M], firstseg[M];
   int nseg[M], nsteps[M], nacc[M], nrej[M], result[M], sres[M], sc[M], nc[M], at_dtmin[M];
   int live[M], cur[M], zero[M];
+  float part[M][8];  // error-norm partials per 8-column tile, summed in order
 };
 
 template <class SH, bool GF>
@@ -996,11 +998,13 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
           if (R.newtraj[row]) A0[e] = 0.f;
           const int jn = R.seg[row] > 0 ? R.seg[row] : 0;
           for (int jj = jn; jj < R.jold[row]; jj++)
-            A0[e] += Q.grad_ys[(i * P.n_save + jj) * D + col];
+            A0[e] += *GBDX_AT(P, Q.grad_ys, (i * P.n_save + jj) * D + col, 1,
+                              P.batch * P.n_save * D, GBDX_SITE_GRAD_YS);
           if (R.done[row]) {
             Q.grad_y0[i * D + col] = A0[e];
           } else {
-            Y0[e] = Q.ys[(i * P.n_save + R.seg[row]) * D + col];
+            Y0[e] = *GBDX_AT(P, Q.ys, (i * P.n_save + R.seg[row]) * D + col, 1,
+                             P.batch * P.n_save * D, GBDX_SITE_GRAD_YS);
           }
         }
       }
@@ -1145,8 +1149,15 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
           }
           part += __shfl_xor_sync(0xffffffffu, part, 1);
           part += __shfl_xor_sync(0xffffffffu, part, 2);
-          if ((lane & 3) == 0) atomicAdd(&R.acc[row], part);
+          if ((lane & 3) == 0) R.part[row][(warp * SH::TPW + j) % SH::NT] = part;
         }
+      }
+      __syncthreads();
+      if (tid < M && R.live[tid]) {
+        float a = 0.f;
+#pragma unroll
+        for (int n = 0; n < SH::NT; n++) a += R.part[tid][n];
+        R.acc[tid] = a;
       }
       __syncthreads();
       // the a_theta part of the norm: one parameter pass per live row

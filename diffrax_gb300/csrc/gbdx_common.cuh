@@ -515,7 +515,37 @@ struct SolveParams {
   double newton_rtol, newton_atol;
   double ev_coef[6 * GBDX_MAX_EVENTS];
   int32_t *event_index;       // [batch] condition that ended the solve, -1 none
+  // Resuming (gbdx_fwd_extras): [batch, GBDX_STATE_HEAD + dim] FP64 records
+  const double *state_in;
+  double *state_out;
+  // Bounds-checked builds: the first out-of-range index (site << 56 | index)
+  // and the sink that takes its access (null in release builds)
+  unsigned long long *bounds;
+  void *bounds_sink;
 };
+
+// GBDX_AT(P, base, off, width, extent, site): base + off, where the access
+// covers elements [off, off + width) of a buffer of `extent` elements.  In a
+// bounds-checked build (-DGBDX_BOUNDS) an access outside [0, extent) records
+// (site, off) in P.bounds -- the first of the launch -- and goes to
+// P.bounds_sink instead (GBDX_BOUNDS_BYTES - 256 bytes); the release build
+// compiles to the plain pointer arithmetic.
+#ifdef GBDX_BOUNDS
+template <class T>
+__device__ __forceinline__ T *bounds_at(unsigned long long *rec, void *sink, T *base,
+                                        int64_t off, int64_t width, int64_t extent, int site) {
+  if (off >= 0 && off + width <= extent) return base + off;
+  atomicCAS(rec, 0ull,
+            (static_cast<unsigned long long>(site) << 56) |
+                (static_cast<unsigned long long>(off) & 0x00ffffffffffffffull));
+  return reinterpret_cast<T *>(sink);
+}
+#define GBDX_AT(P, base, off, width, extent, site)                                     \
+  ::gbdx::bounds_at((P).bounds, (P).bounds_sink, (base), int64_t(off), int64_t(width), \
+                    int64_t(extent), (site))
+#else
+#define GBDX_AT(P, base, off, width, extent, site) ((base) + (off))
+#endif
 
 // BacksolveAdjoint backward arguments.
 struct BsParams {

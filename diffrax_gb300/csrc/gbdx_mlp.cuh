@@ -52,6 +52,7 @@ struct MlpShape {
   static_assert(MT * NT % WARPS == 0 && TPW >= 1, "tile split");
   static_assert(MT * NTH % WARPS == 0 && NTH % TPWH == 0, "hidden tile split");
   static_assert(NT % TPW == 0, "output tile split");
+  static_assert(NT <= 8, "error-norm partials: at most 8 column tiles");
   // flat parameter offsets (FP32, row-major [out][in])
   static constexpr int OW0 = 0, OB0 = OW0 + H * D, OW1 = OB0 + H, OB1 = OW1 + H * H,
                        OW2 = OB1 + H, OB2 = OW2 + D * H, OWS = OB2 + D, OBS = OWS + D * D;
@@ -65,6 +66,11 @@ struct RowState {
   int active[M], first[M], keep[M], anynan[M], dir[M], save_index[M], ts_index[M];
   int nsteps[M], nacc[M], nrej[M], result[M], sflag[M], sslot[M], fin[M], nfill[M];
   int loaded[M], sc[M], nc[M], cpstride[M], cpslot[M], cpcompact[M], at_dtmin[M], live[M];
+  int sdown[M], stslot[M];  // SaveAt(steps=n): steps to the next save; this step's slot
+  int sidx[M], jidx[M];     // ClipStepSizeController: search hints into step_ts / jump_ts
+  // the error norm's partial sums per 8-column output tile, added in a fixed
+  // order (results do not depend on warp timing)
+  float part[M][8];
 };
 
 template <class SH, bool PRECISE, bool SDE>
@@ -325,6 +331,7 @@ __device__ void row_init(RowState<M> &R, int r, int64_t i, const SolveParams &P)
     if (P.has_dtmax) h = fmin(h, P.dtmax);
     if (P.has_dtmin) h = fmax(h, P.dtmin);
     tn = a + h;
+    if (P.n_step_ts > 0 || P.n_jump_ts > 0) tn = clip_start(P, dir, R.sidx[r], R.jidx[r], a, tn);
     R.hist1[r] = 0.f;
     R.hist2[r] = 0.f;
   } else {
@@ -351,10 +358,19 @@ __device__ void row_init(RowState<M> &R, int r, int64_t i, const SolveParams &P)
   R.at_dtmin[r] = 0;
   R.live[r] = 0;
   if (P.save_t0) {
-    P.ts_out[i * P.n_save] = a * dir;
+    *GBDX_AT(P, P.ts_out, i * P.n_save, 1, P.batch * P.n_save, GBDX_SITE_TS) = a * dir;
     R.save_index[r] = 1;
   }
-  if (P.tape_t) P.tape_t[i * (P.max_steps + 1)] = a;
+  if (P.tape_t)
+    *GBDX_AT(P, P.tape_t, i * (P.max_steps + 1), 1, P.batch * (P.max_steps + 1),
+             GBDX_SITE_TAPE_T) = a;
+  R.sdown[r] = P.save_steps;
+  R.stslot[r] = -1;
+  // dense_ts[0] = t0 in the loop's time; the rest of the dense buffers was
+  // filled with +inf before the launch (_integrate.py:1315-1323)
+  if (P.dense_ts)
+    *GBDX_AT(P, P.dense_ts, i * (P.max_steps + 1), 1, P.batch * (P.max_steps + 1),
+             GBDX_SITE_DENSE_TS) = a;
 }
 
 // The controller's decision for row r after the error norm acc = sum of
@@ -404,6 +420,12 @@ __device__ void row_control(RowState<M> &R, int r, int D, const SolveParams &P) 
     nt1 = tn;
     dtn = tn - nt0;
   }
+  // ClipStepSizeController around the PID controller (clip.py:330-389)
+  bool made_jump = false;
+  if (P.controller == GBDX_PID && (P.n_step_ts > 0 || P.n_jump_ts > 0)) {
+    made_jump = clip_next(P, R.dir[r], R.sidx[r], R.jidx[r], nt0, nt1);
+    dtn = nt1 - nt0;
+  }
   if (order_key(nt1) > order_key(R.floor1[r])) {
     nt1 = keep ? R.t1[r] : nt0 + 0.5 * (R.t1[r] - nt0);
     dtn = nt1 - nt0;
@@ -413,8 +435,12 @@ __device__ void row_control(RowState<M> &R, int r, int D, const SolveParams &P) 
   R.tn_old[r] = R.tnext[r];
   if (keep) {
     R.nacc[r]++;
-    R.first[r] = 0;
-    if (P.tape_t) P.tape_t[R.idx[r] * (P.max_steps + 1) + R.nacc[r]] = R.tnext[r];
+    // after a jump the FSAL solvers evaluate the first stage afresh
+    // (runge_kutta.py:684-700)
+    R.first[r] = made_jump ? 1 : 0;
+    if (P.tape_t)
+      *GBDX_AT(P, P.tape_t, R.idx[r] * (P.max_steps + 1) + R.nacc[r], 1,
+               P.batch * (P.max_steps + 1), GBDX_SITE_TAPE_T) = R.tnext[r];
     // Online thinning of the state checkpoints: every accepted step while the
     // slots last, then every 2nd, 4th, ... step.
     if (P.tape_y) {
@@ -509,12 +535,14 @@ __device__ __forceinline__ void load_rows(float (&Y0)[NE], float (&F0)[NE], floa
       Y0[e + 1] = y0[1];
       F0[e] = F0[e + 1] = 0.f;
       if (P.save_t0) {
-        float *o = reinterpret_cast<float *>(P.ys_out) + (i * P.n_save) * D + col;
+        float *o = GBDX_AT(P, reinterpret_cast<float *>(P.ys_out), (i * P.n_save) * D + col, 2,
+                           P.batch * P.n_save * D, GBDX_SITE_YS);
         o[0] = Y0[e];
         o[1] = Y0[e + 1];
       }
       if (P.tape_y) {
-        float *o = P.tape_y + (i * P.checkpoints) * D + col;
+        float *o = GBDX_AT(P, P.tape_y, (i * P.checkpoints) * D + col, 2,
+                           P.batch * P.checkpoints * D, GBDX_SITE_TAPE_Y);
         o[0] = Y0[e];
         o[1] = Y0[e + 1];
       }
@@ -669,8 +697,15 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
           }
           part += __shfl_xor_sync(0xffffffffu, part, 1);
           part += __shfl_xor_sync(0xffffffffu, part, 2);
-          if ((lane & 3) == 0) atomicAdd(&R.acc[row], part);
+          if ((lane & 3) == 0) R.part[row][(warp * SH::TPW + j) % SH::NT] = part;
         }
+      }
+      __syncthreads();
+      if (tid < M && live) {
+        float a = 0.f;
+#pragma unroll
+        for (int n = 0; n < SH::NT; n++) a += R.part[tid][n];
+        R.acc[tid] = a;
       }
     }
     __syncthreads();
@@ -688,7 +723,8 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
             const double tp = R.tp_old[tid], tn = R.tn_old[tid];
             R.theta[tid] = float(tp == tn ? 0.0 : (tsd - tp) / (tn - tp));
             R.sslot[tid] = R.save_index[tid];
-            P.ts_out[R.idx[tid] * P.n_save + R.save_index[tid]] = tsv;
+            *GBDX_AT(P, P.ts_out, R.idx[tid] * P.n_save + R.save_index[tid], 1,
+                     P.batch * P.n_save, GBDX_SITE_TS) = tsv;
             R.ts_index[tid]++;
             R.save_index[tid]++;
             R.sflag[tid] = 1;
@@ -727,8 +763,30 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
           } else {
             v = Y0[e] + th * (Y1[e] - Y0[e]);
           }
-          reinterpret_cast<float *>(P.ys_out)[(R.idx[row] * P.n_save + R.sslot[row]) * D + col] =
-              v;
+          *GBDX_AT(P, reinterpret_cast<float *>(P.ys_out),
+                   (R.idx[row] * P.n_save + R.sslot[row]) * D + col, 1, P.batch * P.n_save * D,
+                   GBDX_SITE_YS) = v;
+        }
+      }
+      __syncthreads();
+    }
+    // ---- SaveAt(steps=n), after the step's ts saves (_integrate.py:492-527),
+    // and SaveAt(dense=True) step times (:529-540) ----------------------------
+    if (P.save_steps > 0 || P.dense_ts) {
+      if (tid < M) {
+        R.stslot[tid] = -1;
+        if (live && R.keep[tid]) {
+          const int64_t i = R.idx[tid];
+          if (P.save_steps > 0 && --R.sdown[tid] == 0) {
+            R.sdown[tid] = P.save_steps;
+            R.stslot[tid] = R.save_index[tid]++;
+            *GBDX_AT(P, P.ts_out, i * P.n_save + R.stslot[tid], 1, P.batch * P.n_save,
+                     GBDX_SITE_TS) = R.dir[tid] * R.tn_old[tid];
+          }
+          // nacc already counts this step
+          if (P.dense_ts)
+            *GBDX_AT(P, P.dense_ts, i * (P.max_steps + 1) + R.nacc[tid], 1,
+                     P.batch * (P.max_steps + 1), GBDX_SITE_DENSE_TS) = R.tn_old[tid];
         }
       }
       __syncthreads();
@@ -739,14 +797,32 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
       int row, col;
       elem_rc<SH>(e, warp, lane, row, col);
       if (R.live[row] && R.keep[row]) {
+        if (R.stslot[row] >= 0)
+          *GBDX_AT(P, reinterpret_cast<float *>(P.ys_out),
+                   (R.idx[row] * P.n_save + R.stslot[row]) * D + col, 1,
+                   P.batch * P.n_save * D, GBDX_SITE_YS) = Y1[e];
+        if (P.dense_info) {
+          // the step's (y0, y1, k_0..k_{S-1}), component col of each
+          constexpr int REC = (2 + S) * D;
+          float *rec = GBDX_AT(P, static_cast<float *>(P.dense_info),
+                               (R.idx[row] * P.max_steps + R.nacc[row] - 1) * REC, REC,
+                               P.batch * P.max_steps * REC, GBDX_SITE_DENSE_INFO);
+          rec[col] = Y0[e];
+          rec[D + col] = Y1[e];
+#pragma unroll
+          for (int j = 0; j < S; j++) rec[(2 + j) * D + col] = K[j][e];
+        }
         Y0[e] = Y1[e];
         if (TB::FSAL) F0[e] = F[e];  // field value of the last stage (FSAL)
         if (SDE) Wb[e] = Wn[e];
         if (P.tape_y && R.cpslot[row] >= 0) {
-          float *base = P.tape_y + R.idx[row] * P.checkpoints * D + col;
+          const int64_t b0 = R.idx[row] * P.checkpoints * D + col;
+          const int64_t ext = P.batch * P.checkpoints * D;
           if (R.cpcompact[row] & 1)
-            for (int s2 = 1; s2 < P.checkpoints / 2; s2++) base[s2 * D] = base[2 * s2 * D];
-          base[R.cpslot[row] * D] = Y0[e];
+            for (int s2 = 1; s2 < P.checkpoints / 2; s2++)
+              *GBDX_AT(P, P.tape_y, b0 + s2 * D, 1, ext, GBDX_SITE_TAPE_Y) =
+                  *GBDX_AT(P, P.tape_y, b0 + 2 * s2 * D, 1, ext, GBDX_SITE_TAPE_Y);
+          *GBDX_AT(P, P.tape_y, b0 + R.cpslot[row] * D, 1, ext, GBDX_SITE_TAPE_Y) = Y0[e];
         }
       }
     }
@@ -761,10 +837,20 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
         int si = R.save_index[tid];
         R.nfill[tid] = (t0 == R.t1[tid]) ? P.n_ts : 0;
         R.sslot[tid] = si;  // first slot written by the element pass
-        for (int m = 0; m < R.nfill[tid]; m++) P.ts_out[i * P.n_save + si + m] = t0 * dir;
+        const int64_t tse = P.batch * P.n_save;
+        for (int m = 0; m < R.nfill[tid]; m++)
+          *GBDX_AT(P, P.ts_out, i * P.n_save + si + m, 1, tse, GBDX_SITE_TS) = t0 * dir;
         si += R.nfill[tid];
-        if (P.save_t1) P.ts_out[i * P.n_save + si++] = R.tprev[tid] * dir;
-        for (int m = si; m < P.n_save; m++) P.ts_out[i * P.n_save + m] = INFINITY;
+        // the t1 value is already saved when SaveAt(steps=n) saved the last
+        // step (_integrate.py:847-877)
+        R.sflag[tid] = P.save_t1 && !(P.save_steps > 0 && R.sdown[tid] == P.save_steps);
+        if (R.sflag[tid])
+          *GBDX_AT(P, P.ts_out, i * P.n_save + si++, 1, tse, GBDX_SITE_TS) = R.tprev[tid] * dir;
+        if (!P.saves_prefilled)
+          for (int m = si; m < P.n_save; m++)  // direction * inf
+            *GBDX_AT(P, P.ts_out, i * P.n_save + m, 1, tse, GBDX_SITE_TS) =
+                dir > 0 ? INFINITY : -INFINITY;
+        if (P.dense_n) P.dense_n[i] = R.nacc[tid] + 1;
         int res = R.result[tid];
         if (res == GBDX_SUCCESSFUL && order_key(R.tprev[tid]) < order_key(R.t1[tid]))
           res = GBDX_MAX_STEPS_REACHED;
@@ -786,12 +872,16 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
         int row, col;
         elem_rc<SH>(e, warp, lane, row, col);
         if (R.fin[row]) {
-          float *o = reinterpret_cast<float *>(P.ys_out) + R.idx[row] * P.n_save * D + col;
+          float *o = reinterpret_cast<float *>(P.ys_out);
+          const int64_t b0 = R.idx[row] * P.n_save * D + col, ext = P.batch * P.n_save * D;
           int si = R.sslot[row];
-          for (int m = 0; m < R.nfill[row]; m++) o[(si + m) * D] = Y0[e];
+          for (int m = 0; m < R.nfill[row]; m++)
+            *GBDX_AT(P, o, b0 + (si + m) * D, 1, ext, GBDX_SITE_YS) = Y0[e];
           si += R.nfill[row];
-          if (P.save_t1) o[(si++) * D] = Y0[e];
-          for (int m = si; m < P.n_save; m++) o[m * D] = INFINITY;
+          if (R.sflag[row]) *GBDX_AT(P, o, b0 + (si++) * D, 1, ext, GBDX_SITE_YS) = Y0[e];
+          if (!P.saves_prefilled)
+            for (int m = si; m < P.n_save; m++)
+              *GBDX_AT(P, o, b0 + m * D, 1, ext, GBDX_SITE_YS) = INFINITY;
         }
       }
       __syncthreads();

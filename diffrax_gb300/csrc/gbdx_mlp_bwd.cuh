@@ -361,7 +361,8 @@ __device__ void bwd_row_init(BwdRows<SH::M> &R, int r, int64_t i, const SolvePar
   R.active[r] = 1;
   R.fin[r] = 0;
   // number of ts saved: those <= t_N (all of them unless max_steps stopped it)
-  const double tN = P.tape_t[i * (P.max_steps + 1) + N];
+  const double tN = *GBDX_AT(P, P.tape_t, i * (P.max_steps + 1) + N, 1,
+                             P.batch * (P.max_steps + 1), GBDX_SITE_TAPE_T);
   int k = 0;
   while (k < P.n_ts && dir * P.save_ts[k] <= tN) k++;
   R.k_hi[r] = k;
@@ -436,17 +437,21 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
         float g = 0.f;
         int slot = (P.save_t0 ? 1 : 0) + R.k_hi[row];
         if (R.N[row] == 0) {
-          for (int m2 = 0; m2 < P.n_ts; m2++) g += gys[(slot + m2) * D];
+          for (int m2 = 0; m2 < P.n_ts; m2++)
+            g += *GBDX_AT(P, gys, (slot + m2) * D, 1, (n_save - 1) * D + 1, GBDX_SITE_GRAD_YS);
           slot += P.n_ts;
         }
-        if (P.save_t1) g += gys[slot * D];
+        if (P.save_t1)
+          g += *GBDX_AT(P, gys, slot * D, 1, (n_save - 1) * D + 1, GBDX_SITE_GRAD_YS);
         GY[e] = g;
         Y[e] = 0.f;
       }
       if (R.ld_kind[row] == kLoadCheckpoint)
-        Y[e] = P.tape_y[(R.idx[row] * P.checkpoints + R.ld_slot[row]) * D + col];
+        Y[e] = *GBDX_AT(P, P.tape_y, (R.idx[row] * P.checkpoints + R.ld_slot[row]) * D + col, 1,
+                        P.batch * P.checkpoints * D, GBDX_SITE_TAPE_Y);
       else if (R.ld_kind[row] == kLoadScratch)
-        Y[e] = Q.scratch[(R.idx[row] * Q.seg_max + R.ld_slot[row]) * D + col];
+        Y[e] = *GBDX_AT(P, Q.scratch, (R.idx[row] * Q.seg_max + R.ld_slot[row]) * D + col, 1,
+                        P.batch * Q.seg_max * D, GBDX_SITE_SCRATCH);
     }
   };
 #pragma unroll
@@ -471,7 +476,8 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
       if (R.active[tid] && (R.mode[tid] == kModeFwd || R.n[tid] >= 0)) {
         R.live[tid] = 1;
         const int j = R.mode[tid] == kModeBwd ? R.n[tid] : R.m[tid];
-        const double *tt = P.tape_t + R.idx[tid] * (P.max_steps + 1);
+        const double *tt = GBDX_AT(P, P.tape_t, R.idx[tid] * (P.max_steps + 1) + j, 2,
+                                   P.batch * (P.max_steps + 1), GBDX_SITE_TAPE_T) - j;
         R.t_lo[tid] = tt[j];
         R.t_hi[tid] = tt[j + 1];
         const double dt = tt[j + 1] - tt[j];
@@ -546,7 +552,8 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
       GY0[e] = 0.f;
       GY1[e] = 0.f;
       if (R.live[row] && R.mode[row] == kModeFwd) {
-        Q.scratch[(R.idx[row] * Q.seg_max + (R.m[row] - R.cs[row])) * D + col] = Y1[e];
+        *GBDX_AT(P, Q.scratch, (R.idx[row] * Q.seg_max + (R.m[row] - R.cs[row])) * D + col, 1,
+                 P.batch * Q.seg_max * D, GBDX_SITE_SCRATCH) = Y1[e];
       } else if (R.live[row]) {
         GY1[e] = GY[e];
       }
@@ -572,7 +579,8 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
         int row, col;
         elem_rc<SH>(e, warp, lane, row, col);
         if (R.sflag[row]) {
-          const float gb = Q.grad_ys[(R.idx[row] * n_save + R.sslot[row]) * D + col];
+          const float gb = *GBDX_AT(P, Q.grad_ys, (R.idx[row] * n_save + R.sslot[row]) * D + col,
+                                    1, P.batch * n_save * D, GBDX_SITE_GRAD_YS);
           float ay0, ay1, gg[7];
           interp_coeffs<SOLVER>(R.theta[row], ay0, ay1, gg);
           GY0[e] = fmaf(ay0, gb, GY0[e]);

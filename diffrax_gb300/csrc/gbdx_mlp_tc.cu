@@ -109,7 +109,7 @@ __device__ void init_row(Row &R, int64_t i, const SolveParams &P) {
   R.active = 1;
   R.at_dtmin = 0;
   if (P.save_t0) {
-    P.ts_out[i * P.n_save] = a * dir;
+    *GBDX_AT(P, P.ts_out, i * P.n_save, 1, P.batch * P.n_save, GBDX_SITE_TS) = a * dir;
     R.save_index = 1;
   }
 }
@@ -364,7 +364,8 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
 #pragma unroll
       for (int n = 0; n < kDH; n++) y[n] = y0[n];
       if (P.save_t0) {
-        float *o = reinterpret_cast<float *>(P.ys_out) + R.idx * P.n_save * kD + col0;
+        float *o = GBDX_AT(P, reinterpret_cast<float *>(P.ys_out), R.idx * P.n_save * kD + col0,
+                           kDH, P.batch * P.n_save * kD, GBDX_SITE_YS);
 #pragma unroll
         for (int n = 0; n < kDH; n++) o[n] = y[n];
       }
@@ -492,8 +493,9 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
         }
       }
       if (!__any_sync(0xffffffffu, pend)) break;
-      float *o = reinterpret_cast<float *>(P.ys_out) +
-                 (R.idx * P.n_save + (pend ? R.save_index : 0)) * kD + col0;
+      float *o = GBDX_AT(P, reinterpret_cast<float *>(P.ys_out),
+                         (R.idx * P.n_save + (pend ? R.save_index : 0)) * kD + col0, kDH,
+                         P.batch * P.n_save * kD, GBDX_SITE_YS);
 #pragma unroll
       for (int c = 0; c < kDH; c += 16) {
         float v[16], kv[16];
@@ -517,7 +519,9 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
         }
       }
       if (pend) {
-        if (part == 0) P.ts_out[R.idx * P.n_save + R.save_index] = tsv;
+        if (part == 0)
+          *GBDX_AT(P, P.ts_out, R.idx * P.n_save + R.save_index, 1, P.batch * P.n_save,
+                   GBDX_SITE_TS) = tsv;
         R.ts_index++;
         R.save_index++;
       }
@@ -556,22 +560,30 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
       const int64_t i = R.idx;
       const int dir = R.dir;
       const double t0 = P.t0[i * P.time_stride] * dir;
-      float *o = reinterpret_cast<float *>(P.ys_out) + i * P.n_save * kD + col0;
+      float *o = reinterpret_cast<float *>(P.ys_out);
+      const int64_t yb = i * P.n_save * kD + col0, ye = P.batch * P.n_save * kD;
+      const int64_t te = P.batch * P.n_save;
       int si = R.save_index;
       if (t0 == R.t1) {
         for (int m = 0; m < P.n_ts; m++, si++) {
-          if (part == 0) P.ts_out[i * P.n_save + si] = t0 * dir;
-          for (int n = 0; n < kDH; n++) o[si * kD + n] = y[n];
+          if (part == 0) *GBDX_AT(P, P.ts_out, i * P.n_save + si, 1, te, GBDX_SITE_TS) = t0 * dir;
+          float *r = GBDX_AT(P, o, yb + si * kD, kDH, ye, GBDX_SITE_YS);
+          for (int n = 0; n < kDH; n++) r[n] = y[n];
         }
       }
       if (P.save_t1) {
-        if (part == 0) P.ts_out[i * P.n_save + si] = R.tprev * dir;
-        for (int n = 0; n < kDH; n++) o[si * kD + n] = y[n];
+        if (part == 0)
+          *GBDX_AT(P, P.ts_out, i * P.n_save + si, 1, te, GBDX_SITE_TS) = R.tprev * dir;
+        float *r = GBDX_AT(P, o, yb + si * kD, kDH, ye, GBDX_SITE_YS);
+        for (int n = 0; n < kDH; n++) r[n] = y[n];
         si++;
       }
       for (int m = si; m < P.n_save; m++) {
-        if (part == 0) P.ts_out[i * P.n_save + m] = dir > 0 ? INFINITY : -INFINITY;
-        for (int n = 0; n < kDH; n++) o[m * kD + n] = INFINITY;
+        if (part == 0)
+          *GBDX_AT(P, P.ts_out, i * P.n_save + m, 1, te, GBDX_SITE_TS) =
+              dir > 0 ? INFINITY : -INFINITY;
+        float *r = GBDX_AT(P, o, yb + m * kD, kDH, ye, GBDX_SITE_YS);
+        for (int n = 0; n < kDH; n++) r[n] = INFINITY;
       }
       if (part == 0) {
         int res = R.result;

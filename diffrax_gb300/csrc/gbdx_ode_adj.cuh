@@ -106,23 +106,27 @@ __global__ void __launch_bounds__(128) ode_rc_bwd_kernel(SolveParams P, AdjParam
   // SaveAt(ts) points the forward reached (all of them unless max_steps
   // stopped it); the t1 save sits in the slot after them.
   int n_saved = 0;
-  const double tN = tt[N];
+  const double tN = *GBDX_AT(P, tt, N, 1, P.max_steps + 1, GBDX_SITE_TAPE_T);
   if (t0 == t1) {
     n_saved = P.n_ts;
     for (int m = 0; m < P.n_ts; m++)
 #pragma unroll
-      for (int n = 0; n < D; n++) gy[n] += G[(P.save_t0 + m) * D + n];
+      for (int n = 0; n < D; n++)
+        gy[n] += GBDX_AT(P, G, (P.save_t0 + m) * D, D, P.n_save * D, GBDX_SITE_GRAD_YS)[n];
   } else {
     while (n_saved < P.n_ts && dir * P.save_ts[n_saved] <= tN) n_saved++;
   }
   if (P.save_t1)
 #pragma unroll
-    for (int n = 0; n < D; n++) gy[n] += G[(P.save_t0 + n_saved) * D + n];
+    for (int n = 0; n < D; n++)
+      gy[n] += GBDX_AT(P, G, (P.save_t0 + n_saved) * D, D, P.n_save * D, GBDX_SITE_GRAD_YS)[n];
   T ys[S][D], k[S][D], kbar[S][D], gy0[D], gy1[D], f[D], dw[D];
   int m_hi = t0 == t1 ? 0 : n_saved;  // saves not yet visited: [0, m_hi)
 #pragma unroll 1
   for (int s = N - 1; s >= 0; s--) {
-    const double ta = tt[s], tb = tt[s + 1];
+    const double *tp = GBDX_AT(P, tt, s, 2, P.max_steps + 1, GBDX_SITE_TAPE_T);
+    const double ta = tp[0], tb = tp[1];
+    const T *tys = GBDX_AT(P, ty, s * D, D, int64_t(P.checkpoints) * D, GBDX_SITE_TAPE_Y);
     const T h = T(dir * (tb - ta));  // the step's control
     if constexpr (F::SDE) {
 #pragma unroll
@@ -142,7 +146,7 @@ __global__ void __launch_bounds__(128) ode_rc_bwd_kernel(SolveParams P, AdjParam
 #pragma unroll
         for (int j = 0; j < st; j++)
           if (TB::a(st, j) != 0.0) inc += T(TB::a(st, j)) * k[j][n];
-        ys[st][n] = ty[s * D + n] + inc;
+        ys[st][n] = tys[n] + inc;
       }
       F::vf(P, a, ys[st], f);
       if constexpr (F::SDE) {
@@ -355,10 +359,12 @@ __global__ void __launch_bounds__(128) ode_bs_kernel(SolveParams P, AdjParams Q)
     const int jn = R.seg[0] > 0 ? R.seg[0] : 0;
     for (int jj = jn; jj < R.jold[0]; jj++)
 #pragma unroll
-      for (int n = 0; n < D; n++) av[n] += G[jj * D + n];
+      for (int n = 0; n < D; n++)
+        av[n] += GBDX_AT(P, G, jj * D, D, P.n_save * D, GBDX_SITE_GRAD_YS)[n];
     if (R.done[0]) break;
 #pragma unroll
-    for (int n = 0; n < D; n++) y[n] = Ys[R.seg[0] * D + n];
+    for (int n = 0; n < D; n++)
+      y[n] = GBDX_AT(P, Ys, R.seg[0] * D, D, P.n_save * D, GBDX_SITE_GRAD_YS)[n];
     R.active[0] = 1;
     bool have_f0 = false;  // made_jump: the segment's first step evaluates f afresh
     while (bs_running(R, 0, P.max_steps)) {

@@ -126,6 +126,63 @@ __device__ __forceinline__ int clip_find(const double *ts, int n, int dir, doubl
   return i;
 }
 
+// ClipStepSizeController.init (clip.py:215-276): the first step ends no
+// later than the first step time after t0, and just before the first jump.
+// sidx / jidx: the trajectory's search hints into step_ts / jump_ts.
+__device__ __forceinline__ double clip_start(const SolveParams &P, int dir, int &sidx,
+                                             int &jidx, double a, double tn) {
+  sidx = jidx = 0;
+  if (P.n_step_ts > 0) {
+    sidx = clip_find(P.step_ts, P.n_step_ts, dir, a, 0);
+    const double st = clip_get(P.step_ts, P.n_step_ts, sidx, dir);
+    if (ckey(st) < ckey(tn)) tn = st;
+  }
+  if (P.n_jump_ts > 0) {
+    jidx = clip_find(P.jump_ts, P.n_jump_ts, dir, a, 0);
+    const double jt = next_down(clip_get(P.jump_ts, P.n_jump_ts, jidx, dir));
+    if (ckey(jt) < ckey(tn)) tn = jt;
+  }
+  return tn;
+}
+
+// ClipStepSizeController.adapt_step_size after the PID controller
+// (clip.py:330-389).  A step that ended at x or just before x, for x a
+// jump time, restarts past x (_bump_next_t0, clip.py:79-99: the sorted
+// times equal to nt0 or to nextafter(nt0) sit just below and at the first
+// index above nt0); the next step ends no later than the next step time and
+// just before the next jump.  Returns made_jump.
+__device__ __forceinline__ bool clip_next(const SolveParams &P, int dir, int &sidx, int &jidx,
+                                          double &nt0, double &nt1) {
+  bool made = false;
+  if (P.n_step_ts > 0) {
+    const int n = P.n_step_ts;
+    const int i = clip_find(P.step_ts, n, dir, nt0, sidx);
+    const double n1 = next_up(nt0);
+    double b0 = nt0;
+    if (i < n && ckey(clip_get(P.step_ts, n, i, dir)) == ckey(n1)) b0 = next_up(n1);
+    if (i > 0 && ckey(clip_get(P.step_ts, n, i - 1, dir)) == ckey(nt0)) b0 = n1;
+    sidx = clip_find(P.step_ts, n, dir, b0, i);
+    const double st = clip_get(P.step_ts, n, sidx, dir);
+    if (ckey(st) < ckey(nt1)) nt1 = st;
+  }
+  if (P.n_jump_ts > 0) {
+    const int n = P.n_jump_ts;
+    const int i = clip_find(P.jump_ts, n, dir, nt0, jidx);
+    const double n1 = next_up(nt0);
+    const bool m1 = i < n && ckey(clip_get(P.jump_ts, n, i, dir)) == ckey(n1);
+    const bool m2 = i > 0 && ckey(clip_get(P.jump_ts, n, i - 1, dir)) == ckey(nt0);
+    if (m1) nt0 = next_up(n1);
+    if (m2) nt0 = n1;
+    made = m1 || m2;
+    const double lo = next_up(nt0);  // never an empty interval (clip.py:354-372)
+    if (ckey(lo) > ckey(nt1)) nt1 = lo;
+    jidx = clip_find(P.jump_ts, n, dir, nt0, i);
+    const double jt = next_down(clip_get(P.jump_ts, n, jidx, dir));
+    if (ckey(jt) < ckey(nt1)) nt1 = jt;
+  }
+  return made;
+}
+
 // LAT selects the form of the FP32 copy of dt for the FP32-state kernels: the
 // hardware conversion (shortest latency; the fused kernel, whose time is set
 // by the step latency of its longest trajectories) or the integer-pipe one
@@ -180,7 +237,11 @@ struct Traj {
   }
 
   __device__ __forceinline__ T *ys_row(const SolveParams &P, int slot) const {
-    return reinterpret_cast<T *>(P.ys_out) + (idx * P.n_save + slot) * D;
+    return GBDX_AT(P, reinterpret_cast<T *>(P.ys_out), (idx * P.n_save + slot) * D, D,
+                   P.batch * P.n_save * D, GBDX_SITE_YS);
+  }
+  __device__ __forceinline__ double *ts_at(const SolveParams &P, int slot) const {
+    return GBDX_AT(P, P.ts_out, idx * P.n_save + slot, 1, P.batch * P.n_save, GBDX_SITE_TS);
   }
 
   __device__ void init(const SolveParams &P, int64_t i) {
@@ -220,6 +281,26 @@ struct Traj {
       t1s = fin ? b : h;
       tn = a + h;
     }
+    // A controller state passed from a previous solve replaces the init
+    // above; its first step is then t0 + dt0, unclipped (dt0=None keeps the
+    // controller's initial step) (_integrate.py:1252-1265).
+    const double *st_in =
+        P.state_in ? GBDX_AT(P, P.state_in, i * int64_t(GBDX_STATE_HEAD + D), GBDX_STATE_HEAD + D,
+                             P.batch * (GBDX_STATE_HEAD + D), GBDX_SITE_STATE)
+                   : nullptr;
+    if (st_in && st_in[4] != 0.0) {
+      if (P.controller == GBDX_PID) {
+        h1 = F32 ? T(log2(st_in[0])) : T(st_in[0]);  // FP32 keeps the log2 domain
+        h2 = F32 ? T(log2(st_in[1])) : T(st_in[1]);
+        at_dtmin = st_in[2] != 0.0;
+        if (P.dt0) tn = a + P.dt0[ti] * dir;
+      } else {
+        sc = int(st_in[0]);
+        nc = int(st_in[1]);
+        t0s = st_in[2];
+        t1s = st_in[3];
+      }
+    }
     tnext = fmin(tn, b);
     dtc = tnext - a;
     pend = false;
@@ -247,6 +328,13 @@ struct Traj {
       }
     }
     first = 1;
+    // a passed solver state (first_step, f0) and made_jump: FSAL solvers
+    // reuse f0 unless first_step or made_jump (runge_kutta.py:684-700)
+    if (st_in && TB::FSAL && st_in[5] == 0.0 && st_in[6] == 0.0) {
+      first = 0;
+#pragma unroll
+      for (int n = 0; n < D; n++) f0[n] = T(st_in[GBDX_STATE_HEAD + n]);
+    }
     save_index = 0;
     ts_index = 0;
     nsteps = nacc = nrej = 0;
@@ -254,8 +342,10 @@ struct Traj {
     if constexpr (FIELD::TAPE) {
       // full gradient tape: the time and state at every accepted step
       if (P.tape_t) {
-        P.tape_t[i * (P.max_steps + 1)] = a;
-        T *o = reinterpret_cast<T *>(P.tape_y) + i * int64_t(P.checkpoints) * D;
+        *GBDX_AT(P, P.tape_t, i * (P.max_steps + 1), 1, P.batch * (P.max_steps + 1),
+                 GBDX_SITE_TAPE_T) = a;
+        T *o = GBDX_AT(P, reinterpret_cast<T *>(P.tape_y), i * int64_t(P.checkpoints) * D, D,
+                       P.batch * P.checkpoints * D, GBDX_SITE_TAPE_Y);
 #pragma unroll
         for (int n = 0; n < D; n++) o[n] = y[n];
       }
@@ -264,14 +354,16 @@ struct Traj {
       T *o = ys_row(P, 0);
 #pragma unroll
       for (int n = 0; n < D; n++) o[n] = y[n];
-      P.ts_out[idx * P.n_save] = a * dir;
+      *ts_at(P, 0) = a * dir;
       save_index = 1;
     }
     if constexpr (XO) {
       sdown = P.save_steps;
       // dense_ts[0] = t0 in the loop's time (_integrate.py:1315-1323); the
       // rest of the buffers was filled with +inf before the launch.
-      if (P.dense_ts) P.dense_ts[i * (P.max_steps + 1)] = a;
+      if (P.dense_ts)
+        *GBDX_AT(P, P.dense_ts, i * (P.max_steps + 1), 1, P.batch * (P.max_steps + 1),
+                 GBDX_SITE_DENSE_TS) = a;
       // Event values at (t0, y0) (_integrate.py:1333-1426): a boolean
       // condition that already holds ends the solve before its first step.
       evi = -1;
@@ -400,58 +492,11 @@ struct Traj {
     return t;
   }
 
-  // ClipStepSizeController.init (clip.py:215-276): the first step ends no
-  // later than the first step time after t0, and just before the first jump.
   __device__ double clip_init(const SolveParams &P, double a, double tn) {
-    sidx = jidx = 0;
-    if (P.n_step_ts > 0) {
-      sidx = clip_find(P.step_ts, P.n_step_ts, dir, a, 0);
-      const double st = clip_get(P.step_ts, P.n_step_ts, sidx, dir);
-      if (ckey(st) < ckey(tn)) tn = st;
-    }
-    if (P.n_jump_ts > 0) {
-      jidx = clip_find(P.jump_ts, P.n_jump_ts, dir, a, 0);
-      const double jt = next_down(clip_get(P.jump_ts, P.n_jump_ts, jidx, dir));
-      if (ckey(jt) < ckey(tn)) tn = jt;
-    }
-    return tn;
+    return clip_start(P, dir, sidx, jidx, a, tn);
   }
-
-  // ClipStepSizeController.adapt_step_size after the PID controller
-  // (clip.py:330-389).  A step that ended at x or just before x, for x a
-  // jump time, restarts past x (_bump_next_t0, clip.py:79-99: the sorted
-  // times equal to nt0 or to nextafter(nt0) sit just below and at the first
-  // index above nt0); the next step ends no later than the next step time and
-  // just before the next jump.  Returns made_jump.
   __device__ __forceinline__ bool clip_adapt(const SolveParams &P, double &nt0, double &nt1) {
-    bool made = false;
-    if (P.n_step_ts > 0) {
-      const int n = P.n_step_ts;
-      const int i = clip_find(P.step_ts, n, dir, nt0, sidx);
-      const double n1 = next_up(nt0);
-      double b0 = nt0;
-      if (i < n && ckey(clip_get(P.step_ts, n, i, dir)) == ckey(n1)) b0 = next_up(n1);
-      if (i > 0 && ckey(clip_get(P.step_ts, n, i - 1, dir)) == ckey(nt0)) b0 = n1;
-      sidx = clip_find(P.step_ts, n, dir, b0, i);
-      const double st = clip_get(P.step_ts, n, sidx, dir);
-      if (ckey(st) < ckey(nt1)) nt1 = st;
-    }
-    if (P.n_jump_ts > 0) {
-      const int n = P.n_jump_ts;
-      const int i = clip_find(P.jump_ts, n, dir, nt0, jidx);
-      const double n1 = next_up(nt0);
-      const bool m1 = i < n && ckey(clip_get(P.jump_ts, n, i, dir)) == ckey(n1);
-      const bool m2 = i > 0 && ckey(clip_get(P.jump_ts, n, i - 1, dir)) == ckey(nt0);
-      if (m1) nt0 = next_up(n1);
-      if (m2) nt0 = n1;
-      made = m1 || m2;
-      const double lo = next_up(nt0);  // never an empty interval (clip.py:354-372)
-      if (ckey(lo) > ckey(nt1)) nt1 = lo;
-      jidx = clip_find(P.jump_ts, n, dir, nt0, i);
-      const double jt = next_down(clip_get(P.jump_ts, n, jidx, dir));
-      if (ckey(jt) < ckey(nt1)) nt1 = jt;
-    }
-    return made;
+    return clip_next(P, dir, sidx, jidx, nt0, nt1);
   }
 
   // One loop iteration.
@@ -818,7 +863,7 @@ struct Traj {
         T *o = ys_row(P, save_index);
 #pragma unroll
         for (int n = 0; n < D; n++) o[n] = interp(th, n, k, y1);
-        P.ts_out[idx * P.n_save + save_index] = tsv;
+        *ts_at(P, save_index) = tsv;
         ts_index++;
         save_index++;
       }
@@ -831,16 +876,18 @@ struct Traj {
             T *o = ys_row(P, save_index);
 #pragma unroll
             for (int n = 0; n < D; n++) o[n] = y1[n];
-            P.ts_out[idx * P.n_save + save_index] = dir > 0 ? tnext : -tnext;
+            *ts_at(P, save_index) = dir > 0 ? tnext : -tnext;
             save_index++;
           }
         }
         // SaveAt(dense=True): the step's end time and (y0, y1, k_0..k_{S-1})
         // (_integrate.py:529-540).
         if (P.dense_ts) {
-          P.dense_ts[idx * (P.max_steps + 1) + nacc + 1] = tnext;
-          T *r = reinterpret_cast<T *>(P.dense_info) +
-                 (idx * P.max_steps + nacc) * int64_t((2 + S) * D);
+          *GBDX_AT(P, P.dense_ts, idx * (P.max_steps + 1) + nacc + 1, 1,
+                   P.batch * (P.max_steps + 1), GBDX_SITE_DENSE_TS) = tnext;
+          T *r = GBDX_AT(P, reinterpret_cast<T *>(P.dense_info),
+                         (idx * P.max_steps + nacc) * int64_t((2 + S) * D), (2 + S) * D,
+                         P.batch * P.max_steps * int64_t((2 + S) * D), GBDX_SITE_DENSE_INFO);
 #pragma unroll
           for (int n = 0; n < D; n++) {
             r[n] = y[n];
@@ -862,8 +909,11 @@ struct Traj {
       }
       if constexpr (FIELD::TAPE) {
         if (P.tape_t) {
-          P.tape_t[idx * (P.max_steps + 1) + nacc + 1] = tnext;
-          T *o = reinterpret_cast<T *>(P.tape_y) + (idx * int64_t(P.checkpoints) + nacc + 1) * D;
+          *GBDX_AT(P, P.tape_t, idx * (P.max_steps + 1) + nacc + 1, 1,
+                   P.batch * (P.max_steps + 1), GBDX_SITE_TAPE_T) = tnext;
+          T *o = GBDX_AT(P, reinterpret_cast<T *>(P.tape_y),
+                         (idx * int64_t(P.checkpoints) + nacc + 1) * D, D,
+                         P.batch * P.checkpoints * D, GBDX_SITE_TAPE_Y);
 #pragma unroll
           for (int n = 0; n < D; n++) o[n] = y1[n];
         }
@@ -940,7 +990,7 @@ struct Traj {
         T *o = ys_row(P, save_index);
 #pragma unroll
         for (int n = 0; n < D; n++) o[n] = y[n];
-        P.ts_out[idx * P.n_save + save_index] = t0 * dir;
+        *ts_at(P, save_index) = t0 * dir;
         save_index++;
       }
     }
@@ -962,7 +1012,7 @@ struct Traj {
       T *o = ys_row(P, save_index);
 #pragma unroll
       for (int n = 0; n < D; n++) o[n] = y[n];
-      P.ts_out[idx * P.n_save + save_index] = tf * dir;
+      *ts_at(P, save_index) = tf * dir;
       save_index++;
     }
     if (!P.saves_prefilled) {
@@ -970,7 +1020,7 @@ struct Traj {
         T *o = ys_row(P, m);
 #pragma unroll
         for (int n = 0; n < D; n++) o[n] = T(INFINITY);
-        P.ts_out[idx * P.n_save + m] = dir > 0 ? INFINITY : -INFINITY;  // direction * inf
+        *ts_at(P, m) = dir > 0 ? INFINITY : -INFINITY;  // direction * inf
       }
     }
     if constexpr (XO) {
@@ -989,6 +1039,30 @@ struct Traj {
     P.stats_out[idx * 3 + 0] = nsteps;
     P.stats_out[idx * 3 + 1] = nacc;
     P.stats_out[idx * 3 + 2] = nrej;
+    if (P.state_out) {
+      // SaveAt(controller_state=, solver_state=, made_jump=) (_integrate.py:
+      // 1489-1500): the record gbdx_fwd_extras documents
+      double *so = GBDX_AT(P, P.state_out, idx * int64_t(GBDX_STATE_HEAD + D),
+                           GBDX_STATE_HEAD + D, P.batch * (GBDX_STATE_HEAD + D),
+                           GBDX_SITE_STATE);
+      if (P.controller == GBDX_PID) {
+        so[0] = F32 ? exp2(double(h1)) : double(h1);
+        so[1] = F32 ? exp2(double(h2)) : double(h2);
+        so[2] = at_dtmin ? 1.0 : 0.0;
+        so[3] = 0.0;
+      } else {
+        so[0] = sc;
+        so[1] = nc;
+        so[2] = t0s;
+        so[3] = t1s;
+      }
+      const bool fsal_valid = TB::FSAL && !first;
+      so[4] = 1.0;
+      so[5] = fsal_valid ? 0.0 : 1.0;
+      so[6] = 0.0;  // made_jump: set by a ClipStepSizeController only
+#pragma unroll
+      for (int n = 0; n < D; n++) so[GBDX_STATE_HEAD + n] = fsal_valid ? double(f0[n]) : 0.0;
+    }
   }
 };
 

@@ -116,8 +116,34 @@ enum gbdx_status {
   GBDX_ERR_INVALID = -1,     /* a ValueError in the reference */
   GBDX_ERR_UNSUPPORTED = -2, /* combination outside this library's scope */
   GBDX_ERR_CUDA = -3,        /* a CUDA runtime error */
-  GBDX_ERR_WORKSPACE = -4    /* workspace too small */
+  GBDX_ERR_WORKSPACE = -4,   /* workspace too small */
+  GBDX_ERR_BOUNDS = -5       /* bounds-checked build: a kernel index left its buffer */
 };
+
+/* Bounds-checked build (libgbdx_bounds.so: the same sources compiled with
+ * -DGBDX_BOUNDS).  Every kernel index into a caller buffer or a workspace
+ * region (saved ys / ts, the checkpoint tape, the dense records, the resume
+ * records, the backward's segment scratch) is checked against the extent the
+ * call defines.  An index outside it records (site, index) -- the first one
+ * of the launch -- and the access goes to a scratch sink in the workspace
+ * instead, so the launch completes.  The call then synchronizes its stream
+ * (unless the stream is capturing a graph) and returns GBDX_ERR_BOUNDS with
+ * the site and index in gbdx_last_error().  The workspace grows by
+ * GBDX_BOUNDS_BYTES.  In the release build gbdx_bounds_checked() is 0 and
+ * no check is compiled. */
+enum gbdx_bounds_site {
+  GBDX_SITE_YS = 1,          /* ys_out */
+  GBDX_SITE_TS = 2,          /* ts_out */
+  GBDX_SITE_TAPE_T = 3,      /* the tape's accepted-step times */
+  GBDX_SITE_TAPE_Y = 4,      /* the tape's checkpoint states */
+  GBDX_SITE_DENSE_TS = 5,    /* dense_ts */
+  GBDX_SITE_DENSE_INFO = 6,  /* dense_info */
+  GBDX_SITE_STATE = 7,       /* state_in / state_out */
+  GBDX_SITE_SCRATCH = 8,     /* the backward's segment recompute states */
+  GBDX_SITE_GRAD_YS = 9      /* grad_ys / the saved ys read by a backward */
+};
+#define GBDX_BOUNDS_BYTES (256 + 65536)
+int gbdx_bounds_checked(void);
 
 /* Problem descriptor.  The leading block is shared with the FP64 oracle's
  * descriptor; the trailing block selects precision and kernels. */
@@ -189,7 +215,27 @@ typedef struct gbdx_fwd_extras {
   /* Event: device int32 [batch], the index of the condition that ended the
    * solve (the reference's event_mask), -1 where none did. */
   int32_t *event_index;
+  /* Resuming a solve (diffeqsolve's solver_state / controller_state /
+   * made_jump inputs and SaveAt(solver_state=, controller_state=,
+   * made_jump=) outputs, diffrax/_integrate.py:1252-1271, 1309, 1489-1500):
+   * device f64 [batch, GBDX_STATE_HEAD + dim] records of
+   *   [0..3] the controller state: PID (prev_inv_scaled_error,
+   *          prev_prev_inv_scaled_error, at_dtmin, 0); ConstantStepSize
+   *          (steps_completed, num_steps, t0, t1 or dt0) in the loop's
+   *          direction-flipped time;
+   *   [4]    1 when [0..3] holds a controller state (state_in: the first step
+   *          is then t0 + dt0 unclipped, or the controller's initial step for
+   *          dt0 = NULL);
+   *   [5]    the solver state's first_step (1: no FSAL value yet);
+   *   [6]    made_jump;
+   *   [7..]  the FSAL value f0 (Tsit5, Dopri5, Dopri8).
+   * state_in resumes from such a record, state_out receives the final one.
+   * Analytic fields without a ClipStepSizeController. */
+  const double *state_in;
+  double *state_out;
 } gbdx_fwd_extras;
+
+#define GBDX_STATE_HEAD 7
 
 typedef struct gbdx_problem gbdx_problem;
 

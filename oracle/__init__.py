@@ -144,6 +144,9 @@ def load():
     lib.orc_solve.restype = ctypes.c_int
     lib.orc_solve_dense.argtypes = lib.orc_solve.argtypes[:-1] + [dp, dp, ip, ip, ctypes.c_int]
     lib.orc_solve_dense.restype = ctypes.c_int
+    lib.orc_solve_state.argtypes = lib.orc_solve.argtypes[:-1] + [dp, dp, ip, ip, dp, dp,
+                                                                  ctypes.c_int]
+    lib.orc_solve_state.restype = ctypes.c_int
     lib.orc_dense_evaluate.argtypes = [ctypes.POINTER(OracleDesc), i64, dp, dp, i64, dp, dp,
                                        dp, ip, i64, dp, i64, ctypes.c_int, ctypes.c_int, dp]
     lib.orc_dense_evaluate.restype = ctypes.c_int
@@ -233,11 +236,17 @@ def clip_times(desc: OracleDesc, ts=None, step_ts=None, jump_ts=None):
     return np.concatenate(parts)
 
 
+STATE_HEAD = 7  # the resume record: 7 + dim doubles per trajectory (gbdx_oracle.c)
+
+
 def solve(desc: OracleDesc, t0, t1, dt0, y0, args=None, params=None, ts=None,
-          nthreads: int = 1, callback=None, step_ts=None, jump_ts=None):
+          nthreads: int = 1, callback=None, step_ts=None, jump_ts=None, state_in=None,
+          want_state=False):
     """Run the oracle.  Returns dict(ys [B,n_save,D], ts [B,n_save], result [B],
     stats [B,3] = (num_steps, num_accepted, num_rejected)).  step_ts / jump_ts
-    wrap the PID controller in ClipStepSizeController (clip.py)."""
+    wrap the PID controller in ClipStepSizeController (clip.py).  state_in
+    [B, STATE_HEAD + D] resumes from a previous solve's record; want_state
+    returns this solve's final record as "state"."""
     lib = load()
     if step_ts is not None or jump_ts is not None:
         ts = clip_times(desc, ts, step_ts, jump_ts)
@@ -268,20 +277,26 @@ def solve(desc: OracleDesc, t0, t1, dt0, y0, args=None, params=None, ts=None,
         keep = cb = VF_CB(_cb)
     ip = ctypes.POINTER(ctypes.c_int32)
     ev = np.full(B, -1, dtype=np.int32) if desc.n_event else None
-    rc = lib.orc_solve_dense(ctypes.byref(desc), B, _dptr(t0), _dptr(t1), _dptr(dt0), tstride,
+    st_in = None if state_in is None else np.ascontiguousarray(
+        np.asarray(state_in, dtype=np.float64).reshape(B, STATE_HEAD + desc.dim))
+    st_out = np.empty((B, STATE_HEAD + desc.dim)) if want_state else None
+    rc = lib.orc_solve_state(ctypes.byref(desc), B, _dptr(t0), _dptr(t1), _dptr(dt0), tstride,
                              _dptr(y0), _dptr(args_arr), astride, _dptr(params), _dptr(ts), cb,
                              None, _dptr(ys), _dptr(ts_out), res.ctypes.data_as(ip),
                              stats.ctypes.data_as(ip),
                              _dptr(dense["ts"]) if dense else None,
                              _dptr(dense["info"]) if dense else None,
                              dense["n"].ctypes.data_as(ip) if dense else None,
-                             ev.ctypes.data_as(ip) if ev is not None else None, int(nthreads))
+                             ev.ctypes.data_as(ip) if ev is not None else None,
+                             _dptr(st_in), _dptr(st_out), int(nthreads))
     del keep
     if rc != 0:
         raise ValueError(f"oracle rejected the problem (code {rc})")
     out = dict(ys=ys, ts=ts_out, result=res, stats=stats)
     if ev is not None:
         out["event_index"] = ev
+    if st_out is not None:
+        out["state"] = st_out
     if dense:
         out.update(dense_ts=dense["ts"], dense_info=dense["info"], dense_n=dense["n"])
     return out

@@ -1223,7 +1223,17 @@ typedef struct {
   int32_t *dense_n;
   /* Event: the index of the condition that ended the solve, -1 if none [B] */
   int32_t *event_index;
+  /* Resuming (_integrate.py:1252-1271, 1489-1500): per trajectory a record
+   * of ORC_STATE_HEAD + dim doubles -- the controller state (PID: prev_inv,
+   * prev_prev_inv, at_dtmin, 0; constant: steps_completed, num_steps, t0,
+   * t1 or dt0, in the direction-flipped time), whether a controller state is
+   * given, the solver state's first_step, made_jump, and the FSAL value f0.
+   * state_in NULL: a fresh solve; state_out NULL: not reported. */
+  const double *state_in;
+  double *state_out;
 } SolveIO;
+
+#define ORC_STATE_HEAD 7
 
 /* A record of one accepted step, kept for the discretise-then-optimise VJP. */
 typedef struct {
@@ -1309,6 +1319,23 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
     cs.t0_sim = t0; cs.t1_sim = isfinite(t1) ? t1 : dt0;
     tnext = t0 + dt0;
   }
+  /* a passed controller state replaces the controller's init; the first
+   * step is then t0 + dt0, unclipped (dt0=None keeps the initial step) */
+  const double *st_in = io->state_in ? io->state_in + bidx * (int64_t)(ORC_STATE_HEAD + D)
+                                     : NULL;
+  if (st_in && st_in[4] != 0.0) {
+    if (d->controller == ORC_PID) {
+      cs.prev_inv = st_in[0];
+      cs.prev_prev_inv = st_in[1];
+      cs.at_dtmin = st_in[2] != 0.0;
+      if (has_dt0) tnext = t0 + dt0;
+    } else {
+      cs.steps_completed = (int)st_in[0];
+      cs.num_steps = (int)st_in[1];
+      cs.t0_sim = st_in[2];
+      cs.t1_sim = st_in[3];
+    }
+  }
   tnext = tnext < t1 ? tnext : t1;
   double tprev = t0;
   double t1_clip_floor = t1;
@@ -1336,6 +1363,13 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
   int made_jump = 0; /* _integrate.py:1309, 425 */
   double f0[64];
   memset(f0, 0, sizeof f0);
+  if (st_in) { /* a passed solver state and made_jump */
+    made_jump = st_in[6] != 0.0;
+    if (tab->fsal && st_in[5] == 0.0) {
+      first_step = 0;
+      memcpy(f0, st_in + ORC_STATE_HEAD, sizeof(double) * D);
+    }
+  }
   int result = ORC_SUCCESSFUL;
   int num_steps = 0, num_acc = 0, num_rej = 0;
   StepOut so;
@@ -1484,6 +1518,19 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
   }
   if (result == ORC_SUCCESSFUL && tprev < t1) result = ORC_MAX_STEPS_REACHED;
   for (int i = 0; i < n_save; i++) tso[i] *= dir;
+  if (io->state_out) { /* SaveAt(controller_state, solver_state, made_jump) */
+    double *so_ = io->state_out + bidx * (int64_t)(ORC_STATE_HEAD + D);
+    if (d->controller == ORC_PID) {
+      so_[0] = cs.prev_inv; so_[1] = cs.prev_prev_inv; so_[2] = cs.at_dtmin; so_[3] = 0.0;
+    } else {
+      so_[0] = cs.steps_completed; so_[1] = cs.num_steps; so_[2] = cs.t0_sim; so_[3] = cs.t1_sim;
+    }
+    const int fsal_valid = tab->fsal && !first_step;
+    so_[4] = 1.0;
+    so_[5] = fsal_valid ? 0.0 : 1.0;
+    so_[6] = made_jump;
+    for (int n = 0; n < D; n++) so_[ORC_STATE_HEAD + n] = fsal_valid ? f0[n] : 0.0;
+  }
   io->result[bidx] = result;
   if (io->dense_n) io->dense_n[bidx] = num_acc + 1;
   if (io->event_index) io->event_index[bidx] = ev_idx;
@@ -1494,6 +1541,14 @@ static void solve_one(const SolveIO *io, int64_t bidx, Tape *tape) {
 
 static void validate_desc(const orc_desc *d) { (void)d; init_tableaus(); }
 
+int orc_solve_state(const orc_desc *d, int64_t B, const double *t0, const double *t1,
+                    const double *dt0, int64_t time_stride, const double *y0,
+                    const double *args, int64_t args_stride, const double *params,
+                    const double *ts, orc_vf_cb cb, void *cb_ctx, double *ys_out,
+                    double *ts_out, int32_t *result, int32_t *stats, double *dense_ts,
+                    double *dense_info, int32_t *dense_n, int32_t *event_index,
+                    const double *state_in, double *state_out, int nthreads);
+
 int orc_solve_dense(const orc_desc *d, int64_t B, const double *t0, const double *t1,
                     const double *dt0, int64_t time_stride, const double *y0,
                     const double *args, int64_t args_stride, const double *params,
@@ -1501,6 +1556,19 @@ int orc_solve_dense(const orc_desc *d, int64_t B, const double *t0, const double
                     double *ts_out, int32_t *result, int32_t *stats, double *dense_ts,
                     double *dense_info, int32_t *dense_n, int32_t *event_index,
                     int nthreads) {
+  return orc_solve_state(d, B, t0, t1, dt0, time_stride, y0, args, args_stride, params, ts, cb,
+                         cb_ctx, ys_out, ts_out, result, stats, dense_ts, dense_info, dense_n,
+                         event_index, NULL, NULL, nthreads);
+}
+
+/* orc_solve_dense with the resume records (SolveIO.state_in / state_out). */
+int orc_solve_state(const orc_desc *d, int64_t B, const double *t0, const double *t1,
+                    const double *dt0, int64_t time_stride, const double *y0,
+                    const double *args, int64_t args_stride, const double *params,
+                    const double *ts, orc_vf_cb cb, void *cb_ctx, double *ys_out,
+                    double *ts_out, int32_t *result, int32_t *stats, double *dense_ts,
+                    double *dense_info, int32_t *dense_n, int32_t *event_index,
+                    const double *state_in, double *state_out, int nthreads) {
   validate_desc(d);
   if (d->dim > 64 || d->dim < 1) return -1;
   if (d->save_steps < 0) return -1;
@@ -1513,9 +1581,10 @@ int orc_solve_dense(const orc_desc *d, int64_t B, const double *t0, const double
   if (ORC_IS_SRK(d->solver) && (d->diffusion == ORC_DIFF_NONE || !d->levy_area)) return -1;
   /* pid.py:437-447: adaptive steps need an error estimate */
   if (d->controller == ORC_PID && d->solver == ORC_SEA) return -1;
+  if ((state_in || state_out) && (d->n_step_ts || d->n_jump_ts)) return -2;
   SolveIO io = {d, t0, t1, dt0, time_stride, y0, args, args_stride, params, ts,
                 cb, cb_ctx, ys_out, ts_out, result, stats, dense_ts, dense_info, dense_n,
-                event_index};
+                event_index, state_in, state_out};
 #ifdef _OPENMP
   if (nthreads > 0 && d->field != ORC_CALLBACK) {
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)

@@ -99,8 +99,14 @@ def test_host_checks():
 def test_saveat_validation():
     with pytest.raises(ValueError):
         dfx.SaveAt()
-    with pytest.raises(NotImplementedError):
-        dfx.SaveAt(t1=True, solver_state=True)
+    s = dfx.SaveAt(t1=True, solver_state=True)
+    assert s.solver_state and not s.controller_state and not s.state_only
+    assert dfx.SaveAt(made_jump=True).state_only
+    # the states alone still save one point internally (the final state)
+    f = dfx.lower(dfx.ODETerm(dfx.VanDerPol()), dfx.Dopri5(), dfx.ConstantStepSize(),
+                  dfx.SaveAt(controller_state=True), dim=2, dtype=torch.float32,
+                  max_steps=8, n_ts=0)
+    assert f["save_t1"] == 1
 
 
 def test_backsolve_kwargs_validation():
@@ -349,15 +355,28 @@ def test_sde_extended_output_scope():
                           max_steps=64, n_ts=0, event=event)
             p = _lib.Problem(f)
             assert p.n_save == (32 if saveat.steps else (0 if saveat.dense else 1))
-    W = [torch.zeros(8, 4), torch.zeros(8, 8), torch.zeros(4, 8)]
-    b = [torch.zeros(8), torch.zeros(8), torch.zeros(4)]
-    bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (4,), key=0)
+    # the MLP SDE: step saves, dense steps and the clip controller on the fused
+    # kernel; not events, nor the plain or tensor-core kernels
+    W = [torch.zeros(64, 32), torch.zeros(64, 64), torch.zeros(32, 64)]
+    b = [torch.zeros(64), torch.zeros(64), torch.zeros(32)]
+    bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (32,), key=0)
     terms = dfx.MultiTerm(dfx.ODETerm(dfx.MLPField(W, b)),
-                          dfx.ControlTerm(dfx.TanhDiagonalDiffusion(torch.zeros(4, 4),
-                                                                    torch.zeros(4)), bm))
-    f = dfx.lower(terms, dfx.Heun(), dfx.ConstantStepSize(), dfx.SaveAt(steps=2, t1=True),
-                  dim=4, dtype=torch.float32, max_steps=64, n_ts=0)
-    with pytest.raises(_lib.GbdxError, match="Ornstein-Uhlenbeck SDE"):
+                          dfx.ControlTerm(dfx.TanhDiagonalDiffusion(torch.zeros(32, 32),
+                                                                    torch.zeros(32)), bm))
+    for saveat in (dfx.SaveAt(steps=2, t1=True), dfx.SaveAt(dense=True)):
+        f = dfx.lower(terms, dfx.Heun(), dfx.ConstantStepSize(), saveat, dim=32,
+                      dtype=torch.float32, max_steps=64, n_ts=0)
+        assert _lib.Problem(f).n_save == (32 if saveat.steps else 0)
+        with pytest.raises(_lib.GbdxError, match="fused kernel"):
+            _lib.Problem(dict(f, kernel=1))
+    f = dfx.lower(terms, dfx.Heun(), dfx.ClipStepSizeController(pid, step_ts=[0.5]),
+                  dfx.SaveAt(t1=True), dim=32, dtype=torch.float32, max_steps=64, n_ts=0)
+    assert _lib.Problem(f).n_save == 1
+    with pytest.raises(_lib.GbdxError, match="fused kernel"):
+        _lib.Problem(dict(f, kernel=3))
+    f = dfx.lower(terms, dfx.Heun(), pid, dfx.SaveAt(t1=True), dim=32, dtype=torch.float32,
+                  max_steps=64, n_ts=0, event=dfx.Event(dfx.steady_state_event()))
+    with pytest.raises(_lib.GbdxError, match="all but events"):
         _lib.Problem(f)
 
 
@@ -386,3 +405,23 @@ def test_autotune_cache_round_trip(tmp_path, monkeypatch):
     assert _tune.load_cache(path, "GPU-A") == 2
     open(path, "w").write("{not json")
     assert _tune.load_cache(path, "GPU-A") == 0
+
+
+def test_release_build_has_no_bounds_checks():
+    # GBDX_BOUNDS=1 would select libgbdx_bounds.so (covered on the GPU)
+    assert _lib.load().gbdx_bounds_checked() == (1 if _lib.bounds_requested() else 0)
+
+
+def test_bounds_checked_abi_compiles():
+    """The bounds-checked boundary (workspace area, record reset and report)
+    compiles; the kernels' checks are compiled and run by the GPU test."""
+    import subprocess
+    from diffrax_gb300 import _build
+    obj = os.path.join(os.environ.get("TMPDIR", "/tmp"), f"gbdx_abi_bounds_{os.getpid()}.o")
+    src = os.path.join(ROOT, "diffrax_gb300", "csrc", "gbdx_abi.cu")
+    cmd = [_build.nvcc()] + _build.NVCC_FLAGS + ["-DGBDX_BOUNDS", "-I",
+                                                 os.path.join(ROOT, "include"), "-c", src,
+                                                 "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    os.unlink(obj)

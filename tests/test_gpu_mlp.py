@@ -211,3 +211,23 @@ def test_neural_sde_bf16_error_level():
     err = per_traj_err(sol, r)
     print(f"neural SDE bf16: median rel err {np.median(err):.2e} max {err.max():.2e}")
     assert err.max() < 1e-4
+
+
+@pytest.mark.parametrize("widths", [[64, 128, 128, 64], [64, 256, 256, 64]])
+def test_mlp_adaptive_solve_is_deterministic(widths):
+    # the PID error norm sums its per-tile partials in a fixed order, so
+    # repeated solves give bit-identical saves and step counts
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(31)
+    Ws, bs = mlp_params(widths, 9, bias_scale=0.1)
+    field = dfx.MLPField([torch.tensor(W, dtype=torch.float32, device=dev) for W in Ws],
+                         [torch.tensor(b, dtype=torch.float32, device=dev) for b in bs])
+    y0 = torch.tensor(rng.standard_normal((1024, 64)), dtype=torch.float32, device=dev)
+    t1 = torch.tensor(rng.uniform(0.5, 2.0, 1024), dtype=torch.float64, device=dev)
+    runs = [dfx.diffeqsolve(dfx.ODETerm(field), dfx.Tsit5(), 0.0, t1, None, y0,
+                            saveat=dfx.SaveAt(ts=[0.25, 0.5], t1=True),
+                            stepsize_controller=dfx.PIDController(rtol=1e-5, atol=1e-7))
+            for _ in range(3)]
+    for r in runs[1:]:
+        assert torch.equal(r.ys, runs[0].ys)
+        assert torch.equal(r.stats["num_steps"], runs[0].stats["num_steps"])

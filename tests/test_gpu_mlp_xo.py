@@ -1,0 +1,181 @@
+"""SaveAt(steps=n), SaveAt(dense=True) and ClipStepSizeController on the MLP
+fields (the fused MLP integrator) against the FP64 oracle on the same inputs
+(diffrax/_integrate.py:492-540, 847-877, 1273-1323;
+diffrax/_global_interpolation.py:315-393; _step_size_controller/clip.py).
+
+With constant steps both precisions (FP32 parity mode, three-piece BF16)
+take the oracle's steps and must reproduce its step saves, step times and
+interpolated values to FP32 accuracy.  Adaptive solves run at a tolerance
+well above FP32 rounding, where the FP32 controller takes the oracle's step
+counts (its step sizes differ by the FP32 rounding of the factors).
+"""
+import numpy as np
+import pytest
+import torch
+
+import diffrax_gb300 as dfx
+import oracle as O
+from test_gpu_mlp import mlp_params, flat, sde_setup
+
+pytestmark = pytest.mark.gpu
+
+
+def mlp_pair(widths, solver, controller, saveat, t1, dt0, y0, precision, seed=0,
+             diffusion=None, bm=None, max_steps=256, step_ts=None, jump_ts=None):
+    dev = torch.device("cuda")
+    Ws, bs = mlp_params(widths, seed, bias_scale=0.1)
+    Ws = [W.astype(np.float32).astype(np.float64) for W in Ws]
+    bs = [b.astype(np.float32).astype(np.float64) for b in bs]
+    field = dfx.MLPField([torch.tensor(W, dtype=torch.float32, device=dev) for W in Ws],
+                         [torch.tensor(b, dtype=torch.float32, device=dev) for b in bs],
+                         precision=precision)
+    params = flat(Ws, bs)
+    if diffusion is not None:
+        Wsig, bsig = diffusion
+        terms = dfx.MultiTerm(dfx.ODETerm(field), dfx.ControlTerm(
+            dfx.TanhDiagonalDiffusion(torch.tensor(Wsig, dtype=torch.float32, device=dev),
+                                      torch.tensor(bsig, dtype=torch.float32, device=dev)),
+            bm))
+        params = np.concatenate([params, Wsig.reshape(-1), bsig])
+    else:
+        terms = dfx.ODETerm(field)
+    sol = dfx.diffeqsolve(terms, solver, 0.0, t1, dt0,
+                          torch.tensor(y0, dtype=torch.float32, device=dev), saveat=saveat,
+                          stepsize_controller=controller, max_steps=max_steps, throw=False)
+    torch.cuda.synchronize()
+    fields = dfx.lower(terms, solver, controller, saveat, dim=y0.shape[1],
+                       dtype=torch.float32, max_steps=max_steps, n_ts=0)
+    d = O.make_desc(**O.oracle_fields(fields))
+    r = O.solve(d, 0.0, t1, dt0, y0, params=params, nthreads=8, step_ts=step_ts,
+                jump_ts=jump_ts)
+    return sol, r, d
+
+
+def compare_rows(sol, r, tol, ts_tol=1e-12):
+    """Trajectories with the oracle's step counts (at least 95 %): saved ys
+    within tol and ts within ts_tol of the row's largest value, the same
+    +inf padding."""
+    same = sol.stats["num_accepted_steps"].cpu().numpy() == r["stats"][:, 1]
+    assert same.mean() >= 0.95, f"only {same.mean():.3f} took the oracle's steps"
+    ys = sol.ys.cpu().double().numpy()[same]
+    ts = sol.ts.cpu().numpy()[same]
+    ry, rt = r["ys"][same], r["ts"][same]
+    assert np.array_equal(np.isfinite(ys), np.isfinite(ry))
+    assert np.array_equal(np.isfinite(ts), np.isfinite(rt))
+    fin = np.isfinite(rt)
+    assert np.abs(ts[fin] - rt[fin]).max() <= ts_tol * np.abs(rt[fin]).max()
+    fy = np.isfinite(ry)
+    err = np.abs(ys[fy] - ry[fy]).max() / np.abs(ry[fy]).max()
+    print(f"steps equal {same.mean():.3f}, max rel err {err:.2e}")
+    assert err < tol
+    return same
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+@pytest.mark.parametrize("solver", ["tsit5", "dopri5"])
+@pytest.mark.parametrize("steps", [1, 3])
+def test_mlp_saveat_steps_matches_oracle(steps, solver, precision):
+    # 64 -> 128 -> 128 -> 64, ConstantStepSize dt 0.05 on [0, 1] (20 steps):
+    # every (steps=1) or every 3rd step saved, then t1 unless a step save
+    # already holds it; max_steps 64 leaves +inf slots
+    rng = np.random.default_rng(21)
+    y0 = rng.standard_normal((192, 64))
+    solver = {"tsit5": dfx.Tsit5(), "dopri5": dfx.Dopri5()}[solver]
+    sol, r, _ = mlp_pair([64, 128, 128, 64], solver, dfx.ConstantStepSize(),
+                         dfx.SaveAt(steps=steps, t1=True), 1.0, 0.05, y0, precision, seed=3,
+                         max_steps=64)
+    assert sol.ys.shape == r["ys"].shape
+    compare_rows(sol, r, 5e-6)
+
+
+def test_mlp_wide_saveat_steps_and_dense_match_oracle():
+    # 64 -> 256 -> 256 -> 64, Dopri5, dt 0.1 on [0, 1]: step saves and the
+    # dense interpolation (value and derivative) at 33 times
+    rng = np.random.default_rng(22)
+    y0 = rng.standard_normal((128, 64))
+    sol, r, d = mlp_pair([64, 256, 256, 64], dfx.Dopri5(), dfx.ConstantStepSize(),
+                         dfx.SaveAt(steps=2, t1=True, dense=True), 1.0, 0.1, y0, "fp32",
+                         seed=4, max_steps=32)
+    compare_rows(sol, r, 5e-6)
+    q = np.linspace(0.0, 1.0, 33)
+    ev = sol.evaluate(torch.tensor(q, dtype=torch.float64, device="cuda")).cpu().double()
+    rq = O.dense_evaluate(d, 0.0, 1.0, y0, r, q)
+    err = np.abs(ev.numpy() - rq).max() / np.abs(rq).max()
+    print(f"dense evaluation max rel err {err:.2e}")
+    assert err < 5e-6
+    dv = sol.derivative(torch.tensor(q, dtype=torch.float64, device="cuda")).cpu().double()
+    rd = O.dense_evaluate(d, 0.0, 1.0, y0, r, q, order=1)
+    errd = np.abs(dv.numpy() - rd).max() / np.abs(rd).max()
+    print(f"dense derivative max rel err {errd:.2e}")
+    assert errd < 5e-5
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_mlp_adaptive_step_saves(precision):
+    # Tsit5 + PID(1e-3, 1e-4) on [0, 3], a tolerance well above FP32 rounding
+    # (the FP32 controller then takes the FP64 oracle's step counts): every
+    # accepted step saved, the padding, the t1 rule; the step times agree to
+    # the FP32 rounding of the step-size factors, the values to the tolerance
+    rng = np.random.default_rng(27)
+    y0 = rng.standard_normal((128, 64))
+    sol, r, _ = mlp_pair([64, 128, 128, 64], dfx.Tsit5(),
+                         dfx.PIDController(rtol=1e-3, atol=1e-4), dfx.SaveAt(steps=1, t1=True),
+                         3.0, None, y0, precision, seed=1)
+    n = sol.stats["num_accepted_steps"].cpu().numpy()
+    fin = np.isfinite(sol.ts.cpu().numpy()).sum(axis=1)
+    assert np.array_equal(fin, n)  # steps=1 saves every step; t1 is the last one
+    compare_rows(sol, r, 1e-2, ts_tol=1e-4)
+
+
+def test_mlp_dense_is_consistent_with_step_saves_bf16():
+    # the dense record at an accepted step's end time reproduces that step's
+    # saved value (both written by the same kernel from the same registers)
+    rng = np.random.default_rng(23)
+    y0 = rng.standard_normal((256, 64))
+    ctrl = dfx.PIDController(rtol=1e-5, atol=1e-7)
+    sol, _, _ = mlp_pair([64, 128, 128, 64], dfx.Tsit5(), ctrl,
+                         dfx.SaveAt(steps=1, dense=True), 1.0, None, y0, "bf16", seed=5)
+    ts = sol.ts.clone()
+    ok = torch.isfinite(ts)
+    ts[~ok] = 0.0
+    ev = sol.evaluate(ts)  # [B, Q, D] at each trajectory's own step times
+    diff = (ev - sol.ys)[ok]
+    assert float(diff.abs().max()) <= 1e-6 * float(sol.ys[ok].abs().max())
+
+
+def test_neural_sde_saveat_steps_matches_oracle():
+    # drift 32 -> 64 -> 64 -> 32, diffusion 0.1 tanh(W y + b), Heun dt 0.05,
+    # the same Brownian path: every 2nd step saved
+    rng = np.random.default_rng(24)
+    y0 = rng.standard_normal((128, 32))
+    bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (32,), key=77)
+    sol, r, _ = mlp_pair([32, 64, 64, 32], dfx.Heun(), dfx.ConstantStepSize(),
+                         dfx.SaveAt(steps=2, t1=True), 1.0, 0.05, y0, "fp32", seed=6,
+                         diffusion=sde_setup(25), bm=bm)
+    assert sol.ys.shape[1] == 128  # max_steps / 2 slots, t1 already a step save
+    compare_rows(sol, r, 1e-4)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_mlp_clip_controller_matches_oracle(precision):
+    # Tsit5 + ClipStepSizeController(PID(1e-3, 1e-4), step_ts, jump_ts) on
+    # the 64 -> 128 -> 128 -> 64 field over [0, 3], every step saved: the step
+    # times hit every step_ts exactly, end just before each jump and restart
+    # past it; the step counts are the oracle's
+    rng = np.random.default_rng(26)
+    y0 = rng.standard_normal((160, 64))
+    step_ts = np.array([0.3, 0.75, 1.5, 2.25])
+    jump_ts = np.array([1.0, 2.0])
+    ctrl = dfx.ClipStepSizeController(dfx.PIDController(rtol=1e-3, atol=1e-4),
+                                      step_ts=step_ts, jump_ts=jump_ts)
+    sol, r, _ = mlp_pair([64, 128, 128, 64], dfx.Tsit5(), ctrl, dfx.SaveAt(steps=1), 3.0,
+                         None, y0, precision, seed=8, step_ts=step_ts, jump_ts=jump_ts)
+    same = compare_rows(sol, r, 1e-2, ts_tol=1e-4)
+    ts = sol.ts.cpu().numpy()
+    for row in range(ts.shape[0]):
+        t = ts[row][np.isfinite(ts[row])]
+        for st in step_ts:
+            assert st in t
+        for jt in jump_ts:
+            assert np.nextafter(jt, -np.inf) in t
+    assert np.array_equal(sol.stats["num_steps"].cpu().numpy()[same], r["stats"][same, 0])
