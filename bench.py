@@ -399,7 +399,11 @@ def workload_next_rows(dev, flush, steps, warmup):
     2.5, 5, 7.5), Event(x crosses 0 upwards, Newton(1e-5, 1e-5) root), Dopri8.
     SDE rows: Ornstein-Uhlenbeck dim 2 (theta 1.5, mu 0.5, sigma 0.6) on
     [0, 1], dt 0.01, tree tol 1e-3, batch 16384: Heun on the W-only tree,
-    Heun / ShARK / SRA1 / SEA on the space-time Levy area tree."""
+    Heun / ShARK / SRA1 / SEA on the space-time Levy area tree.
+    MLP rows: the neural-ODE field (64 -> 128 -> 128 -> 64), Tsit5 + PID(1e-5,
+    1e-7), batch 8192: SaveAt(steps=1), SaveAt(dense=True), the clip
+    controller, a linear event with Newton root finding (final values against
+    the oracle on 64 trajectories)."""
     import torch
     import diffrax_gb300 as dfx
     import oracle as O
@@ -413,7 +417,8 @@ def workload_next_rows(dev, flush, steps, warmup):
     mu_d = torch.tensor(mu[:, None], dtype=torch.float32, device=dev)
     pid = dfx.PIDController(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4)
     term = dfx.ODETerm(dfx.VanDerPol())
-    out = {"workload": "vdp_dopri5_pid_t10_b16384 and ou_sde_dt0.01_b16384",
+    out = {"workload": "vdp_dopri5_pid_t10_b16384, ou_sde_dt0.01_b16384 and "
+                       "neural_ode_64_128_b8192",
            "ode": {}, "sde": {}}
 
     def ode_row(solver, saveat, ctrl, event=None):
@@ -510,6 +515,58 @@ def workload_next_rows(dev, flush, steps, warmup):
             sde_base = ms
         row["time_over_heun_w_tree"] = ms / sde_base
         out["sde"][name] = row
+
+    # MLP rows: the neural-ODE field 64 -> 128 -> 128 -> 64 (BF16 weights,
+    # three-piece operands), Tsit5 + PID(1e-5, 1e-7) on [0, 1], batch 8192
+    Bm, n_m = 8192, 64
+    Ws, bs = _mlp_np([64, 128, 128, 64], 21)
+    field = dfx.MLPField([torch.tensor(W, dtype=torch.float32, device=dev) for W in Ws],
+                         [torch.tensor(b, dtype=torch.float32, device=dev) for b in bs])
+    params = np.concatenate([np.concatenate([W.reshape(-1), b]) for W, b in zip(Ws, bs)])
+    ym = rng.standard_normal((Bm, 64)).astype(np.float32).astype(np.float64)
+    ym_d = torch.tensor(ym, dtype=torch.float32, device=dev)
+    pidm = dfx.PIDController(rtol=1e-5, atol=1e-7)
+    mterm = dfx.ODETerm(field)
+    out["mlp"] = {"workload": "neural_ode_64_128_tsit5_pid_b8192"}
+    mbase = None
+    for name, saveat, ctrl, event in (
+            ("base_saveat_t1", dfx.SaveAt(t1=True), pidm, None),
+            ("saveat_steps1", dfx.SaveAt(steps=1, t1=True), pidm, None),
+            ("saveat_dense", dfx.SaveAt(dense=True, t1=True), pidm, None),
+            ("clip_controller", dfx.SaveAt(t1=True),
+             dfx.ClipStepSizeController(pidm, step_ts=np.linspace(0.0, 1.0, 11),
+                                        jump_ts=np.array([0.5])), None),
+            ("event_linear_newton", dfx.SaveAt(t1=True), pidm,
+             dfx.Event(dfx.LinearCondition([1.0, 0.5], offset=-0.25),
+                       dfx.Newton(1e-5, 1e-5)))):
+        low = Lowered(mterm, dfx.Tsit5(), 0.0, 1.0, None, ym_d, None, saveat, ctrl, None, 256,
+                      "fused", 0, 0, event=event)
+        ex = saveat.dense or event is not None
+        run = low.run_forward_ex if ex else low.run_forward
+        ms = _events_time(run, steps, warmup, flush)
+        outs = run()
+        kw = {}
+        if isinstance(ctrl, dfx.ClipStepSizeController):
+            kw = dict(step_ts=ctrl.step_ts, jump_ts=ctrl.jump_ts)
+        r = O.solve(O.make_desc(**O.oracle_fields(low.fields)), 0.0, 1.0, None, ym[:n_m],
+                    params=params, nthreads=cores, **kw)
+        k = np.isfinite(outs[1][:n_m].cpu().numpy()).sum(axis=1) - 1
+        last = outs[0][:n_m].double().cpu().numpy()[np.arange(n_m), k]
+        kr = np.isfinite(r["ts"]).sum(axis=1) - 1
+        ref = r["ys"][np.arange(n_m), kr]
+        e = np.abs(last - ref).max(axis=1) / np.abs(ref).max()
+        row = {"traj_per_s": Bm / (ms / 1e3), "ms": ms,
+               "mean_attempted_steps": float(outs[3][:, 0].float().mean().item()),
+               "final_rel_err_vs_fp64_oracle": {"median": float(np.median(e)),
+                                                "max": float(e.max())}}
+        if mbase is None:
+            mbase = ms
+        row["time_over_base"] = ms / mbase
+        if event is not None:
+            row["event_fired_frac"] = float((outs[5] >= 0).float().mean().item())
+            row["event_index_agrees_with_oracle"] = float(
+                (outs[5][:n_m].cpu().numpy() == r["event_index"]).mean())
+        out["mlp"][name] = row
     return out
 
 

@@ -403,19 +403,16 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       delete p;
       return fail(GBDX_ERR_INVALID, "unknown event condition kind or direction");
     }
-    if (d.ev_kind[e] != GBDX_EV_STEADY && d.dim > 4) {
-      delete p;
-      return fail(GBDX_ERR_UNSUPPORTED, "linear event conditions take a state of dim <= 4");
-    }
+
   }
   if (d.n_event > 0 && d.event_root && !(d.newton_rtol >= 0 && d.newton_atol > 0)) {
     delete p;
     return fail(GBDX_ERR_INVALID, "the root finder needs rtol >= 0 and atol > 0");
   }
   const bool xo = d.save_steps > 0 || d.save_dense || clip || d.n_event > 0;
-  // The MLP integrator (K2) records step saves and dense steps and runs the
-  // clip controller; the plain and tensor-core MLP kernels do not.
-  const bool xo_mlp = d.field == GBDX_MLP && d.n_event == 0 && d.adjoint == GBDX_ADJ_NONE &&
+  // The MLP integrator (K2) records step saves and dense steps, runs the clip
+  // controller and the events; the plain and tensor-core MLP kernels do not.
+  const bool xo_mlp = d.field == GBDX_MLP && d.adjoint == GBDX_ADJ_NONE &&
                       d.kernel != GBDX_KERNEL_PLAIN && d.kernel != GBDX_KERNEL_TC;
   if (xo && !xo_mlp &&
       (d.field == GBDX_MLP || d.adjoint != GBDX_ADJ_NONE ||
@@ -424,8 +421,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
     return fail(GBDX_ERR_UNSUPPORTED,
                 "SaveAt(steps=...), SaveAt(dense=True), ClipStepSizeController and events "
                 "are available for forward solves of the analytic fields (ODEs and the "
-                "Ornstein-Uhlenbeck SDE); all but events also for forward solves of the MLP "
-                "fields on the fused kernel");
+                "Ornstein-Uhlenbeck SDE) and of the MLP fields on the fused kernel");
   }
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
                d.field == GBDX_ORNSTEIN_UHLENBECK)) {
@@ -566,9 +562,15 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       *out = p;
       return GBDX_OK;
     }
-    if (D == 64 && H == 128) p->ode = gbdx::find_mlp_entry_d64h128(d.solver, precise, sde);
-    if (D == 64 && H == 256) p->ode = gbdx::find_mlp_entry_d64h256(d.solver, precise, sde);
-    if (D == 32 && H == 64) p->ode = gbdx::find_mlp_entry_d32h64(d.solver, precise, sde);
+    if (D == 64 && H == 128)
+      p->ode = xo ? gbdx::find_mlp_xo_entry_d64h128(d.solver, precise, sde)
+                  : gbdx::find_mlp_entry_d64h128(d.solver, precise, sde);
+    if (D == 64 && H == 256)
+      p->ode = xo ? gbdx::find_mlp_xo_entry_d64h256(d.solver, precise, sde)
+                  : gbdx::find_mlp_entry_d64h256(d.solver, precise, sde);
+    if (D == 32 && H == 64)
+      p->ode = xo ? gbdx::find_mlp_xo_entry_d32h64(d.solver, precise, sde)
+                  : gbdx::find_mlp_entry_d32h64(d.solver, precise, sde);
     if (!p->ode.launch) {
       delete p;
       return fail(GBDX_ERR_UNSUPPORTED,

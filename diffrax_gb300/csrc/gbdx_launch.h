@@ -105,6 +105,10 @@ OdeEntry find_mlp_entry_d64h128(int solver, bool precise, bool sde);
 OdeEntry find_mlp_tc_entry(int solver, int D, int H, bool sde);
 OdeEntry find_mlp_entry_d64h256(int solver, bool precise, bool sde);
 OdeEntry find_mlp_entry_d32h64(int solver, bool precise, bool sde);
+// the extended-output forms (SaveAt(steps / dense), clip controller, events)
+OdeEntry find_mlp_xo_entry_d64h128(int solver, bool precise, bool sde);
+OdeEntry find_mlp_xo_entry_d64h256(int solver, bool precise, bool sde);
+OdeEntry find_mlp_xo_entry_d32h64(int solver, bool precise, bool sde);
 // Gradients of the analytic-field solves (y0 and args): the forward with the
 // full tape, the RecursiveCheckpointAdjoint and BacksolveAdjoint backwards.
 struct AdjParams;

@@ -73,6 +73,21 @@ struct RowState {
   float part[M][8];
 };
 
+// Events (registered conditions) of the extended-output integrator, in the
+// dynamic shared memory after the kernel's own: the conditions' last values,
+// the one that fired (-1: none), the event time, the latest time a save may
+// take (the event time once a root was found), the root's theta in its step
+// (-1: no root); components 0..3 of y0, y1 and the stage increments for the
+// root find; the steady-state norms' per-tile partials (f.f, y.y).
+template <int M>
+struct RowEvents {
+  double evv[M][GBDX_MAX_EVENTS], tfin[M], tsave[M];
+  int evi[M];
+  float thfin[M];
+  float ey0[M][4], ey1[M][4], ek[M][7][4];
+  float pf[M][8], py[M][8];
+};
+
 template <class SH, bool PRECISE, bool SDE>
 struct MlpSmem;
 
@@ -315,8 +330,9 @@ __device__ __forceinline__ bool row_running(const RowState<M> &R, int r, int max
          R.result[r] == GBDX_SUCCESSFUL && R.nsteps[r] < max_steps;
 }
 
-template <int M>
-__device__ void row_init(RowState<M> &R, int r, int64_t i, const SolveParams &P) {
+template <int M, bool XO>
+__device__ void row_init(RowState<M> &R, RowEvents<M> *EV, int r, int64_t i,
+                         const SolveParams &P, int D) {
   const int64_t ti = i * P.time_stride;
   double a = P.t0[ti], b = P.t1[ti];
   const int dir = (a < b) ? 1 : -1;
@@ -331,7 +347,10 @@ __device__ void row_init(RowState<M> &R, int r, int64_t i, const SolveParams &P)
     if (P.has_dtmax) h = fmin(h, P.dtmax);
     if (P.has_dtmin) h = fmax(h, P.dtmin);
     tn = a + h;
-    if (P.n_step_ts > 0 || P.n_jump_ts > 0) tn = clip_start(P, dir, R.sidx[r], R.jidx[r], a, tn);
+    if constexpr (XO) {
+      if (P.n_step_ts > 0 || P.n_jump_ts > 0)
+        tn = clip_start(P, dir, R.sidx[r], R.jidx[r], a, tn);
+    }
     R.hist1[r] = 0.f;
     R.hist2[r] = 0.f;
   } else {
@@ -364,8 +383,34 @@ __device__ void row_init(RowState<M> &R, int r, int64_t i, const SolveParams &P)
   if (P.tape_t)
     *GBDX_AT(P, P.tape_t, i * (P.max_steps + 1), 1, P.batch * (P.max_steps + 1),
              GBDX_SITE_TAPE_T) = a;
+  if constexpr (!XO) return;
   R.sdown[r] = P.save_steps;
   R.stslot[r] = -1;
+  EV->evi[r] = -1;
+  EV->tfin[r] = a;
+  EV->thfin[r] = -1.f;
+  if (P.n_event > 0) {
+    // values at (t0, y0) (_integrate.py:1333-1426): a boolean linear
+    // condition that already holds ends the solve before its first step; a
+    // steady-state condition is checked once f(y0) is known (the first step's
+    // first stage)
+    const float *y0 = static_cast<const float *>(P.y0) + i * D;
+#pragma unroll
+    for (int e = 0; e < GBDX_MAX_EVENTS; e++) {
+      if (e < P.n_event) {
+        double v = 0.0;
+        if (P.ev_kind[e] != GBDX_EV_STEADY) {
+          for (int n = 0; n < (D < 4 ? D : 4); n++)
+            v += P.ev_coef[6 * e + n] * double(y0[n]);
+          v += P.ev_coef[6 * e + 4] * a + P.ev_coef[6 * e + 5];
+          if (P.ev_kind[e] == GBDX_EV_LINEAR_BOOL) v = v > 0 ? 1.0 : 0.0;
+          if (EV->evi[r] < 0 && P.ev_kind[e] == GBDX_EV_LINEAR_BOOL && v != 0.0) EV->evi[r] = e;
+        }
+        EV->evv[r][e] = v;
+      }
+    }
+    if (EV->evi[r] >= 0) R.result[r] = GBDX_EVENT_OCCURRED;
+  }
   // dense_ts[0] = t0 in the loop's time; the rest of the dense buffers was
   // filled with +inf before the launch (_integrate.py:1315-1323)
   if (P.dense_ts)
@@ -376,7 +421,7 @@ __device__ void row_init(RowState<M> &R, int r, int64_t i, const SolveParams &P)
 // The controller's decision for row r after the error norm acc = sum of
 // squared scaled errors over the D components (pid.py:466-567,
 // constant.py:59-104, _integrate.py:410-413).
-template <int M>
+template <int M, bool XO>
 __device__ void row_control(RowState<M> &R, int r, int D, const SolveParams &P) {
   const double dt = R.dtc[r];
   bool keep;
@@ -422,9 +467,11 @@ __device__ void row_control(RowState<M> &R, int r, int D, const SolveParams &P) 
   }
   // ClipStepSizeController around the PID controller (clip.py:330-389)
   bool made_jump = false;
-  if (P.controller == GBDX_PID && (P.n_step_ts > 0 || P.n_jump_ts > 0)) {
-    made_jump = clip_next(P, R.dir[r], R.sidx[r], R.jidx[r], nt0, nt1);
-    dtn = nt1 - nt0;
+  if constexpr (XO) {
+    if (P.controller == GBDX_PID && (P.n_step_ts > 0 || P.n_jump_ts > 0)) {
+      made_jump = clip_next(P, R.dir[r], R.sidx[r], R.jidx[r], nt0, nt1);
+      dtn = nt1 - nt0;
+    }
   }
   if (order_key(nt1) > order_key(R.floor1[r])) {
     nt1 = keep ? R.t1[r] : nt0 + 0.5 * (R.t1[r] - nt0);
@@ -550,10 +597,146 @@ __device__ __forceinline__ void load_rows(float (&Y0)[NE], float (&F0)[NE], floa
   }
 }
 
+// Whether condition e fires between its values vo and vn: a boolean when it
+// holds, a real value on the chosen sign change (_integrate.py:585-602).
+__device__ __forceinline__ bool mlp_ev_fires(const SolveParams &P, int e, double vo, double vn) {
+  if (P.ev_kind[e] != GBDX_EV_LINEAR) return vn != 0.0;
+  const double so = isnan(vo) ? vo : double((vo > 0) - (vo < 0));
+  const double sn = isnan(vn) ? vn : double((vn > 0) - (vn < 0));
+  if (P.ev_dir[e] == GBDX_EV_UP) return so <= 0 && sn > 0;
+  if (P.ev_dir[e] == GBDX_EV_DOWN) return so > 0 && sn <= 0;
+  return so != sn;
+}
+
+// Per-tile partial sums of f.f and y.y of every row (the steady-state
+// condition's norms, _event.py:120-175), one slot per 8-column tile.
+template <class SH, int M, int NE>
+__device__ __forceinline__ void steady_partials(RowEvents<M> &R, const float (&F)[NE],
+                                                const float (&Y)[NE], int warp, int lane) {
+#pragma unroll
+  for (int j = 0; j < SH::TPW; j++) {
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+      int row, col;
+      elem_rc<SH>(j * 4 + half * 2, warp, lane, row, col);
+      float pf = 0.f, py = 0.f;
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        const int e = j * 4 + half * 2 + q;
+        pf = fmaf(F[e], F[e], pf);
+        py = fmaf(Y[e], Y[e], py);
+      }
+      pf += __shfl_xor_sync(0xffffffffu, pf, 1);
+      pf += __shfl_xor_sync(0xffffffffu, pf, 2);
+      py += __shfl_xor_sync(0xffffffffu, py, 1);
+      py += __shfl_xor_sync(0xffffffffu, py, 2);
+      if ((lane & 3) == 0) {
+        R.pf[row][(warp * SH::TPW + j) % SH::NT] = pf;
+        R.py[row][(warp * SH::TPW + j) % SH::NT] = py;
+      }
+    }
+  }
+}
+
+// Value of steady-state condition e for row r from its partials.
+template <class SH, int M>
+__device__ __forceinline__ double steady_value(const SolveParams &P, const RowEvents<M> &R, int r,
+                                               int e) {
+  float sf = 0.f, sy = 0.f;
+#pragma unroll
+  for (int n = 0; n < SH::NT; n++) {
+    sf += R.pf[r][n];
+    sy += R.py[r][n];
+  }
+  return sqrt(double(sf) / SH::D) < P.ev_coef[6 * e + 1] + P.ev_coef[6 * e] * sqrt(double(sy) / SH::D)
+             ? 1.0
+             : 0.0;
+}
+
+// The solver's local interpolant inside a step, one component: its value at
+// theta or its theta-derivative, from y0, y1 and the stage increments k(j)
+// (the trajectory kernels' formulas).
+template <int SOLVER, int S, bool DERIV, class KF>
+__device__ __forceinline__ float mlp_interp(float th, float y0, float y1, const KF &k) {
+  if constexpr (SOLVER == GBDX_TSIT5) {
+    float a = 0.f;
+#pragma unroll
+    for (int j = 0; j < 7; j++)
+      a = fmaf(DERIV ? tsit5_dw<float>(j, th) : tsit5_w<float>(j, th), k(j < S ? j : 0), a);
+    return DERIV ? a : y0 + a;
+  } else if constexpr (SOLVER == GBDX_DOPRI5) {
+    float cm = 0.f;
+#pragma unroll
+    for (int j = 0; j < S; j++) cm = fmaf(float(Tab<GBDX_DOPRI5>::cmid(j < 7 ? j : 0)), k(j), cm);
+    const float ym = y0 + cm, fa = k(0), fb = k(S - 1);
+    const float a = 2.f * (fb - fa) - 8.f * (y1 + y0) + 16.f * ym;
+    const float b = 5.f * fa - 3.f * fb + 18.f * y0 + 14.f * y1 - 32.f * ym;
+    const float c = fb - 4.f * fa - 11.f * y0 - 5.f * y1 + 16.f * ym;
+    if (DERIV) return ((4.f * a * th + 3.f * b) * th + 2.f * c) * th + fa;
+    return (((a * th + b) * th + c) * th + fa) * th + y0;
+  } else if constexpr (SOLVER == GBDX_HEUN) {
+    const float ka = k(0), kb = k(S - 1);
+    const float a = ka + kb + 2.f * y0 - 2.f * y1;
+    const float b = -2.f * ka - kb - 3.f * y0 + 3.f * y1;
+    if (DERIV) return (3.f * a * th + 2.f * b) * th + ka;
+    return ((a * th + b) * th + ka) * th + y0;
+  } else {
+    return DERIV ? y1 - y0 : y0 + th * (y1 - y0);
+  }
+}
+
+// The event's root find on row r's last step (_integrate.py:704-779), as the
+// trajectory kernels do it: Newton's method with cauchy termination on
+// g(t) = w . interp(t) + wt t + c over [tp, tn] from t = tn, each iterate
+// clipped to the step; components 0..3 of the step's y0, y1 and stages come
+// from the row state.  Returns the root; ok = false after 256 iterations.
+template <int SOLVER, int S, int M>
+__device__ double mlp_ev_root(const SolveParams &P, const RowEvents<M> &R, int r,
+                              const double (&cf)[6], int nc, double tp, double tn, bool &ok) {
+  ok = true;
+  const double span = tn - tp;
+  double t = tn;
+  for (int it = 1; it <= 256; it++) {
+    const float th = float(span == 0.0 ? 0.0 : (t - tp) / span);
+    double g = 0.0, gp = 0.0;
+    for (int n = 0; n < nc; n++) {
+      auto k = [&](int j) { return R.ek[r][j][n]; };
+      g += cf[n] * double(mlp_interp<SOLVER, S, false>(th, R.ey0[r][n], R.ey1[r][n], k));
+      gp += cf[n] * (span == 0.0 ? 0.0
+                                 : double(mlp_interp<SOLVER, S, true>(th, R.ey0[r][n],
+                                                                       R.ey1[r][n], k)) / span);
+    }
+    g += cf[4] * t;
+    g += cf[5];
+    gp += cf[4];
+    const double diff = g / gp;
+    double nt = t - diff;
+    nt = fmax(fmin(nt, tn), tp);
+    if (isnan(nt)) {
+      ok = false;
+      return t;
+    }
+    const double size = fabs(diff) / (P.newton_atol + P.newton_rtol * fabs(nt));
+    t = nt;
+    if (it >= 2 && size < 1.0 && fabs(g) < P.newton_atol) return t;
+  }
+  ok = false;
+  return t;
+}
+
 // ---------------------------------------------------------------------------
 // The kernel.
 // ---------------------------------------------------------------------------
-template <int SOLVER, int D, int H, bool PRECISE, bool SDE>
+// Bytes of dynamic shared memory before the event state of the XO kernel.
+template <class Sm>
+constexpr size_t mlp_events_offset() {
+  return (sizeof(Sm) + 15) / 16 * 16;
+}
+
+// XO (extended outputs: SaveAt(steps=n), SaveAt(dense=True), the clip
+// controller and events) is a template flag, as in the trajectory kernels, so
+// that the kernels without them keep their registers.
+template <int SOLVER, int D, int H, bool PRECISE, bool SDE, bool XO>
 __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
   using SH = MlpShape<D, H>;
   using FLD = MlpField<SH, PRECISE, SDE>;
@@ -563,14 +746,22 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Sm &sm = *reinterpret_cast<Sm *>(smem_raw);
   RowState<M> &R = sm.rows;
+  RowEvents<M> *EV =
+      XO ? reinterpret_cast<RowEvents<M> *>(smem_raw + mlp_events_offset<Sm>()) : nullptr;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const float *W = P.mlp;
 
   FLD::stage(sm, P, tid);
+  bool ev_steady = false;
+  if constexpr (XO) {
+#pragma unroll
+    for (int e = 0; e < GBDX_MAX_EVENTS; e++)
+      ev_steady |= e < P.n_event && P.ev_kind[e] == GBDX_EV_STEADY;
+  }
   if (tid < M) {
     const unsigned long long q = atomicAdd(P.queue, 1ull);
     if (q < (unsigned long long)P.batch) {
-      row_init(R, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P);
+      row_init<M, XO>(R, EV, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P, D);
       R.loaded[tid] = 1;
     } else {
       R.active[tid] = 0;
@@ -632,6 +823,33 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
     } else {
 #pragma unroll
       for (int e = 0; e < NE; e++) F[e] = F0[e];
+    }
+    // a steady-state condition already true at (t0, y0) ends the solve before
+    // its first step (_integrate.py:1333-1426); F holds f(y0) for a fresh row
+    if constexpr (XO) {
+      if (ev_steady) {
+        const int fresh = tid < M && live && R.nsteps[tid] == 0;
+        if (__syncthreads_or(fresh)) {
+          steady_partials<SH>(*EV, F, Y0, warp, lane);
+          __syncthreads();
+          if (fresh) {
+#pragma unroll
+            for (int e = 0; e < GBDX_MAX_EVENTS; e++) {
+              if (e < P.n_event && P.ev_kind[e] == GBDX_EV_STEADY) {
+                const double v = steady_value<SH>(P, *EV, tid, e);
+                EV->evv[tid][e] = v;
+                if (EV->evi[tid] < 0 && v != 0.0) EV->evi[tid] = e;
+              }
+            }
+            if (EV->evi[tid] >= 0) {
+              R.result[tid] = GBDX_EVENT_OCCURRED;
+              live = 0;
+              R.live[tid] = 0;
+            }
+          }
+          __syncthreads();
+        }
+      }
     }
 #pragma unroll
     for (int e = 0; e < NE; e++) K[0][e] = SDE ? F[e] * hrow[e] + sig[e] * dW[e] : F[e] * hrow[e];
@@ -709,8 +927,85 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
       }
     }
     __syncthreads();
-    if (tid < M && live) row_control(R, tid, D, P);
+    if (tid < M && live) row_control<M, XO>(R, tid, D, P);
     __syncthreads();
+    // ---- events at the new state (_integrate.py:542-633) --------------------
+    // The first condition (in order) that fires ends the solve; with a root
+    // finder the final time is the root inside this step and no save after
+    // it is made.
+    if constexpr (XO) {
+    if (P.n_event > 0) {
+      RowEvents<M> &E = *EV;
+      if constexpr (!TB::FSAL) {
+        // f(y1) for a steady-state condition (FSAL solvers have it in F)
+        if (ev_steady && __syncthreads_or(tid < M && live && R.keep[tid])) {
+          FLD::put_x(sm, Y1, warp, lane);
+          __syncthreads();
+          FLD::eval(sm, W, F, sig, tid, warp, lane);
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        if (col < 4 && R.live[row] && R.keep[row]) {
+          E.ey0[row][col] = Y0[e];
+          E.ey1[row][col] = Y1[e];
+#pragma unroll
+          for (int j = 0; j < S; j++) E.ek[row][j][col] = K[j][e];
+        }
+      }
+      if (ev_steady) steady_partials<SH>(E, F, Y1, warp, lane);
+      __syncthreads();
+      if (tid < M) {
+        E.tsave[tid] = R.tn_old[tid];
+        if (live && R.keep[tid]) {
+          const double tn = R.tn_old[tid], tp = R.tp_old[tid];
+          int fired = -1;
+#pragma unroll
+          for (int e = 0; e < GBDX_MAX_EVENTS; e++) {
+            if (e < P.n_event) {
+              double v;
+              if (P.ev_kind[e] == GBDX_EV_STEADY) {
+                v = steady_value<SH>(P, E, tid, e);
+              } else {
+                v = 0.0;
+                for (int n = 0; n < (D < 4 ? D : 4); n++)
+                  v += P.ev_coef[6 * e + n] * double(E.ey1[tid][n]);
+                v += P.ev_coef[6 * e + 4] * tn;
+                v += P.ev_coef[6 * e + 5];
+                if (P.ev_kind[e] == GBDX_EV_LINEAR_BOOL) v = v > 0 ? 1.0 : 0.0;
+              }
+              if (fired < 0 && mlp_ev_fires(P, e, E.evv[tid][e], v)) fired = e;
+              E.evv[tid][e] = v;
+            }
+          }
+          if (fired >= 0) {
+            E.evi[tid] = fired;
+            R.result[tid] = GBDX_EVENT_OCCURRED;
+            E.tfin[tid] = tn;
+            if (P.event_root) {
+              // a boolean condition's root is the end of the step
+              double root = tn;
+              if (P.ev_kind[fired] == GBDX_EV_LINEAR) {
+                double cf[6];
+#pragma unroll
+                for (int n = 0; n < 6; n++) cf[n] = P.ev_coef[6 * fired + n];
+                bool ok = true;
+                root = mlp_ev_root<SOLVER, S>(P, E, tid, cf, D < 4 ? D : 4, tp, tn, ok);
+                if (!ok) R.result[tid] = GBDX_NONLINEAR_MAX_STEPS;
+              }
+              const double span = tn - tp;
+              E.tfin[tid] = root;
+              E.tsave[tid] = root;
+              E.thfin[tid] = float(span == 0.0 ? 0.0 : (root - tp) / span);
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+    }
     // ---- SaveAt(ts) inside accepted steps (_integrate.py:456-487) ----------
     while (true) {
       int fl = 0;
@@ -719,7 +1014,7 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
         if (live && R.keep[tid] && R.ts_index[tid] < P.n_ts) {
           const double tsv = __ldg(P.save_ts + R.ts_index[tid]);
           const double tsd = R.dir[tid] * tsv;
-          if (tsd <= R.tn_old[tid]) {
+          if (tsd <= ((XO && P.n_event > 0) ? EV->tsave[tid] : R.tn_old[tid])) {
             const double tp = R.tp_old[tid], tn = R.tn_old[tid];
             R.theta[tid] = float(tp == tn ? 0.0 : (tsd - tp) / (tn - tp));
             R.sslot[tid] = R.save_index[tid];
@@ -772,16 +1067,19 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
     }
     // ---- SaveAt(steps=n), after the step's ts saves (_integrate.py:492-527),
     // and SaveAt(dense=True) step times (:529-540) ----------------------------
-    if (P.save_steps > 0 || P.dense_ts) {
+    if (XO && (P.save_steps > 0 || P.dense_ts != nullptr)) {
       if (tid < M) {
         R.stslot[tid] = -1;
         if (live && R.keep[tid]) {
           const int64_t i = R.idx[tid];
           if (P.save_steps > 0 && --R.sdown[tid] == 0) {
             R.sdown[tid] = P.save_steps;
-            R.stslot[tid] = R.save_index[tid]++;
-            *GBDX_AT(P, P.ts_out, i * P.n_save + R.stslot[tid], 1, P.batch * P.n_save,
-                     GBDX_SITE_TS) = R.dir[tid] * R.tn_old[tid];
+            // not past an event's root
+            if (!(P.n_event > 0 && order_key(R.tn_old[tid]) > order_key(EV->tsave[tid]))) {
+              R.stslot[tid] = R.save_index[tid]++;
+              *GBDX_AT(P, P.ts_out, i * P.n_save + R.stslot[tid], 1, P.batch * P.n_save,
+                       GBDX_SITE_TS) = R.dir[tid] * R.tn_old[tid];
+            }
           }
           // nacc already counts this step
           if (P.dense_ts)
@@ -797,6 +1095,7 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
       int row, col;
       elem_rc<SH>(e, warp, lane, row, col);
       if (R.live[row] && R.keep[row]) {
+        if constexpr (XO) {
         if (R.stslot[row] >= 0)
           *GBDX_AT(P, reinterpret_cast<float *>(P.ys_out),
                    (R.idx[row] * P.n_save + R.stslot[row]) * D + col, 1,
@@ -811,6 +1110,12 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
           rec[D + col] = Y1[e];
 #pragma unroll
           for (int j = 0; j < S; j++) rec[(2 + j) * D + col] = K[j][e];
+        }
+        if (P.n_event > 0 && EV->evi[row] >= 0 && EV->thfin[row] >= 0.f) {
+          // the state at the event's root (or the step's end for a boolean)
+          Y1[e] = mlp_interp<SOLVER, S, false>(EV->thfin[row], Y0[e], Y1[e],
+                                               [&](int j) { return K[j][e]; });
+        }
         }
         Y0[e] = Y1[e];
         if (TB::FSAL) F0[e] = F[e];  // field value of the last stage (FSAL)
@@ -842,15 +1147,25 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
           *GBDX_AT(P, P.ts_out, i * P.n_save + si + m, 1, tse, GBDX_SITE_TS) = t0 * dir;
         si += R.nfill[tid];
         // the t1 value is already saved when SaveAt(steps=n) saved the last
-        // step (_integrate.py:847-877)
-        R.sflag[tid] = P.save_t1 && !(P.save_steps > 0 && R.sdown[tid] == P.save_steps);
+        // step (_integrate.py:847-877); with an event root finder the final
+        // value is saved whenever the steps saved the t1 value, as that save
+        // fell after the event (:860-872), and the final time is the event's
+        R.sflag[tid] = P.save_t1;
+        double tf = R.tprev[tid];
+        if constexpr (XO) {
+          const bool via_steps = P.save_steps > 0 && R.sdown[tid] == P.save_steps;
+          const bool root = P.n_event > 0 && P.event_root;
+          R.sflag[tid] = root ? (P.save_t1 || via_steps) : (P.save_t1 && !via_steps);
+          if (root && EV->evi[tid] >= 0) tf = EV->tfin[tid];
+          if (P.event_index) P.event_index[i] = EV->evi[tid];
+          if (P.dense_n) P.dense_n[i] = R.nacc[tid] + 1;
+        }
         if (R.sflag[tid])
-          *GBDX_AT(P, P.ts_out, i * P.n_save + si++, 1, tse, GBDX_SITE_TS) = R.tprev[tid] * dir;
+          *GBDX_AT(P, P.ts_out, i * P.n_save + si++, 1, tse, GBDX_SITE_TS) = tf * dir;
         if (!P.saves_prefilled)
           for (int m = si; m < P.n_save; m++)  // direction * inf
             *GBDX_AT(P, P.ts_out, i * P.n_save + m, 1, tse, GBDX_SITE_TS) =
                 dir > 0 ? INFINITY : -INFINITY;
-        if (P.dense_n) P.dense_n[i] = R.nacc[tid] + 1;
         int res = R.result[tid];
         if (res == GBDX_SUCCESSFUL && order_key(R.tprev[tid]) < order_key(R.t1[tid]))
           res = GBDX_MAX_STEPS_REACHED;
@@ -888,7 +1203,7 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
       if (tid < M && R.fin[tid]) {
         const unsigned long long q = atomicAdd(P.queue, 1ull);
         if (q < (unsigned long long)P.batch) {
-          row_init(R, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P);
+          row_init<M, XO>(R, EV, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P, D);
           R.loaded[tid] = 1;
         } else {
           R.active[tid] = 0;

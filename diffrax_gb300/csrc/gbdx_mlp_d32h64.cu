@@ -4,6 +4,6 @@
 
 namespace gbdx {
 OdeEntry find_mlp_entry_d32h64(int solver, bool precise, bool sde) {
-  return mlp_entry<32, 64, true>(solver, precise, sde);
+  return mlp_entry<32, 64, true, false>(solver, precise, sde);
 }
 }  // namespace gbdx

@@ -4,6 +4,6 @@
 
 namespace gbdx {
 OdeEntry find_mlp_entry_d64h256(int solver, bool precise, bool sde) {
-  return mlp_entry<64, 256, false>(solver, precise, sde);
+  return mlp_entry<64, 256, false, false>(solver, precise, sde);
 }
 }  // namespace gbdx

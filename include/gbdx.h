@@ -102,7 +102,7 @@ enum gbdx_result {
 /* Registered event conditions (diffrax/_event.py:13-175).  A condition is
  * evaluated at the loop's time t (time runs forward: t * sign(t1 - t0), the
  * time the reference hands to cond_fn) and state y:
- *   LINEAR       value = sum_n w_n y_n + wt t + c  (real-valued; dim <= 4)
+ *   LINEAR       value = sum_n w_n y_n + wt t + c  (real-valued; n < min(dim, 4))
  *   LINEAR_BOOL  value > 0 of the same form      (boolean)
  *   STEADY       rms(f(t, y)) < atol + rtol rms(y) (steady_state_event)  */
 enum gbdx_event_kind { GBDX_EV_LINEAR = 0, GBDX_EV_LINEAR_BOOL = 1, GBDX_EV_STEADY = 2 };

@@ -106,7 +106,7 @@ typedef struct {
   int32_t n_step_ts, n_jump_ts;
   /* Event(cond_fn=[...], root_finder, direction): n_event conditions of kind
    * ev_kind (ORC_EV_*) and direction ev_dir (ORC_EV_EITHER/UP/DOWN); linear:
-   * ev_coef[6 i + n] = w_n (n < dim <= 4), [6 i + 4] = wt, [6 i + 5] = c;
+   * ev_coef[6 i + n] = w_n (n < min(dim, 4)), [6 i + 4] = wt, [6 i + 5] = c;
    * steady state: [6 i] = rtol, [6 i + 1] = atol.  event_root = 1 finds the
    * event time by Newton's method with newton_rtol / newton_atol. */
   int32_t n_event, event_root;
@@ -1135,8 +1135,9 @@ static double ev_value(const Field *F, int dir, int i, double t, const double *y
     field_drift(F, dir * t, y, f);
     return rms_norm(f, d->dim) < c[1] + c[0] * rms_norm(y, d->dim) ? 1.0 : 0.0;
   }
+  /* at most four state coefficients: components 0 .. min(dim, 4) - 1 */
   double v = 0.0;
-  for (int n = 0; n < d->dim; n++) v += c[n] * y[n];
+  for (int n = 0; n < (d->dim < 4 ? d->dim : 4); n++) v += c[n] * y[n];
   v += c[4] * t;
   v += c[5];
   if (d->ev_kind[i] == ORC_EV_LINEAR_BOOL) return v > 0 ? 1.0 : 0.0;
@@ -1163,7 +1164,7 @@ static int ev_triggered(const orc_desc *d, int i, double old_v, double new_v) {
  * the step.  Returns the root; *ok = 0 if it did not converge. */
 static double ev_root(const Field *F, const Tableau *tab, int i, const StepOut *so, int *ok) {
   const orc_desc *d = F->d;
-  const int D = d->dim;
+  const int D = d->dim < 4 ? d->dim : 4; /* the condition's state coefficients */
   *ok = 1;
   if (d->ev_kind[i] != ORC_EV_LINEAR) return so->tnext;
   const double *c = d->ev_coef + 6 * i;
@@ -1574,8 +1575,6 @@ int orc_solve_state(const orc_desc *d, int64_t B, const double *t0, const double
   if (d->save_steps < 0) return -1;
   if ((dense_ts != NULL) != (d->save_dense != 0)) return -1;
   if (d->n_event < 0 || d->n_event > ORC_MAX_EVENTS) return -1;
-  for (int i = 0; i < d->n_event; i++)
-    if (d->ev_kind[i] != ORC_EV_STEADY && d->dim > 4) return -1;
   if (d->levy_area != 0 && d->levy_area != 1) return -1;
   /* the SRKs take the SpaceTimeLevyArea of an SDE's tree (srk.py:374-379) */
   if (ORC_IS_SRK(d->solver) && (d->diffusion == ORC_DIFF_NONE || !d->levy_area)) return -1;

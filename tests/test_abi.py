@@ -355,8 +355,8 @@ def test_sde_extended_output_scope():
                           max_steps=64, n_ts=0, event=event)
             p = _lib.Problem(f)
             assert p.n_save == (32 if saveat.steps else (0 if saveat.dense else 1))
-    # the MLP SDE: step saves, dense steps and the clip controller on the fused
-    # kernel; not events, nor the plain or tensor-core kernels
+    # the MLP SDE: step saves, dense steps, the clip controller and events on
+    # the fused kernel; not on the plain or tensor-core kernels
     W = [torch.zeros(64, 32), torch.zeros(64, 64), torch.zeros(32, 64)]
     b = [torch.zeros(64), torch.zeros(64), torch.zeros(32)]
     bm = dfx.VirtualBrownianTree(0.0, 1.0, 1e-3, (32,), key=0)
@@ -376,8 +376,9 @@ def test_sde_extended_output_scope():
         _lib.Problem(dict(f, kernel=3))
     f = dfx.lower(terms, dfx.Heun(), pid, dfx.SaveAt(t1=True), dim=32, dtype=torch.float32,
                   max_steps=64, n_ts=0, event=dfx.Event(dfx.steady_state_event()))
-    with pytest.raises(_lib.GbdxError, match="all but events"):
-        _lib.Problem(f)
+    assert _lib.Problem(f).n_save == 1
+    with pytest.raises(_lib.GbdxError, match="fused kernel"):
+        _lib.Problem(dict(f, kernel=1))
 
 
 def test_autotune_cache_round_trip(tmp_path, monkeypatch):
