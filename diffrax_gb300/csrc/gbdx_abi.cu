@@ -59,6 +59,9 @@ struct gbdx_problem {
   int n_save;
   double c1, c2, c3;  // PID exponents
   gbdx::OdeEntry ode;
+  // the extended-output form of an analytic-field forward: it also reads and
+  // writes the resume records (gbdx_fwd_extras state_in / state_out)
+  gbdx::OdeEntry ode_xo;
   gbdx::BwdEntry bwd;  // RecursiveCheckpointAdjoint backward (MLP fields)
   gbdx::BsEntry bs;    // BacksolveAdjoint backward (MLP fields)
   gbdx::AdjEntry adj;  // gradients of the analytic fields (y0 and args)
@@ -425,9 +428,10 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   }
   if (!sde && (d.field == GBDX_LOTKA_VOLTERRA || d.field == GBDX_VAN_DER_POL ||
                d.field == GBDX_ORNSTEIN_UHLENBECK)) {
+    p->ode_xo = d.dtype == GBDX_F32 ? gbdx::find_ode_entry_f32_xo(d.solver, d.field, d.dim)
+                                    : gbdx::find_ode_entry_f64_xo(d.solver, d.field, d.dim);
     if (xo)
-      p->ode = d.dtype == GBDX_F32 ? gbdx::find_ode_entry_f32_xo(d.solver, d.field, d.dim)
-                                   : gbdx::find_ode_entry_f64_xo(d.solver, d.field, d.dim);
+      p->ode = p->ode_xo;
     else
       p->ode = d.dtype == GBDX_F32 ? gbdx::find_ode_entry_f32(d.solver, d.field, d.dim)
                                    : gbdx::find_ode_entry_f64(d.solver, d.field, d.dim);
@@ -457,10 +461,12 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       return fail(GBDX_ERR_UNSUPPORTED,
                   "the Ornstein-Uhlenbeck SDE runs with FP32 state (FP32 Brownian tree)");
     }
-    p->ode = d.levy_area == GBDX_LEVY_SPACE_TIME
-                 ? (xo ? gbdx::find_ode_sde_levy_entry_f32_xo(d.solver, d.dim)
-                       : gbdx::find_ode_sde_levy_entry_f32(d.solver, d.dim))
-                 : (xo ? gbdx::find_ode_sde_entry_f32_xo(d.solver, d.dim)
+    p->ode_xo = d.levy_area == GBDX_LEVY_SPACE_TIME
+                    ? gbdx::find_ode_sde_levy_entry_f32_xo(d.solver, d.dim)
+                    : gbdx::find_ode_sde_entry_f32_xo(d.solver, d.dim);
+    p->ode = xo ? p->ode_xo
+                : (d.levy_area == GBDX_LEVY_SPACE_TIME
+                       ? gbdx::find_ode_sde_levy_entry_f32(d.solver, d.dim)
                        : gbdx::find_ode_sde_entry_f32(d.solver, d.dim));
     if (!p->ode.launch) {
       delete p;
@@ -792,10 +798,11 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
   int32_t *dense_n = ex ? ex->dense_n : nullptr;
   const gbdx_problem_desc &d = problem->d;
   const bool resume = ex && (ex->state_in || ex->state_out);
-  if (resume && (d.field == GBDX_MLP || d.n_step_ts > 0 || d.n_jump_ts > 0))
+  if (resume && (d.field == GBDX_MLP || d.n_step_ts > 0 || d.n_jump_ts > 0 ||
+                 d.adjoint != GBDX_ADJ_NONE || !problem->ode_xo.launch))
     return fail(GBDX_ERR_UNSUPPORTED,
-                "solver and controller states are available for the analytic fields without "
-                "a ClipStepSizeController");
+                "solver and controller states are available for forward solves of the analytic "
+                "fields without a ClipStepSizeController");
   if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
   if (batch == 0) return GBDX_OK;
   if ((problem->n_save > 0 && (!ys_out || !ts_out)) || !result_out || !stats_out)
@@ -873,7 +880,7 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
     rc = device_sm_count(&sms);
     if (rc != GBDX_OK) return rc;
     int occ = 0;
-    cudaError_t e = problem->ode.occupancy(cfg.block, &occ);
+    cudaError_t e = (resume ? problem->ode_xo : problem->ode).occupancy(cfg.block, &occ);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
     if (occ < 1) occ = 1;
     int per_sm = d.ctas_per_sm;
@@ -895,7 +902,8 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
     rc = start_queue(problem, P, workspace, s);
     if (rc != GBDX_OK) return rc;
   }
-  cudaError_t e = problem->ode.launch(P, cfg, s);
+  // resume records are read and written by the extended-output form
+  cudaError_t e = (resume ? problem->ode_xo : problem->ode).launch(P, cfg, s);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
   return bounds_report(P, s, "gbdx_solve_fwd");
 }

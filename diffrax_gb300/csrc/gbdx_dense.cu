@@ -47,12 +47,14 @@ __global__ void fill_saves_kernel(T *ys, double *ts, int64_t batch, int n_save, 
                                   const double *t0, const double *t1, int64_t time_stride) {
   const int64_t n = batch * n_save;
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const int64_t b = i / n_save;
-    const int64_t ti = b * time_stride;
+  const int64_t first = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (int64_t i = first; i < n; i += stride) {
+    const int64_t ti = (i / n_save) * time_stride;
     ts[i] = __ldg(t0 + ti) < __ldg(t1 + ti) ? INFINITY : -INFINITY;
-    for (int c = 0; c < dim; c++) ys[i * dim + c] = T(INFINITY);
   }
+  // ys as one flat array: consecutive threads write consecutive elements
+  const int64_t ny = n * dim;
+  for (int64_t i = first; i < ny; i += stride) ys[i] = T(INFINITY);
 }
 
 template <class T>

@@ -284,10 +284,12 @@ struct Traj {
     // A controller state passed from a previous solve replaces the init
     // above; its first step is then t0 + dt0, unclipped (dt0=None keeps the
     // controller's initial step) (_integrate.py:1252-1265).
+    // (the extended-output kernels only: the others keep their shorter init)
     const double *st_in =
-        P.state_in ? GBDX_AT(P, P.state_in, i * int64_t(GBDX_STATE_HEAD + D), GBDX_STATE_HEAD + D,
-                             P.batch * (GBDX_STATE_HEAD + D), GBDX_SITE_STATE)
-                   : nullptr;
+        (XO && P.state_in)
+            ? GBDX_AT(P, P.state_in, i * int64_t(GBDX_STATE_HEAD + D), GBDX_STATE_HEAD + D,
+                      P.batch * (GBDX_STATE_HEAD + D), GBDX_SITE_STATE)
+            : nullptr;
     if (st_in && st_in[4] != 0.0) {
       if (P.controller == GBDX_PID) {
         h1 = F32 ? T(log2(st_in[0])) : T(st_in[0]);  // FP32 keeps the log2 domain
@@ -330,7 +332,7 @@ struct Traj {
     first = 1;
     // a passed solver state (first_step, f0) and made_jump: FSAL solvers
     // reuse f0 unless first_step or made_jump (runge_kutta.py:684-700)
-    if (st_in && TB::FSAL && st_in[5] == 0.0 && st_in[6] == 0.0) {
+    if (XO && st_in && TB::FSAL && st_in[5] == 0.0 && st_in[6] == 0.0) {
       first = 0;
 #pragma unroll
       for (int n = 0; n < D; n++) f0[n] = T(st_in[GBDX_STATE_HEAD + n]);
@@ -1039,7 +1041,7 @@ struct Traj {
     P.stats_out[idx * 3 + 0] = nsteps;
     P.stats_out[idx * 3 + 1] = nacc;
     P.stats_out[idx * 3 + 2] = nrej;
-    if (P.state_out) {
+    if (XO && P.state_out) {
       // SaveAt(controller_state=, solver_state=, made_jump=) (_integrate.py:
       // 1489-1500): the record gbdx_fwd_extras documents
       double *so = GBDX_AT(P, P.state_out, idx * int64_t(GBDX_STATE_HEAD + D),
