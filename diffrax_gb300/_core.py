@@ -434,14 +434,20 @@ class Event:
 
 class SaveAt:
     """diffrax/_saveat.py:69-105.  ``steps`` is a bool or an int n (save every
-    n-th accepted step); ``dense=True`` records the solution's dense output
+    n-th accepted step); ``fn(t, y, args)`` maps the saved values (called on
+    the batched saves); ``dense=True`` records the solution's dense output
     (``Solution.evaluate`` / ``Solution.derivative``); ``solver_state``,
     ``controller_state`` and ``made_jump`` keep the final states, which a
     later ``diffeqsolve`` resumes from."""
 
     def __init__(self, *, t0: bool = False, t1: bool = False, ts=None, steps=False,
-                 dense: bool = False, solver_state: bool = False,
+                 fn=None, dense: bool = False, solver_state: bool = False,
                  controller_state: bool = False, made_jump: bool = False):
+        # fn(t, y, args) is applied to every saved value (SubSaveAt.fn,
+        # _saveat.py:20-43); it is called once on the whole batch of saves
+        # (t [B, n_save], y [B, n_save, dim]) and must broadcast over those
+        # leading dimensions, as a vmapped function would
+        self.fn = fn
         self.solver_state, self.controller_state = bool(solver_state), bool(controller_state)
         self.made_jump = bool(made_jump)
         # SubSaveAt.__init__: steps=True means every step (_saveat.py:40-43)

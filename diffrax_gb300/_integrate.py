@@ -195,6 +195,27 @@ def _scalar_time(x, n: int, dev) -> torch.Tensor:
     return t
 
 
+# max_steps=None: an unbounded loop (_integrate.py:1283-1292, 1316-1319); the
+# kernels take the largest step count they can count to
+UNBOUNDED_STEPS = 2**31 - 1
+
+
+def _max_steps(max_steps, saveat, recursive_grad):
+    """The step bound handed to the kernels, with the reference's checks of
+    max_steps=None (_integrate.py:1283-1292, 1316-1319; _adjoint.py:283-292)."""
+    if max_steps is not None:
+        return int(max_steps)
+    if saveat.steps:
+        raise ValueError("`max_steps=None` is incompatible with saving at `steps=n`")
+    if saveat.dense:
+        raise ValueError("`max_steps=None` is incompatible with `saveat.dense=True`")
+    if recursive_grad:
+        # the tape holds every accepted step's time, so it needs the bound
+        raise NotImplementedError("gradients through RecursiveCheckpointAdjoint need a "
+                                  "finite max_steps")
+    return UNBOUNDED_STEPS
+
+
 def _time_arrays(t0, t1, dt0, B, dev):
     """t0, t1, dt0 as FP64 device arrays: one entry each (stride 0) when all
     are scalars, else B entries each (stride 1)."""
@@ -258,8 +279,8 @@ class Lowered:
         self.dtype = y0.dtype
         self.B, self.dim = int(y0.shape[0]), int(y0.shape[1])
         self.y0 = _to_dev(y0, dev).contiguous()
-        if max_steps is None:
-            raise NotImplementedError("max_steps=None is not supported")
+        max_steps = _max_steps(max_steps, saveat, want_grad and not isinstance(
+            adjoint, BacksolveAdjoint))
         ts = saveat.ts
         if ts is not None:
             ts = torch.as_tensor(ts, dtype=torch.float64).to(dev).reshape(-1).contiguous()
@@ -296,7 +317,8 @@ class Lowered:
             self.bwd_fields = lower(terms, kw.get("solver", solver),
                                     kw.get("stepsize_controller", stepsize_controller), saveat,
                                     dim=self.dim, dtype=self.dtype,
-                                    max_steps=kw.get("max_steps", max_steps), n_ts=n_ts,
+                                    max_steps=_max_steps(kw.get("max_steps", max_steps),
+                                                         saveat, False), n_ts=n_ts,
                                     adjoint=self.adjoint, kernel=kernel, schedule=schedule)
             self.bwd_problem = _lib.get_problem(self.bwd_fields)
             self.bwd_throw = bool(kw.get("throw", throw))
@@ -677,6 +699,8 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     if low.n_save == 0 or saveat.state_only:
         # SaveAt(dense=True) or the states alone save no ys (_integrate.py:1527-1539)
         ys = ts_out = None
+    elif getattr(saveat, "fn", None) is not None:
+        ys = saveat.fn(ts_out, ys, args)
     sol = Solution(t0=t0, t1=t1, ts=ts_out, ys=ys,
                    stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],
                               num_rejected_steps=stats[:, 2], max_steps=max_steps),

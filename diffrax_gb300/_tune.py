@@ -209,6 +209,7 @@ class GraphedSolve:
         from ._core import ConstantStepSize
         if stepsize_controller is None:
             stepsize_controller = ConstantStepSize()
+        self._fn = getattr(saveat, "fn", None)
         if saveat.dense:
             raise NotImplementedError("GraphedSolve replays solves without dense output")
         dev = torch.device("cuda", torch.cuda.current_device())
@@ -315,6 +316,8 @@ class GraphedSolve:
             torch.cuda.current_stream().synchronize()
             outs = [h if h is not None else o for o, h in zip(outs, self._host_out)]
         ys, ts, res, stats = outs[:4]
+        if self._fn is not None:
+            ys = self._fn(ts, ys, self.low.args if args is None else args)
         sol = Solution(t0=self.low.t0, t1=self.low.t1, ts=ts, ys=ys,
                        stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],
                                   num_rejected_steps=stats[:, 2], max_steps=self.max_steps),

@@ -334,6 +334,13 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
   if (d.kernel == GBDX_KERNEL_TC && d.field != GBDX_MLP)
     return fail(GBDX_ERR_UNSUPPORTED, "the tensor-core (TC) kernel integrates MLP fields");
   if (d.max_steps < 1) return fail(GBDX_ERR_INVALID, "max_steps must be a positive integer");
+  // the tape and the step-indexed outputs are sized by max_steps: an unbounded
+  // solve (max_steps=None, passed as INT32_MAX) has none of them
+  if (d.max_steps > (1 << 30) &&
+      (d.adjoint == GBDX_ADJ_RECURSIVE || d.save_dense || d.save_steps > 0))
+    return fail(GBDX_ERR_INVALID,
+                "max_steps above 2^30 (an unbounded solve) takes neither SaveAt(steps=n), "
+                "SaveAt(dense=True) nor RecursiveCheckpointAdjoint");
   if (d.n_ts < 0) return fail(GBDX_ERR_INVALID, "negative number of SaveAt(ts=...) points");
   if (d.save_steps < 0) return fail(GBDX_ERR_INVALID, "SaveAt(steps=n) needs n >= 0");
   // Output length (_integrate.py:1273-1293): SaveAt(steps=n) reserves

@@ -153,7 +153,9 @@ typedef struct gbdx_problem_desc {
   double dtmin, dtmax; /* NaN means None */
   int32_t force_dtmin;
   double error_order;  /* 0 means the solver's own (diffrax/_solver/base.py:97-120) */
-  int32_t n_ts, save_t0, save_t1, max_steps;
+  int32_t n_ts, save_t0, save_t1;
+  int32_t max_steps;     /* INT32_MAX: max_steps=None (no SaveAt(steps / dense), no
+                            RecursiveCheckpointAdjoint) */
   int32_t n_args;
   int32_t mlp_depth;     /* number of linear layers */
   int32_t mlp_widths[9]; /* widths[0] = dim, widths[mlp_depth] = dim */

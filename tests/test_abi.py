@@ -426,3 +426,20 @@ def test_bounds_checked_abi_compiles():
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
     os.unlink(obj)
+
+
+def test_max_steps_none_rules():
+    # diffrax/_integrate.py:1283-1292, 1316-1319, _adjoint.py:283-292
+    from diffrax_gb300._integrate import _max_steps, UNBOUNDED_STEPS
+    assert _max_steps(None, dfx.SaveAt(t1=True), False) == UNBOUNDED_STEPS
+    assert _max_steps(17, dfx.SaveAt(steps=2), True) == 17
+    with pytest.raises(ValueError, match="steps=n"):
+        _max_steps(None, dfx.SaveAt(steps=1), False)
+    with pytest.raises(ValueError, match="dense=True"):
+        _max_steps(None, dfx.SaveAt(dense=True), False)
+    with pytest.raises(NotImplementedError, match="finite max_steps"):
+        _max_steps(None, dfx.SaveAt(t1=True), True)
+    # the C ABI takes INT32_MAX for an unbounded forward solve only
+    assert _lib.Problem(_fields(max_steps=UNBOUNDED_STEPS)).n_save == 1
+    with pytest.raises(ValueError, match="unbounded"):
+        _lib.Problem(_fields(max_steps=UNBOUNDED_STEPS, save_steps=1))
