@@ -7,7 +7,7 @@ from ._core import (
     AbstractAdjoint, AbstractField, AbstractSolver, AbstractStepSizeController, AbstractTerm,
     BacksolveAdjoint, ClipStepSizeController, ConstantStepSize, ControlTerm, Dopri5, Dopri8, Euler, Heun, LotkaVolterra,
     MLPField, MultiTerm, ODETerm, OrnsteinUhlenbeck, TanhDiagonalDiffusion, PIDController, RecursiveCheckpointAdjoint,
-    RESULTS, SaveAt, Solution, Tsit5, VanDerPol, VirtualBrownianTree, adjoint_rms_seminorm,
+    RESULTS, SaveAt, SubSaveAt, Solution, Tsit5, VanDerPol, VirtualBrownianTree, adjoint_rms_seminorm,
     rms_norm, Event, LinearCondition, Newton, SteadyStateCondition, steady_state_event,
     AbstractBrownianIncrement, BrownianIncrement, SEA, ShARK, SpaceTimeLevyArea, SRA1,
 )

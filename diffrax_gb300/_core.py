@@ -432,17 +432,67 @@ class Event:
 # ---------------------------------------------------------------------------
 
 
+class SubSaveAt:
+    """diffrax/_saveat.py:14-57: one set of saves (t0, ts, every n-th step,
+    t1) with its own map fn(t, y, args) (called on the batched saves)."""
+
+    def __init__(self, *, t0: bool = False, t1: bool = False, ts=None, steps=False, fn=None):
+        if isinstance(steps, bool):
+            steps = 1 if steps else 0
+        steps = int(steps)
+        if steps < 0:
+            raise ValueError("SaveAt(steps=n) needs n >= 0")
+        if not (t0 or t1 or ts is not None or steps):
+            raise ValueError("Empty saveat -- nothing will be saved.")
+        self.t0, self.t1, self.ts, self.steps, self.fn = bool(t0), bool(t1), ts, steps, fn
+
+
+def _tree_leaves(tree):
+    """The SubSaveAt leaves of a list / tuple / dict tree, in order."""
+    if isinstance(tree, SubSaveAt):
+        return [tree]
+    if isinstance(tree, dict):
+        return [x for k in sorted(tree) for x in _tree_leaves(tree[k])]
+    if isinstance(tree, (list, tuple)):
+        return [x for v in tree for x in _tree_leaves(v)]
+    raise TypeError("SaveAt(subs=...) takes SubSaveAt leaves in lists, tuples and dicts")
+
+
+def _tree_unflatten(tree, leaves):
+    """`tree` with its SubSaveAt leaves replaced, in order, by `leaves`."""
+    it = iter(leaves)
+
+    def go(t):
+        if isinstance(t, SubSaveAt):
+            return next(it)
+        if isinstance(t, dict):
+            out = {k: None for k in t}
+            for k in sorted(t):
+                out[k] = go(t[k])
+            return out
+        return type(t)(go(v) for v in t)
+    return go(tree)
+
+
 class SaveAt:
     """diffrax/_saveat.py:69-105.  ``steps`` is a bool or an int n (save every
     n-th accepted step); ``fn(t, y, args)`` maps the saved values (called on
-    the batched saves); ``dense=True`` records the solution's dense output
-    (``Solution.evaluate`` / ``Solution.derivative``); ``solver_state``,
-    ``controller_state`` and ``made_jump`` keep the final states, which a
-    later ``diffeqsolve`` resumes from."""
+    the batched saves); ``subs`` is a tree (lists, tuples, dicts) of
+    SubSaveAt, whose solution ``ys`` / ``ts`` have the same tree (one solve
+    per SubSaveAt: the solves take the same steps); ``dense=True`` records
+    the solution's dense output (``Solution.evaluate`` / ``.derivative``);
+    ``solver_state``, ``controller_state`` and ``made_jump`` keep the final
+    states, which a later ``diffeqsolve`` resumes from."""
 
     def __init__(self, *, t0: bool = False, t1: bool = False, ts=None, steps=False,
-                 fn=None, dense: bool = False, solver_state: bool = False,
+                 fn=None, subs=None, dense: bool = False, solver_state: bool = False,
                  controller_state: bool = False, made_jump: bool = False):
+        if subs is not None:
+            if t0 or t1 or (ts is not None) or steps:
+                raise ValueError("Cannot pass both `subs` and any of `t0`, `t1`, `ts`, "
+                                 "`steps` to `SaveAt`.")
+            _tree_leaves(subs)  # type check
+        self.subs = subs
         # fn(t, y, args) is applied to every saved value (SubSaveAt.fn,
         # _saveat.py:20-43); it is called once on the whole batch of saves
         # (t [B, n_save], y [B, n_save, dim]) and must broadcast over those
@@ -457,7 +507,7 @@ class SaveAt:
         if steps < 0:
             raise ValueError("SaveAt(steps=n) needs n >= 0")
         # the states alone save no ys (subs = None, _saveat.py:91-93)
-        self.state_only = not (t0 or t1 or ts is not None or steps or dense)
+        self.state_only = subs is None and not (t0 or t1 or ts is not None or steps or dense)
         if self.state_only and not (solver_state or controller_state or made_jump):
             raise ValueError("Empty saveat -- nothing will be saved.")
         self.t0, self.t1, self.ts = bool(t0), bool(t1), ts

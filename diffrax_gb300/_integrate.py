@@ -20,7 +20,7 @@ from ._core import (
     ConstantStepSize, ControlTerm, Event, LinearCondition, SteadyStateCondition,
     Euler, MultiTerm, SpaceTimeLevyArea, ODETerm, OrnsteinUhlenbeck, PIDController,
     RecursiveCheckpointAdjoint, SaveAt, Solution, VirtualBrownianTree, adjoint_rms_seminorm,
-)
+    _tree_leaves, _tree_unflatten)
 
 KERNELS = {"auto": 0, "plain": 1, "fused": 2, "tc": 3}
 SCHEDULES = {"auto": 0, "index": 1, "longest_first": 2}
@@ -663,6 +663,29 @@ def diffeqsolve(terms, solver, t0, t1, dt0, y0, args=None, *,
     device asynchronously, so they must not be modified until the solution's
     tensors have been read.
     """
+    if getattr(saveat, "subs", None) is not None:
+        # one solve per SubSaveAt (the solves take the same steps); the first
+        # also carries the dense output and the states
+        leaves = _tree_leaves(saveat.subs)
+        sols = []
+        for k, sub in enumerate(leaves):
+            first = k == 0
+            sa = SaveAt(t0=sub.t0, t1=sub.t1, ts=sub.ts, steps=sub.steps, fn=sub.fn,
+                        dense=saveat.dense and first,
+                        solver_state=saveat.solver_state and first,
+                        controller_state=saveat.controller_state and first,
+                        made_jump=saveat.made_jump and first)
+            sols.append(diffeqsolve(
+                terms, solver, t0, t1, dt0, y0, args, saveat=sa,
+                stepsize_controller=stepsize_controller, adjoint=adjoint, event=event,
+                max_steps=max_steps, throw=throw, progress_meter=progress_meter,
+                solver_state=solver_state, controller_state=controller_state,
+                made_jump=made_jump, kernel=kernel, block_threads=block_threads,
+                ctas_per_sm=ctas_per_sm, schedule=schedule, autotune=autotune))
+        sol = sols[0]
+        sol.ys = _tree_unflatten(saveat.subs, [x.ys for x in sols])
+        sol.ts = _tree_unflatten(saveat.subs, [x.ts for x in sols])
+        return sol
     resume = solver_state is not None or controller_state is not None or made_jump is not None
     keep_state = saveat.solver_state or saveat.controller_state or saveat.made_jump
     from ._autograd import needs_grad, solve_with_grad

@@ -443,3 +443,20 @@ def test_max_steps_none_rules():
     assert _lib.Problem(_fields(max_steps=UNBOUNDED_STEPS)).n_save == 1
     with pytest.raises(ValueError, match="unbounded"):
         _lib.Problem(_fields(max_steps=UNBOUNDED_STEPS, save_steps=1))
+
+
+def test_saveat_subs_surface():
+    # _saveat.py:14-105: SubSaveAt leaves in a tree; not with t0/t1/ts/steps
+    from diffrax_gb300._core import _tree_leaves, _tree_unflatten
+    a, b = dfx.SubSaveAt(t1=True), dfx.SubSaveAt(ts=[0.5, 1.0], fn=lambda t, y, args: y)
+    tree = {"end": a, "grid": [b]}
+    assert _tree_leaves(tree) == [a, b]
+    assert _tree_unflatten(tree, [1, 2]) == {"end": 1, "grid": [2]}
+    s = dfx.SaveAt(subs=tree, dense=True)
+    assert s.subs is tree and not s.state_only
+    with pytest.raises(ValueError, match="Cannot pass both"):
+        dfx.SaveAt(subs=tree, t1=True)
+    with pytest.raises(ValueError, match="Empty saveat"):
+        dfx.SubSaveAt()
+    with pytest.raises(TypeError):
+        dfx.SaveAt(subs=[a, 3])

@@ -64,3 +64,23 @@ def test_saveat_fn_maps_the_saves():
                              saveat=dfx.SaveAt(ts=ts, fn=fn), stepsize_controller=pid)
     assert mapped.ys.shape == (512, 3, 1)
     assert torch.equal(mapped.ys, fn(plain.ts, plain.ys, mu))
+
+
+def test_saveat_subs_tree_of_solves():
+    # SaveAt(subs={...}): each SubSaveAt's saves, as separate SaveAt solves give them
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(44)
+    y0 = torch.tensor(rng.uniform(-2, 2, (256, 2)), dtype=torch.float32, device=dev)
+    mu = torch.ones((1,), dtype=torch.float32, device=dev)
+    pid = dfx.PIDController(rtol=1e-6, atol=1e-9)
+    term = dfx.ODETerm(dfx.VanDerPol())
+    subs = {"t1": dfx.SubSaveAt(t1=True), "grid": [dfx.SubSaveAt(ts=[0.5, 1.5], t0=True),
+                                                   dfx.SubSaveAt(steps=2)]}
+    sol = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, 2.0, None, y0, mu,
+                          saveat=dfx.SaveAt(subs=subs), stepsize_controller=pid)
+    for got, sa in ((sol.ys["t1"], dfx.SaveAt(t1=True)),
+                    (sol.ys["grid"][0], dfx.SaveAt(ts=[0.5, 1.5], t0=True)),
+                    (sol.ys["grid"][1], dfx.SaveAt(steps=2))):
+        want = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, 2.0, None, y0, mu, saveat=sa,
+                               stepsize_controller=pid)
+        assert torch.equal(got, want.ys)
