@@ -570,6 +570,113 @@ def workload_next_rows(dev, flush, steps, warmup):
     return out
 
 
+def workload_analytic_grads(dev, flush, steps, warmup):
+    """Gradients of the analytic fields, forward + backward timed on the
+    device, errors (per trajectory, relative to the batch's largest gradient)
+    against the FP64 oracle's gradients on 256 trajectories; loss = sum of
+    y(t1)^2, gradients with respect to y0 and the per-trajectory args.
+
+    vdp: the uneven Van der Pol batch (mu ~ LogU[0.1, 10], (x0, y0) ~
+    U[-2, 2]^2, t1 ~ U[5, 50], Dopri5 + PID(1e-6, 1e-9, p=.3, i=.4), B =
+    65 536, FP32 state) through RecursiveCheckpointAdjoint (the full step
+    tape), fused and plain forms.  BacksolveAdjoint is not run on it: the
+    Van der Pol limit cycle attracts forward in time and repels backward, so
+    the reverse solve of y diverges over these horizons (in the oracle too).
+    lv: Lotka-Volterra (args 0.1, 0.02, 0.4, 0.02 x U[0.8, 1.2] per
+    trajectory, y0 ~ U[5, 15]^2, t in [0, 20], Tsit5 + PID(1e-6, 1e-8), B =
+    65 536, FP32 state) through both adjoints."""
+    import torch
+    import diffrax_gb300 as dfx
+    import oracle as O
+    from diffrax_gb300._integrate import Lowered
+    B, n_chk = 65536, 256
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(2024)
+    cases = {}
+    mu = np.exp(rng.uniform(np.log(0.1), np.log(10.0), B))
+    cases["vdp"] = dict(term=dfx.ODETerm(dfx.VanDerPol()), solver=dfx.Dopri5(),
+                        ctrl=dfx.PIDController(rtol=1e-6, atol=1e-9, pcoeff=0.3, icoeff=0.4),
+                        y0=rng.uniform(-2, 2, (B, 2)), args=mu[:, None],
+                        t1=rng.uniform(5.0, 50.0, B),
+                        rows=(("recursive_fused", dfx.RecursiveCheckpointAdjoint(), "fused"),
+                              ("recursive_plain", dfx.RecursiveCheckpointAdjoint(), "plain")))
+    lv = np.array([0.1, 0.02, 0.4, 0.02])
+    cases["lv"] = dict(term=dfx.ODETerm(dfx.LotkaVolterra()), solver=dfx.Tsit5(),
+                       ctrl=dfx.PIDController(rtol=1e-6, atol=1e-8),
+                       y0=rng.uniform(5, 15, (B, 2)), args=lv * rng.uniform(0.8, 1.2, (B, 4)),
+                       t1=np.full(B, 20.0),
+                       rows=(("recursive_fused", dfx.RecursiveCheckpointAdjoint(), "fused"),
+                             ("backsolve_fused", dfx.BacksolveAdjoint(), "fused")))
+    out = {"workload": "vdp_dopri5_pid_uneven_t1_b65536 and lv_tsit5_pid_t20_b65536, "
+                       "loss sum y(t1)^2, gradients wrt y0 and args",
+           "unit": "trajectory gradients/s"}
+    for cname, c in cases.items():
+        y0_d = torch.tensor(c["y0"], dtype=torch.float32, device=dev)
+        a_d = torch.tensor(c["args"], dtype=torch.float32, device=dev)
+        t1_d = torch.tensor(c["t1"], dtype=torch.float64, device=dev)
+        res_c, ref = {}, {}
+        for name, adjoint, kernel in c["rows"]:
+            low = Lowered(c["term"], c["solver"], 0.0, t1_d, None, y0_d, a_d,
+                          dfx.SaveAt(t1=True), c["ctrl"], adjoint, 4096, kernel, 0, 0,
+                          want_grad=True)
+            backsolve = isinstance(adjoint, dfx.BacksolveAdjoint)
+
+            def step():
+                if backsolve:
+                    ys, ts_out, _, _ = low.run_forward()
+                    return low.run_backsolve_args(ts_out, ys, 2.0 * ys, low.args)
+                ys, _, _, _, ws = low.run_forward(keep_workspace=True)
+                return low.run_backward_args(ws, 2.0 * ys, low.y0, low.args)
+            ms = _events_time(step, steps, warmup, flush)
+            ys, ts_out, res, _ = low.run_forward()
+            g = step()
+            torch.cuda.synchronize()
+            kind = "backsolve" if backsolve else "recursive"
+            if kind not in ref:
+                G = 2.0 * ys[:n_chk].double().cpu().numpy()
+                if backsolve:
+                    d = O.make_desc(**O.oracle_fields(low.bwd_fields))
+                    ref[kind] = O.backsolve(d, 0.0, c["t1"][:n_chk], None,
+                                            ts_out[:n_chk].cpu().numpy(),
+                                            ys[:n_chk].double().cpu().numpy(), G,
+                                            args=c["args"][:n_chk], nthreads=cores)
+                else:
+                    d = O.make_desc(**O.oracle_fields(low.fields))
+                    ref[kind] = O.grad_recursive(d, 0.0, c["t1"][:n_chk], None,
+                                                 c["y0"][:n_chk], G, args=c["args"][:n_chk],
+                                                 nthreads=cores)
+                    # the CPU baseline: the oracle's forward + backward on a
+                    # larger sample of the same batch (the library is loaded)
+                    n_cpu = 16384
+                    Gc = 2.0 * ys[:n_cpu].double().cpu().numpy()
+                    t = time.perf_counter()
+                    O.grad_recursive(d, 0.0, c["t1"][:n_cpu], None, c["y0"][:n_cpu], Gc,
+                                     args=c["args"][:n_cpu], nthreads=cores)
+                    ref["cpu_s"] = time.perf_counter() - t
+                    ref["cpu_n"] = n_cpu
+            r = ref[kind]
+            gy = g[0][:n_chk].double().cpu().numpy()
+            ga = g[1][:n_chk].double().cpu().numpy()
+            ey = np.abs(gy - r["grad_y0"]).max(axis=1) / np.abs(r["grad_y0"]).max()
+            ea = np.abs(ga - r["grad_args"]).max(axis=1) / np.abs(r["grad_args"]).max()
+            res_c[name] = {"grads_per_s": B / (ms / 1e3), "ms": ms,
+                           "all_successful": bool((res == 0).all().item()),
+                           "dL_dy0_rel_err_vs_fp64_oracle": {"median": float(np.median(ey)),
+                                                             "max": float(ey.max())},
+                           "dL_dargs_rel_err_vs_fp64_oracle": {"median": float(np.median(ea)),
+                                                               "max": float(ea.max())}}
+        res_c["cpu_baseline"] = {"value": ref["cpu_n"] / ref["cpu_s"],
+                                 "unit": "trajectory gradients/s", "cores": cores,
+                                 "kind": "port",
+                                 "sample": f"{ref['cpu_n']} trajectories forward + recursive "
+                                           f"backward, FP64 oracle, {ref['cpu_s']:.2f} s"}
+        out[cname] = res_c
+    v = out["vdp"]
+    v["recursive_fused_over_plain"] = (v["recursive_fused"]["grads_per_s"] /
+                                       v["recursive_plain"]["grads_per_s"])
+    return out
+
+
 def _per_row_max(a, b):
     """max over rows of max|a - b| / max|b| within the row."""
     return float(_rel_per_traj(a, b).max())
@@ -1162,7 +1269,8 @@ def main():
                         ("neural_ode", lambda: workload_neural(dev, flush, 5, 3, "ode")),
                         ("neural_ode_wide", lambda: workload_neural(dev, flush, 5, 3, "wide")),
                         ("neural_sde", lambda: workload_neural(dev, flush, 5, 3, "sde")),
-                        ("next_rows", lambda: workload_next_rows(dev, flush, 10, 3))):
+                        ("next_rows", lambda: workload_next_rows(dev, flush, 10, 3)),
+                        ("analytic_grads", lambda: workload_analytic_grads(dev, flush, 5, 3))):
             try:
                 others[key] = fn()
             except Exception as exc:  # report, never hide the headline line

@@ -772,14 +772,19 @@ static int prepare(const gbdx_problem *problem, int64_t batch, const double *t0,
 
 // Reset the work counter and (per-trajectory intervals) build the
 // longest-first order, both on stream s.
+// Whether the fused kernels take the trajectories longest-first: per-trajectory
+// intervals and the schedule allowing it.
+static bool longest_first_order(const gbdx_problem_desc &d, int64_t time_stride) {
+  return time_stride == 1 && (d.schedule == GBDX_SCHED_LONGEST_FIRST ||
+                              d.schedule == GBDX_SCHED_AUTO);
+}
+
 static int start_queue(const gbdx_problem *problem, gbdx::SolveParams &P, void *workspace,
                        cudaStream_t s) {
   const gbdx_problem_desc &d = problem->d;
   cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return cuda_fail(e, "queue reset");
-  const bool longest_first = d.schedule == GBDX_SCHED_LONGEST_FIRST ||
-                             (d.schedule == GBDX_SCHED_AUTO && P.time_stride == 1);
-  if (longest_first && P.time_stride == 1) {
+  if (longest_first_order(d, P.time_stride)) {
     int32_t *order = nullptr;
     e = gbdx::build_longest_first_order(P.t0, P.t1, P.batch,
                                         static_cast<char *>(workspace) + kQueueBytes, &order,
@@ -1019,7 +1024,11 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   if (rc != GBDX_OK) return rc;
   if (problem->adj.rc_bwd) {
     // analytic fields: grad_params receives dL/dargs, per trajectory
-    // [batch, n_args] when args has a row per trajectory, else [n_args]
+    // [batch, n_args] when args has a row per trajectory, else [n_args].  The
+    // tape rows are the forward's queue slots: its work order (left in the
+    // workspace by the forward) maps them back to trajectories.
+    if (problem->d.kernel != GBDX_KERNEL_PLAIN && longest_first_order(problem->d, time_stride))
+      P.order = reinterpret_cast<const int32_t *>(static_cast<char *>(workspace) + kQueueBytes);
     gbdx::AdjParams A;
     memset(&A, 0, sizeof A);
     A.grad_ys = grad_ys;

@@ -85,14 +85,18 @@ template <int SOLVER, class F, class T>
 __global__ void __launch_bounds__(128) ode_rc_bwd_kernel(SolveParams P, AdjParams Q) {
   using TB = Tab<SOLVER>;
   constexpr int S = TB::S, D = F::D, NA = F::NARGS;
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= P.batch) return;
+  // thread q takes the trajectory the forward took from queue slot q, whose
+  // tape is row q (the forward's work order, when it had one): neighbouring
+  // threads read neighbouring rows and have similar step counts
+  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= P.batch) return;
+  const int64_t i = P.order ? int64_t(P.order[q]) : q;
   const int64_t ti = i * P.time_stride;
   const int dir = (P.t0[ti] < P.t1[ti]) ? 1 : -1;
   const double t0 = dir * P.t0[ti], t1 = dir * P.t1[ti];
-  const int N = P.tape_n[i];
-  const double *tt = P.tape_t + i * int64_t(P.max_steps + 1);
-  const T *ty = reinterpret_cast<const T *>(P.tape_y) + i * int64_t(P.checkpoints) * D;
+  const int N = P.tape_n[q];
+  const double *tt = P.tape_t + q * int64_t(P.max_steps + 1);
+  const T *ty = reinterpret_cast<const T *>(P.tape_y) + q * int64_t(P.checkpoints) * D;
   const T *G = static_cast<const T *>(Q.grad_ys) + i * int64_t(P.n_save) * D;
   const T *ap = static_cast<const T *>(P.args) + i * P.args_stride;
   T a[NA];

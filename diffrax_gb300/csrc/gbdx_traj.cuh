@@ -226,6 +226,10 @@ struct Traj {
   int evi;
   double tfin;
   int64_t idx;
+  // the trajectory's row of the gradient tape: its queue slot, so that the
+  // rows a warp writes together are neighbours however the work order
+  // permutes the trajectories (scattered rows cost page-translation misses)
+  int64_t trow;
   T wb[FIELD::SDE ? D : 1];  // SDE: W(tprev) of every component (FP32 fields only)
   // Levy area tree: wb holds W_unit(r) and hb bar H_unit(r) at the unit time
   // rb of tprev (unscaled, for Chen's relation)
@@ -244,8 +248,9 @@ struct Traj {
     return GBDX_AT(P, P.ts_out, idx * P.n_save + slot, 1, P.batch * P.n_save, GBDX_SITE_TS);
   }
 
-  __device__ void init(const SolveParams &P, int64_t i) {
+  __device__ void init(const SolveParams &P, int64_t i, int64_t row) {
     idx = i;
+    trow = row;
     const int64_t ti = i * P.time_stride;
     double a = P.t0[ti], b = P.t1[ti];
     dir = (a < b) ? 1 : -1;  // _integrate.py:1160
@@ -344,9 +349,9 @@ struct Traj {
     if constexpr (FIELD::TAPE) {
       // full gradient tape: the time and state at every accepted step
       if (P.tape_t) {
-        *GBDX_AT(P, P.tape_t, i * (P.max_steps + 1), 1, P.batch * (P.max_steps + 1),
+        *GBDX_AT(P, P.tape_t, row * (P.max_steps + 1), 1, P.batch * (P.max_steps + 1),
                  GBDX_SITE_TAPE_T) = a;
-        T *o = GBDX_AT(P, reinterpret_cast<T *>(P.tape_y), i * int64_t(P.checkpoints) * D, D,
+        T *o = GBDX_AT(P, reinterpret_cast<T *>(P.tape_y), row * int64_t(P.checkpoints) * D, D,
                        P.batch * P.checkpoints * D, GBDX_SITE_TAPE_Y);
 #pragma unroll
         for (int n = 0; n < D; n++) o[n] = y[n];
@@ -911,10 +916,10 @@ struct Traj {
       }
       if constexpr (FIELD::TAPE) {
         if (P.tape_t) {
-          *GBDX_AT(P, P.tape_t, idx * (P.max_steps + 1) + nacc + 1, 1,
+          *GBDX_AT(P, P.tape_t, trow * (P.max_steps + 1) + nacc + 1, 1,
                    P.batch * (P.max_steps + 1), GBDX_SITE_TAPE_T) = tnext;
           T *o = GBDX_AT(P, reinterpret_cast<T *>(P.tape_y),
-                         (idx * int64_t(P.checkpoints) + nacc + 1) * D, D,
+                         (trow * int64_t(P.checkpoints) + nacc + 1) * D, D,
                          P.batch * P.checkpoints * D, GBDX_SITE_TAPE_Y);
 #pragma unroll
           for (int n = 0; n < D; n++) o[n] = y1[n];
@@ -1034,8 +1039,8 @@ struct Traj {
     P.result_out[idx] = r;
     if constexpr (FIELD::TAPE) {
       if (P.tape_n) {
-        P.tape_n[idx] = nacc;
-        P.tape_stride[idx] = 1;
+        P.tape_n[trow] = nacc;
+        P.tape_stride[trow] = 1;
       }
     }
     P.stats_out[idx * 3 + 0] = nsteps;
@@ -1076,7 +1081,7 @@ __global__ void __launch_bounds__(128) plain_kernel(SolveParams P) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= P.batch) return;
   Traj<SOLVER, FIELD, T, false, XO> tr;
-  tr.init(P, i);
+  tr.init(P, i, i);
   while (tr.running(P)) tr.step(P);
   tr.finish(P);
 }
@@ -1105,7 +1110,7 @@ __global__ void __launch_bounds__(256) fused_kernel(SolveParams P) {
         if (!active) {
           const unsigned long long mine = base + __popc(need & lt_mask);
           if (mine < (unsigned long long)P.batch) {
-            tr.init(P, P.order ? (int64_t)P.order[mine] : (int64_t)mine);
+            tr.init(P, P.order ? (int64_t)P.order[mine] : (int64_t)mine, (int64_t)mine);
             active = true;
           }
         }
