@@ -581,9 +581,9 @@ def _state_record(low: "Lowered", solver_state, controller_state, made_jump):
     solver_state / controller_state / made_jump (_integrate.py:1252-1271,
     1309), in the layouts Solution documents."""
     f = low.fields
-    if f["n_step_ts"] or f["n_jump_ts"] or f["field"] == 3:
-        raise NotImplementedError("resuming is supported for the analytic fields without "
-                                  "a ClipStepSizeController")
+    if f["n_step_ts"] or f["n_jump_ts"] or (f["field"] == 3 and f["kernel"] in (1, 3)):
+        raise NotImplementedError("resuming is supported without a ClipStepSizeController, "
+                                  "on the trajectory kernels and the fused MLP kernel")
     B, D, dev = low.B, low.dim, low.device
     rec = torch.zeros((B, STATE_HEAD + D), dtype=torch.float64, device=dev)
     rec[:, 5] = 1.0

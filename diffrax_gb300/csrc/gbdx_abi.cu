@@ -575,15 +575,18 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
       *out = p;
       return GBDX_OK;
     }
-    if (D == 64 && H == 128)
-      p->ode = xo ? gbdx::find_mlp_xo_entry_d64h128(d.solver, precise, sde)
-                  : gbdx::find_mlp_entry_d64h128(d.solver, precise, sde);
-    if (D == 64 && H == 256)
-      p->ode = xo ? gbdx::find_mlp_xo_entry_d64h256(d.solver, precise, sde)
-                  : gbdx::find_mlp_entry_d64h256(d.solver, precise, sde);
-    if (D == 32 && H == 64)
-      p->ode = xo ? gbdx::find_mlp_xo_entry_d32h64(d.solver, precise, sde)
-                  : gbdx::find_mlp_entry_d32h64(d.solver, precise, sde);
+    if (D == 64 && H == 128) {
+      p->ode_xo = gbdx::find_mlp_xo_entry_d64h128(d.solver, precise, sde);
+      p->ode = xo ? p->ode_xo : gbdx::find_mlp_entry_d64h128(d.solver, precise, sde);
+    }
+    if (D == 64 && H == 256) {
+      p->ode_xo = gbdx::find_mlp_xo_entry_d64h256(d.solver, precise, sde);
+      p->ode = xo ? p->ode_xo : gbdx::find_mlp_entry_d64h256(d.solver, precise, sde);
+    }
+    if (D == 32 && H == 64) {
+      p->ode_xo = gbdx::find_mlp_xo_entry_d32h64(d.solver, precise, sde);
+      p->ode = xo ? p->ode_xo : gbdx::find_mlp_entry_d32h64(d.solver, precise, sde);
+    }
     if (!p->ode.launch) {
       delete p;
       return fail(GBDX_ERR_UNSUPPORTED,
@@ -810,11 +813,11 @@ static int solve_fwd(const gbdx_problem *problem, int64_t batch, const double *t
   int32_t *dense_n = ex ? ex->dense_n : nullptr;
   const gbdx_problem_desc &d = problem->d;
   const bool resume = ex && (ex->state_in || ex->state_out);
-  if (resume && (d.field == GBDX_MLP || d.n_step_ts > 0 || d.n_jump_ts > 0 ||
-                 d.adjoint != GBDX_ADJ_NONE || !problem->ode_xo.launch))
+  if (resume && (d.n_step_ts > 0 || d.n_jump_ts > 0 || d.adjoint != GBDX_ADJ_NONE ||
+                 !problem->ode_xo.launch))
     return fail(GBDX_ERR_UNSUPPORTED,
-                "solver and controller states are available for forward solves of the analytic "
-                "fields without a ClipStepSizeController");
+                "solver and controller states are available for forward solves without a "
+                "ClipStepSizeController on the trajectory kernels and the fused MLP kernel");
   if (batch < 0) return fail(GBDX_ERR_INVALID, "negative batch");
   if (batch == 0) return GBDX_OK;
   if ((problem->n_save > 0 && (!ys_out || !ts_out)) || !result_out || !stats_out)

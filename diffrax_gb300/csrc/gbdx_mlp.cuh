@@ -332,7 +332,7 @@ __device__ __forceinline__ bool row_running(const RowState<M> &R, int r, int max
 
 template <int M, bool XO>
 __device__ void row_init(RowState<M> &R, RowEvents<M> *EV, int r, int64_t i,
-                         const SolveParams &P, int D) {
+                         const SolveParams &P, int D, bool fsal) {
   const int64_t ti = i * P.time_stride;
   double a = P.t0[ti], b = P.t1[ti];
   const int dir = (a < b) ? 1 : -1;
@@ -376,6 +376,34 @@ __device__ void row_init(RowState<M> &R, RowEvents<M> *EV, int r, int64_t i,
   R.cpcompact[r] = 0;
   R.at_dtmin[r] = 0;
   R.live[r] = 0;
+  if constexpr (XO) {
+    // a passed controller and solver state (the resume record of
+    // gbdx_fwd_extras, _integrate.py:1252-1271, 1309): the PID history (held
+    // here as log2) or the constant grid, and whether the FSAL value the
+    // element pass loads replaces the first evaluation
+    if (P.state_in) {
+      const double *st =
+          GBDX_AT(P, P.state_in, i * int64_t(GBDX_STATE_HEAD + D), GBDX_STATE_HEAD + D,
+                  P.batch * (GBDX_STATE_HEAD + D), GBDX_SITE_STATE);
+      if (st[4] != 0.0) {
+        if (P.controller == GBDX_PID) {
+          R.hist1[r] = float(log2(st[0]));
+          R.hist2[r] = float(log2(st[1]));
+          R.at_dtmin[r] = st[2] != 0.0;
+          if (P.dt0) {  // the first step is t0 + dt0, unclipped by dtmin / dtmax
+            R.tnext[r] = fmin(a + P.dt0[ti] * dir, b);
+            R.dtc[r] = R.tnext[r] - a;
+          }
+        } else {
+          R.sc[r] = int(st[0]);
+          R.nc[r] = int(st[1]);
+          R.t0s[r] = st[2];
+          R.t1s[r] = st[3];
+        }
+      }
+      if (fsal && st[5] == 0.0 && st[6] == 0.0) R.first[r] = 0;
+    }
+  }
   if (P.save_t0) {
     *GBDX_AT(P, P.ts_out, i * P.n_save, 1, P.batch * P.n_save, GBDX_SITE_TS) = a * dir;
     R.save_index[r] = 1;
@@ -653,6 +681,23 @@ __device__ __forceinline__ double steady_value(const SolveParams &P, const RowEv
              : 0.0;
 }
 
+// The FSAL values of freshly loaded rows resumed from a record with a valid
+// solver state (row_init cleared their `first`).
+template <class SH, int M, int NE>
+__device__ __forceinline__ void load_fsal_state(float (&F0)[NE], const SolveParams &P,
+                                                const RowState<M> &R, int warp, int lane) {
+  constexpr int D = SH::D;
+#pragma unroll
+  for (int e = 0; e < NE; e++) {
+    int row, col;
+    elem_rc<SH>(e, warp, lane, row, col);
+    if (R.loaded[row] && !R.first[row])
+      F0[e] = float(*GBDX_AT(P, P.state_in, R.idx[row] * int64_t(GBDX_STATE_HEAD + D) +
+                                                GBDX_STATE_HEAD + col,
+                             1, P.batch * (GBDX_STATE_HEAD + D), GBDX_SITE_STATE));
+  }
+}
+
 // The solver's local interpolant inside a step, one component: its value at
 // theta or its theta-derivative, from y0, y1 and the stage increments k(j)
 // (the trajectory kernels' formulas).
@@ -761,7 +806,8 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
   if (tid < M) {
     const unsigned long long q = atomicAdd(P.queue, 1ull);
     if (q < (unsigned long long)P.batch) {
-      row_init<M, XO>(R, EV, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P, D);
+      row_init<M, XO>(R, EV, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P, D,
+                       TB::FSAL);
       R.loaded[tid] = 1;
     } else {
       R.active[tid] = 0;
@@ -783,6 +829,9 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
   vc.traj = -1;
   vc.node = 0;
   load_rows<SH, SDE>(Y0, F0, Wb, P, R, warp, lane);
+  if constexpr (XO && TB::FSAL) {
+    if (P.state_in) load_fsal_state<SH>(F0, P, R, warp, lane);
+  }
   if constexpr (SDE) load_brownian<SH>(P, R, vc, Wb, warp, lane);
   __syncthreads();
   if (tid < M) R.loaded[tid] = 0;
@@ -1159,6 +1208,28 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
           if (root && EV->evi[tid] >= 0) tf = EV->tfin[tid];
           if (P.event_index) P.event_index[i] = EV->evi[tid];
           if (P.dense_n) P.dense_n[i] = R.nacc[tid] + 1;
+          if (P.state_out) {
+            // SaveAt(controller_state=, solver_state=, made_jump=)
+            // (_integrate.py:1489-1500): the head of the record; the
+            // element pass writes the FSAL value
+            double *so = GBDX_AT(P, P.state_out, i * int64_t(GBDX_STATE_HEAD + D),
+                                 GBDX_STATE_HEAD, P.batch * (GBDX_STATE_HEAD + D),
+                                 GBDX_SITE_STATE);
+            if (P.controller == GBDX_PID) {
+              so[0] = exp2(double(R.hist1[tid]));
+              so[1] = exp2(double(R.hist2[tid]));
+              so[2] = R.at_dtmin[tid] ? 1.0 : 0.0;
+              so[3] = 0.0;
+            } else {
+              so[0] = R.sc[tid];
+              so[1] = R.nc[tid];
+              so[2] = R.t0s[tid];
+              so[3] = R.t1s[tid];
+            }
+            so[4] = 1.0;
+            so[5] = (TB::FSAL && !R.first[tid]) ? 0.0 : 1.0;
+            so[6] = 0.0;  // made_jump: set by a ClipStepSizeController only
+          }
         }
         if (R.sflag[tid])
           *GBDX_AT(P, P.ts_out, i * P.n_save + si++, 1, tse, GBDX_SITE_TS) = tf * dir;
@@ -1197,13 +1268,21 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
           if (!P.saves_prefilled)
             for (int m = si; m < P.n_save; m++)
               *GBDX_AT(P, o, b0 + m * D, 1, ext, GBDX_SITE_YS) = INFINITY;
+          if constexpr (XO) {
+            if (P.state_out)  // the record's FSAL value (0 where there is none)
+              *GBDX_AT(P, P.state_out,
+                       R.idx[row] * int64_t(GBDX_STATE_HEAD + D) + GBDX_STATE_HEAD + col, 1,
+                       P.batch * (GBDX_STATE_HEAD + D), GBDX_SITE_STATE) =
+                  (TB::FSAL && !R.first[row]) ? double(F0[e]) : 0.0;
+          }
         }
       }
       __syncthreads();
       if (tid < M && R.fin[tid]) {
         const unsigned long long q = atomicAdd(P.queue, 1ull);
         if (q < (unsigned long long)P.batch) {
-          row_init<M, XO>(R, EV, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P, D);
+          row_init<M, XO>(R, EV, tid, P.order ? (int64_t)P.order[q] : (int64_t)q, P, D,
+                       TB::FSAL);
           R.loaded[tid] = 1;
         } else {
           R.active[tid] = 0;
@@ -1211,6 +1290,9 @@ __global__ void __launch_bounds__(256) mlp_fused_kernel(SolveParams P) {
       }
       __syncthreads();
       load_rows<SH, SDE>(Y0, F0, Wb, P, R, warp, lane);
+      if constexpr (XO && TB::FSAL) {
+        if (P.state_in) load_fsal_state<SH>(F0, P, R, warp, lane);
+      }
       if constexpr (SDE) load_brownian<SH>(P, R, vc, Wb, warp, lane);
       __syncthreads();
       if (tid < M) R.loaded[tid] = 0;

@@ -178,3 +178,46 @@ def test_states_alone_save_no_ys_and_unsupported_forms_raise():
     with pytest.raises(NotImplementedError, match="ClipStepSizeController"):
         dfx.diffeqsolve(dfx.ODETerm(dfx.VanDerPol()), dfx.Heun(), 0.0, 1.0, 0.1, y0, mu,
                         stepsize_controller=clip, saveat=dfx.SaveAt(t1=True, made_jump=True))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_mlp_resume_matches_oracle(precision):
+    # 64 -> 128 -> 128 -> 64 (BF16 weights), Tsit5 + PID(1e-5, 1e-7): leg 1 on
+    # [0, 0.5] saving the states, leg 2 on [0.5, 1] resumed from them, against
+    # the oracle resumed from the same records
+    from test_gpu_mlp import mlp_params, flat
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(61)
+    B, D = 128, 64
+    y0 = rng.standard_normal((B, D))
+    Ws, bs = mlp_params([64, 128, 128, 64], 13, bias_scale=0.1)
+    Ws = [W.astype(np.float32).astype(np.float64) for W in Ws]
+    bs = [b.astype(np.float32).astype(np.float64) for b in bs]
+    field = dfx.MLPField([torch.tensor(W, dtype=torch.float32, device=dev) for W in Ws],
+                         [torch.tensor(b, dtype=torch.float32, device=dev) for b in bs],
+                         precision=precision)
+    ctrl = dfx.PIDController(rtol=1e-5, atol=1e-7)
+    sa = dfx.SaveAt(t1=True, **STATES)
+    s1 = dfx.diffeqsolve(dfx.ODETerm(field), dfx.Tsit5(), 0.0, 0.5, 0.05,
+                         torch.tensor(y0, dtype=torch.float32, device=dev), saveat=sa,
+                         stepsize_controller=ctrl)
+    rec1 = _record(s1)
+    assert (rec1[:, 4] == 1).all() and (rec1[:, 5] == 0).all()  # states and an FSAL value
+    s2 = dfx.diffeqsolve(dfx.ODETerm(field), dfx.Tsit5(), 0.5, 1.0, 0.05, s1.ys[:, -1],
+                         saveat=sa, stepsize_controller=ctrl, solver_state=s1.solver_state,
+                         controller_state=s1.controller_state, made_jump=s1.made_jump)
+    torch.cuda.synchronize()
+    fields = dfx.lower(dfx.ODETerm(field), dfx.Tsit5(), ctrl, sa, dim=D, dtype=torch.float32,
+                       max_steps=4096, n_ts=0)
+    d = O.make_desc(**O.oracle_fields(fields))
+    r2 = O.solve(d, 0.5, 1.0, 0.05, s1.ys[:, -1].double().cpu().numpy(),
+                 params=flat(Ws, bs), state_in=rec1, want_state=True, nthreads=8)
+    ys = s2.ys.double().cpu().numpy()
+    err = np.abs(ys - r2["ys"]).max() / np.abs(r2["ys"]).max()
+    print(f"MLP resume {precision}: max rel err {err:.2e}")
+    assert err < 2e-5
+    # the FSAL value in the record is the field at the final state
+    rec2 = _record(s2)
+    f_end = rec2[:, 7:]
+    fr = r2["state"][:, 7:]
+    assert np.abs(f_end - fr).max() < 1e-4 * np.abs(fr).max()
