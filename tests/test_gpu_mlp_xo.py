@@ -291,3 +291,46 @@ def test_mlp_linear_event_root_matches_oracle(direction, precision):
     last = np.array([ys[b][np.isfinite(ts[b])][-1] for b in range(ys.shape[0])])
     g = last[:, 0] + 0.5 * last[:, 1] - 0.25
     assert np.abs(g[ok]).max() < 1e-4
+
+
+def test_mlp_reverse_time_steps_dense_and_event():
+    # t0 = 1 > t1 = 0, Tsit5 dt 0.05 (the loop runs in flipped time): step
+    # saves, the dense output and a downward crossing with Newton, against
+    # the oracle
+    rng = np.random.default_rng(30)
+    B = 128
+    y0 = rng.standard_normal((B, 64))
+    Ws, bs = mlp_params([64, 128, 128, 64], 12, bias_scale=0.1)
+    Ws = [W.astype(np.float32).astype(np.float64) for W in Ws]
+    bs = [b.astype(np.float32).astype(np.float64) for b in bs]
+    dev = torch.device("cuda")
+    field = dfx.MLPField([torch.tensor(W, dtype=torch.float32, device=dev) for W in Ws],
+                         [torch.tensor(b, dtype=torch.float32, device=dev) for b in bs],
+                         precision="fp32")
+    ev = dfx.Event(dfx.LinearCondition([1.0], offset=-0.5), dfx.Newton(1e-6, 1e-6),
+                   direction=False)
+    saveat = dfx.SaveAt(steps=2, t1=True, dense=True)
+    sol = dfx.diffeqsolve(dfx.ODETerm(field), dfx.Tsit5(), 1.0, 0.0, -0.05,
+                          torch.tensor(y0, dtype=torch.float32, device=dev), saveat=saveat,
+                          stepsize_controller=dfx.ConstantStepSize(), event=ev, max_steps=64,
+                          throw=False)
+    torch.cuda.synchronize()
+    fields = dfx.lower(dfx.ODETerm(field), dfx.Tsit5(), dfx.ConstantStepSize(), saveat, dim=64,
+                       dtype=torch.float32, max_steps=64, n_ts=0, event=ev)
+    d = O.make_desc(**O.oracle_fields(fields))
+    r = O.solve(d, 1.0, 0.0, -0.05, y0, params=flat(Ws, bs), nthreads=8)
+    res = sol.result.cpu().numpy()
+    agree = (res == r["result"]) & (sol.event_mask.cpu().numpy() == (r["event_index"] == 0))
+    assert agree.mean() >= 0.97
+    ts, rt = sol.ts.cpu().numpy()[agree], r["ts"][agree]
+    assert np.array_equal(np.isneginf(ts), np.isneginf(rt))  # direction * inf padding
+    fin = np.isfinite(rt)
+    assert np.abs(ts[fin] - rt[fin]).max() < 1e-5
+    ys, ry = sol.ys.cpu().double().numpy()[agree], r["ys"][agree]
+    fy = np.isfinite(ry)
+    assert np.abs(ys[fy] - ry[fy]).max() < 1e-4 * np.abs(ry[fy]).max()
+    q = np.linspace(1.0, 0.3, 15)
+    ev_q = sol.evaluate(torch.tensor(q, dtype=torch.float64, device=dev)).cpu().double().numpy()
+    rq = O.dense_evaluate(d, 1.0, 0.0, y0, r, q)
+    ok = np.isfinite(rq).all(axis=(1, 2)) & agree
+    assert np.abs(ev_q[ok] - rq[ok]).max() < 1e-4 * np.abs(rq[ok]).max()
