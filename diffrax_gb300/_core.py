@@ -292,9 +292,23 @@ def adjoint_rms_seminorm(x):  # marker, diffrax/_misc.py:85-116
     raise NotImplementedError("adjoint_rms_seminorm is evaluated inside the kernels")
 
 
+class _MetaPID(type):
+    """PIDController(..., step_ts=s, jump_ts=j) is
+    ClipStepSizeController(PIDController(...), s, j) (pid.py:88-97)."""
+
+    def __call__(cls, *args, **kwargs):
+        step_ts = kwargs.pop("step_ts", None)
+        jump_ts = kwargs.pop("jump_ts", None)
+        if step_ts is not None or jump_ts is not None:
+            return ClipStepSizeController(super().__call__(*args, **kwargs), step_ts=step_ts,
+                                          jump_ts=jump_ts)
+        return super().__call__(*args, **kwargs)
+
+
 @dataclasses.dataclass(frozen=True)
-class PIDController(AbstractStepSizeController):
-    """diffrax/_step_size_controller/pid.py:109-580 (same fields and defaults)."""
+class PIDController(AbstractStepSizeController, metaclass=_MetaPID):
+    """diffrax/_step_size_controller/pid.py:109-580 (same fields and defaults;
+    ``step_ts`` / ``jump_ts`` build the ClipStepSizeController)."""
     rtol: float
     atol: float
     pcoeff: float = 0.0

@@ -460,3 +460,11 @@ def test_saveat_subs_surface():
         dfx.SubSaveAt()
     with pytest.raises(TypeError):
         dfx.SaveAt(subs=[a, 3])
+
+
+def test_pid_step_ts_builds_the_clip_controller():
+    # pid.py:88-97: PIDController(..., step_ts=, jump_ts=) is the clip wrapper
+    c = dfx.PIDController(rtol=1e-3, atol=1e-6, step_ts=[0.5, 1.0], jump_ts=[0.75])
+    assert isinstance(c, dfx.ClipStepSizeController)
+    assert isinstance(c.controller, dfx.PIDController) and c.controller.rtol == 1e-3
+    assert isinstance(dfx.PIDController(rtol=1e-3, atol=1e-6, step_ts=None), dfx.PIDController)
