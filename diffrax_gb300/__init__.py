@@ -10,6 +10,7 @@ from ._core import (
     RESULTS, SaveAt, SubSaveAt, Solution, Tsit5, VanDerPol, VirtualBrownianTree, adjoint_rms_seminorm,
     rms_norm, Event, LinearCondition, Newton, SteadyStateCondition, steady_state_event,
     AbstractBrownianIncrement, BrownianIncrement, SEA, ShARK, SpaceTimeLevyArea, SRA1,
+    AbstractProgressMeter, NoProgressMeter, TextProgressMeter, TqdmProgressMeter,
 )
 from ._integrate import DenseInterpolation, diffeqsolve, lower
 from ._tune import GraphedSolve, autotune_launch, tuned_shapes

@@ -446,6 +446,30 @@ class Event:
 # ---------------------------------------------------------------------------
 
 
+# ---------------------------------------------------------------------------
+# Progress meters (diffrax/_progress_meter.py): accepted for the reference's
+# signature; a solve is one launch with no host loop to report from.
+# ---------------------------------------------------------------------------
+
+
+class AbstractProgressMeter:
+    pass
+
+
+class NoProgressMeter(AbstractProgressMeter):
+    pass
+
+
+class TextProgressMeter(AbstractProgressMeter):
+    def __init__(self, minimum_increase: float = 0.02):
+        self.minimum_increase = minimum_increase
+
+
+class TqdmProgressMeter(AbstractProgressMeter):
+    def __init__(self, refresh_steps: int = 20):
+        self.refresh_steps = refresh_steps
+
+
 class SubSaveAt:
     """diffrax/_saveat.py:14-57: one set of saves (t0, ts, every n-th step,
     t1) with its own map fn(t, y, args) (called on the batched saves)."""
