@@ -48,8 +48,9 @@ def _key(fields: dict, batch: int):
 
 def tc_eligible(fields: dict) -> bool:
     """Whether the tcgen05 forward (kernel "tc") serves this problem: BF16
-    forward solves of 64 -> 128 -> 128 -> 64 MLP ODE fields with Tsit5."""
-    return (fields.get("field") == 3 and fields.get("solver") == 3 and
+    forward solves of 64 -> 128 -> 128 -> 64 MLP ODE fields with Tsit5 or
+    Dopri5."""
+    return (fields.get("field") == 3 and fields.get("solver") in (2, 3) and
             tuple(fields.get("mlp_widths", ())) == (64, 128, 128, 64) and
             fields.get("mlp_precision", 0) == 0 and fields.get("adjoint", 0) == 0 and
             fields.get("diffusion", 0) == 0 and not fields.get("save_steps") and

@@ -538,7 +538,7 @@ int gbdx_problem_create(const gbdx_problem_desc *desc, gbdx_problem **out) {
         delete p;
         return fail(GBDX_ERR_UNSUPPORTED,
                     "the tensor-core (TC) kernel takes 64 -> 128 -> 128 -> 64 ODE fields with "
-                    "Tsit5 (got dim %d, width %d, solver %d%s)", D, H, d.solver,
+                    "Tsit5 or Dopri5 (got dim %d, width %d, solver %d%s)", D, H, d.solver,
                     sde ? ", SDE" : "");
       }
       p->mlp = true;

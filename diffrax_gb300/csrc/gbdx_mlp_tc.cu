@@ -498,24 +498,42 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(SolveParams P) {
                          P.batch * P.n_save * kD, GBDX_SITE_YS);
 #pragma unroll
       for (int c = 0; c < kDH; c += 16) {
-        float v[16], kv[16];
+        // Tsit5: y0 + sum_s w_s(theta) k_s (tsit5.py:103-156); Dopri5: the
+        // quartic through y0, y1, the midpoint y0 + sum_s cmid_s k_s and the
+        // end slopes k_0, k_6 (dopri5.py:36-47, _local_interpolation.py:95-139)
+        float v[16], y1[16], kv[16], fa[16];
 #pragma unroll
-        for (int j = 0; j < 16; j++) v[j] = 0.f;
+        for (int j = 0; j < 16; j++) {
+          v[j] = 0.f;
+          y1[j] = y[c + j];
+        }
 #pragma unroll
         for (int s = 0; s < 7; s++) {
           if (s < 6) tc::tmem_ld16(lane_addr + 64u * s + col0 + c, kv);
           else tc::tmem_ld16(lane_addr + kAcc + col0 + c, kv);
-          const float w = tsit5_w<float>(s, th);
 #pragma unroll
           for (int j = 0; j < 16; j++) {
             const float k =
                 s == 0 ? kv[j] * h : s == 6 ? (kv[j] + sm.b2[col0 + c + j]) * h : kv[j];
-            v[j] = fmaf(w, k, v[j]);
+            if constexpr (SOLVER == GBDX_DOPRI5) {
+              v[j] = fmaf(float(Tab<GBDX_DOPRI5>::cmid(s)), k, v[j]);
+              if (s < 6) y1[j] = fmaf(float(TB::a(6, s)), k, y1[j]);
+              if (s == 0) fa[j] = k;
+              if (s == 6) {
+                const float y0 = y[c + j], ym = y0 + v[j], fb = k;
+                const float a = 2.f * (fb - fa[j]) - 8.f * (y1[j] + y0) + 16.f * ym;
+                const float b = 5.f * fa[j] - 3.f * fb + 18.f * y0 + 14.f * y1[j] - 32.f * ym;
+                const float cc = fb - 4.f * fa[j] - 11.f * y0 - 5.f * y1[j] + 16.f * ym;
+                v[j] = (((a * th + b) * th + cc) * th + fa[j]) * th + y0;  // the value
+              }
+            } else {
+              v[j] = fmaf(tsit5_w<float>(s, th), k, v[j]);
+            }
           }
         }
         if (pend) {
 #pragma unroll
-          for (int j = 0; j < 16; j++) o[c + j] = y[c + j] + v[j];
+          for (int j = 0; j < 16; j++) o[c + j] = SOLVER == GBDX_DOPRI5 ? v[j] : y[c + j] + v[j];
         }
       }
       if (pend) {
@@ -639,6 +657,7 @@ cudaError_t occupancy_tc(int, int *ctas) {
 OdeEntry find_mlp_tc_entry(int solver, int D, int H, bool sde) {
   if (sde || D != kD || H != kH) return OdeEntry{nullptr, nullptr};
   if (solver == GBDX_TSIT5) return OdeEntry{&launch_tc<GBDX_TSIT5>, &occupancy_tc<GBDX_TSIT5>};
+  if (solver == GBDX_DOPRI5) return OdeEntry{&launch_tc<GBDX_DOPRI5>, &occupancy_tc<GBDX_DOPRI5>};
   return OdeEntry{nullptr, nullptr};
 }
 

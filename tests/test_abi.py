@@ -243,7 +243,8 @@ def test_autotune_cache_key_ignores_launch_shape():
                     dtype=torch.float32, max_steps=64, n_ts=0)
     assert _tune.tc_eligible(mlp) and ("tc", 0, 1) in _tune.candidates(mlp, 8192)
     assert ("tc", 0, 1) not in _tune.candidates(dict(mlp, kernel=2), 8192)
-    assert not _tune.tc_eligible(dict(mlp, solver=2))
+    assert _tune.tc_eligible(dict(mlp, solver=2))  # Dopri5
+    assert not _tune.tc_eligible(dict(mlp, solver=1))  # Heun
 
 
 def test_ou_sde_scope():
@@ -266,7 +267,7 @@ def test_ou_sde_scope():
 
 def test_tc_kernel_scope():
     # kernel="tc": BF16 forward solves of 64 -> 128 -> 128 -> 64 MLP fields
-    # with Tsit5; anything else is rejected at problem creation
+    # with Tsit5 or Dopri5; anything else is rejected at problem creation
     W = [torch.zeros(128, 64), torch.zeros(128, 128), torch.zeros(64, 128)]
     b = [torch.zeros(128), torch.zeros(128), torch.zeros(64)]
     term = dfx.ODETerm(dfx.MLPField(W, b))
@@ -276,8 +277,9 @@ def test_tc_kernel_scope():
         return dfx.lower(term, solver, pid, dfx.SaveAt(t1=True), dim=64, dtype=torch.float32,
                          max_steps=64, n_ts=0, kernel="tc", **kw)
     assert _lib.Problem(fields(dfx.Tsit5())).n_save == 1
-    with pytest.raises(_lib.GbdxError, match="Tsit5"):
-        _lib.Problem(fields(dfx.Dopri5()))
+    assert _lib.Problem(fields(dfx.Dopri5())).n_save == 1
+    with pytest.raises(_lib.GbdxError, match="Tsit5 or Dopri5"):
+        _lib.Problem(fields(dfx.Heun()))
     with pytest.raises(_lib.GbdxError, match="adjoint"):
         _lib.Problem(fields(dfx.Tsit5(), adjoint=dfx.RecursiveCheckpointAdjoint(8)))
     with pytest.raises(_lib.GbdxError, match="MLP"):

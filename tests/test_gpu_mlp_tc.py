@@ -13,7 +13,8 @@ from test_gpu_mlp import flat, mlp_params, per_traj_err
 pytestmark = pytest.mark.gpu
 
 
-def solve(kernel, y0, saveat, ctrl, seed=5, t1=1.0, bias_scale=0.0):
+def solve(kernel, y0, saveat, ctrl, seed=5, t1=1.0, bias_scale=0.0, solver=None):
+    solver = dfx.Tsit5() if solver is None else solver
     dev = torch.device("cuda")
     Ws, bs = mlp_params([64, 128, 128, 64], seed, bias_scale)
     Ws = [W.astype(np.float32).astype(np.float64) for W in Ws]
@@ -22,16 +23,17 @@ def solve(kernel, y0, saveat, ctrl, seed=5, t1=1.0, bias_scale=0.0):
                          [torch.tensor(b, dtype=torch.float32, device=dev) for b in bs])
     tt = lambda x: torch.tensor(x, dtype=torch.float64, device=dev) if isinstance(  # noqa
         x, np.ndarray) else x
-    sol = dfx.diffeqsolve(dfx.ODETerm(field), dfx.Tsit5(), 0.0, tt(t1), None,
+    sol = dfx.diffeqsolve(dfx.ODETerm(field), solver, 0.0, tt(t1), None,
                           torch.tensor(y0, dtype=torch.float32, device=dev), saveat=saveat,
                           stepsize_controller=ctrl, throw=False, kernel=kernel)
     torch.cuda.synchronize()
     return sol, field, flat(Ws, bs)
 
 
-def oracle(field, params, y0, saveat, ctrl, t1=1.0):
+def oracle(field, params, y0, saveat, ctrl, t1=1.0, solver=None):
+    solver = dfx.Tsit5() if solver is None else solver
     ts = None if saveat.ts is None else np.asarray(saveat.ts, dtype=np.float64)
-    fields = dfx.lower(dfx.ODETerm(field), dfx.Tsit5(), ctrl, saveat, dim=64,
+    fields = dfx.lower(dfx.ODETerm(field), solver, ctrl, saveat, dim=64,
                        dtype=torch.float32, max_steps=4096, n_ts=0 if ts is None else ts.size)
     d = O.make_desc(**O.oracle_fields(fields))
     return O.solve(d, 0.0, t1, None, y0, params=params, ts=ts, nthreads=8)
@@ -89,3 +91,24 @@ def test_tc_uneven_t1_refill_and_constant_steps():
                         stepsize_controller=const, kernel="fused")
     assert (a.stats["num_steps"] == 20).all()
     assert float((a.ys - b.ys).abs().max() / b.ys.abs().max()) < 2e-5
+
+
+def test_tc_dopri5_matches_oracle_and_rowtile():
+    # Dopri5 on the tensor-core tiles: its quartic interpolant for the ts saves
+    rng = np.random.default_rng(62)
+    y0 = rng.standard_normal((300, 64))
+    pid = dfx.PIDController(rtol=1e-5, atol=1e-7)
+    saveat = dfx.SaveAt(t0=True, ts=np.linspace(0.0, 1.0, 9), t1=True)
+    sol, field, params = solve("tc", y0, saveat, pid, solver=dfx.Dopri5(), bias_scale=0.1)
+    ref, _, _ = solve("fused", y0, saveat, pid, solver=dfx.Dopri5(), bias_scale=0.1)
+    r = oracle(field, params, y0, saveat, pid, solver=dfx.Dopri5())
+    assert (sol.result == 0).all()
+    err = per_traj_err(sol, r)
+    err_ref = per_traj_err(ref, r)
+    print(f"tc Dopri5: rel err vs FP64 oracle median {np.median(err):.2e} max {err.max():.2e} "
+          f"(row tile {np.median(err_ref):.2e} / {err_ref.max():.2e})")
+    # the solve's tolerance level (FP32 and FP64 controllers take different
+    # steps), and the row-tile kernel's
+    assert err.max() < 5e-5 and err.max() < 1.5 * err_ref.max()
+    d = (sol.ys - ref.ys).abs().max() / ref.ys.abs().max()
+    assert float(d) < 1e-4
