@@ -334,3 +334,32 @@ def test_mlp_reverse_time_steps_dense_and_event():
     rq = O.dense_evaluate(d, 1.0, 0.0, y0, r, q)
     ok = np.isfinite(rq).all(axis=(1, 2)) & agree
     assert np.abs(ev_q[ok] - rq[ok]).max() < 1e-4 * np.abs(rq[ok]).max()
+
+
+def test_mlp_two_conditions_with_steps_and_dense():
+    # a boolean condition on time and a real one on y1, no root finder, with
+    # every 3rd step saved and the dense output (the first condition that
+    # fires, in order, ends the solve at the step's end)
+    rng = np.random.default_rng(31)
+    B = 128
+    y0 = rng.standard_normal((B, 64))
+    Ws, bs = mlp_params([64, 128, 128, 64], 14, bias_scale=0.1)
+    Ws = [W.astype(np.float32).astype(np.float64) for W in Ws]
+    bs = [b.astype(np.float32).astype(np.float64) for b in bs]
+    ev = dfx.Event([dfx.LinearCondition([], t_coeff=1.0, offset=-0.6, boolean=True),
+                    dfx.LinearCondition([0.0, 1.0], offset=-0.3)])
+    saveat = dfx.SaveAt(steps=3, t1=True, dense=True)
+    sol, r = mlp_event_pair(Ws, bs, dfx.Tsit5(), dfx.ConstantStepSize(), saveat, ev, 1.0, 0.05,
+                            y0, "fp32", max_steps=64)
+    masks = [m.cpu().numpy() for m in sol.event_mask]
+    evi = np.where(masks[0], 0, np.where(masks[1], 1, -1))
+    agree = (evi == r["event_index"]) & (sol.result.cpu().numpy() == r["result"])
+    print(f"two conditions: fired {np.bincount(r['event_index'] + 1)}, agree {agree.mean():.3f}")
+    assert agree.mean() >= 0.97 and (r["event_index"] == 0).any() and (r["event_index"] == 1).any()
+    ts, rt = sol.ts.cpu().numpy()[agree], r["ts"][agree]
+    assert np.array_equal(np.isfinite(ts), np.isfinite(rt))
+    fin = np.isfinite(rt)
+    assert np.abs(ts[fin] - rt[fin]).max() < 1e-9
+    ys, ry = sol.ys.cpu().double().numpy()[agree], r["ys"][agree]
+    fy = np.isfinite(ry)
+    assert np.abs(ys[fy] - ry[fy]).max() < 1e-5 * np.abs(ry[fy]).max()
