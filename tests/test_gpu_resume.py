@@ -221,3 +221,41 @@ def test_mlp_resume_matches_oracle(precision):
     f_end = rec2[:, 7:]
     fr = r2["state"][:, 7:]
     assert np.abs(f_end - fr).max() < 1e-4 * np.abs(fr).max()
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_split_equals_whole_on_the_gpu(dtype):
+    # the GPU form of the oracle pin: a PID solve stopped after k attempted
+    # steps and resumed from its records (dt0 = the whole solve's next step)
+    # takes the whole solve's remaining steps bit for bit
+    dev = torch.device("cuda")
+    y0 = torch.tensor([[1.2, -0.3], [-0.8, 0.6]], dtype=dtype, device=dev)
+    mu = torch.tensor([1.5], dtype=dtype, device=dev)
+    ctrl = dfx.PIDController(rtol=1e-6, atol=1e-8)
+    term = dfx.ODETerm(dfx.VanDerPol())
+
+    def run(t0, dt0, y, k, **kw):
+        return dfx.diffeqsolve(term, dfx.Tsit5(), t0, 3.0, dt0, y, mu,
+                               saveat=dfx.SaveAt(steps=1, **STATES), stepsize_controller=ctrl,
+                               max_steps=k, throw=False, **kw)
+    whole = run(0.0, 0.05, y0, 4096)
+    acc = [run(0.0, 0.05, y0, k).stats["num_accepted_steps"].cpu().numpy() for k in range(1, 41)]
+    k = next(k for k in range(10, 40)
+             if (acc[k - 1] == acc[k - 2] + 1).all() and (acc[k] == acc[k - 1] + 1).all())
+    leg1 = run(0.0, 0.05, y0, k)
+    ka = leg1.stats["num_accepted_steps"].cpu().numpy()
+    assert (ka == ka[0]).all()
+    ka = int(ka[0])
+    wts = whole.ts
+    tk = wts[:, ka - 1].contiguous()
+    assert torch.equal(leg1.ts[:, ka - 1], tk)
+    leg2 = run(tk, (wts[:, ka] - tk).contiguous(), leg1.ys[:, ka - 1].contiguous(), 4096,
+               solver_state=leg1.solver_state, controller_state=leg1.controller_state,
+               made_jump=leg1.made_jump)
+    n = whole.stats["num_accepted_steps"].cpu().numpy()
+    for b in range(2):
+        m = int(n[b]) - ka
+        assert int(leg2.stats["num_accepted_steps"][b]) == m
+        assert torch.equal(leg2.ts[b, :m], wts[b, ka:n[b]])
+        assert torch.equal(leg2.ys[b, :m], whole.ys[b, ka:n[b]])
+    assert np.array_equal(_record(leg2), _record(whole))

@@ -1097,3 +1097,72 @@ def test_event_constant_step_infinite_t1():
     r = O.solve(d, 0.0, np.inf, 0.5, [[0.0]], callback=_const_field([1.0]))
     ts = r["ts"][0]
     assert list(ts[np.isfinite(ts)]) == [0.5, 1.0, 1.5, 2.0, 2.5, 3.0]
+
+
+# ---------------------------------------------------------------------------
+# Resuming a solve (diffeqsolve's solver_state / controller_state / made_jump,
+# _integrate.py:1252-1271, 1309, 1489-1500): split = whole.
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("solver", [O.DOPRI5, O.TSIT5, O.HEUN])
+def test_resume_pid_split_reproduces_the_whole_solve(solver):
+    # A PID solve stopped after k attempted steps (max_steps) and resumed from
+    # its records, with dt0 = the whole solve's next step size, takes the
+    # whole solve's remaining steps bit for bit: the controller's history and
+    # the FSAL value carry over (FSAL solvers skip the first evaluation).  The
+    # split is taken where attempts k and k + 1 are both accepted, so that the
+    # next step size is the whole solve's next step.
+    tol = 1e-4 if solver == O.HEUN else 1e-6  # a second-order method at a looser tolerance
+
+    def desc(max_steps):
+        return O.make_desc(solver=solver, controller=O.PID, field=O.VAN_DER_POL, dim=2,
+                           rtol=tol, atol=tol * 1e-2, n_args=1, save_steps=1,
+                           max_steps=max_steps)
+    y0 = np.array([[1.2, -0.3]])
+    mu = [1.5]
+    whole = O.solve(desc(4096), 0.0, 3.0, 0.05, y0, args=mu, want_state=True)
+    n = int(whole["stats"][0, 1])
+    assert whole["result"][0] == 0
+    acc = [int(O.solve(desc(k), 0.0, 3.0, 0.05, y0, args=mu)["stats"][0, 1])
+           for k in range(1, 41)]
+    k = next(k for k in range(10, 40) if acc[k - 1] == acc[k - 2] + 1 and acc[k] == acc[k - 1] + 1)
+    leg1 = O.solve(desc(k), 0.0, 3.0, 0.05, y0, args=mu, want_state=True)
+    st = leg1["state"]
+    assert st[0, 4] == 1 and st[0, 5] == (0 if solver != O.HEUN else 1)  # FSAL value or none
+    ka = int(leg1["stats"][0, 1])
+    tk = whole["ts"][0, ka - 1]
+    assert leg1["ts"][0, ka - 1] == tk
+    leg2 = O.solve(desc(4096), tk, 3.0, whole["ts"][0, ka] - tk, leg1["ys"][:, ka - 1], args=mu,
+                   state_in=st, want_state=True)
+    m = n - ka
+    assert leg2["stats"][0, 1] == m
+    assert np.array_equal(leg2["ts"][0, :m], whole["ts"][0, ka:n])
+    assert np.array_equal(leg2["ys"][0, :m], whole["ys"][0, ka:n])
+    # the final records of the whole and of the resumed leg agree
+    assert np.array_equal(leg2["state"], whole["state"])
+
+
+def test_resume_constant_grid_and_fresh_state_defaults():
+    # ConstantStepSize: steps_completed starts at 1 and the grid is
+    # t0 + (t1 - t0) n / N (constant.py:30-104); a leg resumed with the grid
+    # state ends on the whole solve's t1 value.  A record without a
+    # controller state ([4] = 0) or with first_step set changes nothing.
+    d = O.make_desc(solver=O.TSIT5, controller=O.CONSTANT, field=O.LOTKA_VOLTERRA, dim=2,
+                    n_args=4, save_steps=1, max_steps=4096)
+    args = [[0.1, 0.02, 0.4, 0.02]]
+    y0 = np.array([[10.0, 5.0]])
+    whole = O.solve(d, 0.0, 20.0, 0.1, y0, args=args, want_state=True)
+    assert whole["state"][0, 0] == 201 and whole["state"][0, 1] == 200
+    d1 = O.make_desc(solver=O.TSIT5, controller=O.CONSTANT, field=O.LOTKA_VOLTERRA, dim=2,
+                     n_args=4, save_steps=1, max_steps=70)
+    leg1 = O.solve(d1, 0.0, 20.0, 0.1, y0, args=args, want_state=True)
+    assert leg1["state"][0, 0] == 71
+    leg2 = O.solve(d, leg1["ts"][0, 69], 20.0, 0.1, leg1["ys"][:, 69], args=args,
+                   state_in=leg1["state"], want_state=True)
+    assert leg2["stats"][0, 0] == 130 and leg2["state"][0, 0] == 201
+    assert tree_allclose(leg2["ys"][0, 129], whole["ys"][0, 199], rtol=1e-12, atol=1e-12)
+    blank = np.zeros_like(leg1["state"])
+    blank[:, 5] = 1.0  # no controller state, first_step
+    fresh = O.solve(d, 0.0, 20.0, 0.1, y0, args=args, state_in=blank)
+    assert np.array_equal(fresh["ys"], whole["ys"])
