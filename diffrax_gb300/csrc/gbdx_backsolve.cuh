@@ -109,16 +109,24 @@ struct BsAct {
   __nv_bfloat16 R1[SH::M][SH::PH], R1l[SH::M][SH::PH], R1l2[SH::M][SH::PH];
   __nv_bfloat16 R2[SH::M][SH::PH], R2l[SH::M][SH::PH], R2l2[SH::M][SH::PH];
 };
-// Operands of the tensor-core parameter pass of one row and layer:
-// o-side vectors U0 = -h u0, A2 = sum_j b_j du_j, A3 = sum_j e_j du_j and the
-// stage differences du_j = -h (u_j - u_0) (BF16, [o][k = j - 1]); i-side
-// vectors v0, B1 = v0 + sum_j b_j dv_j, B3 = sum_j e_j dv_j and b_j dv_j,
-// e_j dv_j (BF16, [k][i]).
+// Operands of the tensor-core parameter pass of one row and one layer
+// W [NO][NI]: o-side vectors U0 = -h u0, A2 = sum_j b_j du_j,
+// A3 = sum_j e_j du_j and the stage differences du_j = -h (u_j - u_0) (BF16,
+// [o][k = j - 1]); i-side vectors v0, B1 = v0 + sum_j b_j dv_j,
+// B3 = sum_j e_j dv_j and b_j dv_j, e_j dv_j (BF16, [k][i]).
+template <int NO, int NI>
+struct __align__(16) BsLayerOps {
+  float U0[NO], A2[NO], A3[NO], v0[NI], B1[NI], B3[NI];
+  __nv_bfloat16 Du[NO][24];
+  __nv_bfloat16 Bb[16][NI + 8], Be[16][NI + 8];
+};
+// The three layers of one row together, so that the row's weight tiles
+// stream as one sequence.
 template <class SH>
 struct BsPassOps {
-  float U0[SH::H], A2[SH::H], A3[SH::H], v0[SH::H], B1[SH::H], B3[SH::H];
-  __nv_bfloat16 Du[SH::H][24];
-  __nv_bfloat16 Bb[16][SH::PH], Be[16][SH::PH];
+  BsLayerOps<SH::H, SH::D> l0;
+  BsLayerOps<SH::H, SH::H> l1;
+  BsLayerOps<SH::D, SH::H> l2;
 };
 
 template <class SH>
@@ -130,6 +138,7 @@ struct BsSmem<SH, false> : BsWeights<SH, SH::GFRAG> {
     float cf[SH::H][16];  // FP32 parameter-pass coefficients
   };
   float red[SH::WARPS];
+  float rsum[SH::WARPS][SH::M];  // per-warp parameter-pass norm partials
   BsRows<SH::M> rows;
 };
 
@@ -565,7 +574,7 @@ __device__ __forceinline__ float theta_pass(float (*cf)[16], const float *rec_r,
   return s;
 }
 
-// Tensor-core parameter pass of one row and one layer under the tracked norm.
+// Tensor-core parameter pass under the tracked norm.
 // With du_j = -h (u_j - u_0), dv_j = v_j - v_0 and sum_j b_j = 1, sum_j e_j = 0,
 //   da  = -h sum_j b_j u_j v_j = U0 B1 + A2 v0 + sum_j du_j (b_j dv_j),
 //   err = -h sum_j e_j u_j v_j = U0 B3 + A3 v0 + sum_j du_j (e_j dv_j):
@@ -573,15 +582,95 @@ __device__ __forceinline__ float theta_pass(float (*cf)[16], const float *rec_r,
 // stages whose factors are O(h) stage differences, so one BF16 tensor-core
 // product per m16n8 tile carries it to well below FP32 rounding of da.  The
 // error estimate loses no digits to the cancellation of its weights.
-// The a_theta0 values of U consecutive tiles of this warp.  In the tensor-core
-// mode a row's weight gradients are stored in fragment order: tile t of a
-// layer holds its 128 values at WOFF + 128 t + 4 lane + q, q indexing the
-// accumulator elements (g, 2c), (g, 2c + 1), (g + 8, 2c), (g + 8, 2c + 1).
-template <int U, int TPW, int WOFF>
-__device__ __forceinline__ void tc_load(float (&x)[U][4], const float *a0, int tb, int warp,
-                                        int lane) {
+//
+// In the tensor-core mode a row's weight gradients are stored in fragment
+// order: tile t of a layer holds its 128 values at WOFF + 128 t + 4 lane + q,
+// q indexing the accumulator elements (g, 2c), (g, 2c + 1), (g + 8, 2c),
+// (g + 8, 2c + 1).  Warp w takes a contiguous run of each layer's m16n8
+// tiles.
+
+// Layer L of the field: W [NO][NI], its stage vectors u (record offset UOFF)
+// and v (VOFF), its weights and biases in the flat parameter vector.
+template <class SH, int L>
+struct BsLayer;
+template <class SH>
+struct BsLayer<SH, 0> {
+  static constexpr int NO = SH::H, NI = SH::D, UOFF = SH::RZ0, VOFF = SH::RX, WOFF = SH::OW0,
+                       BOFF = SH::OB0;
+  __device__ static BsLayerOps<NO, NI> &ops(BsPassOps<SH> &p) { return p.l0; }
+};
+template <class SH>
+struct BsLayer<SH, 1> {
+  static constexpr int NO = SH::H, NI = SH::H, UOFF = SH::RZ1, VOFF = SH::RH1, WOFF = SH::OW1,
+                       BOFF = SH::OB1;
+  __device__ static BsLayerOps<NO, NI> &ops(BsPassOps<SH> &p) { return p.l1; }
+};
+template <class SH>
+struct BsLayer<SH, 2> {
+  static constexpr int NO = SH::D, NI = SH::H, UOFF = SH::RG, VOFF = SH::RH2, WOFF = SH::OW2,
+                       BOFF = SH::OB2;
+  __device__ static BsLayerOps<NO, NI> &ops(BsPassOps<SH> &p) { return p.l2; }
+};
+
+// A row's weight tiles as one sequence of batches of U tiles per warp: the
+// one batch of layer 0, the NB1 batches of layer 1, the one batch of layer 2.
+// A batch's a_theta0 loads are issued one batch ahead (two register buffers),
+// across layer and row boundaries.
+template <class SH>
+struct BsTiles {
+  template <int L>
+  static constexpr int tpw() {
+    return (BsLayer<SH, L>::NO / 16) * (BsLayer<SH, L>::NI / 8) / SH::WARPS;
+  }
+  static constexpr int T0 = tpw<0>(), T1 = tpw<1>(), T2 = tpw<2>();
+  static constexpr int U = T0 < 16 ? T0 : 16, NB1 = T1 / U, NB = NB1 + 2;
+  static constexpr int PF = 2;  // L2 prefetch distance, in batches
+  static_assert(T0 * SH::WARPS == (BsLayer<SH, 0>::NO / 16) * (BsLayer<SH, 0>::NI / 8) &&
+                    T1 * SH::WARPS == (BsLayer<SH, 1>::NO / 16) * (BsLayer<SH, 1>::NI / 8) &&
+                    T2 * SH::WARPS == (BsLayer<SH, 2>::NO / 16) * (BsLayer<SH, 2>::NI / 8),
+                "parameter tiles split over the warps");
+  static_assert(T0 == U && T2 == U && T1 % (2 * U) == 0, "parameter tile batches");
+};
+
+// Batch i (0 <= i < NB) of a row in this warp's run: layer 0, NB1 batches of
+// layer 1, layer 2.
+template <class SH>
+__device__ __forceinline__ const float *batch_ptr(const float *a0, int i, int warp) {
+  using TL = BsTiles<SH>;
+  if (i == 0) return a0 + BsLayer<SH, 0>::WOFF + warp * TL::T0 * 128;
+  if (i <= TL::NB1) return a0 + BsLayer<SH, 1>::WOFF + (warp * TL::T1 + (i - 1) * TL::U) * 128;
+  return a0 + BsLayer<SH, 2>::WOFF + warp * TL::T2 * 128;
+}
+
+// Bulk prefetch into L2 of batch i of the row (i >= NB: batch i - NB of the
+// next row, when there is one), PF batches ahead of the register loads, so
+// that those find their lines in L2.
+template <class SH>
+__device__ __forceinline__ void batch_prefetch(const float *a0, const float *a0n, bool next,
+                                               int i, int warp, int lane) {
+  using TL = BsTiles<SH>;
+  const float *base = a0;
+  if (i >= TL::NB) {
+    i -= TL::NB;
+    base = next ? a0n : nullptr;
+  }
+  if (lane == 0 && base && i < TL::NB) {
+    const float *p = batch_ptr<SH>(base, i, warp);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p),
+                 "r"(uint32_t(TL::U * 128 * sizeof(float)))
+                 : "memory");
+  }
+}
+
+// The a_theta0 values of U tiles of layer L from tile tb of this warp's run
+// (zeros for a row whose a_theta is still zero).
+template <class SH, int L>
+__device__ __forceinline__ void batch_load(float (&x)[BsTiles<SH>::U][4], const float *a0,
+                                           int tb, int warp, int lane) {
+  using TL = BsTiles<SH>;
+  constexpr int TPW = TL::template tpw<L>(), WOFF = BsLayer<SH, L>::WOFF;
 #pragma unroll
-  for (int u = 0; u < U; u++) {
+  for (int u = 0; u < TL::U; u++) {
     const int t = warp * TPW + tb + u;
     if (a0) {
       const float4 v = __ldcs(reinterpret_cast<const float4 *>(a0 + WOFF + t * 128 + lane * 4));
@@ -595,20 +684,25 @@ __device__ __forceinline__ void tc_load(float (&x)[U][4], const float *a0, int t
   }
 }
 
-// U tiles: a1 = a0 + da (fragment layout); returns the tiles' share of the
-// scaled squared errors when NORM.
-template <class SH, int S, int U, int NTL, int TPW, int NI, int WOFF, bool NORM>
-__device__ __forceinline__ float tc_tiles(BsPassOps<SH> &ps, const float (&x0)[U][4], float *a1,
-                                          int tb, int warp, int lane, float rtol, float atol) {
+// U tiles of layer L from tile tb: a1 = a0 + da (fragment layout); returns
+// their share of the scaled squared errors when NORM.
+template <class SH, int S, int L, bool NORM>
+__device__ __forceinline__ float batch_tiles(BsPassOps<SH> &pp,
+                                             const float (&x0)[BsTiles<SH>::U][4], float *a1,
+                                             int tb, int warp, int lane, float rtol, float atol) {
+  using TL = BsTiles<SH>;
+  using LY = BsLayer<SH, L>;
+  constexpr int TPW = TL::template tpw<L>(), NI = LY::NI, NTL = NI / 8, WOFF = LY::WOFF;
+  auto &ps = LY::ops(pp);
   const int g = lane >> 2, c = lane & 3;
   float accn = 0.f;
 #pragma unroll
-  for (int u = 0; u < U; u++) {
+  for (int u = 0; u < TL::U; u++) {
     const int t = warp * TPW + tb + u, ot = t / NTL, nt = t % NTL;
     const int og = ot * 16 + g, ic = nt * 8 + 2 * c;
     uint32_t a[4], bb[2], be[2];
     ldsm_a(a, &ps.Du[ot * 16][0], 24, lane);
-    ldsm_bt1(bb, &ps.Bb[0][0], SH::PH, 0, nt * 8, lane);
+    ldsm_bt1(bb, &ps.Bb[0][0], NI + 8, 0, nt * 8, lane);
     const float u0a = ps.U0[og], u0b = ps.U0[og + 8];
     const float a2a = ps.A2[og], a2b = ps.A2[og + 8];
     const float2 v0 = *reinterpret_cast<const float2 *>(&ps.v0[ic]);
@@ -620,7 +714,7 @@ __device__ __forceinline__ float tc_tiles(BsPassOps<SH> &ps, const float (&x0)[U
 #pragma unroll
     for (int q = 0; q < 4; q++) x1[q] = x0[u][q] + cb[q];
     if constexpr (NORM) {
-      ldsm_bt1(be, &ps.Be[0][0], SH::PH, 0, nt * 8, lane);
+      ldsm_bt1(be, &ps.Be[0][0], NI + 8, 0, nt * 8, lane);
       const float a3a = ps.A3[og], a3b = ps.A3[og + 8];
       const float2 b3 = *reinterpret_cast<const float2 *>(&ps.B3[ic]);
       float ce[4] = {fmaf(u0a, b3.x, a3a * v0.x), fmaf(u0a, b3.y, a3a * v0.y),
@@ -635,38 +729,82 @@ __device__ __forceinline__ float tc_tiles(BsPassOps<SH> &ps, const float (&x0)[U
   return accn;
 }
 
-template <class SH, int SOLVER, int NO, int NI, int UOFF, int VOFF, int WOFF, int BOFF, bool NORM>
-__device__ __forceinline__ float theta_layer_tc(BsPassOps<SH> &ps, const float *rec_r, float h,
-                                                const float *a0, float *a1, float rtol,
-                                                float atol, int tid, int warp, int lane) {
-  using TB = Tab<SOLVER>;
-  constexpr int S = TB::S, STR = SH::M * SH::REC;
-  static_assert(S - 1 <= 16, "stage differences fit one k16 slice");
-  constexpr int NTL = NI / 8, TILES = (NO / 16) * NTL, TPW = TILES / SH::WARPS;
-  static_assert(TILES % SH::WARPS == 0, "parameter tiles split");
-  constexpr int U = TPW < 16 ? TPW : 16;  // tiles per load batch
-  static_assert(TPW % U == 0, "parameter tile batches");
-  float accn = 0.f;
-  // 1. operands.  The record loads go first, then the first tile batch of
-  // a_theta0 (independent of the operands), then the operand arithmetic.
-  static_assert(NI <= SH::THREADS && NO <= SH::THREADS, "one operand row per thread");
-  const bool own_i = tid < NI, own_o = tid < NO;
-  float vv[S], uu[S];
+// A row's tiles, its layer-0 batch already loading into xa and its first
+// layer-1 batch into xb; ends with batch 0 of the next row (a0n, when next)
+// loading into xa.
+template <class SH, int S, bool NORM>
+__device__ __forceinline__ float row_tiles(BsPassOps<SH> &pp, float (&xa)[BsTiles<SH>::U][4],
+                                           float (&xb)[BsTiles<SH>::U][4], const float *a0,
+                                           float *a1, bool next, const float *a0n, int warp,
+                                           int lane, float rtol, float atol) {
+  using TL = BsTiles<SH>;
+  constexpr int U = TL::U;
+  float s = batch_tiles<SH, S, 0, NORM>(pp, xa, a1, 0, warp, lane, rtol, atol);
+#pragma unroll 1
+  for (int tb = 0, i = 2; tb < TL::T1; tb += 2 * U, i += 2) {
+    // batch i: layer-1 tile tb + U; batch i + 1: the next
+    batch_load<SH, 1>(xa, a0, tb + U, warp, lane);
+    batch_prefetch<SH>(a0, a0n, next, i + TL::PF, warp, lane);
+    s += batch_tiles<SH, S, 1, NORM>(pp, xb, a1, tb, warp, lane, rtol, atol);
+    if (tb + 2 * U < TL::T1)
+      batch_load<SH, 1>(xb, a0, tb + 2 * U, warp, lane);
+    else
+      batch_load<SH, 2>(xb, a0, 0, warp, lane);
+    batch_prefetch<SH>(a0, a0n, next, i + 1 + TL::PF, warp, lane);
+    s += batch_tiles<SH, S, 1, NORM>(pp, xa, a1, tb + U, warp, lane, rtol, atol);
+  }
+  if (next) {
+    batch_load<SH, 0>(xa, a0n, 0, warp, lane);
+    batch_prefetch<SH>(a0, a0n, next, TL::NB + TL::PF, warp, lane);
+  }
+  s += batch_tiles<SH, S, 2, NORM>(pp, xb, a1, 0, warp, lane, rtol, atol);
+  return s;
+}
+
+// One layer's stage records of a row, loaded into registers (this thread's
+// i-side value v_j[tid], o-side value -h u_j[tid]) with the bias's a_theta0.
+template <int S>
+struct LayerRecs {
+  float vv[S], uu[S], xb;
+};
+template <class SH, int L>
+__device__ __forceinline__ float bias_load(const float *a0, int tid) {
+  return (tid < BsLayer<SH, L>::NO && a0) ? a0[BsLayer<SH, L>::BOFF + tid] : 0.f;
+}
+template <class SH, int S, int L>
+__device__ __forceinline__ void layer_recs(LayerRecs<S> &lr, const float *rec_r, float h,
+                                           float xb, int tid) {
+  using LY = BsLayer<SH, L>;
+  constexpr int STR = SH::M * SH::REC;
+  static_assert(LY::NI <= SH::THREADS && LY::NO <= SH::THREADS, "one operand row per thread");
+  const bool own_i = tid < LY::NI, own_o = tid < LY::NO;
 #pragma unroll
   for (int j = 0; j < S; j++) {
-    vv[j] = own_i ? rec_r[j * STR + VOFF + tid] : 0.f;
-    uu[j] = own_o ? -h * rec_r[j * STR + UOFF + tid] : 0.f;
+    lr.vv[j] = own_i ? rec_r[j * STR + LY::VOFF + tid] : 0.f;
+    lr.uu[j] = own_o ? -h * rec_r[j * STR + LY::UOFF + tid] : 0.f;
   }
-  float xa[U][4], xb[U][4];
-  tc_load<U, TPW, WOFF>(xa, a0, 0, warp, lane);
-  if (own_i) {
+  lr.xb = xb;
+}
+
+// The layer's operands from its records, and its bias: da = U0 + A2,
+// err = A3 (the bias's v is 1).  Returns the bias's scaled squared error.
+template <class SH, int SOLVER, int L, bool NORM>
+__device__ __forceinline__ float layer_ops(BsPassOps<SH> &pp, const LayerRecs<Tab<SOLVER>::S> &lr,
+                                           float *a1, float rtol, float atol, int tid) {
+  using TB = Tab<SOLVER>;
+  using LY = BsLayer<SH, L>;
+  constexpr int S = TB::S;
+  static_assert(S - 1 <= 16, "stage differences fit one k16 slice");
+  auto &ps = LY::ops(pp);
+  float accn = 0.f;
+  if (tid < LY::NI) {
     const int i = tid;
-    float b1 = vv[0], b3 = 0.f;
+    float b1 = lr.vv[0], b3 = 0.f;
 #pragma unroll
     for (int k = 0; k < 16; k++) {
       float bb = 0.f, be = 0.f;
       if (k + 1 < S) {
-        const float dv = vv[k + 1] - vv[0];
+        const float dv = lr.vv[k + 1] - lr.vv[0];
         bb = float(TB::b(k + 1)) * dv;
         be = float(TB::e(k + 1)) * dv;
         b1 += bb;
@@ -675,64 +813,93 @@ __device__ __forceinline__ float theta_layer_tc(BsPassOps<SH> &ps, const float *
       ps.Bb[k][i] = __float2bfloat16_rn(bb);
       ps.Be[k][i] = __float2bfloat16_rn(be);
     }
-    ps.v0[i] = vv[0];
+    ps.v0[i] = lr.vv[0];
     ps.B1[i] = b1;
     ps.B3[i] = b3;
   }
-  if (own_o) {
+  if (tid < LY::NO) {
     const int o = tid;
     float a2 = 0.f, a3 = 0.f;
 #pragma unroll
     for (int k = 0; k < 16; k++) {
       float du = 0.f;
       if (k + 1 < S) {
-        du = uu[k + 1] - uu[0];
+        du = lr.uu[k + 1] - lr.uu[0];
         a2 = fmaf(float(TB::b(k + 1)), du, a2);
         a3 = fmaf(float(TB::e(k + 1)), du, a3);
       }
       ps.Du[o][k] = __float2bfloat16_rn(du);
     }
-    ps.U0[o] = uu[0];
+    ps.U0[o] = lr.uu[0];
     ps.A2[o] = a2;
     ps.A3[o] = a3;
+    const float x1 = lr.xb + (lr.uu[0] + a2);
+    a1[LY::BOFF + o] = x1;
+    if (NORM) accn = scaled_sq(lr.xb, x1, a3, rtol, atol);
   }
-  __syncthreads();  // the operands are complete
-  // 2. the weight tiles: warp w takes a contiguous run of m16n8 tiles, in
-  // batches of U whose loads are issued one batch ahead (double buffered)
-#pragma unroll 1
-  for (int tb = 0; tb < TPW; tb += 2 * U) {
-    if (tb + U < TPW) tc_load<U, TPW, WOFF>(xb, a0, tb + U, warp, lane);
-    accn += tc_tiles<SH, S, U, NTL, TPW, NI, WOFF, NORM>(ps, xa, a1, tb, warp, lane, rtol, atol);
-    if (tb + U >= TPW) break;
-    if (tb + 2 * U < TPW) tc_load<U, TPW, WOFF>(xa, a0, tb + 2 * U, warp, lane);
-    accn += tc_tiles<SH, S, U, NTL, TPW, NI, WOFF, NORM>(ps, xb, a1, tb + U, warp, lane, rtol,
-                                                         atol);
-  }
-  // 3. biases: da = U0 + A2, err = A3
-  for (int o = tid; o < NO; o += SH::THREADS) {
-    const int p = BOFF + o;
-    const float x0 = a0 ? a0[p] : 0.f;
-    const float x1 = x0 + (ps.U0[o] + ps.A2[o]);
-    a1[p] = x1;
-    if (NORM) accn += scaled_sq(x0, x1, ps.A3[o], rtol, atol);
-  }
-  __syncthreads();  // the operands are rewritten by the next layer
   return accn;
 }
 
-template <class SH, int SOLVER, bool NORM>
-__device__ __forceinline__ float theta_pass_tc(BsPassOps<SH> &ps, const float *rec_r, float h,
-                                               const float *a0, float *a1, float rtol,
-                                               float atol, int tid, int warp, int lane) {
-  constexpr int D = SH::D, H = SH::H;
-  float s = 0.f;
-  s += theta_layer_tc<SH, SOLVER, H, D, SH::RZ0, SH::RX, SH::OW0, SH::OB0, NORM>(
-      ps, rec_r, h, a0, a1, rtol, atol, tid, warp, lane);
-  s += theta_layer_tc<SH, SOLVER, H, H, SH::RZ1, SH::RH1, SH::OW1, SH::OB1, NORM>(
-      ps, rec_r, h, a0, a1, rtol, atol, tid, warp, lane);
-  s += theta_layer_tc<SH, SOLVER, D, H, SH::RG, SH::RH2, SH::OW2, SH::OB2, NORM>(
-      ps, rec_r, h, a0, a1, rtol, atol, tid, warp, lane);
-  return s;
+// The parameter pass over the CTA's selected rows (sel(r): CTA-uniform), a
+// row's a_theta0 / a_theta1 from ptrs(r, a0, a1).  Per row: its stage
+// records and bias values are loaded, the three layers' operands written,
+// one barrier, then the row's tiles as one stream whose loads run one batch
+// ahead, into the next row's first batch.  NORM: warp w's share of row r's
+// scaled squared errors goes to rsum[w][r] (the caller sums over w).
+template <class SH, int SOLVER, bool NORM, class Sel, class Ptrs>
+__device__ __forceinline__ void theta_rows_tc(BsPassOps<SH> &pp, float (*rsum)[SH::M],
+                                              const float *rec, const float *hrow, Sel sel,
+                                              Ptrs ptrs, float rtol, float atol, int tid,
+                                              int warp, int lane) {
+  using TL = BsTiles<SH>;
+  constexpr int S = Tab<SOLVER>::S, M = SH::M;
+  auto next_row = [&](int r) {
+    for (r = r + 1; r < M; r++)
+      if (sel(r)) break;
+    return r;
+  };
+  int r = next_row(-1);
+  if (r >= M) return;
+  const float *a0;
+  float *a1;
+  ptrs(r, a0, a1);
+  float xa[TL::U][4], xb[TL::U][4];
+  batch_load<SH, 0>(xa, a0, 0, warp, lane);
+#pragma unroll
+  for (int i = 1; i <= TL::PF; i++) batch_prefetch<SH>(a0, nullptr, false, i, warp, lane);
+  while (r < M) {
+    const int rn = next_row(r);
+    const float *a0n = nullptr;
+    float *a1n = nullptr;
+    if (rn < M) ptrs(rn, a0n, a1n);
+    const float *rec_r = rec + size_t(r) * SH::REC;
+    const float h = hrow[r];
+    float accn;
+    {
+      const float xb0 = bias_load<SH, 0>(a0, tid), xb1 = bias_load<SH, 1>(a0, tid),
+                  xb2 = bias_load<SH, 2>(a0, tid);
+      batch_load<SH, 1>(xb, a0, 0, warp, lane);
+      batch_prefetch<SH>(a0, a0n, rn < M, 1 + TL::PF, warp, lane);
+      LayerRecs<S> lr;
+      layer_recs<SH, S, 0>(lr, rec_r, h, xb0, tid);
+      accn = layer_ops<SH, SOLVER, 0, NORM>(pp, lr, a1, rtol, atol, tid);
+      layer_recs<SH, S, 1>(lr, rec_r, h, xb1, tid);
+      accn += layer_ops<SH, SOLVER, 1, NORM>(pp, lr, a1, rtol, atol, tid);
+      layer_recs<SH, S, 2>(lr, rec_r, h, xb2, tid);
+      accn += layer_ops<SH, SOLVER, 2, NORM>(pp, lr, a1, rtol, atol, tid);
+    }
+    __syncthreads();  // the operands are complete
+    accn += row_tiles<SH, S, NORM>(pp, xa, xb, a0, a1, rn < M, a0n, warp, lane, rtol, atol);
+    if constexpr (NORM) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) accn += __shfl_xor_sync(0xffffffffu, accn, o);
+      if (lane == 0) rsum[warp][r] = accn;
+    }
+    __syncthreads();  // the operands are rewritten for the next row
+    r = rn;
+    a0 = a0n;
+    a1 = a1n;
+  }
 }
 
 // Fold a finished row's a_theta into the CTA's Kahan partial.  The partial
@@ -1162,19 +1329,30 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
       __syncthreads();
       // the a_theta part of the norm: one parameter pass per live row
       if (Q.track) {
-        for (int r = 0; r < M; r++) {
-          if (!R.live[r]) continue;
-          const float *a0p = R.zero[r] ? nullptr : ath + (size_t(r) * 2 + R.cur[r]) * NP;
-          float *a1p = ath + (size_t(r) * 2 + (R.cur[r] ^ 1)) * NP;
-          float s;
-          if constexpr (PRECISE)
-            s = theta_pass<SH, SOLVER, true>(sm.cf, rec + size_t(r) * REC, R.h[r], a0p, a1p,
-                                             psum, pcomp, rtol, atol, tid);
-          else
-            s = theta_pass_tc<SH, SOLVER, true>(sm.p, rec + size_t(r) * REC, R.h[r], a0p, a1p,
-                                                rtol, atol, tid, warp, lane);
-          const float tot = block_sum<SH>(sm.red, s, tid);
-          if (tid == 0) R.acc[r] += tot;
+        if constexpr (PRECISE) {
+          for (int r = 0; r < M; r++) {
+            if (!R.live[r]) continue;
+            const float *a0p = R.zero[r] ? nullptr : ath + (size_t(r) * 2 + R.cur[r]) * NP;
+            float *a1p = ath + (size_t(r) * 2 + (R.cur[r] ^ 1)) * NP;
+            const float s = theta_pass<SH, SOLVER, true>(sm.cf, rec + size_t(r) * REC, R.h[r],
+                                                         a0p, a1p, psum, pcomp, rtol, atol, tid);
+            const float tot = block_sum<SH>(sm.red, s, tid);
+            if (tid == 0) R.acc[r] += tot;
+          }
+        } else {
+          theta_rows_tc<SH, SOLVER, true>(
+              sm.p, sm.rsum, rec, R.h, [&](int r) { return R.live[r] != 0; },
+              [&](int r, const float *&a0p, float *&a1p) {
+                a0p = R.zero[r] ? nullptr : ath + (size_t(r) * 2 + R.cur[r]) * NP;
+                a1p = ath + (size_t(r) * 2 + (R.cur[r] ^ 1)) * NP;
+              },
+              rtol, atol, tid, warp, lane);
+          if (tid < M && R.live[tid]) {
+            float t = 0.f;
+#pragma unroll
+            for (int w = 0; w < SH::WARPS; w++) t += sm.rsum[w][tid];
+            R.acc[tid] += t;
+          }
         }
         __syncthreads();
       }
@@ -1183,16 +1361,22 @@ __global__ void __launch_bounds__(256, 1) mlp_backsolve_kernel(SolveParams P, Bs
     __syncthreads();
     // untracked a_theta: add the accepted increments in place
     if (!Q.track) {
-      for (int r = 0; r < M; r++) {
-        if (!(R.live[r] && R.keep[r])) continue;
-        float *ap = ath + size_t(r) * 2 * NP;
-        const float *a0p = R.zero[r] ? nullptr : ap;
-        if constexpr (PRECISE)
+      if constexpr (PRECISE) {
+        for (int r = 0; r < M; r++) {
+          if (!(R.live[r] && R.keep[r])) continue;
+          float *ap = ath + size_t(r) * 2 * NP;
+          const float *a0p = R.zero[r] ? nullptr : ap;
           theta_pass<SH, SOLVER, false>(sm.cf, rec + size_t(r) * REC, R.h[r], a0p, ap, psum,
                                         pcomp, rtol, atol, tid);
-        else
-          theta_pass_tc<SH, SOLVER, false>(sm.p, rec + size_t(r) * REC, R.h[r], a0p, ap, rtol,
-                                           atol, tid, warp, lane);
+        }
+      } else {
+        theta_rows_tc<SH, SOLVER, false>(
+            sm.p, sm.rsum, rec, R.h, [&](int r) { return R.live[r] && R.keep[r]; },
+            [&](int r, const float *&a0p, float *&a1p) {
+              a1p = ath + size_t(r) * 2 * NP;
+              a0p = R.zero[r] ? nullptr : a1p;
+            },
+            rtol, atol, tid, warp, lane);
       }
     }
     // ---- accept: state, FSAL vectors and records, a_theta buffers --------------
