@@ -11,8 +11,10 @@ CUDA graph.  Inputs are seeded synthetic draws of exactly that distribution.
 One step = one solve of the whole batch.  `value` is trajectories/s with
 inputs resident in HBM (fused kernel K1); `e2e` is the same metric through the
 public API for a repeated solve, GraphedSolve(host_io=True) (one solve captured
-as a CUDA graph, the counterpart of a jitted diffeqsolve, with the copies of the
-pinned host inputs in and of the results out inside the graph) every step; `e2e_eager` the same through a fresh
+as a CUDA graph, the counterpart of a jitted diffeqsolve; its kernels read the
+page-locked host inputs and write the results into page-locked host memory in
+place over NVLink-C2C -- or, where the GPU does not map them, the graph copies
+them in and out) every step; `e2e_eager` the same through a fresh
 diffeqsolve call every step.  The plain one-trajectory-per-thread kernel K0 is timed the
 same way and reported beside it, together with the max relative error of both
 against the FP64 oracle and the oracle's own throughput on the host cores.
@@ -1215,8 +1217,10 @@ def main():
         torch.cuda.synchronize()
 
     # the page-locked inputs are the graph's staging buffers: each replay
-    # copies them to the device, solves, and copies ys, ts, result and stats
-    # back into page-locked host tensors (one graph launch per solve)
+    # solves with the kernels reading them and writing ys, ts, result and
+    # stats into page-locked host tensors in place (one graph launch per
+    # solve; copies in and out inside the graph where the GPU does not map
+    # page-locked memory)
     graphed = dfx.GraphedSolve(term, dfx.Dopri5(), 0.0, t1_h, None, y0_h, mu_h,
                                stepsize_controller=pid, throw=False, host_io=True)
     graphed_out = {}
@@ -1346,6 +1350,8 @@ def main():
                        "l2": "256 MB buffer written between timed solves"},
             "e2e": {"value": B * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h_graphed, "api": "GraphedSolve(host_io=True)",
+                    "transfer": ("kernels read and write page-locked host memory in place"
+                                 if graphed.zero_copy else "copies inside the graph"),
                     "results_equal_device_run": e2e_ok},
             "e2e_eager": {"value": B * world / eager_s, "unit": UNIT,
                           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -361,42 +361,55 @@ class Lowered:
         self.n_save = self.problem.n_save
         self.device = dev
 
-    def run_forward(self, stream=None, y0=None, params=None, keep_workspace=False):
+    def _outputs(self, io):
+        """ys, ts, result, stats on the device, None for those `io` gives."""
+        dev, B = self.device, self.B
+        shapes = (("ys", (B, self.n_save, self.dim), self.dtype),
+                  ("ts", (B, self.n_save), torch.float64), ("result", (B,), torch.int32),
+                  ("stats", (B, 3), torch.int32))
+        return [None if io and name in io else torch.empty(shape, dtype=dt, device=dev)
+                for name, shape, dt in shapes]
+
+    def run_forward(self, stream=None, y0=None, params=None, keep_workspace=False, io=None):
+        """Forward solve through gbdx_solve_fwd.  `io` maps any of t0, t1, dt0,
+        y0, args (inputs) and ys, ts, result, stats (outputs, then returned as
+        None) to addresses used instead of this object's buffers: the
+        zero-copy host I/O of GraphedSolve."""
         dev = self.device
-        B, D, n_save = self.B, self.dim, self.n_save
+        B = self.B
         y0 = self.y0 if y0 is None else y0
         params = self.params if params is None else params
-        ys = torch.empty((B, n_save, D), dtype=self.dtype, device=dev)
-        ts_out = torch.empty((B, n_save), dtype=torch.float64, device=dev)
-        res = torch.empty((B,), dtype=torch.int32, device=dev)
-        stats = torch.empty((B, 3), dtype=torch.int32, device=dev)
+        ys, ts_out, res, stats = self._outputs(io)
         ws_bytes = self.problem.workspace_size(B)
         ws = torch.empty((max(ws_bytes, 1),), dtype=torch.uint8, device=dev)
         if stream is None:
             stream = torch.cuda.current_stream(dev).cuda_stream
         p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        # io[name] when given (a device address of mapped page-locked host
+        # memory), else the buffer's own address
+        a = lambda name, t: io[name] if io and name in io else p(t)  # noqa: E731
         rc = self.problem.lib.gbdx_solve_fwd(
-            self.problem.handle, B, p(self.t0), p(self.t1), p(self.dt0), self.tstride,
-            p(y0), p(self.args), self.args_stride, p(params), p(self.save_ts),
-            p(ys), p(ts_out), p(res), p(stats), p(ws), ws_bytes, stream)
+            self.problem.handle, B, a("t0", self.t0), a("t1", self.t1), a("dt0", self.dt0),
+            self.tstride, a("y0", y0), a("args", self.args), self.args_stride, p(params),
+            p(self.save_ts), a("ys", ys), a("ts", ts_out), a("result", res), a("stats", stats),
+            p(ws), ws_bytes, stream)
         _lib.check(rc, "gbdx_solve_fwd")
         if keep_workspace:
             return ys, ts_out, res, stats, ws
         return ys, ts_out, res, stats
 
-    def run_forward_ex(self, stream=None, state_in=None, want_state=False):
+    def run_forward_ex(self, stream=None, state_in=None, want_state=False, io=None):
         """Forward solve through gbdx_solve_fwd_ex: the saved outputs plus the
         dense buffers (SaveAt(dense=True)) and the index of the event condition
         that ended each trajectory (-1 for none).  state_in ([B, GBDX_STATE_HEAD
         + dim] f64, include/gbdx.h) resumes a solve; want_state leaves the
-        final record in self.state_record."""
+        final record in self.state_record.  `io` as in run_forward, plus
+        event_index."""
         dev = self.device
         B, D, n_save = self.B, self.dim, self.n_save
-        ys = torch.empty((B, n_save, D), dtype=self.dtype, device=dev)
-        ts_out = torch.empty((B, n_save), dtype=torch.float64, device=dev)
-        res = torch.empty((B,), dtype=torch.int32, device=dev)
-        stats = torch.empty((B, 3), dtype=torch.int32, device=dev)
+        ys, ts_out, res, stats = self._outputs(io)
         p = lambda t: None if t is None or t.numel() == 0 else t.data_ptr()  # noqa: E731
+        a = lambda name, t: io[name] if io and name in io else p(t)  # noqa: E731
         ex = _lib.FwdExtras()
         interp = ev = None
         if self.fields["save_dense"]:
@@ -408,8 +421,11 @@ class Lowered:
             ex.dense_ts, ex.dense_info, ex.dense_n = p(dense_ts), p(dense_info), p(dense_n)
             interp = DenseInterpolation(self, dense_ts, dense_info, dense_n)
         if self.fields["n_event"]:
-            ev = torch.empty((B,), dtype=torch.int32, device=dev)
-            ex.event_index = p(ev)
+            if io and "event_index" in io:
+                ex.event_index = io["event_index"]
+            else:
+                ev = torch.empty((B,), dtype=torch.int32, device=dev)
+                ex.event_index = p(ev)
         self.state_record = None
         if state_in is not None:
             state_in = state_in.to(device=dev, dtype=torch.float64).contiguous()
@@ -423,9 +439,10 @@ class Lowered:
         if stream is None:
             stream = torch.cuda.current_stream(dev).cuda_stream
         rc = self.problem.lib.gbdx_solve_fwd_ex(
-            self.problem.handle, B, p(self.t0), p(self.t1), p(self.dt0), self.tstride,
-            p(self.y0), p(self.args), self.args_stride, p(self.params), p(self.save_ts),
-            p(ys), p(ts_out), p(res), p(stats), ctypes.byref(ex), p(ws), ws_bytes, stream)
+            self.problem.handle, B, a("t0", self.t0), a("t1", self.t1), a("dt0", self.dt0),
+            self.tstride, a("y0", self.y0), a("args", self.args), self.args_stride,
+            p(self.params), p(self.save_ts), a("ys", ys), a("ts", ts_out), a("result", res),
+            a("stats", stats), ctypes.byref(ex), p(ws), ws_bytes, stream)
         _lib.check(rc, "gbdx_solve_fwd_ex")
         return ys, ts_out, res, stats, interp, ev
 

@@ -103,6 +103,8 @@ def load():
         lib.gbdx_version.restype = i32
         lib.gbdx_bounds_checked.argtypes = []
         lib.gbdx_bounds_checked.restype = i32
+        lib.gbdx_host_device_pointer.argtypes = [vp, _c.POINTER(vp)]
+        lib.gbdx_host_device_pointer.restype = i32
         if bool(lib.gbdx_bounds_checked()) != bounds:
             raise RuntimeError(f"{os.path.basename(path)} is not the requested build")
         lib.gbdx_problem_desc_size.restype = _c.c_size_t
@@ -132,6 +134,16 @@ def check(rc: int, what: str):
         if rc == -5:
             raise GbdxBoundsError(f"{what}: {msg}")
         raise GbdxError(f"{what} failed ({rc}): {msg}")
+
+
+def host_device_pointer(ptr: int):
+    """The device address of page-locked host memory at `ptr` (kernels read
+    and write it in place), or None when it is not mapped for the current
+    device."""
+    out = _c.c_void_p()
+    if load().gbdx_host_device_pointer(_c.c_void_p(ptr), _c.byref(out)) != 0:
+        return None
+    return out.value
 
 
 def make_desc(fields: dict) -> ProblemDesc:

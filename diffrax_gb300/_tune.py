@@ -29,6 +29,7 @@ import tempfile
 
 import torch
 
+from . import _lib
 from ._core import RESULT_MESSAGES, RESULTS, SaveAt, Solution
 from ._integrate import Lowered, _raise_on_failure
 
@@ -194,19 +195,24 @@ class GraphedSolve:
 
     ``host_io=True`` serves a host-side caller with one graph launch per solve:
     the inputs given as page-locked host tensors become the solve's staging
-    buffers, copied to the device inside the graph, and the outputs (ys, ts,
-    result, stats, and the event index) are copied into page-locked host
-    tensors inside it too.  A call then writes any new inputs into the staging
-    buffers (or the caller writes them there itself), replays the graph,
-    waits for it, and returns a Solution of host tensors (overwritten by the
-    next call).
+    buffers and the outputs (ys, ts, result, stats, and the event index) are
+    page-locked host tensors.  Where the GPU maps them (every page-locked
+    buffer on a system with unified addressing; NVLink-C2C on Grace), the
+    solve's kernels read the inputs and write the outputs in place, with no
+    copy before or after them (``zero_copy`` is True); otherwise, or with
+    ``host_io="copy"``, the graph copies the inputs to the device and the
+    outputs back.  A call then writes
+    any new inputs into the staging buffers (or the caller writes them there
+    itself), replays the graph, waits for it, and returns a Solution of host
+    tensors (the same object each call when it carries no SaveAt fn or event
+    mask; overwritten by the next call).
     """
 
     def __init__(self, terms, solver, t0, t1, dt0, y0, args=None, *,
                  saveat: SaveAt = SaveAt(t1=True), stepsize_controller=None,
                  max_steps: int = 4096, throw: bool = True, kernel: str = "auto",
                  schedule: str = "auto", autotune: bool = False, event=None,
-                 host_io: bool = False):
+                 host_io=False):
         from ._core import ConstantStepSize
         if stepsize_controller is None:
             stepsize_controller = ConstantStepSize()
@@ -230,6 +236,10 @@ class GraphedSolve:
                     if not v.is_pinned():
                         raise ValueError(f"host_io needs page-locked host tensors ({name}: "
                                          "use Tensor.pin_memory())")
+                    if not v.is_contiguous():
+                        # the graph reads the staging buffer itself: a strided
+                        # view would be gathered once, at capture
+                        raise ValueError(f"host_io needs contiguous host tensors ({name})")
                     self._host_in[name] = v
         y0 = own(y0)
         if y0.dtype not in (torch.float32, torch.float64):
@@ -268,13 +278,20 @@ class GraphedSolve:
         warm = run()  # warm-up outside the capture (first-use set-up of the library)
         self.host_io = bool(host_io)
         self._host_out = []
+        self._io = None
         if host_io:
             self._host_out = [None if o is None else torch.empty(o.shape, dtype=o.dtype,
                                                                   pin_memory=True)
                               for o in warm]
+            if host_io != "copy":
+                self._io = self._mapped_io()
+        self.zero_copy = self._io is not None
         torch.cuda.synchronize()
 
         def staged():
+            if self._io is not None:
+                run(io=self._io)  # the kernels read and write the host buffers in place
+                return list(self._host_out)
             for name, h in self._host_in.items():
                 dst = getattr(low, name)
                 dst.copy_(h.reshape(dst.shape), non_blocking=True)
@@ -287,6 +304,23 @@ class GraphedSolve:
         with torch.cuda.graph(self.graph):
             self._outs = staged()
         torch.cuda.synchronize()
+        self._sol = None
+
+    # the solve's outputs in the order run_forward(_ex) returns them
+    _OUT_NAMES = ("ys", "ts", "result", "stats", None, "event_index")
+
+    def _mapped_io(self):
+        """Device addresses of the page-locked inputs and outputs, or None
+        (the copy path) unless every one of them is mapped."""
+        io = {}
+        pairs = list(self._host_in.items()) + [
+            (n, h) for n, h in zip(self._OUT_NAMES, self._host_out) if n and h is not None]
+        for name, h in pairs:
+            d = _lib.host_device_pointer(h.data_ptr())
+            if d is None:
+                return None
+            io[name] = d
+        return io
 
     def _copy_in(self, name, value):
         dst = getattr(self.low, name)
@@ -317,12 +351,21 @@ class GraphedSolve:
             torch.cuda.current_stream().synchronize()
             outs = [h if h is not None else o for o, h in zip(outs, self._host_out)]
         ys, ts, res, stats = outs[:4]
+        # a Solution of the same host tensors serves every call when nothing
+        # in it is computed per call
+        reuse = self.host_io and self._fn is None and self._event is None
+        if reuse and self._sol is not None:
+            if self.throw:
+                _raise_on_failure(res)
+            return self._sol
         if self._fn is not None:
             ys = self._fn(ts, ys, self.low.args if args is None else args)
         sol = Solution(t0=self.low.t0, t1=self.low.t1, ts=ts, ys=ys,
                        stats=dict(num_steps=stats[:, 0], num_accepted_steps=stats[:, 1],
                                   num_rejected_steps=stats[:, 2], max_steps=self.max_steps),
                        result=res)
+        if reuse:
+            self._sol = sol
         if self._event is not None:
             ev = outs[5]
             masks = [ev == i for i in range(len(self._event._conds))]

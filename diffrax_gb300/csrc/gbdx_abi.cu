@@ -287,6 +287,28 @@ int gbdx_bounds_checked(void) {
 
 size_t gbdx_problem_desc_size(void) { return sizeof(gbdx_problem_desc); }
 
+int gbdx_host_device_pointer(const void *host, void **device) {
+  if (!host || !device) return fail(GBDX_ERR_INVALID, "gbdx_host_device_pointer: null argument");
+  *device = nullptr;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, host);
+  if (e != cudaSuccess || a.type != cudaMemoryTypeHost) {
+    cudaGetLastError();
+    return fail(GBDX_ERR_INVALID, "gbdx_host_device_pointer: %p is not page-locked host memory",
+                host);
+  }
+  void *d = nullptr;
+  e = cudaHostGetDevicePointer(&d, const_cast<void *>(host), 0);
+  if (e != cudaSuccess || !d) {
+    cudaGetLastError();
+    return fail(GBDX_ERR_INVALID,
+                "gbdx_host_device_pointer: %p is not mapped for the current device (%s)", host,
+                cudaGetErrorString(e));
+  }
+  *device = d;
+  return GBDX_OK;
+}
+
 const char *gbdx_last_error(void) { return g_last_error.c_str(); }
 
 static int solver_order(int solver) {

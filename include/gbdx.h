@@ -3,8 +3,9 @@
  *
  * One problem handle describes a vmapped Diffrax solve: the solver, the step
  * size controller, the registered vector field, what to save and how to
- * differentiate.  Every array argument is a caller-owned CUDA device pointer;
- * the library performs no allocation inside a solve and never synchronises the
+ * differentiate.  Every array argument is a caller-owned CUDA device pointer
+ * (device memory, or page-locked host memory through the address
+ * gbdx_host_device_pointer gives); the library performs no allocation inside a solve and never synchronises the
  * host (results, including per-trajectory RESULTS codes, stay on the device).
  * Every call returns 0 on success or a negative gbdx_status; the message of the
  * last failure on the calling thread is available from gbdx_last_error().
@@ -431,6 +432,16 @@ int64_t gbdx_param_count(const gbdx_problem *problem);
 
 /* sizeof(gbdx_problem_desc), for bindings to check their struct layout. */
 size_t gbdx_problem_desc_size(void);
+
+/* The device address of page-locked host memory (no counterpart in the
+ * reference, where jax.device_put moves a host array to the device): on
+ * success *device is the address under which kernels read and write the
+ * host buffer at `host` directly (over NVLink-C2C on a Grace system), and it
+ * may be passed as any array argument of a solve -- a solve then moves its
+ * inputs and results itself, with no copy before or after it.  The buffer
+ * must stay allocated while such a solve runs.  GBDX_ERR_INVALID when `host`
+ * is not page-locked host memory mapped for the current device. */
+int gbdx_host_device_pointer(const void *host, void **device);
 
 /* Library version and the message of the last error on this thread. */
 int gbdx_version(void);

@@ -107,6 +107,9 @@ def test_graphed_solve_host_io():
     y0_h, mu_h, t1_h = (x.cpu().pin_memory() for x in (y0, mu, t1))
     g = dfx.GraphedSolve(term, dfx.Dopri5(), 0.0, t1_h, None, y0_h, mu_h,
                          stepsize_controller=PID, throw=False, host_io=True)
+    # page-locked buffers are mapped on this GPU: the kernels read and write
+    # them in place
+    assert g.zero_copy
     sol = g()
     ref = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1, None, y0, mu, stepsize_controller=PID)
     assert sol.ys.device.type == "cpu" and sol.ys.is_pinned()
@@ -114,10 +117,51 @@ def test_graphed_solve_host_io():
     # new inputs written into the staging buffers by the caller, or passed
     y0n, mun, t1n = vdp_inputs(4096, 8)
     y0_h.copy_(y0n.cpu())
-    sol = g(args=mun.cpu(), t1=t1n.cpu())
+    sol2 = g(args=mun.cpu(), t1=t1n.cpu())
+    assert sol2 is sol  # the same host tensors, overwritten
     ref = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1n, None, y0n, mun, stepsize_controller=PID)
     assert torch.equal(sol.ys, ref.ys.cpu())
+    assert torch.equal(sol.ts, ref.ts.cpu())
     assert torch.equal(sol.stats["num_steps"], ref.stats["num_steps"].cpu())
+    # the copy path: the graph copies the staging buffers in and the
+    # results out
+    gc = dfx.GraphedSolve(term, dfx.Dopri5(), 0.0, t1_h, None, y0_h, mu_h,
+                          stepsize_controller=PID, throw=False, host_io="copy")
+    assert not gc.zero_copy
+    y0_h.copy_(y0.cpu())
+    t1_h.copy_(t1.cpu())
+    mu_h.copy_(mu.cpu())
+    ref = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1, None, y0, mu, stepsize_controller=PID)
+    solc = gc()
+    assert torch.equal(solc.ys, ref.ys.cpu()) and torch.equal(solc.result, ref.result.cpu())
+    # a strided staging buffer would be gathered once, at capture
+    y0_t = torch.empty((2, 4096), dtype=torch.float32).pin_memory()
+    with pytest.raises(ValueError, match="contiguous"):
+        dfx.GraphedSolve(term, dfx.Dopri5(), 0.0, t1_h, None, y0_t.t(), mu_h,
+                         stepsize_controller=PID, host_io=True)
     with pytest.raises(ValueError, match="page-locked"):
         dfx.GraphedSolve(term, dfx.Dopri5(), 0.0, t1.cpu(), None, y0.cpu(), mu.cpu(),
                          stepsize_controller=PID, host_io=True)
+
+
+def test_graphed_solve_host_io_with_events():
+    # zero-copy host I/O with the event index among the outputs
+    term = dfx.ODETerm(dfx.VanDerPol())
+    y0, mu, t1 = vdp_inputs(2048, 9)
+    y0_h, mu_h, t1_h = (x.cpu().pin_memory() for x in (y0, mu, t1))
+    ev = dfx.Event(dfx.LinearCondition([1.0, 0.0]), dfx.Newton(1e-5, 1e-5), direction=False)
+    g = dfx.GraphedSolve(term, dfx.Dopri5(), 0.0, t1_h, None, y0_h, mu_h,
+                         stepsize_controller=PID, throw=False, event=ev, host_io=True)
+    assert g.zero_copy
+    sol = g()
+    ref = dfx.diffeqsolve(term, dfx.Dopri5(), 0.0, t1, None, y0, mu, stepsize_controller=PID,
+                          event=ev, throw=False)
+    assert sol.event_mask.device.type == "cpu"
+    assert torch.equal(sol.ys, ref.ys.cpu()) and torch.equal(sol.event_mask, ref.event_mask.cpu())
+
+
+def test_host_device_pointer():
+    from diffrax_gb300 import _lib
+    assert _lib.host_device_pointer(torch.zeros(16).pin_memory().data_ptr()) is not None
+    assert _lib.host_device_pointer(torch.zeros(16).data_ptr()) is None  # pageable
+    assert _lib.host_device_pointer(torch.zeros(16, device="cuda").data_ptr()) is None
