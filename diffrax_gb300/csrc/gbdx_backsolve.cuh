@@ -80,6 +80,7 @@ struct BsRows {
   int active[M], want[M], first[M], keep[M], nan_y[M], nan_a[M], dir[M];
   int seg[M], jold[M], trans[M], newtraj[M], done[M], firstseg[M];
   int nseg[M], nsteps[M], nacc[M], nrej[M], result[M], sres[M], sc[M], nc[M], at_dtmin[M];
+  double ginv[M];  // RN(1 / nc), for the grid fraction
   int live[M], cur[M], zero[M];
   float part[M][8];  // error-norm partials per 8-column tile, summed in order
 };
@@ -999,6 +1000,7 @@ __device__ void bs_next_segment(BsRows<M> &R, int r, const SolveParams &P) {
       if (R.firstseg[r]) {
         R.sc[r] = 1;
         R.nc[r] = (int)ceil((te - ts_) / next_up(h0));
+        R.ginv[r] = 1.0 / double(R.nc[r]);
         R.t0s[r] = ts_;
         R.t1s[r] = te;
       }
@@ -1059,7 +1061,7 @@ __device__ void bs_row_control(BsRows<M> &R, int r, float n_norm, const SolvePar
   } else {
     keep = true;
     const int s2 = R.sc[r] + 1;
-    double tn = R.t0s[r] + (R.t1s[r] - R.t0s[r]) * (double(s2) / double(R.nc[r]));
+    double tn = grid_time(R.t0s[r], R.t1s[r], s2, R.nc[r], R.ginv[r]);
     if (s2 == R.nc[r]) tn = R.t1s[r];
     R.sc[r] = s2;
     nt0 = R.tnext[r];

@@ -353,6 +353,28 @@ __device__ __forceinline__ double next_down(double x) {
   return from_order_key(k);
 }
 
+// The ConstantStepSize grid fraction RN(s / n) (constant.py:84-86) for
+// integers 0 < s <= n < 2^31, from inv = RN(1 / n) formed once per
+// trajectory: q = RN(s inv) lies within one ulp of s / n, the remainder
+// s - q n is exact under an FMA, and RN(q + r inv) is then the correctly
+// rounded quotient (Markstein's theorem on the final correction step of
+// Newton-Raphson division).  Three dependent FP64 operations instead of a
+// division, whose dependent chain GB300's narrow FP64 pipe makes the longest
+// part of a constant step.
+__device__ __forceinline__ double grid_fraction(int s, int n, double inv) {
+  const double sd = double(s);
+  const double q = __dmul_rn(sd, inv);
+  const double r = fma(-q, double(n), sd);
+  return fma(r, inv, q);
+}
+
+// The grid time t0 + (t1 - t0) RN(s / n) rounded as the reference rounds it:
+// a multiply, then an add, never contracted into an FMA (the FP32-state
+// kernels are compiled with contraction on).
+__device__ __forceinline__ double grid_time(double t0s, double t1s, int s, int n, double inv) {
+  return __dadd_rn(t0s, __dmul_rn(t1s - t0s, grid_fraction(s, n, inv)));
+}
+
 // t1 minus 100 ULP (_integrate.py:319-322): 100 applications of
 // nextafter(., -inf), the threshold above which tnext snaps to t1.
 __device__ __forceinline__ double t1_clip_floor(double t1) {

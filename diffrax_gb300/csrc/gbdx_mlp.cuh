@@ -66,6 +66,7 @@ struct RowState {
   int active[M], first[M], keep[M], anynan[M], dir[M], save_index[M], ts_index[M];
   int nsteps[M], nacc[M], nrej[M], result[M], sflag[M], sslot[M], fin[M], nfill[M];
   int loaded[M], sc[M], nc[M], cpstride[M], cpslot[M], cpcompact[M], at_dtmin[M], live[M];
+  double ginv[M];  // RN(1 / nc), for the grid fraction
   int sdown[M], stslot[M];  // SaveAt(steps=n): steps to the next save; this step's slot
   int sidx[M], jidx[M];     // ClipStepSizeController: search hints into step_ts / jump_ts
   // the error norm's partial sums per 8-column output tile, added in a fixed
@@ -404,6 +405,7 @@ __device__ void row_init(RowState<M> &R, RowEvents<M> *EV, int r, int64_t i,
       if (fsal && st[5] == 0.0 && st[6] == 0.0) R.first[r] = 0;
     }
   }
+  if (P.controller != GBDX_PID) R.ginv[r] = 1.0 / double(R.nc[r]);
   if (P.save_t0) {
     *GBDX_AT(P, P.ts_out, i * P.n_save, 1, P.batch * P.n_save, GBDX_SITE_TS) = a * dir;
     R.save_index[r] = 1;
@@ -486,7 +488,7 @@ __device__ void row_control(RowState<M> &R, int r, int D, const SolveParams &P) 
   } else {
     keep = true;
     const int s2 = R.sc[r] + 1;
-    double tn = R.t0s[r] + (R.t1s[r] - R.t0s[r]) * (double(s2) / double(R.nc[r]));
+    double tn = grid_time(R.t0s[r], R.t1s[r], s2, R.nc[r], R.ginv[r]);
     if (s2 == R.nc[r]) tn = R.t1s[r];
     R.sc[r] = s2;
     nt0 = R.tnext[r];

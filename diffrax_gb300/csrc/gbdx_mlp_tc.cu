@@ -151,7 +151,8 @@ __device__ void control_row(Row &R, float acc, const SolveParams &P) {
   } else {
     keep = true;
     const int s2 = R.sc + 1;
-    double tn = R.t0s + (R.t1s - R.t0s) * (double(s2) / double(R.nc));
+    // the reference's rounding: a multiply, then an add (no contraction)
+    double tn = __dadd_rn(R.t0s, __dmul_rn(R.t1s - R.t0s, double(s2) / double(R.nc)));
     if (s2 == R.nc) tn = R.t1s;
     R.sc = s2;
     nt0 = R.tnext;

@@ -277,7 +277,7 @@ __device__ __forceinline__ void bs_control_f64(BsRows<1> &R, double scaled, doub
   } else {
     keep = true;
     const int s2 = R.sc[0] + 1;
-    double tn = R.t0s[0] + (R.t1s[0] - R.t0s[0]) * (double(s2) / double(R.nc[0]));
+    double tn = grid_time(R.t0s[0], R.t1s[0], s2, R.nc[0], R.ginv[0]);
     if (s2 == R.nc[0]) tn = R.t1s[0];
     R.sc[0] = s2;
     nt0 = R.tnext[0];

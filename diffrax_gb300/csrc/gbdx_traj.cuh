@@ -217,6 +217,7 @@ struct Traj {
   int at_dtmin;
   int sc, nc;  // ConstantStepSize state (constant.py:41-57)
   double t0s, t1s;
+  double ginv;  // RN(1 / nc), for the grid fraction
   int first, dir, save_index, ts_index, nsteps, nacc, nrej, result;
   int sdown;  // XO: accepted steps left until the next SaveAt(steps=n) save
   int sidx, jidx;  // XO: ClipStepSizeController step / jump indices (hints)
@@ -308,6 +309,7 @@ struct Traj {
         t1s = st_in[3];
       }
     }
+    if (P.controller != GBDX_PID) ginv = 1.0 / double(nc);
     tnext = fmin(tn, b);
     dtc = tnext - a;
     pend = false;
@@ -773,7 +775,7 @@ struct Traj {
     } else {
       keep = true;
       const int s2 = sc + 1;
-      double tn = t0s + (t1s - t0s) * (double(s2) / double(nc));
+      double tn = grid_time(t0s, t1s, s2, nc, ginv);
       if (s2 == nc) tn = t1s;
       if (nc < 0) tn = tnext + t1s;
       sc = s2;

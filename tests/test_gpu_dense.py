@@ -116,6 +116,28 @@ def test_saveat_steps_reverse_time_with_ts(kernel):
 
 
 @pytest.mark.parametrize("kernel", ["plain", "fused"])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("reverse", [False, True])
+def test_constant_grid_times_equal_oracle_bit_for_bit(kernel, dtype, reverse):
+    # ConstantStepSize steps to t0 + (t1 - t0) (n / N) (constant.py:84-86).
+    # The kernels form n / N from RN(1 / N) with an FMA correction and round
+    # the product and the sum separately: every step time must equal the
+    # oracle's (a C division, no contraction) bit for bit, for per-trajectory
+    # t1 (N from 73 to 219) and an awkward dt0, forward and backward in time
+    rng = np.random.default_rng(31)
+    B = 256
+    y0 = rng.uniform(5, 15, (B, 2))
+    ends = rng.uniform(1.0, 3.0, B)
+    t0, t1, dt0 = (ends, 0.0, -0.0137) if reverse else (0.0, ends, 0.0137)
+    sol, r, _ = solve_pair(dfx.LotkaVolterra(), dfx.Euler(), dfx.ConstantStepSize(),
+                           dfx.SaveAt(steps=1, t1=True), t0, t1, dt0, y0, LV_ARGS, dtype,
+                           kernel, max_steps=256)
+    assert (sol.result.cpu().numpy() == 0).all()
+    assert np.array_equal(sol.stats["num_steps"].cpu().numpy(), r["stats"][:, 0])
+    assert np.array_equal(sol.ts.cpu().numpy(), r["ts"])
+
+
+@pytest.mark.parametrize("kernel", ["plain", "fused"])
 @pytest.mark.parametrize("solver", ["euler", "heun", "dopri5", "tsit5"])
 def test_dense_fp64_matches_oracle(kernel, solver):
     rng = np.random.default_rng(9)
