@@ -1094,9 +1094,14 @@ int gbdx_solve_bwd(const gbdx_problem *problem, int64_t batch, const double *t0,
   }
   if (plain)
     e = gbdx::launch_reduce_columns(Q.part_sum, np, batch, static_cast<float *>(grad_params), s);
-  else
+  else if (problem->d.mlp_precision == GBDX_MLP_FP32)
     e = gbdx::launch_reduce_partials(Q.part_sum, Q.part_comp, batch > 0 ? L.n_cta : 0, np,
                                      static_cast<float *>(grad_params), s);
+  else  // the tensor-core mode keeps the weight blocks in fragment order
+    e = gbdx::launch_reduce_partials_frag(
+        Q.part_sum, Q.part_comp, batch > 0 ? L.n_cta : 0, problem->d.dim,
+        problem->d.mlp_widths[1], problem->d.diffusion != GBDX_DIFF_NONE,
+        static_cast<float *>(grad_params), s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
   return bounds_report(P, s, "gbdx_solve_bwd");
 }
@@ -1216,7 +1221,7 @@ int gbdx_backsolve_bwd_ex(const gbdx_problem *problem, int64_t batch, const doub
     e = gbdx::launch_reduce_partials(Q.psum, Q.pcomp, batch > 0 ? L.n_cta : 0, np,
                                      static_cast<float *>(grad_params), s);
   else
-    e = gbdx::launch_reduce_partials_frag(Q.psum, Q.pcomp, batch > 0 ? L.n_cta : 0, D, H,
+    e = gbdx::launch_reduce_partials_frag(Q.psum, Q.pcomp, batch > 0 ? L.n_cta : 0, D, H, 0,
                                           static_cast<float *>(grad_params), s);
   if (e != cudaSuccess) return cuda_fail(e, "gradient reduction");
   return bounds_report(P, s, "gbdx_backsolve_bwd");

@@ -89,10 +89,11 @@ BsEntry find_plain_backsolve_entry(int solver, int D, int H);
 // BF16 mma B fragments of B[k][n] = trans ? W[n][k] : W[k][n] (K x N).
 cudaError_t launch_frag_prep(const float *W, int ldw, int K, int N, int trans, uint2 *out,
                              cudaStream_t s);
-// The same for backsolve partials whose weight blocks are in mma-fragment order
-// (MLP D -> H -> H -> D), written to grad in the flat order.
+// The same for partials whose weight blocks are in mma-fragment order (MLP
+// D -> H -> H -> D, then with `diffusion` the neural SDE's D x D diffusion),
+// written to grad in the flat order.
 cudaError_t launch_reduce_partials_frag(const float *psum, const float *pcomp, int n_cta, int D,
-                                        int H, float *out, cudaStream_t s);
+                                        int H, int diffusion, float *out, cudaStream_t s);
 OdeEntry find_mlp_plain_entry(int solver, int D, int H, bool sde);
 // The plain (one trajectory per thread) RecursiveCheckpointAdjoint backward:
 // full tape, per-trajectory parameter cotangents dP [n_params][batch].

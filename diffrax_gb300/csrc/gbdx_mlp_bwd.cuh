@@ -105,9 +105,14 @@ struct BwdSmem<SH, true, SDE> {
   BwdRows<SH::M> rows;
 };
 
-// dW[o][n] (at flat offset `off`, row length N) += G^T S over the tile's rows,
+// dW[o][n] (the [O][N] block at offset `off`) += G^T S over the tile's rows,
 // with G and S held as three BF16 pieces each (warp_tile_gemm_tt3),
-// accumulated into this CTA's Kahan partials.
+// accumulated into this CTA's Kahan partials.  The partials of a weight block
+// are in mma-fragment order: m16n8 tile t = (o / 16) (N / 8) + n / 8 holds its
+// 128 values at off + 128 t + 4 lane + q, q indexing the accumulator elements
+// (g, 2c), (g, 2c + 1), (g + 8, 2c), (g + 8, 2c + 1), so a lane's four values
+// are one 16-byte load and store (the final reduction restores the flat
+// order).
 template <class SH, int O, int N>
 __device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *const (&G)[3], int ldg,
                                          const __nv_bfloat16 *const (&S)[3], int lds, int off,
@@ -124,32 +129,32 @@ __device__ __forceinline__ void dw_tiles(const __nv_bfloat16 *const (&G)[3], int
     const int ot = t / (N / 8), nt0 = t % (N / 8);
     // the partials this chunk updates are loaded before its products, so the
     // L2 latency overlaps the tensor-core work
-    float2 ps[CH][2], pc[CH][2];
+    float4 ps[CH], pc[CH];
 #pragma unroll
-    for (int j = 0; j < CH; j++)
-#pragma unroll
-      for (int hr = 0; hr < 2; hr++) {
-        const int p = off + (ot * 16 + g + hr * 8) * N + (nt0 + j) * 8 + 2 * c;
-        ps[j][hr] = *reinterpret_cast<const float2 *>(psum + p);
-        pc[j][hr] = *reinterpret_cast<const float2 *>(pcomp + p);
-      }
+    for (int j = 0; j < CH; j++) {
+      const int p = off + (t + j) * 128 + lane * 4;
+      ps[j] = *reinterpret_cast<const float4 *>(psum + p);
+      pc[j] = *reinterpret_cast<const float4 *>(pcomp + p);
+    }
     float acc[CH][4];
 #pragma unroll
     for (int j = 0; j < CH; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
     warp_tile_gemm_tt3<SH::M, CH>(acc, G, ldg, ot * 16, S, lds, nt0 * 8, lane);
 #pragma unroll
-    for (int j = 0; j < CH; j++)
+    for (int j = 0; j < CH; j++) {
+      float sv[4] = {ps[j].x, ps[j].y, ps[j].z, ps[j].w};
+      float cv[4] = {pc[j].x, pc[j].y, pc[j].z, pc[j].w};
 #pragma unroll
-      for (int hr = 0; hr < 2; hr++) {
-        const int p = off + (ot * 16 + g + hr * 8) * N + (nt0 + j) * 8 + 2 * c;
-        float s0 = ps[j][hr].x, s1 = ps[j][hr].y, c0 = pc[j][hr].x, c1 = pc[j][hr].y;
-        const float y0 = acc[j][2 * hr] - c0, y1 = acc[j][2 * hr + 1] - c1;
-        const float t0 = s0 + y0, t1 = s1 + y1;
-        c0 = (t0 - s0) - y0;
-        c1 = (t1 - s1) - y1;
-        *reinterpret_cast<float2 *>(psum + p) = make_float2(t0, t1);
-        *reinterpret_cast<float2 *>(pcomp + p) = make_float2(c0, c1);
+      for (int q = 0; q < 4; q++) {
+        const float y = acc[j][q] - cv[q];
+        const float tq = sv[q] + y;
+        cv[q] = (tq - sv[q]) - y;
+        sv[q] = tq;
       }
+      const int p = off + (t + j) * 128 + lane * 4;
+      *reinterpret_cast<float4 *>(psum + p) = make_float4(sv[0], sv[1], sv[2], sv[3]);
+      *reinterpret_cast<float4 *>(pcomp + p) = make_float4(cv[0], cv[1], cv[2], cv[3]);
+    }
   }
 }
 
