@@ -69,6 +69,11 @@ struct BwdRows {
   float h[M], theta[M];
   int active[M], loaded[M], fin[M], dir[M], mode[M], n[M], m[M], N[M], s[M], cs[M];
   int k_lo[M], k_hi[M], sflag[M], sslot[M], ld_kind[M], ld_slot[M], live[M];
+  // SDE: the time whose Brownian value W the row's threads carry from the
+  // row's previous iteration (NaN: none), and which ends of this iteration's
+  // step still need a tree evaluation
+  double wt[M];
+  int w_lo[M], w_hi[M];
 };
 enum { kModeBwd = 0, kModeFwd = 1 };
 enum { kLoadNone = 0, kLoadCheckpoint = 1, kLoadScratch = 2 };
@@ -365,6 +370,7 @@ __device__ void bwd_row_init(BwdRows<SH::M> &R, int r, int64_t i, const SolvePar
   R.s[r] = s;
   R.active[r] = 1;
   R.fin[r] = 0;
+  R.wt[r] = __longlong_as_double(0x7ff8000000000000LL);  // no carried W
   // number of ts saved: those <= t_N (all of them unless max_steps stopped it)
   const double tN = *GBDX_AT(P, P.tape_t, i * (P.max_steps + 1) + N, 1,
                              P.batch * (P.max_steps + 1), GBDX_SITE_TAPE_T);
@@ -469,6 +475,9 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
   }
 
   float K[S][NE], F[NE], sig[NE], dW[NE];
+  float Wc[SDE ? NE : 1];  // the carried Brownian values of the owned elements
+#pragma unroll
+  for (int e = 0; e < (SDE ? NE : 1); e++) Wc[e] = 0.f;
   VbtQuadCache vc;  // this lane's tree path (SDE)
   vc.traj = -1;
   vc.node = 0;
@@ -495,6 +504,10 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
           R.k_lo[tid] = R.k_hi[tid];
         }
       }
+      if constexpr (SDE) {
+        R.w_lo[tid] = R.live[tid] && !(R.wt[tid] == R.t_lo[tid]);
+        R.w_hi[tid] = R.live[tid] && !(R.wt[tid] == R.t_hi[tid]);
+      }
     }
     __syncthreads();
     float hrow[NE];
@@ -505,13 +518,28 @@ __global__ void __launch_bounds__(256) mlp_bwd_kernel(SolveParams P, BwdParams Q
       hrow[e] = R.h[row];
     }
     if constexpr (SDE) {
-      // W at both ends of the step from the lane's cached tree path (the
-      // evaluations of consecutive iterations lie within a step or two)
+      // W at both ends of the step.  A row's consecutive iterations share an
+      // end (a recompute step's t_hi is the next one's t_lo; a backpropagated
+      // step's t_lo is the previous step's t_hi), whose value its threads
+      // carry: W(t) is a function of (seed, trajectory, t), so the carried
+      // value is the one a fresh evaluation gives.  The other ends come from
+      // the lane's cached tree path (consecutive evaluations lie within a
+      // step or two).
       float wa[NE], wb[NE];
-      vbt_owned<SH>(P, R, R.live, R.t_lo, vc, wa, warp, lane);
-      vbt_owned<SH>(P, R, R.live, R.t_hi, vc, wb, warp, lane);
+      vbt_owned<SH>(P, R, R.w_lo, R.t_lo, vc, wa, warp, lane);
+      vbt_owned<SH>(P, R, R.w_hi, R.t_hi, vc, wb, warp, lane);
 #pragma unroll
-      for (int e = 0; e < NE; e++) dW[e] = wb[e] - wa[e];
+      for (int e = 0; e < NE; e++) {
+        int row, col;
+        elem_rc<SH>(e, warp, lane, row, col);
+        if (R.live[row]) {
+          if (!R.w_lo[row]) wa[e] = Wc[e];
+          if (!R.w_hi[row]) wb[e] = Wc[e];
+          Wc[e] = R.mode[row] == kModeFwd ? wb[e] : wa[e];
+        }
+        dW[e] = wb[e] - wa[e];
+      }
+      if (tid < M && R.live[tid]) R.wt[tid] = R.mode[tid] == kModeFwd ? R.t_hi[tid] : R.t_lo[tid];
     }
     // ---- B. forward stages of the step ----------------------------------
     float Yi[NE];
