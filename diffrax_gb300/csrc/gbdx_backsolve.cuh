@@ -697,15 +697,39 @@ __device__ __forceinline__ float batch_tiles(BsPassOps<SH> &pp,
   auto &ps = LY::ops(pp);
   const int g = lane >> 2, c = lane & 3;
   float accn = 0.f;
+  // A batch starts on a multiple of U tiles; when U divides the tiles of an
+  // output block, its tiles share one block: its A fragment and o-side
+  // values are loaded once for the batch.
+  constexpr bool ONE_BLOCK = NTL % TL::U == 0;
+  const int tf = warp * TPW + tb;
+  uint32_t ab[4];
+  float u0a_b = 0.f, u0b_b = 0.f, a2a_b = 0.f, a2b_b = 0.f, a3a_b = 0.f, a3b_b = 0.f;
+  if constexpr (ONE_BLOCK) {
+    const int ot = tf / NTL, og = ot * 16 + g;
+    ldsm_a(ab, &ps.Du[ot * 16][0], 24, lane);
+    u0a_b = ps.U0[og];
+    u0b_b = ps.U0[og + 8];
+    a2a_b = ps.A2[og];
+    a2b_b = ps.A2[og + 8];
+    if constexpr (NORM) {
+      a3a_b = ps.A3[og];
+      a3b_b = ps.A3[og + 8];
+    }
+  }
 #pragma unroll
   for (int u = 0; u < TL::U; u++) {
-    const int t = warp * TPW + tb + u, ot = t / NTL, nt = t % NTL;
+    const int t = tf + u, ot = t / NTL, nt = t % NTL;
     const int og = ot * 16 + g, ic = nt * 8 + 2 * c;
     uint32_t a[4], bb[2], be[2];
-    ldsm_a(a, &ps.Du[ot * 16][0], 24, lane);
+    if constexpr (ONE_BLOCK) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) a[k] = ab[k];
+    } else {
+      ldsm_a(a, &ps.Du[ot * 16][0], 24, lane);
+    }
     ldsm_bt1(bb, &ps.Bb[0][0], NI + 8, 0, nt * 8, lane);
-    const float u0a = ps.U0[og], u0b = ps.U0[og + 8];
-    const float a2a = ps.A2[og], a2b = ps.A2[og + 8];
+    const float u0a = ONE_BLOCK ? u0a_b : ps.U0[og], u0b = ONE_BLOCK ? u0b_b : ps.U0[og + 8];
+    const float a2a = ONE_BLOCK ? a2a_b : ps.A2[og], a2b = ONE_BLOCK ? a2b_b : ps.A2[og + 8];
     const float2 v0 = *reinterpret_cast<const float2 *>(&ps.v0[ic]);
     const float2 b1 = *reinterpret_cast<const float2 *>(&ps.B1[ic]);
     float cb[4] = {fmaf(u0a, b1.x, a2a * v0.x), fmaf(u0a, b1.y, a2a * v0.y),
@@ -716,7 +740,7 @@ __device__ __forceinline__ float batch_tiles(BsPassOps<SH> &pp,
     for (int q = 0; q < 4; q++) x1[q] = x0[u][q] + cb[q];
     if constexpr (NORM) {
       ldsm_bt1(be, &ps.Be[0][0], NI + 8, 0, nt * 8, lane);
-      const float a3a = ps.A3[og], a3b = ps.A3[og + 8];
+      const float a3a = ONE_BLOCK ? a3a_b : ps.A3[og], a3b = ONE_BLOCK ? a3b_b : ps.A3[og + 8];
       const float2 b3 = *reinterpret_cast<const float2 *>(&ps.B3[ic]);
       float ce[4] = {fmaf(u0a, b3.x, a3a * v0.x), fmaf(u0a, b3.y, a3a * v0.y),
                      fmaf(u0b, b3.x, a3b * v0.x), fmaf(u0b, b3.y, a3b * v0.y)};
