@@ -625,7 +625,13 @@ struct BsTiles {
   }
   static constexpr int T0 = tpw<0>(), T1 = tpw<1>(), T2 = tpw<2>();
   static constexpr int U = T0 < 16 ? T0 : 16, NB1 = T1 / U, NB = NB1 + 2;
-  static constexpr int PF = 2;  // L2 prefetch distance, in batches
+  // L2 prefetch distance, in batches: measured best at 2 for the tracked
+  // norm's pass (a_theta0 read, the candidate written to the other buffer)
+  // and 3 for the in-place pass of the seminorm
+  template <bool NORM>
+  static constexpr int pf() {
+    return NORM ? 2 : 3;
+  }
   static_assert(T0 * SH::WARPS == (BsLayer<SH, 0>::NO / 16) * (BsLayer<SH, 0>::NI / 8) &&
                     T1 * SH::WARPS == (BsLayer<SH, 1>::NO / 16) * (BsLayer<SH, 1>::NI / 8) &&
                     T2 * SH::WARPS == (BsLayer<SH, 2>::NO / 16) * (BsLayer<SH, 2>::NI / 8),
@@ -644,8 +650,8 @@ __device__ __forceinline__ const float *batch_ptr(const float *a0, int i, int wa
 }
 
 // Bulk prefetch into L2 of batch i of the row (i >= NB: batch i - NB of the
-// next row, when there is one), PF batches ahead of the register loads, so
-// that those find their lines in L2.
+// next row, when there is one), BsTiles::pf batches ahead of the register
+// loads, so that those find their lines in L2.
 template <class SH>
 __device__ __forceinline__ void batch_prefetch(const float *a0, const float *a0n, bool next,
                                                int i, int warp, int lane) {
@@ -769,18 +775,18 @@ __device__ __forceinline__ float row_tiles(BsPassOps<SH> &pp, float (&xa)[BsTile
   for (int tb = 0, i = 2; tb < TL::T1; tb += 2 * U, i += 2) {
     // batch i: layer-1 tile tb + U; batch i + 1: the next
     batch_load<SH, 1>(xa, a0, tb + U, warp, lane);
-    batch_prefetch<SH>(a0, a0n, next, i + TL::PF, warp, lane);
+    batch_prefetch<SH>(a0, a0n, next, i + TL::template pf<NORM>(), warp, lane);
     s += batch_tiles<SH, S, 1, NORM>(pp, xb, a1, tb, warp, lane, rtol, atol);
     if (tb + 2 * U < TL::T1)
       batch_load<SH, 1>(xb, a0, tb + 2 * U, warp, lane);
     else
       batch_load<SH, 2>(xb, a0, 0, warp, lane);
-    batch_prefetch<SH>(a0, a0n, next, i + 1 + TL::PF, warp, lane);
+    batch_prefetch<SH>(a0, a0n, next, i + 1 + TL::template pf<NORM>(), warp, lane);
     s += batch_tiles<SH, S, 1, NORM>(pp, xa, a1, tb + U, warp, lane, rtol, atol);
   }
   if (next) {
     batch_load<SH, 0>(xa, a0n, 0, warp, lane);
-    batch_prefetch<SH>(a0, a0n, next, TL::NB + TL::PF, warp, lane);
+    batch_prefetch<SH>(a0, a0n, next, TL::NB + TL::template pf<NORM>(), warp, lane);
   }
   s += batch_tiles<SH, S, 2, NORM>(pp, xb, a1, 0, warp, lane, rtol, atol);
   return s;
@@ -891,7 +897,8 @@ __device__ __forceinline__ void theta_rows_tc(BsPassOps<SH> &pp, float (*rsum)[S
   float xa[TL::U][4], xb[TL::U][4];
   batch_load<SH, 0>(xa, a0, 0, warp, lane);
 #pragma unroll
-  for (int i = 1; i <= TL::PF; i++) batch_prefetch<SH>(a0, nullptr, false, i, warp, lane);
+  for (int i = 1; i <= TL::template pf<NORM>(); i++)
+    batch_prefetch<SH>(a0, nullptr, false, i, warp, lane);
   while (r < M) {
     const int rn = next_row(r);
     const float *a0n = nullptr;
@@ -904,7 +911,7 @@ __device__ __forceinline__ void theta_rows_tc(BsPassOps<SH> &pp, float (*rsum)[S
       const float xb0 = bias_load<SH, 0>(a0, tid), xb1 = bias_load<SH, 1>(a0, tid),
                   xb2 = bias_load<SH, 2>(a0, tid);
       batch_load<SH, 1>(xb, a0, 0, warp, lane);
-      batch_prefetch<SH>(a0, a0n, rn < M, 1 + TL::PF, warp, lane);
+      batch_prefetch<SH>(a0, a0n, rn < M, 1 + TL::template pf<NORM>(), warp, lane);
       LayerRecs<S> lr;
       layer_recs<SH, S, 0>(lr, rec_r, h, xb0, tid);
       accn = layer_ops<SH, SOLVER, 0, NORM>(pp, lr, a1, rtol, atol, tid);
