@@ -470,3 +470,17 @@ def test_pid_step_ts_builds_the_clip_controller():
     assert isinstance(c, dfx.ClipStepSizeController)
     assert isinstance(c.controller, dfx.PIDController) and c.controller.rtol == 1e-3
     assert isinstance(dfx.PIDController(rtol=1e-3, atol=1e-6, step_ts=None), dfx.PIDController)
+
+
+def test_host_device_pointer_rejects_unmapped_memory():
+    # zero-copy host I/O takes only page-locked memory the GPU maps: null
+    # arguments are invalid, and pageable host memory (or, without a GPU,
+    # any memory) is reported as unmapped rather than passed on
+    lib = _lib.load()
+    out = ctypes.c_void_p()
+    assert lib.gbdx_host_device_pointer(None, ctypes.byref(out)) == -1
+    buf = ctypes.create_string_buffer(64)
+    assert lib.gbdx_host_device_pointer(ctypes.addressof(buf), None) == -1
+    assert lib.gbdx_host_device_pointer(ctypes.addressof(buf), ctypes.byref(out)) == -1
+    assert out.value is None
+    assert _lib.host_device_pointer(ctypes.addressof(buf)) is None
